@@ -1,0 +1,204 @@
+// jgcm_internal.cuh -- shared definitions of libjgcm (GB300 / sm_103a).
+//
+// Device data layout (all fields resident in HBM, one allocation per field):
+//   grid      T   g[k][j][i]         k < L, j < nlat (south->north), i < nlon   (= Julia layout)
+//   spectral  T2  s[m][n][k]         m <= N, n <= N+1, k < L  ("MNK": levels innermost, so a
+//                                      per-m Legendre block and a per-(m,n) vertical column both
+//                                      read contiguous memory); entries n < m are kept at zero
+//   fourier   T2  F[m][j][c]         m <= N, j < nlat, c < C (c = (field, level) column of a batch)
+//   tables    T   P[m][n][jh]        jh < nlat/2 (southern hemisphere; the north follows by parity)
+// T is double (JGCM_FP64) or float (the mixed-precision modes).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "jgcm.h"
+
+#define JGCM_MAX_GROUPS 8
+#define JGCM_MAX_ND 64
+
+namespace jgcm {
+
+void set_error(const char* fmt, ...);
+
+#define JG_CUDA(expr)                                                                         \
+  do {                                                                                        \
+    cudaError_t e_ = (expr);                                                                  \
+    if (e_ != cudaSuccess) {                                                                  \
+      jgcm::set_error("%s:%d %s -> %s", __FILE__, __LINE__, #expr, cudaGetErrorString(e_)); \
+      return JGCM_E_CUDA;                                                                     \
+    }                                                                                         \
+  } while (0)
+#define JG_TRY(expr)          \
+  do {                        \
+    int s_ = (expr);          \
+    if (s_ != JGCM_OK) return s_; \
+  } while (0)
+#define JG_ARG(cond, ...)               \
+  do {                                  \
+    if (!(cond)) {                      \
+      jgcm::set_error(__VA_ARGS__);     \
+      return JGCM_E_ARG;                \
+    }                                   \
+  } while (0)
+
+template <typename T>
+struct C2;
+template <>
+struct C2<float> {
+  using t = float2;
+};
+template <>
+struct C2<double> {
+  using t = double2;
+};
+
+// ------------------------------------------------------------------------------------------
+// Tables used by the kernels, one set per arithmetic type.
+template <typename T>
+struct Tables {
+  const T* P;     // [m][n][jh]  P_n^m(mu_j)                          (S2G)
+  const T* PW;    // [m][n][jh]  P_n^m(mu_j) w_j                      (G2S, x0.5 applied after the sum)
+  const T* CA;    // [m][n][jh]  m w P / cos^2 / (2a)                 (alpha operator, i*A term)
+  const T* CB;    // [m][n][jh]  -w dP/dmu / (2a)                     (alpha operator, B term)
+  const T* dlam;  // [m][n]  m/a
+  const T* dthm;  // [m][n]  -(n-1) eps_n / a
+  const T* dthp;  // [m][n]  (n+2) eps_{n+1} / a
+  const T* uvm;   // [m][n]  a eps_n / n
+  const T* uvc;   // [m][n]  -a m / (n(n+1))
+  const T* uvp;   // [m][n]  -a eps_{n+1} / (n+1)
+  const T* eig;   // [m][n]  -n(n+1)/a^2
+  const T* cosj;  // [nlat]
+  const T* sinj;  // [nlat]
+  const T* tw;    // [nlon/2][2]  cos, sin of 2 pi k / nlon
+  const double* wts;  // [nlat] FP64 Gaussian weights (for FP64 global sums)
+};
+
+template <typename T>
+struct TableStore {
+  T *P, *PW, *CA, *CB, *dlam, *dthm, *dthp, *uvm, *uvc, *uvp, *eig, *cosj, *sinj, *tw;
+  Tables<T> view(const double* wts) const {
+    return Tables<T>{P, PW, CA, CB, dlam, dthm, dthp, uvm, uvc, uvp, eig, cosj, sinj, tw, wts};
+  }
+};
+
+// ------------------------------------------------------------------------------------------
+// Transform plans.  A launch processes a batch of columns; each group maps a contiguous
+// column range [col0, col0+L) to one field (one column per level).
+enum S2GOp { S2G_PLAIN = 0, S2G_DLAM = 1, S2G_DTH = 2, S2G_UCOS = 3, S2G_VCOS = 4 };
+struct S2GGroup {
+  const void* a;  // spectral field (MNK, L levels)
+  const void* b;  // second field (UCOS/VCOS: divergence; a = vorticity)
+  int op, L, col0, pad;
+};
+struct S2GPlan {
+  int ng, C;
+  S2GGroup g[JGCM_MAX_GROUPS];
+};
+
+enum GridEpi { EPI_NONE = 0, EPI_DIVCOS = 1, EPI_EXP2 = 2, EPI_DIVCOS_MULPS = 3 };
+struct GridOutGroup {
+  void* dst;
+  void* dst2;      // EPI_EXP2: exp(x)
+  const void* ps;  // EPI_DIVCOS_MULPS: surface pressure grid [nlat][nlon]
+  int epi, L, col0, pad;
+};
+struct IFFTPlan {
+  int ng, C;
+  GridOutGroup g[JGCM_MAX_GROUPS];
+};
+
+enum GridPro { PRO_NONE = 0, PRO_MULCOS = 1, PRO_FLUXU = 2, PRO_FLUXV = 3, PRO_KIN = 4, PRO_SWH = 5 };
+struct GridInGroup {
+  const void* src;  // NONE/MULCOS: field; FLUX*: u ; KIN: u ; SWH: h
+  const void* s1;   // FLUX*: v ; KIN: v ; SWH: u
+  const void* s2;   // FLUX*: vor ; SWH: v
+  const void* s3;   // SWH: dlam_h
+  const void* s4;   // SWH: dth_h
+  const void* s5;   // SWH: div
+  const void* s6;   // SWH: h_eq
+  int pro, L, col0, pad;
+};
+struct FFTPlan {
+  int ng, C;
+  double kappa_m, kappa_t;
+  const void* coriolis;  // [nlat] in T
+  GridInGroup g[JGCM_MAX_GROUPS];
+};
+
+enum G2SOp { G2S_PLAIN = 0, G2S_VOR = 1, G2S_DIV = 2, G2S_BARO = 3, G2S_SW = 4 };
+// Fused time-stepping parameters for the G2S epilogues (barotropic / shallow water).
+struct StepParams {
+  int init_step;
+  int dt;
+  double robert, implicit_coef, h0;
+  const void* damping;  // [m][n] in T
+};
+struct SpecOutGroup {
+  void* dst;          // PLAIN/VOR/DIV: output; BARO: vor_n; SW: vor_n
+  void* dst2;         // SW: div_n
+  void* dst3;         // SW: h_n
+  const void* extra;  // DIV: spectral field added to G2S(E) before the Laplacian (SW: h_c), nullable
+  const void* qc[3];  // BARO/SW: current level (vor, div, h) -- updated in place by the RA filter
+  const void* qp[3];  // BARO/SW: previous level
+  int op, L, col0;
+  int colA, colB, colE, colH;  // Fourier-buffer base columns of the input slots (-1 = unused)
+};
+struct G2SPlan {
+  int ng, C;  // C = number of output columns
+  StepParams sp;
+  SpecOutGroup g[JGCM_MAX_GROUPS];
+};
+
+}  // namespace jgcm
+
+// ------------------------------------------------------------------------------------------
+struct jgcm_mesh {
+  int N, ns, nlat, nlon, nd, nh, logn, precision;
+  double radius;
+  cudaStream_t stream;
+  // FP64 reference-layout tables generated on the GPU
+  double *d_sinth, *d_wts, *d_costh, *d_qnm, *d_dqnm;
+  double* d_ref2;  // scratch for reference-layout 2-D tables on export
+  jgcm::TableStore<double> t64;
+  jgcm::TableStore<float> t32;
+  // workspace
+  int Cmax;
+  void* d_fbuf;       // Fourier buffer [m][j][c] complex T, c < Cmax
+  double* d_stage;    // FP64 host-layout staging, 4 slots of max(spec,grid) * nd
+  size_t stage_slot;  // doubles per slot
+  void* d_grid[4];    // native grid scratch (T), nd levels each
+  void* d_spec[4];    // native spectral scratch (T2), nd levels each
+  double* d_red;      // reduction scratch (FP64)
+  unsigned int* d_counter;
+  std::string name;
+};
+
+namespace jgcm {
+inline bool is_fp64(const jgcm_mesh* m) { return m->precision == JGCM_FP64; }
+inline size_t spec_elems(const jgcm_mesh* m, int L) { return (size_t)(m->N + 1) * (m->ns + 1) * L; }
+inline size_t grid_elems(const jgcm_mesh* m, int L) { return (size_t)m->nlon * m->nlat * L; }
+inline size_t tsize(const jgcm_mesh* m) { return is_fp64(m) ? 8 : 4; }
+
+// transforms.cu
+template <typename T>
+int launch_s2g(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, cudaStream_t st);
+template <typename T>
+int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp, cudaStream_t st);
+template <typename T>
+int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp, cudaStream_t st);
+int spec_host_to_dev(jgcm_mesh* m, const double* d_host_layout, void* d_native, int L, cudaStream_t st);
+int spec_dev_to_host(jgcm_mesh* m, const void* d_native, double* d_host_layout, int L, cudaStream_t st);
+int grid_host_to_dev(jgcm_mesh* m, const double* d_src, void* d_native, size_t n, cudaStream_t st);
+int grid_dev_to_host(jgcm_mesh* m, const void* d_native, double* d_dst, size_t n, cudaStream_t st);
+int fourier_dev_to_host(jgcm_mesh* m, int L, double* d_dst, cudaStream_t st);
+int apply_laplacian(jgcm_mesh* m, void* d_spec, int L, cudaStream_t st);
+int area_mean(jgcm_mesh* m, const void* d_grid, double* d_out, cudaStream_t st);
+template <typename T>
+Tables<T> tables(const jgcm_mesh* m);
+
+// mesh.cu
+int mesh_build_tables(jgcm_mesh* m);
+}  // namespace jgcm

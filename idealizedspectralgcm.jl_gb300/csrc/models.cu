@@ -1,0 +1,1566 @@
+// models.cu -- device-resident time stepping of the three JGCM models.
+//
+//   Barotropic_Dynamics!        Barotropic_Dynamics.jl:2-46                 4 launches / step
+//   Shallow_Water_Dynamics!     Shallow_Water_Dynamics.jl:7-179             6 launches / step
+//   Atmosphere_Update! (HS)     Spectral_Dynamics.jl:206-365, 452-490,
+//                               HS_Forcing.jl:1-130, Semi_Implicit.jl       10 launches / step
+//
+// Dyn_Data lives on the device in the model's precision.  Time levels p/c/n rotate by
+// pointer (Time_Advance!, Dyn_Data.jl:326-364, copies instead); steady steps are captured
+// once per rotation phase as CUDA graphs and replayed.  The semi-implicit wave matrices
+// (Semi_Implicit.jl:165-180) are inverted on the device in FP64, the per-(m,n) vertical
+// solve runs in FP64 (one warp per spectral mode, lanes over levels) and the mass/energy
+// fixers (Spectral_Dynamics.jl:5-68) use deterministic FP64 reductions.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "jgcm_internal.cuh"
+
+using namespace jgcm;
+
+namespace {
+constexpr unsigned FULL = 0xffffffffu;
+
+template <typename T>
+using V2 = typename C2<T>::t;
+
+struct VertCoef {  // Vert_Coordinate (even_sigma) and the semi-implicit reference column
+  double ak[JGCM_MAX_ND + 1], bk[JGCM_MAX_ND + 1], dak[JGCM_MAX_ND], dbk[JGCM_MAX_ND];
+  double dp_ref[JGCM_MAX_ND], lnph_ref[JGCM_MAX_ND + 1], lnpf_ref[JGCM_MAX_ND], t_ref[JGCM_MAX_ND],
+      h[JGCM_MAX_ND];
+};
+}  // namespace
+
+struct jgcm_model {
+  jgcm_mesh* mesh;
+  jgcm_params P;
+  int nd, init_step, rot, sw_adv_from_n, steps_done;
+  double cp_air;
+  // time-levelled state (index by rotation)
+  void *spe_vor[3], *spe_div[3], *spe_lnps[3], *spe_t[3];
+  void *grid_u[3], *grid_v[3], *grid_ps[3], *grid_t[3];
+  // single-level state and diagnostics
+  void *grid_vor, *grid_div, *grid_lnps, *grid_t_eq, *grid_geopots, *grid_h_eq, *spe_zero;
+  // tendencies and scratch
+  void *spe_dvor, *spe_ddiv, *spe_dlnps, *spe_dt;
+  void *g_dlps, *g_dtps, *g_dlT, *g_dtT, *g_ducos, *g_dvcos, *g_dt, *g_energy, *g_dlnps, *g_diag;
+  void *coriolis, *damping;  // [nlat], [m][n] in T
+  double* damping64;         // [m][n] FP64 (semi-implicit kernel)
+  // FP64 semi-implicit data
+  VertCoef vc;
+  double* div_mat;  // host nd*nd column-major
+  double* d_W;      // device [2][N+1][nd][nd] (transposed: [c][r])
+  int2* d_pairs;    // (m, n) pairs with n >= m
+  int npairs;
+  double *d_partials, *d_scalars;
+  unsigned* d_counter;
+  cudaGraphExec_t graph[3];
+  cudaEvent_t ev0, ev1;
+};
+
+namespace {
+
+int lvl(const jgcm_model* md, int which) { return (md->rot + which) % 3; }  // 0 = p, 1 = c, 2 = n
+
+// ------------------------------------------------------------------------------------------
+// warp scans over levels (lanes >= nd hold zero)
+__device__ __forceinline__ double scan_incl(double x, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    double y = __shfl_up_sync(FULL, x, o);
+    if (lane >= o) x += y;
+  }
+  return x;
+}
+__device__ __forceinline__ double rscan_incl(double x, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    double y = __shfl_down_sync(FULL, x, o);
+    if (lane + o < 32) x += y;
+  }
+  return x;
+}
+__device__ __forceinline__ double warp_sum(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+  return x;
+}
+template <typename T>
+__device__ __forceinline__ T shfl_up1(T x, int lane, T fill) {
+  T y = __shfl_up_sync(FULL, x, 1);
+  return lane == 0 ? fill : y;
+}
+template <typename T>
+__device__ __forceinline__ T shfl_dn1(T x, int lane, int nd, T fill) {
+  T y = __shfl_down_sync(FULL, x, 1);
+  return lane + 1 >= nd ? fill : y;
+}
+
+// Deterministic grid-wide FP64 reduction over a (x = column chunk, y = latitude) grid.  Thread 0
+// of every block passes its NV block sums; the last block to finish (atomic ticket) folds the
+// partials in a fixed order, sum_j w_j sum_b partial[v][j][b], and returns true with the NV
+// totals in out[] (valid in every thread of that block).  All other blocks return false.
+template <int NV>
+__device__ bool grid_reduce_last(const double* vals, double* partials, unsigned* counter, const double* wts,
+                                 double* out) {
+  __shared__ bool am_last;
+  __shared__ double red[NV][256];
+  const int nb = gridDim.x * gridDim.y;
+  const int bid = blockIdx.y * gridDim.x + blockIdx.x;
+  if (threadIdx.x == 0) {
+    for (int v = 0; v < NV; v++) partials[(size_t)v * nb + bid] = vals[v];
+    __threadfence();
+    unsigned t = atomicAdd(counter, 1u);
+    am_last = (t == (unsigned)nb - 1);
+  }
+  __syncthreads();
+  if (!am_last) return false;
+  __threadfence();
+  double s[NV];
+  for (int v = 0; v < NV; v++) s[v] = 0.0;
+  for (int jj = threadIdx.x; jj < (int)gridDim.y; jj += blockDim.x) {
+    for (int v = 0; v < NV; v++) {
+      double r = 0.0;
+      for (int b = 0; b < (int)gridDim.x; b++) r += __ldcg(partials + (size_t)v * nb + (size_t)jj * gridDim.x + b);
+      s[v] += r * wts[jj];
+    }
+  }
+  for (int v = 0; v < NV; v++) red[v][threadIdx.x] = s[v];
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int v = 0; v < NV; v++) red[v][threadIdx.x] += red[v][threadIdx.x + st];
+    __syncthreads();
+  }
+  for (int v = 0; v < NV; v++) out[v] = red[v][0];
+  if (threadIdx.x == 0) *counter = 0u;
+  return true;
+}
+
+// ------------------------------------------------------------------------------------------
+// Held-Suarez: physics (HS_Forcing!, previous time level) + corrections-init sums +
+// Four_In_One! + Compute_Geopotential! + Vert_Advection! x3 + horizontal advection of T +
+// absolute-vorticity fluxes + energy, fused.  One warp per grid column, lane = level.
+template <typename T>
+struct HSColArgs {
+  const T *u_p, *v_p, *t_p, *ps_p, *ps_c, *u_c, *v_c, *t_c, *div, *vor, *dlps, *dtps, *dlT, *dtT, *geopots, *coriolis,
+      *sinj, *cosj;
+  T *ducos, *dvcos, *dtg, *energy, *dlnps, *t_eq;
+  const double* wts;
+  double *partials, *scalars;
+  unsigned* counter;
+  int nd, nlat, nlon, Dt;
+  double sigma_b, k_f, k_a, k_s, dT_y, dtheta_z, kappa, rdgas, cp, grav;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_hs_column(HSColArgs<T> a, VertCoef vc) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * 8 + w, j = blockIdx.y;
+  const int nd = a.nd, nlon = a.nlon;
+  const bool act = lane < nd && i < nlon;
+  const int k = act ? lane : 0;
+  const size_t col = (size_t)j * nlon + (i < nlon ? i : 0);
+  const size_t x = (size_t)k * a.nlat * nlon + col;
+  const T day = (T)86400;
+  // ---- pressure variables from ps_c (Pressure_Variables!, Press_And_Geopot.jl:36-67)
+  const T ps = a.ps_c[col];
+  const T ph0 = (T)vc.ak[k] + (T)vc.bk[k] * ps, ph1 = (T)vc.ak[k + 1] + (T)vc.bk[k + 1] * ps;
+  const T dp = ph1 - ph0;
+  const T lnph1 = log(ph1);
+  const T lnph0 = (k == 0) ? (T)0 : log(ph0);
+  const T lnpf = (k == 0) ? lnph1 - (T)1.0 : lnph1 + ph0 * (lnph1 - lnph0) / dp - (T)1.0;
+  const T pfull = exp(lnpf);
+  const T psurf = (T)vc.ak[nd] + (T)vc.bk[nd] * ps;
+  // ---- HS_Forcing! on the previous level
+  const int Dt = a.Dt;
+  T up = 0, vp = 0, tp = 0;
+  if (act) {
+    up = a.u_p[x];
+    vp = a.v_p[x];
+    tp = a.t_p[x];
+  }
+  const T sb = (T)a.sigma_b;
+  T sig = pfull / psurf;
+  T s = sig - sb;
+  T smax = s > (T)0 ? s : (T)0;
+  T k_v = ((T)a.k_f / day) / ((T)1.0 - sb) * smax;
+  T du = -k_v * up, dv = -k_v * vp;
+  T dt = -((up + (T)0.5 * du * (T)Dt) * du + (vp + (T)0.5 * dv * (T)Dt) * dv) / (T)a.cp;
+  const T sj = a.sinj[j];
+  const T s2 = sj * sj, c2 = (T)1.0 - s2, c4 = c2 * c2;
+  T pn = pfull / (T)1.0e5;
+  T teq = ((T)315.0 - (T)a.dT_y * s2 - (T)a.dtheta_z * c2 * log(pn)) * pow(pn, (T)a.kappa);
+  teq = teq > (T)200.0 ? teq : (T)200.0;
+  T ka = (T)a.k_a / day, ks = (T)a.k_s / day;
+  T k_t = ka + (ks - ka) / ((T)1.0 - sb) * smax * c4;
+  dt = dt - k_t * (tp - teq);
+  if (act) a.t_eq[x] = teq;
+  // ---- Compute_Corrections_Init sums (FP64): column energy integral with ps_p
+  const double psp = (double)a.ps_p[col];
+  double e_p = 0.0;
+  if (act) {
+    double ua = (double)up + Dt * (double)du, va = (double)vp + Dt * (double)dv;
+    double E = 0.5 * (ua * ua + va * va) + a.cp * ((double)tp + Dt * (double)dt);
+    e_p = E * (vc.dak[k] + vc.dbk[k] * psp);
+  }
+  const double col_e = warp_sum(e_p);
+  // ---- Four_In_One! (Spectral_Dynamics.jl:88-183) on the current level
+  T u = 0, v = 0, t = 0, dvg = 0, vor = 0, dlT = 0, dtT = 0;
+  if (act) {
+    u = a.u_c[x];
+    v = a.v_c[x];
+    t = a.t_c[x];
+    dvg = a.div[x];
+    vor = a.vor[x];
+    dlT = a.dlT[x];
+    dtT = a.dtT[x];
+  }
+  const T dlps = a.dlps[col], dtps = a.dtps[col];
+  const T R = (T)a.rdgas, kap = (T)a.rdgas / (T)a.cp;
+  const T dlnp_p = lnph1 - lnpf, dlnp_m = lnpf - lnph0, dlnp = lnph1 - lnph0;
+  const T x1 = ((T)vc.bk[k] * dlnp_m + (T)vc.bk[k + 1] * dlnp_p) / dp;
+  const T dlnp_dl = x1 * dlps, dlnp_dt = x1 * dtps;
+  du = du - R * t * dlnp_dl;
+  dv = dv - R * t * dlnp_dt;
+  T dmean = dvg * dp + (T)vc.dbk[k] * (u * dlps + v * dtps);
+  if (!act) dmean = 0;
+  double incl = scan_incl((double)dmean, lane);
+  double tot_d = __shfl_sync(FULL, incl, nd - 1);
+  T excl = (T)shfl_up1(incl, lane, 0.0);
+  T x5 = -(excl * dlnp + dmean * dlnp_p) / dp + u * dlnp_dl + v * dlnp_dt;
+  dt = dt + kap * t * x5;
+  const T tot = (T)tot_d;
+  // M_{k+1/2}: -sum_{r<=k} D_r + B_{k+1/2} sum_r D_r ; zero at top and surface
+  T Mhi = (lane + 1 <= nd - 1) ? -(T)incl + tot * (T)vc.bk[k + 1] : (T)0;
+  T Mlo = shfl_up1(Mhi, lane, (T)0);
+  // ---- Compute_Geopotential! (Press_And_Geopot.jl:71-111), bottom-up
+  T term = act ? R * t * (lnph1 - lnph0) : (T)0;
+  double rs = rscan_incl((double)term, lane);        // sum_{r>=k} term_r
+  T gs = act ? a.geopots[col] : (T)0;
+  gs = __shfl_sync(FULL, gs, 0);
+  T ghalf_hi = gs + (T)shfl_dn1(rs, lane, nd, 0.0);  // Phi_{k+1/2}
+  T gfull = ghalf_hi + R * t * (lnph1 - lnpf);
+  // ---- Vert_Advection! (second_centered_wts) for u, v, T
+  T dp_m = shfl_up1(dp, lane, (T)1);
+  auto vadv = [&](T r) -> T {
+    T r_m = shfl_up1(r, lane, (T)0);
+    T flux_lo = (lane >= 1) ? Mlo * (r_m + (r - r_m) * dp_m / (dp_m + dp)) : (T)0;
+    T flux_hi = shfl_dn1(flux_lo, lane, nd, (T)0);
+    return (flux_lo - flux_hi + r * (Mhi - Mlo)) / dp;
+  };
+  du = du + vadv(u);
+  dv = dv + vadv(v);
+  dt = dt + vadv(t);
+  // ---- Add_Horizontal_Advection!(spe_t_c), Compute_Abs_Vor! fluxes, energy
+  dt = dt - (u * dlT + v * dtT);
+  const T absvor = vor + a.coriolis[j];
+  du = du + absvor * v;
+  dv = dv - absvor * u;
+  const T cj = a.cosj[j];
+  if (act) {
+    a.ducos[x] = du * cj;
+    a.dvcos[x] = dv * cj;
+    a.dtg[x] = dt;
+    a.energy[x] = gfull + (T)0.5 * (u * u + v * v);
+    if (lane == 0) a.dlnps[col] = (-tot) / ps;
+  }
+  // ---- block partials for mean_ps_p and mean_energy_p
+  __shared__ double sm[2][8];
+  if (lane == 0) {
+    sm[0][w] = (i < nlon) ? psp : 0.0;
+    sm[1][w] = (i < nlon) ? col_e : 0.0;
+  }
+  __syncthreads();
+  double vals[2] = {0, 0};
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 8; q++) {
+      vals[0] += sm[0][q];
+      vals[1] += sm[1][q];
+    }
+  double tot2[2];
+  if (grid_reduce_last<2>(vals, a.partials, a.counter, a.wts, tot2) && threadIdx.x == 0) {
+    a.scalars[0] = tot2[0] / (2.0 * nlon);           // mean_ps_p   (Area_Weighted_Global_Mean)
+    a.scalars[1] = tot2[1] / (2.0 * nlon) / a.grav;  // mean_energy_p (Mass_Weighted_Global_Integral)
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Semi-implicit correction (Adjust_δlnps_δt_δdiv! + Implicit_Correction!, Semi_Implicit.jl:
+// 271-513) followed by Compute_Spectral_Damping! and Filtered_Leapfrog! for vor, div, T, lnps
+// (Spectral_Dynamics.jl:313-327).  One warp per spectral mode (m,n), lane = level, FP64.
+template <typename T>
+struct ImplArgs {
+  const V2<T>*dvor, *ddiv, *dtend, *dlnps;  // spectral tendencies from the analysis
+  V2<T> *vor_p, *vor_c, *vor_n, *div_p, *div_c, *div_n, *t_p, *t_c, *t_n, *lnps_p, *lnps_c, *lnps_n;
+  const double *eig, *damping;  // FP64 [m][n]
+  const double* W;              // [N+1][c][r]
+  const int2* pairs;
+  int npairs, nd, ns, N, init_step, dt;
+  double xi, ps_ref, kappa, rdgas, robert;
+};
+
+struct C64 {
+  double x, y;
+};
+
+__device__ __forceinline__ void linear_ps_t(const VertCoef& vc, int lane, int nd, double kappa, C64 d, C64& dps,
+                                            C64& dtt) {
+  const bool act = lane < nd;
+  const int k = act ? lane : 0;
+  double dpr = vc.dp_ref[k];
+  C64 dm = {act ? d.x * dpr : 0.0, act ? d.y * dpr : 0.0};
+  double ix = scan_incl(dm.x, lane), iy = scan_incl(dm.y, lane);
+  double tx = __shfl_sync(FULL, ix, nd - 1), ty = __shfl_sync(FULL, iy, nd - 1);
+  double ex = shfl_up1(ix, lane, 0.0), ey = shfl_up1(iy, lane, 0.0);
+  double dlnp = vc.lnph_ref[k + 1] - vc.lnph_ref[k], dlnp_p = vc.lnph_ref[k + 1] - vc.lnpf_ref[k];
+  double c = -kappa * vc.t_ref[k];
+  dtt.x = c * (ex * dlnp + dm.x * dlnp_p) / dpr;
+  dtt.y = c * (ey * dlnp + dm.y * dlnp_p) / dpr;
+  // M_{k+1/2} (k <= nd-2) and the centred vertical-advection term with (t_ref[k] - t_ref[k-1])
+  double bk1 = vc.bk[k + 1];
+  double mhx = (lane + 1 <= nd - 1) ? -ix + tx * bk1 : 0.0, mhy = (lane + 1 <= nd - 1) ? -iy + ty * bk1 : 0.0;
+  double tdh = (lane + 1 <= nd - 1) ? vc.t_ref[k + 1] - vc.t_ref[k] : 0.0;
+  double mdhx = mhx * tdh, mdhy = mhy * tdh;  // Mdt_{k+1/2}
+  double mdlx = shfl_up1(mdhx, lane, 0.0), mdly = shfl_up1(mdhy, lane, 0.0);
+  dtt.x = dtt.x - 0.5 * (mdhx + mdlx) / dpr;
+  dtt.y = dtt.y - 0.5 * (mdhy + mdly) / dpr;
+  dps.x = -tx;
+  dps.y = -ty;
+}
+
+template <typename T>
+__device__ __forceinline__ void lf64(const ImplArgs<T>& a, double d, double& dq, double qp, double& qc, double& qn) {
+  const double r = a.robert;
+  if (a.init_step) {
+    dq = (dq - qc * d) / (1.0 + a.dt * d);
+    qn = qc + a.dt * dq;
+    qc = qc + r * (-1.0 * qc + qn);
+  } else {
+    dq = (dq - qp * d) / (1.0 + (2 * a.dt) * d);
+    qc = qc + r * (qp - 2 * qc);
+    qn = qp + (2 * a.dt) * dq;
+    qc = qc + r * qn;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, VertCoef vc) {
+  const int lane = threadIdx.x & 31;
+  const int pid = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (pid >= a.npairs) return;  // whole warp exits together
+  const int2 mn = a.pairs[pid];
+  const int m = mn.x, n = mn.y, nd = a.nd;
+  const bool act = lane < nd;
+  const int k = act ? lane : 0;
+  const size_t row = (size_t)m * (a.ns + 1) + n;
+  const size_t s = row * nd + k;
+  auto ld = [&](const V2<T>* p) -> C64 {
+    if (!act) return C64{0, 0};
+    V2<T> v = p[s];
+    return C64{(double)v.x, (double)v.y};
+  };
+  C64 ddiv = ld(a.ddiv), dtt = ld(a.dtend), dvor = ld(a.dvor);
+  C64 divp = ld(a.div_p), divc = ld(a.div_c), tp = ld(a.t_p), tc = ld(a.t_c), vorp = ld(a.vor_p), vorc = ld(a.vor_c);
+  V2<T> l0 = a.dlnps[row], lp0 = a.lnps_p[row], lc0 = a.lnps_c[row];
+  C64 dl = {(double)l0.x, (double)l0.y}, lp = {(double)lp0.x, (double)lp0.y}, lc = {(double)lc0.x, (double)lc0.y};
+  const double xi = a.xi, psr = a.ps_ref, eig = a.eig[row];
+  // Adjust_δlnps_δt_δdiv! :360-404
+  C64 dps, dtmp;
+  linear_ps_t(vc, lane, nd, a.kappa, C64{divp.x - divc.x, divp.y - divc.y}, dps, dtmp);
+  dtt.x = dtt.x + dtmp.x;
+  dtt.y = dtt.y + dtmp.y;
+  dl.x = dl.x + dps.x / psr;
+  dl.y = dl.y + dps.y / psr;
+  C64 t2 = {tp.x - tc.x + xi * dtt.x, tp.y - tc.y + xi * dtt.y};
+  C64 l2 = {lp.x - lc.x + xi * dl.x, lp.y - lc.y + xi * dl.y};
+  // Linear_Geopot_δt! :213-241
+  double dh = vc.lnph_ref[k + 1] - vc.lnph_ref[k];
+  double tmx = act ? a.rdgas * (t2.x * dh) : 0.0, tmy = act ? a.rdgas * (t2.y * dh) : 0.0;
+  double rx = rscan_incl(tmx, lane), ry = rscan_incl(tmy, lane);
+  double hx = shfl_dn1(rx, lane, nd, 0.0), hy = shfl_dn1(ry, lane, nd, 0.0);  // Φ_{k+1/2}
+  double df = vc.lnph_ref[k + 1] - vc.lnpf_ref[k];
+  double gx = hx + a.rdgas * (t2.x * df), gy = hy + a.rdgas * (t2.y * df);
+  double hk = vc.h[k] * psr;
+  ddiv.x = ddiv.x - eig * (gx + hk * l2.x);
+  ddiv.y = ddiv.y - eig * (gy + hk * l2.y);
+  // wave-matrix solve, n <= N only
+  if (n <= a.N) {
+    const double* W = a.W + (size_t)n * nd * nd;
+    double sx = 0, sy = 0;
+    for (int c = 0; c < nd; c++) {
+      double bx = __shfl_sync(FULL, ddiv.x, c), by = __shfl_sync(FULL, ddiv.y, c);
+      double wv = act ? W[(size_t)c * nd + k] : 0.0;
+      sx = sx + wv * bx;
+      sy = sy + wv * by;
+    }
+    ddiv.x = act ? sx : 0.0;
+    ddiv.y = act ? sy : 0.0;
+  }
+  linear_ps_t(vc, lane, nd, a.kappa, ddiv, dps, dtmp);
+  dtt.x = dtt.x + xi * dtmp.x;
+  dtt.y = dtt.y + xi * dtmp.y;
+  dl.x = dl.x + xi / psr * dps.x;
+  dl.y = dl.y + xi / psr * dps.y;
+  // damping + leapfrog
+  const double d = a.damping[row];
+  if (act) {
+    C64 vn, dn, tn;
+    lf64(a, d, dvor.x, vorp.x, vorc.x, vn.x);
+    lf64(a, d, dvor.y, vorp.y, vorc.y, vn.y);
+    lf64(a, d, ddiv.x, divp.x, divc.x, dn.x);
+    lf64(a, d, ddiv.y, divp.y, divc.y, dn.y);
+    lf64(a, d, dtt.x, tp.x, tc.x, tn.x);
+    lf64(a, d, dtt.y, tp.y, tc.y, tn.y);
+    V2<T> o;
+    o.x = (T)vn.x; o.y = (T)vn.y; a.vor_n[s] = o;
+    o.x = (T)vorc.x; o.y = (T)vorc.y; a.vor_c[s] = o;
+    o.x = (T)dn.x; o.y = (T)dn.y; a.div_n[s] = o;
+    o.x = (T)divc.x; o.y = (T)divc.y; a.div_c[s] = o;
+    o.x = (T)tn.x; o.y = (T)tn.y; a.t_n[s] = o;
+    o.x = (T)tc.x; o.y = (T)tc.y; a.t_c[s] = o;
+  }
+  if (lane == 0) {  // lnps: leapfrog without damping
+    C64 ln;
+    lf64(a, 0.0, dl.x, lp.x, lc.x, ln.x);
+    lf64(a, 0.0, dl.y, lp.y, lc.y, ln.y);
+    V2<T> o;
+    o.x = (T)ln.x; o.y = (T)ln.y; a.lnps_n[row] = o;
+    o.x = (T)lc.x; o.y = (T)lc.y; a.lnps_c[row] = o;
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Compute_Corrections! (Spectral_Dynamics.jl:30-68): FP64 sums of ps_n and of the column
+// energy (split into the Δa and Δb·ps parts so the mass correction can be applied after the
+// sum), then the spectral (m,n)=(0,0) fixes in the last block.  k_hs_corr_apply follows.
+template <typename T>
+struct CorrArgs {
+  const T *u_n, *v_n, *t_n, *ps_n;
+  V2<T>*lnps_n, *t_spec_n;
+  const double* wts;
+  double *partials, *scalars;
+  unsigned* counter;
+  int nd, nlat, nlon, do_mass, do_energy;
+  double cp, grav;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, VertCoef vc) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * 8 + w, j = blockIdx.y, nd = a.nd;
+  const bool act = lane < nd && i < a.nlon;
+  const size_t col = (size_t)j * a.nlon + (i < a.nlon ? i : 0);
+  const size_t x = (size_t)(act ? lane : 0) * a.nlat * a.nlon + col;
+  double ps = (i < a.nlon) ? (double)a.ps_n[col] : 0.0;
+  double ea = 0, eb = 0;
+  if (act) {
+    double u = a.u_n[x], v = a.v_n[x], t = a.t_n[x];
+    double E = 0.5 * (u * u + v * v) + a.cp * t;
+    ea = E * vc.dak[lane];
+    eb = E * (vc.dbk[lane] * ps);
+  }
+  ea = warp_sum(ea);
+  eb = warp_sum(eb);
+  __shared__ double sm[3][8];
+  if (lane == 0) {
+    sm[0][w] = ps;
+    sm[1][w] = ea;
+    sm[2][w] = eb;
+  }
+  __syncthreads();
+  double vals[3] = {0, 0, 0};
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 8; q++) {
+      vals[0] += sm[0][q];
+      vals[1] += sm[1][q];
+      vals[2] += sm[2][q];
+    }
+  double tot3[3];
+  if (grid_reduce_last<3>(vals, a.partials, a.counter, a.wts, tot3) && threadIdx.x == 0) {
+    double two_n = 2.0 * a.nlon;
+    double mean_ps_p = a.scalars[0], mean_energy_p = a.scalars[1];
+    double factor = 1.0, corr = 0.0;
+    if (a.do_mass) {
+      double mean_ps_n = tot3[0] / two_n;
+      factor = mean_ps_p / mean_ps_n;
+      V2<T> l = a.lnps_n[0];  // spe_lnps_n[1,1,1] += log(factor)  (P_00 = 1)
+      l.x = (T)((double)l.x + log(factor));
+      a.lnps_n[0] = l;
+    }
+    if (a.do_energy) {
+      // Δp_k = Δa_k + Δb_k (factor ps_n): the mass correction enters linearly
+      double mean_energy_n = (tot3[1] + factor * tot3[2]) / two_n / a.grav;
+      corr = a.grav * (mean_energy_p - mean_energy_n) / (a.cp * mean_ps_p);
+      for (int k = 0; k < nd; k++) {  // spe_t_n[1,1,:] .+= temperature_correction
+        V2<T> tt = a.t_spec_n[k];
+        tt.x = (T)((double)tt.x + corr);
+        a.t_spec_n[k] = tt;
+      }
+    }
+    a.scalars[2] = factor;
+    a.scalars[3] = corr;
+  }
+}
+
+template <typename T>
+__global__ void k_hs_corr_apply(T* t_n, T* ps_n, const double* scalars, size_t nt, size_t nps) {
+  const T factor = (T)scalars[2], corr = (T)scalars[3];
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nt; q += (size_t)gridDim.x * blockDim.x) {
+    t_n[q] = t_n[q] + corr;
+    if (q < nps) ps_n[q] = ps_n[q] * factor;
+  }
+}
+
+// Pressure variables and heights on demand (Compute_Pressures_And_Heights!, Press_And_Geopot.jl:3-19).
+// out: [0]=p_half (nd+1) [1]=lnp_half (nd+1) [2]=dp (nd) [3]=p_full (nd) [4]=lnp_full (nd)
+//      [5]=z_full (nd) [6]=z_half (nd+1), each stored at its own offset in `diag`.
+template <typename T>
+__global__ void k_pressure_heights(const T* ps_c, const T* t_c, const T* geopots, double* diag, VertCoef vc, int nd,
+                                   size_t G, double rdgas, double grav) {
+  size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (c >= G) return;
+  double* ph = diag;
+  double* lph = ph + G * (nd + 1);
+  double* dpp = lph + G * (nd + 1);
+  double* pf = dpp + G * nd;
+  double* lpf = pf + G * nd;
+  double* zf = lpf + G * nd;
+  double* zh = zf + G * nd;
+  double ps = ps_c[c];
+  for (int k = 0; k <= nd; k++) ph[c + G * k] = vc.ak[k] + vc.bk[k] * ps;
+  for (int k = 0; k < nd; k++) dpp[c + G * k] = ph[c + G * (k + 1)] - ph[c + G * k];
+  for (int k = 1; k <= nd; k++) lph[c + G * k] = log(ph[c + G * k]);
+  for (int k = 1; k < nd; k++)
+    lpf[c + G * k] = lph[c + G * (k + 1)] + ph[c + G * k] * (lph[c + G * (k + 1)] - lph[c + G * k]) / dpp[c + G * k] - 1.0;
+  lph[c] = 0.0;
+  lpf[c] = lph[c + G] - 1.0;
+  for (int k = 0; k < nd; k++) pf[c + G * k] = exp(lpf[c + G * k]);
+  zh[c + G * nd] = (double)geopots[c];
+  zh[c] = 0.0;
+  for (int k = nd - 1; k >= 1; k--)
+    zh[c + G * k] = zh[c + G * (k + 1)] + rdgas * (double)t_c[c + G * k] * (lph[c + G * (k + 1)] - lph[c + G * k]);
+  for (int k = 0; k < nd; k++)
+    zf[c + G * k] = zh[c + G * (k + 1)] + rdgas * (double)t_c[c + G * k] * (lph[c + G * (k + 1)] - lpf[c + G * k]);
+  for (int k = 0; k < nd; k++) zf[c + G * k] /= grav;
+  for (int k = 0; k <= nd; k++) zh[c + G * k] /= grav;
+}
+
+// Build_Wave_Matrices (Semi_Implicit.jl:165-180): W_n = (I - ξ² eig_n div_mat)^{-1}, one
+// block per n, Gauss-Jordan with partial pivoting in shared memory, FP64.  Output [n][c][r].
+__global__ void k_wave_matrices(const double* div_mat, const double* eig0, double xi, int nd, int N, double* W,
+                                int* status) {
+  extern __shared__ double sh[];
+  double* A = sh;            // [nd][nd] column-major
+  double* B = sh + nd * nd;  // inverse
+  __shared__ int piv;
+  const int n = blockIdx.x;
+  double factor = xi * xi * eig0[n];
+  for (int q = threadIdx.x; q < nd * nd; q += blockDim.x) {
+    int r = q % nd, c = q / nd;
+    A[q] = (r == c ? 1.0 : 0.0) - factor * div_mat[q];
+    B[q] = (r == c) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  for (int c = 0; c < nd; c++) {
+    if (threadIdx.x == 0) {
+      int p = c;
+      for (int r = c + 1; r < nd; r++)
+        if (fabs(A[r + nd * c]) > fabs(A[p + nd * c])) p = r;
+      piv = p;
+      if (A[p + nd * c] == 0.0) atomicExch(status, 1);
+    }
+    __syncthreads();
+    int p = piv;
+    if (p != c)
+      for (int q = threadIdx.x; q < nd; q += blockDim.x) {
+        double t = A[c + nd * q]; A[c + nd * q] = A[p + nd * q]; A[p + nd * q] = t;
+        t = B[c + nd * q]; B[c + nd * q] = B[p + nd * q]; B[p + nd * q] = t;
+      }
+    __syncthreads();
+    double pv = A[c + nd * c];
+    __syncthreads();
+    for (int q = threadIdx.x; q < nd; q += blockDim.x) {
+      A[c + nd * q] /= pv;
+      B[c + nd * q] /= pv;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nd * nd; q += blockDim.x) {
+      int r = q % nd, cc = q / nd;
+      if (r == c) continue;
+      double f = A[r + nd * c];
+      if (cc != c) {
+        A[r + nd * cc] -= f * A[c + nd * cc];
+      }
+      B[r + nd * cc] -= f * B[c + nd * cc];
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < nd; r += blockDim.x)
+      if (r != c) A[r + nd * c] = 0.0;
+    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < nd * nd; q += blockDim.x) {
+    int r = q % nd, c = q / nd;
+    W[(size_t)n * nd * nd + (size_t)c * nd + r] = B[r + nd * c];
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// host-side vertical setup: Vert_Coordinate (even_sigma), reference pressures and
+// Build_Implicit_Matrices (Semi_Implicit.jl:40-160), FP64.
+void press_vars_col(const VertCoef& vc, int nd, double ps, double* ph, double* dp, double* lph, double* pf, double* lpf) {
+  for (int k = 0; k <= nd; k++) ph[k] = vc.ak[k] + vc.bk[k] * ps;
+  for (int k = 0; k < nd; k++) dp[k] = ph[k + 1] - ph[k];
+  for (int k = 1; k <= nd; k++) lph[k] = std::log(ph[k]);
+  for (int k = 1; k < nd; k++) lpf[k] = lph[k + 1] + ph[k] * (lph[k + 1] - lph[k]) / dp[k] - 1.0;
+  lph[0] = 0.0;
+  lpf[0] = lph[1] - 1.0;
+  for (int k = 0; k < nd; k++) pf[k] = std::exp(lpf[k]);
+}
+
+void lin_ps_t_col(const VertCoef& vc, int nd, double kappa, const double* d, double* dps, double* dtt) {
+  std::vector<double> Mh(nd + 1, 0.0), Mdt(nd + 1, 0.0);
+  double tot = 0.0;
+  for (int k = 0; k < nd; k++) {
+    double dlnp_p = vc.lnph_ref[k + 1] - vc.lnpf_ref[k], dlnp = vc.lnph_ref[k + 1] - vc.lnph_ref[k];
+    double dmean = d[k] * vc.dp_ref[k];
+    dtt[k] = -kappa * vc.t_ref[k] * (tot * dlnp + dmean * dlnp_p) / vc.dp_ref[k];
+    tot = tot + dmean;
+    Mh[k + 1] = -tot;
+  }
+  *dps = -tot;
+  for (int k = 0; k < nd - 1; k++) Mh[k + 1] = Mh[k + 1] + tot * vc.bk[k + 1];
+  Mh[0] = Mh[nd] = 0.0;
+  for (int k = 1; k < nd; k++) Mdt[k] = Mh[k] * (vc.t_ref[k] - vc.t_ref[k - 1]);
+  for (int k = 0; k < nd; k++) dtt[k] = dtt[k] - 0.5 * (Mdt[k + 1] + Mdt[k]) / vc.dp_ref[k];
+}
+
+void lin_geo_col(const VertCoef& vc, int nd, double R, const double* dtt, double* geo) {
+  std::vector<double> gh(nd + 1, 0.0);
+  for (int k = nd - 1; k >= 1; k--) gh[k] = gh[k + 1] + R * (dtt[k] * (vc.lnph_ref[k + 1] - vc.lnph_ref[k]));
+  for (int k = 0; k < nd; k++) geo[k] = gh[k + 1] + R * (dtt[k] * (vc.lnph_ref[k + 1] - vc.lnpf_ref[k]));
+}
+
+void vertical_setup(jgcm_model* md) {
+  int nd = md->nd;
+  VertCoef& vc = md->vc;
+  memset(&vc, 0, sizeof(vc));
+  for (int k = 0; k <= nd; k++) {
+    double t = (double)k / (double)nd;
+    vc.ak[k] = 0.0;
+    vc.bk[k] = (1 - t) * 0.0 + t * 1.0;
+  }
+  for (int k = 0; k < nd; k++) {
+    vc.dak[k] = vc.ak[k + 1] - vc.ak[k];
+    vc.dbk[k] = vc.bk[k + 1] - vc.bk[k];
+  }
+  if (md->P.kind != JGCM_HELD_SUAREZ) return;
+  std::vector<double> ph(nd + 1), pf(nd), dlh(nd + 1), dlf(nd);
+  double lph[JGCM_MAX_ND + 1], lpf[JGCM_MAX_ND];
+  press_vars_col(vc, nd, md->P.ps_ref, ph.data(), vc.dp_ref, lph, pf.data(), lpf);
+  for (int k = 0; k <= nd; k++) vc.lnph_ref[k] = lph[k];
+  for (int k = 0; k < nd; k++) vc.lnpf_ref[k] = lpf[k];
+  for (int k = 0; k < nd; k++) vc.t_ref[k] = md->P.t_ref;
+  for (int k = 0; k <= nd; k++) dlh[k] = vc.bk[k] / ph[k];
+  for (int k = 0; k < nd; k++)
+    dlf[k] = (vc.bk[k + 1] * (vc.lnph_ref[k + 1] - vc.lnpf_ref[k]) + vc.bk[k] * (vc.lnpf_ref[k] - vc.lnph_ref[k])) /
+             vc.dp_ref[k];
+  std::vector<double> tau(nd * nd), gamma(nd * nd), nu(nd), e(nd), dtt(nd), geo(nd);
+  for (int k = 0; k < nd; k++) {
+    std::fill(e.begin(), e.end(), 0.0);
+    e[k] = 1.0;
+    double dps;
+    lin_ps_t_col(vc, nd, md->P.kappa, e.data(), &dps, dtt.data());
+    nu[k] = -dps;
+    for (int r = 0; r < nd; r++) tau[r + nd * k] = -dtt[r];
+    lin_geo_col(vc, nd, md->P.rdgas, e.data(), geo.data());
+    for (int r = 0; r < nd; r++) gamma[r + nd * k] = geo[r];
+  }
+  double R = md->P.rdgas;
+  std::vector<double> h1(nd), h2(nd), gh2(nd + 1, 0.0);
+  for (int k = 0; k < nd; k++)
+    h1[k] = R * vc.t_ref[k] *
+            (vc.bk[k + 1] * (vc.lnph_ref[k + 1] - vc.lnpf_ref[k]) + vc.bk[k] * (vc.lnpf_ref[k] - vc.lnph_ref[k])) /
+            vc.dp_ref[k];
+  for (int k = nd - 1; k >= 1; k--) gh2[k] = gh2[k + 1] + R * (vc.t_ref[k] * (dlh[k + 1] - dlh[k]));
+  for (int k = 0; k < nd; k++) h2[k] = gh2[k + 1] + R * (vc.t_ref[k] * (dlh[k + 1] - dlf[k]));
+  for (int k = 0; k < nd; k++) vc.h[k] = h1[k] + h2[k];
+  for (int r = 0; r < nd; r++)
+    for (int c = 0; c < nd; c++) {
+      double s = 0.0;
+      for (int q = 0; q < nd; q++) s += gamma[r + nd * q] * tau[q + nd * c];
+      md->div_mat[r + nd * c] = vc.h[r] * nu[c] + s;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+template <typename T>
+__global__ void k_fill_damping(const double* eig, T* damping, int N, int ns, double coef, int order) {
+  // Time_Integrator.jl:31: damping = coef (eig / eig[1, num_spherical])^order
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (N + 1) * (ns + 1)) return;
+  double e0 = eig[0 * (ns + 1) + (ns - 1)];
+  damping[t] = (T)(coef * pow(eig[t] / e0, (double)order));
+}
+template <typename T>
+__global__ void k_fill_coriolis(const double* sinth, T* f, int nlat, double omega) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nlat) f[t] = (T)(2 * omega * sinth[t]);
+}
+
+int alloc(void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    set_error("cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    return JGCM_E_NOMEM;
+  }
+  e = cudaMemset(*p, 0, bytes);
+  if (e != cudaSuccess) {
+    set_error("cudaMemset: %s", cudaGetErrorString(e));
+    return JGCM_E_CUDA;
+  }
+  return JGCM_OK;
+}
+
+void model_free(jgcm_model* md) {
+  if (!md) return;
+  for (int i = 0; i < 3; i++) {
+    void* ps[] = {md->spe_vor[i], md->spe_div[i], md->spe_lnps[i], md->spe_t[i],
+                  md->grid_u[i], md->grid_v[i], md->grid_ps[i], md->grid_t[i]};
+    for (auto p : ps)
+      if (p) cudaFree(p);
+    if (md->graph[i]) cudaGraphExecDestroy(md->graph[i]);
+  }
+  void* ps[] = {md->grid_vor, md->grid_div, md->grid_lnps, md->grid_t_eq, md->grid_geopots, md->grid_h_eq,
+                md->spe_zero, md->spe_dvor, md->spe_ddiv, md->spe_dlnps, md->spe_dt, md->g_dlps, md->g_dtps,
+                md->g_dlT, md->g_dtT, md->g_ducos, md->g_dvcos, md->g_dt, md->g_energy, md->g_dlnps, md->g_diag,
+                md->coriolis, md->damping, md->damping64, md->d_W, md->d_pairs, md->d_partials, md->d_scalars,
+                md->d_counter};
+  for (auto p : ps)
+    if (p) cudaFree(p);
+  delete[] md->div_mat;
+  if (md->ev0) cudaEventDestroy(md->ev0);
+  if (md->ev1) cudaEventDestroy(md->ev1);
+  delete md;
+}
+
+int build_wave(jgcm_model* md) {
+  jgcm_mesh* m = md->mesh;
+  int nd = md->nd, N = m->N;
+  double *d_div = nullptr, *d_eig0 = nullptr;
+  int* d_status = nullptr;
+  JG_TRY(alloc((void**)&d_div, nd * nd * 8));
+  JG_TRY(alloc((void**)&d_eig0, (N + 1) * 8));
+  JG_TRY(alloc((void**)&d_status, 4));
+  std::vector<double> eig0(N + 1);
+  for (int n = 0; n <= N; n++) eig0[n] = (double)(-n * (n + 1)) / (m->radius * m->radius);
+  JG_CUDA(cudaMemcpy(d_div, md->div_mat, nd * nd * 8, cudaMemcpyHostToDevice));
+  JG_CUDA(cudaMemcpy(d_eig0, eig0.data(), (N + 1) * 8, cudaMemcpyHostToDevice));
+  const double a = md->P.implicit_coef;
+  double xis[2] = {md->P.dt * a, (2 * md->P.dt) * a};  // Get_ξ for the init step and afterwards
+  for (int s = 0; s < 2; s++) {
+    k_wave_matrices<<<N + 1, 128, 2 * nd * nd * 8, m->stream>>>(d_div, d_eig0, xis[s], nd, N,
+                                                                 md->d_W + (size_t)s * (N + 1) * nd * nd, d_status);
+    JG_CUDA(cudaGetLastError());
+  }
+  int st = 0;
+  JG_CUDA(cudaMemcpyAsync(&st, d_status, 4, cudaMemcpyDeviceToHost, m->stream));
+  JG_CUDA(cudaStreamSynchronize(m->stream));
+  cudaFree(d_div);
+  cudaFree(d_eig0);
+  cudaFree(d_status);
+  if (st) {
+    set_error("singular semi-implicit wave matrix");
+    return JGCM_E_NUMERIC;
+  }
+  return JGCM_OK;
+}
+
+int model_alloc(jgcm_model* md) {
+  jgcm_mesh* m = md->mesh;
+  const int nd = md->nd, N = m->N, ns = m->ns;
+  const size_t ts = tsize(m);
+  const size_t S = spec_elems(m, nd) * 2 * ts, S1 = spec_elems(m, 1) * 2 * ts;
+  const size_t G = grid_elems(m, nd) * ts, G1 = grid_elems(m, 1) * ts;
+  for (int i = 0; i < 3; i++) {
+    JG_TRY(alloc(&md->spe_vor[i], S));
+    JG_TRY(alloc(&md->spe_div[i], S));
+    JG_TRY(alloc(&md->spe_lnps[i], S1));
+    JG_TRY(alloc(&md->spe_t[i], S));
+    JG_TRY(alloc(&md->grid_u[i], G));
+    JG_TRY(alloc(&md->grid_v[i], G));
+    JG_TRY(alloc(&md->grid_ps[i], G1));
+    JG_TRY(alloc(&md->grid_t[i], G));
+  }
+  void** gnd[] = {&md->grid_vor, &md->grid_div, &md->grid_t_eq, &md->g_dlT, &md->g_dtT, &md->g_ducos, &md->g_dvcos,
+                  &md->g_dt, &md->g_energy};
+  for (auto p : gnd) JG_TRY(alloc(p, G));
+  void** g1[] = {&md->grid_lnps, &md->grid_geopots, &md->grid_h_eq, &md->g_dlps, &md->g_dtps, &md->g_dlnps};
+  for (auto p : g1) JG_TRY(alloc(p, G1));
+  void** snd[] = {&md->spe_zero, &md->spe_dvor, &md->spe_ddiv, &md->spe_dt};
+  for (auto p : snd) JG_TRY(alloc(p, S));
+  JG_TRY(alloc(&md->spe_dlnps, S1));
+  JG_TRY(alloc(&md->g_diag, grid_elems(m, 1) * (7 * (size_t)nd + 3) * 8));
+  JG_TRY(alloc(&md->coriolis, (size_t)m->nlat * ts));
+  JG_TRY(alloc(&md->damping, (size_t)(N + 1) * (ns + 1) * ts));
+  JG_TRY(alloc((void**)&md->d_W, 2 * (size_t)(N + 1) * nd * nd * 8));
+  std::vector<int2> pairs;
+  for (int mm = 0; mm <= N; mm++)
+    for (int n = mm; n <= ns; n++) pairs.push_back(make_int2(mm, n));
+  md->npairs = (int)pairs.size();
+  JG_TRY(alloc((void**)&md->d_pairs, pairs.size() * sizeof(int2)));
+  JG_CUDA(cudaMemcpy(md->d_pairs, pairs.data(), pairs.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  int nblk = ((m->nlon + 7) / 8) * m->nlat;
+  JG_TRY(alloc((void**)&md->d_partials, (size_t)3 * nblk * 8));
+  JG_TRY(alloc((void**)&md->d_scalars, 16 * 8));
+  JG_TRY(alloc((void**)&md->d_counter, 16 * sizeof(unsigned)));
+  int nt = (N + 1) * (ns + 1);
+  JG_TRY(alloc((void**)&md->damping64, (size_t)nt * 8));
+  k_fill_damping<double><<<(nt + 127) / 128, 128, 0, m->stream>>>(m->t64.eig, md->damping64, N, ns,
+                                                                  md->P.damping_coef, md->P.damping_order);
+  if (is_fp64(m)) {
+    k_fill_damping<double><<<(nt + 127) / 128, 128, 0, m->stream>>>(m->t64.eig, (double*)md->damping, N, ns,
+                                                                    md->P.damping_coef, md->P.damping_order);
+    k_fill_coriolis<double><<<(m->nlat + 127) / 128, 128, 0, m->stream>>>(m->d_sinth, (double*)md->coriolis, m->nlat,
+                                                                          md->P.omega);
+  } else {
+    k_fill_damping<float><<<(nt + 127) / 128, 128, 0, m->stream>>>(m->t64.eig, (float*)md->damping, N, ns,
+                                                                   md->P.damping_coef, md->P.damping_order);
+    k_fill_coriolis<float><<<(m->nlat + 127) / 128, 128, 0, m->stream>>>(m->d_sinth, (float*)md->coriolis, m->nlat,
+                                                                         md->P.omega);
+  }
+  JG_CUDA(cudaGetLastError());
+  JG_CUDA(cudaEventCreate(&md->ev0));
+  JG_CUDA(cudaEventCreate(&md->ev1));
+  md->div_mat = new double[nd * nd]();
+  vertical_setup(md);
+  if (md->P.kind == JGCM_HELD_SUAREZ) JG_TRY(build_wave(md));
+  JG_CUDA(cudaStreamSynchronize(m->stream));
+  return JGCM_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// plan builders
+S2GGroup sg(int op, const void* a, const void* b, int L, int col0) {
+  S2GGroup g;
+  memset(&g, 0, sizeof(g));
+  g.op = op; g.a = a; g.b = b; g.L = L; g.col0 = col0;
+  return g;
+}
+GridOutGroup og(int epi, void* dst, int L, int col0, void* dst2 = nullptr, const void* ps = nullptr) {
+  GridOutGroup g;
+  memset(&g, 0, sizeof(g));
+  g.epi = epi; g.dst = dst; g.dst2 = dst2; g.ps = ps; g.L = L; g.col0 = col0;
+  return g;
+}
+GridInGroup ig(int pro, const void* src, int L, int col0) {
+  GridInGroup g;
+  memset(&g, 0, sizeof(g));
+  g.pro = pro; g.src = src; g.L = L; g.col0 = col0;
+  return g;
+}
+SpecOutGroup og2(int op, void* dst, int L, int col0, int colA, int colB, int colE, int colH = -1) {
+  SpecOutGroup g;
+  memset(&g, 0, sizeof(g));
+  g.op = op; g.dst = dst; g.L = L; g.col0 = col0; g.colA = colA; g.colB = colB; g.colE = colE; g.colH = colH;
+  return g;
+}
+
+StepParams step_params(const jgcm_model* md) {
+  StepParams sp;
+  memset(&sp, 0, sizeof(sp));
+  sp.init_step = md->init_step;
+  sp.dt = md->P.dt;
+  sp.robert = md->P.robert_coef;
+  sp.implicit_coef = md->P.implicit_coef;
+  sp.h0 = md->P.h0;
+  sp.damping = md->damping;
+  return sp;
+}
+
+template <typename T>
+int s2g_final_uv(jgcm_model* md, int lev_n, cudaStream_t st);
+
+// Barotropic_Dynamics! (Barotropic_Dynamics.jl:2-46)
+template <typename T>
+int step_barotropic(jgcm_model* md, cudaStream_t st) {
+  jgcm_mesh* m = md->mesh;
+  const int nd = md->nd, p = lvl(md, 0), c = lvl(md, 1), n = lvl(md, 2);
+  FFTPlan fp;
+  memset(&fp, 0, sizeof(fp));
+  fp.ng = 2;
+  fp.C = 2 * nd;
+  fp.kappa_m = 0.0;
+  fp.coriolis = md->coriolis;
+  fp.g[0] = ig(PRO_FLUXU, md->grid_u[c], nd, 0);
+  fp.g[0].s1 = md->grid_v[c];
+  fp.g[0].s2 = md->grid_vor;
+  fp.g[1] = ig(PRO_FLUXV, md->grid_u[c], nd, nd);
+  fp.g[1].s1 = md->grid_v[c];
+  fp.g[1].s2 = md->grid_vor;
+  G2SPlan gp;
+  memset(&gp, 0, sizeof(gp));
+  gp.ng = 1;
+  gp.C = nd;
+  gp.sp = step_params(md);
+  gp.g[0] = og2(G2S_BARO, md->spe_vor[n], nd, 0, nd, 0, -1);  // A = δv cos, B = δu cos
+  gp.g[0].qc[0] = md->spe_vor[c];
+  gp.g[0].qp[0] = md->spe_vor[p];
+  JG_TRY(launch_g2s<T>(m, fp, gp, st));
+  S2GPlan sp;
+  memset(&sp, 0, sizeof(sp));
+  sp.ng = 3;
+  sp.C = 3 * nd;
+  sp.g[0] = sg(S2G_PLAIN, md->spe_vor[n], nullptr, nd, 0);
+  sp.g[1] = sg(S2G_UCOS, md->spe_vor[n], md->spe_zero, nd, nd);
+  sp.g[2] = sg(S2G_VCOS, md->spe_vor[n], md->spe_zero, nd, 2 * nd);
+  IFFTPlan ip;
+  memset(&ip, 0, sizeof(ip));
+  ip.ng = 3;
+  ip.C = 3 * nd;
+  ip.g[0] = og(EPI_NONE, md->grid_vor, nd, 0);
+  ip.g[1] = og(EPI_DIVCOS, md->grid_u[n], nd, nd);
+  ip.g[2] = og(EPI_DIVCOS, md->grid_v[n], nd, 2 * nd);
+  JG_TRY(launch_s2g<T>(m, sp, ip, st));
+  return JGCM_OK;
+}
+
+// Shallow_Water_Physics! + Shallow_Water_Dynamics! (Shallow_Water_Dynamics.jl:7-179).
+// h lives in the lnps/ps slots; the advected height is spe_h_n, which equals spe_h_c after the
+// first Time_Advance! (Shallow_Water_Dynamics.jl:147).
+template <typename T>
+int step_shallow_water(jgcm_model* md, cudaStream_t st) {
+  jgcm_mesh* m = md->mesh;
+  const int p = lvl(md, 0), c = lvl(md, 1), n = lvl(md, 2);
+  const void* h_adv = md->sw_adv_from_n ? md->spe_lnps[n] : md->spe_lnps[c];
+  S2GPlan sp;
+  memset(&sp, 0, sizeof(sp));
+  sp.ng = 2;
+  sp.C = 2;
+  sp.g[0] = sg(S2G_DLAM, h_adv, nullptr, 1, 0);
+  sp.g[1] = sg(S2G_DTH, h_adv, nullptr, 1, 1);
+  IFFTPlan ip;
+  memset(&ip, 0, sizeof(ip));
+  ip.ng = 2;
+  ip.C = 2;
+  ip.g[0] = og(EPI_DIVCOS, md->g_dlps, 1, 0);
+  ip.g[1] = og(EPI_DIVCOS, md->g_dtps, 1, 1);
+  JG_TRY(launch_s2g<T>(m, sp, ip, st));
+  FFTPlan fp;
+  memset(&fp, 0, sizeof(fp));
+  fp.ng = 4;
+  fp.C = 4;
+  fp.kappa_m = md->P.kappa_m;
+  fp.kappa_t = md->P.kappa_t;
+  fp.coriolis = md->coriolis;
+  fp.g[0] = ig(PRO_FLUXU, md->grid_u[c], 1, 0);
+  fp.g[0].s1 = md->grid_v[c];
+  fp.g[0].s2 = md->grid_vor;
+  fp.g[1] = ig(PRO_FLUXV, md->grid_u[c], 1, 1);
+  fp.g[1].s1 = md->grid_v[c];
+  fp.g[1].s2 = md->grid_vor;
+  fp.g[2] = ig(PRO_KIN, md->grid_u[c], 1, 2);
+  fp.g[2].s1 = md->grid_v[c];
+  fp.g[3] = ig(PRO_SWH, md->grid_ps[c], 1, 3);
+  fp.g[3].s1 = md->grid_u[c];
+  fp.g[3].s2 = md->grid_v[c];
+  fp.g[3].s3 = md->g_dlps;
+  fp.g[3].s4 = md->g_dtps;
+  fp.g[3].s5 = md->grid_div;
+  fp.g[3].s6 = md->grid_h_eq;
+  G2SPlan gp;
+  memset(&gp, 0, sizeof(gp));
+  gp.ng = 1;
+  gp.C = 1;
+  gp.sp = step_params(md);
+  gp.g[0] = og2(G2S_SW, md->spe_vor[n], 1, 0, 0, 1, 2, 3);
+  gp.g[0].dst2 = md->spe_div[n];
+  gp.g[0].dst3 = md->spe_lnps[n];
+  gp.g[0].qc[0] = md->spe_vor[c];
+  gp.g[0].qc[1] = md->spe_div[c];
+  gp.g[0].qc[2] = md->spe_lnps[c];
+  gp.g[0].qp[0] = md->spe_vor[p];
+  gp.g[0].qp[1] = md->spe_div[p];
+  gp.g[0].qp[2] = md->spe_lnps[p];
+  JG_TRY(launch_g2s<T>(m, fp, gp, st));
+  S2GPlan sp2;
+  memset(&sp2, 0, sizeof(sp2));
+  sp2.ng = 5;
+  sp2.C = 5;
+  sp2.g[0] = sg(S2G_PLAIN, md->spe_vor[n], nullptr, 1, 0);
+  sp2.g[1] = sg(S2G_PLAIN, md->spe_div[n], nullptr, 1, 1);
+  sp2.g[2] = sg(S2G_PLAIN, md->spe_lnps[n], nullptr, 1, 2);
+  sp2.g[3] = sg(S2G_UCOS, md->spe_vor[n], md->spe_div[n], 1, 3);
+  sp2.g[4] = sg(S2G_VCOS, md->spe_vor[n], md->spe_div[n], 1, 4);
+  IFFTPlan ip2;
+  memset(&ip2, 0, sizeof(ip2));
+  ip2.ng = 5;
+  ip2.C = 5;
+  ip2.g[0] = og(EPI_NONE, md->grid_vor, 1, 0);
+  ip2.g[1] = og(EPI_NONE, md->grid_div, 1, 1);
+  ip2.g[2] = og(EPI_NONE, md->grid_ps[n], 1, 2);
+  ip2.g[3] = og(EPI_DIVCOS, md->grid_u[n], 1, 3);
+  ip2.g[4] = og(EPI_DIVCOS, md->grid_v[n], 1, 4);
+  JG_TRY(launch_s2g<T>(m, sp2, ip2, st));
+  return JGCM_OK;
+}
+
+// Atmosphere_Update! (Spectral_Dynamics.jl:470-490) for Held-Suarez.
+template <typename T>
+int step_held_suarez(jgcm_model* md, cudaStream_t st) {
+  jgcm_mesh* m = md->mesh;
+  const int nd = md->nd, p = lvl(md, 0), c = lvl(md, 1), n = lvl(md, 2);
+  const int Dt = md->init_step ? md->P.dt : 2 * md->P.dt;
+  // 1. gradients of lnps_c (-> ∇ps = ∇lnps * ps) and of T_c
+  S2GPlan sp;
+  memset(&sp, 0, sizeof(sp));
+  sp.ng = 4;
+  sp.C = 2 + 2 * nd;
+  sp.g[0] = sg(S2G_DLAM, md->spe_lnps[c], nullptr, 1, 0);
+  sp.g[1] = sg(S2G_DTH, md->spe_lnps[c], nullptr, 1, 1);
+  sp.g[2] = sg(S2G_DLAM, md->spe_t[c], nullptr, nd, 2);
+  sp.g[3] = sg(S2G_DTH, md->spe_t[c], nullptr, nd, 2 + nd);
+  IFFTPlan ip;
+  memset(&ip, 0, sizeof(ip));
+  ip.ng = 4;
+  ip.C = 2 + 2 * nd;
+  ip.g[0] = og(EPI_DIVCOS_MULPS, md->g_dlps, 1, 0, nullptr, md->grid_ps[c]);
+  ip.g[1] = og(EPI_DIVCOS_MULPS, md->g_dtps, 1, 1, nullptr, md->grid_ps[c]);
+  ip.g[2] = og(EPI_DIVCOS, md->g_dlT, nd, 2);
+  ip.g[3] = og(EPI_DIVCOS, md->g_dtT, nd, 2 + nd);
+  JG_TRY(launch_s2g<T>(m, sp, ip, st));
+  // 2. physics + grid dynamics (one warp per column)
+  Tables<T> tb = tables<T>(m);
+  HSColArgs<T> a;
+  memset(&a, 0, sizeof(a));
+  a.u_p = (const T*)md->grid_u[p];
+  a.v_p = (const T*)md->grid_v[p];
+  a.t_p = (const T*)md->grid_t[p];
+  a.ps_p = (const T*)md->grid_ps[p];
+  a.ps_c = (const T*)md->grid_ps[c];
+  a.u_c = (const T*)md->grid_u[c];
+  a.v_c = (const T*)md->grid_v[c];
+  a.t_c = (const T*)md->grid_t[c];
+  a.div = (const T*)md->grid_div;
+  a.vor = (const T*)md->grid_vor;
+  a.dlps = (const T*)md->g_dlps;
+  a.dtps = (const T*)md->g_dtps;
+  a.dlT = (const T*)md->g_dlT;
+  a.dtT = (const T*)md->g_dtT;
+  a.geopots = (const T*)md->grid_geopots;
+  a.coriolis = (const T*)md->coriolis;
+  a.sinj = tb.sinj;
+  a.cosj = tb.cosj;
+  a.ducos = (T*)md->g_ducos;
+  a.dvcos = (T*)md->g_dvcos;
+  a.dtg = (T*)md->g_dt;
+  a.energy = (T*)md->g_energy;
+  a.dlnps = (T*)md->g_dlnps;
+  a.t_eq = (T*)md->grid_t_eq;
+  a.wts = m->d_wts;
+  a.partials = md->d_partials;
+  a.scalars = md->d_scalars;
+  a.counter = md->d_counter;
+  a.nd = nd;
+  a.nlat = m->nlat;
+  a.nlon = m->nlon;
+  a.Dt = Dt;
+  a.sigma_b = md->P.sigma_b;
+  a.k_f = md->P.k_f;
+  a.k_a = md->P.k_a;
+  a.k_s = md->P.k_s;
+  a.dT_y = md->P.dT_y;
+  a.dtheta_z = md->P.dtheta_z;
+  a.kappa = md->P.kappa;
+  a.rdgas = md->P.rdgas;
+  a.cp = md->cp_air;
+  a.grav = md->P.grav;
+  dim3 gcol((m->nlon + 7) / 8, m->nlat);
+  k_hs_column<T><<<gcol, 256, 0, st>>>(a, md->vc);
+  JG_CUDA(cudaGetLastError());
+  // 3. forward transforms: δu cos, δv cos, δT, energy, δlnps -> vor/div tendencies (alpha
+  //    operator, δdiv -= ∇²E), δT, δlnps
+  FFTPlan fp;
+  memset(&fp, 0, sizeof(fp));
+  fp.ng = 5;
+  fp.C = 4 * nd + 1;
+  fp.g[0] = ig(PRO_NONE, md->g_ducos, nd, 0);
+  fp.g[1] = ig(PRO_NONE, md->g_dvcos, nd, nd);
+  fp.g[2] = ig(PRO_NONE, md->g_dt, nd, 2 * nd);
+  fp.g[3] = ig(PRO_NONE, md->g_energy, nd, 3 * nd);
+  fp.g[4] = ig(PRO_NONE, md->g_dlnps, 1, 4 * nd);
+  G2SPlan gp;
+  memset(&gp, 0, sizeof(gp));
+  gp.ng = 4;
+  gp.C = 3 * nd + 1;
+  gp.g[0] = og2(G2S_VOR, md->spe_dvor, nd, 0, nd, 0, -1);
+  gp.g[1] = og2(G2S_DIV, md->spe_ddiv, nd, nd, 0, nd, 3 * nd);
+  gp.g[2] = og2(G2S_PLAIN, md->spe_dt, nd, 2 * nd, 2 * nd, -1, -1);
+  gp.g[3] = og2(G2S_PLAIN, md->spe_dlnps, 1, 3 * nd, 4 * nd, -1, -1);
+  JG_TRY(launch_g2s<T>(m, fp, gp, st));
+  // 4. semi-implicit correction, damping, leapfrog (FP64, warp per mode)
+  ImplArgs<T> ia;
+  memset(&ia, 0, sizeof(ia));
+  using V = V2<T>;
+  ia.dvor = (const V*)md->spe_dvor;
+  ia.ddiv = (const V*)md->spe_ddiv;
+  ia.dtend = (const V*)md->spe_dt;
+  ia.dlnps = (const V*)md->spe_dlnps;
+  ia.vor_p = (V*)md->spe_vor[p]; ia.vor_c = (V*)md->spe_vor[c]; ia.vor_n = (V*)md->spe_vor[n];
+  ia.div_p = (V*)md->spe_div[p]; ia.div_c = (V*)md->spe_div[c]; ia.div_n = (V*)md->spe_div[n];
+  ia.t_p = (V*)md->spe_t[p]; ia.t_c = (V*)md->spe_t[c]; ia.t_n = (V*)md->spe_t[n];
+  ia.lnps_p = (V*)md->spe_lnps[p]; ia.lnps_c = (V*)md->spe_lnps[c]; ia.lnps_n = (V*)md->spe_lnps[n];
+  ia.eig = m->t64.eig;
+  ia.damping = md->damping64;
+  ia.W = md->d_W + (md->init_step ? 0 : (size_t)(m->N + 1) * nd * nd);
+  ia.pairs = md->d_pairs;
+  ia.npairs = md->npairs;
+  ia.nd = nd;
+  ia.ns = m->ns;
+  ia.N = m->N;
+  ia.init_step = md->init_step;
+  ia.dt = md->P.dt;
+  ia.xi = md->init_step ? md->P.dt * md->P.implicit_coef : (2 * md->P.dt) * md->P.implicit_coef;
+  ia.ps_ref = md->P.ps_ref;
+  ia.kappa = md->P.kappa;
+  ia.rdgas = md->P.rdgas;
+  ia.robert = md->P.robert_coef;
+  k_hs_implicit<T><<<(md->npairs + 7) / 8, 256, 0, st>>>(ia, md->vc);
+  JG_CUDA(cudaGetLastError());
+  // 5. back to the grid: vor, div, u, v, T, lnps (+ ps = exp(lnps))
+  S2GPlan s2;
+  memset(&s2, 0, sizeof(s2));
+  s2.ng = 6;
+  s2.C = 5 * nd + 1;
+  s2.g[0] = sg(S2G_PLAIN, md->spe_vor[n], nullptr, nd, 0);
+  s2.g[1] = sg(S2G_PLAIN, md->spe_div[n], nullptr, nd, nd);
+  s2.g[2] = sg(S2G_UCOS, md->spe_vor[n], md->spe_div[n], nd, 2 * nd);
+  s2.g[3] = sg(S2G_VCOS, md->spe_vor[n], md->spe_div[n], nd, 3 * nd);
+  s2.g[4] = sg(S2G_PLAIN, md->spe_t[n], nullptr, nd, 4 * nd);
+  s2.g[5] = sg(S2G_PLAIN, md->spe_lnps[n], nullptr, 1, 5 * nd);
+  IFFTPlan i2;
+  memset(&i2, 0, sizeof(i2));
+  i2.ng = 6;
+  i2.C = 5 * nd + 1;
+  i2.g[0] = og(EPI_NONE, md->grid_vor, nd, 0);
+  i2.g[1] = og(EPI_NONE, md->grid_div, nd, nd);
+  i2.g[2] = og(EPI_DIVCOS, md->grid_u[n], nd, 2 * nd);
+  i2.g[3] = og(EPI_DIVCOS, md->grid_v[n], nd, 3 * nd);
+  i2.g[4] = og(EPI_NONE, md->grid_t[n], nd, 4 * nd);
+  i2.g[5] = og(EPI_EXP2, md->grid_lnps, 1, 5 * nd, md->grid_ps[n]);
+  JG_TRY(launch_s2g<T>(m, s2, i2, st));
+  // 6. mass and energy fixers
+  CorrArgs<T> ca;
+  memset(&ca, 0, sizeof(ca));
+  ca.u_n = (const T*)md->grid_u[n];
+  ca.v_n = (const T*)md->grid_v[n];
+  ca.t_n = (const T*)md->grid_t[n];
+  ca.ps_n = (const T*)md->grid_ps[n];
+  ca.lnps_n = (V*)md->spe_lnps[n];
+  ca.t_spec_n = (V*)md->spe_t[n];
+  ca.wts = m->d_wts;
+  ca.partials = md->d_partials;
+  ca.scalars = md->d_scalars;
+  ca.counter = md->d_counter;
+  ca.nd = nd;
+  ca.nlat = m->nlat;
+  ca.nlon = m->nlon;
+  ca.do_mass = md->P.do_mass_correction;
+  ca.do_energy = md->P.do_energy_correction;
+  ca.cp = md->cp_air;
+  ca.grav = md->P.grav;
+  k_hs_corr_reduce<T><<<gcol, 256, 0, st>>>(ca, md->vc);
+  JG_CUDA(cudaGetLastError());
+  size_t nt = grid_elems(m, nd), nps = grid_elems(m, 1);
+  int nb = (int)((nt + 255) / 256);
+  if (nb > 4 * 152) nb = 4 * 152;
+  k_hs_corr_apply<T><<<nb, 256, 0, st>>>((T*)md->grid_t[n], (T*)md->grid_ps[n], md->d_scalars, nt, nps);
+  JG_CUDA(cudaGetLastError());
+  return JGCM_OK;
+}
+
+template <typename T>
+int issue_step(jgcm_model* md, cudaStream_t st) {
+  switch (md->P.kind) {
+    case JGCM_BAROTROPIC:
+      return step_barotropic<T>(md, st);
+    case JGCM_SHALLOW_WATER:
+      return step_shallow_water<T>(md, st);
+    default:
+      return step_held_suarez<T>(md, st);
+  }
+}
+
+int issue(jgcm_model* md, cudaStream_t st) {
+  return is_fp64(md->mesh) ? issue_step<double>(md, st) : issue_step<float>(md, st);
+}
+
+void after_step(jgcm_model* md) {
+  md->rot = (md->rot + 1) % 3;
+  md->init_step = 0;
+  md->sw_adv_from_n = 0;
+  md->steps_done++;
+}
+
+// One steady step through a CUDA graph captured for the current rotation phase.
+int graph_step(jgcm_model* md) {
+  jgcm_mesh* m = md->mesh;
+  int ph = md->rot;
+  if (!md->graph[ph]) {
+    cudaGraph_t g;
+    JG_CUDA(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+    int s = issue(md, m->stream);
+    cudaError_t e = cudaStreamEndCapture(m->stream, &g);
+    if (s != JGCM_OK) {
+      if (e == cudaSuccess) cudaGraphDestroy(g);
+      return s;
+    }
+    JG_CUDA(e);
+    cudaError_t e2 = cudaGraphInstantiate(&md->graph[ph], g, 0);
+    cudaGraphDestroy(g);
+    JG_CUDA(e2);
+  }
+  JG_CUDA(cudaGraphLaunch(md->graph[ph], m->stream));
+  after_step(md);
+  return JGCM_OK;
+}
+
+int model_step(jgcm_model* md) {
+  if (md->init_step || md->sw_adv_from_n) {
+    JG_TRY(issue(md, md->mesh->stream));
+    after_step(md);
+    return JGCM_OK;
+  }
+  return graph_step(md);
+}
+
+// ------------------------------------------------------------------------------------------
+struct FieldRef {
+  void* ptr;
+  int L;        // levels
+  bool spec;    // spectral (complex) vs grid
+  bool derived; // computed on demand, FP64 in g_diag at `off`
+  size_t off;
+  bool state;   // writable
+};
+
+bool lookup(jgcm_model* md, const std::string& nm, FieldRef* f) {
+  const int nd = md->nd;
+  const size_t G = grid_elems(md->mesh, 1);
+  auto lev = [&](const std::string& suf) -> int {
+    if (suf == "p") return lvl(md, 0);
+    if (suf == "c") return lvl(md, 1);
+    if (suf == "n") return lvl(md, 2);
+    return -1;
+  };
+  *f = FieldRef{nullptr, 0, false, false, 0, true};
+  auto tl = [&](const char* base, void* const* arr, int L, bool spec) -> bool {
+    std::string b(base);
+    if (nm.size() == b.size() + 2 && nm.compare(0, b.size(), b) == 0 && nm[b.size()] == '_') {
+      int l = lev(nm.substr(b.size() + 1));
+      if (l < 0) return false;
+      *f = FieldRef{arr[l], L, spec, false, 0, true};
+      return true;
+    }
+    return false;
+  };
+  if (tl("spe_vor", md->spe_vor, nd, true) || tl("spe_div", md->spe_div, nd, true) ||
+      tl("spe_lnps", md->spe_lnps, 1, true) || tl("spe_t", md->spe_t, nd, true) || tl("grid_u", md->grid_u, nd, false) ||
+      tl("grid_v", md->grid_v, nd, false) || tl("grid_ps", md->grid_ps, 1, false) || tl("grid_t", md->grid_t, nd, false))
+    return true;
+  struct {
+    const char* n;
+    void* p;
+    int L;
+    bool spec;
+  } single[] = {{"grid_vor", md->grid_vor, nd, false},   {"grid_div", md->grid_div, nd, false},
+                {"grid_lnps", md->grid_lnps, 1, false},  {"grid_t_eq", md->grid_t_eq, nd, false},
+                {"grid_geopots", md->grid_geopots, 1, false}, {"grid_h_eq", md->grid_h_eq, 1, false}};
+  for (auto& s : single)
+    if (nm == s.n) {
+      *f = FieldRef{s.p, s.L, s.spec, false, 0, true};
+      return true;
+    }
+  struct {
+    const char* n;
+    int L;
+    size_t off;
+  } der[] = {{"grid_p_half", nd + 1, 0},
+             {"grid_lnp_half", nd + 1, G * (nd + 1)},
+             {"grid_dp", nd, 2 * G * (nd + 1)},
+             {"grid_p_full", nd, 2 * G * (nd + 1) + G * nd},
+             {"grid_lnp_full", nd, 2 * G * (nd + 1) + 2 * G * nd},
+             {"grid_z_full", nd, 2 * G * (nd + 1) + 3 * G * nd},
+             {"grid_z_half", nd + 1, 2 * G * (nd + 1) + 4 * G * nd}};
+  for (auto& d : der)
+    if (nm == d.n) {
+      *f = FieldRef{nullptr, d.L, false, true, d.off, false};
+      return true;
+    }
+  return false;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+extern "C" int jgcm_model_create(jgcm_mesh* mesh, const jgcm_params* params, jgcm_model** out) {
+  JG_ARG(mesh && params && out, "NULL argument");
+  *out = nullptr;
+  JG_ARG(params->kind >= JGCM_BAROTROPIC && params->kind <= JGCM_HELD_SUAREZ, "unknown model kind");
+  JG_ARG(params->dt > 0, "dt must be positive");
+  JG_ARG(params->damping_order % 2 == 0, "damping_order must be even (Time_Integrator.jl:24)");
+  if (params->kind != JGCM_HELD_SUAREZ) JG_ARG(mesh->nd == 1 || params->kind == JGCM_BAROTROPIC, "shallow water needs nd = 1");
+  if (params->kind == JGCM_SHALLOW_WATER) JG_ARG(mesh->nd == 1, "shallow water needs nd = 1");
+  if (params->kind == JGCM_HELD_SUAREZ) JG_ARG(mesh->nd <= 32, "Held-Suarez supports nd <= 32 (one warp per column)");
+  jgcm_model* md = new jgcm_model();
+  md->mesh = mesh;
+  md->P = *params;
+  md->nd = mesh->nd;
+  md->init_step = 1;
+  md->sw_adv_from_n = 1;
+  md->cp_air = params->rdgas / params->kappa;
+  int s = model_alloc(md);
+  if (s != JGCM_OK) {
+    model_free(md);
+    return s;
+  }
+  *out = md;
+  return JGCM_OK;
+}
+
+extern "C" int jgcm_model_destroy(jgcm_model* md) {
+  if (!md) return JGCM_OK;
+  cudaStreamSynchronize(md->mesh->stream);
+  model_free(md);
+  return JGCM_OK;
+}
+
+extern "C" int jgcm_model_step(jgcm_model* md, int nsteps) {
+  JG_ARG(md && nsteps >= 0, "bad arguments");
+  for (int s = 0; s < nsteps; s++) JG_TRY(model_step(md));
+  JG_CUDA(cudaStreamSynchronize(md->mesh->stream));
+  return JGCM_OK;
+}
+
+extern "C" int jgcm_model_init_step(jgcm_model* md, int* init_step) {
+  JG_ARG(md && init_step, "NULL argument");
+  *init_step = md->init_step;
+  return JGCM_OK;
+}
+
+extern "C" int jgcm_model_launches_per_step(jgcm_model* md, int* launches) {
+  JG_ARG(md && launches, "NULL argument");
+  *launches = md->P.kind == JGCM_BAROTROPIC ? 4 : md->P.kind == JGCM_SHALLOW_WATER ? 6 : 10;
+  return JGCM_OK;
+}
+
+extern "C" int jgcm_model_time_steps(jgcm_model* md, int nsteps, float* ms) {
+  JG_ARG(md && ms && nsteps > 0, "bad arguments");
+  jgcm_mesh* m = md->mesh;
+  if (md->init_step) JG_TRY(model_step(md));
+  // make sure every phase is captured before timing
+  for (int s = 0; s < 3 && md->steps_done < 4; s++) JG_TRY(model_step(md));
+  JG_CUDA(cudaStreamSynchronize(m->stream));
+  JG_CUDA(cudaEventRecord(md->ev0, m->stream));
+  for (int s = 0; s < nsteps; s++) JG_TRY(graph_step(md));
+  JG_CUDA(cudaEventRecord(md->ev1, m->stream));
+  JG_CUDA(cudaEventSynchronize(md->ev1));
+  JG_CUDA(cudaEventElapsedTime(ms, md->ev0, md->ev1));
+  return JGCM_OK;
+}
+
+extern "C" int jgcm_model_get_field(jgcm_model* md, const char* name, double* host, long cap, long* count) {
+  JG_ARG(md && name, "NULL argument");
+  FieldRef f;
+  JG_ARG(lookup(md, name, &f), "unknown field '%s'", name);
+  jgcm_mesh* m = md->mesh;
+  size_t n = f.spec ? 2 * spec_elems(m, f.L) : grid_elems(m, f.L);
+  if (count) *count = (long)n;
+  if (!host) return JGCM_OK;
+  JG_ARG(cap >= (long)n, "buffer too small for '%s'", name);
+  cudaStream_t st = m->stream;
+  double* stage = m->d_stage;
+  if (f.derived) {
+    size_t G = grid_elems(m, 1);
+    int nb = (int)((G + 127) / 128);
+    int c = lvl(md, 1);
+    if (is_fp64(m))
+      k_pressure_heights<double><<<nb, 128, 0, st>>>((const double*)md->grid_ps[c], (const double*)md->grid_t[c],
+                                                     (const double*)md->grid_geopots, (double*)md->g_diag, md->vc,
+                                                     md->nd, G, md->P.rdgas, md->P.grav);
+    else
+      k_pressure_heights<float><<<nb, 128, 0, st>>>((const float*)md->grid_ps[c], (const float*)md->grid_t[c],
+                                                    (const float*)md->grid_geopots, (double*)md->g_diag, md->vc,
+                                                    md->nd, G, md->P.rdgas, md->P.grav);
+    JG_CUDA(cudaGetLastError());
+    JG_CUDA(cudaMemcpyAsync(host, (double*)md->g_diag + f.off, n * 8, cudaMemcpyDeviceToHost, st));
+  } else if (f.spec) {
+    JG_TRY(spec_dev_to_host(m, f.ptr, stage, f.L, st));
+    JG_CUDA(cudaMemcpyAsync(host, stage, n * 8, cudaMemcpyDeviceToHost, st));
+  } else {
+    JG_TRY(grid_dev_to_host(m, f.ptr, stage, n, st));
+    JG_CUDA(cudaMemcpyAsync(host, stage, n * 8, cudaMemcpyDeviceToHost, st));
+  }
+  JG_CUDA(cudaStreamSynchronize(st));
+  return JGCM_OK;
+}
+
+extern "C" int jgcm_model_set_field(jgcm_model* md, const char* name, const double* host, long count) {
+  JG_ARG(md && name && host, "NULL argument");
+  FieldRef f;
+  JG_ARG(lookup(md, name, &f), "unknown field '%s'", name);
+  JG_ARG(f.state, "field '%s' is derived and cannot be set", name);
+  jgcm_mesh* m = md->mesh;
+  size_t n = f.spec ? 2 * spec_elems(m, f.L) : grid_elems(m, f.L);
+  JG_ARG(count == (long)n, "field '%s' needs %zu doubles, got %ld", name, n, count);
+  cudaStream_t st = m->stream;
+  JG_CUDA(cudaStreamSynchronize(st));
+  JG_CUDA(cudaMemcpyAsync(m->d_stage, host, n * 8, cudaMemcpyHostToDevice, st));
+  if (f.spec)
+    JG_TRY(spec_host_to_dev(m, m->d_stage, f.ptr, f.L, st));
+  else
+    JG_TRY(grid_host_to_dev(m, m->d_stage, f.ptr, n, st));
+  if (!strcmp(name, "spe_lnps_n")) md->sw_adv_from_n = 1;
+  JG_CUDA(cudaStreamSynchronize(st));
+  return JGCM_OK;
+}
+
+extern "C" int jgcm_model_semi_implicit(jgcm_model* md, const char* name, double* out, long cap, long* count) {
+  JG_ARG(md && name, "NULL argument");
+  JG_ARG(md->P.kind == JGCM_HELD_SUAREZ, "semi-implicit matrices exist for Held-Suarez only");
+  const int nd = md->nd, N = md->mesh->N;
+  std::string nm(name);
+  std::vector<double> res;
+  if (nm == "div_mat") res.assign(md->div_mat, md->div_mat + nd * nd);
+  else if (nm == "h") res.assign(md->vc.h, md->vc.h + nd);
+  else if (nm == "wave_matrix") {
+    std::vector<double> w((size_t)(N + 1) * nd * nd);
+    size_t off = md->init_step ? 0 : (size_t)(N + 1) * nd * nd;
+    JG_CUDA(cudaMemcpy(w.data(), md->d_W + off, w.size() * 8, cudaMemcpyDeviceToHost));
+    res.assign(w.size(), 0.0);
+    for (int n = 0; n <= N; n++)
+      for (int c = 0; c < nd; c++)
+        for (int r = 0; r < nd; r++) res[(size_t)n * nd * nd + r + (size_t)nd * c] = w[(size_t)n * nd * nd + (size_t)c * nd + r];
+  } else {
+    set_error("unknown semi-implicit item '%s'", name);
+    return JGCM_E_ARG;
+  }
+  if (count) *count = (long)res.size();
+  if (out) {
+    JG_ARG(cap >= (long)res.size(), "buffer too small");
+    memcpy(out, res.data(), res.size() * 8);
+  }
+  return JGCM_OK;
+}
+
+// Spectral_Initialize_Fields! (Spectral_Dynamics.jl:372-449) on the device.
+extern "C" int jgcm_spectral_initialize_fields(jgcm_model* md, const double* grid_t_pert, int vorticity_seed) {
+  JG_ARG(md, "NULL model");
+  jgcm_mesh* m = md->mesh;
+  const int nd = md->nd, N = m->N, ns = m->ns;
+  const size_t G = grid_elems(m, 1);
+  JG_ARG(N >= 5 && ns >= 9 || !vorticity_seed, "the vorticity seed needs num_fourier >= 5");
+  // host-side grid fields (FP64), uploaded through set_field
+  std::vector<double> gt(G * nd), geo(G), lnps(G), ps(G), spv(2 * spec_elems(m, nd), 0.0);
+  long cnt = 0;
+  JG_TRY(jgcm_model_get_field(md, "grid_geopots", geo.data(), (long)geo.size(), &cnt));
+  for (size_t x = 0; x < G * nd; x++) gt[x] = md->P.init_t + (grid_t_pert ? grid_t_pert[x] : 0.0);
+  for (size_t x = 0; x < G; x++) lnps[x] = std::log(md->P.sea_level_ps_ref) - geo[x] / (md->P.rdgas * md->P.init_t);
+  for (size_t x = 0; x < G; x++) ps[x] = std::exp(lnps[x]);
+  if (vorticity_seed) {
+    double ip = 1.0e-7 / std::sqrt(2.0);
+    auto six = [&](int mm, int n, int k) { return 2 * ((size_t)mm + (size_t)(N + 1) * ((size_t)n + (size_t)(ns + 1) * k)); };
+    for (int k = nd - 3; k < nd; k++) {
+      if (k < 0) continue;
+      spv[six(1, 4, k)] = ip;
+      spv[six(5, 8, k)] = ip;
+      spv[six(1, 3, k)] = ip;
+      spv[six(5, 7, k)] = ip;
+    }
+  }
+  std::vector<double> zero(spv.size(), 0.0);
+  JG_TRY(jgcm_model_set_field(md, "grid_t_c", gt.data(), (long)gt.size()));
+  JG_TRY(jgcm_model_set_field(md, "grid_lnps", lnps.data(), (long)lnps.size()));
+  JG_TRY(jgcm_model_set_field(md, "grid_ps_c", ps.data(), (long)ps.size()));
+  JG_TRY(jgcm_model_set_field(md, "spe_div_c", zero.data(), (long)zero.size()));
+  JG_TRY(jgcm_model_set_field(md, "spe_vor_c", spv.data(), (long)spv.size()));
+  const int c = lvl(md, 1), p = lvl(md, 0);
+  cudaStream_t st = m->stream;
+  auto run = [&](auto tag) -> int {
+    using T = decltype(tag);
+    // UV_Grid_From_Vor_Div!(vor_c, div_c) -> u_c, v_c
+    auto uv = [&]() -> int {
+      S2GPlan sp;
+      memset(&sp, 0, sizeof(sp));
+      sp.ng = 2; sp.C = 2 * nd;
+      sp.g[0] = sg(S2G_UCOS, md->spe_vor[c], md->spe_div[c], nd, 0);
+      sp.g[1] = sg(S2G_VCOS, md->spe_vor[c], md->spe_div[c], nd, nd);
+      IFFTPlan ip;
+      memset(&ip, 0, sizeof(ip));
+      ip.ng = 2; ip.C = 2 * nd;
+      ip.g[0] = og(EPI_DIVCOS, md->grid_u[c], nd, 0);
+      ip.g[1] = og(EPI_DIVCOS, md->grid_v[c], nd, nd);
+      return launch_s2g<T>(m, sp, ip, st);
+    };
+    auto g2s_plain = [&](const void* grid, void* spec, int L) -> int {
+      FFTPlan fp;
+      memset(&fp, 0, sizeof(fp));
+      fp.ng = 1; fp.C = L;
+      fp.g[0] = ig(PRO_NONE, grid, L, 0);
+      G2SPlan gp;
+      memset(&gp, 0, sizeof(gp));
+      gp.ng = 1; gp.C = L;
+      gp.g[0] = og2(G2S_PLAIN, spec, L, 0, 0, -1, -1);
+      return launch_g2s<T>(m, fp, gp, st);
+    };
+    auto s2g_plain = [&](const void* spec, void* grid, int L, int epi, void* dst2) -> int {
+      S2GPlan sp;
+      memset(&sp, 0, sizeof(sp));
+      sp.ng = 1; sp.C = L;
+      sp.g[0] = sg(S2G_PLAIN, spec, nullptr, L, 0);
+      IFFTPlan ip;
+      memset(&ip, 0, sizeof(ip));
+      ip.ng = 1; ip.C = L;
+      ip.g[0] = og(epi, grid, L, 0, dst2);
+      return launch_s2g<T>(m, sp, ip, st);
+    };
+    JG_TRY(uv());
+    JG_TRY(g2s_plain(md->grid_t[c], md->spe_t[c], nd));
+    JG_TRY(s2g_plain(md->spe_t[c], md->grid_t[c], nd, EPI_NONE, nullptr));
+    JG_TRY(g2s_plain(md->grid_lnps, md->spe_lnps[c], 1));
+    JG_TRY(s2g_plain(md->spe_lnps[c], md->grid_lnps, 1, EPI_EXP2, md->grid_ps[c]));
+    {  // Vor_Div_From_Grid_UV!(u_c, v_c) -> vor_c, div_c
+      FFTPlan fp;
+      memset(&fp, 0, sizeof(fp));
+      fp.ng = 2; fp.C = 2 * nd;
+      fp.g[0] = ig(PRO_MULCOS, md->grid_u[c], nd, 0);
+      fp.g[1] = ig(PRO_MULCOS, md->grid_v[c], nd, nd);
+      G2SPlan gp;
+      memset(&gp, 0, sizeof(gp));
+      gp.ng = 2; gp.C = 2 * nd;
+      gp.g[0] = og2(G2S_VOR, md->spe_vor[c], nd, 0, nd, 0, -1);
+      gp.g[1] = og2(G2S_DIV, md->spe_div[c], nd, nd, 0, nd, -1);
+      JG_TRY(launch_g2s<T>(m, fp, gp, st));
+    }
+    JG_TRY(uv());
+    JG_TRY(s2g_plain(md->spe_vor[c], md->grid_vor, nd, EPI_NONE, nullptr));
+    JG_TRY(s2g_plain(md->spe_div[c], md->grid_div, nd, EPI_NONE, nullptr));
+    return JGCM_OK;
+  };
+  JG_TRY(is_fp64(m) ? run(double()) : run(float()));
+  const size_t ts = tsize(m);
+  const size_t S = spec_elems(m, nd) * 2 * ts, S1 = spec_elems(m, 1) * 2 * ts, Gb = grid_elems(m, nd) * ts,
+               G1 = G * ts;
+  JG_CUDA(cudaMemcpyAsync(md->spe_vor[p], md->spe_vor[c], S, cudaMemcpyDeviceToDevice, st));
+  JG_CUDA(cudaMemcpyAsync(md->spe_div[p], md->spe_div[c], S, cudaMemcpyDeviceToDevice, st));
+  JG_CUDA(cudaMemcpyAsync(md->spe_lnps[p], md->spe_lnps[c], S1, cudaMemcpyDeviceToDevice, st));
+  JG_CUDA(cudaMemcpyAsync(md->spe_t[p], md->spe_t[c], S, cudaMemcpyDeviceToDevice, st));
+  JG_CUDA(cudaMemcpyAsync(md->grid_u[p], md->grid_u[c], Gb, cudaMemcpyDeviceToDevice, st));
+  JG_CUDA(cudaMemcpyAsync(md->grid_v[p], md->grid_v[c], Gb, cudaMemcpyDeviceToDevice, st));
+  JG_CUDA(cudaMemcpyAsync(md->grid_ps[p], md->grid_ps[c], G1, cudaMemcpyDeviceToDevice, st));
+  JG_CUDA(cudaMemcpyAsync(md->grid_t[p], md->grid_t[c], Gb, cudaMemcpyDeviceToDevice, st));
+  JG_CUDA(cudaStreamSynchronize(st));
+  return JGCM_OK;
+}

@@ -1,0 +1,730 @@
+// transforms.cu -- spectral transforms of the JGCM dynamical core on sm_103a.
+//
+// spectral -> grid (Trans_Spherical_To_Grid!, Spectral_Spherical_Mesh.jl:143-217) runs as
+//   k_s2g_legendre : per zonal wavenumber m, the even/odd-split Legendre synthesis
+//                    F[m][j] = sum_n P_n^m(mu_j) s_n^m over n = m..N+1 (the reference's extra
+//                    row N+1 included), a dense (nlat/2 x K) x (K x C) contraction per m,
+//                    mirrored to the northern hemisphere by parity;
+//   k_ifft         : inverse real zonal FFT of every (latitude, column) row, two real rows per
+//                    complex FFT, radix-2 in shared memory, fused epilogue (÷cos, exp, ×ps).
+// grid -> spectral (Trans_Grid_To_Spherical!, :221-293; Vor_Div_From_Grid_UV!, :349-459) runs as
+//   k_fft          : forward real zonal FFT (fft/nlon) with fused prologue (×cos, vorticity
+//                    fluxes, kinetic energy, shallow-water height tendency);
+//   k_g2s_legendre : per m, Gaussian quadrature over the hemisphere pairs, for plain analysis
+//                    (row N+1 zeroed) and the alpha operator (vor/div from u cos, v cos), with
+//                    fused epilogues (Laplacian of the energy, spectral damping, the leapfrog with
+//                    Robert-Asselin filter and the shallow-water semi-implicit correction).
+// Spectral prologues build the inputs of the synthesis on the fly from neighbouring total
+// wavenumbers (gradient, Compute_Gradient_Cos! :655-692; ucos/vcos, :517-580).
+#include <cmath>
+
+#include "jgcm_internal.cuh"
+
+namespace jgcm {
+
+template <typename T>
+using V2 = typename C2<T>::t;
+
+__host__ __device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+__device__ __forceinline__ int brev(int x, int logn) { return (int)(__brev((unsigned)x) >> (32 - logn)); }
+
+template <typename G>
+__device__ __forceinline__ const G& group_of(const G* g, int ng, int c, int* k) {
+  int i = 0;
+  for (; i < ng - 1; i++)
+    if (c < g[i].col0 + g[i].L) break;
+  *k = c - g[i].col0;
+  return g[i];
+}
+
+// ------------------------------------------------------------------------------------------
+// radix-2 DIT stages over `npair` rows of length n held as (re, im) in shared memory, input in
+// bit-reversed order, output in natural order.  SIGN = -1 forward (fft), +1 backward (ifft).
+template <typename T, int SIGN>
+__device__ __forceinline__ void fft_stages(T* re, T* im, const T* tw, int npair, int n, int logn) {
+  const int hn = n >> 1;
+  for (int s = 1; s <= logn; s++) {
+    const int half = 1 << (s - 1);
+    const int tshift = logn - s;  // twiddle index = k * (n / 2^s)
+    for (int b = threadIdx.x; b < npair * hn; b += blockDim.x) {
+      int p = b / hn, bb = b - p * hn;
+      int grp = bb >> (s - 1), k = bb & (half - 1);
+      int i0 = p * n + (grp << s) + k, i1 = i0 + half;
+      int ti = k << tshift;
+      T wr = tw[2 * ti], wi = (T)SIGN * tw[2 * ti + 1];
+      T xr = re[i1], xi = im[i1];
+      T tr = xr * wr - xi * wi, tI = xr * wi + xi * wr;
+      T ar = re[i0], ai = im[i0];
+      re[i1] = ar - tr;
+      im[i1] = ai - tI;
+      re[i0] = ar + tr;
+      im[i0] = ai + tI;
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// spectral -> Fourier: Legendre synthesis.  grid (ceil(C/CT), N+1), 256 threads.
+template <typename T>
+__global__ void __launch_bounds__(256) k_s2g_legendre(S2GPlan plan, Tables<T> tb, V2<T>* __restrict__ F, int ns,
+                                                      int nlat, int CT) {
+  using V = V2<T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int m = blockIdx.y;
+  const int nh = nlat >> 1;
+  const int K = ns + 1 - m;
+  T* Ps = (T*)smem;
+  V* X = (V*)(smem + align16((size_t)(ns + 1) * nh * sizeof(T)));
+  const int C = plan.C;
+  const int cbase = blockIdx.x * CT;
+  const size_t mrow = (size_t)m * (ns + 1);
+  const T* Pm = tb.P + (mrow + m) * nh;
+  for (int i = threadIdx.x; i < K * nh; i += blockDim.x) Ps[i] = Pm[i];
+  for (int i = threadIdx.x; i < K * CT; i += blockDim.x) {
+    int r = i / CT, cl = i - r * CT, n = m + r, c = cbase + cl;
+    V x;
+    x.x = 0;
+    x.y = 0;
+    if (c < C) {
+      int k;
+      const S2GGroup& g = group_of(plan.g, plan.ng, c, &k);
+      const int L = g.L;
+      const V* a = (const V*)g.a;
+      switch (g.op) {
+        case S2G_PLAIN:
+          x = a[(mrow + n) * L + k];
+          break;
+        case S2G_DLAM: {  // coef_dlam .* (i h)
+          T cf = tb.dlam[mrow + n];
+          V h = a[(mrow + n) * L + k];
+          x.x = cf * (-h.y);
+          x.y = cf * h.x;
+        } break;
+        case S2G_DTH: {  // coef_dthp h_{n+1} + coef_dthm h_{n-1}
+          if (n <= ns - 1) {
+            T cp = tb.dthp[mrow + n];
+            V h = a[(mrow + n + 1) * L + k];
+            x.x = cp * h.x;
+            x.y = cp * h.y;
+          }
+          if (n - 1 >= m) {
+            T cm = tb.dthm[mrow + n];
+            V h = a[(mrow + n - 1) * L + k];
+            x.x = x.x + cm * h.x;
+            x.y = x.y + cm * h.y;
+          }
+        } break;
+        case S2G_UCOS:
+        case S2G_VCOS: {
+          // ucos = uvc (i div) - uvm vor_{n-1} - uvp vor_{n+1}
+          // vcos = uvc (i vor) + uvm div_{n-1} + uvp div_{n+1}
+          const V* vor = a;
+          const V* dv = (const V*)g.b;
+          const bool u = g.op == S2G_UCOS;
+          const V* ic = u ? dv : vor;  // term multiplied by i*uvc
+          const V* nb = u ? vor : dv;  // neighbour terms
+          T sg = u ? (T)-1 : (T)1;
+          T cc = tb.uvc[mrow + n];
+          V z = ic[(mrow + n) * L + k];
+          x.x = cc * (-z.y);
+          x.y = cc * z.x;
+          if (n - 1 >= m) {
+            T cm = tb.uvm[mrow + n];
+            V h = nb[(mrow + n - 1) * L + k];
+            x.x = x.x + sg * (cm * h.x);
+            x.y = x.y + sg * (cm * h.y);
+          }
+          if (n + 1 <= ns) {
+            T cp = tb.uvp[mrow + n];
+            V h = nb[(mrow + n + 1) * L + k];
+            x.x = x.x + sg * (cp * h.x);
+            x.y = x.y + sg * (cp * h.y);
+          }
+        } break;
+      }
+    }
+    X[i] = x;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nh * CT; i += blockDim.x) {
+    int j = i / CT, cl = i - j * CT, c = cbase + cl;
+    T er = 0, ei = 0, orr = 0, oi = 0;
+    int r = 0;
+    for (; r + 1 < K; r += 2) {
+      T p0 = Ps[r * nh + j], p1 = Ps[(r + 1) * nh + j];
+      V x0 = X[r * CT + cl], x1 = X[(r + 1) * CT + cl];
+      er += p0 * x0.x;
+      ei += p0 * x0.y;
+      orr += p1 * x1.x;
+      oi += p1 * x1.y;
+    }
+    if (r < K) {
+      T p0 = Ps[r * nh + j];
+      V x0 = X[r * CT + cl];
+      er += p0 * x0.x;
+      ei += p0 * x0.y;
+    }
+    if (c < C) {
+      V s, nn;
+      s.x = er + orr;
+      s.y = ei + oi;
+      nn.x = er - orr;
+      nn.y = ei - oi;
+      F[((size_t)m * nlat + j) * C + c] = s;
+      F[((size_t)m * nlat + (nlat - 1 - j)) * C + c] = nn;
+    }
+  }
+}
+
+// Fourier -> grid: inverse real FFT, two columns per complex transform.
+// grid (ceil(C/(2*CP)), nlat), 256 threads.  Row x(t) = Re g_0 + 2 Re sum_{m=1}^{N} g_m e^{imλ_t},
+// i.e. 2 nλ Re(ifft(g)) with g_0 halved as in Spectral_Spherical_Mesh.jl:211-215.
+template <typename T>
+__global__ void __launch_bounds__(256) k_ifft(IFFTPlan plan, Tables<T> tb, const V2<T>* __restrict__ F, int N,
+                                              int nlat, int nlon, int logn, int CP) {
+  using V = V2<T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  T* re = (T*)smem;
+  T* im = re + CP * nlon;
+  T* tw = im + CP * nlon;
+  V* G = (V*)(smem + align16((size_t)(2 * CP * nlon + nlon) * sizeof(T)));  // [N+1][2CP]
+  const int j = blockIdx.y;
+  const int C = plan.C;
+  const int ncol = 2 * CP;
+  const int cbase = blockIdx.x * ncol;
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) tw[i] = tb.tw[i];
+  for (int i = threadIdx.x; i < CP * nlon; i += blockDim.x) {
+    re[i] = 0;
+    im[i] = 0;
+  }
+  for (int i = threadIdx.x; i < (N + 1) * ncol; i += blockDim.x) {
+    int mm = i / ncol, cc = i - mm * ncol, c = cbase + cc;
+    V g;
+    g.x = 0;
+    g.y = 0;
+    if (c < C) g = F[((size_t)mm * nlat + j) * C + c];
+    G[i] = g;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < (N + 1) * CP; i += blockDim.x) {
+    int mm = i / CP, p = i - mm * CP;
+    V g = G[mm * ncol + 2 * p], h = G[mm * ncol + 2 * p + 1];
+    T* R = re + p * nlon;
+    T* I = im + p * nlon;
+    if (mm == 0) {
+      R[0] = g.x;
+      I[0] = h.x;
+    } else {
+      int a = brev(mm, logn), b = brev(nlon - mm, logn);
+      R[a] = g.x - h.y;
+      I[a] = g.y + h.x;
+      R[b] = g.x + h.y;
+      I[b] = h.x - g.y;
+    }
+  }
+  __syncthreads();
+  fft_stages<T, 1>(re, im, tw, CP, nlon, logn);
+  for (int i = threadIdx.x; i < ncol * nlon; i += blockDim.x) {
+    int cc = i / nlon, t = i - cc * nlon, c = cbase + cc;
+    if (c >= C) continue;
+    int p = cc >> 1;
+    T x = (cc & 1) ? im[p * nlon + t] : re[p * nlon + t];
+    int k;
+    const GridOutGroup& g = group_of(plan.g, plan.ng, c, &k);
+    size_t idx = ((size_t)k * nlat + j) * nlon + t;
+    T* dst = (T*)g.dst;
+    switch (g.epi) {
+      case EPI_NONE:
+        dst[idx] = x;
+        break;
+      case EPI_DIVCOS:
+        dst[idx] = x / tb.cosj[j];
+        break;
+      case EPI_EXP2:
+        dst[idx] = x;
+        ((T*)g.dst2)[idx] = exp(x);
+        break;
+      case EPI_DIVCOS_MULPS:
+        dst[idx] = (x / tb.cosj[j]) * ((const T*)g.ps)[(size_t)j * nlon + t];
+        break;
+    }
+  }
+}
+
+// Grid -> Fourier: forward real FFT (fft/nlon), two columns per complex transform, modes 0..N.
+template <typename T>
+__global__ void __launch_bounds__(256) k_fft(FFTPlan plan, Tables<T> tb, V2<T>* __restrict__ F, int N, int nlat,
+                                             int nlon, int logn, int CP) {
+  using V = V2<T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  T* re = (T*)smem;
+  T* im = re + CP * nlon;
+  T* tw = im + CP * nlon;
+  const int j = blockIdx.y;
+  const int C = plan.C;
+  const int ncol = 2 * CP;
+  const int cbase = blockIdx.x * ncol;
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) tw[i] = tb.tw[i];
+  const T cj = tb.cosj[j];
+  for (int i = threadIdx.x; i < ncol * nlon; i += blockDim.x) {
+    int cc = i / nlon, t = i - cc * nlon, c = cbase + cc;
+    T x = 0;
+    if (c < C) {
+      int k;
+      const GridInGroup& g = group_of(plan.g, plan.ng, c, &k);
+      size_t idx = ((size_t)k * nlat + j) * nlon + t;
+      const T* s0 = (const T*)g.src;
+      switch (g.pro) {
+        case PRO_NONE:
+          x = s0[idx];
+          break;
+        case PRO_MULCOS:
+          x = s0[idx] * cj;
+          break;
+        case PRO_FLUXU: {  // (-kappa_m u + (vor + f) v) cos   (Shallow_Water_Dynamics.jl:129, Barotropic :28)
+          T u = s0[idx], v = ((const T*)g.s1)[idx], vor = ((const T*)g.s2)[idx];
+          T absvor = vor + ((const T*)plan.coriolis)[j];
+          x = ((-(T)plan.kappa_m) * u + absvor * v) * cj;
+        } break;
+        case PRO_FLUXV: {  // (-kappa_m v + (-(vor + f)) u) cos
+          T u = s0[idx], v = ((const T*)g.s1)[idx], vor = ((const T*)g.s2)[idx];
+          T absvor = vor + ((const T*)plan.coriolis)[j];
+          x = ((-(T)plan.kappa_m) * v + (-absvor) * u) * cj;
+        } break;
+        case PRO_KIN: {  // 0.5 (u^2 + v^2)
+          T u = s0[idx], v = ((const T*)g.s1)[idx];
+          x = (T)0.5 * (u * u + v * v);
+        } break;
+        case PRO_SWH: {  // -kappa_t (h - h_eq) - (u dlam_h + v dth_h) - h div
+          T h = s0[idx], u = ((const T*)g.s1)[idx], v = ((const T*)g.s2)[idx];
+          T dl = ((const T*)g.s3)[idx], dt = ((const T*)g.s4)[idx], dv = ((const T*)g.s5)[idx];
+          T heq = ((const T*)g.s6)[idx];
+          T d = (-(T)plan.kappa_t) * (h - heq);
+          d = d - (u * dl + v * dt);
+          x = d - h * dv;
+        } break;
+      }
+    }
+    int p = cc >> 1, pos = brev(t, logn);
+    if (cc & 1)
+      im[p * nlon + pos] = x;
+    else
+      re[p * nlon + pos] = x;
+  }
+  // columns beyond C inside the last pair were written as zero above (x = 0)
+  __syncthreads();
+  fft_stages<T, -1>(re, im, tw, CP, nlon, logn);
+  const T scale = (T)(0.5 / nlon);
+  for (int i = threadIdx.x; i < (N + 1) * ncol; i += blockDim.x) {
+    int mm = i / ncol, cc = i - mm * ncol, c = cbase + cc;
+    if (c >= C) continue;
+    int p = cc >> 1, mn = (nlon - mm) & (nlon - 1);
+    T zr = re[p * nlon + mm], zi = im[p * nlon + mm], wr = re[p * nlon + mn], wi = im[p * nlon + mn];
+    V o;
+    if (cc & 1) {
+      o.x = (zi + wi) * scale;
+      o.y = (wr - zr) * scale;
+    } else {
+      o.x = (zr + wr) * scale;
+      o.y = (zi - wi) * scale;
+    }
+    F[((size_t)mm * nlat + j) * C + c] = o;
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Fused spectral time stepping used by the G2S epilogues (Time_Integrator.jl:58-101).
+template <typename T>
+__device__ __forceinline__ void damp_leapfrog(const StepParams& sp, T d, T& dq, T qp, T& qc, T& qn) {
+  const T r = (T)sp.robert;
+  const int Dt = sp.dt;
+  if (sp.init_step) {
+    dq = (dq - qc * d) / ((T)1.0 + (T)Dt * d);
+    qn = qc + (T)Dt * dq;
+    qc = qc + r * ((T)-1.0 * qc + qn);
+  } else {
+    dq = (dq - qp * d) / ((T)1.0 + (T)(2 * Dt) * d);
+    qc = qc + r * (qp - (T)2 * qc);
+    qn = qp + (T)(2 * Dt) * dq;
+    qc = qc + r * qn;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void leapfrog_c(const StepParams& sp, T d, V2<T>& dq, V2<T> qp, V2<T>& qc, V2<T>& qn,
+                                           bool damp) {
+  if (!damp) d = 0;
+  damp_leapfrog<T>(sp, d, dq.x, qp.x, qc.x, qn.x);
+  damp_leapfrog<T>(sp, d, dq.y, qp.y, qc.y, qn.y);
+}
+
+// Fourier -> spectral: Gaussian quadrature per m.  grid (ceil(Cout/CT), N+1), 256 threads.
+// Shared memory holds, for 4 input slots, the hemisphere-symmetric and -antisymmetric
+// combinations g(mu_j) +/- g(-mu_j) of the tile's columns.
+template <typename T>
+__global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb, const V2<T>* __restrict__ F,
+                                                      int ns, int nlat, int Cin, int CT) {
+  using V = V2<T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int m = blockIdx.y;
+  const int nh = nlat >> 1;
+  const int K = ns + 1 - m;
+  const int C = plan.C;
+  const int cbase = blockIdx.x * CT;
+  V* S = (V*)smem;              // [4][CT][nh] symmetric
+  V* A = S + 4 * CT * nh;       // [4][CT][nh] antisymmetric
+  const size_t mrow = (size_t)m * (ns + 1);
+  for (int i = threadIdx.x; i < 4 * CT * nh; i += blockDim.x) {
+    int slot = i / (CT * nh), rem = i - slot * CT * nh, jh = rem / CT, cl = rem - jh * CT, c = cbase + cl;
+    V s, a;
+    s.x = s.y = a.x = a.y = 0;
+    if (c < C) {
+      int k;
+      const SpecOutGroup& g = group_of(plan.g, plan.ng, c, &k);
+      int col = slot == 0 ? g.colA : slot == 1 ? g.colB : slot == 2 ? g.colE : g.colH;
+      if (col >= 0) {
+        col += k;
+        V x = F[((size_t)m * nlat + jh) * Cin + col];
+        V y = F[((size_t)m * nlat + (nlat - 1 - jh)) * Cin + col];
+        s.x = x.x + y.x;
+        s.y = x.y + y.y;
+        a.x = x.x - y.x;
+        a.y = x.y - y.y;
+      }
+    }
+    S[(slot * CT + cl) * nh + jh] = s;
+    A[(slot * CT + cl) * nh + jh] = a;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < K * CT; i += blockDim.x) {
+    int r = i / CT, cl = i - r * CT, n = m + r, c = cbase + cl;
+    if (c >= C) continue;
+    int k;
+    const SpecOutGroup& g = group_of(plan.g, plan.ng, c, &k);
+    const bool even = (r & 1) == 0;
+    const T* pw = tb.PW + (mrow + n) * nh;
+    const T* ca = tb.CA + (mrow + n) * nh;
+    const T* cb = tb.CB + (mrow + n) * nh;
+    const size_t sidx = (mrow + n) * g.L + k;
+    auto plain = [&](int slot) -> V {
+      const V* src = (even ? S : A) + (slot * CT + cl) * nh;
+      T sr = 0, si = 0;
+      for (int jh = 0; jh < nh; jh++) {
+        T w = pw[jh];
+        sr += src[jh].x * w;
+        si += src[jh].y * w;
+      }
+      V o;
+      o.x = (n == ns) ? (T)0 : sr * (T)0.5;
+      o.y = (n == ns) ? (T)0 : si * (T)0.5;
+      return o;
+    };
+    // alpha operator: i * sum CA (A) + sign * sum CB (B), all latitudes folded by parity
+    auto alpha = [&](int slotA, int slotB, T sign) -> V {
+      const V* sa = (even ? S : A) + (slotA * CT + cl) * nh;
+      const V* sb = (even ? A : S) + (slotB * CT + cl) * nh;
+      T ar = 0, ai = 0, br = 0, bi = 0;
+      for (int jh = 0; jh < nh; jh++) {
+        T wa = ca[jh], wb = cb[jh];
+        ar += (-sa[jh].y) * wa;
+        ai += sa[jh].x * wa;
+        br += sb[jh].x * wb;
+        bi += sb[jh].y * wb;
+      }
+      V o;
+      o.x = (n == ns) ? (T)0 : ar + sign * br;
+      o.y = (n == ns) ? (T)0 : ai + sign * bi;
+      return o;
+    };
+    const T eig = tb.eig[mrow + n];
+    switch (g.op) {
+      case G2S_PLAIN:
+        ((V*)g.dst)[sidx] = plain(0);
+        break;
+      case G2S_VOR:
+        ((V*)g.dst)[sidx] = alpha(0, 1, (T)-1);
+        break;
+      case G2S_DIV: {
+        V v = alpha(0, 1, (T)1);
+        if (g.colE >= 0) {  // - laplacian(G2S(E) + extra)
+          V e = plain(2);
+          if (g.extra) {
+            V x = ((const V*)g.extra)[sidx];
+            e.x = e.x + x.x;
+            e.y = e.y + x.y;
+          }
+          v.x = v.x - eig * e.x;
+          v.y = v.y - eig * e.y;
+        }
+        ((V*)g.dst)[sidx] = v;
+      } break;
+      case G2S_BARO: {  // Barotropic_Dynamics.jl:31-36: vorticity tendency, damping, leapfrog
+        V dq = alpha(0, 1, (T)-1);
+        V* qc = (V*)g.qc[0];
+        const V* qp = (const V*)g.qp[0];
+        V c0 = qc[sidx], p0 = qp[sidx], n0;
+        T d = ((const T*)plan.sp.damping)[mrow + n];
+        leapfrog_c<T>(plan.sp, d, dq, p0, c0, n0, true);
+        qc[sidx] = c0;
+        ((V*)g.dst)[sidx] = n0;
+      } break;
+      case G2S_SW: {  // Shallow_Water_Dynamics.jl:133-165
+        // slots: 0 = du cos, 1 = dv cos, 2 = kinetic energy, 3 = dh
+        V dvor = alpha(1, 0, (T)-1);
+        V ddiv = alpha(0, 1, (T)1);
+        V kin = plain(2);
+        V dh = plain(3);
+        const V* hc_p = (const V*)g.qc[2];
+        V hc = hc_p[sidx], hp = ((const V*)g.qp[2])[sidx];
+        V dc = ((const V*)g.qc[1])[sidx], dp = ((const V*)g.qp[1])[sidx];
+        // spe_energy = (kin + h_c) * eig ; ddiv -= spe_energy
+        ddiv.x = ddiv.x - eig * (kin.x + hc.x);
+        ddiv.y = ddiv.y - eig * (kin.y + hc.y);
+        // Implicit_Correction! (SW) :25-54
+        const T h0 = (T)plan.sp.h0;
+        const T Dt = plan.sp.init_step ? (T)plan.sp.dt : (T)(2.0 * plan.sp.dt);
+        ddiv.x = ddiv.x + eig * (hc.x - hp.x);
+        ddiv.y = ddiv.y + eig * (hc.y - hp.y);
+        dh.x = dh.x + h0 * (dc.x - dp.x);
+        dh.y = dh.y + h0 * (dc.y - dp.y);
+        const T mu = (T)plan.sp.implicit_coef * Dt, mu2 = mu * mu;
+        const T den = (T)1.0 - mu2 * eig * h0;
+        ddiv.x = (ddiv.x - mu * eig * dh.x) / den;
+        ddiv.y = (ddiv.y - mu * eig * dh.y) / den;
+        dh.x = dh.x - mu * h0 * ddiv.x;
+        dh.y = dh.y - mu * h0 * ddiv.y;
+        const T d = ((const T*)plan.sp.damping)[mrow + n];
+        V vc = ((V*)g.qc[0])[sidx], vp = ((const V*)g.qp[0])[sidx], vn, dn, hn;
+        leapfrog_c<T>(plan.sp, d, dvor, vp, vc, vn, true);
+        leapfrog_c<T>(plan.sp, d, ddiv, dp, dc, dn, true);
+        leapfrog_c<T>(plan.sp, d, dh, hp, hc, hn, true);
+        ((V*)g.qc[0])[sidx] = vc;
+        ((V*)g.qc[1])[sidx] = dc;
+        ((V*)g.qc[2])[sidx] = hc;
+        ((V*)g.dst)[sidx] = vn;
+        ((V*)g.dst2)[sidx] = dn;
+        ((V*)g.dst3)[sidx] = hn;
+      } break;
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+static int g_smem_configured[2] = {0, 0};
+
+template <typename T>
+static int configure_smem() {
+  int idx = sizeof(T) == 8 ? 1 : 0;
+  if (g_smem_configured[idx]) return JGCM_OK;
+  const int big = 200 * 1024;
+  JG_CUDA(cudaFuncSetAttribute(k_s2g_legendre<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  JG_CUDA(cudaFuncSetAttribute(k_ifft<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  JG_CUDA(cudaFuncSetAttribute(k_fft<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  JG_CUDA(cudaFuncSetAttribute(k_g2s_legendre<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  g_smem_configured[idx] = 1;
+  return JGCM_OK;
+}
+
+static inline int s2g_ct(int nh) { return nh >= 256 ? 1 : 256 / nh; }
+static inline int fft_cp(int nlon) { return nlon >= 512 ? 1 : 512 / nlon; }
+static inline int g2s_ct(int nh) { return nh >= 64 ? 4 : nh >= 32 ? 8 : 16; }
+
+template <typename T>
+int launch_s2g(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, cudaStream_t st) {
+  using V = V2<T>;
+  JG_TRY(configure_smem<T>());
+  JG_ARG(sp.C == ip.C && sp.C <= m->Cmax && sp.C > 0, "bad S2G plan");
+  Tables<T> tb = tables<T>(m);
+  const int nh = m->nh, ct = s2g_ct(nh);
+  size_t sm1 = align16((size_t)(m->ns + 1) * nh * sizeof(T)) + (size_t)(m->ns + 1) * ct * sizeof(V);
+  dim3 g1((sp.C + ct - 1) / ct, m->N + 1);
+  k_s2g_legendre<T><<<g1, 256, sm1, st>>>(sp, tb, (V*)m->d_fbuf, m->ns, m->nlat, ct);
+  JG_CUDA(cudaGetLastError());
+  const int cp = fft_cp(m->nlon);
+  size_t sm2 = align16((size_t)(2 * cp * m->nlon + m->nlon) * sizeof(T)) + (size_t)(m->N + 1) * 2 * cp * sizeof(V);
+  dim3 g2((ip.C + 2 * cp - 1) / (2 * cp), m->nlat);
+  k_ifft<T><<<g2, 256, sm2, st>>>(ip, tb, (const V*)m->d_fbuf, m->N, m->nlat, m->nlon, m->logn, cp);
+  JG_CUDA(cudaGetLastError());
+  return JGCM_OK;
+}
+
+template <typename T>
+int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp, cudaStream_t st) {
+  using V = V2<T>;
+  JG_TRY(configure_smem<T>());
+  JG_ARG(fp.C <= m->Cmax && fp.C > 0, "bad FFT plan");
+  Tables<T> tb = tables<T>(m);
+  const int cp = fft_cp(m->nlon);
+  size_t sm = (size_t)(2 * cp * m->nlon + m->nlon) * sizeof(T);
+  dim3 g((fp.C + 2 * cp - 1) / (2 * cp), m->nlat);
+  k_fft<T><<<g, 256, sm, st>>>(fp, tb, (V*)m->d_fbuf, m->N, m->nlat, m->nlon, m->logn, cp);
+  JG_CUDA(cudaGetLastError());
+  return JGCM_OK;
+}
+
+template <typename T>
+int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp, cudaStream_t st) {
+  using V = V2<T>;
+  JG_TRY(launch_fft_only<T>(m, fp, st));
+  Tables<T> tb = tables<T>(m);
+  const int nh = m->nh, ct = g2s_ct(nh);
+  size_t sm = (size_t)8 * ct * nh * sizeof(V);
+  dim3 g((gp.C + ct - 1) / ct, m->N + 1);
+  k_g2s_legendre<T><<<g, 256, sm, st>>>(gp, tb, (const V*)m->d_fbuf, m->ns, m->nlat, fp.C, ct);
+  JG_CUDA(cudaGetLastError());
+  return JGCM_OK;
+}
+
+template int launch_s2g<float>(jgcm_mesh*, const S2GPlan&, const IFFTPlan&, cudaStream_t);
+template int launch_s2g<double>(jgcm_mesh*, const S2GPlan&, const IFFTPlan&, cudaStream_t);
+template int launch_g2s<float>(jgcm_mesh*, const FFTPlan&, const G2SPlan&, cudaStream_t);
+template int launch_g2s<double>(jgcm_mesh*, const FFTPlan&, const G2SPlan&, cudaStream_t);
+template int launch_fft_only<float>(jgcm_mesh*, const FFTPlan&, cudaStream_t);
+template int launch_fft_only<double>(jgcm_mesh*, const FFTPlan&, cudaStream_t);
+
+// ------------------------------------------------------------------------------------------
+// Layout / precision conversion between the reference host layout (FP64) and device layout.
+template <typename T>
+__global__ void k_spec_h2d(const double* __restrict__ src, V2<T>* __restrict__ dst, int N, int ns, int L) {
+  size_t total = (size_t)(N + 1) * (ns + 1) * L;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    int k = (int)(t % L);
+    size_t mn = t / L;
+    int n = (int)(mn % (ns + 1)), m = (int)(mn / (ns + 1));
+    size_t h = 2 * ((size_t)m + (size_t)(N + 1) * ((size_t)n + (size_t)(ns + 1) * k));
+    V2<T> v;
+    v.x = (n >= m) ? (T)src[h] : (T)0;
+    v.y = (n >= m) ? (T)src[h + 1] : (T)0;
+    dst[t] = v;
+  }
+}
+template <typename T>
+__global__ void k_spec_d2h(const V2<T>* __restrict__ src, double* __restrict__ dst, int N, int ns, int L) {
+  size_t total = (size_t)(N + 1) * (ns + 1) * L;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    int m = (int)(t % (N + 1));
+    size_t r = t / (N + 1);
+    int n = (int)(r % (ns + 1)), k = (int)(r / (ns + 1));
+    V2<T> v = src[((size_t)m * (ns + 1) + n) * L + k];
+    dst[2 * t] = (double)v.x;
+    dst[2 * t + 1] = (double)v.y;
+  }
+}
+template <typename A, typename B>
+__global__ void k_cast(const A* __restrict__ src, B* __restrict__ dst, size_t n) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    dst[t] = (B)src[t];
+}
+// Fourier buffer [m][j][c] -> host [c][j][m] (modes 0..N)
+template <typename T>
+__global__ void k_fourier_d2h(const V2<T>* __restrict__ F, double* __restrict__ dst, int N, int nlat, int L) {
+  size_t total = (size_t)(N + 1) * nlat * L;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    int m = (int)(t % (N + 1));
+    size_t r = t / (N + 1);
+    int j = (int)(r % nlat), k = (int)(r / nlat);
+    V2<T> v = F[((size_t)m * nlat + j) * L + k];
+    dst[2 * t] = (double)v.x;
+    dst[2 * t + 1] = (double)v.y;
+  }
+}
+
+static inline int nblk(size_t n) {
+  size_t b = (n + 255) / 256;
+  return (int)(b > 1184 ? 1184 : (b < 1 ? 1 : b));
+}
+
+int spec_host_to_dev(jgcm_mesh* m, const double* src, void* dst, int L, cudaStream_t st) {
+  size_t n = spec_elems(m, L);
+  if (is_fp64(m))
+    k_spec_h2d<double><<<nblk(n), 256, 0, st>>>(src, (double2*)dst, m->N, m->ns, L);
+  else
+    k_spec_h2d<float><<<nblk(n), 256, 0, st>>>(src, (float2*)dst, m->N, m->ns, L);
+  JG_CUDA(cudaGetLastError());
+  return JGCM_OK;
+}
+int spec_dev_to_host(jgcm_mesh* m, const void* src, double* dst, int L, cudaStream_t st) {
+  size_t n = spec_elems(m, L);
+  if (is_fp64(m))
+    k_spec_d2h<double><<<nblk(n), 256, 0, st>>>((const double2*)src, dst, m->N, m->ns, L);
+  else
+    k_spec_d2h<float><<<nblk(n), 256, 0, st>>>((const float2*)src, dst, m->N, m->ns, L);
+  JG_CUDA(cudaGetLastError());
+  return JGCM_OK;
+}
+int grid_host_to_dev(jgcm_mesh* m, const double* src, void* dst, size_t n, cudaStream_t st) {
+  if (is_fp64(m))
+    JG_CUDA(cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyDeviceToDevice, st));
+  else
+    k_cast<double, float><<<nblk(n), 256, 0, st>>>(src, (float*)dst, n);
+  JG_CUDA(cudaGetLastError());
+  return JGCM_OK;
+}
+int grid_dev_to_host(jgcm_mesh* m, const void* src, double* dst, size_t n, cudaStream_t st) {
+  if (is_fp64(m))
+    JG_CUDA(cudaMemcpyAsync(dst, src, n * 8, cudaMemcpyDeviceToDevice, st));
+  else
+    k_cast<float, double><<<nblk(n), 256, 0, st>>>((const float*)src, dst, n);
+  JG_CUDA(cudaGetLastError());
+  return JGCM_OK;
+}
+int fourier_dev_to_host(jgcm_mesh* m, int L, double* dst, cudaStream_t st) {
+  size_t n = (size_t)(m->N + 1) * m->nlat * L;
+  if (is_fp64(m))
+    k_fourier_d2h<double><<<nblk(n), 256, 0, st>>>((const double2*)m->d_fbuf, dst, m->N, m->nlat, L);
+  else
+    k_fourier_d2h<float><<<nblk(n), 256, 0, st>>>((const float2*)m->d_fbuf, dst, m->N, m->nlat, L);
+  JG_CUDA(cudaGetLastError());
+  return JGCM_OK;
+}
+
+template <typename T>
+__global__ void k_laplacian(V2<T>* s, const T* eig, int N, int ns, int L) {
+  size_t total = (size_t)(N + 1) * (ns + 1) * L;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    T e = eig[t / L];
+    V2<T> v = s[t];
+    v.x = e * v.x;
+    v.y = e * v.y;
+    s[t] = v;
+  }
+}
+int apply_laplacian(jgcm_mesh* m, void* d_spec, int L, cudaStream_t st) {
+  size_t n = spec_elems(m, L);
+  if (is_fp64(m))
+    k_laplacian<double><<<nblk(n), 256, 0, st>>>((double2*)d_spec, m->t64.eig, m->N, m->ns, L);
+  else
+    k_laplacian<float><<<nblk(n), 256, 0, st>>>((float2*)d_spec, m->t32.eig, m->N, m->ns, L);
+  JG_CUDA(cudaGetLastError());
+  return JGCM_OK;
+}
+
+// Area_Weighted_Global_Mean (Spectral_Spherical_Mesh.jl:746-760): one block, FP64, fixed order.
+template <typename T>
+__global__ void k_area_mean(const T* __restrict__ g, const double* __restrict__ w, int nlat, int nlon, double* out) {
+  __shared__ double red[256];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+    double r = 0.0;
+    for (int j = 0; j < nlat; j++) r += (double)g[(size_t)j * nlon + i] * w[j];
+    acc += r;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0] / (2.0 * nlon);
+}
+int area_mean(jgcm_mesh* m, const void* d_grid, double* d_out, cudaStream_t st) {
+  if (is_fp64(m))
+    k_area_mean<double><<<1, 256, 0, st>>>((const double*)d_grid, m->d_wts, m->nlat, m->nlon, d_out);
+  else
+    k_area_mean<float><<<1, 256, 0, st>>>((const float*)d_grid, m->d_wts, m->nlat, m->nlon, d_out);
+  JG_CUDA(cudaGetLastError());
+  return JGCM_OK;
+}
+
+}  // namespace jgcm

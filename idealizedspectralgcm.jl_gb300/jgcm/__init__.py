@@ -1,0 +1,363 @@
+"""jgcm -- Python host interface of libjgcm, the GB300-native JGCM spectral dynamical core.
+
+Mirrors the reference's ``Atmos_Spectral`` call surface (CliMA/IdealizedSpectralGCM.jl,
+module JGCM) through the C ABI declared in ``include/jgcm.h``:
+
+* ``Spectral_Spherical_Mesh(num_fourier, num_spherical, nθ, nλ, nd, radius)``
+  (Spectral_Spherical_Mesh.jl:69-139) plus a ``precision`` keyword;
+* ``Trans_Spherical_To_Grid``, ``Trans_Grid_To_Spherical``, ``Trans_Grid_To_Fourier``,
+  ``Vor_Div_From_Grid_UV``, ``UV_Grid_From_Vor_Div``, ``Compute_Gradients``,
+  ``Add_Horizontal_Advection``, ``Apply_Laplacian``, ``Area_Weighted_Global_Mean`` -- the
+  reference methods without the ``!``, mutating their output arguments as the reference does;
+* ``Model`` -- Dyn_Data + Filtered_Leapfrog (+ Semi_Implicit_Solver) resident on the GPU,
+  stepping Barotropic_Dynamics!, Shallow_Water_Dynamics! or Atmosphere_Update!.
+
+Arrays follow the reference's Julia layout: numpy Fortran order, grid ``float64[nλ, nθ, nlev]``,
+spectral ``complex128[N+1, N+2, nlev]``.  Shape errors raise ``AssertionError`` like the
+reference's ``@assert``; library failures raise ``JGCMError`` with the library's message.
+There is no CPU fallback: importing this package without a built ``libjgcm.so`` or calling
+it without a CUDA device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+__all__ = [
+    "FP64", "FP32", "TF32X3", "BF16X3", "JGCMError", "Spectral_Spherical_Mesh", "Trans_Spherical_To_Grid",
+    "Trans_Grid_To_Spherical", "Trans_Grid_To_Fourier", "Vor_Div_From_Grid_UV", "UV_Grid_From_Vor_Div",
+    "Compute_Gradients", "Add_Horizontal_Advection", "Apply_Laplacian", "Area_Weighted_Global_Mean", "Model",
+    "lib", "lib_path",
+]
+
+FP64, FP32, TF32X3, BF16X3 = 0, 1, 2, 3
+PRECISIONS = {"fp64": FP64, "fp32": FP32, "tf32x3": TF32X3, "bf16x3": BF16X3}
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def lib_path() -> str:
+    return os.path.join(_HERE, "libjgcm.so")
+
+
+class JGCMError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def lib():
+    """Load libjgcm.so (built by ``build_lib.py``); raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        raise JGCMError(f"libjgcm.so not built ({path}); run __graft_entry__.build()")
+    L = C.CDLL(path)
+    P, I, D, Lg = C.c_void_p, C.c_int, C.c_double, C.c_long
+    PP = C.POINTER(C.c_void_p)
+    sig = {
+        "jgcm_last_error": (C.c_char_p, []),
+        "jgcm_version": (I, []),
+        "jgcm_device_info": (I, [C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
+        "jgcm_mesh_create": (I, [I, I, I, I, I, D, I, PP]),
+        "jgcm_mesh_destroy": (I, [P]),
+        "jgcm_mesh_precision": (I, [P]),
+        "jgcm_mesh_table": (I, [P, C.c_char_p, P, Lg, C.POINTER(Lg)]),
+        "jgcm_mesh_synchronize": (I, [P]),
+        "jgcm_trans_spherical_to_grid": (I, [P, P, I, P]),
+        "jgcm_trans_grid_to_spherical": (I, [P, P, I, P]),
+        "jgcm_trans_grid_to_fourier": (I, [P, P, I, P]),
+        "jgcm_vor_div_from_grid_uv": (I, [P, P, P, I, P, P]),
+        "jgcm_uv_grid_from_vor_div": (I, [P, P, P, I, P, P]),
+        "jgcm_compute_gradients": (I, [P, P, I, P, P]),
+        "jgcm_add_horizontal_advection": (I, [P, P, P, P, I, P]),
+        "jgcm_apply_laplacian": (I, [P, P, I]),
+        "jgcm_area_weighted_global_mean": (I, [P, P, C.POINTER(D)]),
+        "jgcm_model_create": (I, [P, P, PP]),
+        "jgcm_model_destroy": (I, [P]),
+        "jgcm_model_get_field": (I, [P, C.c_char_p, P, Lg, C.POINTER(Lg)]),
+        "jgcm_model_set_field": (I, [P, C.c_char_p, P, Lg]),
+        "jgcm_model_step": (I, [P, I]),
+        "jgcm_model_init_step": (I, [P, C.POINTER(I)]),
+        "jgcm_spectral_initialize_fields": (I, [P, P, I]),
+        "jgcm_model_semi_implicit": (I, [P, C.c_char_p, P, Lg, C.POINTER(Lg)]),
+        "jgcm_model_time_steps": (I, [P, I, C.POINTER(C.c_float)]),
+        "jgcm_model_launches_per_step": (I, [P, C.POINTER(I)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(status: int) -> None:
+    if status != 0:
+        msg = lib().jgcm_last_error().decode(errors="replace")
+        if status == -1:
+            raise AssertionError(msg)
+        raise JGCMError(f"libjgcm status {status}: {msg}")
+
+
+def _ptr(a: np.ndarray):
+    assert a.flags.f_contiguous, "arrays must be Fortran-ordered (Julia layout)"
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def device_info():
+    sm, ma, mi = C.c_int(), C.c_int(), C.c_int()
+    _check(lib().jgcm_device_info(C.byref(sm), C.byref(ma), C.byref(mi)))
+    return {"sm_count": sm.value, "cc": (ma.value, mi.value)}
+
+
+class Spectral_Spherical_Mesh:
+    """Spectral_Spherical_Mesh.jl:69-139, device-resident; tables generated on the GPU in FP64."""
+
+    _TABLES3 = ("qnm", "dqnm", "qwg", "coef_alp_a", "coef_alp_b")
+    _TABLES2 = ("epsilon", "coef_uvm", "coef_uvc", "coef_uvp", "coef_dlam", "coef_dthm", "coef_dthp",
+                "laplacian_eig")
+
+    def __init__(self, num_fourier, num_spherical, nlat, nlon, nd, radius, precision="fp64"):
+        if isinstance(precision, str):
+            precision = PRECISIONS[precision]
+        self.num_fourier, self.num_spherical = int(num_fourier), int(num_spherical)
+        self.nlat, self.nlon, self.nd, self.radius = int(nlat), int(nlon), int(nd), float(radius)
+        self.precision = int(precision)
+        h = C.c_void_p()
+        _check(lib().jgcm_mesh_create(self.num_fourier, self.num_spherical, self.nlat, self.nlon, self.nd,
+                                      self.radius, self.precision, C.byref(h)))
+        self._h = h
+        self._cache = {}
+
+    def __getattr__(self, name):
+        if name.startswith("_"):
+            raise AttributeError(name)
+        if name in ("sinth", "costh", "wts", "lonc", "latc") + self._TABLES3 + self._TABLES2:
+            if name not in self._cache:
+                self._cache[name] = self._table(name)
+            return self._cache[name]
+        raise AttributeError(name)
+
+    def _table(self, name):
+        n = C.c_long()
+        _check(lib().jgcm_mesh_table(self._h, name.encode(), None, 0, C.byref(n)))
+        out = np.zeros(n.value)
+        _check(lib().jgcm_mesh_table(self._h, name.encode(), _ptr(out), n.value, C.byref(n)))
+        N1, S1 = self.num_fourier + 1, self.num_spherical + 1
+        if name in self._TABLES3:
+            return out.reshape((N1, S1, self.nlat), order="F")
+        if name in self._TABLES2:
+            return out.reshape((N1, S1), order="F")
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().jgcm_mesh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def spectral(self, nlev):
+        return np.zeros((self.num_fourier + 1, self.num_spherical + 1, nlev), dtype=np.complex128, order="F")
+
+    def grid(self, nlev):
+        return np.zeros((self.nlon, self.nlat, nlev), order="F")
+
+
+def _nlev_spec(mesh, a):
+    assert isinstance(a, np.ndarray) and a.dtype == np.complex128
+    assert a.ndim == 3 and a.shape[:2] == (mesh.num_fourier + 1, mesh.num_spherical + 1)
+    assert a.shape[2] in (mesh.nd, 1)
+    return a.shape[2]
+
+
+def _nlev_grid(mesh, a):
+    assert isinstance(a, np.ndarray) and a.dtype == np.float64
+    assert a.ndim == 3 and a.shape[:2] == (mesh.nlon, mesh.nlat)
+    assert a.shape[2] in (mesh.nd, 1)
+    return a.shape[2]
+
+
+def Trans_Spherical_To_Grid(mesh, snm, pfield):
+    """Spectral_Spherical_Mesh.jl:143-217 (sums total wavenumbers m..N+1)."""
+    n = _nlev_spec(mesh, snm)
+    assert _nlev_grid(mesh, pfield) == n
+    _check(lib().jgcm_trans_spherical_to_grid(mesh._h, _ptr(snm), n, _ptr(pfield)))
+
+
+def Trans_Grid_To_Spherical(mesh, pfield, snm):
+    """Spectral_Spherical_Mesh.jl:221-293 (row N+1 set to zero)."""
+    n = _nlev_grid(mesh, pfield)
+    assert _nlev_spec(mesh, snm) == n
+    _check(lib().jgcm_trans_grid_to_spherical(mesh._h, _ptr(pfield), n, _ptr(snm)))
+
+
+def Trans_Grid_To_Fourier(mesh, pfield, fourier):
+    """Spectral_Spherical_Mesh.jl:295-330.  ``fourier`` is complex128[N+1, nθ, nlev] (modes 0..N)."""
+    n = _nlev_grid(mesh, pfield)
+    assert fourier.dtype == np.complex128 and fourier.shape == (mesh.num_fourier + 1, mesh.nlat, n)
+    _check(lib().jgcm_trans_grid_to_fourier(mesh._h, _ptr(pfield), n, _ptr(fourier)))
+
+
+def Vor_Div_From_Grid_UV(mesh, grid_u, grid_v, vor, div):
+    """Spectral_Spherical_Mesh.jl:349-393."""
+    n = _nlev_grid(mesh, grid_u)
+    assert _nlev_grid(mesh, grid_v) == n and _nlev_spec(mesh, vor) == n and _nlev_spec(mesh, div) == n
+    _check(lib().jgcm_vor_div_from_grid_uv(mesh._h, _ptr(grid_u), _ptr(grid_v), n, _ptr(vor), _ptr(div)))
+
+
+def UV_Grid_From_Vor_Div(mesh, vor, div, grid_u, grid_v):
+    """Spectral_Spherical_Mesh.jl:462-482."""
+    n = _nlev_spec(mesh, vor)
+    assert _nlev_spec(mesh, div) == n and _nlev_grid(mesh, grid_u) == n and _nlev_grid(mesh, grid_v) == n
+    _check(lib().jgcm_uv_grid_from_vor_div(mesh._h, _ptr(vor), _ptr(div), n, _ptr(grid_u), _ptr(grid_v)))
+
+
+def Compute_Gradients(mesh, spe_hs, grid_dlam_hs, grid_dth_hs):
+    """Spectral_Spherical_Mesh.jl:721-741."""
+    n = _nlev_spec(mesh, spe_hs)
+    assert _nlev_grid(mesh, grid_dlam_hs) == n and _nlev_grid(mesh, grid_dth_hs) == n
+    _check(lib().jgcm_compute_gradients(mesh._h, _ptr(spe_hs), n, _ptr(grid_dlam_hs), _ptr(grid_dth_hs)))
+
+
+def Add_Horizontal_Advection(mesh, spe_hs, grid_u, grid_v, grid_dhs):
+    """Spectral_Spherical_Mesh.jl:694-718 (grid_dhs -= u ∂λhs + v ∂θhs)."""
+    n = _nlev_spec(mesh, spe_hs)
+    assert _nlev_grid(mesh, grid_u) == n and _nlev_grid(mesh, grid_v) == n and _nlev_grid(mesh, grid_dhs) == n
+    _check(lib().jgcm_add_horizontal_advection(mesh._h, _ptr(spe_hs), _ptr(grid_u), _ptr(grid_v), n,
+                                               _ptr(grid_dhs)))
+
+
+def Apply_Laplacian(mesh, spe):
+    """Spectral_Spherical_Mesh.jl:614-621."""
+    _check(lib().jgcm_apply_laplacian(mesh._h, _ptr(spe), _nlev_spec(mesh, spe)))
+
+
+def Area_Weighted_Global_Mean(mesh, grid):
+    """Spectral_Spherical_Mesh.jl:746-760 (level 1)."""
+    _nlev_grid(mesh, grid)
+    out = C.c_double()
+    _check(lib().jgcm_area_weighted_global_mean(mesh._h, _ptr(grid), C.byref(out)))
+    return out.value
+
+
+class _Params(C.Structure):
+    _fields_ = [("kind", C.c_int), ("robert_coef", C.c_double), ("damping_order", C.c_int),
+                ("damping_coef", C.c_double), ("implicit_coef", C.c_double), ("dt", C.c_int),
+                ("omega", C.c_double), ("grav", C.c_double), ("rdgas", C.c_double), ("kappa", C.c_double),
+                ("do_mass_correction", C.c_int), ("do_energy_correction", C.c_int),
+                ("h0", C.c_double), ("kappa_m", C.c_double), ("kappa_t", C.c_double),
+                ("sigma_b", C.c_double), ("k_f", C.c_double), ("k_a", C.c_double), ("k_s", C.c_double),
+                ("dT_y", C.c_double), ("dtheta_z", C.c_double), ("ps_ref", C.c_double), ("t_ref", C.c_double),
+                ("sea_level_ps_ref", C.c_double), ("init_t", C.c_double)]
+
+
+KINDS = {"barotropic": 0, "shallow_water": 1, "held_suarez": 2}
+
+
+class Model:
+    """Dyn_Data + Filtered_Leapfrog (+ Semi_Implicit_Solver) on the GPU.
+
+    ``params`` is a dict with the fields of ``jgcm_params`` (see jgcm.configs).  Fields are
+    read and written by their Dyn_Data names with δ spelled ``d`` (``spe_vor_c``,
+    ``grid_u_p``, ``grid_t_eq``, ...).  ``step(n)`` runs n Barotropic_Dynamics! /
+    Shallow_Water_Physics!+Shallow_Water_Dynamics! / Atmosphere_Update! steps, the first one
+    being the reference drivers' init step followed by Update_Init_Step!.
+    """
+
+    def __init__(self, mesh: Spectral_Spherical_Mesh, params: dict):
+        self.mesh = mesh
+        self.params = dict(params)
+        p = _Params()
+        for name, _ in _Params._fields_:
+            if name == "kind":
+                p.kind = KINDS[params["kind"]]
+            elif name in params:
+                setattr(p, name, params[name])
+        self._p = p
+        h = C.c_void_p()
+        _check(lib().jgcm_model_create(mesh._h, C.byref(p), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().jgcm_model_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _shape(self, name, n):
+        m = self.mesh
+        N1, S1 = m.num_fourier + 1, m.num_spherical + 1
+        if name.startswith("spe_"):
+            return (N1, S1, n // (2 * N1 * S1)), np.complex128
+        return (m.nlon, m.nlat, n // (m.nlon * m.nlat)), np.float64
+
+    def get(self, name):
+        n = C.c_long()
+        _check(lib().jgcm_model_get_field(self._h, name.encode(), None, 0, C.byref(n)))
+        shape, dt = self._shape(name, n.value)
+        out = np.zeros(shape, dtype=dt, order="F")
+        _check(lib().jgcm_model_get_field(self._h, name.encode(), _ptr(out), n.value, C.byref(n)))
+        return out
+
+    def set(self, name, arr):
+        n = C.c_long()
+        _check(lib().jgcm_model_get_field(self._h, name.encode(), None, 0, C.byref(n)))
+        shape, dt = self._shape(name, n.value)
+        a = np.asfortranarray(np.asarray(arr, dtype=dt).reshape(shape, order="F"))
+        _check(lib().jgcm_model_set_field(self._h, name.encode(), _ptr(a), n.value))
+
+    @property
+    def init_step(self):
+        v = C.c_int()
+        _check(lib().jgcm_model_init_step(self._h, C.byref(v)))
+        return bool(v.value)
+
+    def step(self, nsteps=1):
+        _check(lib().jgcm_model_step(self._h, int(nsteps)))
+
+    def spectral_initialize_fields(self, grid_t_pert=None, vorticity_seed=True):
+        """Spectral_Dynamics.jl:372-449 on the device."""
+        if grid_t_pert is not None:
+            g = np.asfortranarray(grid_t_pert, dtype=np.float64)
+            _check(lib().jgcm_spectral_initialize_fields(self._h, _ptr(g), int(vorticity_seed)))
+        else:
+            _check(lib().jgcm_spectral_initialize_fields(self._h, None, int(vorticity_seed)))
+
+    def semi_implicit(self, name):
+        n = C.c_long()
+        _check(lib().jgcm_model_semi_implicit(self._h, name.encode(), None, 0, C.byref(n)))
+        out = np.zeros(n.value)
+        _check(lib().jgcm_model_semi_implicit(self._h, name.encode(), _ptr(out), n.value, C.byref(n)))
+        nd = self.mesh.nd
+        if name == "div_mat":
+            return out.reshape((nd, nd), order="F")
+        if name == "wave_matrix":
+            return out.reshape((nd, nd, -1), order="F")
+        return out
+
+    def time_steps(self, nsteps):
+        """Advance nsteps steady steps (CUDA graphs) and return the CUDA-event time in ms."""
+        ms = C.c_float()
+        _check(lib().jgcm_model_time_steps(self._h, int(nsteps), C.byref(ms)))
+        return float(ms.value)
+
+    def launches_per_step(self):
+        v = C.c_int()
+        _check(lib().jgcm_model_launches_per_step(self._h, C.byref(v)))
+        return v.value

@@ -1,0 +1,151 @@
+/*
+ * jgcm.h -- C ABI of libjgcm, the GB300-native (sm_103a) spectral-transform dynamical core.
+ *
+ * Drop-in for the Atmos_Spectral hot path of CliMA/IdealizedSpectralGCM.jl (module JGCM).
+ * Every entry point below replaces one Julia method of the reference; the comment above
+ * each cites the file:line of the method it replaces.  A Julia host binds these with
+ * `ccall` (the shim is shown in INTEGRATION.md); the tests bind them with ctypes.
+ *
+ * Conventions
+ *  - Every function returns an int status: JGCM_OK (0) or a negative JGCM_E_* code.
+ *    jgcm_last_error() returns a message for the calling thread's last failure.
+ *    Nothing aborts, traps or throws across the ABI.
+ *  - Host arrays use the reference's Julia layout (column-major, 1-based in Julia,
+ *    0-based here):  grid  double[nlev][nlat][nlon]   (Array{Float64,3}(nlon,nlat,nlev))
+ *                    spec  double[nlev][N+2][N+1][2]  (Array{ComplexF64,3}(N+1,N+2,nlev),
+ *                                                       re/im interleaved, m fastest)
+ *    with N = num_fourier, num_spherical = N+1, latitudes south->north (Gaussian).
+ *    nlev is the array's third dimension and must be nd or 1, as in the reference.
+ *  - Host arrays are always FP64; the device computes in the mesh's precision mode.
+ *  - A mesh owns one CUDA stream, its device tables and its transform workspace.  Calls on
+ *    one mesh (and the models built on it) are not re-entrant, matching the reference,
+ *    whose mesh owns shared scratch buffers (Spectral_Spherical_Mesh.jl:51-64).
+ */
+#ifndef JGCM_H
+#define JGCM_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility push(default) /* the library builds with -fvisibility=hidden */
+#endif
+
+#define JGCM_OK 0
+#define JGCM_E_ARG -1      /* bad argument / shape (reference: AssertionError) */
+#define JGCM_E_CUDA -2     /* CUDA runtime failure */
+#define JGCM_E_NOMEM -3    /* device allocation failed */
+#define JGCM_E_STATE -4    /* call not valid in this state */
+#define JGCM_E_NUMERIC -5  /* non-finite value detected by a device check */
+
+/* Precision modes (jgcm_mesh_create). */
+#define JGCM_FP64 0       /* all device arithmetic FP64 (the FP64 GPU path) */
+#define JGCM_FP32 1       /* FP32 state/transforms, FP64 tables, implicit solve and sums */
+#define JGCM_TF32X3 2     /* as FP32, Legendre contraction on tcgen05 tensor cores, 3xTF32 split */
+#define JGCM_BF16X3 3     /* as FP32, Legendre contraction on tcgen05, 3-term split-BF16 */
+
+typedef struct jgcm_mesh jgcm_mesh;
+typedef struct jgcm_model jgcm_model;
+
+const char* jgcm_last_error(void);
+int jgcm_version(void);
+/* Device properties of the current device: SM count, compute capability. */
+int jgcm_device_info(int* sm_count, int* cc_major, int* cc_minor);
+
+/* Spectral_Spherical_Mesh constructor, Spectral_Spherical_Mesh.jl:69-139 (argument order
+ * num_fourier, num_spherical, nθ, nλ, nd, radius as in the reference).  Gaussian nodes
+ * (Gauss_And_Legendre.jl:69-118) and Legendre tables (:4-66) are generated on the GPU
+ * in FP64. */
+int jgcm_mesh_create(int num_fourier, int num_spherical, int nlat, int nlon, int nd, double radius,
+                     int precision, jgcm_mesh** out);
+int jgcm_mesh_destroy(jgcm_mesh* mesh);
+int jgcm_mesh_precision(const jgcm_mesh* mesh);
+/* Copy a mesh table to the host, FP64, reference layout: "sinth","costh","wts","lonc","latc"
+ * ([nlat] or [nlon]), "qnm","dqnm","qwg","coef_alp_a","coef_alp_b" ([nlat][N+2][N+1]),
+ * "epsilon","coef_uvm","coef_uvc","coef_uvp","coef_dlam","coef_dthm","coef_dthp",
+ * "laplacian_eig" ([N+2][N+1]).  Writes *count = element count; out may be NULL to query. */
+int jgcm_mesh_table(jgcm_mesh* mesh, const char* name, double* out, long cap, long* count);
+/* Block until all work queued on the mesh stream is done. */
+int jgcm_mesh_synchronize(jgcm_mesh* mesh);
+
+/* Trans_Spherical_To_Grid!  Spectral_Spherical_Mesh.jl:143-217 */
+int jgcm_trans_spherical_to_grid(jgcm_mesh* mesh, const double* snm, int nlev, double* pfield);
+/* Trans_Grid_To_Spherical!  Spectral_Spherical_Mesh.jl:221-293 */
+int jgcm_trans_grid_to_spherical(jgcm_mesh* mesh, const double* pfield, int nlev, double* snm);
+/* Trans_Grid_To_Fourier!  Spectral_Spherical_Mesh.jl:295-330; writes fourier modes m = 0..N
+ * of fft/nλ as complex double[nlev][nlat][N+1] (modes above N are not used downstream). */
+int jgcm_trans_grid_to_fourier(jgcm_mesh* mesh, const double* pfield, int nlev, double* fourier);
+/* Vor_Div_From_Grid_UV!  Spectral_Spherical_Mesh.jl:349-393 (+ Compute_Alpha_Operator! :424-459) */
+int jgcm_vor_div_from_grid_uv(jgcm_mesh* mesh, const double* grid_u, const double* grid_v, int nlev,
+                              double* vor, double* div);
+/* UV_Grid_From_Vor_Div!  Spectral_Spherical_Mesh.jl:462-482 (+ :517-580) */
+int jgcm_uv_grid_from_vor_div(jgcm_mesh* mesh, const double* vor, const double* div, int nlev,
+                              double* grid_u, double* grid_v);
+/* Compute_Gradients!  Spectral_Spherical_Mesh.jl:721-741 (+ Compute_Gradient_Cos! :655-692) */
+int jgcm_compute_gradients(jgcm_mesh* mesh, const double* spe_hs, int nlev, double* grid_dlam_hs,
+                           double* grid_dth_hs);
+/* Add_Horizontal_Advection!  Spectral_Spherical_Mesh.jl:694-718 (grid_dhs updated in place) */
+int jgcm_add_horizontal_advection(jgcm_mesh* mesh, const double* spe_hs, const double* grid_u,
+                                  const double* grid_v, int nlev, double* grid_dhs);
+/* Apply_Laplacian!  Spectral_Spherical_Mesh.jl:614-621 (in place) */
+int jgcm_apply_laplacian(jgcm_mesh* mesh, double* spe, int nlev);
+/* Area_Weighted_Global_Mean  Spectral_Spherical_Mesh.jl:746-760 (level 1; FP64 sum) */
+int jgcm_area_weighted_global_mean(jgcm_mesh* mesh, const double* grid, double* out);
+
+/* ---- models: Dyn_Data + Filtered_Leapfrog (+ Semi_Implicit_Solver) kept on the device ---- */
+#define JGCM_BAROTROPIC 0     /* Barotropic_Dynamics!  Barotropic_Dynamics.jl:2-46 */
+#define JGCM_SHALLOW_WATER 1  /* Shallow_Water_Physics! + Shallow_Water_Dynamics!
+                                 Shallow_Water_Dynamics.jl:7-179 */
+#define JGCM_HELD_SUAREZ 2    /* Atmosphere_Update!  Spectral_Dynamics.jl:470-490 */
+
+/* Run parameters.  Mirrors the arguments of Filtered_Leapfrog (Time_Integrator.jl:20-38),
+ * Atmo_Data (Atmo_Data.jl:34-55), Semi_Implicit_Solver (Semi_Implicit.jl:40-97), the SW
+ * driver (exp/Shallow_Water/SW.jl:12-25) and the HS physics Dict (exp/HSt42/Run_HS.jl:12). */
+typedef struct {
+  int kind;
+  double robert_coef;
+  int damping_order;
+  double damping_coef;
+  double implicit_coef;
+  int dt; /* seconds */
+  double omega, grav, rdgas, kappa;
+  int do_mass_correction, do_energy_correction;
+  double h0, kappa_m, kappa_t;
+  double sigma_b, k_f, k_a, k_s, dT_y, dtheta_z;
+  double ps_ref, t_ref;
+  double sea_level_ps_ref, init_t;
+} jgcm_params;
+
+int jgcm_model_create(jgcm_mesh* mesh, const jgcm_params* params, jgcm_model** out);
+int jgcm_model_destroy(jgcm_model* model);
+/* Read / write one Dyn_Data field (Dyn_Data.jl:4-156) by its reference name with the
+ * δ spelled "d": "spe_vor_c", "grid_u_p", "spe_dt", "grid_t_eq", "grid_p_full",
+ * "grid_z_full", "grid_h_eq", ...  Layout as above; *count = doubles in the field. */
+int jgcm_model_get_field(jgcm_model* model, const char* name, double* host, long cap, long* count);
+int jgcm_model_set_field(jgcm_model* model, const char* name, const double* host, long count);
+/* Advance nsteps model steps.  The first step of a fresh model is the forward (init) step
+ * and is followed by Update_Init_Step! (Time_Integrator.jl:40-43, Semi_Implicit.jl:182-188),
+ * exactly as the reference drivers do (exp/HSt42/HS.jl:73-81).  Steady-state steps run as
+ * captured CUDA graphs. */
+int jgcm_model_step(jgcm_model* model, int nsteps);
+int jgcm_model_init_step(jgcm_model* model, int* init_step);
+/* Spectral_Initialize_Fields!  Spectral_Dynamics.jl:372-449.  grid_t_pert (nullable,
+ * grid[nd]) is added to the isothermal init_t before the spectral filtering;
+ * vorticity_seed != 0 keeps the reference's deterministic vorticity seed (:401-409). */
+int jgcm_spectral_initialize_fields(jgcm_model* model, const double* grid_t_pert, int vorticity_seed);
+/* Semi_Implicit_Solver internals: "div_mat" (nd*nd), "h" (nd), "wave_matrix"
+ * (nd*nd*(N+1)), column-major as in Semi_Implicit.jl:112-180. */
+int jgcm_model_semi_implicit(jgcm_model* model, const char* name, double* out, long cap, long* count);
+/* Time nsteps steady-state steps with CUDA events on the model stream (milliseconds). */
+int jgcm_model_time_steps(jgcm_model* model, int nsteps, float* ms);
+/* Number of kernel launches one steady-state step issues. */
+int jgcm_model_launches_per_step(jgcm_model* model, int* launches);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#ifdef __cplusplus
+}
+#endif
+#endif

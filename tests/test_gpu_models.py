@@ -1,0 +1,110 @@
+"""GPU model steps vs the FP64 oracle from identical states, through the C ABI.
+
+The GPU model is loaded with the oracle's state (copy_state), both advance the same steps,
+and every prognostic field is compared by relative L2.  Tolerances: FP64 path 1e-10 after a
+few steps (summation order differs; HS's chaotic growth is slow over a few steps), FP32 path
+5e-5.  The barotropic T42 workload runs its full 480 steps (10 days) in FP64.
+"""
+import numpy as np
+import pytest
+
+from jgcm import configs
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(jg, orc, name, prec):
+    params = configs.PARAMS[name]
+    gm = configs.make_mesh(jg, name, precision=prec)
+    om = configs.make_mesh(orc, name)
+    return gm, om, jg.Model(gm, params), orc.Model(om, params)
+
+
+def _compare(gmod, omod, kind, tol):
+    errs = {}
+    for f in configs.PROGNOSTIC[kind]:
+        errs[f] = configs.rel_l2(gmod.get(f), omod.get(f))
+    bad = {k: v for k, v in errs.items() if not v < tol}
+    assert not bad, f"fields above {tol}: {bad}"
+    return errs
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("fp32", 5e-5)])
+def test_barotropic_steps(jg, orc, prec, tol):
+    gm, om, gmod, omod = _pair(jg, orc, "barotropic_t42", prec)
+    configs.init_barotropic_rh4(orc, om, omod)
+    configs.copy_state(omod, gmod, "barotropic")
+    for n in (1, 1, 5):
+        gmod.step(n)
+        omod.step(n)
+        _compare(gmod, omod, "barotropic", tol)
+    assert not gmod.init_step and not omod.init_step
+
+
+def test_barotropic_10_days_fp64(jg, orc):
+    gm, om, gmod, omod = _pair(jg, orc, "barotropic_t42", "fp64")
+    configs.init_barotropic_rh4(orc, om, omod)
+    configs.copy_state(omod, gmod, "barotropic")
+    gmod.step(480)
+    omod.step(480)
+    _compare(gmod, omod, "barotropic", 1e-9)
+
+
+def test_barotropic_init_parity(jg, orc):
+    """The IC driver run on the GPU library reproduces the oracle's."""
+    gm, om, gmod, omod = _pair(jg, orc, "barotropic_t42", "fp64")
+    configs.init_barotropic_rh4(orc, om, omod)
+    configs.init_barotropic_rh4(jg, gm, gmod)
+    _compare(gmod, omod, "barotropic", 1e-12)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("fp32", 5e-5)])
+def test_shallow_water_steps(jg, orc, prec, tol):
+    gm, om, gmod, omod = _pair(jg, orc, "sw_t85", prec)
+    configs.init_shallow_water_jet(orc, om, omod)
+    configs.copy_state(omod, gmod, "shallow_water")
+    for n in (1, 1, 4):
+        gmod.step(n)
+        omod.step(n)
+        _compare(gmod, omod, "shallow_water", tol)
+
+
+@pytest.mark.parametrize("name", ["hs_t21l10", "hs_t42l20"])
+def test_held_suarez_init_parity(jg, orc, name):
+    gm, om, gmod, omod = _pair(jg, orc, name, "fp64")
+    noise = configs.hs_temperature_noise(om)
+    omod.spectral_initialize_fields(noise, True)
+    gmod.spectral_initialize_fields(noise, True)
+    _compare(gmod, omod, "held_suarez", 1e-12)
+
+
+@pytest.mark.parametrize("name,prec,tol", [("hs_t21l10", "fp64", 1e-10), ("hs_t42l20", "fp64", 1e-10),
+                                           ("hs_t42l20", "fp32", 5e-5)])
+def test_held_suarez_steps(jg, orc, name, prec, tol):
+    gm, om, gmod, omod = _pair(jg, orc, name, prec)
+    omod.spectral_initialize_fields(configs.hs_temperature_noise(om), True)
+    configs.copy_state(omod, gmod, "held_suarez")
+    for n in (1, 1, 2):
+        gmod.step(n)
+        omod.step(n)
+        _compare(gmod, omod, "held_suarez", tol)
+    for f in ("grid_t_eq", "grid_p_full", "grid_p_half", "grid_z_full"):
+        assert configs.rel_l2(gmod.get(f), omod.get(f)) < tol, f
+
+
+def test_held_suarez_semi_implicit_matrices(jg, orc):
+    gm, om, gmod, omod = _pair(jg, orc, "hs_t42l20", "fp64")
+    assert configs.rel_l2(gmod.semi_implicit("div_mat"), omod.semi_implicit("div_mat")) < 1e-13
+    assert configs.rel_l2(gmod.semi_implicit("h"), omod.semi_implicit("h")) < 1e-13
+    assert configs.rel_l2(gmod.semi_implicit("wave_matrix"), omod.semi_implicit("wave_matrix")) < 1e-12
+
+
+def test_held_suarez_conservation(jg, orc):
+    """The mass fixer keeps the area-mean surface pressure at its previous value."""
+    gm, om, gmod, omod = _pair(jg, orc, "hs_t42l20", "fp32")
+    gmod.spectral_initialize_fields(configs.hs_temperature_noise(gm), True)
+    ps0 = jg.Area_Weighted_Global_Mean(gm, gmod.get("grid_ps_c"))
+    gmod.step(10)
+    ps1 = jg.Area_Weighted_Global_Mean(gm, gmod.get("grid_ps_c"))
+    assert abs(ps1 - ps0) / ps0 < 1e-6
+    assert np.isfinite(gmod.get("grid_t_c")).all()

@@ -1,0 +1,142 @@
+"""GPU transforms vs the FP64 oracle, through the C ABI (ctypes).
+
+Tolerances (relative L2 over the whole array): FP64 path 1e-12 (the oracle and the GPU sum in
+different orders); FP32 path 5e-6 for single transforms.
+"""
+import numpy as np
+import pytest
+
+from jgcm import configs
+
+pytestmark = pytest.mark.gpu
+
+CASES = [(21, 32, 64, 3), (42, 64, 128, 20), (85, 128, 256, 2)]
+TOL = {"fp64": 1e-12, "fp32": 5e-6}
+
+
+def _meshes(jg, orc, N, nlat, nlon, nd, prec, radius=6371.0e3):
+    return (jg.Spectral_Spherical_Mesh(N, N + 1, nlat, nlon, nd, radius, precision=prec),
+            orc.Spectral_Spherical_Mesh(N, N + 1, nlat, nlon, nd, radius))
+
+
+def _grid(m, nlev, seed):
+    return np.asfortranarray(configs.normal(seed, m.nlon * m.nlat * nlev).reshape((m.nlon, m.nlat, nlev), order="F"))
+
+
+def _spec(m, nlev, seed, lower=True):
+    N1, S1 = m.num_fourier + 1, m.num_spherical + 1
+    z = configs.normal(seed, 2 * N1 * S1 * nlev)
+    s = (z[0::2] + 1j * z[1::2]).reshape((N1, S1, nlev), order="F")
+    # decay with n like a smooth field
+    n = np.arange(S1)[None, :, None]
+    s = s / (1.0 + n) ** 1.5
+    if not lower:
+        for mm in range(N1):
+            s[mm, :mm, :] = 0
+    return np.asfortranarray(s)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("case", CASES)
+def test_tables(jg, orc, case, prec):
+    N, nlat, nlon, nd = case
+    gm, om = _meshes(jg, orc, N, nlat, nlon, nd, prec)
+    assert np.max(np.abs(gm.sinth - om.sinth)) < 2e-15
+    assert np.max(np.abs(gm.wts - om.wts) / om.wts) < 1e-13
+    assert configs.rel_l2(gm.qnm, om.qnm) < 1e-14
+    assert configs.rel_l2(gm.dqnm, om.dqnm) < 1e-12
+    for name in ("epsilon", "coef_uvm", "coef_uvc", "coef_uvp", "coef_dlam", "coef_dthm", "coef_dthp",
+                 "laplacian_eig", "coef_alp_a", "coef_alp_b", "qwg"):
+        assert configs.rel_l2(getattr(gm, name), getattr(om, name)) < 1e-13, name
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("case", CASES)
+def test_spherical_to_grid(jg, orc, case, prec):
+    N, nlat, nlon, nd = case
+    gm, om = _meshes(jg, orc, N, nlat, nlon, nd, prec)
+    for nlev in sorted({nd, 1}):
+        s = _spec(om, nlev, 11 + nlev)  # includes junk below the diagonal: ignored by both
+        a, b = gm.grid(nlev), om.grid(nlev)
+        jg.Trans_Spherical_To_Grid(gm, s, a)
+        orc.Trans_Spherical_To_Grid(om, s, b)
+        assert configs.rel_l2(a, b) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("case", CASES)
+def test_grid_to_spherical(jg, orc, case, prec):
+    N, nlat, nlon, nd = case
+    gm, om = _meshes(jg, orc, N, nlat, nlon, nd, prec)
+    for nlev in sorted({nd, 1}):
+        g = _grid(om, nlev, 5 + nlev)
+        a, b = gm.spectral(nlev), om.spectral(nlev)
+        jg.Trans_Grid_To_Spherical(gm, g, a)
+        orc.Trans_Grid_To_Spherical(om, g, b)
+        assert configs.rel_l2(a, b) < TOL[prec]
+        assert np.all(a[:, N + 1, :] == 0)  # the extra total wavenumber is zeroed (:290)
+        for mm in range(N + 1):
+            assert np.all(a[mm, :mm, :] == 0)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("case", CASES[:2])
+def test_grid_to_fourier(jg, orc, case, prec):
+    N, nlat, nlon, nd = case
+    gm, om = _meshes(jg, orc, N, nlat, nlon, nd, prec)
+    g = _grid(om, nd, 3)
+    f = np.zeros((N + 1, nlat, nd), dtype=np.complex128, order="F")
+    jg.Trans_Grid_To_Fourier(gm, g, f)
+    ref = np.zeros((nlon, nlat, nd), dtype=np.complex128, order="F")
+    orc.Trans_Grid_To_Fourier(om, g, ref)
+    assert configs.rel_l2(f, ref[: N + 1]) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("case", CASES)
+def test_vor_div_uv(jg, orc, case, prec):
+    N, nlat, nlon, nd = case
+    gm, om = _meshes(jg, orc, N, nlat, nlon, nd, prec)
+    u, v = _grid(om, nd, 21), _grid(om, nd, 22)
+    vg, dg, vr, dr = gm.spectral(nd), gm.spectral(nd), om.spectral(nd), om.spectral(nd)
+    jg.Vor_Div_From_Grid_UV(gm, u, v, vg, dg)
+    orc.Vor_Div_From_Grid_UV(om, u, v, vr, dr)
+    assert configs.rel_l2(vg, vr) < TOL[prec] and configs.rel_l2(dg, dr) < TOL[prec]
+    s1, s2 = _spec(om, nd, 31, lower=False), _spec(om, nd, 32, lower=False)
+    ug, vgg, ur, vrr = gm.grid(nd), gm.grid(nd), om.grid(nd), om.grid(nd)
+    jg.UV_Grid_From_Vor_Div(gm, s1, s2, ug, vgg)
+    orc.UV_Grid_From_Vor_Div(om, s1, s2, ur, vrr)
+    assert configs.rel_l2(ug, ur) < TOL[prec] and configs.rel_l2(vgg, vrr) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("case", CASES)
+def test_gradients_advection_laplacian(jg, orc, case, prec):
+    N, nlat, nlon, nd = case
+    gm, om = _meshes(jg, orc, N, nlat, nlon, nd, prec)
+    s = _spec(om, nd, 41, lower=False)
+    a1, a2, b1, b2 = gm.grid(nd), gm.grid(nd), om.grid(nd), om.grid(nd)
+    jg.Compute_Gradients(gm, s, a1, a2)
+    orc.Compute_Gradients(om, s, b1, b2)
+    assert configs.rel_l2(a1, b1) < TOL[prec] and configs.rel_l2(a2, b2) < TOL[prec]
+    u, v, dh = _grid(om, nd, 42), _grid(om, nd, 43), _grid(om, nd, 44)
+    dg, dr = dh.copy(order="F"), dh.copy(order="F")
+    jg.Add_Horizontal_Advection(gm, s, u, v, dg)
+    orc.Add_Horizontal_Advection(om, s, u, v, dr)
+    assert configs.rel_l2(dg - dh, dr - dh) < 10 * TOL[prec]
+    lg, lr = s.copy(order="F"), s.copy(order="F")
+    jg.Apply_Laplacian(gm, lg)
+    orc.Apply_Laplacian(om, lr)
+    assert configs.rel_l2(lg, lr) < TOL[prec]
+    g1 = _grid(om, 1, 45) + 3.0
+    assert abs(jg.Area_Weighted_Global_Mean(gm, g1) - orc.Area_Weighted_Global_Mean(om, g1)) < 10 * TOL[prec] * 3
+
+
+def test_shape_errors(jg):
+    gm = jg.Spectral_Spherical_Mesh(21, 22, 32, 64, 3, 1.0)
+    with pytest.raises(AssertionError):
+        jg.Trans_Spherical_To_Grid(gm, gm.spectral(2), gm.grid(2))  # third dim must be nd or 1
+    with pytest.raises(AssertionError):
+        jg.Spectral_Spherical_Mesh(21, 23, 32, 64, 3, 1.0)  # num_spherical must be N+1
+    with pytest.raises(AssertionError):
+        jg.Spectral_Spherical_Mesh(21, 22, 31, 64, 3, 1.0)  # odd nlat (reference @assert)
