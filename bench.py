@@ -1,0 +1,406 @@
+#!/usr/bin/env python
+"""Held-Suarez T42L20 throughput on GB300: mixed precision vs the FP64 GPU path, at stated error.
+
+One bench "step" is one simulated day (72 model steps of dt = 1200 s) of the Held-Suarez T42L20
+dry dynamical core (128 x 64 Gaussian grid, 20 sigma levels), the reference's headline experiment
+(exp/HSt42/HS.jl).  The initial state is the reference's Spectral_Initialize_Fields! (isothermal
+264 K at rest, ps = 1e5 Pa, its vorticity seed) plus seeded N(0, 0.1^2) K white noise on the grid
+(synthetic input; there is no dataset).
+
+value      sim-days/s of the mixed-precision path (FP32 state, transforms and tendencies; FP64 wave-
+           matrix solve and global sums), device-resident, CUDA-event timed over K sim-days, L2 flushed
+           (256 MiB write) before every timed sim-day.
+e2e        the same through the C ABI with host (pinned) buffers: per sim-day the prognostic state is
+           uploaded, 72 steps run, and the state is read back; wall-clock.
+fp64       the FP64 GPU path on the same workload, same timing; error_vs_fp64 = relative L2 of
+           T, u, v, ps between the two paths after the same number of days.
+roofline   the dominant kernel of the mixed step (largest summed CUDA-event time), its algorithmic
+           bytes per launch / its mean launch time, against the measured HBM copy bandwidth.
+cpu_baseline  the FP64 C oracle (a restatement of the reference on the host) timed on a bounded sample.
+--impl reference  times that oracle on all host threads on the same workload (the reference itself is
+           Julia and Julia is not installed on the GPU hosts).
+Multi-GPU: replicas only (independent members, different seeds), value = sum of sim-days / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "idealizedspectralgcm.jl_gb300")
+sys.path[:0] = [PKG]
+
+WORKLOAD = "hs_t42l20"
+METRIC = "Held-Suarez T42L20 sim-days/s: mixed-precision vs FP64 GPU at stated error"
+STATE_FIELDS = ["spe_vor_c", "spe_vor_p", "spe_div_c", "spe_div_p", "spe_lnps_c", "spe_lnps_p", "spe_t_c",
+                "spe_t_p", "grid_u_c", "grid_u_p", "grid_v_c", "grid_v_p", "grid_ps_c", "grid_ps_p", "grid_t_c",
+                "grid_t_p", "grid_vor", "grid_div"]
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ------------------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+            time.sleep(0.4)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        load = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+class L2Flush:
+    """Writes a 256 MiB device buffer (> 129 MB L2) between timed iterations."""
+
+    def __init__(self, device: int):
+        self.buf = None
+        try:
+            import torch
+
+            self.torch = torch
+            self.buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{device}")
+        except Exception as e:  # torch without CUDA
+            log("L2 flush unavailable:", e)
+
+    def __call__(self):
+        if self.buf is not None:
+            self.buf.fill_(1.0)
+            self.torch.cuda.synchronize()
+
+
+def pinned_like(arr):
+    try:
+        import torch
+
+        t = torch.empty(arr.size, dtype=torch.float64 if arr.dtype.kind == "f" else torch.complex128,
+                        pin_memory=True)
+        out = t.numpy().reshape(arr.shape, order="F")
+        out[...] = arr
+        return out, t
+    except Exception:
+        return arr.copy(order="F"), None
+
+
+# ------------------------------------------------------------------------------------------------
+def algorithmic_bytes(name: str, N: int, nlat: int, nlon: int, nd: int, esize: int) -> float:
+    """Bytes a kernel of the HS step must move per launch (each input read once, each output
+    written once), for state element size `esize` (4 FP32, 8 FP64)."""
+    G = nlon * nlat                     # grid points per level
+    S = (N + 1) * (N + 4) // 2          # spectral modes n >= m per level (complex)
+    F = (N + 1) * nlat                  # Fourier coefficients per column (complex)
+    c = 2 * esize                       # complex element
+    table = {
+        "s2g_legendre(grad lnps,T)": (1 + nd) * S * c + (2 + 2 * nd) * F * c,
+        "ifft(grad lnps,T)": (2 + 2 * nd) * F * c + (2 + 2 * nd) * G * esize + G * esize,
+        "hs_column": (10 * nd + 5) * G * esize + (5 * nd + 1) * G * esize,
+        "fft(tendencies)": (4 * nd + 1) * G * esize + (4 * nd + 1) * F * c,
+        "g2s_legendre(vor,div,T,lnps)": (4 * nd + 1) * F * c + (3 * nd + 1) * S * c,
+        "hs_implicit": (9 * nd + 3) * S * c + (6 * nd + 2) * S * c + (N + 1) * nd * nd * 8,
+        "s2g_legendre(vor,div,u,v,T,lnps)": (3 * nd + 1) * S * c + (5 * nd + 1) * F * c,
+        "ifft(vor,div,u,v,T,lnps)": (5 * nd + 1) * F * c + (5 * nd + 2) * G * esize,
+        "hs_corr_reduce": (3 * nd + 1) * G * esize,
+        "hs_corr_apply": 2 * (nd + 1) * G * esize,
+    }
+    return float(table[name])
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get(kernel)
+    except Exception:
+        return None
+
+
+# ------------------------------------------------------------------------------------------------
+def cpu_baseline(seconds_target: float = 12.0):
+    """The FP64 C oracle on the host cores: bounded sample of the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from jgcm import configs
+
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    m = configs.make_mesh(oracle, WORKLOAD)
+    md = oracle.Model(m, configs.PARAMS[WORKLOAD])
+    configs.init_held_suarez(oracle, m, md)
+    md.step(1)  # init step
+    t0 = time.perf_counter()
+    md.step(2)
+    per = (time.perf_counter() - t0) / 2
+    n = max(2, min(720, int(seconds_target / max(per, 1e-6))))
+    t0 = time.perf_counter()
+    md.step(n)
+    el = time.perf_counter() - t0
+    spd = configs.STEPS_PER_DAY[WORKLOAD]
+    return {"value": (n / spd) / el, "unit": "sim-days/s", "cores": threads, "kind": "port",
+            "sample": f"{n} steady steps ({n / spd:.2f} sim-days) of HS T42L20 in FP64 on the C oracle, "
+                      f"{threads} OpenMP threads, {el:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from jgcm import configs
+
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    m = configs.make_mesh(oracle, WORKLOAD)
+    md = oracle.Model(m, configs.PARAMS[WORKLOAD])
+    configs.init_held_suarez(oracle, m, md)
+    spd = configs.STEPS_PER_DAY[WORKLOAD]
+    md.step(1)
+    for _ in range(args.warmup):
+        md.step(spd)
+    t0 = time.perf_counter()
+    md.step(spd * args.steps)
+    el = time.perf_counter() - t0
+    v = args.steps / el
+    line = {"metric": METRIC, "value": v, "unit": "sim-days/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * el / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "Held-Suarez T42L20 (128x64x20), dt 1200 s, 1 step = 1 sim-day",
+                       "implementation": "FP64 C oracle restating the reference (Julia absent on the host)"},
+            "cpu_baseline": {"value": v, "unit": "sim-days/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} sim-days after {args.warmup} warm-up sim-days"},
+            "e2e": {"value": v, "unit": "sim-days/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------------------------------------
+def run_jgcm(args):
+    import numpy as np
+
+    import jgcm
+    from jgcm import configs
+
+    rank, world, local = dist_env()
+    jgcm.set_device(local)
+    K, W = args.steps, args.warmup
+    spd = configs.STEPS_PER_DAY[WORKLOAD]
+    params = configs.PARAMS[WORKLOAD]
+    g = configs.GRIDS[WORKLOAD]
+    N, nlat, nlon, nd = g["num_fourier"], g["nlat"], g["nlon"], g["nd"]
+    seed = configs.BASE_SEED + rank
+
+    m64 = configs.make_mesh(jgcm, WORKLOAD, precision="fp64")
+    mod64 = jgcm.Model(m64, params)
+    configs.init_held_suarez(jgcm, m64, mod64, seed=seed)
+    mmx = configs.make_mesh(jgcm, WORKLOAD, precision=args.precision)
+    modmx = jgcm.Model(mmx, params)
+    configs.copy_state(mod64, modmx, "held_suarez")  # identical start (FP64 init, rounded)
+    init_state = {f: mod64.get(f) for f in STATE_FIELDS}
+
+    flush = L2Flush(local)
+    for mdl in (modmx, mod64):
+        mdl.step(spd * W)  # warm-up sim-days (the first step is the reference's init step)
+    # ---- timed: mixed precision
+    clocks = ClockSampler(local)
+    barrier(world)
+    clocks.start()
+    ms_mx = []
+    for _ in range(K):
+        flush()
+        ms_mx.append(modmx.time_steps(spd))
+    clk = clocks.stop()
+    barrier(world)
+    # ---- FP64 GPU path, same timing
+    ms_64 = []
+    for _ in range(K):
+        flush()
+        ms_64.append(mod64.time_steps(spd))
+    days_done = W + K
+    err = {}
+    for key, f in (("T", "grid_t_c"), ("u", "grid_u_c"), ("v", "grid_v_c"), ("ps", "grid_ps_c")):
+        err[key] = configs.rel_l2(modmx.get(f), mod64.get(f))
+    # ---- end to end through host buffers
+    e2e_model = jgcm.Model(mmx, params)
+    host = {f: pinned_like(a) for f, a in init_state.items()}
+    bytes_io = sum(a.nbytes for a, _ in host.values())
+    for f, (a, _) in host.items():
+        e2e_model.set(f, a)
+    e2e_model.step(1)  # the init step; every timed sim-day below restarts from host state
+    t_e2e = 0.0
+    ne2e = max(1, K)
+    for _ in range(ne2e):
+        flush()
+        t0 = time.perf_counter()
+        for f, (a, _) in host.items():
+            e2e_model.set(f, a)
+        e2e_model.step(spd)
+        for f, (a, _) in host.items():
+            a[...] = e2e_model.get(f)
+        t_e2e += time.perf_counter() - t0
+    # ---- per-kernel times and the roofline of the dominant kernel
+    kt = modmx.kernel_times(spd)
+    esize = 8 if args.precision == "fp64" else 4
+    dom = max(kt, key=kt.get)
+    alg = algorithmic_bytes(dom, N, nlat, nlon, nd, esize)
+    peak, peak_kind = measured_peaks()
+    achieved = alg / (kt[dom] * 1e-3) / 1e9
+    # ---- aggregate over ranks
+    t_mx = max_over_ranks(sum(ms_mx) / 1000.0, world)
+    t_64 = max_over_ranks(sum(ms_64) / 1000.0, world)
+    t_e2e = max_over_ranks(t_e2e, world)
+    value = world * K / t_mx
+    value64 = world * K / t_64
+    if rank != 0:
+        return 0
+    base = None
+    if not args.no_cpu_baseline and world == 1:
+        try:
+            base = cpu_baseline()
+        except Exception as e:  # the checker must not take the GPU result down
+            base = {"value": None, "unit": "sim-days/s", "cores": os.cpu_count(), "kind": "port",
+                    "sample": f"failed: {e}"}
+    launches = modmx.launches_per_step()
+    line = {
+        "metric": METRIC, "value": value, "unit": "sim-days/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": 1000.0 * t_mx / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if args.precision != "fp64" else "f64", "data": "synthetic",
+        "config": {"workload": "Held-Suarez T42L20 (128x64 Gaussian, 20 sigma levels), dt 1200 s; 1 step = 1 "
+                               "sim-day = 72 model steps",
+                   "precision": f"{args.precision} state/transforms/tendencies, fp64 semi-implicit solve and "
+                                f"global mass/energy sums",
+                   "initial_state": "isothermal 264 K at rest, ps 1e5 Pa, reference vorticity seed, seeded "
+                                    "N(0,0.1^2) K grid noise",
+                   "l2": "flushed (256 MiB write) before every timed sim-day; working set ~20 MB is otherwise "
+                         "L2-resident within a day", "parallelism": f"replicas x{world}",
+                   "ms_per_model_step": 1000.0 * t_mx / (K * spd)},
+        "fp64": {"value": value64, "unit": "sim-days/s", "ms_per_step": 1000.0 * t_64 / K},
+        "speedup_vs_fp64": value / value64,
+        "error_vs_fp64": {"after_sim_days": round(days_done, 3), **{k: v for k, v in err.items()}},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "algorithmic_bytes": alg,
+                     "launch_ms": kt[dom], "traffic": profile_traffic(dom),
+                     "step_kernels_ms": {k: round(v, 5) for k, v in kt.items()}},
+        "cpu_baseline": base,
+        "e2e": {"value": world * ne2e / t_e2e, "unit": "sim-days/s", "h2d_bytes_per_step": bytes_io,
+                "d2h_bytes_per_step": bytes_io},
+        "gpu_launches": launches * spd * K,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5, help="timed sim-days")
+    ap.add_argument("--warmup", type=int, default=3, help="warm-up sim-days")
+    ap.add_argument("--impl", default="jgcm", choices=["jgcm", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "tf32x3", "bf16x3"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, _ = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    try:
+        if args.impl == "reference":
+            return run_reference(args)
+        return run_jgcm(args)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

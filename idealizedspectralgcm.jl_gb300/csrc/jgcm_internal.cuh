@@ -173,10 +173,22 @@ struct jgcm_mesh {
   void* d_spec[4];    // native spectral scratch (T2), nd levels each
   double* d_red;      // reduction scratch (FP64)
   unsigned int* d_counter;
+  int refs;           // 1 for the caller's handle + 1 per live model built on the mesh
   std::string name;
 };
 
 namespace jgcm {
+// Per-launch CUDA-event markers for kernel timing (jgcm_model_kernel_times): while a Marker is
+// installed on the calling thread, every kernel launch of the library records an event after it.
+struct Marker {
+  cudaEvent_t* ev;
+  int n, cap;
+};
+extern thread_local Marker* g_marker;
+inline void mark(cudaStream_t st) {
+  if (g_marker && g_marker->n < g_marker->cap) cudaEventRecord(g_marker->ev[g_marker->n++], st);
+}
+
 inline bool is_fp64(const jgcm_mesh* m) { return m->precision == JGCM_FP64; }
 inline size_t spec_elems(const jgcm_mesh* m, int L) { return (size_t)(m->N + 1) * (m->ns + 1) * L; }
 inline size_t grid_elems(const jgcm_mesh* m, int L) { return (size_t)m->nlon * m->nlat * L; }
@@ -201,4 +213,6 @@ Tables<T> tables(const jgcm_mesh* m);
 
 // mesh.cu
 int mesh_build_tables(jgcm_mesh* m);
+void mesh_retain(jgcm_mesh* m);
+void mesh_release(jgcm_mesh* m);  // frees the mesh when the last reference goes
 }  // namespace jgcm

@@ -17,6 +17,7 @@
 
 namespace jgcm {
 
+thread_local Marker* g_marker = nullptr;
 static thread_local char g_err[1024] = "";
 void set_error(const char* fmt, ...) {
   va_list ap;
@@ -230,6 +231,11 @@ using namespace jgcm;
 extern "C" const char* jgcm_last_error(void) { return jgcm::last_error(); }
 extern "C" int jgcm_version(void) { return 1; }
 
+extern "C" int jgcm_set_device(int device) {
+  JG_CUDA(cudaSetDevice(device));
+  return JGCM_OK;
+}
+
 extern "C" int jgcm_device_info(int* sm_count, int* cc_major, int* cc_minor) {
   int dev = 0;
   JG_CUDA(cudaGetDevice(&dev));
@@ -323,14 +329,25 @@ extern "C" int jgcm_mesh_create(int num_fourier, int num_spherical, int nlat, in
   MCHK(cuda(cudaMemset(m->d_counter, 0, 64 * sizeof(unsigned int)), "memset"));
   MCHK(cuda(cudaMalloc(&m->d_ref2, T3 * 8), "alloc ref2"));
 #undef MCHK
+  m->refs = 1;
   *out = m;
   return JGCM_OK;
 }
 
-extern "C" int jgcm_mesh_destroy(jgcm_mesh* m) {
-  if (!m) return JGCM_OK;
+namespace jgcm {
+void mesh_retain(jgcm_mesh* m) { m->refs++; }
+void mesh_release(jgcm_mesh* m) {
+  if (--m->refs > 0) return;
   cudaStreamSynchronize(m->stream);
   mesh_free(m);
+}
+}  // namespace jgcm
+
+// Models hold a reference, so a mesh released before its models stays alive until the
+// last of them is destroyed (host garbage collectors may finalise in any order).
+extern "C" int jgcm_mesh_destroy(jgcm_mesh* m) {
+  if (!m) return JGCM_OK;
+  mesh_release(m);
   return JGCM_OK;
 }
 

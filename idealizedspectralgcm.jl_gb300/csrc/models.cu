@@ -12,6 +12,7 @@
 // solve runs in FP64 (one warp per spectral mode, lanes over levels) and the mass/energy
 // fixers (Spectral_Dynamics.jl:5-68) use deterministic FP64 reductions.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -28,8 +29,8 @@ using V2 = typename C2<T>::t;
 
 struct VertCoef {  // Vert_Coordinate (even_sigma) and the semi-implicit reference column
   double ak[JGCM_MAX_ND + 1], bk[JGCM_MAX_ND + 1], dak[JGCM_MAX_ND], dbk[JGCM_MAX_ND];
-  double dp_ref[JGCM_MAX_ND], lnph_ref[JGCM_MAX_ND + 1], lnpf_ref[JGCM_MAX_ND], t_ref[JGCM_MAX_ND],
-      h[JGCM_MAX_ND];
+  double dp_ref[JGCM_MAX_ND], rdp_ref[JGCM_MAX_ND], lnph_ref[JGCM_MAX_ND + 1], lnpf_ref[JGCM_MAX_ND],
+      t_ref[JGCM_MAX_ND], h[JGCM_MAX_ND];
 };
 }  // namespace
 
@@ -47,7 +48,7 @@ struct jgcm_model {
   void *spe_dvor, *spe_ddiv, *spe_dlnps, *spe_dt;
   void *g_dlps, *g_dtps, *g_dlT, *g_dtT, *g_ducos, *g_dvcos, *g_dt, *g_energy, *g_dlnps, *g_diag;
   void *coriolis, *damping;  // [nlat], [m][n] in T
-  double* damping64;         // [m][n] FP64 (semi-implicit kernel)
+  void* dfac[2];             // [m][n] in T: 1/(1 + Δt d) (init step), 1/(1 + 2Δt d) (afterwards)
   // FP64 semi-implicit data
   VertCoef vc;
   double* div_mat;  // host nd*nd column-major
@@ -66,18 +67,20 @@ int lvl(const jgcm_model* md, int which) { return (md->rot + which) % 3; }  // 0
 
 // ------------------------------------------------------------------------------------------
 // warp scans over levels (lanes >= nd hold zero)
-__device__ __forceinline__ double scan_incl(double x, int lane) {
+template <typename R>
+__device__ __forceinline__ R scan_incl(R x, int lane) {
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    double y = __shfl_up_sync(FULL, x, o);
+    R y = __shfl_up_sync(FULL, x, o);
     if (lane >= o) x += y;
   }
   return x;
 }
-__device__ __forceinline__ double rscan_incl(double x, int lane) {
+template <typename R>
+__device__ __forceinline__ R rscan_incl(R x, int lane) {
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    double y = __shfl_down_sync(FULL, x, o);
+    R y = __shfl_down_sync(FULL, x, o);
     if (lane + o < 32) x += y;
   }
   return x;
@@ -118,18 +121,22 @@ __device__ bool grid_reduce_last(const double* vals, double* partials, unsigned*
   __syncthreads();
   if (!am_last) return false;
   __threadfence();
+  // fold with the first nt threads (blockDim is a power of two; nt <= 256)
+  const int nt = blockDim.x < 256 ? blockDim.x : 256;
   double s[NV];
   for (int v = 0; v < NV; v++) s[v] = 0.0;
-  for (int jj = threadIdx.x; jj < (int)gridDim.y; jj += blockDim.x) {
-    for (int v = 0; v < NV; v++) {
-      double r = 0.0;
-      for (int b = 0; b < (int)gridDim.x; b++) r += __ldcg(partials + (size_t)v * nb + (size_t)jj * gridDim.x + b);
-      s[v] += r * wts[jj];
+  if (threadIdx.x < nt)
+    for (int jj = threadIdx.x; jj < (int)gridDim.y; jj += nt) {
+      for (int v = 0; v < NV; v++) {
+        double r = 0.0;
+        for (int b = 0; b < (int)gridDim.x; b++) r += __ldcg(partials + (size_t)v * nb + (size_t)jj * gridDim.x + b);
+        s[v] += r * wts[jj];
+      }
     }
-  }
-  for (int v = 0; v < NV; v++) red[v][threadIdx.x] = s[v];
+  if (threadIdx.x < nt)
+    for (int v = 0; v < NV; v++) red[v][threadIdx.x] = s[v];
   __syncthreads();
-  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+  for (int st = nt / 2; st > 0; st >>= 1) {
     if (threadIdx.x < st)
       for (int v = 0; v < NV; v++) red[v][threadIdx.x] += red[v][threadIdx.x + st];
     __syncthreads();
@@ -169,9 +176,10 @@ __global__ void __launch_bounds__(256) k_hs_column(HSColArgs<T> a, VertCoef vc) 
   const T ps = a.ps_c[col];
   const T ph0 = (T)vc.ak[k] + (T)vc.bk[k] * ps, ph1 = (T)vc.ak[k + 1] + (T)vc.bk[k + 1] * ps;
   const T dp = ph1 - ph0;
+  const T rdp = (T)1 / dp;
   const T lnph1 = log(ph1);
   const T lnph0 = (k == 0) ? (T)0 : log(ph0);
-  const T lnpf = (k == 0) ? lnph1 - (T)1.0 : lnph1 + ph0 * (lnph1 - lnph0) / dp - (T)1.0;
+  const T lnpf = (k == 0) ? lnph1 - (T)1.0 : lnph1 + ph0 * (lnph1 - lnph0) * rdp - (T)1.0;
   const T pfull = exp(lnpf);
   const T psurf = (T)vc.ak[nd] + (T)vc.bk[nd] * ps;
   // ---- HS_Forcing! on the previous level
@@ -198,13 +206,13 @@ __global__ void __launch_bounds__(256) k_hs_column(HSColArgs<T> a, VertCoef vc) 
   T k_t = ka + (ks - ka) / ((T)1.0 - sb) * smax * c4;
   dt = dt - k_t * (tp - teq);
   if (act) a.t_eq[x] = teq;
-  // ---- Compute_Corrections_Init sums (FP64): column energy integral with ps_p
+  // ---- Compute_Corrections_Init sums: column energy integral with ps_p, accumulated in FP64
   const double psp = (double)a.ps_p[col];
   double e_p = 0.0;
   if (act) {
-    double ua = (double)up + Dt * (double)du, va = (double)vp + Dt * (double)dv;
-    double E = 0.5 * (ua * ua + va * va) + a.cp * ((double)tp + Dt * (double)dt);
-    e_p = E * (vc.dak[k] + vc.dbk[k] * psp);
+    T ua = up + (T)Dt * du, va = vp + (T)Dt * dv;
+    T E = (T)0.5 * (ua * ua + va * va) + (T)a.cp * (tp + (T)Dt * dt);
+    e_p = (double)E * (vc.dak[k] + vc.dbk[k] * psp);
   }
   const double col_e = warp_sum(e_p);
   // ---- Four_In_One! (Spectral_Dynamics.jl:88-183) on the current level
@@ -221,35 +229,35 @@ __global__ void __launch_bounds__(256) k_hs_column(HSColArgs<T> a, VertCoef vc) 
   const T dlps = a.dlps[col], dtps = a.dtps[col];
   const T R = (T)a.rdgas, kap = (T)a.rdgas / (T)a.cp;
   const T dlnp_p = lnph1 - lnpf, dlnp_m = lnpf - lnph0, dlnp = lnph1 - lnph0;
-  const T x1 = ((T)vc.bk[k] * dlnp_m + (T)vc.bk[k + 1] * dlnp_p) / dp;
+  const T x1 = ((T)vc.bk[k] * dlnp_m + (T)vc.bk[k + 1] * dlnp_p) * rdp;
   const T dlnp_dl = x1 * dlps, dlnp_dt = x1 * dtps;
   du = du - R * t * dlnp_dl;
   dv = dv - R * t * dlnp_dt;
   T dmean = dvg * dp + (T)vc.dbk[k] * (u * dlps + v * dtps);
   if (!act) dmean = 0;
-  double incl = scan_incl((double)dmean, lane);
-  double tot_d = __shfl_sync(FULL, incl, nd - 1);
-  T excl = (T)shfl_up1(incl, lane, 0.0);
-  T x5 = -(excl * dlnp + dmean * dlnp_p) / dp + u * dlnp_dl + v * dlnp_dt;
+  const T incl = scan_incl<T>(dmean, lane);         // sum_{r<=k} D_r
+  const T tot = __shfl_sync(FULL, incl, nd - 1);
+  const T excl = shfl_up1(incl, lane, (T)0);
+  T x5 = -(excl * dlnp + dmean * dlnp_p) * rdp + u * dlnp_dl + v * dlnp_dt;
   dt = dt + kap * t * x5;
-  const T tot = (T)tot_d;
   // M_{k+1/2}: -sum_{r<=k} D_r + B_{k+1/2} sum_r D_r ; zero at top and surface
-  T Mhi = (lane + 1 <= nd - 1) ? -(T)incl + tot * (T)vc.bk[k + 1] : (T)0;
+  T Mhi = (lane + 1 <= nd - 1) ? -incl + tot * (T)vc.bk[k + 1] : (T)0;
   T Mlo = shfl_up1(Mhi, lane, (T)0);
   // ---- Compute_Geopotential! (Press_And_Geopot.jl:71-111), bottom-up
   T term = act ? R * t * (lnph1 - lnph0) : (T)0;
-  double rs = rscan_incl((double)term, lane);        // sum_{r>=k} term_r
+  const T rs = rscan_incl<T>(term, lane);           // sum_{r>=k} term_r
   T gs = act ? a.geopots[col] : (T)0;
   gs = __shfl_sync(FULL, gs, 0);
-  T ghalf_hi = gs + (T)shfl_dn1(rs, lane, nd, 0.0);  // Phi_{k+1/2}
+  T ghalf_hi = gs + shfl_dn1(rs, lane, nd, (T)0);  // Phi_{k+1/2}
   T gfull = ghalf_hi + R * t * (lnph1 - lnpf);
   // ---- Vert_Advection! (second_centered_wts) for u, v, T
   T dp_m = shfl_up1(dp, lane, (T)1);
+  const T wlo = dp_m / (dp_m + dp);
   auto vadv = [&](T r) -> T {
     T r_m = shfl_up1(r, lane, (T)0);
-    T flux_lo = (lane >= 1) ? Mlo * (r_m + (r - r_m) * dp_m / (dp_m + dp)) : (T)0;
+    T flux_lo = (lane >= 1) ? Mlo * (r_m + (r - r_m) * wlo) : (T)0;
     T flux_hi = shfl_dn1(flux_lo, lane, nd, (T)0);
-    return (flux_lo - flux_hi + r * (Mhi - Mlo)) / dp;
+    return (flux_lo - flux_hi + r * (Mhi - Mlo)) * rdp;
   };
   du = du + vadv(u);
   dv = dv + vadv(v);
@@ -290,64 +298,72 @@ __global__ void __launch_bounds__(256) k_hs_column(HSColArgs<T> a, VertCoef vc) 
 // ------------------------------------------------------------------------------------------
 // Semi-implicit correction (Adjust_δlnps_δt_δdiv! + Implicit_Correction!, Semi_Implicit.jl:
 // 271-513) followed by Compute_Spectral_Damping! and Filtered_Leapfrog! for vor, div, T, lnps
-// (Spectral_Dynamics.jl:313-327).  One warp per spectral mode (m,n), lane = level, FP64.
+// (Spectral_Dynamics.jl:313-327).  One warp per spectral mode (m,n), lane = level.  The
+// per-n solve with W_n = (I - ξ² ∇²_n D)^{-1} runs in FP64; the linearised vertical operators
+// and the time filter run in the state precision T (FP64 on the FP64 path).
 template <typename T>
 struct ImplArgs {
   const V2<T>*dvor, *ddiv, *dtend, *dlnps;  // spectral tendencies from the analysis
   V2<T> *vor_p, *vor_c, *vor_n, *div_p, *div_c, *div_n, *t_p, *t_c, *t_n, *lnps_p, *lnps_c, *lnps_n;
-  const double *eig, *damping;  // FP64 [m][n]
-  const double* W;              // [N+1][c][r]
+  const T *eig, *damping, *dfac;  // [m][n]: -n(n+1)/a², damping, 1/(1 + Δt' damping) for this step
+  const double* W;                // [N+1][c][r]
   const int2* pairs;
   int npairs, nd, ns, N, init_step, dt;
   double xi, ps_ref, kappa, rdgas, robert;
 };
 
-struct C64 {
-  double x, y;
+template <typename R>
+struct CX {
+  R x, y;
 };
 
-__device__ __forceinline__ void linear_ps_t(const VertCoef& vc, int lane, int nd, double kappa, C64 d, C64& dps,
-                                            C64& dtt) {
+// Linear_Ps_T_δdiv! (Semi_Implicit.jl:271-341) for one (m,n) column held one level per lane.
+template <typename R>
+__device__ __forceinline__ void linear_ps_t(const VertCoef& vc, int lane, int nd, R kappa, CX<R> d, CX<R>& dps,
+                                            CX<R>& dtt) {
   const bool act = lane < nd;
   const int k = act ? lane : 0;
-  double dpr = vc.dp_ref[k];
-  C64 dm = {act ? d.x * dpr : 0.0, act ? d.y * dpr : 0.0};
-  double ix = scan_incl(dm.x, lane), iy = scan_incl(dm.y, lane);
-  double tx = __shfl_sync(FULL, ix, nd - 1), ty = __shfl_sync(FULL, iy, nd - 1);
-  double ex = shfl_up1(ix, lane, 0.0), ey = shfl_up1(iy, lane, 0.0);
-  double dlnp = vc.lnph_ref[k + 1] - vc.lnph_ref[k], dlnp_p = vc.lnph_ref[k + 1] - vc.lnpf_ref[k];
-  double c = -kappa * vc.t_ref[k];
-  dtt.x = c * (ex * dlnp + dm.x * dlnp_p) / dpr;
-  dtt.y = c * (ey * dlnp + dm.y * dlnp_p) / dpr;
+  const R dpr = (R)vc.dp_ref[k], rdpr = (R)vc.rdp_ref[k];
+  CX<R> dm = {act ? d.x * dpr : (R)0, act ? d.y * dpr : (R)0};
+  R ix = scan_incl<R>(dm.x, lane), iy = scan_incl<R>(dm.y, lane);
+  R tx = __shfl_sync(FULL, ix, nd - 1), ty = __shfl_sync(FULL, iy, nd - 1);
+  R ex = shfl_up1(ix, lane, (R)0), ey = shfl_up1(iy, lane, (R)0);
+  R dlnp = (R)(vc.lnph_ref[k + 1] - vc.lnph_ref[k]), dlnp_p = (R)(vc.lnph_ref[k + 1] - vc.lnpf_ref[k]);
+  R c = -kappa * (R)vc.t_ref[k];
+  dtt.x = c * (ex * dlnp + dm.x * dlnp_p) * rdpr;
+  dtt.y = c * (ey * dlnp + dm.y * dlnp_p) * rdpr;
   // M_{k+1/2} (k <= nd-2) and the centred vertical-advection term with (t_ref[k] - t_ref[k-1])
-  double bk1 = vc.bk[k + 1];
-  double mhx = (lane + 1 <= nd - 1) ? -ix + tx * bk1 : 0.0, mhy = (lane + 1 <= nd - 1) ? -iy + ty * bk1 : 0.0;
-  double tdh = (lane + 1 <= nd - 1) ? vc.t_ref[k + 1] - vc.t_ref[k] : 0.0;
-  double mdhx = mhx * tdh, mdhy = mhy * tdh;  // Mdt_{k+1/2}
-  double mdlx = shfl_up1(mdhx, lane, 0.0), mdly = shfl_up1(mdhy, lane, 0.0);
-  dtt.x = dtt.x - 0.5 * (mdhx + mdlx) / dpr;
-  dtt.y = dtt.y - 0.5 * (mdhy + mdly) / dpr;
+  const bool inner = lane + 1 <= nd - 1;
+  R bk1 = (R)vc.bk[k + 1];
+  R mhx = inner ? -ix + tx * bk1 : (R)0, mhy = inner ? -iy + ty * bk1 : (R)0;
+  R tdh = inner ? (R)(vc.t_ref[k + 1] - vc.t_ref[k]) : (R)0;
+  R mdhx = mhx * tdh, mdhy = mhy * tdh;  // Mdt_{k+1/2}
+  R mdlx = shfl_up1(mdhx, lane, (R)0), mdly = shfl_up1(mdhy, lane, (R)0);
+  dtt.x = dtt.x - (R)0.5 * (mdhx + mdlx) * rdpr;
+  dtt.y = dtt.y - (R)0.5 * (mdhy + mdly) * rdpr;
   dps.x = -tx;
   dps.y = -ty;
 }
 
-template <typename T>
-__device__ __forceinline__ void lf64(const ImplArgs<T>& a, double d, double& dq, double qp, double& qc, double& qn) {
-  const double r = a.robert;
-  if (a.init_step) {
-    dq = (dq - qc * d) / (1.0 + a.dt * d);
-    qn = qc + a.dt * dq;
-    qc = qc + r * (-1.0 * qc + qn);
+// Compute_Spectral_Damping! + Filtered_Leapfrog! (Time_Integrator.jl:58-101); f = 1/(1 + Δt' d).
+template <typename R>
+__device__ __forceinline__ void lf(int init, int Dt, R rob, R d, R f, R& dq, R qp, R& qc, R& qn) {
+  if (init) {
+    dq = (dq - qc * d) * f;
+    qn = qc + (R)Dt * dq;
+    qc = qc + rob * ((R)-1.0 * qc + qn);
   } else {
-    dq = (dq - qp * d) / (1.0 + (2 * a.dt) * d);
-    qc = qc + r * (qp - 2 * qc);
-    qn = qp + (2 * a.dt) * dq;
-    qc = qc + r * qn;
+    dq = (dq - qp * d) * f;
+    qc = qc + rob * (qp - (R)2 * qc);
+    qn = qp + (R)(2 * Dt) * dq;
+    qc = qc + rob * qn;
   }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, VertCoef vc) {
+  using R = T;
+  using C = CX<R>;
   const int lane = threadIdx.x & 31;
   const int pid = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (pid >= a.npairs) return;  // whole warp exits together
@@ -357,78 +373,81 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, VertCoef vc)
   const int k = act ? lane : 0;
   const size_t row = (size_t)m * (a.ns + 1) + n;
   const size_t s = row * nd + k;
-  auto ld = [&](const V2<T>* p) -> C64 {
-    if (!act) return C64{0, 0};
+  auto ld = [&](const V2<T>* p) -> C {
+    if (!act) return C{0, 0};
     V2<T> v = p[s];
-    return C64{(double)v.x, (double)v.y};
+    return C{v.x, v.y};
   };
-  C64 ddiv = ld(a.ddiv), dtt = ld(a.dtend), dvor = ld(a.dvor);
-  C64 divp = ld(a.div_p), divc = ld(a.div_c), tp = ld(a.t_p), tc = ld(a.t_c), vorp = ld(a.vor_p), vorc = ld(a.vor_c);
+  C ddiv = ld(a.ddiv), dtt = ld(a.dtend), dvor = ld(a.dvor);
+  C divp = ld(a.div_p), divc = ld(a.div_c), tp = ld(a.t_p), tc = ld(a.t_c), vorp = ld(a.vor_p), vorc = ld(a.vor_c);
   V2<T> l0 = a.dlnps[row], lp0 = a.lnps_p[row], lc0 = a.lnps_c[row];
-  C64 dl = {(double)l0.x, (double)l0.y}, lp = {(double)lp0.x, (double)lp0.y}, lc = {(double)lc0.x, (double)lc0.y};
-  const double xi = a.xi, psr = a.ps_ref, eig = a.eig[row];
+  C dl = {l0.x, l0.y}, lp = {lp0.x, lp0.y}, lc = {lc0.x, lc0.y};
+  const R xi = (R)a.xi, rpsr = (R)(1.0 / a.ps_ref), xipsr = (R)(a.xi / a.ps_ref), eig = a.eig[row];
+  const R kap = (R)a.kappa, Rg = (R)a.rdgas;
   // Adjust_δlnps_δt_δdiv! :360-404
-  C64 dps, dtmp;
-  linear_ps_t(vc, lane, nd, a.kappa, C64{divp.x - divc.x, divp.y - divc.y}, dps, dtmp);
+  C dps, dtmp;
+  linear_ps_t<R>(vc, lane, nd, kap, C{divp.x - divc.x, divp.y - divc.y}, dps, dtmp);
   dtt.x = dtt.x + dtmp.x;
   dtt.y = dtt.y + dtmp.y;
-  dl.x = dl.x + dps.x / psr;
-  dl.y = dl.y + dps.y / psr;
-  C64 t2 = {tp.x - tc.x + xi * dtt.x, tp.y - tc.y + xi * dtt.y};
-  C64 l2 = {lp.x - lc.x + xi * dl.x, lp.y - lc.y + xi * dl.y};
+  dl.x = dl.x + dps.x * rpsr;
+  dl.y = dl.y + dps.y * rpsr;
+  C t2 = {tp.x - tc.x + xi * dtt.x, tp.y - tc.y + xi * dtt.y};
+  C l2 = {lp.x - lc.x + xi * dl.x, lp.y - lc.y + xi * dl.y};
   // Linear_Geopot_δt! :213-241
-  double dh = vc.lnph_ref[k + 1] - vc.lnph_ref[k];
-  double tmx = act ? a.rdgas * (t2.x * dh) : 0.0, tmy = act ? a.rdgas * (t2.y * dh) : 0.0;
-  double rx = rscan_incl(tmx, lane), ry = rscan_incl(tmy, lane);
-  double hx = shfl_dn1(rx, lane, nd, 0.0), hy = shfl_dn1(ry, lane, nd, 0.0);  // Φ_{k+1/2}
-  double df = vc.lnph_ref[k + 1] - vc.lnpf_ref[k];
-  double gx = hx + a.rdgas * (t2.x * df), gy = hy + a.rdgas * (t2.y * df);
-  double hk = vc.h[k] * psr;
+  R dh = (R)(vc.lnph_ref[k + 1] - vc.lnph_ref[k]);
+  R tmx = act ? Rg * (t2.x * dh) : (R)0, tmy = act ? Rg * (t2.y * dh) : (R)0;
+  R rx = rscan_incl<R>(tmx, lane), ry = rscan_incl<R>(tmy, lane);
+  R hx = shfl_dn1(rx, lane, nd, (R)0), hy = shfl_dn1(ry, lane, nd, (R)0);  // Φ_{k+1/2}
+  R df = (R)(vc.lnph_ref[k + 1] - vc.lnpf_ref[k]);
+  R gx = hx + Rg * (t2.x * df), gy = hy + Rg * (t2.y * df);
+  R hk = (R)(vc.h[k] * a.ps_ref);
   ddiv.x = ddiv.x - eig * (gx + hk * l2.x);
   ddiv.y = ddiv.y - eig * (gy + hk * l2.y);
-  // wave-matrix solve, n <= N only
+  // wave-matrix solve in FP64, n <= N only (Implicit_Correction! :486-497)
   if (n <= a.N) {
     const double* W = a.W + (size_t)n * nd * nd;
+    const double bxl = (double)ddiv.x, byl = (double)ddiv.y;
     double sx = 0, sy = 0;
     for (int c = 0; c < nd; c++) {
-      double bx = __shfl_sync(FULL, ddiv.x, c), by = __shfl_sync(FULL, ddiv.y, c);
+      double bx = __shfl_sync(FULL, bxl, c), by = __shfl_sync(FULL, byl, c);
       double wv = act ? W[(size_t)c * nd + k] : 0.0;
       sx = sx + wv * bx;
       sy = sy + wv * by;
     }
-    ddiv.x = act ? sx : 0.0;
-    ddiv.y = act ? sy : 0.0;
+    ddiv.x = act ? (R)sx : (R)0;
+    ddiv.y = act ? (R)sy : (R)0;
   }
-  linear_ps_t(vc, lane, nd, a.kappa, ddiv, dps, dtmp);
+  linear_ps_t<R>(vc, lane, nd, kap, ddiv, dps, dtmp);
   dtt.x = dtt.x + xi * dtmp.x;
   dtt.y = dtt.y + xi * dtmp.y;
-  dl.x = dl.x + xi / psr * dps.x;
-  dl.y = dl.y + xi / psr * dps.y;
+  dl.x = dl.x + xipsr * dps.x;
+  dl.y = dl.y + xipsr * dps.y;
   // damping + leapfrog
-  const double d = a.damping[row];
+  const R d = a.damping[row], f = a.dfac[row], rob = (R)a.robert;
+  const int ini = a.init_step, Dt = a.dt;
   if (act) {
-    C64 vn, dn, tn;
-    lf64(a, d, dvor.x, vorp.x, vorc.x, vn.x);
-    lf64(a, d, dvor.y, vorp.y, vorc.y, vn.y);
-    lf64(a, d, ddiv.x, divp.x, divc.x, dn.x);
-    lf64(a, d, ddiv.y, divp.y, divc.y, dn.y);
-    lf64(a, d, dtt.x, tp.x, tc.x, tn.x);
-    lf64(a, d, dtt.y, tp.y, tc.y, tn.y);
+    C vn, dn, tn;
+    lf<R>(ini, Dt, rob, d, f, dvor.x, vorp.x, vorc.x, vn.x);
+    lf<R>(ini, Dt, rob, d, f, dvor.y, vorp.y, vorc.y, vn.y);
+    lf<R>(ini, Dt, rob, d, f, ddiv.x, divp.x, divc.x, dn.x);
+    lf<R>(ini, Dt, rob, d, f, ddiv.y, divp.y, divc.y, dn.y);
+    lf<R>(ini, Dt, rob, d, f, dtt.x, tp.x, tc.x, tn.x);
+    lf<R>(ini, Dt, rob, d, f, dtt.y, tp.y, tc.y, tn.y);
     V2<T> o;
-    o.x = (T)vn.x; o.y = (T)vn.y; a.vor_n[s] = o;
-    o.x = (T)vorc.x; o.y = (T)vorc.y; a.vor_c[s] = o;
-    o.x = (T)dn.x; o.y = (T)dn.y; a.div_n[s] = o;
-    o.x = (T)divc.x; o.y = (T)divc.y; a.div_c[s] = o;
-    o.x = (T)tn.x; o.y = (T)tn.y; a.t_n[s] = o;
-    o.x = (T)tc.x; o.y = (T)tc.y; a.t_c[s] = o;
+    o.x = vn.x; o.y = vn.y; a.vor_n[s] = o;
+    o.x = vorc.x; o.y = vorc.y; a.vor_c[s] = o;
+    o.x = dn.x; o.y = dn.y; a.div_n[s] = o;
+    o.x = divc.x; o.y = divc.y; a.div_c[s] = o;
+    o.x = tn.x; o.y = tn.y; a.t_n[s] = o;
+    o.x = tc.x; o.y = tc.y; a.t_c[s] = o;
   }
-  if (lane == 0) {  // lnps: leapfrog without damping
-    C64 ln;
-    lf64(a, 0.0, dl.x, lp.x, lc.x, ln.x);
-    lf64(a, 0.0, dl.y, lp.y, lc.y, ln.y);
+  if (lane == 0) {  // lnps: leapfrog without damping (d = 0, f = 1)
+    C ln;
+    lf<R>(ini, Dt, rob, (R)0, (R)1, dl.x, lp.x, lc.x, ln.x);
+    lf<R>(ini, Dt, rob, (R)0, (R)1, dl.y, lp.y, lc.y, ln.y);
     V2<T> o;
-    o.x = (T)ln.x; o.y = (T)ln.y; a.lnps_n[row] = o;
-    o.x = (T)lc.x; o.y = (T)lc.y; a.lnps_c[row] = o;
+    o.x = ln.x; o.y = ln.y; a.lnps_n[row] = o;
+    o.x = lc.x; o.y = lc.y; a.lnps_c[row] = o;
   }
 }
 
@@ -448,32 +467,36 @@ struct CorrArgs {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, VertCoef vc) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int i = blockIdx.x * 8 + w, j = blockIdx.y, nd = a.nd;
-  const bool act = lane < nd && i < a.nlon;
-  const size_t col = (size_t)j * a.nlon + (i < a.nlon ? i : 0);
-  const size_t x = (size_t)(act ? lane : 0) * a.nlat * a.nlon + col;
-  double ps = (i < a.nlon) ? (double)a.ps_n[col] : 0.0;
+__global__ void __launch_bounds__(1024) k_hs_corr_reduce(CorrArgs<T> a, VertCoef vc) {
+  // one block per latitude row, one thread per column (coalesced along longitude)
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  const int i = threadIdx.x, j = blockIdx.y, nd = a.nd;
+  const bool act = i < a.nlon;
+  const size_t G = (size_t)a.nlat * a.nlon, col = (size_t)j * a.nlon + (act ? i : 0);
+  double ps = act ? (double)a.ps_n[col] : 0.0;
   double ea = 0, eb = 0;
   if (act) {
-    double u = a.u_n[x], v = a.v_n[x], t = a.t_n[x];
-    double E = 0.5 * (u * u + v * v) + a.cp * t;
-    ea = E * vc.dak[lane];
-    eb = E * (vc.dbk[lane] * ps);
+    const T cp = (T)a.cp;
+    for (int k = 0; k < nd; k++) {
+      size_t x = (size_t)k * G + col;
+      T u = a.u_n[x], v = a.v_n[x], t = a.t_n[x];
+      T E = (T)0.5 * (u * u + v * v) + cp * t;
+      ea += (double)E * vc.dak[k];
+      eb += (double)E * vc.dbk[k];
+    }
+    eb *= ps;
   }
-  ea = warp_sum(ea);
-  eb = warp_sum(eb);
-  __shared__ double sm[3][8];
+  const double s0 = warp_sum(ps), s1 = warp_sum(ea), s2 = warp_sum(eb);
+  __shared__ double sm[3][32];
   if (lane == 0) {
-    sm[0][w] = ps;
-    sm[1][w] = ea;
-    sm[2][w] = eb;
+    sm[0][w] = s0;
+    sm[1][w] = s1;
+    sm[2][w] = s2;
   }
   __syncthreads();
   double vals[3] = {0, 0, 0};
   if (threadIdx.x == 0)
-    for (int q = 0; q < 8; q++) {
+    for (int q = 0; q < nw; q++) {
       vals[0] += sm[0][q];
       vals[1] += sm[1][q];
       vals[2] += sm[2][q];
@@ -663,6 +686,7 @@ void vertical_setup(jgcm_model* md) {
   for (int k = 0; k <= nd; k++) vc.lnph_ref[k] = lph[k];
   for (int k = 0; k < nd; k++) vc.lnpf_ref[k] = lpf[k];
   for (int k = 0; k < nd; k++) vc.t_ref[k] = md->P.t_ref;
+  for (int k = 0; k < nd; k++) vc.rdp_ref[k] = 1.0 / vc.dp_ref[k];
   for (int k = 0; k <= nd; k++) dlh[k] = vc.bk[k] / ph[k];
   for (int k = 0; k < nd; k++)
     dlf[k] = (vc.bk[k + 1] * (vc.lnph_ref[k + 1] - vc.lnpf_ref[k]) + vc.bk[k] * (vc.lnpf_ref[k] - vc.lnph_ref[k])) /
@@ -697,12 +721,14 @@ void vertical_setup(jgcm_model* md) {
 
 // ------------------------------------------------------------------------------------------
 template <typename T>
-__global__ void k_fill_damping(const double* eig, T* damping, int N, int ns, double coef, int order) {
-  // Time_Integrator.jl:31: damping = coef (eig / eig[1, num_spherical])^order
+__global__ void k_fill_damping(const double* eig, T* out, int N, int ns, double coef, int order, double dt_eff) {
+  // Time_Integrator.jl:31: damping = coef (eig / eig[1, num_spherical])^order; with dt_eff > 0
+  // the implicit damping factor 1/(1 + dt_eff damping) of Compute_Spectral_Damping! (:76-80)
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (N + 1) * (ns + 1)) return;
   double e0 = eig[0 * (ns + 1) + (ns - 1)];
-  damping[t] = (T)(coef * pow(eig[t] / e0, (double)order));
+  double d = coef * pow(eig[t] / e0, (double)order);
+  out[t] = (T)(dt_eff > 0.0 ? 1.0 / (1.0 + dt_eff * d) : d);
 }
 template <typename T>
 __global__ void k_fill_coriolis(const double* sinth, T* f, int nlat, double omega) {
@@ -736,7 +762,8 @@ void model_free(jgcm_model* md) {
   void* ps[] = {md->grid_vor, md->grid_div, md->grid_lnps, md->grid_t_eq, md->grid_geopots, md->grid_h_eq,
                 md->spe_zero, md->spe_dvor, md->spe_ddiv, md->spe_dlnps, md->spe_dt, md->g_dlps, md->g_dtps,
                 md->g_dlT, md->g_dtT, md->g_ducos, md->g_dvcos, md->g_dt, md->g_energy, md->g_dlnps, md->g_diag,
-                md->coriolis, md->damping, md->damping64, md->d_W, md->d_pairs, md->d_partials, md->d_scalars,
+                md->coriolis, md->damping, md->dfac[0], md->dfac[1], md->d_W, md->d_pairs, md->d_partials,
+                md->d_scalars,
                 md->d_counter};
   for (auto p : ps)
     if (p) cudaFree(p);
@@ -817,17 +844,20 @@ int model_alloc(jgcm_model* md) {
   JG_TRY(alloc((void**)&md->d_scalars, 16 * 8));
   JG_TRY(alloc((void**)&md->d_counter, 16 * sizeof(unsigned)));
   int nt = (N + 1) * (ns + 1);
-  JG_TRY(alloc((void**)&md->damping64, (size_t)nt * 8));
-  k_fill_damping<double><<<(nt + 127) / 128, 128, 0, m->stream>>>(m->t64.eig, md->damping64, N, ns,
-                                                                  md->P.damping_coef, md->P.damping_order);
+  JG_TRY(alloc(&md->dfac[0], (size_t)nt * ts));
+  JG_TRY(alloc(&md->dfac[1], (size_t)nt * ts));
+  const double cf = md->P.damping_coef, dt1 = md->P.dt, dt2 = 2.0 * md->P.dt;
+  const int od = md->P.damping_order, nb = (nt + 127) / 128;
   if (is_fp64(m)) {
-    k_fill_damping<double><<<(nt + 127) / 128, 128, 0, m->stream>>>(m->t64.eig, (double*)md->damping, N, ns,
-                                                                    md->P.damping_coef, md->P.damping_order);
+    k_fill_damping<double><<<nb, 128, 0, m->stream>>>(m->t64.eig, (double*)md->damping, N, ns, cf, od, 0.0);
+    k_fill_damping<double><<<nb, 128, 0, m->stream>>>(m->t64.eig, (double*)md->dfac[0], N, ns, cf, od, dt1);
+    k_fill_damping<double><<<nb, 128, 0, m->stream>>>(m->t64.eig, (double*)md->dfac[1], N, ns, cf, od, dt2);
     k_fill_coriolis<double><<<(m->nlat + 127) / 128, 128, 0, m->stream>>>(m->d_sinth, (double*)md->coriolis, m->nlat,
                                                                           md->P.omega);
   } else {
-    k_fill_damping<float><<<(nt + 127) / 128, 128, 0, m->stream>>>(m->t64.eig, (float*)md->damping, N, ns,
-                                                                   md->P.damping_coef, md->P.damping_order);
+    k_fill_damping<float><<<nb, 128, 0, m->stream>>>(m->t64.eig, (float*)md->damping, N, ns, cf, od, 0.0);
+    k_fill_damping<float><<<nb, 128, 0, m->stream>>>(m->t64.eig, (float*)md->dfac[0], N, ns, cf, od, dt1);
+    k_fill_damping<float><<<nb, 128, 0, m->stream>>>(m->t64.eig, (float*)md->dfac[1], N, ns, cf, od, dt2);
     k_fill_coriolis<float><<<(m->nlat + 127) / 128, 128, 0, m->stream>>>(m->d_sinth, (float*)md->coriolis, m->nlat,
                                                                          md->P.omega);
   }
@@ -1079,6 +1109,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   a.grav = md->P.grav;
   dim3 gcol((m->nlon + 7) / 8, m->nlat);
   k_hs_column<T><<<gcol, 256, 0, st>>>(a, md->vc);
+  mark(st);
   JG_CUDA(cudaGetLastError());
   // 3. forward transforms: δu cos, δv cos, δT, energy, δlnps -> vor/div tendencies (alpha
   //    operator, δdiv -= ∇²E), δT, δlnps
@@ -1112,8 +1143,9 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ia.div_p = (V*)md->spe_div[p]; ia.div_c = (V*)md->spe_div[c]; ia.div_n = (V*)md->spe_div[n];
   ia.t_p = (V*)md->spe_t[p]; ia.t_c = (V*)md->spe_t[c]; ia.t_n = (V*)md->spe_t[n];
   ia.lnps_p = (V*)md->spe_lnps[p]; ia.lnps_c = (V*)md->spe_lnps[c]; ia.lnps_n = (V*)md->spe_lnps[n];
-  ia.eig = m->t64.eig;
-  ia.damping = md->damping64;
+  ia.eig = tb.eig;
+  ia.damping = (const T*)md->damping;
+  ia.dfac = (const T*)md->dfac[md->init_step ? 0 : 1];
   ia.W = md->d_W + (md->init_step ? 0 : (size_t)(m->N + 1) * nd * nd);
   ia.pairs = md->d_pairs;
   ia.npairs = md->npairs;
@@ -1128,6 +1160,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ia.rdgas = md->P.rdgas;
   ia.robert = md->P.robert_coef;
   k_hs_implicit<T><<<(md->npairs + 7) / 8, 256, 0, st>>>(ia, md->vc);
+  mark(st);
   JG_CUDA(cudaGetLastError());
   // 5. back to the grid: vor, div, u, v, T, lnps (+ ps = exp(lnps))
   S2GPlan s2;
@@ -1171,12 +1204,14 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ca.do_energy = md->P.do_energy_correction;
   ca.cp = md->cp_air;
   ca.grav = md->P.grav;
-  k_hs_corr_reduce<T><<<gcol, 256, 0, st>>>(ca, md->vc);
+  k_hs_corr_reduce<T><<<dim3(1, m->nlat), m->nlon < 32 ? 32 : m->nlon, 0, st>>>(ca, md->vc);
+  mark(st);
   JG_CUDA(cudaGetLastError());
   size_t nt = grid_elems(m, nd), nps = grid_elems(m, 1);
   int nb = (int)((nt + 255) / 256);
   if (nb > 4 * 152) nb = 4 * 152;
   k_hs_corr_apply<T><<<nb, 256, 0, st>>>((T*)md->grid_t[n], (T*)md->grid_ps[n], md->d_scalars, nt, nps);
+  mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;
 }
@@ -1326,14 +1361,17 @@ extern "C" int jgcm_model_create(jgcm_mesh* mesh, const jgcm_params* params, jgc
     model_free(md);
     return s;
   }
+  mesh_retain(mesh);
   *out = md;
   return JGCM_OK;
 }
 
 extern "C" int jgcm_model_destroy(jgcm_model* md) {
   if (!md) return JGCM_OK;
-  cudaStreamSynchronize(md->mesh->stream);
+  jgcm_mesh* m = md->mesh;
+  cudaStreamSynchronize(m->stream);
   model_free(md);
+  mesh_release(m);
   return JGCM_OK;
 }
 
@@ -1350,10 +1388,81 @@ extern "C" int jgcm_model_init_step(jgcm_model* md, int* init_step) {
   return JGCM_OK;
 }
 
+extern "C" int jgcm_model_update_init_step(jgcm_model* md) {
+  JG_ARG(md, "NULL argument");
+  JG_ARG(md->init_step, "Update_Init_Step!: the model is not in its init step (@assert(integrator.init_step))");
+  md->init_step = 0;  // the steady wave matrices are already built; the next step selects them
+  return JGCM_OK;
+}
+
+static int launches_per_step(const jgcm_model* md) {
+  return md->P.kind == JGCM_BAROTROPIC ? 4 : md->P.kind == JGCM_SHALLOW_WATER ? 6 : 10;
+}
+
 extern "C" int jgcm_model_launches_per_step(jgcm_model* md, int* launches) {
   JG_ARG(md && launches, "NULL argument");
-  *launches = md->P.kind == JGCM_BAROTROPIC ? 4 : md->P.kind == JGCM_SHALLOW_WATER ? 6 : 10;
+  *launches = launches_per_step(md);
   return JGCM_OK;
+}
+
+extern "C" int jgcm_model_kernel_name(jgcm_model* md, int slot, char* buf, int cap) {
+  JG_ARG(md && buf && cap > 0, "bad arguments");
+  static const char* hs[] = {"s2g_legendre(grad lnps,T)", "ifft(grad lnps,T)", "hs_column", "fft(tendencies)",
+                             "g2s_legendre(vor,div,T,lnps)", "hs_implicit", "s2g_legendre(vor,div,u,v,T,lnps)",
+                             "ifft(vor,div,u,v,T,lnps)", "hs_corr_reduce", "hs_corr_apply"};
+  static const char* bt[] = {"fft(flux)", "g2s_legendre(vor+leapfrog)", "s2g_legendre(vor,u,v)", "ifft(vor,u,v)"};
+  static const char* sw[] = {"s2g_legendre(grad h)", "ifft(grad h)", "fft(fluxes,kin,dh)",
+                             "g2s_legendre(vor,div,h+implicit+leapfrog)", "s2g_legendre(vor,div,h,u,v)",
+                             "ifft(vor,div,h,u,v)"};
+  const char** names = md->P.kind == JGCM_HELD_SUAREZ ? hs : md->P.kind == JGCM_BAROTROPIC ? bt : sw;
+  JG_ARG(slot >= 0 && slot < launches_per_step(md), "slot out of range");
+  snprintf(buf, cap, "%s", names[slot]);
+  return JGCM_OK;
+}
+
+// Per-kernel device times of steady steps: every launch is followed by an event (eager launches,
+// events on the model stream), ms[slot] = mean over nsteps of event(slot) - event(slot - 1).
+extern "C" int jgcm_model_kernel_times(jgcm_model* md, int nsteps, float* ms, int cap, int* count) {
+  JG_ARG(md && ms && count && nsteps > 0, "bad arguments");
+  jgcm_mesh* m = md->mesh;
+  const int L = launches_per_step(md);
+  JG_ARG(cap >= L, "buffer too small");
+  if (md->init_step) JG_TRY(model_step(md));
+  std::vector<cudaEvent_t> ev((size_t)nsteps * L + 1);
+  for (auto& e : ev) JG_CUDA(cudaEventCreate(&e));
+  Marker mk{ev.data() + 1, 0, nsteps * L};
+  JG_CUDA(cudaStreamSynchronize(m->stream));
+  JG_CUDA(cudaEventRecord(ev[0], m->stream));
+  g_marker = &mk;
+  int st = JGCM_OK;
+  for (int s = 0; s < nsteps && st == JGCM_OK; s++) {
+    st = issue(md, m->stream);
+    if (st == JGCM_OK) after_step(md);
+  }
+  g_marker = nullptr;
+  if (st == JGCM_OK) {
+    cudaError_t e = cudaEventSynchronize(ev.back());
+    if (e != cudaSuccess) {
+      set_error("kernel timing: %s", cudaGetErrorString(e));
+      st = JGCM_E_CUDA;
+    }
+  }
+  if (st == JGCM_OK && mk.n != nsteps * L) {
+    set_error("kernel timing: %d launches recorded, %d expected", mk.n, nsteps * L);
+    st = JGCM_E_STATE;
+  }
+  if (st == JGCM_OK) {
+    for (int k = 0; k < L; k++) ms[k] = 0.0f;
+    for (int s = 0; s < nsteps; s++)
+      for (int k = 0; k < L; k++) {
+        float t = 0.0f;
+        cudaEventElapsedTime(&t, ev[(size_t)s * L + k], ev[(size_t)s * L + k + 1]);
+        ms[k] += t / nsteps;
+      }
+    *count = L;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return st;
 }
 
 extern "C" int jgcm_model_time_steps(jgcm_model* md, int nsteps, float* ms) {

@@ -5,7 +5,7 @@
 //                    F[m][j] = sum_n P_n^m(mu_j) s_n^m over n = m..N+1 (the reference's extra
 //                    row N+1 included), a dense (nlat/2 x K) x (K x C) contraction per m,
 //                    mirrored to the northern hemisphere by parity;
-//   k_ifft         : inverse real zonal FFT of every (latitude, column) row, two real rows per
+//   k_ifft         : inverse real zonal FFT of every (latitude, column) row as a half-length
 //                    complex FFT, radix-2 in shared memory, fused epilogue (÷cos, exp, ×ps).
 // grid -> spectral (Trans_Grid_To_Spherical!, :221-293; Vor_Div_From_Grid_UV!, :349-459) runs as
 //   k_fft          : forward real zonal FFT (fft/nlon) with fused prologue (×cos, vorticity
@@ -38,18 +38,19 @@ __device__ __forceinline__ const G& group_of(const G* g, int ng, int c, int* k) 
 }
 
 // ------------------------------------------------------------------------------------------
-// radix-2 DIT stages over `npair` rows of length n held as (re, im) in shared memory, input in
-// bit-reversed order, output in natural order.  SIGN = -1 forward (fft), +1 backward (ifft).
+// Complex radix-2 DIT stages over `nrow` rows of length h = nlon/2 held as (re, im) in shared
+// memory (row stride h), input in bit-reversed order, output in natural order.  tw holds
+// e^{2 pi i t / nlon} for t < nlon/2 (cos, sin interleaved).  SIGN = -1 forward, +1 backward.
 template <typename T, int SIGN>
-__device__ __forceinline__ void fft_stages(T* re, T* im, const T* tw, int npair, int n, int logn) {
-  const int hn = n >> 1;
-  for (int s = 1; s <= logn; s++) {
+__device__ __forceinline__ void fft_stages(T* re, T* im, const T* tw, int nrow, int h, int logh) {
+  const int hh = h >> 1;
+  for (int s = 1; s <= logh; s++) {
     const int half = 1 << (s - 1);
-    const int tshift = logn - s;  // twiddle index = k * (n / 2^s)
-    for (int b = threadIdx.x; b < npair * hn; b += blockDim.x) {
-      int p = b / hn, bb = b - p * hn;
+    const int tshift = logh + 1 - s;  // e^{2 pi i k / 2^s} = tw[k * nlon / 2^s]
+    for (int b = threadIdx.x; b < nrow * hh; b += blockDim.x) {
+      int p = b / hh, bb = b - p * hh;
       int grp = bb >> (s - 1), k = bb & (half - 1);
-      int i0 = p * n + (grp << s) + k, i1 = i0 + half;
+      int i0 = p * h + (grp << s) + k, i1 = i0 + half;
       int ti = k << tshift;
       T wr = tw[2 * ti], wi = (T)SIGN * tw[2 * ti + 1];
       T xr = re[i1], xi = im[i1];
@@ -177,59 +178,56 @@ __global__ void __launch_bounds__(256) k_s2g_legendre(S2GPlan plan, Tables<T> tb
   }
 }
 
-// Fourier -> grid: inverse real FFT, two columns per complex transform.
-// grid (ceil(C/(2*CP)), nlat), 256 threads.  Row x(t) = Re g_0 + 2 Re sum_{m=1}^{N} g_m e^{imλ_t},
-// i.e. 2 nλ Re(ifft(g)) with g_0 halved as in Spectral_Spherical_Mesh.jl:211-215.
+// Fourier -> grid: inverse real FFT, one column per half-length (h = nlon/2) complex transform,
+// so rounding never leaks between columns of different magnitude.  grid (ceil(C/CT), nlat),
+// 256 threads.  Row x(λ_t) = Re g_0 + 2 Re sum_{m=1}^{N} g_m e^{imλ_t}, i.e. 2 nλ Re(ifft(g)) with
+// g_0 halved as in Spectral_Spherical_Mesh.jl:211-215.  With X the Hermitian spectrum,
+// Z[m] = (X[m] + conj X[h-m]) + i e^{2πim/nλ} (X[m] - conj X[h-m]) and z = ifft_h(Z) give
+// x[2k] = Re z[k], x[2k+1] = Im z[k].
 template <typename T>
 __global__ void __launch_bounds__(256) k_ifft(IFFTPlan plan, Tables<T> tb, const V2<T>* __restrict__ F, int N,
-                                              int nlat, int nlon, int logn, int CP) {
+                                              int nlat, int nlon, int logh, int CT) {
   using V = V2<T>;
   extern __shared__ __align__(16) unsigned char smem[];
+  const int h = nlon >> 1;
   T* re = (T*)smem;
-  T* im = re + CP * nlon;
-  T* tw = im + CP * nlon;
-  V* G = (V*)(smem + align16((size_t)(2 * CP * nlon + nlon) * sizeof(T)));  // [N+1][2CP]
+  T* im = re + CT * h;
+  T* tw = im + CT * h;
+  V* G = (V*)(smem + align16((size_t)(CT * nlon + nlon) * sizeof(T)));  // [N+1][CT]
   const int j = blockIdx.y;
   const int C = plan.C;
-  const int ncol = 2 * CP;
-  const int cbase = blockIdx.x * ncol;
+  const int cbase = blockIdx.x * CT;
   for (int i = threadIdx.x; i < nlon; i += blockDim.x) tw[i] = tb.tw[i];
-  for (int i = threadIdx.x; i < CP * nlon; i += blockDim.x) {
-    re[i] = 0;
-    im[i] = 0;
-  }
-  for (int i = threadIdx.x; i < (N + 1) * ncol; i += blockDim.x) {
-    int mm = i / ncol, cc = i - mm * ncol, c = cbase + cc;
+  for (int i = threadIdx.x; i < (N + 1) * CT; i += blockDim.x) {
+    int mm = i / CT, cc = i - mm * CT, c = cbase + cc;
     V g;
     g.x = 0;
     g.y = 0;
     if (c < C) g = F[((size_t)mm * nlat + j) * C + c];
+    if (mm == 0) g.y = 0;  // only Re g_0 reaches the grid
     G[i] = g;
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < (N + 1) * CP; i += blockDim.x) {
-    int mm = i / CP, p = i - mm * CP;
-    V g = G[mm * ncol + 2 * p], h = G[mm * ncol + 2 * p + 1];
-    T* R = re + p * nlon;
-    T* I = im + p * nlon;
-    if (mm == 0) {
-      R[0] = g.x;
-      I[0] = h.x;
-    } else {
-      int a = brev(mm, logn), b = brev(nlon - mm, logn);
-      R[a] = g.x - h.y;
-      I[a] = g.y + h.x;
-      R[b] = g.x + h.y;
-      I[b] = h.x - g.y;
-    }
+  for (int i = threadIdx.x; i < CT * h; i += blockDim.x) {
+    int cc = i / h, mm = i - cc * h, q = h - mm;
+    V x, y;
+    x.x = x.y = y.x = y.y = 0;
+    if (mm <= N) x = G[mm * CT + cc];
+    if (mm >= 1 && q <= N) y = G[q * CT + cc];
+    T er = x.x + y.x, ei = x.y - y.y;  // X[m] + conj X[h-m]
+    T dr = x.x - y.x, di = x.y + y.y;  // X[m] - conj X[h-m]
+    T c = tw[2 * mm], s = tw[2 * mm + 1];
+    T orr = dr * c - di * s, oi = dr * s + di * c;
+    int pos = brev(mm, logh);
+    re[cc * h + pos] = er - oi;
+    im[cc * h + pos] = ei + orr;
   }
   __syncthreads();
-  fft_stages<T, 1>(re, im, tw, CP, nlon, logn);
-  for (int i = threadIdx.x; i < ncol * nlon; i += blockDim.x) {
+  fft_stages<T, 1>(re, im, tw, CT, h, logh);
+  for (int i = threadIdx.x; i < CT * nlon; i += blockDim.x) {
     int cc = i / nlon, t = i - cc * nlon, c = cbase + cc;
     if (c >= C) continue;
-    int p = cc >> 1;
-    T x = (cc & 1) ? im[p * nlon + t] : re[p * nlon + t];
+    T x = (t & 1) ? im[cc * h + (t >> 1)] : re[cc * h + (t >> 1)];
     int k;
     const GridOutGroup& g = group_of(plan.g, plan.ng, c, &k);
     size_t idx = ((size_t)k * nlat + j) * nlon + t;
@@ -252,18 +250,21 @@ __global__ void __launch_bounds__(256) k_ifft(IFFTPlan plan, Tables<T> tb, const
   }
 }
 
-// Grid -> Fourier: forward real FFT (fft/nlon), two columns per complex transform, modes 0..N.
+// Grid -> Fourier: forward real FFT (fft/nlon), modes 0..N, one column per half-length complex
+// transform: z[k] = x[2k] + i x[2k+1], Z = fft_h(z), X[m] = E[m] + e^{-2πim/nλ} O[m] with
+// E = (Z[m] + conj Z[h-m])/2, O = (Z[m] - conj Z[h-m])/(2i).  grid (ceil(C/CT), nlat).
 template <typename T>
 __global__ void __launch_bounds__(256) k_fft(FFTPlan plan, Tables<T> tb, V2<T>* __restrict__ F, int N, int nlat,
-                                             int nlon, int logn, int CP) {
+                                             int nlon, int logh, int CT) {
   using V = V2<T>;
   extern __shared__ __align__(16) unsigned char smem[];
+  const int h = nlon >> 1;
   T* re = (T*)smem;
-  T* im = re + CP * nlon;
-  T* tw = im + CP * nlon;
+  T* im = re + CT * h;
+  T* tw = im + CT * h;
   const int j = blockIdx.y;
   const int C = plan.C;
-  const int ncol = 2 * CP;
+  const int ncol = CT;
   const int cbase = blockIdx.x * ncol;
   for (int i = threadIdx.x; i < nlon; i += blockDim.x) tw[i] = tb.tw[i];
   const T cj = tb.cosj[j];
@@ -306,29 +307,26 @@ __global__ void __launch_bounds__(256) k_fft(FFTPlan plan, Tables<T> tb, V2<T>* 
         } break;
       }
     }
-    int p = cc >> 1, pos = brev(t, logn);
-    if (cc & 1)
-      im[p * nlon + pos] = x;
+    int pos = brev(t >> 1, logh);
+    if (t & 1)
+      im[cc * h + pos] = x;
     else
-      re[p * nlon + pos] = x;
+      re[cc * h + pos] = x;
   }
-  // columns beyond C inside the last pair were written as zero above (x = 0)
   __syncthreads();
-  fft_stages<T, -1>(re, im, tw, CP, nlon, logn);
+  fft_stages<T, -1>(re, im, tw, CT, h, logh);
   const T scale = (T)(0.5 / nlon);
   for (int i = threadIdx.x; i < (N + 1) * ncol; i += blockDim.x) {
     int mm = i / ncol, cc = i - mm * ncol, c = cbase + cc;
     if (c >= C) continue;
-    int p = cc >> 1, mn = (nlon - mm) & (nlon - 1);
-    T zr = re[p * nlon + mm], zi = im[p * nlon + mm], wr = re[p * nlon + mn], wi = im[p * nlon + mn];
+    int q = (h - mm) & (h - 1);
+    T zr = re[cc * h + mm], zi = im[cc * h + mm], qr = re[cc * h + q], qi = im[cc * h + q];
+    T er = zr + qr, ei = zi - qi;  // 2 E
+    T orr = zi + qi, oi = qr - zr;  // 2 O
+    T tc = tw[2 * mm], ts = tw[2 * mm + 1];  // e^{-2πim/nλ} = tc - i ts
     V o;
-    if (cc & 1) {
-      o.x = (zi + wi) * scale;
-      o.y = (wr - zr) * scale;
-    } else {
-      o.x = (zr + wr) * scale;
-      o.y = (zi - wi) * scale;
-    }
+    o.x = (er + (tc * orr + ts * oi)) * scale;
+    o.y = (ei + (tc * oi - ts * orr)) * scale;
     F[((size_t)mm * nlat + j) * C + c] = o;
   }
 }
@@ -372,8 +370,8 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
   const int K = ns + 1 - m;
   const int C = plan.C;
   const int cbase = blockIdx.x * CT;
-  V* S = (V*)smem;              // [4][CT][nh] symmetric
-  V* A = S + 4 * CT * nh;       // [4][CT][nh] antisymmetric
+  V* S = (V*)smem;              // [4][nh][CT] symmetric      (column fastest: no bank conflicts)
+  V* A = S + 4 * CT * nh;       // [4][nh][CT] antisymmetric
   const size_t mrow = (size_t)m * (ns + 1);
   for (int i = threadIdx.x; i < 4 * CT * nh; i += blockDim.x) {
     int slot = i / (CT * nh), rem = i - slot * CT * nh, jh = rem / CT, cl = rem - jh * CT, c = cbase + cl;
@@ -393,8 +391,8 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
         a.y = x.y - y.y;
       }
     }
-    S[(slot * CT + cl) * nh + jh] = s;
-    A[(slot * CT + cl) * nh + jh] = a;
+    S[(slot * nh + jh) * CT + cl] = s;
+    A[(slot * nh + jh) * CT + cl] = a;
   }
   __syncthreads();
   for (int i = threadIdx.x; i < K * CT; i += blockDim.x) {
@@ -408,12 +406,13 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
     const T* cb = tb.CB + (mrow + n) * nh;
     const size_t sidx = (mrow + n) * g.L + k;
     auto plain = [&](int slot) -> V {
-      const V* src = (even ? S : A) + (slot * CT + cl) * nh;
+      const V* src = (even ? S : A) + slot * nh * CT + cl;
       T sr = 0, si = 0;
       for (int jh = 0; jh < nh; jh++) {
         T w = pw[jh];
-        sr += src[jh].x * w;
-        si += src[jh].y * w;
+        V x = src[jh * CT];
+        sr += x.x * w;
+        si += x.y * w;
       }
       V o;
       o.x = (n == ns) ? (T)0 : sr * (T)0.5;
@@ -422,15 +421,16 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
     };
     // alpha operator: i * sum CA (A) + sign * sum CB (B), all latitudes folded by parity
     auto alpha = [&](int slotA, int slotB, T sign) -> V {
-      const V* sa = (even ? S : A) + (slotA * CT + cl) * nh;
-      const V* sb = (even ? A : S) + (slotB * CT + cl) * nh;
+      const V* sa = (even ? S : A) + slotA * nh * CT + cl;
+      const V* sb = (even ? A : S) + slotB * nh * CT + cl;
       T ar = 0, ai = 0, br = 0, bi = 0;
       for (int jh = 0; jh < nh; jh++) {
         T wa = ca[jh], wb = cb[jh];
-        ar += (-sa[jh].y) * wa;
-        ai += sa[jh].x * wa;
-        br += sb[jh].x * wb;
-        bi += sb[jh].y * wb;
+        V xa = sa[jh * CT], xb = sb[jh * CT];
+        ar += (-xa.y) * wa;
+        ai += xa.x * wa;
+        br += xb.x * wb;
+        bi += xb.y * wb;
       }
       V o;
       o.x = (n == ns) ? (T)0 : ar + sign * br;
@@ -527,7 +527,8 @@ static int configure_smem() {
 }
 
 static inline int s2g_ct(int nh) { return nh >= 256 ? 1 : 256 / nh; }
-static inline int fft_cp(int nlon) { return nlon >= 512 ? 1 : 512 / nlon; }
+// columns per FFT block: CT * nlon/4 butterflies per stage = 256 threads
+static inline int fft_ct(int nlon) { return nlon >= 1024 ? 1 : 1024 / nlon; }
 static inline int g2s_ct(int nh) { return nh >= 64 ? 4 : nh >= 32 ? 8 : 16; }
 
 template <typename T>
@@ -540,11 +541,13 @@ int launch_s2g(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, cudaStream_t
   size_t sm1 = align16((size_t)(m->ns + 1) * nh * sizeof(T)) + (size_t)(m->ns + 1) * ct * sizeof(V);
   dim3 g1((sp.C + ct - 1) / ct, m->N + 1);
   k_s2g_legendre<T><<<g1, 256, sm1, st>>>(sp, tb, (V*)m->d_fbuf, m->ns, m->nlat, ct);
+  mark(st);
   JG_CUDA(cudaGetLastError());
-  const int cp = fft_cp(m->nlon);
-  size_t sm2 = align16((size_t)(2 * cp * m->nlon + m->nlon) * sizeof(T)) + (size_t)(m->N + 1) * 2 * cp * sizeof(V);
-  dim3 g2((ip.C + 2 * cp - 1) / (2 * cp), m->nlat);
-  k_ifft<T><<<g2, 256, sm2, st>>>(ip, tb, (const V*)m->d_fbuf, m->N, m->nlat, m->nlon, m->logn, cp);
+  const int fc = fft_ct(m->nlon);
+  size_t sm2 = align16((size_t)(fc * m->nlon + m->nlon) * sizeof(T)) + (size_t)(m->N + 1) * fc * sizeof(V);
+  dim3 g2((ip.C + fc - 1) / fc, m->nlat);
+  k_ifft<T><<<g2, 256, sm2, st>>>(ip, tb, (const V*)m->d_fbuf, m->N, m->nlat, m->nlon, m->logn - 1, fc);
+  mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;
 }
@@ -555,10 +558,11 @@ int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp, cudaStream_t st) {
   JG_TRY(configure_smem<T>());
   JG_ARG(fp.C <= m->Cmax && fp.C > 0, "bad FFT plan");
   Tables<T> tb = tables<T>(m);
-  const int cp = fft_cp(m->nlon);
-  size_t sm = (size_t)(2 * cp * m->nlon + m->nlon) * sizeof(T);
-  dim3 g((fp.C + 2 * cp - 1) / (2 * cp), m->nlat);
-  k_fft<T><<<g, 256, sm, st>>>(fp, tb, (V*)m->d_fbuf, m->N, m->nlat, m->nlon, m->logn, cp);
+  const int fc = fft_ct(m->nlon);
+  size_t sm = (size_t)(fc * m->nlon + m->nlon) * sizeof(T);
+  dim3 g((fp.C + fc - 1) / fc, m->nlat);
+  k_fft<T><<<g, 256, sm, st>>>(fp, tb, (V*)m->d_fbuf, m->N, m->nlat, m->nlon, m->logn - 1, fc);
+  mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;
 }
@@ -572,6 +576,7 @@ int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp, cudaStream_t 
   size_t sm = (size_t)8 * ct * nh * sizeof(V);
   dim3 g((gp.C + ct - 1) / ct, m->N + 1);
   k_g2s_legendre<T><<<g, 256, sm, st>>>(gp, tb, (const V*)m->d_fbuf, m->ns, m->nlat, fp.C, ct);
+  mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;
 }

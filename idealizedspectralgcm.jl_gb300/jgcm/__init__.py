@@ -84,10 +84,14 @@ def lib():
         "jgcm_model_set_field": (I, [P, C.c_char_p, P, Lg]),
         "jgcm_model_step": (I, [P, I]),
         "jgcm_model_init_step": (I, [P, C.POINTER(I)]),
+        "jgcm_model_update_init_step": (I, [P]),
         "jgcm_spectral_initialize_fields": (I, [P, P, I]),
         "jgcm_model_semi_implicit": (I, [P, C.c_char_p, P, Lg, C.POINTER(Lg)]),
         "jgcm_model_time_steps": (I, [P, I, C.POINTER(C.c_float)]),
         "jgcm_model_launches_per_step": (I, [P, C.POINTER(I)]),
+        "jgcm_model_kernel_times": (I, [P, I, C.POINTER(C.c_float), I, C.POINTER(I)]),
+        "jgcm_model_kernel_name": (I, [P, I, C.c_char_p, I]),
+        "jgcm_set_device": (I, [I]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -331,6 +335,10 @@ class Model:
     def step(self, nsteps=1):
         _check(lib().jgcm_model_step(self._h, int(nsteps)))
 
+    def update_init_step(self):
+        """Update_Init_Step! (Time_Integrator.jl:40-43): leave the forward init-step mode."""
+        _check(lib().jgcm_model_update_init_step(self._h))
+
     def spectral_initialize_fields(self, grid_t_pert=None, vorticity_seed=True):
         """Spectral_Dynamics.jl:372-449 on the device."""
         if grid_t_pert is not None:
@@ -361,3 +369,20 @@ class Model:
         v = C.c_int()
         _check(lib().jgcm_model_launches_per_step(self._h, C.byref(v)))
         return v.value
+
+    def kernel_times(self, nsteps):
+        """{launch slot name: mean CUDA-event ms} over nsteps eager steady steps (advances the model)."""
+        L = self.launches_per_step()
+        arr = (C.c_float * L)()
+        cnt = C.c_int()
+        _check(lib().jgcm_model_kernel_times(self._h, int(nsteps), arr, L, C.byref(cnt)))
+        out = {}
+        buf = C.create_string_buffer(128)
+        for s in range(cnt.value):
+            _check(lib().jgcm_model_kernel_name(self._h, s, buf, 128))
+            out[buf.value.decode()] = float(arr[s])
+        return out
+
+
+def set_device(device: int) -> None:
+    _check(lib().jgcm_set_device(int(device)))

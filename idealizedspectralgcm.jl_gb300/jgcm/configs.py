@@ -192,6 +192,27 @@ def init_held_suarez(backend, mesh, model, seed=BASE_SEED, amplitude=0.1, vortic
     model.spectral_initialize_fields(hs_temperature_noise(mesh, seed, amplitude), vorticity_seed)
 
 
+def add_hs_flow(backend, mesh, model, u0=20.0, wave=2.0e-6):
+    """Superpose a solid-body zonal flow u0 cos(lat) and a wave-4 vorticity pattern on both time
+    levels of a Held-Suarez state (a developed-flow start for parity checks: from rest,
+    vorticity and divergence are at the roundoff level of the 1e5 m^2/s^2 geopotential)."""
+    nd = mesh.nd
+    for lev in ("c", "p"):
+        vor = model.get(f"spe_vor_{lev}")
+        div = model.get(f"spe_div_{lev}")
+        vor[0, 1, :] += 2.0 * u0 / (mesh.radius * math.sqrt(3.0))  # 2 u0 sin(lat) / a = c P_1^0
+        vor[4, 5, :] += wave * (1.0 + 0.5j) * np.linspace(0.5, 1.5, nd)
+        vor[2, 7, :] += 0.5 * wave * np.linspace(1.5, 0.5, nd)
+        model.set(f"spe_vor_{lev}", vor)
+        u, v, gv = mesh.grid(nd), mesh.grid(nd), mesh.grid(nd)
+        backend.UV_Grid_From_Vor_Div(mesh, vor, div, u, v)
+        model.set(f"grid_u_{lev}", u)
+        model.set(f"grid_v_{lev}", v)
+        if lev == "c":
+            backend.Trans_Spherical_To_Grid(mesh, vor, gv)
+            model.set("grid_vor", gv)
+
+
 PROGNOSTIC = {
     "barotropic": ["spe_vor_c", "spe_vor_p", "grid_u_c", "grid_v_c", "grid_vor"],
     "shallow_water": ["spe_vor_c", "spe_div_c", "spe_lnps_c", "grid_u_c", "grid_v_c", "grid_ps_c", "grid_vor",

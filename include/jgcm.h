@@ -130,6 +130,9 @@ int jgcm_model_set_field(jgcm_model* model, const char* name, const double* host
  * captured CUDA graphs. */
 int jgcm_model_step(jgcm_model* model, int nsteps);
 int jgcm_model_init_step(jgcm_model* model, int* init_step);
+/* Update_Init_Step!  Time_Integrator.jl:40-43 / Semi_Implicit.jl:182-188: leave the forward
+ * init-step mode without stepping (e.g. when restarting from a saved leapfrog state). */
+int jgcm_model_update_init_step(jgcm_model* model);
 /* Spectral_Initialize_Fields!  Spectral_Dynamics.jl:372-449.  grid_t_pert (nullable,
  * grid[nd]) is added to the isothermal init_t before the spectral filtering;
  * vorticity_seed != 0 keeps the reference's deterministic vorticity seed (:401-409). */
@@ -141,6 +144,12 @@ int jgcm_model_semi_implicit(jgcm_model* model, const char* name, double* out, l
 int jgcm_model_time_steps(jgcm_model* model, int nsteps, float* ms);
 /* Number of kernel launches one steady-state step issues. */
 int jgcm_model_launches_per_step(jgcm_model* model, int* launches);
+/* Per-kernel CUDA-event times of nsteps steady steps (eager launches): ms[slot] is the mean
+ * device time of launch `slot` of a step; *count = launches per step.  Advances the model. */
+int jgcm_model_kernel_times(jgcm_model* model, int nsteps, float* ms, int cap, int* count);
+int jgcm_model_kernel_name(jgcm_model* model, int slot, char* buf, int cap);
+/* Select the CUDA device used by subsequently created meshes on this thread. */
+int jgcm_set_device(int device);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop

@@ -89,6 +89,7 @@ void om_model_destroy(om_model* md);
  * (doubles) or -1 */
 long om_model_field(om_model* md, const char* name, double* host, long cap, int set);
 int om_model_init_step(const om_model* md);
+int om_model_update_init_step(om_model* md);
 /* one Barotropic_Dynamics! / Shallow_Water_Physics!+Shallow_Water_Dynamics! /
  * Atmosphere_Update! followed by the driver's Update_Init_Step! after the first step */
 int om_model_step(om_model* md, int nsteps);

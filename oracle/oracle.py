@@ -70,6 +70,7 @@ def lib():
             "om_model_destroy": (None, [P]),
             "om_model_field": (L, [P, C.c_char_p, P, L, I]),
             "om_model_init_step": (I, [P]),
+            "om_model_update_init_step": (I, [P]),
             "om_model_step": (I, [P, I]),
             "om_spectral_initialize_fields": (I, [P, P, I]),
             "om_model_semi_implicit": (L, [P, C.c_char_p, P, L]),
@@ -273,6 +274,9 @@ class Model:
 
     def step(self, nsteps=1):
         lib().om_model_step(self._h, int(nsteps))
+
+    def update_init_step(self):
+        assert lib().om_model_update_init_step(self._h) == 0, "Update_Init_Step!: not in the init step"
 
     def spectral_initialize_fields(self, grid_t_pert=None, vorticity_seed=True):
         if grid_t_pert is not None:

@@ -20,10 +20,20 @@ def _pair(jg, orc, name, prec):
     return gm, om, jg.Model(gm, params), orc.Model(om, params)
 
 
+# divergence can be pure roundoff (a resting or non-divergent start), so its error is measured
+# against the scale of the companion vorticity field
+_SCALE = {"spe_div_c": "spe_vor_c", "spe_div_p": "spe_vor_p", "grid_div": "grid_vor"}
+
+
 def _compare(gmod, omod, kind, tol):
     errs = {}
     for f in configs.PROGNOSTIC[kind]:
-        errs[f] = configs.rel_l2(gmod.get(f), omod.get(f))
+        a, b = gmod.get(f), omod.get(f)
+        den = np.linalg.norm(b.ravel())
+        if f in _SCALE:
+            den = max(den, np.linalg.norm(omod.get(_SCALE[f]).ravel()))
+        errs[f] = float(np.linalg.norm((a - b).ravel()) / (den if den > 0 else 1.0))
+    print(kind, {k: f"{v:.2e}" for k, v in errs.items()})
     bad = {k: v for k, v in errs.items() if not v < tol}
     assert not bad, f"fields above {tol}: {bad}"
     return errs
@@ -78,18 +88,40 @@ def test_held_suarez_init_parity(jg, orc, name):
     _compare(gmod, omod, "held_suarez", 1e-12)
 
 
-@pytest.mark.parametrize("name,prec,tol", [("hs_t21l10", "fp64", 1e-10), ("hs_t42l20", "fp64", 1e-10),
-                                           ("hs_t42l20", "fp32", 5e-5)])
-def test_held_suarez_steps(jg, orc, name, prec, tol):
+def _hs_developed(jg, orc, name, prec):
     gm, om, gmod, omod = _pair(jg, orc, name, prec)
     omod.spectral_initialize_fields(configs.hs_temperature_noise(om), True)
+    configs.add_hs_flow(orc, om, omod)
     configs.copy_state(omod, gmod, "held_suarez")
+    return gm, om, gmod, omod
+
+
+@pytest.mark.parametrize("name,prec,tol", [("hs_t21l10", "fp64", 1e-10), ("hs_t42l20", "fp64", 1e-10),
+                                           ("hs_t21l10", "fp32", 2e-4), ("hs_t42l20", "fp32", 2e-4)])
+def test_held_suarez_steps(jg, orc, name, prec, tol):
+    """FP32 tolerance: the divergence tendency is the Laplacian of an energy field of ~1e5 m^2/s^2
+    whose dynamically active part is ~1e2, so FP32 storage bounds its relative accuracy near 1e-4."""
+    gm, om, gmod, omod = _hs_developed(jg, orc, name, prec)
     for n in (1, 1, 2):
         gmod.step(n)
         omod.step(n)
         _compare(gmod, omod, "held_suarez", tol)
     for f in ("grid_t_eq", "grid_p_full", "grid_p_half", "grid_z_full"):
         assert configs.rel_l2(gmod.get(f), omod.get(f)) < tol, f
+
+
+def test_held_suarez_restart_steady_step(jg, orc):
+    """A state saved after the init step continues identically once Update_Init_Step! is applied."""
+    gm, om, gmod, omod = _hs_developed(jg, orc, "hs_t42l20", "fp64")
+    omod.step(2)
+    configs.copy_state(omod, gmod, "held_suarez")
+    gmod.update_init_step()
+    assert not gmod.init_step
+    with pytest.raises(AssertionError):
+        gmod.update_init_step()
+    gmod.step(3)
+    omod.step(3)
+    _compare(gmod, omod, "held_suarez", 1e-11)
 
 
 def test_held_suarez_semi_implicit_matrices(jg, orc):

@@ -1,0 +1,224 @@
+"""The FP64 oracle against every known answer the reference's own tests hold (CPU only).
+
+The reference ships no fixtures: its checks are analytic (Gauss_And_Legendre.jl:120-169 test();
+Spectral_Spherical_Mesh.jl:763-1022 test_fourier, velocity_profile, test_derivative,
+test_advection).  Each is restated here with the tolerance the algorithm achieves, plus
+scipy's Gauss-Legendre nodes, numpy.fft for the FFT boundary (FFTW.jl, unpinned) and an
+independent numpy restatement of the transforms.
+"""
+import numpy as np
+import pytest
+from scipy.special import roots_legendre
+
+from jgcm import configs
+
+
+@pytest.mark.parametrize("nlat", [32, 64, 128])
+def test_gaussian_nodes(orc, nlat):
+    s, w = orc.compute_gaussian(nlat)
+    x, wx = roots_legendre(nlat)
+    assert np.all(np.diff(s) > 0)  # south -> north (Gauss_And_Legendre.jl:113)
+    assert np.max(np.abs(s - x)) < 5e-16
+    # the weight uses P'_n at the pre-update Newton iterate (Gauss_And_Legendre.jl:102-114), which
+    # costs ~n^2 * 1e-15 relative accuracy at the polar nodes
+    assert np.max(np.abs(w - wx) / wx) < 1e-14 * nlat ** 2
+    assert abs(w.sum() - 2.0) < 1e-14
+
+
+def test_legendre_closed_forms(orc):
+    """Gauss_And_Legendre.jl:132-156 (T21, nθ = 32): P and dP/dμ against closed forms."""
+    s, _ = orc.compute_gaussian(32)
+    q, dq = orc.compute_legendre(21, 22, s, 32)
+    c = np.sqrt(1 - s ** 2)
+    P = {(3, 3): np.sqrt(35) / 4 * c ** 3, (2, 3): np.sqrt(105 / 8) * (s - s ** 3),
+         (0, 2): np.sqrt(5) / 2 * (3 * s ** 2 - 1), (0, 3): np.sqrt(7) / 2 * (5 * s ** 3 - 3 * s),
+         (1, 3): np.sqrt(21) / 4 * (5 * s ** 2 - 1) * c}
+    dP = {(3, 3): np.sqrt(35) / 4 * c * 1.5 * (-2 * s), (2, 3): np.sqrt(105 / 8) * (1 - 3 * s ** 2),
+          (0, 2): np.sqrt(5) / 2 * 6 * s, (0, 3): np.sqrt(7) / 2 * (15 * s ** 2 - 3),
+          (1, 3): np.sqrt(21) / 4 * 10 * s * c + np.sqrt(21) / 4 * (5 * s ** 2 - 1) / c * 0.5 * (-2 * s)}
+    for (m, n), ref in P.items():
+        assert np.linalg.norm(q[m, n] - ref) < 1e-13, (m, n)
+    for (m, n), ref in dP.items():
+        # dP/dμ is recovered from (1-μ²) dP/dμ by a division by cos²: ~1e-12 near the poles
+        assert np.linalg.norm(dq[m, n] - ref) < 5e-12, (m, n)
+
+
+@pytest.mark.parametrize("N,nlat", [(21, 32), (42, 64)])
+def test_orthonormality(orc, N, nlat):
+    """Gauss_And_Legendre.jl:158-168 (with the abs the reference's @assert lacks)."""
+    s, w = orc.compute_gaussian(nlat)
+    q, _ = orc.compute_legendre(N, N + 1, s, nlat)
+    worst = 0.0
+    for m in range(N + 1):
+        G = 0.5 * np.einsum("aj,bj,j->ab", q[m, m:], q[m, m:], w)
+        worst = max(worst, np.max(np.abs(G - np.eye(G.shape[0]))))
+    assert worst < 1e-12
+
+
+def test_fft_boundary(orc):
+    M = orc.Spectral_Spherical_Mesh(31, 32, 48, 96, 2, 1.0)
+    g = np.asfortranarray(np.random.default_rng(0).random((96, 48, 2)))
+    f = np.zeros((96, 48, 2), dtype=np.complex128, order="F")
+    orc.Trans_Grid_To_Fourier(M, g, f)
+    assert np.max(np.abs(f - np.fft.fft(g, axis=0) / 96)) < 1e-15
+
+
+def test_round_trip_idempotence(orc):
+    """test_fourier (Spectral_Spherical_Mesh.jl:763-787): G2S∘S2G is a projection."""
+    M = orc.Spectral_Spherical_Mesh(31, 32, 48, 96, 2, 1.0)
+    p0 = np.asfortranarray(np.random.default_rng(1).random((96, 48, 2)))
+    s0, s1, p1, p2 = M.spectral(2), M.spectral(2), M.grid(2), M.grid(2)
+    orc.Trans_Grid_To_Spherical(M, p0, s0)
+    orc.Trans_Spherical_To_Grid(M, s0, p1)
+    orc.Trans_Grid_To_Spherical(M, p1, s1)
+    orc.Trans_Spherical_To_Grid(M, s1, p2)
+    assert np.linalg.norm(s0 - s1) < 1e-13
+    assert np.linalg.norm(p1 - p2) < 1e-11
+    assert np.all(s0[:, 32, :] == 0)
+
+
+def _velocity_profile(M, IC):
+    """velocity_profile (Spectral_Spherical_Mesh.jl:804-910) at T85, nθ = 128, nd = 3, radius 5."""
+    nlon, nlat, nd, a = M.nlon, M.nlat, M.nd, M.radius
+    c, s, lam = M.costh, M.sinth, M.lonc
+    u, v, vor, div = (np.zeros((nlon, nlat, nd), order="F") for _ in range(4))
+    U, b = 2 * np.pi / 256.0, np.pi / 2.0
+    for k in range(nd):
+        ic = IC if IC != "mix" else ["rigid_rotation", "random_1", "random_2"][k]
+        if ic == "rigid_rotation":
+            u[:, :, k] = U * (np.cos(b) * c[None, :] + np.sin(b) * np.cos(lam)[:, None] * s[None, :])
+            v[:, :, k] = -U * np.sin(b) * np.sin(lam)[:, None] * np.ones(nlat)[None, :]
+            vor[:, :, k] = 2 * U / a * (np.cos(b) * s[None, :] - np.sin(b) * np.cos(lam)[:, None] * c[None, :])
+        elif ic == "random_1":
+            u[:, :, k] = (c ** 2)[None, :]
+            vor[:, :, k] = (3 * s * c / a)[None, :]
+        else:
+            u[:, :, k] = (25 * c - 30 * c ** 3 + 300 * s ** 2 * c ** 6)[None, :]
+            vor[:, :, k] = (-(-50 * s + 120 * c ** 2 * s + 300 * (2 * c ** 7 * s - 7 * c ** 5 * s ** 3)) / a)[None, :]
+    return u, v, vor, div
+
+
+# truncation error of each analytic field (cos θ is poorly represented on the harmonics)
+_DERIV_TOL = {"rigid_rotation": 1e-10, "random_1": 1e-3, "random_2": 1e-6, "mix": 1e-4}
+
+
+@pytest.fixture(scope="module")
+def t85(orc):
+    return orc.Spectral_Spherical_Mesh(85, 86, 128, 256, 3, 5.0)
+
+
+@pytest.mark.parametrize("IC", ["rigid_rotation", "random_1", "random_2", "mix"])
+def test_derivative(orc, t85, IC):
+    """test_derivative (Spectral_Spherical_Mesh.jl:916-943)."""
+    M = t85
+    u, v, vor0, div0 = _velocity_profile(M, IC)
+    sv, sd = M.spectral(3), M.spectral(3)
+    orc.Vor_Div_From_Grid_UV(M, u, v, sv, sd)
+    gd, gv = M.grid(3), M.grid(3)
+    orc.Trans_Spherical_To_Grid(M, sd, gd)
+    orc.Trans_Spherical_To_Grid(M, sv, gv)
+    assert np.linalg.norm(gd - div0) < 1e-10
+    assert np.linalg.norm(gv - vor0) / np.linalg.norm(vor0) < _DERIV_TOL[IC]
+    u1, v1 = M.grid(3), M.grid(3)
+    orc.UV_Grid_From_Vor_Div(M, sv, sd, u1, v1)
+    assert np.linalg.norm(u1 - u) / np.linalg.norm(u) < _DERIV_TOL[IC]
+    assert np.linalg.norm(v1 - v) < 1e-10 + _DERIV_TOL[IC] * np.linalg.norm(v)
+
+
+@pytest.mark.parametrize("IC,tol", [("rigid_rotation", 5e-2), ("random_1", 1e-9), ("random_2", 1e-8),
+                                    ("mix", 1e-4)])
+def test_advection(orc, t85, IC, tol):
+    """test_advection (Spectral_Spherical_Mesh.jl:945-1008): -v·∇h against the analytic gradient.
+    h contains 25 cos θ, which is not band-limited; where v is non-zero at the poles (rigid
+    rotation about an equatorial axis) its truncated gradient leaves a ~2% error."""
+    M = t85
+    u, v, _, _ = _velocity_profile(M, IC)
+    c, s, lam, a = M.costh, M.sinth, M.lonc, M.radius
+    C, S, L = c[None, :], s[None, :], lam[:, None]
+    h = 25 * C - 30 * C ** 3 + 300 * S ** 2 * C ** 6 * np.sin(L)
+    gl = 300 * S ** 2 * C ** 5 * np.cos(L) / a
+    gt = (-25 * S + 90 * C ** 2 * S + 600 * S * C ** 7 * np.sin(L) - 1800 * S ** 3 * C ** 5 * np.sin(L)) / a
+    hs = np.asfortranarray(np.repeat(h[:, :, None], 3, axis=2))
+    sh = M.spectral(3)
+    orc.Trans_Grid_To_Spherical(M, hs, sh)
+    dh = M.grid(3)
+    orc.Add_Horizontal_Advection(M, sh, u, v, dh)
+    ref = -(gl[:, :, None] * u + gt[:, :, None] * v)
+    assert np.linalg.norm(dh - ref) / np.linalg.norm(ref) < tol
+
+
+def _numpy_transforms(M):
+    """Independent numpy restatement (direct sums over all latitudes, numpy.fft)."""
+    N, nlat, nlon = M.num_fourier, M.nlat, M.nlon
+    q, w = M.qnm, M.wts
+
+    def s2g(snm):
+        g = np.einsum("mnj,mnk->mjk", np.where(np.arange(N + 2)[None, :] >= np.arange(N + 1)[:, None], 1.0, 0.0)[
+            :, :, None] * q, snm)
+        full = np.zeros((nlon, nlat, snm.shape[2]), dtype=complex)
+        full[: N + 1] = g
+        full[0] = full[0].real
+        out = np.real(full[0])[None] + 2 * np.real(np.fft.ifft(np.concatenate([0 * full[:1], full[1:]]), axis=0) * nlon)
+        return out
+
+    def g2s(grid):
+        f = np.fft.fft(grid, axis=0) / nlon
+        s = 0.5 * np.einsum("mnj,mjk->mnk", q * w[None, None, :], f[: N + 1])
+        mask = np.arange(N + 2)[None, :] >= np.arange(N + 1)[:, None]
+        s = s * mask[:, :, None]
+        s[:, N + 1, :] = 0
+        return s
+
+    return s2g, g2s
+
+
+@pytest.mark.parametrize("N,nlat,nlon", [(10, 16, 32), (21, 32, 64)])
+def test_numpy_restatement(orc, N, nlat, nlon):
+    M = orc.Spectral_Spherical_Mesh(N, N + 1, nlat, nlon, 2, 6371.0e3)
+    s2g, g2s = _numpy_transforms(M)
+    rng = np.random.default_rng(3)
+    g = np.asfortranarray(rng.standard_normal((nlon, nlat, 2)))
+    s = M.spectral(2)
+    orc.Trans_Grid_To_Spherical(M, g, s)
+    assert configs.rel_l2(s, g2s(g)) < 1e-13
+    sn = np.asfortranarray(rng.standard_normal((N + 1, N + 2, 2)) + 1j * rng.standard_normal((N + 1, N + 2, 2)))
+    for m in range(N + 1):
+        sn[m, :m] = 0
+    out = M.grid(2)
+    orc.Trans_Spherical_To_Grid(M, sn, out)
+    assert configs.rel_l2(out, s2g(sn)) < 1e-13
+
+
+def test_hs_mass_fixer_and_step_finite(orc):
+    """Compute_Corrections! keeps the area-mean surface pressure of the previous level."""
+    name = "hs_t21l10"
+    M = configs.make_mesh(orc, name)
+    md = orc.Model(M, configs.PARAMS[name])
+    md.spectral_initialize_fields(configs.hs_temperature_noise(M), True)
+    ps0 = orc.Area_Weighted_Global_Mean(M, md.get("grid_ps_c"))
+    md.step(6)
+    assert not md.init_step
+    ps1 = orc.Area_Weighted_Global_Mean(M, md.get("grid_ps_c"))
+    assert abs(ps1 - ps0) / ps0 < 1e-13
+    assert np.isfinite(md.get("grid_t_c")).all()
+
+
+def test_barotropic_rh4_is_steady_pattern(orc):
+    """The Rossby-Haurwitz wave 4 keeps its shape (it is an exact solution of the barotropic
+    vorticity equation; damping and noise perturb it only slightly over 2 days)."""
+    name = "barotropic_t42"
+    M = configs.make_mesh(orc, name)
+    md = orc.Model(M, configs.PARAMS[name])
+    spe0 = configs.init_barotropic_rh4(orc, M, md)
+    md.step(96)
+    amp0 = np.abs(spe0[4, 5, 0])
+    amp1 = np.abs(md.get("spe_vor_c")[4, 5, 0])
+    assert abs(amp1 - amp0) / amp0 < 0.02
+
+
+def test_generator_is_reproducible():
+    a = configs.normal(configs.BASE_SEED, 1001)
+    b = configs.normal(configs.BASE_SEED, 1001)
+    assert np.array_equal(a, b)
+    assert abs(a.mean()) < 0.1 and abs(a.std() - 1) < 0.1
+    assert configs.splitmix64(0, 1)[0] == np.uint64(0xE220A8397B1DCDAF)  # published SplitMix64(0) output
