@@ -174,6 +174,7 @@ struct jgcm_mesh {
   double* d_red;      // reduction scratch (FP64)
   unsigned int* d_counter;
   int refs;           // 1 for the caller's handle + 1 per live model built on the mesh
+  int device;         // CUDA device the mesh lives on
   std::string name;
 };
 

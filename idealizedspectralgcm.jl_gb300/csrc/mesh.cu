@@ -330,6 +330,7 @@ extern "C" int jgcm_mesh_create(int num_fourier, int num_spherical, int nlat, in
   MCHK(cuda(cudaMalloc(&m->d_ref2, T3 * 8), "alloc ref2"));
 #undef MCHK
   m->refs = 1;
+  cudaGetDevice(&m->device);
   *out = m;
   return JGCM_OK;
 }

@@ -17,6 +17,7 @@
 // Spectral prologues build the inputs of the synthesis on the fly from neighbouring total
 // wavenumbers (gradient, Compute_Gradient_Cos! :655-692; ucos/vcos, :517-580).
 #include <cmath>
+#include <mutex>
 
 #include "jgcm_internal.cuh"
 
@@ -531,25 +532,32 @@ static inline int s2g_ct(int nh) { return nh >= 256 ? 1 : 256 / nh; }
 static inline int fft_ct(int nlon) { return nlon >= 1024 ? 1 : 1024 / nlon; }
 static inline int g2s_ct(int nh) { return nh >= 64 ? 4 : nh >= 32 ? 8 : 16; }
 
+// Legendre synthesis then inverse FFT, with the Fourier coefficients staged in `fbuf`
+// ((N+1) x nlat x C complex T).
 template <typename T>
-int launch_s2g(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, cudaStream_t st) {
+static int launch_s2g_into(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, cudaStream_t st, V2<T>* fbuf) {
   using V = V2<T>;
   JG_TRY(configure_smem<T>());
-  JG_ARG(sp.C == ip.C && sp.C <= m->Cmax && sp.C > 0, "bad S2G plan");
   Tables<T> tb = tables<T>(m);
   const int nh = m->nh, ct = s2g_ct(nh);
   size_t sm1 = align16((size_t)(m->ns + 1) * nh * sizeof(T)) + (size_t)(m->ns + 1) * ct * sizeof(V);
   dim3 g1((sp.C + ct - 1) / ct, m->N + 1);
-  k_s2g_legendre<T><<<g1, 256, sm1, st>>>(sp, tb, (V*)m->d_fbuf, m->ns, m->nlat, ct);
+  k_s2g_legendre<T><<<g1, 256, sm1, st>>>(sp, tb, fbuf, m->ns, m->nlat, ct);
   mark(st);
   JG_CUDA(cudaGetLastError());
   const int fc = fft_ct(m->nlon);
   size_t sm2 = align16((size_t)(fc * m->nlon + m->nlon) * sizeof(T)) + (size_t)(m->N + 1) * fc * sizeof(V);
   dim3 g2((ip.C + fc - 1) / fc, m->nlat);
-  k_ifft<T><<<g2, 256, sm2, st>>>(ip, tb, (const V*)m->d_fbuf, m->N, m->nlat, m->nlon, m->logn - 1, fc);
+  k_ifft<T><<<g2, 256, sm2, st>>>(ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon, m->logn - 1, fc);
   mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;
+}
+
+template <typename T>
+int launch_s2g(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, cudaStream_t st) {
+  JG_ARG(sp.C == ip.C && sp.C <= m->Cmax && sp.C > 0, "bad S2G plan");
+  return launch_s2g_into<T>(m, sp, ip, st, (V2<T>*)m->d_fbuf);
 }
 
 template <typename T>
@@ -733,3 +741,76 @@ int area_mean(jgcm_mesh* m, const void* d_grid, double* d_out, cudaStream_t st) 
 }
 
 }  // namespace jgcm
+
+// ------------------------------------------------------------------------------------------
+// Allocation-free spectral -> grid transform (jgcm_trans_spherical_to_grid_noalloc).
+//
+// Some callers cannot allocate device memory at the point where they transform: code that runs
+// while a stream is being captured into a CUDA graph, hosts whose device memory is owned by their
+// own pool allocator (so a stray cudaMalloc would break their accounting or fail under a memory
+// cap), and real-time loops that forbid allocation after start-up.  This variant of
+// Trans_Spherical_To_Grid! works on device buffers the caller already owns and stages its Fourier
+// coefficients in a fixed-size scratch array that is part of the library image instead of in
+// memory obtained at run time.  The array lives on every GPU that loads the library until the
+// process exits; every call on a device shares it.
+namespace {
+constexpr size_t kNoAllocScratchBytes = 8u << 20;  // 8 MiB
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+void* g_noalloc_addr[64];  // device address of g_noalloc_scratch, per CUDA device
+std::mutex g_noalloc_mu;
+
+// Once per device, with that device current: resolve the device address of the scratch array
+// (the host-side name is only a stand-in for it).
+int noalloc_scratch_address(int dev, void** out) {
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      jgcm::set_error("cudaGetSymbolAddress(g_noalloc_scratch) failed on device %d: %s", dev,
+                      cudaGetErrorString(e));
+      return JGCM_E_CUDA;
+    }
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return JGCM_OK;
+}
+}  // namespace
+
+extern "C" int jgcm_trans_spherical_to_grid_noalloc(jgcm_mesh* m, const void* d_snm, int nlev, void* d_grid,
+                                                    void* stream) {
+  using namespace jgcm;
+  JG_ARG(m != nullptr && d_snm != nullptr && d_grid != nullptr, "NULL argument");
+  JG_ARG(nlev == m->nd || nlev == 1, "third dimension must be nd=%d or 1 (got %d)", m->nd, nlev);
+  const size_t need = (size_t)(m->N + 1) * m->nlat * nlev * 2 * tsize(m);
+  JG_ARG(need <= kNoAllocScratchBytes,
+         "jgcm_trans_spherical_to_grid_noalloc: needs %zu bytes of scratch for (N+1)=%d x nlat=%d x nlev=%d, the "
+         "static scratch holds %zu bytes",
+         need, m->N + 1, m->nlat, nlev, kNoAllocScratchBytes);
+  int dev = -1;
+  JG_CUDA(cudaGetDevice(&dev));
+  JG_ARG(dev == m->device, "the mesh lives on device %d but device %d is current", m->device, dev);
+  JG_ARG(dev >= 0 && dev < 64, "device index %d out of range", dev);
+  void* scratch = nullptr;
+  JG_TRY(noalloc_scratch_address(dev, &scratch));
+  cudaStream_t st = stream ? (cudaStream_t)stream : m->stream;
+  S2GPlan sp;
+  memset(&sp, 0, sizeof(sp));
+  sp.ng = 1;
+  sp.C = nlev;
+  sp.g[0].op = S2G_PLAIN;
+  sp.g[0].a = d_snm;
+  sp.g[0].L = nlev;
+  IFFTPlan ip;
+  memset(&ip, 0, sizeof(ip));
+  ip.ng = 1;
+  ip.C = nlev;
+  ip.g[0].epi = EPI_NONE;
+  ip.g[0].dst = d_grid;
+  ip.g[0].L = nlev;
+  // The synthesis writes every scratch element (all m <= N, all latitudes, all columns) before
+  // the inverse FFT reads it, so nothing left by an earlier call needs clearing.
+  return is_fp64(m) ? launch_s2g_into<double>(m, sp, ip, st, (double2*)scratch)
+                    : launch_s2g_into<float>(m, sp, ip, st, (float2*)scratch);
+}

@@ -93,6 +93,23 @@ int jgcm_apply_laplacian(jgcm_mesh* mesh, double* spe, int nlev);
 /* Area_Weighted_Global_Mean  Spectral_Spherical_Mesh.jl:746-760 (level 1; FP64 sum) */
 int jgcm_area_weighted_global_mean(jgcm_mesh* mesh, const double* grid, double* out);
 
+/* Spectral -> grid transform that allocates nothing.  No counterpart in the reference: it is an
+ * addition for callers that cannot allocate device memory where they transform -- code running
+ * while a stream is captured into a CUDA graph, hosts whose device memory belongs to their own
+ * pool allocator, and loops that forbid allocation after start-up.
+ *   d_snm   device array, mesh precision, library layout: complex [m][n][k] (N+1 x N+2 x nlev,
+ *           levels innermost; entries n < m are ignored)
+ *   d_grid  device array, mesh precision: [k][nlat][nlon]
+ *   stream  cudaStream_t to run on, or NULL for the mesh's stream; the call is asynchronous.
+ * Same result as jgcm_trans_spherical_to_grid.  The Fourier coefficients are staged in a static
+ * 8 MiB device array owned by the library (every GPU that loads it holds it until exit), so
+ * (N+1) * nlat * nlev complex values must fit: larger sizes return JGCM_E_ARG with a message.
+ * The first call on a device resolves that array's address (set-up), so make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU (different streams,
+ * meshes or threads without ordering) race; nothing in it needs clearing between calls. */
+int jgcm_trans_spherical_to_grid_noalloc(jgcm_mesh* mesh, const void* d_snm, int nlev, void* d_grid,
+                                         void* stream);
+
 /* ---- models: Dyn_Data + Filtered_Leapfrog (+ Semi_Implicit_Solver) kept on the device ---- */
 #define JGCM_BAROTROPIC 0     /* Barotropic_Dynamics!  Barotropic_Dynamics.jl:2-46 */
 #define JGCM_SHALLOW_WATER 1  /* Shallow_Water_Physics! + Shallow_Water_Dynamics!

@@ -1,0 +1,107 @@
+"""The allocation-free spectral -> grid entry point (jgcm_trans_spherical_to_grid_noalloc).
+
+It serves callers that cannot allocate device memory where they transform (stream capture,
+hosts with their own device pool, no-allocation-after-start-up loops).  The test owns its device
+buffers (allocated here through the same CUDA runtime the library links), calls the entry point
+through the C ABI twice in a row, and checks each result against the allocating entry point
+jgcm_trans_spherical_to_grid with the tolerances of the transform tests (FP64 1e-12, FP32 5e-6).
+This file is named to be collected last.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from jgcm import configs
+
+pytestmark = pytest.mark.gpu
+
+_rt = None
+
+
+def cudart():
+    global _rt
+    if _rt is None:
+        _rt = C.CDLL("libcudart.so.13")
+        _rt.cudaMalloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
+        _rt.cudaFree.argtypes = [C.c_void_p]
+        _rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+        _rt.cudaMemset.argtypes = [C.c_void_p, C.c_int, C.c_size_t]
+    return _rt
+
+
+H2D, D2H = 1, 2
+
+
+class DeviceBuffer:
+    def __init__(self, nbytes):
+        self.nbytes = nbytes
+        self.ptr = C.c_void_p()
+        assert cudart().cudaMalloc(C.byref(self.ptr), nbytes) == 0
+
+    def upload(self, a):
+        a = np.ascontiguousarray(a)
+        assert a.nbytes == self.nbytes
+        assert cudart().cudaMemcpy(self.ptr, a.ctypes.data_as(C.c_void_p), a.nbytes, H2D) == 0
+
+    def download(self, shape, dtype):
+        out = np.empty(shape, dtype=dtype)
+        assert cudart().cudaMemcpy(out.ctypes.data_as(C.c_void_p), self.ptr, out.nbytes, D2H) == 0
+        return out
+
+    def poison(self):
+        assert cudart().cudaMemset(self.ptr, 0xFF, self.nbytes) == 0  # NaN pattern
+
+    def free(self):
+        cudart().cudaFree(self.ptr)
+
+
+def _entry(jg):
+    f = jg.lib().jgcm_trans_spherical_to_grid_noalloc
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    f.restype = C.c_int
+    return f
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp32", 5e-6)])
+def test_noalloc_matches_allocating_entry_point(jg, prec, tol):
+    N, nlat, nlon, nd = 42, 64, 128, 20
+    mesh = jg.Spectral_Spherical_Mesh(N, N + 1, nlat, nlon, nd, 6371.0e3, precision=prec)
+    rng = np.random.default_rng(7)
+    s = (rng.standard_normal((N + 1, N + 2, nd)) + 1j * rng.standard_normal((N + 1, N + 2, nd)))
+    s /= (1.0 + np.arange(N + 2))[None, :, None] ** 1.5
+    for m in range(N + 1):
+        s[m, :m, :] = 0
+    s = np.asfortranarray(s)
+    ref = mesh.grid(nd)
+    jg.Trans_Spherical_To_Grid(mesh, s, ref)  # the allocating entry point
+    cdt, rdt = (np.complex128, np.float64) if prec == "fp64" else (np.complex64, np.float32)
+    # library device layout: spectral [m][n][k] (C order of the [m, n, k] array), grid [k][j][i]
+    d_s = DeviceBuffer(s.size * np.dtype(cdt).itemsize)
+    d_g = DeviceBuffer(nlon * nlat * nd * np.dtype(rdt).itemsize)
+    try:
+        d_s.upload(np.ascontiguousarray(s).astype(cdt))
+        f = _entry(jg)
+        for _ in range(2):  # the shared scratch keeps the previous call's contents
+            d_g.poison()
+            assert f(mesh._h, d_s.ptr, nd, d_g.ptr, None) == 0, jg.lib().jgcm_last_error()
+            jg.lib().jgcm_mesh_synchronize(mesh._h)
+            out = d_g.download((nd, nlat, nlon), rdt).astype(np.float64).transpose(2, 1, 0)
+            assert np.isfinite(out).all()
+            assert configs.rel_l2(out, ref) < tol
+    finally:
+        d_s.free()
+        d_g.free()
+
+
+def test_noalloc_rejects_sizes_beyond_its_scratch(jg):
+    N, nlat, nlon, nd = 85, 128, 256, 64  # 86 * 128 * 64 complex doubles = 11.3 MB > 8 MiB
+    mesh = jg.Spectral_Spherical_Mesh(N, N + 1, nlat, nlon, nd, 6371.0e3, precision="fp64")
+    f = _entry(jg)
+    d = DeviceBuffer(16)
+    try:
+        st = f(mesh._h, d.ptr, nd, d.ptr, None)
+        assert st == -1
+        assert b"static scratch holds" in jg.lib().jgcm_last_error()
+    finally:
+        d.free()
