@@ -21,6 +21,23 @@
 
 namespace jgcm {
 
+// Dynamic shared memory the transform kernels may use per block (the SM allows 227 KB).
+constexpr size_t kSmemBudget = 200 * 1024;
+
+// Largest dynamic shared memory the unconditional parts of the transform kernels need for a mesh
+// whose tables hold `ts`-byte reals: the synthesis stages all P rows of one m plus one spectral
+// column tile, the analysis four Fourier slots per hemisphere pair, the FFTs one line per column.
+inline size_t transform_smem_need(int N, int ns, int nlat, int nlon, size_t ts) {
+  const size_t nh = (size_t)nlat / 2;
+  const size_t s2g_ct = nh >= 256 ? 1 : 256 / nh, g2s_ct = nh >= 64 ? 4 : nh >= 32 ? 8 : 16;
+  const size_t fft_ct = nlon >= 1024 ? 1 : 1024 / nlon;
+  size_t s2g = (((size_t)(ns + 1) * nh * ts + 15) & ~(size_t)15) + (size_t)(ns + 1) * s2g_ct * 2 * ts;
+  size_t g2s = 8 * g2s_ct * nh * 2 * ts;
+  size_t fft = (((fft_ct * nlon + nlon) * ts + 15) & ~(size_t)15) + (size_t)(N + 1) * fft_ct * 2 * ts;
+  size_t r = s2g > g2s ? s2g : g2s;
+  return r > fft ? r : fft;
+}
+
 void set_error(const char* fmt, ...);
 
 #define JG_CUDA(expr)                                                                         \

@@ -272,6 +272,12 @@ extern "C" int jgcm_mesh_create(int num_fourier, int num_spherical, int nlat, in
   JG_ARG(nd >= 1 && nd <= JGCM_MAX_ND, "nd must be in [1, %d]", JGCM_MAX_ND);
   JG_ARG(radius > 0, "radius must be positive");
   JG_ARG(precision >= JGCM_FP64 && precision <= JGCM_BF16X3, "unknown precision mode");
+  {
+    const size_t need = transform_smem_need(num_fourier, num_spherical, nlat, nlon,
+                                            precision == JGCM_FP64 ? sizeof(double) : sizeof(float));
+    JG_ARG(need <= kSmemBudget, "mesh too large for the shared-memory tiling: %zu bytes > %zu per block", need,
+           kSmemBudget);
+  }
   jgcm_mesh* m = new jgcm_mesh();  // value-initialised: all pointers start NULL
   m->N = num_fourier;
   m->ns = num_spherical;

@@ -13,6 +13,7 @@
 // fixers (Spectral_Dynamics.jl:5-68) use deterministic FP64 reductions.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -31,6 +32,15 @@ struct VertCoef {  // Vert_Coordinate (even_sigma) and the semi-implicit referen
   double ak[JGCM_MAX_ND + 1], bk[JGCM_MAX_ND + 1], dak[JGCM_MAX_ND], dbk[JGCM_MAX_ND];
   double dp_ref[JGCM_MAX_ND], rdp_ref[JGCM_MAX_ND], lnph_ref[JGCM_MAX_ND + 1], lnpf_ref[JGCM_MAX_ND],
       t_ref[JGCM_MAX_ND], h[JGCM_MAX_ND];
+  // sigma coordinates (a_k = 0): with p = b ps, ln p_{k+1/2} = lb[k+1] + ln ps and
+  // ln p_k = cf[k] + ln ps (Simmons-Burridge, Press_And_Geopot.jl:46-60, zero top), so every
+  // log-pressure difference is a per-level constant and p_k = sf[k] ps
+  double lb[JGCM_MAX_ND + 1];  // ln b_k (k >= 1)
+  double cf[JGCM_MAX_ND];      // ln p_k - ln ps
+  double sf[JGCM_MAX_ND];      // exp(cf) = p_k / ps
+  double dlp_p[JGCM_MAX_ND];   // ln p_{k+1/2} - ln p_k
+  double dlp_m[JGCM_MAX_ND];   // ln p_k - ln p_{k-1/2}   (k >= 1)
+  double dlp[JGCM_MAX_ND];     // ln p_{k+1/2} - ln p_{k-1/2}   (k >= 1)
 };
 }  // namespace
 
@@ -51,6 +61,7 @@ struct jgcm_model {
   void* dfac[2];             // [m][n] in T: 1/(1 + Δt d) (init step), 1/(1 + 2Δt d) (afterwards)
   // FP64 semi-implicit data
   VertCoef vc;
+  VertCoef* d_vc;  // device copy read by the column and semi-implicit kernels
   double* div_mat;  // host nd*nd column-major
   double* d_W;      // device [2][N+1][nd][nd] (transposed: [c][r])
   int2* d_pairs;    // (m, n) pairs with n >= m
@@ -83,6 +94,12 @@ __device__ __forceinline__ R rscan_incl(R x, int lane) {
     R y = __shfl_down_sync(FULL, x, o);
     if (lane + o < 32) x += y;
   }
+  return x;
+}
+template <typename R>
+__device__ __forceinline__ R warp_sum_t(R x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
   return x;
 }
 __device__ __forceinline__ double warp_sum(double x) {
@@ -129,6 +146,7 @@ __device__ bool grid_reduce_last(const double* vals, double* partials, unsigned*
     for (int jj = threadIdx.x; jj < (int)gridDim.y; jj += nt) {
       for (int v = 0; v < NV; v++) {
         double r = 0.0;
+#pragma unroll 8
         for (int b = 0; b < (int)gridDim.x; b++) r += __ldcg(partials + (size_t)v * nb + (size_t)jj * gridDim.x + b);
         s[v] += r * wts[jj];
       }
@@ -149,7 +167,15 @@ __device__ bool grid_reduce_last(const double* vals, double* partials, unsigned*
 // ------------------------------------------------------------------------------------------
 // Held-Suarez: physics (HS_Forcing!, previous time level) + corrections-init sums +
 // Four_In_One! + Compute_Geopotential! + Vert_Advection! x3 + horizontal advection of T +
-// absolute-vorticity fluxes + energy, fused.  One warp per grid column, lane = level.
+// absolute-vorticity fluxes + energy, fused.  A block owns a tile of HS_CW consecutive columns of
+// one latitude row: every input's nd x HS_CW tile is staged in shared memory with coalesced row
+// loads, one warp per column computes with lane = level (scans by shuffles), and the outputs go
+// back through the same tile as coalesced rows.  Sigma coordinates: one log per column, one exp
+// per level (ln p = const_k + ln ps).
+constexpr int HS_CW = 8;           // columns per block (one per warp)
+constexpr int HS_CWP = HS_CW + 1;  // tile pitch: lane-per-level reads fall in distinct banks
+constexpr int HS_NIN = 10;         // staged nd-level inputs
+
 template <typename T>
 struct HSColArgs {
   const T *u_p, *v_p, *t_p, *ps_p, *ps_c, *u_c, *v_c, *t_c, *div, *vor, *dlps, *dtps, *dlT, *dtT, *geopots, *coriolis,
@@ -163,130 +189,157 @@ struct HSColArgs {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_hs_column(HSColArgs<T> a, VertCoef vc) {
+__global__ void __launch_bounds__(256) k_hs_column(HSColArgs<T> a, const VertCoef* __restrict__ vcp) {
+  const VertCoef& vc = *vcp;  // device memory: lanes read consecutive levels
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ double red[2][8];
+  const int nd = a.nd, nlon = a.nlon, nlat = a.nlat;
+  T* tile = (T*)smem;                        // [HS_NIN][nd][HS_CWP]
+  T* sgl = tile + HS_NIN * nd * HS_CWP;      // [5][HS_CW]: ps_c, ps_p, dlps, dtps, geopots
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int i = blockIdx.x * 8 + w, j = blockIdx.y;
-  const int nd = a.nd, nlon = a.nlon;
-  const bool act = lane < nd && i < nlon;
-  const int k = act ? lane : 0;
-  const size_t col = (size_t)j * nlon + (i < nlon ? i : 0);
-  const size_t x = (size_t)k * a.nlat * nlon + col;
+  const int i0 = blockIdx.x * HS_CW, j = blockIdx.y;
+  const size_t G = (size_t)nlat * nlon, row = (size_t)j * nlon;
+  {
+    const T* in[HS_NIN] = {a.u_p, a.v_p, a.t_p, a.u_c, a.v_c, a.t_c, a.div, a.vor, a.dlT, a.dtT};
+    // all HS_NIN loads of one (level, column) are issued back to back before any store
+    for (int r = threadIdx.x; r < nd * HS_CW; r += blockDim.x) {
+      const int k = r / HS_CW, c = r - k * HS_CW, i = i0 + c;
+      const bool ok = i < nlon;
+      const size_t off = k * G + row + i;
+      T x[HS_NIN];
+#pragma unroll
+      for (int f = 0; f < HS_NIN; f++) x[f] = ok ? in[f][off] : (T)0;
+#pragma unroll
+      for (int f = 0; f < HS_NIN; f++) tile[(f * nd + k) * HS_CWP + c] = x[f];
+    }
+    const T* sg[5] = {a.ps_c, a.ps_p, a.dlps, a.dtps, a.geopots};
+    for (int q = threadIdx.x; q < 5 * HS_CW; q += blockDim.x) {
+      int f = q / HS_CW, c = q - f * HS_CW, i = i0 + c;
+      sgl[q] = (i < nlon) ? sg[f][row + i] : (f < 2 ? (T)1 : (T)0);
+    }
+  }
+  __syncthreads();
   const T day = (T)86400;
-  // ---- pressure variables from ps_c (Pressure_Variables!, Press_And_Geopot.jl:36-67)
-  const T ps = a.ps_c[col];
-  const T ph0 = (T)vc.ak[k] + (T)vc.bk[k] * ps, ph1 = (T)vc.ak[k + 1] + (T)vc.bk[k + 1] * ps;
-  const T dp = ph1 - ph0;
-  const T rdp = (T)1 / dp;
-  const T lnph1 = log(ph1);
-  const T lnph0 = (k == 0) ? (T)0 : log(ph0);
-  const T lnpf = (k == 0) ? lnph1 - (T)1.0 : lnph1 + ph0 * (lnph1 - lnph0) * rdp - (T)1.0;
-  const T pfull = exp(lnpf);
-  const T psurf = (T)vc.ak[nd] + (T)vc.bk[nd] * ps;
-  // ---- HS_Forcing! on the previous level
+  const T sj = a.sinj[j], s2 = sj * sj, c2 = (T)1.0 - s2, c4 = c2 * c2, cj = a.cosj[j], fj = a.coriolis[j];
+  const T sb = (T)a.sigma_b, R = (T)a.rdgas, kap = (T)a.rdgas / (T)a.cp, cp = (T)a.cp;
+  const T kv0 = ((T)a.k_f / day) / ((T)1.0 - sb);
+  const T ka = (T)a.k_a / day, ks = (T)a.k_s / day, kt0 = (ks - ka) / ((T)1.0 - sb);
+  const T ln_pref = (T)11.512925464970229;  // ln 1e5 (HS_Forcing.jl:49 p_ref)
   const int Dt = a.Dt;
-  T up = 0, vp = 0, tp = 0;
-  if (act) {
-    up = a.u_p[x];
-    vp = a.v_p[x];
-    tp = a.t_p[x];
+  double accp = 0.0, acce = 0.0;
+  for (int c = w; c < HS_CW; c += 8) {
+    const bool colok = i0 + c < nlon;
+    const bool act = lane < nd && colok;
+    const int k = lane < nd ? lane : 0;
+    auto at = [&](int f) -> T { return act ? tile[(f * nd + k) * HS_CWP + c] : (T)0; };
+    const T up = at(0), vp = at(1), tp = at(2), u = at(3), v = at(4), t = at(5), dvg = at(6), vor = at(7),
+            dlT = at(8), dtT = at(9);
+    const T ps = sgl[c], psp = sgl[HS_CW + c], dlps = sgl[2 * HS_CW + c], dtps = sgl[3 * HS_CW + c],
+            gs = sgl[4 * HS_CW + c];
+    // ---- pressure variables from ps_c (Pressure_Variables!, Press_And_Geopot.jl:36-67)
+    const T lnps = log(ps);
+    const T dp = (T)vc.dak[k] + (T)vc.dbk[k] * ps;
+    const T rdp = (T)1 / dp;
+    const T lnpf = (T)vc.cf[k] + lnps;
+    const T pfull = (T)vc.sf[k] * ps;
+    const T dlnp_p = (T)vc.dlp_p[k];                 // ln p_{k+1/2} - ln p_k
+    const T dlnp_m = k == 0 ? lnpf : (T)vc.dlp_m[k];  // ln p_k - ln p_{k-1/2} (ln p_{1/2} = 0)
+    const T dlnp = k == 0 ? (T)vc.lb[1] + lnps : (T)vc.dlp[k];
+    // ---- HS_Forcing! on the previous level (sigma = p_k / ps = sf[k])
+    const T s = (T)vc.sf[k] - sb;
+    const T smax = s > (T)0 ? s : (T)0;
+    const T k_v = kv0 * smax;
+    T du = -k_v * up, dv = -k_v * vp;
+    T dt = -((up + (T)0.5 * du * (T)Dt) * du + (vp + (T)0.5 * dv * (T)Dt) * dv) / cp;
+    const T lpn = lnpf - ln_pref;  // ln(p / p_ref)
+    T teq = ((T)315.0 - (T)a.dT_y * s2 - (T)a.dtheta_z * c2 * lpn) * exp((T)a.kappa * lpn);
+    teq = teq > (T)200.0 ? teq : (T)200.0;
+    const T k_t = ka + kt0 * smax * c4;
+    dt = dt - k_t * (tp - teq);
+    // ---- Compute_Corrections_Init sums: column energy integral with ps_p, accumulated in FP64
+    // column integral in the state precision (20-term sum); the sum over columns is FP64
+    T e_p = 0;
+    if (act) {
+      T ua = up + (T)Dt * du, va = vp + (T)Dt * dv;
+      T E = (T)0.5 * (ua * ua + va * va) + cp * (tp + (T)Dt * dt);
+      e_p = E * ((T)vc.dak[k] + (T)vc.dbk[k] * psp);
+    }
+    const double col_e = (double)warp_sum_t<T>(e_p);
+    // ---- Four_In_One! (Spectral_Dynamics.jl:88-183) on the current level
+    const T x1 = ((T)vc.bk[k] * dlnp_m + (T)vc.bk[k + 1] * dlnp_p) * rdp;
+    const T dlnp_dl = x1 * dlps, dlnp_dt = x1 * dtps;
+    du = du - R * t * dlnp_dl;
+    dv = dv - R * t * dlnp_dt;
+    T dmean = dvg * dp + (T)vc.dbk[k] * (u * dlps + v * dtps);
+    if (!act) dmean = 0;
+    const T incl = scan_incl<T>(dmean, lane);  // sum_{r<=k} D_r
+    const T tot = __shfl_sync(FULL, incl, nd - 1);
+    const T excl = shfl_up1(incl, lane, (T)0);
+    const T x5 = -(excl * dlnp + dmean * dlnp_p) * rdp + u * dlnp_dl + v * dlnp_dt;
+    dt = dt + kap * t * x5;
+    // M_{k+1/2}: -sum_{r<=k} D_r + B_{k+1/2} sum_r D_r ; zero at top and surface
+    const T Mhi = (lane + 1 <= nd - 1) ? -incl + tot * (T)vc.bk[k + 1] : (T)0;
+    const T Mlo = shfl_up1(Mhi, lane, (T)0);
+    // ---- Compute_Geopotential! (Press_And_Geopot.jl:71-111), bottom-up
+    const T term = act ? R * t * dlnp : (T)0;
+    const T rs = rscan_incl<T>(term, lane);           // sum_{r>=k} term_r
+    const T ghalf_hi = gs + shfl_dn1(rs, lane, nd, (T)0);  // Phi_{k+1/2}
+    const T gfull = ghalf_hi + R * t * dlnp_p;
+    // ---- Vert_Advection! (second_centered_wts) for u, v, T
+    const T dp_m = shfl_up1(dp, lane, (T)1);
+    const T wlo = dp_m / (dp_m + dp);
+    auto vadv = [&](T r) -> T {
+      T r_m = shfl_up1(r, lane, (T)0);
+      T flux_lo = (lane >= 1) ? Mlo * (r_m + (r - r_m) * wlo) : (T)0;
+      T flux_hi = shfl_dn1(flux_lo, lane, nd, (T)0);
+      return (flux_lo - flux_hi + r * (Mhi - Mlo)) * rdp;
+    };
+    du = du + vadv(u);
+    dv = dv + vadv(v);
+    dt = dt + vadv(t);
+    // ---- Add_Horizontal_Advection!(spe_t_c), Compute_Abs_Vor! fluxes, energy
+    dt = dt - (u * dlT + v * dtT);
+    const T absvor = vor + fj;
+    du = du + absvor * v;
+    dv = dv - absvor * u;
+    // outputs overwrite this column's own (already consumed) input slots
+    if (act) {
+      tile[(0 * nd + k) * HS_CWP + c] = du * cj;
+      tile[(1 * nd + k) * HS_CWP + c] = dv * cj;
+      tile[(2 * nd + k) * HS_CWP + c] = dt;
+      tile[(8 * nd + k) * HS_CWP + c] = gfull + (T)0.5 * (u * u + v * v);
+      tile[(9 * nd + k) * HS_CWP + c] = teq;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      sgl[c] = (-tot) / ps;  // grid_δlnps = grid_δps / ps (Spectral_Dynamics.jl:279)
+      if (colok) {
+        accp += (double)psp;
+        acce += col_e;
+      }
+    }
   }
-  const T sb = (T)a.sigma_b;
-  T sig = pfull / psurf;
-  T s = sig - sb;
-  T smax = s > (T)0 ? s : (T)0;
-  T k_v = ((T)a.k_f / day) / ((T)1.0 - sb) * smax;
-  T du = -k_v * up, dv = -k_v * vp;
-  T dt = -((up + (T)0.5 * du * (T)Dt) * du + (vp + (T)0.5 * dv * (T)Dt) * dv) / (T)a.cp;
-  const T sj = a.sinj[j];
-  const T s2 = sj * sj, c2 = (T)1.0 - s2, c4 = c2 * c2;
-  T pn = pfull / (T)1.0e5;
-  T teq = ((T)315.0 - (T)a.dT_y * s2 - (T)a.dtheta_z * c2 * log(pn)) * pow(pn, (T)a.kappa);
-  teq = teq > (T)200.0 ? teq : (T)200.0;
-  T ka = (T)a.k_a / day, ks = (T)a.k_s / day;
-  T k_t = ka + (ks - ka) / ((T)1.0 - sb) * smax * c4;
-  dt = dt - k_t * (tp - teq);
-  if (act) a.t_eq[x] = teq;
-  // ---- Compute_Corrections_Init sums: column energy integral with ps_p, accumulated in FP64
-  const double psp = (double)a.ps_p[col];
-  double e_p = 0.0;
-  if (act) {
-    T ua = up + (T)Dt * du, va = vp + (T)Dt * dv;
-    T E = (T)0.5 * (ua * ua + va * va) + (T)a.cp * (tp + (T)Dt * dt);
-    e_p = (double)E * (vc.dak[k] + vc.dbk[k] * psp);
+  __syncthreads();
+  {
+    T* out[5] = {a.ducos, a.dvcos, a.dtg, a.energy, a.t_eq};
+    const int slot[5] = {0, 1, 2, 8, 9};
+    for (int q = threadIdx.x; q < 5 * nd * HS_CW; q += blockDim.x) {
+      int o = q / (nd * HS_CW), r = q - o * nd * HS_CW, k = r / HS_CW, c = r - k * HS_CW, i = i0 + c;
+      if (i < nlon) out[o][k * G + row + i] = tile[(slot[o] * nd + k) * HS_CWP + c];
+    }
+    if (threadIdx.x < HS_CW && i0 + (int)threadIdx.x < nlon) a.dlnps[row + i0 + threadIdx.x] = sgl[threadIdx.x];
   }
-  const double col_e = warp_sum(e_p);
-  // ---- Four_In_One! (Spectral_Dynamics.jl:88-183) on the current level
-  T u = 0, v = 0, t = 0, dvg = 0, vor = 0, dlT = 0, dtT = 0;
-  if (act) {
-    u = a.u_c[x];
-    v = a.v_c[x];
-    t = a.t_c[x];
-    dvg = a.div[x];
-    vor = a.vor[x];
-    dlT = a.dlT[x];
-    dtT = a.dtT[x];
-  }
-  const T dlps = a.dlps[col], dtps = a.dtps[col];
-  const T R = (T)a.rdgas, kap = (T)a.rdgas / (T)a.cp;
-  const T dlnp_p = lnph1 - lnpf, dlnp_m = lnpf - lnph0, dlnp = lnph1 - lnph0;
-  const T x1 = ((T)vc.bk[k] * dlnp_m + (T)vc.bk[k + 1] * dlnp_p) * rdp;
-  const T dlnp_dl = x1 * dlps, dlnp_dt = x1 * dtps;
-  du = du - R * t * dlnp_dl;
-  dv = dv - R * t * dlnp_dt;
-  T dmean = dvg * dp + (T)vc.dbk[k] * (u * dlps + v * dtps);
-  if (!act) dmean = 0;
-  const T incl = scan_incl<T>(dmean, lane);         // sum_{r<=k} D_r
-  const T tot = __shfl_sync(FULL, incl, nd - 1);
-  const T excl = shfl_up1(incl, lane, (T)0);
-  T x5 = -(excl * dlnp + dmean * dlnp_p) * rdp + u * dlnp_dl + v * dlnp_dt;
-  dt = dt + kap * t * x5;
-  // M_{k+1/2}: -sum_{r<=k} D_r + B_{k+1/2} sum_r D_r ; zero at top and surface
-  T Mhi = (lane + 1 <= nd - 1) ? -incl + tot * (T)vc.bk[k + 1] : (T)0;
-  T Mlo = shfl_up1(Mhi, lane, (T)0);
-  // ---- Compute_Geopotential! (Press_And_Geopot.jl:71-111), bottom-up
-  T term = act ? R * t * (lnph1 - lnph0) : (T)0;
-  const T rs = rscan_incl<T>(term, lane);           // sum_{r>=k} term_r
-  T gs = act ? a.geopots[col] : (T)0;
-  gs = __shfl_sync(FULL, gs, 0);
-  T ghalf_hi = gs + shfl_dn1(rs, lane, nd, (T)0);  // Phi_{k+1/2}
-  T gfull = ghalf_hi + R * t * (lnph1 - lnpf);
-  // ---- Vert_Advection! (second_centered_wts) for u, v, T
-  T dp_m = shfl_up1(dp, lane, (T)1);
-  const T wlo = dp_m / (dp_m + dp);
-  auto vadv = [&](T r) -> T {
-    T r_m = shfl_up1(r, lane, (T)0);
-    T flux_lo = (lane >= 1) ? Mlo * (r_m + (r - r_m) * wlo) : (T)0;
-    T flux_hi = shfl_dn1(flux_lo, lane, nd, (T)0);
-    return (flux_lo - flux_hi + r * (Mhi - Mlo)) * rdp;
-  };
-  du = du + vadv(u);
-  dv = dv + vadv(v);
-  dt = dt + vadv(t);
-  // ---- Add_Horizontal_Advection!(spe_t_c), Compute_Abs_Vor! fluxes, energy
-  dt = dt - (u * dlT + v * dtT);
-  const T absvor = vor + a.coriolis[j];
-  du = du + absvor * v;
-  dv = dv - absvor * u;
-  const T cj = a.cosj[j];
-  if (act) {
-    a.ducos[x] = du * cj;
-    a.dvcos[x] = dv * cj;
-    a.dtg[x] = dt;
-    a.energy[x] = gfull + (T)0.5 * (u * u + v * v);
-    if (lane == 0) a.dlnps[col] = (-tot) / ps;
-  }
-  // ---- block partials for mean_ps_p and mean_energy_p
-  __shared__ double sm[2][8];
+  // ---- block partials for mean_ps_p and mean_energy_p (fixed order)
   if (lane == 0) {
-    sm[0][w] = (i < nlon) ? psp : 0.0;
-    sm[1][w] = (i < nlon) ? col_e : 0.0;
+    red[0][w] = accp;
+    red[1][w] = acce;
   }
   __syncthreads();
   double vals[2] = {0, 0};
   if (threadIdx.x == 0)
     for (int q = 0; q < 8; q++) {
-      vals[0] += sm[0][q];
-      vals[1] += sm[1][q];
+      vals[0] += red[0][q];
+      vals[1] += red[1][q];
     }
   double tot2[2];
   if (grid_reduce_last<2>(vals, a.partials, a.counter, a.wts, tot2) && threadIdx.x == 0) {
@@ -305,7 +358,8 @@ template <typename T>
 struct ImplArgs {
   const V2<T>*dvor, *ddiv, *dtend, *dlnps;  // spectral tendencies from the analysis
   V2<T> *vor_p, *vor_c, *vor_n, *div_p, *div_c, *div_n, *t_p, *t_c, *t_n, *lnps_p, *lnps_c, *lnps_n;
-  const T *eig, *damping, *dfac;  // [m][n]: -n(n+1)/a², damping, 1/(1 + Δt' damping) for this step
+  const T *damping, *dfac;  // [m][n]: damping, 1/(1 + Δt' damping) for this step
+  const double* eig64;      // [m][n]: -n(n+1)/a², FP64
   const double* W;                // [N+1][c][r]
   const int2* pairs;
   int npairs, nd, ns, N, init_step, dt;
@@ -360,9 +414,10 @@ __device__ __forceinline__ void lf(int init, int Dt, R rob, R d, R f, R& dq, R q
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, VertCoef vc) {
-  using R = T;
+// R is the precision of the vertical algebra (FP64 on the FP64 path; selectable on the FP32 path).
+template <typename T, typename R>
+__global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCoef* __restrict__ vcp) {
+  const VertCoef& vc = *vcp;
   using C = CX<R>;
   const int lane = threadIdx.x & 31;
   const int pid = blockIdx.x * 8 + (threadIdx.x >> 5);
@@ -376,13 +431,13 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, VertCoef vc)
   auto ld = [&](const V2<T>* p) -> C {
     if (!act) return C{0, 0};
     V2<T> v = p[s];
-    return C{v.x, v.y};
+    return C{(R)v.x, (R)v.y};
   };
   C ddiv = ld(a.ddiv), dtt = ld(a.dtend), dvor = ld(a.dvor);
   C divp = ld(a.div_p), divc = ld(a.div_c), tp = ld(a.t_p), tc = ld(a.t_c), vorp = ld(a.vor_p), vorc = ld(a.vor_c);
   V2<T> l0 = a.dlnps[row], lp0 = a.lnps_p[row], lc0 = a.lnps_c[row];
-  C dl = {l0.x, l0.y}, lp = {lp0.x, lp0.y}, lc = {lc0.x, lc0.y};
-  const R xi = (R)a.xi, rpsr = (R)(1.0 / a.ps_ref), xipsr = (R)(a.xi / a.ps_ref), eig = a.eig[row];
+  C dl = {(R)l0.x, (R)l0.y}, lp = {(R)lp0.x, (R)lp0.y}, lc = {(R)lc0.x, (R)lc0.y};
+  const R xi = (R)a.xi, rpsr = (R)(1.0 / a.ps_ref), xipsr = (R)(a.xi / a.ps_ref), eig = (R)a.eig64[row];
   const R kap = (R)a.kappa, Rg = (R)a.rdgas;
   // Adjust_δlnps_δt_δdiv! :360-404
   C dps, dtmp;
@@ -407,12 +462,17 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, VertCoef vc)
   if (n <= a.N) {
     const double* W = a.W + (size_t)n * nd * nd;
     const double bxl = (double)ddiv.x, byl = (double)ddiv.y;
+    double wv[32];  // row k of W_n, fetched up front (independent loads in flight together)
+#pragma unroll
+    for (int c = 0; c < 32; c++) wv[c] = (act && c < nd) ? W[(size_t)c * nd + k] : 0.0;
     double sx = 0, sy = 0;
-    for (int c = 0; c < nd; c++) {
-      double bx = __shfl_sync(FULL, bxl, c), by = __shfl_sync(FULL, byl, c);
-      double wv = act ? W[(size_t)c * nd + k] : 0.0;
-      sx = sx + wv * bx;
-      sy = sy + wv * by;
+#pragma unroll
+    for (int c = 0; c < 32; c++) {
+      if (c < nd) {  // nd is warp-uniform
+        double bx = __shfl_sync(FULL, bxl, c), by = __shfl_sync(FULL, byl, c);
+        sx = sx + wv[c] * bx;
+        sy = sy + wv[c] * by;
+      }
     }
     ddiv.x = act ? (R)sx : (R)0;
     ddiv.y = act ? (R)sy : (R)0;
@@ -423,7 +483,7 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, VertCoef vc)
   dl.x = dl.x + xipsr * dps.x;
   dl.y = dl.y + xipsr * dps.y;
   // damping + leapfrog
-  const R d = a.damping[row], f = a.dfac[row], rob = (R)a.robert;
+  const R d = (R)a.damping[row], f = (R)a.dfac[row], rob = (R)a.robert;
   const int ini = a.init_step, Dt = a.dt;
   if (act) {
     C vn, dn, tn;
@@ -434,20 +494,20 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, VertCoef vc)
     lf<R>(ini, Dt, rob, d, f, dtt.x, tp.x, tc.x, tn.x);
     lf<R>(ini, Dt, rob, d, f, dtt.y, tp.y, tc.y, tn.y);
     V2<T> o;
-    o.x = vn.x; o.y = vn.y; a.vor_n[s] = o;
-    o.x = vorc.x; o.y = vorc.y; a.vor_c[s] = o;
-    o.x = dn.x; o.y = dn.y; a.div_n[s] = o;
-    o.x = divc.x; o.y = divc.y; a.div_c[s] = o;
-    o.x = tn.x; o.y = tn.y; a.t_n[s] = o;
-    o.x = tc.x; o.y = tc.y; a.t_c[s] = o;
+    o.x = (T)vn.x; o.y = (T)vn.y; a.vor_n[s] = o;
+    o.x = (T)vorc.x; o.y = (T)vorc.y; a.vor_c[s] = o;
+    o.x = (T)dn.x; o.y = (T)dn.y; a.div_n[s] = o;
+    o.x = (T)divc.x; o.y = (T)divc.y; a.div_c[s] = o;
+    o.x = (T)tn.x; o.y = (T)tn.y; a.t_n[s] = o;
+    o.x = (T)tc.x; o.y = (T)tc.y; a.t_c[s] = o;
   }
   if (lane == 0) {  // lnps: leapfrog without damping (d = 0, f = 1)
     C ln;
     lf<R>(ini, Dt, rob, (R)0, (R)1, dl.x, lp.x, lc.x, ln.x);
     lf<R>(ini, Dt, rob, (R)0, (R)1, dl.y, lp.y, lc.y, ln.y);
     V2<T> o;
-    o.x = ln.x; o.y = ln.y; a.lnps_n[row] = o;
-    o.x = lc.x; o.y = lc.y; a.lnps_c[row] = o;
+    o.x = (T)ln.x; o.y = (T)ln.y; a.lnps_n[row] = o;
+    o.x = (T)lc.x; o.y = (T)lc.y; a.lnps_c[row] = o;
   }
 }
 
@@ -467,64 +527,73 @@ struct CorrArgs {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(1024) k_hs_corr_reduce(CorrArgs<T> a, VertCoef vc) {
-  // one block per latitude row, one thread per column (coalesced along longitude)
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-  const int i = threadIdx.x, j = blockIdx.y, nd = a.nd;
+__global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const VertCoef* __restrict__ vcp) {
+  const VertCoef& vc = *vcp;
+  // block = 32 consecutive columns of one latitude row x 8 level groups: warp ks reads levels
+  // ks, ks + 8, ... of the 32 columns (coalesced rows); column partial sums in the state precision,
+  // folded across level groups and columns in FP64 in a fixed order
+  constexpr int KS = 8;
+  const int i = blockIdx.x * 32 + (threadIdx.x & 31), ks = threadIdx.x >> 5, j = blockIdx.y, nd = a.nd;
   const bool act = i < a.nlon;
   const size_t G = (size_t)a.nlat * a.nlon, col = (size_t)j * a.nlon + (act ? i : 0);
-  double ps = act ? (double)a.ps_n[col] : 0.0;
-  double ea = 0, eb = 0;
+  __shared__ T part[2][KS][32];
+  T ea = 0, eb = 0;
   if (act) {
     const T cp = (T)a.cp;
-    for (int k = 0; k < nd; k++) {
+    for (int k = ks; k < nd; k += KS) {
       size_t x = (size_t)k * G + col;
       T u = a.u_n[x], v = a.v_n[x], t = a.t_n[x];
       T E = (T)0.5 * (u * u + v * v) + cp * t;
-      ea += (double)E * vc.dak[k];
-      eb += (double)E * vc.dbk[k];
+      ea += E * (T)vc.dak[k];
+      eb += E * (T)vc.dbk[k];
     }
-    eb *= ps;
   }
-  const double s0 = warp_sum(ps), s1 = warp_sum(ea), s2 = warp_sum(eb);
-  __shared__ double sm[3][32];
-  if (lane == 0) {
-    sm[0][w] = s0;
-    sm[1][w] = s1;
-    sm[2][w] = s2;
-  }
+  part[0][ks][threadIdx.x & 31] = ea;
+  part[1][ks][threadIdx.x & 31] = eb;
   __syncthreads();
   double vals[3] = {0, 0, 0};
-  if (threadIdx.x == 0)
-    for (int q = 0; q < nw; q++) {
-      vals[0] += sm[0][q];
-      vals[1] += sm[1][q];
-      vals[2] += sm[2][q];
+  if (ks == 0) {
+    const int c = threadIdx.x;
+    double sa = 0.0, sb = 0.0;
+    for (int q = 0; q < KS; q++) {
+      sa += (double)part[0][q][c];
+      sb += (double)part[1][q][c];
     }
+    const double ps = act ? (double)a.ps_n[col] : 0.0;
+    sb *= ps;
+    vals[0] = warp_sum(ps);
+    vals[1] = warp_sum(sa);
+    vals[2] = warp_sum(sb);
+  }
   double tot3[3];
-  if (grid_reduce_last<3>(vals, a.partials, a.counter, a.wts, tot3) && threadIdx.x == 0) {
-    double two_n = 2.0 * a.nlon;
-    double mean_ps_p = a.scalars[0], mean_energy_p = a.scalars[1];
-    double factor = 1.0, corr = 0.0;
-    if (a.do_mass) {
-      double mean_ps_n = tot3[0] / two_n;
-      factor = mean_ps_p / mean_ps_n;
-      V2<T> l = a.lnps_n[0];  // spe_lnps_n[1,1,1] += log(factor)  (P_00 = 1)
-      l.x = (T)((double)l.x + log(factor));
-      a.lnps_n[0] = l;
-    }
-    if (a.do_energy) {
-      // Δp_k = Δa_k + Δb_k (factor ps_n): the mass correction enters linearly
-      double mean_energy_n = (tot3[1] + factor * tot3[2]) / two_n / a.grav;
-      corr = a.grav * (mean_energy_p - mean_energy_n) / (a.cp * mean_ps_p);
-      for (int k = 0; k < nd; k++) {  // spe_t_n[1,1,:] .+= temperature_correction
-        V2<T> tt = a.t_spec_n[k];
-        tt.x = (T)((double)tt.x + corr);
-        a.t_spec_n[k] = tt;
+  __shared__ double fc[2];
+  if (grid_reduce_last<3>(vals, a.partials, a.counter, a.wts, tot3)) {
+    if (threadIdx.x == 0) {
+      double two_n = 2.0 * a.nlon;
+      double mean_ps_p = a.scalars[0], mean_energy_p = a.scalars[1];
+      double factor = 1.0, corr = 0.0;
+      if (a.do_mass) {
+        double mean_ps_n = tot3[0] / two_n;
+        factor = mean_ps_p / mean_ps_n;
+        V2<T> l = a.lnps_n[0];  // spe_lnps_n[1,1,1] += log(factor)  (P_00 = 1)
+        l.x = (T)((double)l.x + log(factor));
+        a.lnps_n[0] = l;
       }
+      if (a.do_energy) {
+        // Δp_k = Δa_k + Δb_k (factor ps_n): the mass correction enters linearly
+        double mean_energy_n = (tot3[1] + factor * tot3[2]) / two_n / a.grav;
+        corr = a.grav * (mean_energy_p - mean_energy_n) / (a.cp * mean_ps_p);
+      }
+      a.scalars[2] = factor;
+      a.scalars[3] = corr;
+      fc[1] = corr;
     }
-    a.scalars[2] = factor;
-    a.scalars[3] = corr;
+    __syncthreads();
+    if (a.do_energy && (int)threadIdx.x < nd) {  // spe_t_n[1,1,:] .+= temperature_correction
+      V2<T> tt = a.t_spec_n[threadIdx.x];
+      tt.x = (T)((double)tt.x + fc[1]);
+      a.t_spec_n[threadIdx.x] = tt;
+    }
   }
 }
 
@@ -541,8 +610,9 @@ __global__ void k_hs_corr_apply(T* t_n, T* ps_n, const double* scalars, size_t n
 // out: [0]=p_half (nd+1) [1]=lnp_half (nd+1) [2]=dp (nd) [3]=p_full (nd) [4]=lnp_full (nd)
 //      [5]=z_full (nd) [6]=z_half (nd+1), each stored at its own offset in `diag`.
 template <typename T>
-__global__ void k_pressure_heights(const T* ps_c, const T* t_c, const T* geopots, double* diag, VertCoef vc, int nd,
+__global__ void k_pressure_heights(const T* ps_c, const T* t_c, const T* geopots, double* diag, const VertCoef* __restrict__ vcp, int nd,
                                    size_t G, double rdgas, double grav) {
+  const VertCoef& vc = *vcp;
   size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (c >= G) return;
   double* ph = diag;
@@ -679,6 +749,15 @@ void vertical_setup(jgcm_model* md) {
     vc.dak[k] = vc.ak[k + 1] - vc.ak[k];
     vc.dbk[k] = vc.bk[k + 1] - vc.bk[k];
   }
+  for (int k = 1; k <= nd; k++) vc.lb[k] = std::log(vc.bk[k]);
+  for (int k = 0; k < nd; k++) {
+    vc.cf[k] = (k == 0) ? vc.lb[1] - 1.0
+                        : vc.lb[k + 1] + vc.bk[k] * (vc.lb[k + 1] - vc.lb[k]) / vc.dbk[k] - 1.0;
+    vc.sf[k] = std::exp(vc.cf[k]);
+    vc.dlp_p[k] = vc.lb[k + 1] - vc.cf[k];
+    vc.dlp_m[k] = (k == 0) ? 0.0 : vc.cf[k] - vc.lb[k];
+    vc.dlp[k] = (k == 0) ? 0.0 : vc.lb[k + 1] - vc.lb[k];
+  }
   if (md->P.kind != JGCM_HELD_SUAREZ) return;
   std::vector<double> ph(nd + 1), pf(nd), dlh(nd + 1), dlf(nd);
   double lph[JGCM_MAX_ND + 1], lpf[JGCM_MAX_ND];
@@ -763,8 +842,7 @@ void model_free(jgcm_model* md) {
                 md->spe_zero, md->spe_dvor, md->spe_ddiv, md->spe_dlnps, md->spe_dt, md->g_dlps, md->g_dtps,
                 md->g_dlT, md->g_dtT, md->g_ducos, md->g_dvcos, md->g_dt, md->g_energy, md->g_dlnps, md->g_diag,
                 md->coriolis, md->damping, md->dfac[0], md->dfac[1], md->d_W, md->d_pairs, md->d_partials,
-                md->d_scalars,
-                md->d_counter};
+                md->d_scalars, md->d_counter, md->d_vc};
   for (auto p : ps)
     if (p) cudaFree(p);
   delete[] md->div_mat;
@@ -866,6 +944,8 @@ int model_alloc(jgcm_model* md) {
   JG_CUDA(cudaEventCreate(&md->ev1));
   md->div_mat = new double[nd * nd]();
   vertical_setup(md);
+  JG_TRY(alloc((void**)&md->d_vc, sizeof(VertCoef)));
+  JG_CUDA(cudaMemcpy(md->d_vc, &md->vc, sizeof(VertCoef), cudaMemcpyHostToDevice));
   if (md->P.kind == JGCM_HELD_SUAREZ) JG_TRY(build_wave(md));
   JG_CUDA(cudaStreamSynchronize(m->stream));
   return JGCM_OK;
@@ -1107,8 +1187,9 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   a.rdgas = md->P.rdgas;
   a.cp = md->cp_air;
   a.grav = md->P.grav;
-  dim3 gcol((m->nlon + 7) / 8, m->nlat);
-  k_hs_column<T><<<gcol, 256, 0, st>>>(a, md->vc);
+  dim3 gcol((m->nlon + HS_CW - 1) / HS_CW, m->nlat);
+  const size_t smcol = ((size_t)HS_NIN * nd * HS_CWP + 5 * HS_CW) * sizeof(T);
+  k_hs_column<T><<<gcol, 256, smcol, st>>>(a, md->d_vc);
   mark(st);
   JG_CUDA(cudaGetLastError());
   // 3. forward transforms: δu cos, δv cos, δT, energy, δlnps -> vor/div tendencies (alpha
@@ -1143,7 +1224,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ia.div_p = (V*)md->spe_div[p]; ia.div_c = (V*)md->spe_div[c]; ia.div_n = (V*)md->spe_div[n];
   ia.t_p = (V*)md->spe_t[p]; ia.t_c = (V*)md->spe_t[c]; ia.t_n = (V*)md->spe_t[n];
   ia.lnps_p = (V*)md->spe_lnps[p]; ia.lnps_c = (V*)md->spe_lnps[c]; ia.lnps_n = (V*)md->spe_lnps[n];
-  ia.eig = tb.eig;
+  ia.eig64 = m->t64.eig;
   ia.damping = (const T*)md->damping;
   ia.dfac = (const T*)md->dfac[md->init_step ? 0 : 1];
   ia.W = md->d_W + (md->init_step ? 0 : (size_t)(m->N + 1) * nd * nd);
@@ -1159,7 +1240,9 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ia.kappa = md->P.kappa;
   ia.rdgas = md->P.rdgas;
   ia.robert = md->P.robert_coef;
-  k_hs_implicit<T><<<(md->npairs + 7) / 8, 256, 0, st>>>(ia, md->vc);
+  // vertical algebra in the state precision (FP64 algebra on the FP32 path measured no more
+  // accurate: its error is set by FP32 storage); the wave-matrix solve is FP64 in both
+  k_hs_implicit<T, T><<<(md->npairs + 7) / 8, 256, 0, st>>>(ia, md->d_vc);
   mark(st);
   JG_CUDA(cudaGetLastError());
   // 5. back to the grid: vor, div, u, v, T, lnps (+ ps = exp(lnps))
@@ -1204,7 +1287,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ca.do_energy = md->P.do_energy_correction;
   ca.cp = md->cp_air;
   ca.grav = md->P.grav;
-  k_hs_corr_reduce<T><<<dim3(1, m->nlat), m->nlon < 32 ? 32 : m->nlon, 0, st>>>(ca, md->vc);
+  k_hs_corr_reduce<T><<<dim3((m->nlon + 31) / 32, m->nlat), 256, 0, st>>>(ca, md->d_vc);
   mark(st);
   JG_CUDA(cudaGetLastError());
   size_t nt = grid_elems(m, nd), nps = grid_elems(m, 1);
@@ -1420,8 +1503,17 @@ extern "C" int jgcm_model_kernel_name(jgcm_model* md, int slot, char* buf, int c
   return JGCM_OK;
 }
 
-// Per-kernel device times of steady steps: every launch is followed by an event (eager launches,
-// events on the model stream), ms[slot] = mean over nsteps of event(slot) - event(slot - 1).
+// Holds the stream for a fixed number of SM clock cycles (bounded: no flag, no external wait), so
+// the launches queued behind it run back to back and their events time the device alone.
+__global__ void k_hold(long long cycles) {
+  const long long t0 = clock64();
+  while (clock64() - t0 < cycles) {
+  }
+}
+
+// Per-kernel device times of steady steps: every launch is followed by an event (eager launches
+// queued behind k_hold, events on the model stream), ms[slot] = mean over nsteps of
+// event(slot) - event(slot - 1).
 extern "C" int jgcm_model_kernel_times(jgcm_model* md, int nsteps, float* ms, int cap, int* count) {
   JG_ARG(md && ms && count && nsteps > 0, "bad arguments");
   jgcm_mesh* m = md->mesh;
@@ -1432,6 +1524,11 @@ extern "C" int jgcm_model_kernel_times(jgcm_model* md, int nsteps, float* ms, in
   for (auto& e : ev) JG_CUDA(cudaEventCreate(&e));
   Marker mk{ev.data() + 1, 0, nsteps * L};
   JG_CUDA(cudaStreamSynchronize(m->stream));
+  // ~1 ms + ~6 us per queued launch at 2 GHz (capped at ~20 ms): the host queues every launch
+  // before the first one starts
+  long long hold = 2000000LL + (long long)nsteps * L * 12000LL;
+  k_hold<<<1, 1, 0, m->stream>>>(hold < 40000000LL ? hold : 40000000LL);
+  JG_CUDA(cudaGetLastError());
   JG_CUDA(cudaEventRecord(ev[0], m->stream));
   g_marker = &mk;
   int st = JGCM_OK;
@@ -1497,11 +1594,11 @@ extern "C" int jgcm_model_get_field(jgcm_model* md, const char* name, double* ho
     int c = lvl(md, 1);
     if (is_fp64(m))
       k_pressure_heights<double><<<nb, 128, 0, st>>>((const double*)md->grid_ps[c], (const double*)md->grid_t[c],
-                                                     (const double*)md->grid_geopots, (double*)md->g_diag, md->vc,
+                                                     (const double*)md->grid_geopots, (double*)md->g_diag, md->d_vc,
                                                      md->nd, G, md->P.rdgas, md->P.grav);
     else
       k_pressure_heights<float><<<nb, 128, 0, st>>>((const float*)md->grid_ps[c], (const float*)md->grid_t[c],
-                                                    (const float*)md->grid_geopots, (double*)md->g_diag, md->vc,
+                                                    (const float*)md->grid_geopots, (double*)md->g_diag, md->d_vc,
                                                     md->nd, G, md->P.rdgas, md->P.grav);
     JG_CUDA(cudaGetLastError());
     JG_CUDA(cudaMemcpyAsync(host, (double*)md->g_diag + f.off, n * 8, cudaMemcpyDeviceToHost, st));

@@ -363,7 +363,7 @@ __device__ __forceinline__ void leapfrog_c(const StepParams& sp, T d, V2<T>& dq,
 // combinations g(mu_j) +/- g(-mu_j) of the tile's columns.
 template <typename T>
 __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb, const V2<T>* __restrict__ F,
-                                                      int ns, int nlat, int Cin, int CT) {
+                                                      int ns, int nlat, int Cin, int CT, int stage) {
   using V = V2<T>;
   extern __shared__ __align__(16) unsigned char smem[];
   const int m = blockIdx.y;
@@ -374,6 +374,23 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
   V* S = (V*)smem;              // [4][nh][CT] symmetric      (column fastest: no bank conflicts)
   V* A = S + 4 * CT * nh;       // [4][nh][CT] antisymmetric
   const size_t mrow = (size_t)m * (ns + 1);
+  // quadrature rows n = m..ns of this m ([K][nh]); staged once per block when they fit
+  const T* tPW = tb.PW + (mrow + m) * nh;
+  const T* tCA = tb.CA + (mrow + m) * nh;
+  const T* tCB = tb.CB + (mrow + m) * nh;
+  if (stage) {
+    T* sPW = (T*)(A + 4 * CT * nh);
+    T* sCA = sPW + K * nh;
+    T* sCB = sCA + K * nh;
+    for (int i = threadIdx.x; i < K * nh; i += blockDim.x) {
+      sPW[i] = tPW[i];
+      sCA[i] = tCA[i];
+      sCB[i] = tCB[i];
+    }
+    tPW = sPW;
+    tCA = sCA;
+    tCB = sCB;
+  }
   for (int i = threadIdx.x; i < 4 * CT * nh; i += blockDim.x) {
     int slot = i / (CT * nh), rem = i - slot * CT * nh, jh = rem / CT, cl = rem - jh * CT, c = cbase + cl;
     V s, a;
@@ -396,25 +413,34 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
     A[(slot * nh + jh) * CT + cl] = a;
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < K * CT; i += blockDim.x) {
-    int r = i / CT, cl = i - r * CT, n = m + r, c = cbase + cl;
-    if (c >= C) continue;
+  // each output is summed by a quad of threads (latitudes jh = q, q+4, ...), then combined with two
+  // masked shuffles; quads never straddle loop iterations (blockDim is a multiple of 4)
+  const unsigned qmask = 0xFu << (threadIdx.x & 28);
+  for (int i = threadIdx.x; i < K * CT * 4; i += blockDim.x) {
+    const int q = i & 3, o = i >> 2;
+    int r = o / CT, cl = o - r * CT, n = m + r, c = cbase + cl;
+    if (c >= C) continue;  // whole quad
     int k;
     const SpecOutGroup& g = group_of(plan.g, plan.ng, c, &k);
     const bool even = (r & 1) == 0;
-    const T* pw = tb.PW + (mrow + n) * nh;
-    const T* ca = tb.CA + (mrow + n) * nh;
-    const T* cb = tb.CB + (mrow + n) * nh;
+    const T* pw = tPW + r * nh;
+    const T* ca = tCA + r * nh;
+    const T* cb = tCB + r * nh;
     const size_t sidx = (mrow + n) * g.L + k;
     auto plain = [&](int slot) -> V {
       const V* src = (even ? S : A) + slot * nh * CT + cl;
       T sr = 0, si = 0;
-      for (int jh = 0; jh < nh; jh++) {
+#pragma unroll 4
+      for (int jh = q; jh < nh; jh += 4) {
         T w = pw[jh];
         V x = src[jh * CT];
         sr += x.x * w;
         si += x.y * w;
       }
+      sr += __shfl_xor_sync(qmask, sr, 1);
+      si += __shfl_xor_sync(qmask, si, 1);
+      sr += __shfl_xor_sync(qmask, sr, 2);
+      si += __shfl_xor_sync(qmask, si, 2);
       V o;
       o.x = (n == ns) ? (T)0 : sr * (T)0.5;
       o.y = (n == ns) ? (T)0 : si * (T)0.5;
@@ -425,7 +451,8 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
       const V* sa = (even ? S : A) + slotA * nh * CT + cl;
       const V* sb = (even ? A : S) + slotB * nh * CT + cl;
       T ar = 0, ai = 0, br = 0, bi = 0;
-      for (int jh = 0; jh < nh; jh++) {
+#pragma unroll 4
+      for (int jh = q; jh < nh; jh += 4) {
         T wa = ca[jh], wb = cb[jh];
         V xa = sa[jh * CT], xb = sb[jh * CT];
         ar += (-xa.y) * wa;
@@ -433,23 +460,51 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
         br += xb.x * wb;
         bi += xb.y * wb;
       }
+      T xr = ar + sign * br, xi = ai + sign * bi;
+      xr += __shfl_xor_sync(qmask, xr, 1);
+      xi += __shfl_xor_sync(qmask, xi, 1);
+      xr += __shfl_xor_sync(qmask, xr, 2);
+      xi += __shfl_xor_sync(qmask, xi, 2);
       V o;
-      o.x = (n == ns) ? (T)0 : ar + sign * br;
-      o.y = (n == ns) ? (T)0 : ai + sign * bi;
+      o.x = (n == ns) ? (T)0 : xr;
+      o.y = (n == ns) ? (T)0 : xi;
       return o;
     };
+    // every lane of the quad takes part in the sums; lane q = 0 applies the epilogue
+    V r0, r1, r2, r3;
+    r0.x = r0.y = r1.x = r1.y = r2.x = r2.y = r3.x = r3.y = 0;
+    switch (g.op) {
+      case G2S_PLAIN:
+        r0 = plain(0);
+        break;
+      case G2S_VOR:
+      case G2S_BARO:
+        r0 = alpha(0, 1, (T)-1);
+        break;
+      case G2S_DIV:
+        r0 = alpha(0, 1, (T)1);
+        if (g.colE >= 0) r2 = plain(2);
+        break;
+      case G2S_SW:
+        r0 = alpha(1, 0, (T)-1);
+        r1 = alpha(0, 1, (T)1);
+        r2 = plain(2);
+        r3 = plain(3);
+        break;
+    }
+    if (q != 0) continue;
     const T eig = tb.eig[mrow + n];
     switch (g.op) {
       case G2S_PLAIN:
-        ((V*)g.dst)[sidx] = plain(0);
+        ((V*)g.dst)[sidx] = r0;
         break;
       case G2S_VOR:
-        ((V*)g.dst)[sidx] = alpha(0, 1, (T)-1);
+        ((V*)g.dst)[sidx] = r0;
         break;
       case G2S_DIV: {
-        V v = alpha(0, 1, (T)1);
+        V v = r0;
         if (g.colE >= 0) {  // - laplacian(G2S(E) + extra)
-          V e = plain(2);
+          V e = r2;
           if (g.extra) {
             V x = ((const V*)g.extra)[sidx];
             e.x = e.x + x.x;
@@ -461,7 +516,7 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
         ((V*)g.dst)[sidx] = v;
       } break;
       case G2S_BARO: {  // Barotropic_Dynamics.jl:31-36: vorticity tendency, damping, leapfrog
-        V dq = alpha(0, 1, (T)-1);
+        V dq = r0;
         V* qc = (V*)g.qc[0];
         const V* qp = (const V*)g.qp[0];
         V c0 = qc[sidx], p0 = qp[sidx], n0;
@@ -472,10 +527,10 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
       } break;
       case G2S_SW: {  // Shallow_Water_Dynamics.jl:133-165
         // slots: 0 = du cos, 1 = dv cos, 2 = kinetic energy, 3 = dh
-        V dvor = alpha(1, 0, (T)-1);
-        V ddiv = alpha(0, 1, (T)1);
-        V kin = plain(2);
-        V dh = plain(3);
+        V dvor = r0;
+        V ddiv = r1;
+        V kin = r2;
+        V dh = r3;
         const V* hc_p = (const V*)g.qc[2];
         V hc = hc_p[sidx], hp = ((const V*)g.qp[2])[sidx];
         V dc = ((const V*)g.qc[1])[sidx], dp = ((const V*)g.qp[1])[sidx];
@@ -518,7 +573,7 @@ template <typename T>
 static int configure_smem() {
   int idx = sizeof(T) == 8 ? 1 : 0;
   if (g_smem_configured[idx]) return JGCM_OK;
-  const int big = 200 * 1024;
+  const int big = (int)kSmemBudget;
   JG_CUDA(cudaFuncSetAttribute(k_s2g_legendre<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   JG_CUDA(cudaFuncSetAttribute(k_ifft<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   JG_CUDA(cudaFuncSetAttribute(k_fft<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
@@ -582,8 +637,11 @@ int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp, cudaStream_t 
   Tables<T> tb = tables<T>(m);
   const int nh = m->nh, ct = g2s_ct(nh);
   size_t sm = (size_t)8 * ct * nh * sizeof(V);
+  const size_t tab = (size_t)3 * (m->ns + 1) * nh * sizeof(T);
+  const int stage = sm + tab <= kSmemBudget;
+  if (stage) sm += tab;
   dim3 g((gp.C + ct - 1) / ct, m->N + 1);
-  k_g2s_legendre<T><<<g, 256, sm, st>>>(gp, tb, (const V*)m->d_fbuf, m->ns, m->nlat, fp.C, ct);
+  k_g2s_legendre<T><<<g, 256, sm, st>>>(gp, tb, (const V*)m->d_fbuf, m->ns, m->nlat, fp.C, ct, stage);
   mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;

