@@ -1661,6 +1661,110 @@ extern "C" int jgcm_model_semi_implicit(jgcm_model* md, const char* name, double
   return JGCM_OK;
 }
 
+// HS_Forcing! (HS_Forcing.jl:1-130) on caller arrays: Rayleigh_Damping! (:101-130), the
+// energy-conserving frictional heating (:21-26) and Newtonian_Damping! (:37-97), elementwise over
+// the [nλ, nθ, nd] grid in the model's precision.  sigma = p_full / ps with ps = p_half[:, :, nd+1],
+// as the reference computes it (the fused step kernel uses the sigma levels of even_sigma instead).
+namespace {
+struct HSForcingArgs {
+  const double *u, *v, *p_half, *p_full, *t, *sinth;
+  double *du, *dv, *t_eq, *dt;
+  int nlon, nlat, nd, Dt;
+  double sigma_b, k_f, k_a, k_s, dT_y, dtheta_z, kappa, cp;
+};
+
+template <typename T>
+__global__ void k_hs_forcing(HSForcingArgs a) {
+  const size_t G = (size_t)a.nlon * a.nlat, n = G * a.nd;
+  const T day = (T)86400, sb = (T)a.sigma_b, Dt = (T)a.Dt;
+  for (size_t x = blockIdx.x * (size_t)blockDim.x + threadIdx.x; x < n; x += (size_t)gridDim.x * blockDim.x) {
+    const size_t k = x / G, c = x - k * G;
+    const int j = (int)(c / a.nlon);
+    const T sj = (T)a.sinth[j], s2 = sj * sj, c2 = (T)1 - s2, c4 = c2 * c2;
+    const T pf = (T)a.p_full[x], ps = (T)a.p_half[c + G * a.nd];
+    const T smax = fmax(pf / ps - sb, (T)0);
+    const T k_v = ((T)a.k_f / day) / ((T)1 - sb) * smax;
+    const T u = (T)a.u[x], v = (T)a.v[x];
+    const T du = -k_v * u, dv = -k_v * v;
+    T dt = -((u + (T)0.5 * du * Dt) * du + (v + (T)0.5 * dv * Dt) * dv) / (T)a.cp;
+    const T pn = pf / (T)1.0e5;
+    T teq = ((T)315 - (T)a.dT_y * s2 - (T)a.dtheta_z * c2 * log(pn)) * pow(pn, (T)a.kappa);
+    teq = fmax(teq, (T)200);
+    const T ka = (T)a.k_a / day, ks = (T)a.k_s / day;
+    const T k_t = ka + (ks - ka) / ((T)1 - sb) * smax * c4;
+    dt -= k_t * ((T)a.t[x] - teq);
+    a.du[x] = (double)du;
+    a.dv[x] = (double)dv;
+    a.t_eq[x] = (double)teq;
+    a.dt[x] = (double)dt;
+  }
+}
+}  // namespace
+
+extern "C" int jgcm_hs_forcing(jgcm_model* md, int Dt, const double* grid_u, const double* grid_v,
+                               const double* grid_p_half, const double* grid_p_full, const double* grid_t,
+                               double* grid_du, double* grid_dv, double* grid_t_eq, double* grid_dt) {
+  JG_ARG(md, "NULL model");
+  JG_ARG(md->P.kind == JGCM_HELD_SUAREZ, "HS_Forcing! needs a Held-Suarez model (its physics parameters)");
+  JG_ARG(Dt > 0, "Δt must be positive");
+  JG_ARG(grid_u && grid_v && grid_p_half && grid_p_full && grid_t && grid_du && grid_dv && grid_t_eq && grid_dt,
+         "NULL array");
+  jgcm_mesh* m = md->mesh;
+  const size_t G = (size_t)m->nlon * m->nlat, n = G * md->nd, nh = G * (md->nd + 1);
+  double* buf = nullptr;
+  JG_CUDA(cudaMalloc(&buf, (8 * n + nh) * sizeof(double)));
+  int st = JGCM_OK;
+  auto cp = [&](cudaError_t e) {
+    if (e != cudaSuccess && st == JGCM_OK) {
+      set_error("HS_Forcing! staging: %s", cudaGetErrorString(e));
+      st = JGCM_E_CUDA;
+    }
+  };
+  HSForcingArgs a;
+  double* d = buf;
+  a.u = d;
+  a.v = d + n;
+  a.p_full = d + 2 * n;
+  a.t = d + 3 * n;
+  a.du = d + 4 * n;
+  a.dv = d + 5 * n;
+  a.t_eq = d + 6 * n;
+  a.dt = d + 7 * n;
+  a.p_half = d + 8 * n;
+  a.sinth = m->d_sinth;
+  cp(cudaMemcpyAsync((void*)a.u, grid_u, n * 8, cudaMemcpyHostToDevice, m->stream));
+  cp(cudaMemcpyAsync((void*)a.v, grid_v, n * 8, cudaMemcpyHostToDevice, m->stream));
+  cp(cudaMemcpyAsync((void*)a.p_full, grid_p_full, n * 8, cudaMemcpyHostToDevice, m->stream));
+  cp(cudaMemcpyAsync((void*)a.t, grid_t, n * 8, cudaMemcpyHostToDevice, m->stream));
+  cp(cudaMemcpyAsync((void*)a.p_half, grid_p_half, nh * 8, cudaMemcpyHostToDevice, m->stream));
+  a.nlon = m->nlon;
+  a.nlat = m->nlat;
+  a.nd = md->nd;
+  a.Dt = Dt;
+  a.sigma_b = md->P.sigma_b;
+  a.k_f = md->P.k_f;
+  a.k_a = md->P.k_a;
+  a.k_s = md->P.k_s;
+  a.dT_y = md->P.dT_y;
+  a.dtheta_z = md->P.dtheta_z;
+  a.kappa = md->P.kappa;
+  a.cp = md->cp_air;
+  if (st == JGCM_OK) {
+    int nb = (int)std::min<size_t>((n + 255) / 256, 4 * 152);
+    if (is_fp64(m)) k_hs_forcing<double><<<nb, 256, 0, m->stream>>>(a);
+    else k_hs_forcing<float><<<nb, 256, 0, m->stream>>>(a);
+    mark(m->stream);
+    cp(cudaGetLastError());
+  }
+  cp(cudaMemcpyAsync(grid_du, a.du, n * 8, cudaMemcpyDeviceToHost, m->stream));
+  cp(cudaMemcpyAsync(grid_dv, a.dv, n * 8, cudaMemcpyDeviceToHost, m->stream));
+  cp(cudaMemcpyAsync(grid_t_eq, a.t_eq, n * 8, cudaMemcpyDeviceToHost, m->stream));
+  cp(cudaMemcpyAsync(grid_dt, a.dt, n * 8, cudaMemcpyDeviceToHost, m->stream));
+  cp(cudaStreamSynchronize(m->stream));
+  cudaFree(buf);
+  return st;
+}
+
 // Spectral_Initialize_Fields! (Spectral_Dynamics.jl:372-449) on the device.
 extern "C" int jgcm_spectral_initialize_fields(jgcm_model* md, const double* grid_t_pert, int vorticity_seed) {
   JG_ARG(md, "NULL model");

@@ -87,6 +87,7 @@ def lib():
         "jgcm_model_update_init_step": (I, [P]),
         "jgcm_spectral_initialize_fields": (I, [P, P, I]),
         "jgcm_model_semi_implicit": (I, [P, C.c_char_p, P, Lg, C.POINTER(Lg)]),
+        "jgcm_hs_forcing": (I, [P, I, P, P, P, P, P, P, P, P, P]),
         "jgcm_model_time_steps": (I, [P, I, C.POINTER(C.c_float)]),
         "jgcm_model_launches_per_step": (I, [P, C.POINTER(I)]),
         "jgcm_model_kernel_times": (I, [P, I, C.POINTER(C.c_float), I, C.POINTER(I)]),
@@ -386,3 +387,15 @@ class Model:
 
 def set_device(device: int) -> None:
     _check(lib().jgcm_set_device(int(device)))
+
+
+def HS_Forcing(model, dt, grid_u, grid_v, grid_p_half, grid_p_full, grid_t, grid_du, grid_dv, grid_t_eq, grid_dt):
+    """HS_Forcing! (HS_Forcing.jl:1-130) on host arrays; the physics parameters (the reference's
+    physics Dict) and c_p (Atmo_Data) come from the model.  Outputs are written in place."""
+    ins = [np.asfortranarray(a, dtype=np.float64) for a in (grid_u, grid_v, grid_p_half, grid_p_full, grid_t)]
+    assert ins[0].shape == ins[1].shape == ins[3].shape == ins[4].shape, "u, v, p_full, t shapes differ"
+    assert ins[2].shape == ins[0].shape[:2] + (ins[0].shape[2] + 1,), "p_half must have nd+1 levels"
+    for a in (grid_du, grid_dv, grid_t_eq, grid_dt):
+        assert a.shape == ins[0].shape and a.dtype == np.float64, "output shape/dtype"
+    _check(lib().jgcm_hs_forcing(model._h, int(dt), *[_ptr(a) for a in ins], _ptr(grid_du), _ptr(grid_dv),
+                                 _ptr(grid_t_eq), _ptr(grid_dt)))

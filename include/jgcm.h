@@ -150,6 +150,14 @@ int jgcm_model_init_step(jgcm_model* model, int* init_step);
 /* Update_Init_Step!  Time_Integrator.jl:40-43 / Semi_Implicit.jl:182-188: leave the forward
  * init-step mode without stepping (e.g. when restarting from a saved leapfrog state). */
 int jgcm_model_update_init_step(jgcm_model* model);
+/* HS_Forcing!  HS_Forcing.jl:1-130 (Rayleigh_Damping! :101-130, energy-conserving heating :21-26,
+ * Newtonian_Damping! :37-97) on host arrays in the reference layout: u, v, t, p_full, du, dv,
+ * t_eq, dt are [nλ,nθ,nd], p_half is [nλ,nθ,nd+1]; Δt in seconds as Get_Δt returns it.  The
+ * physics parameters and c_p come from the model (the reference's physics Dict and Atmo_Data);
+ * computed in the mesh precision. */
+int jgcm_hs_forcing(jgcm_model* model, int dt, const double* grid_u, const double* grid_v,
+                    const double* grid_p_half, const double* grid_p_full, const double* grid_t, double* grid_du,
+                    double* grid_dv, double* grid_t_eq, double* grid_dt);
 /* Spectral_Initialize_Fields!  Spectral_Dynamics.jl:372-449.  grid_t_pert (nullable,
  * grid[nd]) is added to the isothermal init_t before the spectral filtering;
  * vorticity_seed != 0 keeps the reference's deterministic vorticity seed (:401-409). */

@@ -84,6 +84,8 @@ typedef struct {
 } om_params;
 
 om_model* om_model_create(om_mesh* mesh, const om_params* p);
+void om_hs_forcing(om_model* md, int Dt, const double* u, const double* v, const double* p_half,
+                   const double* p_full, const double* t, double* du, double* dv, double* t_eq, double* dtt);
 void om_model_destroy(om_model* md);
 /* named Dyn_Data fields ("spe_vor_c", "grid_u_p", ... , "grid_h_eq"); returns element count
  * (doubles) or -1 */

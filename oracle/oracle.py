@@ -74,6 +74,7 @@ def lib():
             "om_model_step": (I, [P, I]),
             "om_spectral_initialize_fields": (I, [P, P, I]),
             "om_model_semi_implicit": (L, [P, C.c_char_p, P, L]),
+            "om_hs_forcing": (None, [P, I, P, P, P, P, P, P, P, P, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(_lib, name)
@@ -295,3 +296,12 @@ class Model:
         if name == "wave_matrix":
             return out.reshape((nd, nd, -1), order="F")
         return out
+
+
+def HS_Forcing(model, dt, grid_u, grid_v, grid_p_half, grid_p_full, grid_t, grid_du, grid_dv, grid_t_eq, grid_dt):
+    """HS_Forcing! (HS_Forcing.jl:1-130); the physics parameters come from the model."""
+    ins = [np.asfortranarray(a, dtype=np.float64) for a in (grid_u, grid_v, grid_p_half, grid_p_full, grid_t)]
+    for a in (grid_du, grid_dv, grid_t_eq, grid_dt):
+        _ptr(a)
+    lib().om_hs_forcing(model._h, int(dt), *[_ptr(a) for a in ins], _ptr(grid_du), _ptr(grid_dv), _ptr(grid_t_eq),
+                        _ptr(grid_dt))

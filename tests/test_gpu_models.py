@@ -141,3 +141,35 @@ def test_held_suarez_conservation(jg, orc):
     ps1 = jg.Area_Weighted_Global_Mean(gm, gmod.get("grid_ps_c"))
     assert abs(ps1 - ps0) / ps0 < 1e-6
     assert np.isfinite(gmod.get("grid_t_c")).all()
+
+
+def _hs_forcing_inputs(mesh, seed=11):
+    """Grid inputs of HS_Forcing! on even-sigma levels: winds ~20 m/s, T ~ 220-300 K,
+    ps ~ 1e5 Pa +- 2 %, p_half = b_k ps, p_full between the half levels."""
+    rng = np.random.default_rng(seed)
+    nlon, nlat, nd = mesh.nlon, mesh.nlat, mesh.nd
+    u = np.asfortranarray(20.0 * rng.standard_normal((nlon, nlat, nd)))
+    v = np.asfortranarray(10.0 * rng.standard_normal((nlon, nlat, nd)))
+    t = np.asfortranarray(220.0 + 80.0 * rng.random((nlon, nlat, nd)))
+    ps = 1.0e5 * (1.0 + 0.02 * rng.standard_normal((nlon, nlat)))
+    b = np.linspace(0.0, 1.0, nd + 1)
+    p_half = np.asfortranarray(ps[:, :, None] * b[None, None, :])
+    p_full = np.asfortranarray(0.5 * (p_half[:, :, :-1] + p_half[:, :, 1:]))
+    return u, v, p_half, p_full, t
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-13), ("fp32", 2e-5)])
+def test_hs_forcing_entry_point(jg, orc, prec, tol):
+    """HS_Forcing! (HS_Forcing.jl:1-130) through its own entry point, against the oracle."""
+    gm, om, gmod, omod = _pair(jg, orc, "hs_t21l20", prec)
+    ins = _hs_forcing_inputs(gm)
+    outs = {}
+    for key, backend, model in (("gpu", jg, gmod), ("orc", orc, omod)):
+        o = [np.zeros_like(ins[0]) for _ in range(4)]
+        backend.HS_Forcing(model, 2400, *ins, *o)
+        outs[key] = o
+    for name, a, b in zip(("du", "dv", "t_eq", "dt"), outs["gpu"], outs["orc"]):
+        assert np.isfinite(a).all()
+        assert configs.rel_l2(a, b) < tol, (name, configs.rel_l2(a, b))
+    with pytest.raises(AssertionError):
+        jg.HS_Forcing(gmod, 0, *ins, *[np.zeros_like(ins[0]) for _ in range(4)])

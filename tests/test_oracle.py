@@ -222,3 +222,40 @@ def test_generator_is_reproducible():
     assert np.array_equal(a, b)
     assert abs(a.mean()) < 0.1 and abs(a.std() - 1) < 0.1
     assert configs.splitmix64(0, 1)[0] == np.uint64(0xE220A8397B1DCDAF)  # published SplitMix64(0) output
+
+
+def test_hs_forcing_restatement(orc):
+    """The oracle's HS_Forcing! against a numpy restatement of HS_Forcing.jl:1-130."""
+    from jgcm import configs as cf
+
+    name = "hs_t21l10"
+    mesh = cf.make_mesh(orc, name)
+    md = orc.Model(mesh, cf.PARAMS[name])
+    P = cf.PARAMS[name]
+    rng = np.random.default_rng(3)
+    nlon, nlat, nd = mesh.nlon, mesh.nlat, mesh.nd
+    u, v = 20.0 * rng.standard_normal((3, nlon, nlat, nd))[:2]
+    t = 220.0 + 80.0 * rng.random((nlon, nlat, nd))
+    ps = 1.0e5 * (1.0 + 0.02 * rng.standard_normal((nlon, nlat)))
+    p_half = ps[:, :, None] * np.linspace(0.0, 1.0, nd + 1)[None, None, :]
+    p_full = 0.5 * (p_half[:, :, :-1] + p_half[:, :, 1:])
+    u, v, t, p_half, p_full = (np.asfortranarray(a) for a in (u, v, t, p_half, p_full))
+    outs = [np.zeros_like(u, order="F") for _ in range(4)]
+    Dt = 2400
+    orc.HS_Forcing(md, Dt, u, v, p_half, p_full, t, *outs)
+    day, sb = 86400.0, P["sigma_b"]
+    sigma = p_full / p_half[:, :, -1:]
+    smax = np.maximum(0.0, sigma - sb)
+    k_v = P["k_f"] / day / (1.0 - sb) * smax
+    du, dv = -k_v * u, -k_v * v
+    cp = P["rdgas"] / P["kappa"]
+    dt = -((u + 0.5 * du * Dt) * du + (v + 0.5 * dv * Dt) * dv) / cp
+    s, _ = orc.compute_gaussian(nlat)
+    s2 = (s * s)[None, :, None]
+    c2 = 1.0 - s2
+    pn = p_full / 1.0e5
+    teq = np.maximum(200.0, (315.0 - P["dT_y"] * s2 - P["dtheta_z"] * c2 * np.log(pn)) * pn ** P["kappa"])
+    ka, ks = P["k_a"] / day, P["k_s"] / day
+    dt = dt - (ka + (ks - ka) / (1.0 - sb) * smax * c2 * c2) * (t - teq)
+    for a, b in zip(outs, (du, dv, teq, dt)):
+        assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(b))
