@@ -108,6 +108,7 @@ enum S2GOp { S2G_PLAIN = 0, S2G_DLAM = 1, S2G_DTH = 2, S2G_UCOS = 3, S2G_VCOS = 
 struct S2GGroup {
   const void* a;  // spectral field (MNK, L levels)
   const void* b;  // second field (UCOS/VCOS: divergence; a = vorticity)
+  double shift;   // PLAIN: subtracted from the real part of mode (0,0) before the synthesis
   int op, L, col0, pad;
 };
 struct S2GPlan {
@@ -120,6 +121,7 @@ struct GridOutGroup {
   void* dst;
   void* dst2;      // EPI_EXP2: exp(x)
   const void* ps;  // EPI_DIVCOS_MULPS: surface pressure grid [nlat][nlon]
+  double shift;    // EPI_EXP2: x is ln(ps) - shift: dst = x + shift, dst2 = exp(x) exp(shift)
   int epi, L, col0, pad;
 };
 struct IFFTPlan {
@@ -169,6 +171,20 @@ struct G2SPlan {
   SpecOutGroup g[JGCM_MAX_GROUPS];
 };
 
+// Tensor-core (tcgen05) Legendre path of the TF32x3 / BF16x3 precision modes: the tables as
+// hi + lo operand images in the no-swizzle K-major layout of the MMA, one block per m (synthesis)
+// or per (m, K chunk) (analysis), fetched whole by bulk async copies.
+struct TcTables {
+  int on;                  // this mesh runs its Legendre contractions on the tensor cores
+  int esz, per, kstep;     // operand bytes, elements per 16-byte row of a core matrix, MMA K
+  int KC;                  // analysis K chunk (folded latitudes per pass)
+  int Nq;                  // synthesis MMA N = 2 * nh (even | odd parity)
+  int NpM;                 // analysis MMA N for m = 0: roundup(ns + 1, 16); channel stride in TMEM
+  size_t smem_s2g, smem_g2s;
+  unsigned char *s2g, *g2s_p, *g2s_a;          // images (synthesis P; analysis PW/2; alpha CA, CB)
+  long long *s2g_off, *g2s_p_off, *g2s_a_off;  // device [N+1]: byte offset of each m's image
+};
+
 }  // namespace jgcm
 
 // ------------------------------------------------------------------------------------------
@@ -181,6 +197,8 @@ struct jgcm_mesh {
   double* d_ref2;  // scratch for reference-layout 2-D tables on export
   jgcm::TableStore<double> t64;
   jgcm::TableStore<float> t32;
+  jgcm::TcTables tc;
+  unsigned int* d_status;  // device error bits of the tensor-core kernels (bounded waits that gave up)
   // workspace
   int Cmax;
   void* d_fbuf;       // Fourier buffer [m][j][c] complex T, c < Cmax
@@ -228,6 +246,14 @@ int apply_laplacian(jgcm_mesh* m, void* d_spec, int L, cudaStream_t st);
 int area_mean(jgcm_mesh* m, const void* d_grid, double* d_out, cudaStream_t st);
 template <typename T>
 Tables<T> tables(const jgcm_mesh* m);
+
+// legendre_tc.cu
+int tc_check_mesh(int N, int ns, int nlat, int precision);  // JGCM_OK if the tensor path fits
+int tc_tables_build(jgcm_mesh* m);
+void tc_tables_free(jgcm_mesh* m);
+int launch_s2g_legendre_tc(jgcm_mesh* m, const S2GPlan& sp, void* fbuf, cudaStream_t st);
+int launch_g2s_legendre_tc(jgcm_mesh* m, const G2SPlan& gp, int Cin, cudaStream_t st);
+int tc_status(jgcm_mesh* m);  // reads and clears the device error bits
 
 // mesh.cu
 int mesh_build_tables(jgcm_mesh* m);

@@ -251,9 +251,10 @@ static void mesh_free(jgcm_mesh* m) {
   if (!m) return;
   void* ps[] = {m->d_sinth, m->d_wts, m->d_costh, m->d_qnm, m->d_dqnm, m->d_ref2, m->d_fbuf, m->d_stage,
                 m->d_grid[0], m->d_grid[1], m->d_grid[2], m->d_grid[3], m->d_spec[0], m->d_spec[1], m->d_spec[2],
-                m->d_spec[3], m->d_red, m->d_counter};
+                m->d_spec[3], m->d_red, m->d_counter, m->d_status};
   for (auto p : ps)
     if (p) cudaFree(p);
+  tc_tables_free(m);
   free_store(m->t64);
   free_store(m->t32);
   if (m->stream) cudaStreamDestroy(m->stream);
@@ -277,6 +278,10 @@ extern "C" int jgcm_mesh_create(int num_fourier, int num_spherical, int nlat, in
                                             precision == JGCM_FP64 ? sizeof(double) : sizeof(float));
     JG_ARG(need <= kSmemBudget, "mesh too large for the shared-memory tiling: %zu bytes > %zu per block", need,
            kSmemBudget);
+    if (precision == JGCM_TF32X3 || precision == JGCM_BF16X3) {
+      int st = tc_check_mesh(num_fourier, num_spherical, nlat, precision);
+      if (st != JGCM_OK) return st;
+    }
   }
   jgcm_mesh* m = new jgcm_mesh();  // value-initialised: all pointers start NULL
   m->N = num_fourier;
@@ -334,6 +339,9 @@ extern "C" int jgcm_mesh_create(int num_fourier, int num_spherical, int nlat, in
   MCHK(cuda(cudaMalloc(&m->d_counter, 64 * sizeof(unsigned int)), "alloc counter"));
   MCHK(cuda(cudaMemset(m->d_counter, 0, 64 * sizeof(unsigned int)), "memset"));
   MCHK(cuda(cudaMalloc(&m->d_ref2, T3 * 8), "alloc ref2"));
+  MCHK(cuda(cudaMalloc(&m->d_status, sizeof(unsigned int)), "alloc status"));
+  MCHK(cuda(cudaMemset(m->d_status, 0, sizeof(unsigned int)), "memset"));
+  if (precision == JGCM_TF32X3 || precision == JGCM_BF16X3) MCHK(tc_tables_build(m));
 #undef MCHK
   m->refs = 1;
   cudaGetDevice(&m->device);

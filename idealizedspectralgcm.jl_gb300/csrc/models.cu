@@ -76,6 +76,8 @@ namespace {
 
 int lvl(const jgcm_model* md, int which) { return (md->rot + which) % 3; }  // 0 = p, 1 = c, 2 = n
 
+constexpr double kLnPsRef = 11.512925464970229;  // ln 1e5
+
 // ------------------------------------------------------------------------------------------
 // warp scans over levels (lanes >= nd hold zero)
 template <typename R>
@@ -181,6 +183,7 @@ struct HSColArgs {
   const T *u_p, *v_p, *t_p, *ps_p, *ps_c, *u_c, *v_c, *t_c, *div, *vor, *dlps, *dtps, *dlT, *dtT, *geopots, *coriolis,
       *sinj, *cosj;
   T *ducos, *dvcos, *dtg, *energy, *dlnps, *t_eq;
+  const V2<T>* t_spec;  // spe_t_c: its (0,0) modes are the level means of T
   const double* wts;
   double *partials, *scalars;
   unsigned* counter;
@@ -280,11 +283,16 @@ __global__ void __launch_bounds__(256) k_hs_column(HSColArgs<T> a, const VertCoe
     // M_{k+1/2}: -sum_{r<=k} D_r + B_{k+1/2} sum_r D_r ; zero at top and surface
     const T Mhi = (lane + 1 <= nd - 1) ? -incl + tot * (T)vc.bk[k + 1] : (T)0;
     const T Mlo = shfl_up1(Mhi, lane, (T)0);
-    // ---- Compute_Geopotential! (Press_And_Geopot.jl:71-111), bottom-up
-    const T term = act ? R * t * dlnp : (T)0;
+    // ---- Compute_Geopotential! (Press_And_Geopot.jl:71-111), bottom-up, on T - T0_k with T0_k the
+    // level's area mean: the T0 part, sum_{r>k} R T0_r dlnp_r + R T0_k dlnp_p, is a per-level constant
+    // (dlnp_r, r >= 1, and dlnp_p do not vary horizontally), so it only moves the (0,0) mode of the
+    // energy, which the Laplacian annihilates (eig = 0), while the rounding of the scan shrinks with
+    // |T - T0| instead of |T| (it feeds the divergence tendency through the Laplacian)
+    const T tdev = t - (T)a.t_spec[k].x;
+    const T term = act ? R * tdev * dlnp : (T)0;
     const T rs = rscan_incl<T>(term, lane);           // sum_{r>=k} term_r
-    const T ghalf_hi = gs + shfl_dn1(rs, lane, nd, (T)0);  // Phi_{k+1/2}
-    const T gfull = ghalf_hi + R * t * dlnp_p;
+    const T ghalf_hi = gs + shfl_dn1(rs, lane, nd, (T)0);  // Phi_{k+1/2} - const_k
+    const T gfull = ghalf_hi + R * tdev * dlnp_p;
     // ---- Vert_Advection! (second_centered_wts) for u, v, T
     const T dp_m = shfl_up1(dp, lane, (T)1);
     const T wlo = dp_m / (dp_m + dp);
@@ -1169,6 +1177,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   a.energy = (T*)md->g_energy;
   a.dlnps = (T*)md->g_dlnps;
   a.t_eq = (T*)md->grid_t_eq;
+  a.t_spec = (const V2<T>*)md->spe_t[c];
   a.wts = m->d_wts;
   a.partials = md->d_partials;
   a.scalars = md->d_scalars;
@@ -1255,7 +1264,10 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   s2.g[2] = sg(S2G_UCOS, md->spe_vor[n], md->spe_div[n], nd, 2 * nd);
   s2.g[3] = sg(S2G_VCOS, md->spe_vor[n], md->spe_div[n], nd, 3 * nd);
   s2.g[4] = sg(S2G_PLAIN, md->spe_t[n], nullptr, nd, 4 * nd);
+  // ln ps is synthesised as ln ps - ln 1e5 (mode (0,0) shifted; P_00 = 1) and shifted back in the
+  // epilogue, so its rounding scales with |ln(ps / 1e5)| ~ 0.02 instead of ln ps ~ 11.5
   s2.g[5] = sg(S2G_PLAIN, md->spe_lnps[n], nullptr, 1, 5 * nd);
+  s2.g[5].shift = kLnPsRef;
   IFFTPlan i2;
   memset(&i2, 0, sizeof(i2));
   i2.ng = 6;
@@ -1266,6 +1278,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   i2.g[3] = og(EPI_DIVCOS, md->grid_v[n], nd, 3 * nd);
   i2.g[4] = og(EPI_NONE, md->grid_t[n], nd, 4 * nd);
   i2.g[5] = og(EPI_EXP2, md->grid_lnps, 1, 5 * nd, md->grid_ps[n]);
+  i2.g[5].shift = kLnPsRef;
   JG_TRY(launch_s2g<T>(m, s2, i2, st));
   // 6. mass and energy fixers
   CorrArgs<T> ca;

@@ -18,25 +18,16 @@
 // wavenumbers (gradient, Compute_Gradient_Cos! :655-692; ucos/vcos, :517-580).
 #include <cmath>
 #include <mutex>
+#include <type_traits>
 
 #include "jgcm_internal.cuh"
+#include "transform_ops.cuh"
 
 namespace jgcm {
-
-template <typename T>
-using V2 = typename C2<T>::t;
 
 __host__ __device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 __device__ __forceinline__ int brev(int x, int logn) { return (int)(__brev((unsigned)x) >> (32 - logn)); }
 
-template <typename G>
-__device__ __forceinline__ const G& group_of(const G* g, int ng, int c, int* k) {
-  int i = 0;
-  for (; i < ng - 1; i++)
-    if (c < g[i].col0 + g[i].L) break;
-  *k = c - g[i].col0;
-  return g[i];
-}
 
 // ------------------------------------------------------------------------------------------
 // Complex radix-2 DIT stages over `nrow` rows of length h = nlon/2 held as (re, im) in shared
@@ -91,60 +82,7 @@ __global__ void __launch_bounds__(256) k_s2g_legendre(S2GPlan plan, Tables<T> tb
     if (c < C) {
       int k;
       const S2GGroup& g = group_of(plan.g, plan.ng, c, &k);
-      const int L = g.L;
-      const V* a = (const V*)g.a;
-      switch (g.op) {
-        case S2G_PLAIN:
-          x = a[(mrow + n) * L + k];
-          break;
-        case S2G_DLAM: {  // coef_dlam .* (i h)
-          T cf = tb.dlam[mrow + n];
-          V h = a[(mrow + n) * L + k];
-          x.x = cf * (-h.y);
-          x.y = cf * h.x;
-        } break;
-        case S2G_DTH: {  // coef_dthp h_{n+1} + coef_dthm h_{n-1}
-          if (n <= ns - 1) {
-            T cp = tb.dthp[mrow + n];
-            V h = a[(mrow + n + 1) * L + k];
-            x.x = cp * h.x;
-            x.y = cp * h.y;
-          }
-          if (n - 1 >= m) {
-            T cm = tb.dthm[mrow + n];
-            V h = a[(mrow + n - 1) * L + k];
-            x.x = x.x + cm * h.x;
-            x.y = x.y + cm * h.y;
-          }
-        } break;
-        case S2G_UCOS:
-        case S2G_VCOS: {
-          // ucos = uvc (i div) - uvm vor_{n-1} - uvp vor_{n+1}
-          // vcos = uvc (i vor) + uvm div_{n-1} + uvp div_{n+1}
-          const V* vor = a;
-          const V* dv = (const V*)g.b;
-          const bool u = g.op == S2G_UCOS;
-          const V* ic = u ? dv : vor;  // term multiplied by i*uvc
-          const V* nb = u ? vor : dv;  // neighbour terms
-          T sg = u ? (T)-1 : (T)1;
-          T cc = tb.uvc[mrow + n];
-          V z = ic[(mrow + n) * L + k];
-          x.x = cc * (-z.y);
-          x.y = cc * z.x;
-          if (n - 1 >= m) {
-            T cm = tb.uvm[mrow + n];
-            V h = nb[(mrow + n - 1) * L + k];
-            x.x = x.x + sg * (cm * h.x);
-            x.y = x.y + sg * (cm * h.y);
-          }
-          if (n + 1 <= ns) {
-            T cp = tb.uvp[mrow + n];
-            V h = nb[(mrow + n + 1) * L + k];
-            x.x = x.x + sg * (cp * h.x);
-            x.y = x.y + sg * (cp * h.y);
-          }
-        } break;
-      }
+      x = s2g_input<T>(g, tb, m, n, ns, mrow, k);
     }
     X[i] = x;
   }
@@ -241,8 +179,8 @@ __global__ void __launch_bounds__(256) k_ifft(IFFTPlan plan, Tables<T> tb, const
         dst[idx] = x / tb.cosj[j];
         break;
       case EPI_EXP2:
-        dst[idx] = x;
-        ((T*)g.dst2)[idx] = exp(x);
+        dst[idx] = x + (T)g.shift;
+        ((T*)g.dst2)[idx] = exp(x) * (T)exp(g.shift);
         break;
       case EPI_DIVCOS_MULPS:
         dst[idx] = (x / tb.cosj[j]) * ((const T*)g.ps)[(size_t)j * nlon + t];
@@ -330,32 +268,6 @@ __global__ void __launch_bounds__(256) k_fft(FFTPlan plan, Tables<T> tb, V2<T>* 
     o.y = (ei + (tc * oi - ts * orr)) * scale;
     F[((size_t)mm * nlat + j) * C + c] = o;
   }
-}
-
-// ------------------------------------------------------------------------------------------
-// Fused spectral time stepping used by the G2S epilogues (Time_Integrator.jl:58-101).
-template <typename T>
-__device__ __forceinline__ void damp_leapfrog(const StepParams& sp, T d, T& dq, T qp, T& qc, T& qn) {
-  const T r = (T)sp.robert;
-  const int Dt = sp.dt;
-  if (sp.init_step) {
-    dq = (dq - qc * d) / ((T)1.0 + (T)Dt * d);
-    qn = qc + (T)Dt * dq;
-    qc = qc + r * ((T)-1.0 * qc + qn);
-  } else {
-    dq = (dq - qp * d) / ((T)1.0 + (T)(2 * Dt) * d);
-    qc = qc + r * (qp - (T)2 * qc);
-    qn = qp + (T)(2 * Dt) * dq;
-    qc = qc + r * qn;
-  }
-}
-
-template <typename T>
-__device__ __forceinline__ void leapfrog_c(const StepParams& sp, T d, V2<T>& dq, V2<T> qp, V2<T>& qc, V2<T>& qn,
-                                           bool damp) {
-  if (!damp) d = 0;
-  damp_leapfrog<T>(sp, d, dq.x, qp.x, qc.x, qn.x);
-  damp_leapfrog<T>(sp, d, dq.y, qp.y, qc.y, qn.y);
 }
 
 // Fourier -> spectral: Gaussian quadrature per m.  grid (ceil(Cout/CT), N+1), 256 threads.
@@ -493,76 +405,7 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
         break;
     }
     if (q != 0) continue;
-    const T eig = tb.eig[mrow + n];
-    switch (g.op) {
-      case G2S_PLAIN:
-        ((V*)g.dst)[sidx] = r0;
-        break;
-      case G2S_VOR:
-        ((V*)g.dst)[sidx] = r0;
-        break;
-      case G2S_DIV: {
-        V v = r0;
-        if (g.colE >= 0) {  // - laplacian(G2S(E) + extra)
-          V e = r2;
-          if (g.extra) {
-            V x = ((const V*)g.extra)[sidx];
-            e.x = e.x + x.x;
-            e.y = e.y + x.y;
-          }
-          v.x = v.x - eig * e.x;
-          v.y = v.y - eig * e.y;
-        }
-        ((V*)g.dst)[sidx] = v;
-      } break;
-      case G2S_BARO: {  // Barotropic_Dynamics.jl:31-36: vorticity tendency, damping, leapfrog
-        V dq = r0;
-        V* qc = (V*)g.qc[0];
-        const V* qp = (const V*)g.qp[0];
-        V c0 = qc[sidx], p0 = qp[sidx], n0;
-        T d = ((const T*)plan.sp.damping)[mrow + n];
-        leapfrog_c<T>(plan.sp, d, dq, p0, c0, n0, true);
-        qc[sidx] = c0;
-        ((V*)g.dst)[sidx] = n0;
-      } break;
-      case G2S_SW: {  // Shallow_Water_Dynamics.jl:133-165
-        // slots: 0 = du cos, 1 = dv cos, 2 = kinetic energy, 3 = dh
-        V dvor = r0;
-        V ddiv = r1;
-        V kin = r2;
-        V dh = r3;
-        const V* hc_p = (const V*)g.qc[2];
-        V hc = hc_p[sidx], hp = ((const V*)g.qp[2])[sidx];
-        V dc = ((const V*)g.qc[1])[sidx], dp = ((const V*)g.qp[1])[sidx];
-        // spe_energy = (kin + h_c) * eig ; ddiv -= spe_energy
-        ddiv.x = ddiv.x - eig * (kin.x + hc.x);
-        ddiv.y = ddiv.y - eig * (kin.y + hc.y);
-        // Implicit_Correction! (SW) :25-54
-        const T h0 = (T)plan.sp.h0;
-        const T Dt = plan.sp.init_step ? (T)plan.sp.dt : (T)(2.0 * plan.sp.dt);
-        ddiv.x = ddiv.x + eig * (hc.x - hp.x);
-        ddiv.y = ddiv.y + eig * (hc.y - hp.y);
-        dh.x = dh.x + h0 * (dc.x - dp.x);
-        dh.y = dh.y + h0 * (dc.y - dp.y);
-        const T mu = (T)plan.sp.implicit_coef * Dt, mu2 = mu * mu;
-        const T den = (T)1.0 - mu2 * eig * h0;
-        ddiv.x = (ddiv.x - mu * eig * dh.x) / den;
-        ddiv.y = (ddiv.y - mu * eig * dh.y) / den;
-        dh.x = dh.x - mu * h0 * ddiv.x;
-        dh.y = dh.y - mu * h0 * ddiv.y;
-        const T d = ((const T*)plan.sp.damping)[mrow + n];
-        V vc = ((V*)g.qc[0])[sidx], vp = ((const V*)g.qp[0])[sidx], vn, dn, hn;
-        leapfrog_c<T>(plan.sp, d, dvor, vp, vc, vn, true);
-        leapfrog_c<T>(plan.sp, d, ddiv, dp, dc, dn, true);
-        leapfrog_c<T>(plan.sp, d, dh, hp, hc, hn, true);
-        ((V*)g.qc[0])[sidx] = vc;
-        ((V*)g.qc[1])[sidx] = dc;
-        ((V*)g.qc[2])[sidx] = hc;
-        ((V*)g.dst)[sidx] = vn;
-        ((V*)g.dst2)[sidx] = dn;
-        ((V*)g.dst3)[sidx] = hn;
-      } break;
-    }
+    g2s_store<T>(plan, g, tb, mrow, n, sidx, r0, r1, r2, r3);
   }
 }
 
@@ -595,11 +438,15 @@ static int launch_s2g_into(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, 
   JG_TRY(configure_smem<T>());
   Tables<T> tb = tables<T>(m);
   const int nh = m->nh, ct = s2g_ct(nh);
-  size_t sm1 = align16((size_t)(m->ns + 1) * nh * sizeof(T)) + (size_t)(m->ns + 1) * ct * sizeof(V);
-  dim3 g1((sp.C + ct - 1) / ct, m->N + 1);
-  k_s2g_legendre<T><<<g1, 256, sm1, st>>>(sp, tb, fbuf, m->ns, m->nlat, ct);
-  mark(st);
-  JG_CUDA(cudaGetLastError());
+  if (std::is_same<T, float>::value && m->tc.on) {
+    JG_TRY(launch_s2g_legendre_tc(m, sp, fbuf, st));
+  } else {
+    size_t sm1 = align16((size_t)(m->ns + 1) * nh * sizeof(T)) + (size_t)(m->ns + 1) * ct * sizeof(V);
+    dim3 g1((sp.C + ct - 1) / ct, m->N + 1);
+    k_s2g_legendre<T><<<g1, 256, sm1, st>>>(sp, tb, fbuf, m->ns, m->nlat, ct);
+    mark(st);
+    JG_CUDA(cudaGetLastError());
+  }
   const int fc = fft_ct(m->nlon);
   size_t sm2 = align16((size_t)(fc * m->nlon + m->nlon) * sizeof(T)) + (size_t)(m->N + 1) * fc * sizeof(V);
   dim3 g2((ip.C + fc - 1) / fc, m->nlat);
@@ -634,6 +481,7 @@ template <typename T>
 int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp, cudaStream_t st) {
   using V = V2<T>;
   JG_TRY(launch_fft_only<T>(m, fp, st));
+  if (std::is_same<T, float>::value && m->tc.on) return launch_g2s_legendre_tc(m, gp, fp.C, st);
   Tables<T> tb = tables<T>(m);
   const int nh = m->nh, ct = g2s_ct(nh);
   size_t sm = (size_t)8 * ct * nh * sizeof(V);

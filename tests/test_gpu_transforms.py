@@ -1,7 +1,7 @@
 """GPU transforms vs the FP64 oracle, through the C ABI (ctypes).
 
 Tolerances (relative L2 over the whole array): FP64 path 1e-12 (the oracle and the GPU sum in
-different orders); FP32 path 5e-6 for single transforms.
+different orders); FP32 path 5e-6 for single transforms; the tensor-core modes as stated at TOL.
 """
 import numpy as np
 import pytest
@@ -11,7 +11,10 @@ from jgcm import configs
 pytestmark = pytest.mark.gpu
 
 CASES = [(21, 32, 64, 3), (42, 64, 128, 20), (85, 128, 256, 2)]
-TOL = {"fp64": 1e-12, "fp32": 5e-6}
+# tf32x3 / bf16x3: the Legendre contraction on the tensor cores with 3-term split operands
+# (hi*hi + hi*lo + lo*hi, FP32 accumulation); TF32 pairs carry ~21 bits, BF16 pairs ~16
+TOL = {"fp64": 1e-12, "fp32": 5e-6, "tf32x3": 1e-5, "bf16x3": 1e-4}
+PRECS = ["fp64", "fp32", "tf32x3", "bf16x3"]
 
 
 def _meshes(jg, orc, N, nlat, nlon, nd, prec, radius=6371.0e3):
@@ -36,7 +39,7 @@ def _spec(m, nlev, seed, lower=True):
     return np.asfortranarray(s)
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("case", CASES)
 def test_tables(jg, orc, case, prec):
     N, nlat, nlon, nd = case
@@ -50,7 +53,7 @@ def test_tables(jg, orc, case, prec):
         assert configs.rel_l2(getattr(gm, name), getattr(om, name)) < 1e-13, name
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("case", CASES)
 def test_spherical_to_grid(jg, orc, case, prec):
     N, nlat, nlon, nd = case
@@ -63,7 +66,7 @@ def test_spherical_to_grid(jg, orc, case, prec):
         assert configs.rel_l2(a, b) < TOL[prec]
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("case", CASES)
 def test_grid_to_spherical(jg, orc, case, prec):
     N, nlat, nlon, nd = case
@@ -79,7 +82,7 @@ def test_grid_to_spherical(jg, orc, case, prec):
             assert np.all(a[mm, :mm, :] == 0)
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("case", CASES[:2])
 def test_grid_to_fourier(jg, orc, case, prec):
     N, nlat, nlon, nd = case
@@ -92,7 +95,7 @@ def test_grid_to_fourier(jg, orc, case, prec):
     assert configs.rel_l2(f, ref[: N + 1]) < TOL[prec]
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("case", CASES)
 def test_vor_div_uv(jg, orc, case, prec):
     N, nlat, nlon, nd = case
@@ -109,7 +112,7 @@ def test_vor_div_uv(jg, orc, case, prec):
     assert configs.rel_l2(ug, ur) < TOL[prec] and configs.rel_l2(vgg, vrr) < TOL[prec]
 
 
-@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("case", CASES)
 def test_gradients_advection_laplacian(jg, orc, case, prec):
     N, nlat, nlon, nd = case
