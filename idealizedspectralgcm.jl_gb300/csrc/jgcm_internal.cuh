@@ -231,12 +231,15 @@ inline size_t grid_elems(const jgcm_mesh* m, int L) { return (size_t)m->nlon * m
 inline size_t tsize(const jgcm_mesh* m) { return is_fp64(m) ? 8 : 4; }
 
 // transforms.cu
+// fbuf: Fourier buffer of `cap` columns ((N+1) x nlat x cap complex T); NULL = the mesh's own
 template <typename T>
-int launch_s2g(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, cudaStream_t st);
+int launch_s2g(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, cudaStream_t st, void* fbuf = nullptr,
+               int cap = 0);
 template <typename T>
-int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp, cudaStream_t st);
+int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp, cudaStream_t st, void* fbuf = nullptr,
+               int cap = 0);
 template <typename T>
-int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp, cudaStream_t st);
+int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp, cudaStream_t st, void* fbuf = nullptr, int cap = 0);
 int spec_host_to_dev(jgcm_mesh* m, const double* d_host_layout, void* d_native, int L, cudaStream_t st);
 int spec_dev_to_host(jgcm_mesh* m, const void* d_native, double* d_host_layout, int L, cudaStream_t st);
 int grid_host_to_dev(jgcm_mesh* m, const double* d_src, void* d_native, size_t n, cudaStream_t st);
@@ -252,7 +255,7 @@ int tc_check_mesh(int N, int ns, int nlat, int precision);  // JGCM_OK if the te
 int tc_tables_build(jgcm_mesh* m);
 void tc_tables_free(jgcm_mesh* m);
 int launch_s2g_legendre_tc(jgcm_mesh* m, const S2GPlan& sp, void* fbuf, cudaStream_t st);
-int launch_g2s_legendre_tc(jgcm_mesh* m, const G2SPlan& gp, int Cin, cudaStream_t st);
+int launch_g2s_legendre_tc(jgcm_mesh* m, const G2SPlan& gp, int Cin, cudaStream_t st, void* fbuf);
 int tc_status(jgcm_mesh* m);  // reads and clears the device error bits
 
 // mesh.cu

@@ -237,7 +237,14 @@ __global__ void __launch_bounds__(256) k_s2g_tc(S2GPlan plan, Tables<float> tb, 
   __shared__ int issued;
   const int m = blockIdx.y, nh = nlat >> 1, Nq = 2 * nh;
   const int K = ns + 1 - m, Kp = roundup(K, P::kstep);
-  const int C = plan.C, cbase = blockIdx.x * 64;
+  const int C = plan.C;
+  int gi = 0, tile = blockIdx.x;
+  while (gi < plan.ng - 1 && tile >= (plan.g[gi].L + 63) / 64) {
+    tile -= (plan.g[gi].L + 63) / 64;
+    gi++;
+  }
+  const S2GGroup& g = plan.g[gi];
+  const int k0 = tile * 64, ncl = min(64, g.L - k0), cbase = g.col0 + k0;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t sboA = (uint32_t)(Kp / P::per) * 128u, sboB = sboA;
   const size_t opA = (size_t)128 * Kp * sizeof(E), opB = (size_t)Nq * Kp * sizeof(E);
@@ -256,21 +263,29 @@ __global__ void __launch_bounds__(256) k_s2g_tc(S2GPlan plan, Tables<float> tb, 
   if (tid == 0) bulk_load(Bhi, timg + toff[m], (uint32_t)(2 * opB), &bar[0]);
   // prologue: X[row][r] for n = m + r, split into hi / lo
   const size_t mrow = (size_t)m * (ns + 1);
-  for (int i = tid; i < Kp * 64; i += blockDim.x) {
-    const int r = i >> 6, cl = i & 63, c = cbase + cl;
-    float2 x = make_float2(0.f, 0.f);
-    if (r < K && c < C) {
-      int k;
-      const S2GGroup& g = group_of(plan.g, plan.ng, c, &k);
-      x = s2g_input<float>(g, tb, m, m + r, ns, mrow, k);
+  // U items per thread per round: all their loads are issued before any shared-memory store
+  constexpr int U = 4;
+  for (int base = tid; base < Kp * 64; base += U * blockDim.x) {
+    float2 x[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int i = base + u * blockDim.x, r = i >> 6, cl = i & 63;
+      x[u] = make_float2(0.f, 0.f);
+      if (i < Kp * 64 && r < K && cl < ncl) x[u] = s2g_input<float>(g, tb, m, m + r, ns, mrow, k0 + cl);
     }
-    E h, l;
-    split<P>(x.x, h, l);
-    *(E*)(Ahi + cm_off<P>(2 * cl, r, sboA)) = h;
-    *(E*)(Alo + cm_off<P>(2 * cl, r, sboA)) = l;
-    split<P>(x.y, h, l);
-    *(E*)(Ahi + cm_off<P>(2 * cl + 1, r, sboA)) = h;
-    *(E*)(Alo + cm_off<P>(2 * cl + 1, r, sboA)) = l;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int i = base + u * blockDim.x, r = i >> 6, cl = i & 63;
+      if (i < Kp * 64) {
+        E h, l;
+        split<P>(x[u].x, h, l);
+        *(E*)(Ahi + cm_off<P>(2 * cl, r, sboA)) = h;
+        *(E*)(Alo + cm_off<P>(2 * cl, r, sboA)) = l;
+        split<P>(x[u].y, h, l);
+        *(E*)(Ahi + cm_off<P>(2 * cl + 1, r, sboA)) = h;
+        *(E*)(Alo + cm_off<P>(2 * cl + 1, r, sboA)) = l;
+      }
+    }
   }
   fence_async_smem();
   fence_before();
@@ -316,7 +331,7 @@ __global__ void __launch_bounds__(256) k_s2g_tc(S2GPlan plan, Tables<float> tb, 
       float e[8], o[8];
       tmem_ld8(tl + (uint32_t)j0, e);
       tmem_ld8(tl + (uint32_t)(nh + j0), o);
-      if (c < C) {
+      if (cl < ncl) {
 #pragma unroll
         for (int t = 0; t < 8; t++) {
           const int j = j0 + t;
@@ -397,7 +412,14 @@ __global__ void __launch_bounds__(256) k_g2s_tc(G2SPlan plan, Tables<float> tb, 
   __shared__ int flag;
   const int m = blockIdx.y, nh = nlat >> 1;
   const int K = ns + 1 - m, Np = roundup(K, 16) < 16 ? 16 : roundup(K, 16);
-  const int C = plan.C, cbase = blockIdx.x * 64;
+  // tile = 64 consecutive columns of one group (uniform op and channels across the CTA)
+  int gi = 0, tile = blockIdx.x;
+  while (gi < plan.ng - 1 && tile >= (plan.g[gi].L + 63) / 64) {
+    tile -= (plan.g[gi].L + 63) / 64;
+    gi++;
+  }
+  const SpecOutGroup& g = plan.g[gi];
+  const int k0 = tile * 64, ncl = min(64, g.L - k0);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t sbo = (uint32_t)(KC / P::per) * 128u;
   const size_t opA = (size_t)128 * KC * sizeof(E), opB = (size_t)Np * KC * sizeof(E);
@@ -419,94 +441,93 @@ __global__ void __launch_bounds__(256) k_g2s_tc(G2SPlan plan, Tables<float> tb, 
   const size_t mrow = (size_t)m * (ns + 1);
   uint32_t ph0 = 0, ph1 = 0;
   bool ok = true;
-  unsigned started = 0;  // channels whose accumulator holds a first product (thread 0)
-  for (int ch = 0; ch < nchan && ok; ch++) {
-    for (int kind = KIND_ALPHA; kind >= KIND_PLAIN && ok; kind--) {
-      // does any column of this tile contribute (ch, kind)?
-      bool mine = false;
-      if (tid < 64 && cbase + tid < C) {
-        int k, kd, sa, sb;
-        float sg;
-        const SpecOutGroup& g = group_of(plan.g, plan.ng, cbase + tid, &k);
-        mine = chan_spec(g, ch, &kd, &sa, &sb, &sg) && kd == kind;
-      }
-      if (!__syncthreads_or(mine)) continue;
-      const int Kf = (kind == KIND_ALPHA ? 4 : 2) * nh, nch = (Kf + KC - 1) / KC;
-      const unsigned char* img = (kind == KIND_ALPHA ? img_a : img_p) + (kind == KIND_ALPHA ? off_a[m] : off_p[m]);
-      for (int chunk = 0; chunk < nch && ok; chunk++) {
-        if (tid == 0) bulk_load(Bhi, img + (size_t)chunk * 2 * opB, (uint32_t)(2 * opB), &bar[0]);
-        // A[row][kappa]: the folded input of each row's own contraction, zero for other rows
-        for (int i = tid; i < KC * 64; i += blockDim.x) {
-          const int kl = i >> 6, cl = i & 63, c = cbase + cl, kap = chunk * KC + kl;
-          float v0 = 0.f, v1 = 0.f;
-          if (c < C && kap < Kf) {
-            int k, kd, sa, sb;
-            float sg;
-            const SpecOutGroup& g = group_of(plan.g, plan.ng, c, &k);
-            if (chan_spec(g, ch, &kd, &sa, &sb, &sg) && kd == kind) {
-              const int blk = kap / nh, jh = kap - blk * nh;
-              const int slot = (kind == KIND_ALPHA && blk >= 2) ? sb : sa;
-              const int col = slot_col(g, slot) + k;
-              const float2 x = F[((size_t)m * nlat + jh) * Cin + col];
-              const float2 y = F[((size_t)m * nlat + (nlat - 1 - jh)) * Cin + col];
-              const bool sym = (blk & 1) == 0;
-              const float fx = sym ? x.x + y.x : x.x - y.x, fy = sym ? x.y + y.y : x.y - y.y;
-              if (kind == KIND_PLAIN) {
-                v0 = fx;
-                v1 = fy;
-              } else if (blk < 2) {  // i * CA-term: (re, im) <- (-im, re)
-                v0 = -fy;
-                v1 = fx;
-              } else {
-                v0 = sg * fx;
-                v1 = sg * fy;
-              }
-            }
+  for (int ch = 0; ch < 4 && ok; ch++) {
+    int kind, sa, sb;
+    float sg;
+    if (!chan_spec(g, ch, &kind, &sa, &sb, &sg)) continue;
+    const int Kf = (kind == KIND_ALPHA ? 4 : 2) * nh, nch = (Kf + KC - 1) / KC;
+    const unsigned char* img = kind == KIND_ALPHA ? img_a + off_a[m] : img_p + off_p[m];
+    const int colA = slot_col(g, sa) + k0, colB = slot_col(g, sb) + k0;
+    for (int chunk = 0; chunk < nch && ok; chunk++) {
+      if (tid == 0) bulk_load(Bhi, img + (size_t)chunk * 2 * opB, (uint32_t)(2 * opB), &bar[0]);
+      // A[row][kappa]: the folded inputs of this channel's contraction
+      constexpr int U = 8;  // items per thread per round: loads first, then the stores
+      for (int base = tid; base < KC * 64; base += U * blockDim.x) {
+        float2 xs[U], ys[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          const int i = base + u * blockDim.x, kl = i >> 6, cl = i & 63, kap = chunk * KC + kl;
+          xs[u] = ys[u] = make_float2(0.f, 0.f);
+          if (i < KC * 64 && cl < ncl && kap < Kf) {
+            const int blk = kap / nh, jh = kap - blk * nh;
+            const int col = ((kind == KIND_ALPHA && blk >= 2) ? colB : colA) + cl;
+            xs[u] = __ldg(F + ((size_t)m * nlat + jh) * Cin + col);
+            ys[u] = __ldg(F + ((size_t)m * nlat + (nlat - 1 - jh)) * Cin + col);
           }
-          E h, l;
-          split<P>(v0, h, l);
-          *(E*)(Ahi + cm_off<P>(2 * cl, kl, sbo)) = h;
-          *(E*)(Alo + cm_off<P>(2 * cl, kl, sbo)) = l;
-          split<P>(v1, h, l);
-          *(E*)(Ahi + cm_off<P>(2 * cl + 1, kl, sbo)) = h;
-          *(E*)(Alo + cm_off<P>(2 * cl + 1, kl, sbo)) = l;
         }
-        fence_async_smem();
-        fence_before();
-        __syncthreads();
-        fence_after();
-        if (tid == 0) {
-          if (bar_wait(&bar[0], ph0)) {
-            const uint32_t id = idesc<P>(128, Np);
-            const uint32_t d = tmem + (uint32_t)(ch * NpM);
-            const int steps = KC / P::kstep;
-            const uint32_t stepb = (uint32_t)(P::kstep / P::per) * 128u;
-            for (int s = 0; s < steps; s++) {
-              const uint32_t a_hi = su32(Ahi) + s * stepb, a_lo = su32(Alo) + s * stepb;
-              const uint32_t b_hi = su32(Bhi) + s * stepb, b_lo = su32(Blo) + s * stepb;
-              const uint32_t acc = (started >> ch) & 1u;
-              mma<P>(d, sdesc(a_lo, sbo), sdesc(b_hi, sbo), id, acc);
-              started |= 1u << ch;
-              mma<P>(d, sdesc(a_hi, sbo), sdesc(b_lo, sbo), id, 1u);
-              mma<P>(d, sdesc(a_hi, sbo), sdesc(b_hi, sbo), id, 1u);
-            }
-            commit(&bar[1]);
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+        const int i = base + u * blockDim.x, kl = i >> 6, cl = i & 63, kap = chunk * KC + kl;
+        if (i >= KC * 64) continue;
+        float v0 = 0.f, v1 = 0.f;
+        if (cl < ncl && kap < Kf) {
+          const int blk = kap / nh;
+          const float2 x = xs[u], y = ys[u];
+          const bool sym = (blk & 1) == 0;
+          const float fx = sym ? x.x + y.x : x.x - y.x, fy = sym ? x.y + y.y : x.y - y.y;
+          if (kind == KIND_PLAIN) {
+            v0 = fx;
+            v1 = fy;
+          } else if (blk < 2) {  // i * CA-term: (re, im) <- (-im, re)
+            v0 = -fy;
+            v1 = fx;
           } else {
-            atomicOr(status, ST_TABLE_WAIT);
-            flag = 0;
+            v0 = sg * fx;
+            v1 = sg * fy;
           }
         }
-        ph0 ^= 1u;
-        __syncthreads();
-        ok = flag != 0;
-        if (ok && !bar_wait(&bar[1], ph1)) {
-          ok = false;
-          if (lane == 0) atomicOr(status, ST_MMA_WAIT);
+        E h, l;
+        split<P>(v0, h, l);
+        *(E*)(Ahi + cm_off<P>(2 * cl, kl, sbo)) = h;
+        *(E*)(Alo + cm_off<P>(2 * cl, kl, sbo)) = l;
+        split<P>(v1, h, l);
+        *(E*)(Ahi + cm_off<P>(2 * cl + 1, kl, sbo)) = h;
+        *(E*)(Alo + cm_off<P>(2 * cl + 1, kl, sbo)) = l;
         }
-        ph1 ^= 1u;
-        ok = __syncthreads_and(ok);
-        fence_after();
       }
+      fence_async_smem();
+      fence_before();
+      __syncthreads();
+      fence_after();
+      if (tid == 0) {
+        if (bar_wait(&bar[0], ph0)) {
+          const uint32_t id = idesc<P>(128, Np);
+          const uint32_t d = tmem + (uint32_t)(ch * NpM);
+          const int steps = KC / P::kstep;
+          const uint32_t stepb = (uint32_t)(P::kstep / P::per) * 128u;
+          for (int s = 0; s < steps; s++) {
+            const uint32_t a_hi = su32(Ahi) + s * stepb, a_lo = su32(Alo) + s * stepb;
+            const uint32_t b_hi = su32(Bhi) + s * stepb, b_lo = su32(Blo) + s * stepb;
+            mma<P>(d, sdesc(a_lo, sbo), sdesc(b_hi, sbo), id, (chunk > 0 || s > 0) ? 1u : 0u);
+            mma<P>(d, sdesc(a_hi, sbo), sdesc(b_lo, sbo), id, 1u);
+            mma<P>(d, sdesc(a_hi, sbo), sdesc(b_hi, sbo), id, 1u);
+          }
+          commit(&bar[1]);
+        } else {
+          atomicOr(status, ST_TABLE_WAIT);
+          flag = 0;
+        }
+      }
+      ph0 ^= 1u;
+      __syncthreads();
+      ok = flag != 0;
+      if (ok && !bar_wait(&bar[1], ph1)) {
+        ok = false;
+        if (lane == 0) atomicOr(status, ST_MMA_WAIT);
+      }
+      ph1 ^= 1u;
+      ok = __syncthreads_and(ok);
+      fence_after();
     }
   }
   if (!ok && tid == 0) {  // let a copy or MMAs that may still be in flight finish before leaving
@@ -516,14 +537,8 @@ __global__ void __launch_bounds__(256) k_g2s_tc(G2SPlan plan, Tables<float> tb, 
   if (ok) {
     // epilogue: warps 0-3 own the 128 rows; lanes 2c, 2c + 1 hold the two components of column c
     if (warp < 4) {
-      const int row = warp * 32 + lane, cl = row >> 1, reim = row & 1, c = cbase + cl;
+      const int row = warp * 32 + lane, cl = row >> 1, reim = row & 1, k = k0 + cl;
       const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
-      int k = 0, gi = -1;
-      if (c < C) {
-        gi = 0;
-        while (gi < plan.ng - 1 && c >= plan.g[gi].col0 + plan.g[gi].L) gi++;
-        k = c - plan.g[gi].col0;
-      }
       for (int n0 = 0; n0 < Np; n0 += 8) {
         float v[4][8];
 #pragma unroll
@@ -542,9 +557,9 @@ __global__ void __launch_bounds__(256) k_g2s_tc(G2SPlan plan, Tables<float> tb, 
             r[q] = reim ? make_float2(other, mine) : make_float2(mine, other);
           }
           const int n = m + n0 + t;
-          if (gi >= 0 && reim == 0 && n <= ns) {
-            const size_t sidx = (mrow + n) * plan.g[gi].L + k;
-            g2s_store<float>(plan, plan.g[gi], tb, mrow, n, sidx, r[0], r[1], r[2], r[3]);
+          if (cl < ncl && reim == 0 && n <= ns) {
+            const size_t sidx = (mrow + n) * g.L + k;
+            g2s_store<float>(plan, g, tb, mrow, n, sidx, r[0], r[1], r[2], r[3]);
           }
         }
       }
@@ -673,7 +688,9 @@ template <class P>
 static int s2g_tc(jgcm_mesh* m, const S2GPlan& sp, void* fbuf, cudaStream_t st) {
   JG_TRY(tc_configure<P>());
   const TcTables& t = m->tc;
-  dim3 g((sp.C + 63) / 64, m->N + 1);
+  int tiles = 0;
+  for (int i = 0; i < sp.ng; i++) tiles += (sp.g[i].L + 63) / 64;
+  dim3 g(tiles, m->N + 1);
   tc::k_s2g_tc<P><<<g, 256, t.smem_s2g, st>>>(sp, tables<float>(m), t.s2g, t.s2g_off, (float2*)fbuf, m->ns, m->nlat,
                                               m->d_status);
   mark(st);
@@ -682,7 +699,7 @@ static int s2g_tc(jgcm_mesh* m, const S2GPlan& sp, void* fbuf, cudaStream_t st) 
 }
 
 template <class P>
-static int g2s_tc(jgcm_mesh* m, const G2SPlan& gp, int Cin, cudaStream_t st) {
+static int g2s_tc(jgcm_mesh* m, const G2SPlan& gp, int Cin, cudaStream_t st, void* fbuf) {
   JG_TRY(tc_configure<P>());
   const TcTables& t = m->tc;
   int nchan = 1;
@@ -690,9 +707,11 @@ static int g2s_tc(jgcm_mesh* m, const G2SPlan& gp, int Cin, cudaStream_t st) {
     if (gp.g[i].op == G2S_SW) nchan = 4;
     else if (gp.g[i].op == G2S_DIV && gp.g[i].colE >= 0 && nchan < 3) nchan = 3;
   }
-  dim3 g((gp.C + 63) / 64, m->N + 1);
+  int tiles = 0;
+  for (int i = 0; i < gp.ng; i++) tiles += (gp.g[i].L + 63) / 64;
+  dim3 g(tiles, m->N + 1);
   tc::k_g2s_tc<P><<<g, 256, t.smem_g2s, st>>>(gp, tables<float>(m), t.g2s_p, t.g2s_p_off, t.g2s_a, t.g2s_a_off,
-                                              (const float2*)m->d_fbuf, m->ns, m->nlat, Cin, t.KC, t.NpM, nchan,
+                                              (const float2*)fbuf, m->ns, m->nlat, Cin, t.KC, t.NpM, nchan,
                                               m->d_status);
   mark(st);
   JG_CUDA(cudaGetLastError());
@@ -703,8 +722,9 @@ int launch_s2g_legendre_tc(jgcm_mesh* m, const S2GPlan& sp, void* fbuf, cudaStre
   return m->precision == JGCM_TF32X3 ? s2g_tc<tc::TF32x3>(m, sp, fbuf, st) : s2g_tc<tc::BF16x3>(m, sp, fbuf, st);
 }
 
-int launch_g2s_legendre_tc(jgcm_mesh* m, const G2SPlan& gp, int Cin, cudaStream_t st) {
-  return m->precision == JGCM_TF32X3 ? g2s_tc<tc::TF32x3>(m, gp, Cin, st) : g2s_tc<tc::BF16x3>(m, gp, Cin, st);
+int launch_g2s_legendre_tc(jgcm_mesh* m, const G2SPlan& gp, int Cin, cudaStream_t st, void* fbuf) {
+  return m->precision == JGCM_TF32X3 ? g2s_tc<tc::TF32x3>(m, gp, Cin, st, fbuf)
+                                     : g2s_tc<tc::BF16x3>(m, gp, Cin, st, fbuf);
 }
 
 int tc_status(jgcm_mesh* m) {

@@ -48,6 +48,11 @@ struct jgcm_model {
   jgcm_mesh* mesh;
   jgcm_params P;
   int nd, init_step, rot, sw_adv_from_n, steps_done;
+  // ensemble members advanced together: every field holds ne members, member-major (grid level
+  // index e*nd + k, spectral innermost index e*nd + k), so a transform sees L = ne*nd columns
+  int ne, L;
+  void* fbuf;  // Fourier buffer of fcap columns
+  int fcap;
   double cp_air;
   // time-levelled state (index by rotation)
   void *spe_vor[3], *spe_div[3], *spe_lnps[3], *spe_t[3];
@@ -185,8 +190,9 @@ struct HSColArgs {
   T *ducos, *dvcos, *dtg, *energy, *dlnps, *t_eq;
   const V2<T>* t_spec;  // spe_t_c: its (0,0) modes are the level means of T
   const double* wts;
-  double *partials, *scalars;
-  unsigned* counter;
+  double *partials, *scalars;  // per member: partials + e * pstride, scalars + 4 e
+  unsigned* counter;          // per member: counter + e
+  size_t pstride;
   int nd, nlat, nlon, Dt;
   double sigma_b, k_f, k_a, k_s, dT_y, dtheta_z, kappa, rdgas, cp, grav;
 };
@@ -200,10 +206,13 @@ __global__ void __launch_bounds__(256) k_hs_column(HSColArgs<T> a, const VertCoe
   T* tile = (T*)smem;                        // [HS_NIN][nd][HS_CWP]
   T* sgl = tile + HS_NIN * nd * HS_CWP;      // [5][HS_CW]: ps_c, ps_p, dlps, dtps, geopots
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int i0 = blockIdx.x * HS_CW, j = blockIdx.y;
+  const int i0 = blockIdx.x * HS_CW, j = blockIdx.y, e = blockIdx.z;
   const size_t G = (size_t)nlat * nlon, row = (size_t)j * nlon;
+  // member e: its nd levels start at level e*nd, its single-level fields at level e
+  const size_t offL = (size_t)e * nd * G, off1 = (size_t)e * G;
   {
-    const T* in[HS_NIN] = {a.u_p, a.v_p, a.t_p, a.u_c, a.v_c, a.t_c, a.div, a.vor, a.dlT, a.dtT};
+    const T* in[HS_NIN] = {a.u_p + offL, a.v_p + offL, a.t_p + offL, a.u_c + offL, a.v_c + offL,
+                           a.t_c + offL, a.div + offL, a.vor + offL, a.dlT + offL, a.dtT + offL};
     // all HS_NIN loads of one (level, column) are issued back to back before any store
     for (int r = threadIdx.x; r < nd * HS_CW; r += blockDim.x) {
       const int k = r / HS_CW, c = r - k * HS_CW, i = i0 + c;
@@ -215,7 +224,7 @@ __global__ void __launch_bounds__(256) k_hs_column(HSColArgs<T> a, const VertCoe
 #pragma unroll
       for (int f = 0; f < HS_NIN; f++) tile[(f * nd + k) * HS_CWP + c] = x[f];
     }
-    const T* sg[5] = {a.ps_c, a.ps_p, a.dlps, a.dtps, a.geopots};
+    const T* sg[5] = {a.ps_c + off1, a.ps_p + off1, a.dlps + off1, a.dtps + off1, a.geopots + off1};
     for (int q = threadIdx.x; q < 5 * HS_CW; q += blockDim.x) {
       int f = q / HS_CW, c = q - f * HS_CW, i = i0 + c;
       sgl[q] = (i < nlon) ? sg[f][row + i] : (f < 2 ? (T)1 : (T)0);
@@ -288,7 +297,7 @@ __global__ void __launch_bounds__(256) k_hs_column(HSColArgs<T> a, const VertCoe
     // (dlnp_r, r >= 1, and dlnp_p do not vary horizontally), so it only moves the (0,0) mode of the
     // energy, which the Laplacian annihilates (eig = 0), while the rounding of the scan shrinks with
     // |T - T0| instead of |T| (it feeds the divergence tendency through the Laplacian)
-    const T tdev = t - (T)a.t_spec[k].x;
+    const T tdev = t - (T)a.t_spec[e * nd + k].x;
     const T term = act ? R * tdev * dlnp : (T)0;
     const T rs = rscan_incl<T>(term, lane);           // sum_{r>=k} term_r
     const T ghalf_hi = gs + shfl_dn1(rs, lane, nd, (T)0);  // Phi_{k+1/2} - const_k
@@ -329,13 +338,13 @@ __global__ void __launch_bounds__(256) k_hs_column(HSColArgs<T> a, const VertCoe
   }
   __syncthreads();
   {
-    T* out[5] = {a.ducos, a.dvcos, a.dtg, a.energy, a.t_eq};
+    T* out[5] = {a.ducos + offL, a.dvcos + offL, a.dtg + offL, a.energy + offL, a.t_eq + offL};
     const int slot[5] = {0, 1, 2, 8, 9};
     for (int q = threadIdx.x; q < 5 * nd * HS_CW; q += blockDim.x) {
       int o = q / (nd * HS_CW), r = q - o * nd * HS_CW, k = r / HS_CW, c = r - k * HS_CW, i = i0 + c;
       if (i < nlon) out[o][k * G + row + i] = tile[(slot[o] * nd + k) * HS_CWP + c];
     }
-    if (threadIdx.x < HS_CW && i0 + (int)threadIdx.x < nlon) a.dlnps[row + i0 + threadIdx.x] = sgl[threadIdx.x];
+    if (threadIdx.x < HS_CW && i0 + (int)threadIdx.x < nlon) a.dlnps[off1 + row + i0 + threadIdx.x] = sgl[threadIdx.x];
   }
   // ---- block partials for mean_ps_p and mean_energy_p (fixed order)
   if (lane == 0) {
@@ -350,9 +359,10 @@ __global__ void __launch_bounds__(256) k_hs_column(HSColArgs<T> a, const VertCoe
       vals[1] += red[1][q];
     }
   double tot2[2];
-  if (grid_reduce_last<2>(vals, a.partials, a.counter, a.wts, tot2) && threadIdx.x == 0) {
-    a.scalars[0] = tot2[0] / (2.0 * nlon);           // mean_ps_p   (Area_Weighted_Global_Mean)
-    a.scalars[1] = tot2[1] / (2.0 * nlon) / a.grav;  // mean_energy_p (Mass_Weighted_Global_Integral)
+  double* scal = a.scalars + 4 * e;
+  if (grid_reduce_last<2>(vals, a.partials + e * a.pstride, a.counter + e, a.wts, tot2) && threadIdx.x == 0) {
+    scal[0] = tot2[0] / (2.0 * nlon);           // mean_ps_p   (Area_Weighted_Global_Mean)
+    scal[1] = tot2[1] / (2.0 * nlon) / a.grav;  // mean_energy_p (Mass_Weighted_Global_Integral)
   }
 }
 
@@ -370,7 +380,7 @@ struct ImplArgs {
   const double* eig64;      // [m][n]: -n(n+1)/a², FP64
   const double* W;                // [N+1][c][r]
   const int2* pairs;
-  int npairs, nd, ns, N, init_step, dt;
+  int npairs, nd, L, ne, ns, N, init_step, dt;  // spectral innermost index e*nd + k of L = ne*nd
   double xi, ps_ref, kappa, rdgas, robert;
 };
 
@@ -431,11 +441,11 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCo
   const int pid = blockIdx.x * 8 + (threadIdx.x >> 5);
   if (pid >= a.npairs) return;  // whole warp exits together
   const int2 mn = a.pairs[pid];
-  const int m = mn.x, n = mn.y, nd = a.nd;
+  const int m = mn.x, n = mn.y, nd = a.nd, e = blockIdx.y;
   const bool act = lane < nd;
   const int k = act ? lane : 0;
   const size_t row = (size_t)m * (a.ns + 1) + n;
-  const size_t s = row * nd + k;
+  const size_t s = row * a.L + (size_t)e * nd + k, s1 = row * a.ne + e;  // nd-level and single-level index
   auto ld = [&](const V2<T>* p) -> C {
     if (!act) return C{0, 0};
     V2<T> v = p[s];
@@ -443,7 +453,7 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCo
   };
   C ddiv = ld(a.ddiv), dtt = ld(a.dtend), dvor = ld(a.dvor);
   C divp = ld(a.div_p), divc = ld(a.div_c), tp = ld(a.t_p), tc = ld(a.t_c), vorp = ld(a.vor_p), vorc = ld(a.vor_c);
-  V2<T> l0 = a.dlnps[row], lp0 = a.lnps_p[row], lc0 = a.lnps_c[row];
+  V2<T> l0 = a.dlnps[s1], lp0 = a.lnps_p[s1], lc0 = a.lnps_c[s1];
   C dl = {(R)l0.x, (R)l0.y}, lp = {(R)lp0.x, (R)lp0.y}, lc = {(R)lc0.x, (R)lc0.y};
   const R xi = (R)a.xi, rpsr = (R)(1.0 / a.ps_ref), xipsr = (R)(a.xi / a.ps_ref), eig = (R)a.eig64[row];
   const R kap = (R)a.kappa, Rg = (R)a.rdgas;
@@ -514,8 +524,8 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCo
     lf<R>(ini, Dt, rob, (R)0, (R)1, dl.x, lp.x, lc.x, ln.x);
     lf<R>(ini, Dt, rob, (R)0, (R)1, dl.y, lp.y, lc.y, ln.y);
     V2<T> o;
-    o.x = (T)ln.x; o.y = (T)ln.y; a.lnps_n[row] = o;
-    o.x = (T)lc.x; o.y = (T)lc.y; a.lnps_c[row] = o;
+    o.x = (T)ln.x; o.y = (T)ln.y; a.lnps_n[s1] = o;
+    o.x = (T)lc.x; o.y = (T)lc.y; a.lnps_c[s1] = o;
   }
 }
 
@@ -528,8 +538,9 @@ struct CorrArgs {
   const T *u_n, *v_n, *t_n, *ps_n;
   V2<T>*lnps_n, *t_spec_n;
   const double* wts;
-  double *partials, *scalars;
+  double *partials, *scalars;  // per member as in HSColArgs
   unsigned* counter;
+  size_t pstride;
   int nd, nlat, nlon, do_mass, do_energy;
   double cp, grav;
 };
@@ -542,14 +553,16 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   // folded across level groups and columns in FP64 in a fixed order
   constexpr int KS = 8;
   const int i = blockIdx.x * 32 + (threadIdx.x & 31), ks = threadIdx.x >> 5, j = blockIdx.y, nd = a.nd;
+  const int e = blockIdx.z;  // member
   const bool act = i < a.nlon;
   const size_t G = (size_t)a.nlat * a.nlon, col = (size_t)j * a.nlon + (act ? i : 0);
+  const size_t offL = (size_t)e * nd * G, off1 = (size_t)e * G;
   __shared__ T part[2][KS][32];
   T ea = 0, eb = 0;
   if (act) {
     const T cp = (T)a.cp;
     for (int k = ks; k < nd; k += KS) {
-      size_t x = (size_t)k * G + col;
+      size_t x = offL + (size_t)k * G + col;
       T u = a.u_n[x], v = a.v_n[x], t = a.t_n[x];
       T E = (T)0.5 * (u * u + v * v) + cp * t;
       ea += E * (T)vc.dak[k];
@@ -567,7 +580,7 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
       sa += (double)part[0][q][c];
       sb += (double)part[1][q][c];
     }
-    const double ps = act ? (double)a.ps_n[col] : 0.0;
+    const double ps = act ? (double)a.ps_n[off1 + col] : 0.0;
     sb *= ps;
     vals[0] = warp_sum(ps);
     vals[1] = warp_sum(sa);
@@ -575,42 +588,44 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   }
   double tot3[3];
   __shared__ double fc[2];
-  if (grid_reduce_last<3>(vals, a.partials, a.counter, a.wts, tot3)) {
+  double* scal = a.scalars + 4 * e;
+  if (grid_reduce_last<3>(vals, a.partials + e * a.pstride, a.counter + e, a.wts, tot3)) {
     if (threadIdx.x == 0) {
       double two_n = 2.0 * a.nlon;
-      double mean_ps_p = a.scalars[0], mean_energy_p = a.scalars[1];
+      double mean_ps_p = scal[0], mean_energy_p = scal[1];
       double factor = 1.0, corr = 0.0;
       if (a.do_mass) {
         double mean_ps_n = tot3[0] / two_n;
         factor = mean_ps_p / mean_ps_n;
-        V2<T> l = a.lnps_n[0];  // spe_lnps_n[1,1,1] += log(factor)  (P_00 = 1)
+        V2<T> l = a.lnps_n[e];  // spe_lnps_n[1,1,1] += log(factor)  (P_00 = 1)
         l.x = (T)((double)l.x + log(factor));
-        a.lnps_n[0] = l;
+        a.lnps_n[e] = l;
       }
       if (a.do_energy) {
         // Δp_k = Δa_k + Δb_k (factor ps_n): the mass correction enters linearly
         double mean_energy_n = (tot3[1] + factor * tot3[2]) / two_n / a.grav;
         corr = a.grav * (mean_energy_p - mean_energy_n) / (a.cp * mean_ps_p);
       }
-      a.scalars[2] = factor;
-      a.scalars[3] = corr;
+      scal[2] = factor;
+      scal[3] = corr;
       fc[1] = corr;
     }
     __syncthreads();
     if (a.do_energy && (int)threadIdx.x < nd) {  // spe_t_n[1,1,:] .+= temperature_correction
-      V2<T> tt = a.t_spec_n[threadIdx.x];
+      V2<T> tt = a.t_spec_n[e * nd + threadIdx.x];
       tt.x = (T)((double)tt.x + fc[1]);
-      a.t_spec_n[threadIdx.x] = tt;
+      a.t_spec_n[e * nd + threadIdx.x] = tt;
     }
   }
 }
 
 template <typename T>
-__global__ void k_hs_corr_apply(T* t_n, T* ps_n, const double* scalars, size_t nt, size_t nps) {
-  const T factor = (T)scalars[2], corr = (T)scalars[3];
+__global__ void k_hs_corr_apply(T* t_n, T* ps_n, const double* scalars, size_t nt, size_t nps, size_t memL,
+                                size_t mem1) {
+  // member of element q: q / memL for the nd-level T, q / mem1 for ps
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nt; q += (size_t)gridDim.x * blockDim.x) {
-    t_n[q] = t_n[q] + corr;
-    if (q < nps) ps_n[q] = ps_n[q] * factor;
+    t_n[q] = t_n[q] + (T)scalars[4 * (q / memL) + 3];
+    if (q < nps) ps_n[q] = ps_n[q] * (T)scalars[4 * (q / mem1) + 2];
   }
 }
 
@@ -850,7 +865,7 @@ void model_free(jgcm_model* md) {
                 md->spe_zero, md->spe_dvor, md->spe_ddiv, md->spe_dlnps, md->spe_dt, md->g_dlps, md->g_dtps,
                 md->g_dlT, md->g_dtT, md->g_ducos, md->g_dvcos, md->g_dt, md->g_energy, md->g_dlnps, md->g_diag,
                 md->coriolis, md->damping, md->dfac[0], md->dfac[1], md->d_W, md->d_pairs, md->d_partials,
-                md->d_scalars, md->d_counter, md->d_vc};
+                md->d_scalars, md->d_counter, md->d_vc, md->fbuf};
   for (auto p : ps)
     if (p) cudaFree(p);
   delete[] md->div_mat;
@@ -891,12 +906,21 @@ int build_wave(jgcm_model* md) {
   return JGCM_OK;
 }
 
+// FP64 block partials per member: the column kernel folds 2 sums over its (nlon/8) x nlat blocks,
+// the fixer kernel 3 sums over (nlon/32) x nlat blocks
+size_t partial_stride(const jgcm_mesh* m) {
+  size_t a = (size_t)2 * ((m->nlon + HS_CW - 1) / HS_CW) * m->nlat, b = (size_t)3 * ((m->nlon + 31) / 32) * m->nlat;
+  return a > b ? a : b;
+}
+
 int model_alloc(jgcm_model* md) {
   jgcm_mesh* m = md->mesh;
-  const int nd = md->nd, N = m->N, ns = m->ns;
+  const int nd = md->nd, N = m->N, ns = m->ns, ne = md->ne, L = md->L;
   const size_t ts = tsize(m);
-  const size_t S = spec_elems(m, nd) * 2 * ts, S1 = spec_elems(m, 1) * 2 * ts;
-  const size_t G = grid_elems(m, nd) * ts, G1 = grid_elems(m, 1) * ts;
+  const size_t S = spec_elems(m, L) * 2 * ts, S1 = spec_elems(m, ne) * 2 * ts;
+  const size_t G = grid_elems(m, L) * ts, G1 = grid_elems(m, ne) * ts;
+  md->fcap = (5 * nd + 2) * ne;
+  JG_TRY(alloc(&md->fbuf, (size_t)(N + 1) * m->nlat * md->fcap * 2 * ts));
   for (int i = 0; i < 3; i++) {
     JG_TRY(alloc(&md->spe_vor[i], S));
     JG_TRY(alloc(&md->spe_div[i], S));
@@ -925,10 +949,9 @@ int model_alloc(jgcm_model* md) {
   md->npairs = (int)pairs.size();
   JG_TRY(alloc((void**)&md->d_pairs, pairs.size() * sizeof(int2)));
   JG_CUDA(cudaMemcpy(md->d_pairs, pairs.data(), pairs.size() * sizeof(int2), cudaMemcpyHostToDevice));
-  int nblk = ((m->nlon + 7) / 8) * m->nlat;
-  JG_TRY(alloc((void**)&md->d_partials, (size_t)3 * nblk * 8));
-  JG_TRY(alloc((void**)&md->d_scalars, 16 * 8));
-  JG_TRY(alloc((void**)&md->d_counter, 16 * sizeof(unsigned)));
+  JG_TRY(alloc((void**)&md->d_partials, (size_t)ne * partial_stride(m) * 8));
+  JG_TRY(alloc((void**)&md->d_scalars, (size_t)4 * ne * 8));
+  JG_TRY(alloc((void**)&md->d_counter, (size_t)ne * sizeof(unsigned)));
   int nt = (N + 1) * (ns + 1);
   JG_TRY(alloc(&md->dfac[0], (size_t)nt * ts));
   JG_TRY(alloc(&md->dfac[1], (size_t)nt * ts));
@@ -1005,7 +1028,7 @@ int s2g_final_uv(jgcm_model* md, int lev_n, cudaStream_t st);
 template <typename T>
 int step_barotropic(jgcm_model* md, cudaStream_t st) {
   jgcm_mesh* m = md->mesh;
-  const int nd = md->nd, p = lvl(md, 0), c = lvl(md, 1), n = lvl(md, 2);
+  const int nd = md->L, p = lvl(md, 0), c = lvl(md, 1), n = lvl(md, 2);
   FFTPlan fp;
   memset(&fp, 0, sizeof(fp));
   fp.ng = 2;
@@ -1026,7 +1049,7 @@ int step_barotropic(jgcm_model* md, cudaStream_t st) {
   gp.g[0] = og2(G2S_BARO, md->spe_vor[n], nd, 0, nd, 0, -1);  // A = δv cos, B = δu cos
   gp.g[0].qc[0] = md->spe_vor[c];
   gp.g[0].qp[0] = md->spe_vor[p];
-  JG_TRY(launch_g2s<T>(m, fp, gp, st));
+  JG_TRY(launch_g2s<T>(m, fp, gp, st, md->fbuf, md->fcap));
   S2GPlan sp;
   memset(&sp, 0, sizeof(sp));
   sp.ng = 3;
@@ -1041,7 +1064,7 @@ int step_barotropic(jgcm_model* md, cudaStream_t st) {
   ip.g[0] = og(EPI_NONE, md->grid_vor, nd, 0);
   ip.g[1] = og(EPI_DIVCOS, md->grid_u[n], nd, nd);
   ip.g[2] = og(EPI_DIVCOS, md->grid_v[n], nd, 2 * nd);
-  JG_TRY(launch_s2g<T>(m, sp, ip, st));
+  JG_TRY(launch_s2g<T>(m, sp, ip, st, md->fbuf, md->fcap));
   return JGCM_OK;
 }
 
@@ -1051,37 +1074,37 @@ int step_barotropic(jgcm_model* md, cudaStream_t st) {
 template <typename T>
 int step_shallow_water(jgcm_model* md, cudaStream_t st) {
   jgcm_mesh* m = md->mesh;
-  const int p = lvl(md, 0), c = lvl(md, 1), n = lvl(md, 2);
+  const int p = lvl(md, 0), c = lvl(md, 1), n = lvl(md, 2), E = md->ne;
   const void* h_adv = md->sw_adv_from_n ? md->spe_lnps[n] : md->spe_lnps[c];
   S2GPlan sp;
   memset(&sp, 0, sizeof(sp));
   sp.ng = 2;
-  sp.C = 2;
-  sp.g[0] = sg(S2G_DLAM, h_adv, nullptr, 1, 0);
-  sp.g[1] = sg(S2G_DTH, h_adv, nullptr, 1, 1);
+  sp.C = 2 * E;
+  sp.g[0] = sg(S2G_DLAM, h_adv, nullptr, E, 0 * E);
+  sp.g[1] = sg(S2G_DTH, h_adv, nullptr, E, 1 * E);
   IFFTPlan ip;
   memset(&ip, 0, sizeof(ip));
   ip.ng = 2;
-  ip.C = 2;
-  ip.g[0] = og(EPI_DIVCOS, md->g_dlps, 1, 0);
-  ip.g[1] = og(EPI_DIVCOS, md->g_dtps, 1, 1);
-  JG_TRY(launch_s2g<T>(m, sp, ip, st));
+  ip.C = 2 * E;
+  ip.g[0] = og(EPI_DIVCOS, md->g_dlps, E, 0 * E);
+  ip.g[1] = og(EPI_DIVCOS, md->g_dtps, E, 1 * E);
+  JG_TRY(launch_s2g<T>(m, sp, ip, st, md->fbuf, md->fcap));
   FFTPlan fp;
   memset(&fp, 0, sizeof(fp));
   fp.ng = 4;
-  fp.C = 4;
+  fp.C = 4 * E;
   fp.kappa_m = md->P.kappa_m;
   fp.kappa_t = md->P.kappa_t;
   fp.coriolis = md->coriolis;
-  fp.g[0] = ig(PRO_FLUXU, md->grid_u[c], 1, 0);
+  fp.g[0] = ig(PRO_FLUXU, md->grid_u[c], E, 0 * E);
   fp.g[0].s1 = md->grid_v[c];
   fp.g[0].s2 = md->grid_vor;
-  fp.g[1] = ig(PRO_FLUXV, md->grid_u[c], 1, 1);
+  fp.g[1] = ig(PRO_FLUXV, md->grid_u[c], E, 1 * E);
   fp.g[1].s1 = md->grid_v[c];
   fp.g[1].s2 = md->grid_vor;
-  fp.g[2] = ig(PRO_KIN, md->grid_u[c], 1, 2);
+  fp.g[2] = ig(PRO_KIN, md->grid_u[c], E, 2 * E);
   fp.g[2].s1 = md->grid_v[c];
-  fp.g[3] = ig(PRO_SWH, md->grid_ps[c], 1, 3);
+  fp.g[3] = ig(PRO_SWH, md->grid_ps[c], E, 3 * E);
   fp.g[3].s1 = md->grid_u[c];
   fp.g[3].s2 = md->grid_v[c];
   fp.g[3].s3 = md->g_dlps;
@@ -1091,9 +1114,9 @@ int step_shallow_water(jgcm_model* md, cudaStream_t st) {
   G2SPlan gp;
   memset(&gp, 0, sizeof(gp));
   gp.ng = 1;
-  gp.C = 1;
+  gp.C = E;
   gp.sp = step_params(md);
-  gp.g[0] = og2(G2S_SW, md->spe_vor[n], 1, 0, 0, 1, 2, 3);
+  gp.g[0] = og2(G2S_SW, md->spe_vor[n], E, 0, 0, E, 2 * E, 3 * E);
   gp.g[0].dst2 = md->spe_div[n];
   gp.g[0].dst3 = md->spe_lnps[n];
   gp.g[0].qc[0] = md->spe_vor[c];
@@ -1102,26 +1125,26 @@ int step_shallow_water(jgcm_model* md, cudaStream_t st) {
   gp.g[0].qp[0] = md->spe_vor[p];
   gp.g[0].qp[1] = md->spe_div[p];
   gp.g[0].qp[2] = md->spe_lnps[p];
-  JG_TRY(launch_g2s<T>(m, fp, gp, st));
+  JG_TRY(launch_g2s<T>(m, fp, gp, st, md->fbuf, md->fcap));
   S2GPlan sp2;
   memset(&sp2, 0, sizeof(sp2));
   sp2.ng = 5;
-  sp2.C = 5;
-  sp2.g[0] = sg(S2G_PLAIN, md->spe_vor[n], nullptr, 1, 0);
-  sp2.g[1] = sg(S2G_PLAIN, md->spe_div[n], nullptr, 1, 1);
-  sp2.g[2] = sg(S2G_PLAIN, md->spe_lnps[n], nullptr, 1, 2);
-  sp2.g[3] = sg(S2G_UCOS, md->spe_vor[n], md->spe_div[n], 1, 3);
-  sp2.g[4] = sg(S2G_VCOS, md->spe_vor[n], md->spe_div[n], 1, 4);
+  sp2.C = 5 * E;
+  sp2.g[0] = sg(S2G_PLAIN, md->spe_vor[n], nullptr, E, 0 * E);
+  sp2.g[1] = sg(S2G_PLAIN, md->spe_div[n], nullptr, E, 1 * E);
+  sp2.g[2] = sg(S2G_PLAIN, md->spe_lnps[n], nullptr, E, 2 * E);
+  sp2.g[3] = sg(S2G_UCOS, md->spe_vor[n], md->spe_div[n], E, 3 * E);
+  sp2.g[4] = sg(S2G_VCOS, md->spe_vor[n], md->spe_div[n], E, 4 * E);
   IFFTPlan ip2;
   memset(&ip2, 0, sizeof(ip2));
   ip2.ng = 5;
-  ip2.C = 5;
-  ip2.g[0] = og(EPI_NONE, md->grid_vor, 1, 0);
-  ip2.g[1] = og(EPI_NONE, md->grid_div, 1, 1);
-  ip2.g[2] = og(EPI_NONE, md->grid_ps[n], 1, 2);
-  ip2.g[3] = og(EPI_DIVCOS, md->grid_u[n], 1, 3);
-  ip2.g[4] = og(EPI_DIVCOS, md->grid_v[n], 1, 4);
-  JG_TRY(launch_s2g<T>(m, sp2, ip2, st));
+  ip2.C = 5 * E;
+  ip2.g[0] = og(EPI_NONE, md->grid_vor, E, 0 * E);
+  ip2.g[1] = og(EPI_NONE, md->grid_div, E, 1 * E);
+  ip2.g[2] = og(EPI_NONE, md->grid_ps[n], E, 2 * E);
+  ip2.g[3] = og(EPI_DIVCOS, md->grid_u[n], E, 3 * E);
+  ip2.g[4] = og(EPI_DIVCOS, md->grid_v[n], E, 4 * E);
+  JG_TRY(launch_s2g<T>(m, sp2, ip2, st, md->fbuf, md->fcap));
   return JGCM_OK;
 }
 
@@ -1129,26 +1152,26 @@ int step_shallow_water(jgcm_model* md, cudaStream_t st) {
 template <typename T>
 int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   jgcm_mesh* m = md->mesh;
-  const int nd = md->nd, p = lvl(md, 0), c = lvl(md, 1), n = lvl(md, 2);
+  const int nd = md->nd, L = md->L, E = md->ne, p = lvl(md, 0), c = lvl(md, 1), n = lvl(md, 2);
   const int Dt = md->init_step ? md->P.dt : 2 * md->P.dt;
   // 1. gradients of lnps_c (-> ∇ps = ∇lnps * ps) and of T_c
   S2GPlan sp;
   memset(&sp, 0, sizeof(sp));
   sp.ng = 4;
-  sp.C = 2 + 2 * nd;
-  sp.g[0] = sg(S2G_DLAM, md->spe_lnps[c], nullptr, 1, 0);
-  sp.g[1] = sg(S2G_DTH, md->spe_lnps[c], nullptr, 1, 1);
-  sp.g[2] = sg(S2G_DLAM, md->spe_t[c], nullptr, nd, 2);
-  sp.g[3] = sg(S2G_DTH, md->spe_t[c], nullptr, nd, 2 + nd);
+  sp.C = 2 * E + 2 * L;
+  sp.g[0] = sg(S2G_DLAM, md->spe_lnps[c], nullptr, E, 0);
+  sp.g[1] = sg(S2G_DTH, md->spe_lnps[c], nullptr, E, E);
+  sp.g[2] = sg(S2G_DLAM, md->spe_t[c], nullptr, L, 2 * E);
+  sp.g[3] = sg(S2G_DTH, md->spe_t[c], nullptr, L, 2 * E + L);
   IFFTPlan ip;
   memset(&ip, 0, sizeof(ip));
   ip.ng = 4;
-  ip.C = 2 + 2 * nd;
-  ip.g[0] = og(EPI_DIVCOS_MULPS, md->g_dlps, 1, 0, nullptr, md->grid_ps[c]);
-  ip.g[1] = og(EPI_DIVCOS_MULPS, md->g_dtps, 1, 1, nullptr, md->grid_ps[c]);
-  ip.g[2] = og(EPI_DIVCOS, md->g_dlT, nd, 2);
-  ip.g[3] = og(EPI_DIVCOS, md->g_dtT, nd, 2 + nd);
-  JG_TRY(launch_s2g<T>(m, sp, ip, st));
+  ip.C = 2 * E + 2 * L;
+  ip.g[0] = og(EPI_DIVCOS_MULPS, md->g_dlps, E, 0, nullptr, md->grid_ps[c]);
+  ip.g[1] = og(EPI_DIVCOS_MULPS, md->g_dtps, E, E, nullptr, md->grid_ps[c]);
+  ip.g[2] = og(EPI_DIVCOS, md->g_dlT, L, 2 * E);
+  ip.g[3] = og(EPI_DIVCOS, md->g_dtT, L, 2 * E + L);
+  JG_TRY(launch_s2g<T>(m, sp, ip, st, md->fbuf, md->fcap));
   // 2. physics + grid dynamics (one warp per column)
   Tables<T> tb = tables<T>(m);
   HSColArgs<T> a;
@@ -1196,7 +1219,8 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   a.rdgas = md->P.rdgas;
   a.cp = md->cp_air;
   a.grav = md->P.grav;
-  dim3 gcol((m->nlon + HS_CW - 1) / HS_CW, m->nlat);
+  a.pstride = partial_stride(m);
+  dim3 gcol((m->nlon + HS_CW - 1) / HS_CW, m->nlat, E);
   const size_t smcol = ((size_t)HS_NIN * nd * HS_CWP + 5 * HS_CW) * sizeof(T);
   k_hs_column<T><<<gcol, 256, smcol, st>>>(a, md->d_vc);
   mark(st);
@@ -1206,21 +1230,21 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   FFTPlan fp;
   memset(&fp, 0, sizeof(fp));
   fp.ng = 5;
-  fp.C = 4 * nd + 1;
-  fp.g[0] = ig(PRO_NONE, md->g_ducos, nd, 0);
-  fp.g[1] = ig(PRO_NONE, md->g_dvcos, nd, nd);
-  fp.g[2] = ig(PRO_NONE, md->g_dt, nd, 2 * nd);
-  fp.g[3] = ig(PRO_NONE, md->g_energy, nd, 3 * nd);
-  fp.g[4] = ig(PRO_NONE, md->g_dlnps, 1, 4 * nd);
+  fp.C = 4 * L + E;
+  fp.g[0] = ig(PRO_NONE, md->g_ducos, L, 0);
+  fp.g[1] = ig(PRO_NONE, md->g_dvcos, L, L);
+  fp.g[2] = ig(PRO_NONE, md->g_dt, L, 2 * L);
+  fp.g[3] = ig(PRO_NONE, md->g_energy, L, 3 * L);
+  fp.g[4] = ig(PRO_NONE, md->g_dlnps, E, 4 * L);
   G2SPlan gp;
   memset(&gp, 0, sizeof(gp));
   gp.ng = 4;
-  gp.C = 3 * nd + 1;
-  gp.g[0] = og2(G2S_VOR, md->spe_dvor, nd, 0, nd, 0, -1);
-  gp.g[1] = og2(G2S_DIV, md->spe_ddiv, nd, nd, 0, nd, 3 * nd);
-  gp.g[2] = og2(G2S_PLAIN, md->spe_dt, nd, 2 * nd, 2 * nd, -1, -1);
-  gp.g[3] = og2(G2S_PLAIN, md->spe_dlnps, 1, 3 * nd, 4 * nd, -1, -1);
-  JG_TRY(launch_g2s<T>(m, fp, gp, st));
+  gp.C = 3 * L + E;
+  gp.g[0] = og2(G2S_VOR, md->spe_dvor, L, 0, L, 0, -1);
+  gp.g[1] = og2(G2S_DIV, md->spe_ddiv, L, L, 0, L, 3 * L);
+  gp.g[2] = og2(G2S_PLAIN, md->spe_dt, L, 2 * L, 2 * L, -1, -1);
+  gp.g[3] = og2(G2S_PLAIN, md->spe_dlnps, E, 3 * L, 4 * L, -1, -1);
+  JG_TRY(launch_g2s<T>(m, fp, gp, st, md->fbuf, md->fcap));
   // 4. semi-implicit correction, damping, leapfrog (FP64, warp per mode)
   ImplArgs<T> ia;
   memset(&ia, 0, sizeof(ia));
@@ -1240,6 +1264,8 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ia.pairs = md->d_pairs;
   ia.npairs = md->npairs;
   ia.nd = nd;
+  ia.L = L;
+  ia.ne = E;
   ia.ns = m->ns;
   ia.N = m->N;
   ia.init_step = md->init_step;
@@ -1251,35 +1277,35 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ia.robert = md->P.robert_coef;
   // vertical algebra in the state precision (FP64 algebra on the FP32 path measured no more
   // accurate: its error is set by FP32 storage); the wave-matrix solve is FP64 in both
-  k_hs_implicit<T, T><<<(md->npairs + 7) / 8, 256, 0, st>>>(ia, md->d_vc);
+  k_hs_implicit<T, T><<<dim3((md->npairs + 7) / 8, E), 256, 0, st>>>(ia, md->d_vc);
   mark(st);
   JG_CUDA(cudaGetLastError());
   // 5. back to the grid: vor, div, u, v, T, lnps (+ ps = exp(lnps))
   S2GPlan s2;
   memset(&s2, 0, sizeof(s2));
   s2.ng = 6;
-  s2.C = 5 * nd + 1;
-  s2.g[0] = sg(S2G_PLAIN, md->spe_vor[n], nullptr, nd, 0);
-  s2.g[1] = sg(S2G_PLAIN, md->spe_div[n], nullptr, nd, nd);
-  s2.g[2] = sg(S2G_UCOS, md->spe_vor[n], md->spe_div[n], nd, 2 * nd);
-  s2.g[3] = sg(S2G_VCOS, md->spe_vor[n], md->spe_div[n], nd, 3 * nd);
-  s2.g[4] = sg(S2G_PLAIN, md->spe_t[n], nullptr, nd, 4 * nd);
+  s2.C = 5 * L + E;
+  s2.g[0] = sg(S2G_PLAIN, md->spe_vor[n], nullptr, L, 0);
+  s2.g[1] = sg(S2G_PLAIN, md->spe_div[n], nullptr, L, L);
+  s2.g[2] = sg(S2G_UCOS, md->spe_vor[n], md->spe_div[n], L, 2 * L);
+  s2.g[3] = sg(S2G_VCOS, md->spe_vor[n], md->spe_div[n], L, 3 * L);
+  s2.g[4] = sg(S2G_PLAIN, md->spe_t[n], nullptr, L, 4 * L);
   // ln ps is synthesised as ln ps - ln 1e5 (mode (0,0) shifted; P_00 = 1) and shifted back in the
   // epilogue, so its rounding scales with |ln(ps / 1e5)| ~ 0.02 instead of ln ps ~ 11.5
-  s2.g[5] = sg(S2G_PLAIN, md->spe_lnps[n], nullptr, 1, 5 * nd);
+  s2.g[5] = sg(S2G_PLAIN, md->spe_lnps[n], nullptr, E, 5 * L);
   s2.g[5].shift = kLnPsRef;
   IFFTPlan i2;
   memset(&i2, 0, sizeof(i2));
   i2.ng = 6;
-  i2.C = 5 * nd + 1;
-  i2.g[0] = og(EPI_NONE, md->grid_vor, nd, 0);
-  i2.g[1] = og(EPI_NONE, md->grid_div, nd, nd);
-  i2.g[2] = og(EPI_DIVCOS, md->grid_u[n], nd, 2 * nd);
-  i2.g[3] = og(EPI_DIVCOS, md->grid_v[n], nd, 3 * nd);
-  i2.g[4] = og(EPI_NONE, md->grid_t[n], nd, 4 * nd);
-  i2.g[5] = og(EPI_EXP2, md->grid_lnps, 1, 5 * nd, md->grid_ps[n]);
+  i2.C = 5 * L + E;
+  i2.g[0] = og(EPI_NONE, md->grid_vor, L, 0);
+  i2.g[1] = og(EPI_NONE, md->grid_div, L, L);
+  i2.g[2] = og(EPI_DIVCOS, md->grid_u[n], L, 2 * L);
+  i2.g[3] = og(EPI_DIVCOS, md->grid_v[n], L, 3 * L);
+  i2.g[4] = og(EPI_NONE, md->grid_t[n], L, 4 * L);
+  i2.g[5] = og(EPI_EXP2, md->grid_lnps, E, 5 * L, md->grid_ps[n]);
   i2.g[5].shift = kLnPsRef;
-  JG_TRY(launch_s2g<T>(m, s2, i2, st));
+  JG_TRY(launch_s2g<T>(m, s2, i2, st, md->fbuf, md->fcap));
   // 6. mass and energy fixers
   CorrArgs<T> ca;
   memset(&ca, 0, sizeof(ca));
@@ -1294,19 +1320,21 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ca.scalars = md->d_scalars;
   ca.counter = md->d_counter;
   ca.nd = nd;
+  ca.pstride = partial_stride(m);
   ca.nlat = m->nlat;
   ca.nlon = m->nlon;
   ca.do_mass = md->P.do_mass_correction;
   ca.do_energy = md->P.do_energy_correction;
   ca.cp = md->cp_air;
   ca.grav = md->P.grav;
-  k_hs_corr_reduce<T><<<dim3((m->nlon + 31) / 32, m->nlat), 256, 0, st>>>(ca, md->d_vc);
+  k_hs_corr_reduce<T><<<dim3((m->nlon + 31) / 32, m->nlat, E), 256, 0, st>>>(ca, md->d_vc);
   mark(st);
   JG_CUDA(cudaGetLastError());
-  size_t nt = grid_elems(m, nd), nps = grid_elems(m, 1);
+  const size_t G1 = grid_elems(m, 1), nt = grid_elems(m, L), nps = grid_elems(m, E);
   int nb = (int)((nt + 255) / 256);
   if (nb > 4 * 152) nb = 4 * 152;
-  k_hs_corr_apply<T><<<nb, 256, 0, st>>>((T*)md->grid_t[n], (T*)md->grid_ps[n], md->d_scalars, nt, nps);
+  k_hs_corr_apply<T><<<nb, 256, 0, st>>>((T*)md->grid_t[n], (T*)md->grid_ps[n], md->d_scalars, nt, nps,
+                                         (size_t)nd * G1, G1);
   mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;
@@ -1437,8 +1465,14 @@ bool lookup(jgcm_model* md, const std::string& nm, FieldRef* f) {
 
 // ------------------------------------------------------------------------------------------
 extern "C" int jgcm_model_create(jgcm_mesh* mesh, const jgcm_params* params, jgcm_model** out) {
+  return jgcm_model_create_members(mesh, params, 1, out);
+}
+
+extern "C" int jgcm_model_create_members(jgcm_mesh* mesh, const jgcm_params* params, int members,
+                                         jgcm_model** out) {
   JG_ARG(mesh && params && out, "NULL argument");
   *out = nullptr;
+  JG_ARG(members >= 1 && members <= 65535, "members must be in [1, 65535]");
   JG_ARG(params->kind >= JGCM_BAROTROPIC && params->kind <= JGCM_HELD_SUAREZ, "unknown model kind");
   JG_ARG(params->dt > 0, "dt must be positive");
   JG_ARG(params->damping_order % 2 == 0, "damping_order must be even (Time_Integrator.jl:24)");
@@ -1449,6 +1483,8 @@ extern "C" int jgcm_model_create(jgcm_mesh* mesh, const jgcm_params* params, jgc
   md->mesh = mesh;
   md->P = *params;
   md->nd = mesh->nd;
+  md->ne = members;
+  md->L = members * mesh->nd;
   md->init_step = 1;
   md->sw_adv_from_n = 1;
   md->cp_air = params->rdgas / params->kappa;
@@ -1592,6 +1628,7 @@ extern "C" int jgcm_model_time_steps(jgcm_model* md, int nsteps, float* ms) {
 
 extern "C" int jgcm_model_get_field(jgcm_model* md, const char* name, double* host, long cap, long* count) {
   JG_ARG(md && name, "NULL argument");
+  JG_ARG(md->ne == 1, "an ensemble's fields are read through jgcm_model_copy_member into a one-member model");
   FieldRef f;
   JG_ARG(lookup(md, name, &f), "unknown field '%s'", name);
   jgcm_mesh* m = md->mesh;
@@ -1628,6 +1665,7 @@ extern "C" int jgcm_model_get_field(jgcm_model* md, const char* name, double* ho
 
 extern "C" int jgcm_model_set_field(jgcm_model* md, const char* name, const double* host, long count) {
   JG_ARG(md && name && host, "NULL argument");
+  JG_ARG(md->ne == 1, "an ensemble's fields are written through jgcm_model_copy_member from a one-member model");
   FieldRef f;
   JG_ARG(lookup(md, name, &f), "unknown field '%s'", name);
   JG_ARG(f.state, "field '%s' is derived and cannot be set", name);
@@ -1781,6 +1819,7 @@ extern "C" int jgcm_hs_forcing(jgcm_model* md, int Dt, const double* grid_u, con
 // Spectral_Initialize_Fields! (Spectral_Dynamics.jl:372-449) on the device.
 extern "C" int jgcm_spectral_initialize_fields(jgcm_model* md, const double* grid_t_pert, int vorticity_seed) {
   JG_ARG(md, "NULL model");
+  JG_ARG(md->ne == 1, "initialise one-member models and copy them into the ensemble (jgcm_model_copy_member)");
   jgcm_mesh* m = md->mesh;
   const int nd = md->nd, N = m->N, ns = m->ns;
   const size_t G = grid_elems(m, 1);
@@ -1887,3 +1926,77 @@ extern "C" int jgcm_spectral_initialize_fields(jgcm_model* md, const double* gri
   JG_CUDA(cudaStreamSynchronize(st));
   return JGCM_OK;
 }
+
+// ------------------------------------------------------------------------------------------
+// Member copies between models of one mesh and one parameter set (ensembles, member-major).
+namespace {
+// spectral [m][n][ne*L] member slices: dst member dm <- src member sm, L innermost levels each
+template <typename V>
+__global__ void k_spec_member_copy(V* dst, int dne, int dm, const V* src, int sne, int sm, size_t S, int L) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < S * L; q += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = q / L, k = q - r * L;
+    dst[(r * dne + dm) * L + k] = src[(r * sne + sm) * L + k];
+  }
+}
+}  // namespace
+
+extern "C" int jgcm_model_members(jgcm_model* md, int* members) {
+  JG_ARG(md && members, "NULL argument");
+  *members = md->ne;
+  return JGCM_OK;
+}
+
+extern "C" int jgcm_model_copy_member(jgcm_model* dst, int dst_member, jgcm_model* src, int src_member) {
+  JG_ARG(dst && src, "NULL model");
+  JG_ARG(dst->mesh == src->mesh, "members can only be copied between models of one mesh");
+  JG_ARG(dst->P.kind == src->P.kind && dst->P.dt == src->P.dt, "members can only be copied between models of one kind and dt");
+  JG_ARG(dst_member >= 0 && dst_member < dst->ne && src_member >= 0 && src_member < src->ne, "member out of range");
+  if (dst->ne > 1 && dst != src)
+    JG_ARG(dst->init_step == src->init_step && dst->sw_adv_from_n == src->sw_adv_from_n,
+           "ensemble members must share the time-step state (init step) of the ensemble");
+  jgcm_mesh* m = dst->mesh;
+  cudaStream_t st = m->stream;
+  const int nd = dst->nd;
+  const size_t ts = tsize(m), G1 = grid_elems(m, 1), S = (size_t)(m->N + 1) * (m->ns + 1);
+  auto grid = [&](void* d, const void* s_, int L) -> int {  // member slices are contiguous
+    JG_CUDA(cudaMemcpyAsync((char*)d + (size_t)dst_member * L * G1 * ts, (const char*)s_ + (size_t)src_member * L * G1 * ts,
+                            (size_t)L * G1 * ts, cudaMemcpyDeviceToDevice, st));
+    return JGCM_OK;
+  };
+  auto spec = [&](void* d, const void* s_, int L) -> int {
+    int nb = (int)std::min<size_t>((S * L + 255) / 256, 1024);
+    if (is_fp64(m))
+      k_spec_member_copy<double2><<<nb, 256, 0, st>>>((double2*)d, dst->ne, dst_member, (const double2*)s_, src->ne,
+                                                      src_member, S, L);
+    else
+      k_spec_member_copy<float2><<<nb, 256, 0, st>>>((float2*)d, dst->ne, dst_member, (const float2*)s_, src->ne,
+                                                     src_member, S, L);
+    JG_CUDA(cudaGetLastError());
+    return JGCM_OK;
+  };
+  for (int w = 0; w < 3; w++) {  // logical levels p, c, n
+    const int ld = lvl(dst, w), ls = lvl(src, w);
+    JG_TRY(spec(dst->spe_vor[ld], src->spe_vor[ls], nd));
+    JG_TRY(spec(dst->spe_div[ld], src->spe_div[ls], nd));
+    JG_TRY(spec(dst->spe_t[ld], src->spe_t[ls], nd));
+    JG_TRY(spec(dst->spe_lnps[ld], src->spe_lnps[ls], 1));
+    JG_TRY(grid(dst->grid_u[ld], src->grid_u[ls], nd));
+    JG_TRY(grid(dst->grid_v[ld], src->grid_v[ls], nd));
+    JG_TRY(grid(dst->grid_t[ld], src->grid_t[ls], nd));
+    JG_TRY(grid(dst->grid_ps[ld], src->grid_ps[ls], 1));
+  }
+  JG_TRY(grid(dst->grid_vor, src->grid_vor, nd));
+  JG_TRY(grid(dst->grid_div, src->grid_div, nd));
+  JG_TRY(grid(dst->grid_t_eq, src->grid_t_eq, nd));
+  JG_TRY(grid(dst->grid_lnps, src->grid_lnps, 1));
+  JG_TRY(grid(dst->grid_geopots, src->grid_geopots, 1));
+  JG_TRY(grid(dst->grid_h_eq, src->grid_h_eq, 1));
+  if (dst->ne == 1) {  // a one-member model takes the source's time-step state
+    dst->init_step = src->init_step;
+    dst->sw_adv_from_n = src->sw_adv_from_n;
+    dst->steps_done = src->steps_done;
+  }
+  JG_CUDA(cudaStreamSynchronize(st));
+  return JGCM_OK;
+}
+

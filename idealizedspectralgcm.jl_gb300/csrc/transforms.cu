@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(256) k_ifft(IFFTPlan plan, Tables<T> tb, const
         ((T*)g.dst2)[idx] = exp(x) * (T)exp(g.shift);
         break;
       case EPI_DIVCOS_MULPS:
-        dst[idx] = (x / tb.cosj[j]) * ((const T*)g.ps)[(size_t)j * nlon + t];
+        dst[idx] = (x / tb.cosj[j]) * ((const T*)g.ps)[((size_t)k * nlat + j) * nlon + t];  // level k of ps
         break;
     }
   }
@@ -457,31 +457,43 @@ static int launch_s2g_into(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, 
 }
 
 template <typename T>
-int launch_s2g(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, cudaStream_t st) {
-  JG_ARG(sp.C == ip.C && sp.C <= m->Cmax && sp.C > 0, "bad S2G plan");
-  return launch_s2g_into<T>(m, sp, ip, st, (V2<T>*)m->d_fbuf);
+int launch_s2g(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, cudaStream_t st, void* fbuf, int cap) {
+  if (!fbuf) {
+    fbuf = m->d_fbuf;
+    cap = m->Cmax;
+  }
+  JG_ARG(sp.C == ip.C && sp.C <= cap && sp.C > 0, "bad S2G plan");
+  return launch_s2g_into<T>(m, sp, ip, st, (V2<T>*)fbuf);
 }
 
 template <typename T>
-int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp, cudaStream_t st) {
+int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp, cudaStream_t st, void* fbuf, int cap) {
   using V = V2<T>;
   JG_TRY(configure_smem<T>());
-  JG_ARG(fp.C <= m->Cmax && fp.C > 0, "bad FFT plan");
+  if (!fbuf) {
+    fbuf = m->d_fbuf;
+    cap = m->Cmax;
+  }
+  JG_ARG(fp.C <= cap && fp.C > 0, "bad FFT plan");
   Tables<T> tb = tables<T>(m);
   const int fc = fft_ct(m->nlon);
   size_t sm = (size_t)(fc * m->nlon + m->nlon) * sizeof(T);
   dim3 g((fp.C + fc - 1) / fc, m->nlat);
-  k_fft<T><<<g, 256, sm, st>>>(fp, tb, (V*)m->d_fbuf, m->N, m->nlat, m->nlon, m->logn - 1, fc);
+  k_fft<T><<<g, 256, sm, st>>>(fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon, m->logn - 1, fc);
   mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;
 }
 
 template <typename T>
-int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp, cudaStream_t st) {
+int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp, cudaStream_t st, void* fbuf, int cap) {
   using V = V2<T>;
-  JG_TRY(launch_fft_only<T>(m, fp, st));
-  if (std::is_same<T, float>::value && m->tc.on) return launch_g2s_legendre_tc(m, gp, fp.C, st);
+  if (!fbuf) {
+    fbuf = m->d_fbuf;
+    cap = m->Cmax;
+  }
+  JG_TRY(launch_fft_only<T>(m, fp, st, fbuf, cap));
+  if (std::is_same<T, float>::value && m->tc.on) return launch_g2s_legendre_tc(m, gp, fp.C, st, fbuf);
   Tables<T> tb = tables<T>(m);
   const int nh = m->nh, ct = g2s_ct(nh);
   size_t sm = (size_t)8 * ct * nh * sizeof(V);
@@ -489,18 +501,18 @@ int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp, cudaStream_t 
   const int stage = sm + tab <= kSmemBudget;
   if (stage) sm += tab;
   dim3 g((gp.C + ct - 1) / ct, m->N + 1);
-  k_g2s_legendre<T><<<g, 256, sm, st>>>(gp, tb, (const V*)m->d_fbuf, m->ns, m->nlat, fp.C, ct, stage);
+  k_g2s_legendre<T><<<g, 256, sm, st>>>(gp, tb, (const V*)fbuf, m->ns, m->nlat, fp.C, ct, stage);
   mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;
 }
 
-template int launch_s2g<float>(jgcm_mesh*, const S2GPlan&, const IFFTPlan&, cudaStream_t);
-template int launch_s2g<double>(jgcm_mesh*, const S2GPlan&, const IFFTPlan&, cudaStream_t);
-template int launch_g2s<float>(jgcm_mesh*, const FFTPlan&, const G2SPlan&, cudaStream_t);
-template int launch_g2s<double>(jgcm_mesh*, const FFTPlan&, const G2SPlan&, cudaStream_t);
-template int launch_fft_only<float>(jgcm_mesh*, const FFTPlan&, cudaStream_t);
-template int launch_fft_only<double>(jgcm_mesh*, const FFTPlan&, cudaStream_t);
+template int launch_s2g<float>(jgcm_mesh*, const S2GPlan&, const IFFTPlan&, cudaStream_t, void*, int);
+template int launch_s2g<double>(jgcm_mesh*, const S2GPlan&, const IFFTPlan&, cudaStream_t, void*, int);
+template int launch_g2s<float>(jgcm_mesh*, const FFTPlan&, const G2SPlan&, cudaStream_t, void*, int);
+template int launch_g2s<double>(jgcm_mesh*, const FFTPlan&, const G2SPlan&, cudaStream_t, void*, int);
+template int launch_fft_only<float>(jgcm_mesh*, const FFTPlan&, cudaStream_t, void*, int);
+template int launch_fft_only<double>(jgcm_mesh*, const FFTPlan&, cudaStream_t, void*, int);
 
 // ------------------------------------------------------------------------------------------
 // Layout / precision conversion between the reference host layout (FP64) and device layout.

@@ -79,6 +79,9 @@ def lib():
         "jgcm_apply_laplacian": (I, [P, P, I]),
         "jgcm_area_weighted_global_mean": (I, [P, P, C.POINTER(D)]),
         "jgcm_model_create": (I, [P, P, PP]),
+        "jgcm_model_create_members": (I, [P, P, I, PP]),
+        "jgcm_model_members": (I, [P, C.POINTER(I)]),
+        "jgcm_model_copy_member": (I, [P, I, P, I]),
         "jgcm_model_destroy": (I, [P]),
         "jgcm_model_get_field": (I, [P, C.c_char_p, P, Lg, C.POINTER(Lg)]),
         "jgcm_model_set_field": (I, [P, C.c_char_p, P, Lg]),
@@ -278,11 +281,15 @@ class Model:
     ``grid_u_p``, ``grid_t_eq``, ...).  ``step(n)`` runs n Barotropic_Dynamics! /
     Shallow_Water_Physics!+Shallow_Water_Dynamics! / Atmosphere_Update! steps, the first one
     being the reference drivers' init step followed by Update_Init_Step!.
+
+    ``members`` > 1 makes an ensemble: that many independent members advanced together by the
+    same kernels.  Members are loaded and read with ``copy_member`` through one-member models.
     """
 
-    def __init__(self, mesh: Spectral_Spherical_Mesh, params: dict):
+    def __init__(self, mesh: Spectral_Spherical_Mesh, params: dict, members: int = 1):
         self.mesh = mesh
         self.params = dict(params)
+        self.members = int(members)
         p = _Params()
         for name, _ in _Params._fields_:
             if name == "kind":
@@ -291,8 +298,12 @@ class Model:
                 setattr(p, name, params[name])
         self._p = p
         h = C.c_void_p()
-        _check(lib().jgcm_model_create(mesh._h, C.byref(p), C.byref(h)))
+        _check(lib().jgcm_model_create_members(mesh._h, C.byref(p), self.members, C.byref(h)))
         self._h = h
+
+    def copy_member(self, member: int, src: "Model", src_member: int = 0):
+        """Member `member` of this model <- member `src_member` of `src` (same mesh and kind)."""
+        _check(lib().jgcm_model_copy_member(self._h, int(member), src._h, int(src_member)))
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:

@@ -135,6 +135,16 @@ typedef struct {
 } jgcm_params;
 
 int jgcm_model_create(jgcm_mesh* mesh, const jgcm_params* params, jgcm_model** out);
+/* Ensembles (no counterpart in the reference, whose drivers run one member): `members`
+ * independent members of one mesh and parameter set, advanced together by the same kernels
+ * (every field holds all members, member-major).  Members are initialised as one-member models
+ * and copied in; their fields are read by copying a member out into a one-member model. */
+int jgcm_model_create_members(jgcm_mesh* mesh, const jgcm_params* params, int members, jgcm_model** out);
+int jgcm_model_members(jgcm_model* model, int* members);
+/* Copy member src_member of src into member dst_member of dst (same mesh and model kind): every
+ * time level of the prognostic state and the grid diagnostics.  A one-member dst also takes the
+ * source's time-step state (init step); an ensemble dst must already share it. */
+int jgcm_model_copy_member(jgcm_model* dst, int dst_member, jgcm_model* src, int src_member);
 int jgcm_model_destroy(jgcm_model* model);
 /* Read / write one Dyn_Data field (Dyn_Data.jl:4-156) by its reference name with the
  * δ spelled "d": "spe_vor_c", "grid_u_p", "spe_dt", "grid_t_eq", "grid_p_full",
