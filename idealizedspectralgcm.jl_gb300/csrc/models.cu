@@ -53,6 +53,7 @@ struct jgcm_model {
   int ne, L;
   void* fbuf;  // Fourier buffer of fcap columns
   int fcap;
+  int hs_lanes;  // lanes per column of the Held-Suarez column kernel (1, 2 or 4)
   double cp_air;
   // time-levelled state (index by rotation)
   void *spe_vor[3], *spe_div[3], *spe_lnps[3], *spe_t[3];
@@ -174,14 +175,13 @@ __device__ bool grid_reduce_last(const double* vals, double* partials, unsigned*
 // ------------------------------------------------------------------------------------------
 // Held-Suarez: physics (HS_Forcing!, previous time level) + corrections-init sums +
 // Four_In_One! + Compute_Geopotential! + Vert_Advection! x3 + horizontal advection of T +
-// absolute-vorticity fluxes + energy, fused.  A block owns a tile of HS_CW consecutive columns of
-// one latitude row: every input's nd x HS_CW tile is staged in shared memory with coalesced row
-// loads, one warp per column computes with lane = level (scans by shuffles), and the outputs go
-// back through the same tile as coalesced rows.  Sigma coordinates: one log per column, one exp
-// per level (ln p = const_k + ln ps).
-constexpr int HS_CW = 8;           // columns per block (one per warp)
-constexpr int HS_CWP = HS_CW + 1;  // tile pitch: lane-per-level reads fall in distinct banks
-constexpr int HS_NIN = 10;         // staged nd-level inputs
+// absolute-vorticity fluxes + energy, fused.  One thread per grid column (consecutive threads,
+// consecutive longitudes: every level read and write is a coalesced row), levels walked in two
+// passes: bottom-up for the hydrostatic geopotential (Compute_Geopotential!) and the column
+// divergence sum, then top-down for everything else (the mass-flux prefix sum of Four_In_One!
+// and the centred vertical advection, whose flux at k+1/2 is carried to the next level).
+// Sigma coordinates: one log per column, one exp per level (ln p = const_k + ln ps).
+constexpr int HS_CT = 64;  // columns (threads) per block
 
 template <typename T>
 struct HSColArgs {
@@ -197,164 +197,193 @@ struct HSColArgs {
   double sigma_b, k_f, k_a, k_s, dT_y, dtheta_z, kappa, rdgas, cp, grav;
 };
 
-template <typename T>
-__global__ void __launch_bounds__(256) k_hs_column(HSColArgs<T> a, const VertCoef* __restrict__ vcp) {
-  const VertCoef& vc = *vcp;  // device memory: lanes read consecutive levels
-  extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ double red[2][8];
-  const int nd = a.nd, nlon = a.nlon, nlat = a.nlat;
-  T* tile = (T*)smem;                        // [HS_NIN][nd][HS_CWP]
-  T* sgl = tile + HS_NIN * nd * HS_CWP;      // [5][HS_CW]: ps_c, ps_p, dlps, dtps, geopots
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int i0 = blockIdx.x * HS_CW, j = blockIdx.y, e = blockIdx.z;
-  const size_t G = (size_t)nlat * nlon, row = (size_t)j * nlon;
-  // member e: its nd levels start at level e*nd, its single-level fields at level e
-  const size_t offL = (size_t)e * nd * G, off1 = (size_t)e * G;
-  {
-    const T* in[HS_NIN] = {a.u_p + offL, a.v_p + offL, a.t_p + offL, a.u_c + offL, a.v_c + offL,
-                           a.t_c + offL, a.div + offL, a.vor + offL, a.dlT + offL, a.dtT + offL};
-    // all HS_NIN loads of one (level, column) are issued back to back before any store
-    for (int r = threadIdx.x; r < nd * HS_CW; r += blockDim.x) {
-      const int k = r / HS_CW, c = r - k * HS_CW, i = i0 + c;
-      const bool ok = i < nlon;
-      const size_t off = k * G + row + i;
-      T x[HS_NIN];
+// S lanes per column (S = 1, 2, 4): lane s walks levels [s*len, s*len + len), len = ceil(nd/S); the
+// running sums that couple the levels (the geopotential from below, the mass-divergence prefix and
+// column total) are completed across the S lanes with shuffles, so a column's chain of dependent
+// work is nd/S levels long.  Small grids run S = 4 for latency, large ensembles S = 1.
+template <int S, typename R>
+__device__ __forceinline__ R seg_sum(R x) {  // sum over the S lanes of this column
 #pragma unroll
-      for (int f = 0; f < HS_NIN; f++) x[f] = ok ? in[f][off] : (T)0;
+  for (int o = 1; o < S; o <<= 1) x += __shfl_xor_sync(FULL, x, o, S);
+  return x;
+}
+template <int S, typename R>
+__device__ __forceinline__ R seg_excl_prefix(R x, int s) {  // sum over the lanes s' < s
+  R incl = x;
 #pragma unroll
-      for (int f = 0; f < HS_NIN; f++) tile[(f * nd + k) * HS_CWP + c] = x[f];
-    }
-    const T* sg[5] = {a.ps_c + off1, a.ps_p + off1, a.dlps + off1, a.dtps + off1, a.geopots + off1};
-    for (int q = threadIdx.x; q < 5 * HS_CW; q += blockDim.x) {
-      int f = q / HS_CW, c = q - f * HS_CW, i = i0 + c;
-      sgl[q] = (i < nlon) ? sg[f][row + i] : (f < 2 ? (T)1 : (T)0);
-    }
+  for (int o = 1; o < S; o <<= 1) {
+    R y = __shfl_up_sync(FULL, incl, o, S);
+    if (s >= o) incl += y;
   }
-  __syncthreads();
+  return incl - x;
+}
+template <int S, typename R>
+__device__ __forceinline__ R seg_excl_suffix(R x, int s) {  // sum over the lanes s' > s
+  R incl = x;
+#pragma unroll
+  for (int o = 1; o < S; o <<= 1) {
+    R y = __shfl_down_sync(FULL, incl, o, S);
+    if (s + o < S) incl += y;
+  }
+  return incl - x;
+}
+
+template <typename T, int S>
+__global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertCoef* __restrict__ vcp) {
+  const VertCoef& vc = *vcp;
+  __shared__ double red[2][HS_CT / 32];
+  const int nd = a.nd, nlon = a.nlon, nlat = a.nlat;
+  const int seg = threadIdx.x % S, i = blockIdx.x * (HS_CT / S) + threadIdx.x / S, j = blockIdx.y, e = blockIdx.z;
+  const int len = (nd + S - 1) / S, k0 = min(nd, seg * len), k1 = min(nd, k0 + len);
+  const bool act = i < nlon;
+  const size_t G = (size_t)nlat * nlon;
+  // member e: its nd levels start at level e*nd, its single-level fields at level e
+  const size_t col = (size_t)j * nlon + (act ? i : 0), c1 = (size_t)e * G + col, cL = (size_t)e * nd * G + col;
+  const T* __restrict__ u_c = a.u_c + cL;
+  const T* __restrict__ v_c = a.v_c + cL;
+  const T* __restrict__ t_c = a.t_c + cL;
+  const T* __restrict__ dvgp = a.div + cL;
   const T day = (T)86400;
   const T sj = a.sinj[j], s2 = sj * sj, c2 = (T)1.0 - s2, c4 = c2 * c2, cj = a.cosj[j], fj = a.coriolis[j];
   const T sb = (T)a.sigma_b, R = (T)a.rdgas, kap = (T)a.rdgas / (T)a.cp, cp = (T)a.cp;
   const T kv0 = ((T)a.k_f / day) / ((T)1.0 - sb);
   const T ka = (T)a.k_a / day, ks = (T)a.k_s / day, kt0 = (ks - ka) / ((T)1.0 - sb);
   const T ln_pref = (T)11.512925464970229;  // ln 1e5 (HS_Forcing.jl:49 p_ref)
-  const int Dt = a.Dt;
-  double accp = 0.0, acce = 0.0;
-  for (int c = w; c < HS_CW; c += 8) {
-    const bool colok = i0 + c < nlon;
-    const bool act = lane < nd && colok;
-    const int k = lane < nd ? lane : 0;
-    auto at = [&](int f) -> T { return act ? tile[(f * nd + k) * HS_CWP + c] : (T)0; };
-    const T up = at(0), vp = at(1), tp = at(2), u = at(3), v = at(4), t = at(5), dvg = at(6), vor = at(7),
-            dlT = at(8), dtT = at(9);
-    const T ps = sgl[c], psp = sgl[HS_CW + c], dlps = sgl[2 * HS_CW + c], dtps = sgl[3 * HS_CW + c],
-            gs = sgl[4 * HS_CW + c];
-    // ---- pressure variables from ps_c (Pressure_Variables!, Press_And_Geopot.jl:36-67)
-    const T lnps = log(ps);
-    const T dp = (T)vc.dak[k] + (T)vc.dbk[k] * ps;
-    const T rdp = (T)1 / dp;
-    const T lnpf = (T)vc.cf[k] + lnps;
-    const T pfull = (T)vc.sf[k] * ps;
-    const T dlnp_p = (T)vc.dlp_p[k];                 // ln p_{k+1/2} - ln p_k
-    const T dlnp_m = k == 0 ? lnpf : (T)vc.dlp_m[k];  // ln p_k - ln p_{k-1/2} (ln p_{1/2} = 0)
-    const T dlnp = k == 0 ? (T)vc.lb[1] + lnps : (T)vc.dlp[k];
-    // ---- HS_Forcing! on the previous level (sigma = p_k / ps = sf[k])
-    const T s = (T)vc.sf[k] - sb;
-    const T smax = s > (T)0 ? s : (T)0;
-    const T k_v = kv0 * smax;
-    T du = -k_v * up, dv = -k_v * vp;
-    T dt = -((up + (T)0.5 * du * (T)Dt) * du + (vp + (T)0.5 * dv * (T)Dt) * dv) / cp;
-    const T lpn = lnpf - ln_pref;  // ln(p / p_ref)
-    T teq = ((T)315.0 - (T)a.dT_y * s2 - (T)a.dtheta_z * c2 * lpn) * exp((T)a.kappa * lpn);
-    teq = teq > (T)200.0 ? teq : (T)200.0;
-    const T k_t = ka + kt0 * smax * c4;
-    dt = dt - k_t * (tp - teq);
-    // ---- Compute_Corrections_Init sums: column energy integral with ps_p, accumulated in FP64
-    // column integral in the state precision (20-term sum); the sum over columns is FP64
-    T e_p = 0;
-    if (act) {
-      T ua = up + (T)Dt * du, va = vp + (T)Dt * dv;
-      T E = (T)0.5 * (ua * ua + va * va) + cp * (tp + (T)Dt * dt);
-      e_p = E * ((T)vc.dak[k] + (T)vc.dbk[k] * psp);
+  const T tDt = (T)a.Dt;
+  const T ps = act ? a.ps_c[c1] : (T)1, psp = act ? a.ps_p[c1] : (T)0;
+  const T dlps = act ? a.dlps[c1] : (T)0, dtps = act ? a.dtps[c1] : (T)0, gs = act ? a.geopots[c1] : (T)0;
+  // ---- pressure variables from ps_c (Pressure_Variables!, Press_And_Geopot.jl:36-67)
+  const T lnps = log(ps);
+  // ---- pass 1: Compute_Geopotential! (Press_And_Geopot.jl:71-111) on T - T0_k with T0_k the level's
+  // area mean (spectral mode (0,0)): the T0 part is a per-level constant (dlnp_r, r >= 1, and dlnp_p
+  // do not vary horizontally), so it only moves the (0,0) mode of the energy, which the Laplacian
+  // annihilates, while the rounding of the sum shrinks with |T - T0|.  Also the column sum of the
+  // mass divergence D_k.
+  T termS = 0, dmeanS = 0;
+  if (act)
+    for (int k = k0; k < k1; k++) {
+      const size_t x = (size_t)k * G;
+      const T t = t_c[x], u = u_c[x], v = v_c[x], dvg = dvgp[x];
+      const T dlnp = k == 0 ? (T)vc.lb[1] + lnps : (T)vc.dlp[k];
+      termS += R * (t - (T)a.t_spec[e * nd + k].x) * dlnp;
+      dmeanS += dvg * ((T)vc.dak[k] + (T)vc.dbk[k] * ps) + (T)vc.dbk[k] * (u * dlps + v * dtps);
     }
-    const double col_e = (double)warp_sum_t<T>(e_p);
-    // ---- Four_In_One! (Spectral_Dynamics.jl:88-183) on the current level
-    const T x1 = ((T)vc.bk[k] * dlnp_m + (T)vc.bk[k + 1] * dlnp_p) * rdp;
-    const T dlnp_dl = x1 * dlps, dlnp_dt = x1 * dtps;
-    du = du - R * t * dlnp_dl;
-    dv = dv - R * t * dlnp_dt;
-    T dmean = dvg * dp + (T)vc.dbk[k] * (u * dlps + v * dtps);
-    if (!act) dmean = 0;
-    const T incl = scan_incl<T>(dmean, lane);  // sum_{r<=k} D_r
-    const T tot = __shfl_sync(FULL, incl, nd - 1);
-    const T excl = shfl_up1(incl, lane, (T)0);
-    const T x5 = -(excl * dlnp + dmean * dlnp_p) * rdp + u * dlnp_dl + v * dlnp_dt;
-    dt = dt + kap * t * x5;
-    // M_{k+1/2}: -sum_{r<=k} D_r + B_{k+1/2} sum_r D_r ; zero at top and surface
-    const T Mhi = (lane + 1 <= nd - 1) ? -incl + tot * (T)vc.bk[k + 1] : (T)0;
-    const T Mlo = shfl_up1(Mhi, lane, (T)0);
-    // ---- Compute_Geopotential! (Press_And_Geopot.jl:71-111), bottom-up, on T - T0_k with T0_k the
-    // level's area mean: the T0 part, sum_{r>k} R T0_r dlnp_r + R T0_k dlnp_p, is a per-level constant
-    // (dlnp_r, r >= 1, and dlnp_p do not vary horizontally), so it only moves the (0,0) mode of the
-    // energy, which the Laplacian annihilates (eig = 0), while the rounding of the scan shrinks with
-    // |T - T0| instead of |T| (it feeds the divergence tendency through the Laplacian)
-    const T tdev = t - (T)a.t_spec[e * nd + k].x;
-    const T term = act ? R * tdev * dlnp : (T)0;
-    const T rs = rscan_incl<T>(term, lane);           // sum_{r>=k} term_r
-    const T ghalf_hi = gs + shfl_dn1(rs, lane, nd, (T)0);  // Phi_{k+1/2} - const_k
-    const T gfull = ghalf_hi + R * tdev * dlnp_p;
-    // ---- Vert_Advection! (second_centered_wts) for u, v, T
-    const T dp_m = shfl_up1(dp, lane, (T)1);
-    const T wlo = dp_m / (dp_m + dp);
-    auto vadv = [&](T r) -> T {
-      T r_m = shfl_up1(r, lane, (T)0);
-      T flux_lo = (lane >= 1) ? Mlo * (r_m + (r - r_m) * wlo) : (T)0;
-      T flux_hi = shfl_dn1(flux_lo, lane, nd, (T)0);
-      return (flux_lo - flux_hi + r * (Mhi - Mlo)) * rdp;
-    };
-    du = du + vadv(u);
-    dv = dv + vadv(v);
-    dt = dt + vadv(t);
-    // ---- Add_Horizontal_Advection!(spe_t_c), Compute_Abs_Vor! fluxes, energy
-    dt = dt - (u * dlT + v * dtT);
-    const T absvor = vor + fj;
-    du = du + absvor * v;
-    dv = dv - absvor * u;
-    // outputs overwrite this column's own (already consumed) input slots
-    if (act) {
-      tile[(0 * nd + k) * HS_CWP + c] = du * cj;
-      tile[(1 * nd + k) * HS_CWP + c] = dv * cj;
-      tile[(2 * nd + k) * HS_CWP + c] = dt;
-      tile[(8 * nd + k) * HS_CWP + c] = gfull + (T)0.5 * (u * u + v * v);
-      tile[(9 * nd + k) * HS_CWP + c] = teq;
+  const T tot = seg_sum<S>(dmeanS);
+  T rs = seg_excl_suffix<S>(termS, seg);  // sum_{r >= k1} R (T_r - T0_r) dlnp_r
+  const T incl0 = seg_excl_prefix<S>(dmeanS, seg);  // sum_{r < k0} D_r
+  if (act)
+    for (int k = k1 - 1; k >= k0; k--) {  // the energy Φ + |u|^2/2, bottom-up within the segment
+      const size_t x = (size_t)k * G;
+      const T t = t_c[x], u = u_c[x], v = v_c[x];
+      const T tdev = t - (T)a.t_spec[e * nd + k].x;
+      const T dlnp = k == 0 ? (T)vc.lb[1] + lnps : (T)vc.dlp[k];
+      a.energy[cL + x] = gs + rs + R * tdev * (T)vc.dlp_p[k] + (T)0.5 * (u * u + v * v);
+      rs += R * tdev * dlnp;
     }
-    __syncwarp();
-    if (lane == 0) {
-      sgl[c] = (-tot) / ps;  // grid_δlnps = grid_δps / ps (Spectral_Dynamics.jl:279)
-      if (colok) {
-        accp += (double)psp;
-        acce += col_e;
+  // ---- pass 2, top-down within the segment
+  T col_e = 0;
+  if (act && k0 < k1) {
+    T incl = incl0, Mlo = 0, flu = 0, flv = 0, flt = 0;  // M and the advective fluxes at k0-1/2
+    T u = u_c[(size_t)k0 * G], v = v_c[(size_t)k0 * G], t = t_c[(size_t)k0 * G];
+    T dp = (T)vc.dak[k0] + (T)vc.dbk[k0] * ps;
+    if (k0 > 0) {  // the level above the segment: M_{k0-1/2} and its fluxes
+      const size_t x = (size_t)(k0 - 1) * G;
+      const T um = u_c[x], vm = v_c[x], tm = t_c[x], dpm = (T)vc.dak[k0 - 1] + (T)vc.dbk[k0 - 1] * ps;
+      Mlo = -incl0 + tot * (T)vc.bk[k0];
+      const T w = dpm / (dpm + dp);
+      flu = Mlo * (um + (u - um) * w);
+      flv = Mlo * (vm + (v - vm) * w);
+      flt = Mlo * (tm + (t - tm) * w);
+    }
+    for (int k = k0; k < k1; k++) {
+      const size_t x = (size_t)k * G;
+      const T up = a.u_p[cL + x], vp = a.v_p[cL + x], tp = a.t_p[cL + x], dvg = dvgp[x], vor = a.vor[cL + x],
+              dlT = a.dlT[cL + x], dtT = a.dtT[cL + x];
+      const bool below = k + 1 < nd;
+      T u1 = 0, v1 = 0, t1 = 0, dp1 = 1;
+      if (below) {
+        u1 = u_c[x + G];
+        v1 = v_c[x + G];
+        t1 = t_c[x + G];
+        dp1 = (T)vc.dak[k + 1] + (T)vc.dbk[k + 1] * ps;
       }
+      const T rdp = (T)1 / dp;
+      const T lnpf = (T)vc.cf[k] + lnps;
+      const T dlnp_p = (T)vc.dlp_p[k];                 // ln p_{k+1/2} - ln p_k
+      const T dlnp_m = k == 0 ? lnpf : (T)vc.dlp_m[k];  // ln p_k - ln p_{k-1/2} (ln p_{1/2} = 0)
+      const T dlnp = k == 0 ? (T)vc.lb[1] + lnps : (T)vc.dlp[k];
+      // HS_Forcing! on the previous level (sigma = p_k / ps = sf[k])
+      const T sg = (T)vc.sf[k] - sb;
+      const T smax = sg > (T)0 ? sg : (T)0;
+      const T k_v = kv0 * smax;
+      T du = -k_v * up, dv = -k_v * vp;
+      T dt = -((up + (T)0.5 * du * tDt) * du + (vp + (T)0.5 * dv * tDt) * dv) / cp;
+      const T lpn = lnpf - ln_pref;  // ln(p / p_ref)
+      T teq = ((T)315.0 - (T)a.dT_y * s2 - (T)a.dtheta_z * c2 * lpn) * exp((T)a.kappa * lpn);
+      teq = teq > (T)200.0 ? teq : (T)200.0;
+      dt = dt - (ka + kt0 * smax * c4) * (tp - teq);
+      // Compute_Corrections_Init: column energy integral with ps_p in the state precision
+      {
+        const T ua = up + tDt * du, va = vp + tDt * dv;
+        col_e += ((T)0.5 * (ua * ua + va * va) + cp * (tp + tDt * dt)) * ((T)vc.dak[k] + (T)vc.dbk[k] * psp);
+      }
+      // Four_In_One! (Spectral_Dynamics.jl:88-183)
+      const T x1 = ((T)vc.bk[k] * dlnp_m + (T)vc.bk[k + 1] * dlnp_p) * rdp;
+      const T dlnp_dl = x1 * dlps, dlnp_dt = x1 * dtps;
+      du = du - R * t * dlnp_dl;
+      dv = dv - R * t * dlnp_dt;
+      const T dmean = dvg * dp + (T)vc.dbk[k] * (u * dlps + v * dtps);
+      const T excl = incl;
+      incl += dmean;
+      const T x5 = -(excl * dlnp + dmean * dlnp_p) * rdp + u * dlnp_dl + v * dlnp_dt;
+      dt = dt + kap * t * x5;
+      // M_{k+1/2} = -sum_{r<=k} D_r + B_{k+1/2} sum_r D_r, zero at the surface
+      const T Mhi = below ? -incl + tot * (T)vc.bk[k + 1] : (T)0;
+      // Vert_Advection! (second_centered_wts): flux at k+1/2 with weight dp_k / (dp_k + dp_{k+1})
+      const T w1 = dp / (dp + dp1);
+      const T fhu = below ? Mhi * (u + (u1 - u) * w1) : (T)0;
+      const T fhv = below ? Mhi * (v + (v1 - v) * w1) : (T)0;
+      const T fht = below ? Mhi * (t + (t1 - t) * w1) : (T)0;
+      du = du + (flu - fhu + u * (Mhi - Mlo)) * rdp;
+      dv = dv + (flv - fhv + v * (Mhi - Mlo)) * rdp;
+      dt = dt + (flt - fht + t * (Mhi - Mlo)) * rdp;
+      // Add_Horizontal_Advection!(spe_t_c), Compute_Abs_Vor! fluxes
+      dt = dt - (u * dlT + v * dtT);
+      const T absvor = vor + fj;
+      du = du + absvor * v;
+      dv = dv - absvor * u;
+      a.ducos[cL + x] = du * cj;
+      a.dvcos[cL + x] = dv * cj;
+      a.dtg[cL + x] = dt;
+      a.t_eq[cL + x] = teq;
+      Mlo = Mhi;
+      flu = fhu;
+      flv = fhv;
+      flt = fht;
+      u = u1;
+      v = v1;
+      t = t1;
+      dp = dp1;
     }
   }
-  __syncthreads();
-  {
-    T* out[5] = {a.ducos + offL, a.dvcos + offL, a.dtg + offL, a.energy + offL, a.t_eq + offL};
-    const int slot[5] = {0, 1, 2, 8, 9};
-    for (int q = threadIdx.x; q < 5 * nd * HS_CW; q += blockDim.x) {
-      int o = q / (nd * HS_CW), r = q - o * nd * HS_CW, k = r / HS_CW, c = r - k * HS_CW, i = i0 + c;
-      if (i < nlon) out[o][k * G + row + i] = tile[(slot[o] * nd + k) * HS_CWP + c];
-    }
-    if (threadIdx.x < HS_CW && i0 + (int)threadIdx.x < nlon) a.dlnps[off1 + row + i0 + threadIdx.x] = sgl[threadIdx.x];
+  col_e = seg_sum<S>(col_e);
+  double accp = 0.0, acce = 0.0;
+  if (act && seg == 0) {
+    a.dlnps[c1] = (-tot) / ps;  // grid_δlnps = grid_δps / ps (Spectral_Dynamics.jl:279)
+    accp = (double)psp;
+    acce = (double)col_e;
   }
-  // ---- block partials for mean_ps_p and mean_energy_p (fixed order)
-  if (lane == 0) {
-    red[0][w] = accp;
-    red[1][w] = acce;
+  // ---- block partials for mean_ps_p and mean_energy_p (fixed order), then the member's fold
+  accp = warp_sum(accp);
+  acce = warp_sum(acce);
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = accp;
+    red[1][threadIdx.x >> 5] = acce;
   }
   __syncthreads();
   double vals[2] = {0, 0};
   if (threadIdx.x == 0)
-    for (int q = 0; q < 8; q++) {
+    for (int q = 0; q < HS_CT / 32; q++) {
       vals[0] += red[0][q];
       vals[1] += red[1][q];
     }
@@ -364,6 +393,24 @@ __global__ void __launch_bounds__(256) k_hs_column(HSColArgs<T> a, const VertCoe
     scal[0] = tot2[0] / (2.0 * nlon);           // mean_ps_p   (Area_Weighted_Global_Mean)
     scal[1] = tot2[1] / (2.0 * nlon) / a.grav;  // mean_energy_p (Mass_Weighted_Global_Integral)
   }
+}
+
+// lanes per column for a launch: S = 4 for small grids (latency), 1 for large ensembles
+inline int hs_lanes(const jgcm_mesh* m, int ne, int nd) {
+  const size_t cols = (size_t)ne * m->nlat * m->nlon;
+  int S = cols >= 65536 ? 1 : cols >= 32768 ? 2 : 4;
+  while (S > 1 && (nd + S - 1) / S < 2) S >>= 1;
+  return S;
+}
+
+template <typename T>
+int launch_hs_column(const HSColArgs<T>& a, const jgcm_mesh* m, int ne, int S, const VertCoef* vc, cudaStream_t st) {
+  const int cpb = HS_CT / S;  // columns per block
+  dim3 g((m->nlon + cpb - 1) / cpb, m->nlat, ne);
+  if (S == 1) k_hs_column<T, 1><<<g, HS_CT, 0, st>>>(a, vc);
+  else if (S == 2) k_hs_column<T, 2><<<g, HS_CT, 0, st>>>(a, vc);
+  else k_hs_column<T, 4><<<g, HS_CT, 0, st>>>(a, vc);
+  return JGCM_OK;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -906,10 +953,11 @@ int build_wave(jgcm_model* md) {
   return JGCM_OK;
 }
 
-// FP64 block partials per member: the column kernel folds 2 sums over its (nlon/8) x nlat blocks,
+// FP64 block partials per member: the column kernel folds 2 sums over its (nlon/(64/S)) x nlat blocks,
 // the fixer kernel 3 sums over (nlon/32) x nlat blocks
 size_t partial_stride(const jgcm_mesh* m) {
-  size_t a = (size_t)2 * ((m->nlon + HS_CW - 1) / HS_CW) * m->nlat, b = (size_t)3 * ((m->nlon + 31) / 32) * m->nlat;
+  size_t a = (size_t)2 * ((m->nlon + HS_CT / 4 - 1) / (HS_CT / 4)) * m->nlat;
+  size_t b = (size_t)3 * ((m->nlon + 31) / 32) * m->nlat;
   return a > b ? a : b;
 }
 
@@ -1220,9 +1268,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   a.cp = md->cp_air;
   a.grav = md->P.grav;
   a.pstride = partial_stride(m);
-  dim3 gcol((m->nlon + HS_CW - 1) / HS_CW, m->nlat, E);
-  const size_t smcol = ((size_t)HS_NIN * nd * HS_CWP + 5 * HS_CW) * sizeof(T);
-  k_hs_column<T><<<gcol, 256, smcol, st>>>(a, md->d_vc);
+  JG_TRY(launch_hs_column<T>(a, m, E, md->hs_lanes, md->d_vc, st));
   mark(st);
   JG_CUDA(cudaGetLastError());
   // 3. forward transforms: δu cos, δv cos, δT, energy, δlnps -> vor/div tendencies (alpha
@@ -1485,6 +1531,7 @@ extern "C" int jgcm_model_create_members(jgcm_mesh* mesh, const jgcm_params* par
   md->nd = mesh->nd;
   md->ne = members;
   md->L = members * mesh->nd;
+  md->hs_lanes = hs_lanes(mesh, members, mesh->nd);
   md->init_step = 1;
   md->sw_adv_from_n = 1;
   md->cp_air = params->rdgas / params->kappa;
