@@ -260,6 +260,57 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------------------------------------
+ENSEMBLE = [("hs_t21l20", 128), ("hs_t42l20", 32), ("sw_t85", 8)]  # the batched-ensemble configuration
+
+
+def ensemble_bench(jgcm, configs, precisions, days=2):
+    """Member-batched ensembles (one set of kernels advances every member of a truncation): HS
+    T21L20 x128, HS T42L20 x32, SW T85 x8, each member with its own seeded initial state; CUDA-event
+    time of `days` simulated days after one warm-up day.  Reports member-sim-days/s per truncation
+    and the whole ensemble's sim-days/s (every member advanced one day)."""
+    out = {"members": {n: e for n, e in ENSEMBLE}, "days": days}
+    for prec in precisions:
+        per, total_s = {}, 0.0
+        for name, E in ENSEMBLE:
+            params = configs.PARAMS[name]
+            m = configs.make_mesh(jgcm, name, precision=prec)
+            ens = jgcm.Model(m, params, members=E)
+            one = jgcm.Model(m, params)
+            for e in range(E):
+                if params["kind"] == "held_suarez":
+                    configs.init_held_suarez(jgcm, m, one, seed=configs.BASE_SEED + e)
+                else:
+                    configs.init_shallow_water_jet(jgcm, m, one, seed=configs.BASE_SEED + e)
+                ens.copy_member(e, one)
+            spd = configs.STEPS_PER_DAY[name]
+            ens.step(spd)
+            t = sum(ens.time_steps(spd) for _ in range(days)) / 1000.0
+            total_s += t / days
+            per[name] = {"member_sim_days_per_s": E * days / t, "ms_per_step": 1000.0 * t / (days * spd)}
+            ens.close()
+            one.close()
+        out[prec] = {"ensemble_sim_days_per_s": 1.0 / total_s, "per_truncation": per}
+    return out
+
+
+def tensor_core_modes(jgcm, configs, mod64, days):
+    """HS T42L20 with the Legendre contractions on the tensor cores (TF32x3, BF16x3): sim-days/s and
+    the error against the FP64 path after the same days from the same state."""
+    out = {}
+    spd = configs.STEPS_PER_DAY[WORKLOAD]
+    params = configs.PARAMS[WORKLOAD]
+    for prec in ("tf32x3", "bf16x3"):
+        m = configs.make_mesh(jgcm, WORKLOAD, precision=prec)
+        md = jgcm.Model(m, params)
+        configs.init_held_suarez(jgcm, m, md)
+        md.step(spd * days)
+        err = {k: configs.rel_l2(md.get(f), mod64.get(f))
+               for k, f in (("T", "grid_t_c"), ("u", "grid_u_c"), ("v", "grid_v_c"), ("ps", "grid_ps_c"))}
+        ms = md.time_steps(spd)
+        out[prec] = {"value": 1000.0 / ms, "unit": "sim-days/s", "error_vs_fp64_same_days": err}
+    return out
+
+
 def run_jgcm(args):
     import numpy as np
 
@@ -346,6 +397,14 @@ def run_jgcm(args):
             base = {"value": None, "unit": "sim-days/s", "cores": os.cpu_count(), "kind": "port",
                     "sample": f"failed: {e}"}
     launches = modmx.launches_per_step()
+    extra = {}
+    if not args.no_ensemble and world == 1:
+        try:
+            # error of the tensor-core modes after the same W + K days as the FP64 run
+            extra["tensor_core_modes"] = tensor_core_modes(jgcm, configs, mod64, days_done)
+            extra["ensemble"] = ensemble_bench(jgcm, configs, ["fp32", "tf32x3"])
+        except Exception as e:
+            extra["ensemble_error"] = str(e)
     line = {
         "metric": METRIC, "value": value, "unit": "sim-days/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": 1000.0 * t_mx / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -371,6 +430,7 @@ def run_jgcm(args):
                 "d2h_bytes_per_step": bytes_io},
         "gpu_launches": launches * spd * K,
         "clocks": clk,
+        **extra,
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -384,6 +444,7 @@ def main():
     ap.add_argument("--impl", default="jgcm", choices=["jgcm", "reference"])
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "tf32x3", "bf16x3"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble and tensor-core side runs")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, _ = dist_env()
