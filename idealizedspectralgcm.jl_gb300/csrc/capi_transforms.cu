@@ -155,6 +155,51 @@ extern "C" int jgcm_trans_grid_to_spherical(jgcm_mesh* m, const double* pfield, 
   return finish(m);
 }
 
+// Adjoint of Trans_Spherical_To_Grid!: grid cotangent -> spectral cotangent (row N+1 included).
+extern "C" int jgcm_trans_spherical_to_grid_adjoint(jgcm_mesh* m, const double* grid_bar, int nlev, double* spec_bar) {
+  JG_TRY(check_nlev(m, nlev));
+  size_t ns = 2 * spec_elems(m, nlev), ng = grid_elems(m, nlev);
+  JG_TRY(h2d(m, slot(m, 0), grid_bar, ng));
+  JG_TRY(grid_host_to_dev(m, slot(m, 0), m->d_grid[0], ng, m->stream));
+  FFTPlan fp;
+  memset(&fp, 0, sizeof(fp));
+  fp.ng = 1;
+  fp.C = nlev;
+  fp.g[0] = in_group(PRO_NONE, m->d_grid[0], nlev, 0);
+  G2SPlan gp;
+  memset(&gp, 0, sizeof(gp));
+  gp.ng = 1;
+  gp.C = nlev;
+  gp.g[0] = spec_group(G2S_ADJ_S2G, m->d_spec[0], nlev, 0, 0, -1, -1);
+  gp.g[0].scale = m->nlon;
+  JG_TRY(g2s(m, fp, gp));
+  JG_TRY(spec_dev_to_host(m, m->d_spec[0], slot(m, 1), nlev, m->stream));
+  JG_TRY(d2h(m, spec_bar, slot(m, 1), ns));
+  return finish(m);
+}
+
+// Adjoint of Trans_Grid_To_Spherical!: spectral cotangent (row N+1 ignored) -> grid cotangent.
+extern "C" int jgcm_trans_grid_to_spherical_adjoint(jgcm_mesh* m, const double* spec_bar, int nlev, double* grid_bar) {
+  JG_TRY(check_nlev(m, nlev));
+  size_t ns = 2 * spec_elems(m, nlev), ng = grid_elems(m, nlev);
+  JG_TRY(h2d(m, slot(m, 0), spec_bar, ns));
+  JG_TRY(spec_host_to_dev(m, slot(m, 0), m->d_spec[0], nlev, m->stream));
+  S2GPlan sp;
+  memset(&sp, 0, sizeof(sp));
+  sp.ng = 1;
+  sp.C = nlev;
+  sp.g[0] = s2g_group(S2G_ADJ_G2S, m->d_spec[0], nullptr, nlev, 0);
+  IFFTPlan ip;
+  memset(&ip, 0, sizeof(ip));
+  ip.ng = 1;
+  ip.C = nlev;
+  ip.g[0] = out_group(EPI_ADJ_G2S, m->d_grid[0], nlev, 0);
+  JG_TRY(s2g(m, sp, ip));
+  JG_TRY(grid_dev_to_host(m, m->d_grid[0], slot(m, 1), ng, m->stream));
+  JG_TRY(d2h(m, grid_bar, slot(m, 1), ng));
+  return finish(m);
+}
+
 extern "C" int jgcm_trans_grid_to_fourier(jgcm_mesh* m, const double* pfield, int nlev, double* fourier) {
   JG_TRY(check_nlev(m, nlev));
   size_t ng = grid_elems(m, nlev), nf = 2 * (size_t)(m->N + 1) * m->nlat * nlev;

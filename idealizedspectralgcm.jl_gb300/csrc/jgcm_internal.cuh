@@ -104,7 +104,8 @@ struct TableStore {
 // ------------------------------------------------------------------------------------------
 // Transform plans.  A launch processes a batch of columns; each group maps a contiguous
 // column range [col0, col0+L) to one field (one column per level).
-enum S2GOp { S2G_PLAIN = 0, S2G_DLAM = 1, S2G_DTH = 2, S2G_UCOS = 3, S2G_VCOS = 4 };
+// S2G_ADJ_G2S: input of the adjoint of the analysis (m >= 1 halved, row N+1 dropped)
+enum S2GOp { S2G_PLAIN = 0, S2G_DLAM = 1, S2G_DTH = 2, S2G_UCOS = 3, S2G_VCOS = 4, S2G_ADJ_G2S = 5 };
 struct S2GGroup {
   const void* a;  // spectral field (MNK, L levels)
   const void* b;  // second field (UCOS/VCOS: divergence; a = vorticity)
@@ -116,7 +117,8 @@ struct S2GPlan {
   S2GGroup g[JGCM_MAX_GROUPS];
 };
 
-enum GridEpi { EPI_NONE = 0, EPI_DIVCOS = 1, EPI_EXP2 = 2, EPI_DIVCOS_MULPS = 3 };
+// EPI_ADJ_G2S: x w_j / (2 nlon), the output scaling of the adjoint of the analysis
+enum GridEpi { EPI_NONE = 0, EPI_DIVCOS = 1, EPI_EXP2 = 2, EPI_DIVCOS_MULPS = 3, EPI_ADJ_G2S = 4 };
 struct GridOutGroup {
   void* dst;
   void* dst2;      // EPI_EXP2: exp(x)
@@ -147,7 +149,8 @@ struct FFTPlan {
   GridInGroup g[JGCM_MAX_GROUPS];
 };
 
-enum G2SOp { G2S_PLAIN = 0, G2S_VOR = 1, G2S_DIV = 2, G2S_BARO = 3, G2S_SW = 4 };
+// G2S_ADJ_S2G: adjoint of the synthesis, c_m nlon sum_j P F (unweighted quadrature, row N+1 kept)
+enum G2SOp { G2S_PLAIN = 0, G2S_VOR = 1, G2S_DIV = 2, G2S_BARO = 3, G2S_SW = 4, G2S_ADJ_S2G = 5 };
 // Fused time-stepping parameters for the G2S epilogues (barotropic / shallow water).
 struct StepParams {
   int init_step;
@@ -162,6 +165,7 @@ struct SpecOutGroup {
   const void* extra;  // DIV: spectral field added to G2S(E) before the Laplacian (SW: h_c), nullable
   const void* qc[3];  // BARO/SW: current level (vor, div, h) -- updated in place by the RA filter
   const void* qp[3];  // BARO/SW: previous level
+  double scale;       // ADJ_S2G: nlon
   int op, L, col0;
   int colA, colB, colE, colH;  // Fourier-buffer base columns of the input slots (-1 = unused)
 };

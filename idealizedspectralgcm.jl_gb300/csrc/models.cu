@@ -134,7 +134,7 @@ template <int NV>
 __device__ bool grid_reduce_last(const double* vals, double* partials, unsigned* counter, const double* wts,
                                  double* out) {
   __shared__ bool am_last;
-  __shared__ double red[NV][256];
+  __shared__ double red[NV][32];
   const int nb = gridDim.x * gridDim.y;
   const int bid = blockIdx.y * gridDim.x + blockIdx.x;
   if (threadIdx.x == 0) {
@@ -146,28 +146,24 @@ __device__ bool grid_reduce_last(const double* vals, double* partials, unsigned*
   __syncthreads();
   if (!am_last) return false;
   __threadfence();
-  // fold with the first nt threads (blockDim is a power of two; nt <= 256)
-  const int nt = blockDim.x < 256 ? blockDim.x : 256;
+  // every thread folds a fixed strided subset of the block partials (weighted by the latitude of
+  // the block's row), then warps and the block combine in a fixed order: deterministic
   double s[NV];
   for (int v = 0; v < NV; v++) s[v] = 0.0;
-  if (threadIdx.x < nt)
-    for (int jj = threadIdx.x; jj < (int)gridDim.y; jj += nt) {
-      for (int v = 0; v < NV; v++) {
-        double r = 0.0;
-#pragma unroll 8
-        for (int b = 0; b < (int)gridDim.x; b++) r += __ldcg(partials + (size_t)v * nb + (size_t)jj * gridDim.x + b);
-        s[v] += r * wts[jj];
-      }
-    }
-  if (threadIdx.x < nt)
-    for (int v = 0; v < NV; v++) red[v][threadIdx.x] = s[v];
-  __syncthreads();
-  for (int st = nt / 2; st > 0; st >>= 1) {
-    if (threadIdx.x < st)
-      for (int v = 0; v < NV; v++) red[v][threadIdx.x] += red[v][threadIdx.x + st];
-    __syncthreads();
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    const double w = wts[b / gridDim.x];
+    for (int v = 0; v < NV; v++) s[v] += __ldcg(partials + (size_t)v * nb + b) * w;
   }
-  for (int v = 0; v < NV; v++) out[v] = red[v][0];
+  for (int v = 0; v < NV; v++) s[v] = warp_sum(s[v]);
+  const int nw = (blockDim.x + 31) >> 5;
+  if ((threadIdx.x & 31) == 0)
+    for (int v = 0; v < NV; v++) red[v][threadIdx.x >> 5] = s[v];
+  __syncthreads();
+  for (int v = 0; v < NV; v++) {
+    double t = 0.0;
+    for (int q = 0; q < nw; q++) t += red[v][q];
+    out[v] = t;
+  }
   if (threadIdx.x == 0) *counter = 0u;
   return true;
 }
@@ -667,12 +663,14 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
 }
 
 template <typename T>
-__global__ void k_hs_corr_apply(T* t_n, T* ps_n, const double* scalars, size_t nt, size_t nps, size_t memL,
-                                size_t mem1) {
-  // member of element q: q / memL for the nd-level T, q / mem1 for ps
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < nt; q += (size_t)gridDim.x * blockDim.x) {
-    t_n[q] = t_n[q] + (T)scalars[4 * (q / memL) + 3];
-    if (q < nps) ps_n[q] = ps_n[q] * (T)scalars[4 * (q / mem1) + 2];
+__global__ void k_hs_corr_apply(T* t_n, T* ps_n, const double* scalars, size_t memL, size_t mem1) {
+  const int e = blockIdx.y;  // member: ps *= factor, T += correction
+  const T factor = (T)scalars[4 * e + 2], corr = (T)scalars[4 * e + 3];
+  T* t = t_n + (size_t)e * memL;
+  T* ps = ps_n + (size_t)e * mem1;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < memL; q += (size_t)gridDim.x * blockDim.x) {
+    t[q] = t[q] + corr;
+    if (q < mem1) ps[q] = ps[q] * factor;
   }
 }
 
@@ -1376,11 +1374,11 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   k_hs_corr_reduce<T><<<dim3((m->nlon + 31) / 32, m->nlat, E), 256, 0, st>>>(ca, md->d_vc);
   mark(st);
   JG_CUDA(cudaGetLastError());
-  const size_t G1 = grid_elems(m, 1), nt = grid_elems(m, L), nps = grid_elems(m, E);
-  int nb = (int)((nt + 255) / 256);
-  if (nb > 4 * 152) nb = 4 * 152;
-  k_hs_corr_apply<T><<<nb, 256, 0, st>>>((T*)md->grid_t[n], (T*)md->grid_ps[n], md->d_scalars, nt, nps,
-                                         (size_t)nd * G1, G1);
+  const size_t G1 = grid_elems(m, 1);
+  int nb = (int)(((size_t)nd * G1 + 255) / 256);
+  if (nb * E > 8 * 152) nb = (8 * 152 + E - 1) / E;
+  k_hs_corr_apply<T><<<dim3(nb, E), 256, 0, st>>>((T*)md->grid_t[n], (T*)md->grid_ps[n], md->d_scalars,
+                                                  (size_t)nd * G1, G1);
   mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;

@@ -62,6 +62,15 @@ __device__ __forceinline__ V2<T> s2g_input(const S2GGroup& g, const Tables<T>& t
       x = a[(mrow + n) * L + k];
       if (m == 0 && n == 0) x.x = x.x - (T)g.shift;
       break;
+    case S2G_ADJ_G2S:  // the synthesis weights every m >= 1 twice; the analysis never sees row N+1
+      if (n < ns) {
+        x = a[(mrow + n) * L + k];
+        if (m > 0) {
+          x.x = x.x * (T)0.5;
+          x.y = x.y * (T)0.5;
+        }
+      }
+      break;
     case S2G_DLAM: {  // coef_dlam .* (i h)
       T cf = tb.dlam[mrow + n];
       V h = a[(mrow + n) * L + k];
@@ -122,6 +131,7 @@ __device__ __forceinline__ void g2s_store(const G2SPlan& plan, const SpecOutGrou
   const T eig = tb.eig[mrow + n];
   switch (g.op) {
     case G2S_PLAIN:
+    case G2S_ADJ_S2G:
       ((V*)g.dst)[sidx] = r0;
       break;
     case G2S_VOR:

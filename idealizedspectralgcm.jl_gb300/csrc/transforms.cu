@@ -185,6 +185,9 @@ __global__ void __launch_bounds__(256) k_ifft(IFFTPlan plan, Tables<T> tb, const
       case EPI_DIVCOS_MULPS:
         dst[idx] = (x / tb.cosj[j]) * ((const T*)g.ps)[((size_t)k * nlat + j) * nlon + t];  // level k of ps
         break;
+      case EPI_ADJ_G2S:
+        dst[idx] = x * (T)(tb.wts[j] / (2.0 * nlon));
+        break;
     }
   }
 }
@@ -382,12 +385,37 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
       o.y = (n == ns) ? (T)0 : xi;
       return o;
     };
+    // adjoint of the synthesis: unweighted quadrature with P, c_m nlon, row N+1 kept
+    auto plain_adj = [&]() -> V {
+      const V* src = (even ? S : A) + cl;
+      const T* p = tb.P + (mrow + n) * nh;
+      T sr = 0, si = 0;
+#pragma unroll 4
+      for (int jh = q; jh < nh; jh += 4) {
+        T w = p[jh];
+        V x = src[jh * CT];
+        sr += x.x * w;
+        si += x.y * w;
+      }
+      sr += __shfl_xor_sync(qmask, sr, 1);
+      si += __shfl_xor_sync(qmask, si, 1);
+      sr += __shfl_xor_sync(qmask, sr, 2);
+      si += __shfl_xor_sync(qmask, si, 2);
+      const T sc = (T)((m == 0 ? 1.0 : 2.0) * g.scale);  // scale = nlon (the FFT returned fft / nlon)
+      V o;
+      o.x = sr * sc;
+      o.y = si * sc;
+      return o;
+    };
     // every lane of the quad takes part in the sums; lane q = 0 applies the epilogue
     V r0, r1, r2, r3;
     r0.x = r0.y = r1.x = r1.y = r2.x = r2.y = r3.x = r3.y = 0;
     switch (g.op) {
       case G2S_PLAIN:
         r0 = plain(0);
+        break;
+      case G2S_ADJ_S2G:
+        r0 = plain_adj();
         break;
       case G2S_VOR:
       case G2S_BARO:
@@ -493,7 +521,9 @@ int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp, cudaStream_t 
     cap = m->Cmax;
   }
   JG_TRY(launch_fft_only<T>(m, fp, st, fbuf, cap));
-  if (std::is_same<T, float>::value && m->tc.on) return launch_g2s_legendre_tc(m, gp, fp.C, st, fbuf);
+  bool adj = false;
+  for (int i = 0; i < gp.ng; i++) adj = adj || gp.g[i].op == G2S_ADJ_S2G;
+  if (std::is_same<T, float>::value && m->tc.on && !adj) return launch_g2s_legendre_tc(m, gp, fp.C, st, fbuf);
   Tables<T> tb = tables<T>(m);
   const int nh = m->nh, ct = g2s_ct(nh);
   size_t sm = (size_t)8 * ct * nh * sizeof(V);

@@ -72,6 +72,8 @@ def lib():
         "jgcm_trans_spherical_to_grid": (I, [P, P, I, P]),
         "jgcm_trans_grid_to_spherical": (I, [P, P, I, P]),
         "jgcm_trans_grid_to_fourier": (I, [P, P, I, P]),
+        "jgcm_trans_spherical_to_grid_adjoint": (I, [P, P, I, P]),
+        "jgcm_trans_grid_to_spherical_adjoint": (I, [P, P, I, P]),
         "jgcm_vor_div_from_grid_uv": (I, [P, P, P, I, P, P]),
         "jgcm_uv_grid_from_vor_div": (I, [P, P, P, I, P, P]),
         "jgcm_compute_gradients": (I, [P, P, I, P, P]),
@@ -208,6 +210,22 @@ def Trans_Grid_To_Spherical(mesh, pfield, snm):
     n = _nlev_grid(mesh, pfield)
     assert _nlev_spec(mesh, snm) == n
     _check(lib().jgcm_trans_grid_to_spherical(mesh._h, _ptr(pfield), n, _ptr(snm)))
+
+
+def Trans_Spherical_To_Grid_Adjoint(mesh, grid_bar, spec_bar):
+    """Adjoint of Trans_Spherical_To_Grid!: spec_bar = S2G^T grid_bar (row N+1 included)."""
+    nlev = _nlev_grid(mesh, grid_bar)
+    assert _nlev_spec(mesh, spec_bar) == nlev
+    _check(lib().jgcm_trans_spherical_to_grid_adjoint(mesh._h, _ptr(np.asfortranarray(grid_bar)), nlev,
+                                                      _ptr(spec_bar)))
+
+
+def Trans_Grid_To_Spherical_Adjoint(mesh, spec_bar, grid_bar):
+    """Adjoint of Trans_Grid_To_Spherical!: grid_bar = G2S^T spec_bar (row N+1 ignored)."""
+    nlev = _nlev_spec(mesh, spec_bar)
+    assert _nlev_grid(mesh, grid_bar) == nlev
+    _check(lib().jgcm_trans_grid_to_spherical_adjoint(mesh._h, _ptr(np.asfortranarray(spec_bar)), nlev,
+                                                      _ptr(grid_bar)))
 
 
 def Trans_Grid_To_Fourier(mesh, pfield, fourier):

@@ -73,6 +73,14 @@ int jgcm_mesh_synchronize(jgcm_mesh* mesh);
 int jgcm_trans_spherical_to_grid(jgcm_mesh* mesh, const double* snm, int nlev, double* pfield);
 /* Trans_Grid_To_Spherical!  Spectral_Spherical_Mesh.jl:221-293 */
 int jgcm_trans_grid_to_spherical(jgcm_mesh* mesh, const double* pfield, int nlev, double* snm);
+/* Adjoints of the two transforms (no counterpart in the reference; the differentiation pattern
+ * of the dynamical core): for the Euclidean inner products of the host arrays (complex entries as
+ * (re, im) pairs, entries n < m excluded), <S2G s, g> = <s, S2G^T g> and <G2S g, s> = <g, G2S^T s>.
+ * S2G^T is the transposed quadrature: forward DFT, then the unweighted Legendre sum c_m nlon
+ * sum_j P_n^m(mu_j) G_m(mu_j) (c_0 = 1, c_m = 2), row N+1 included; G2S^T synthesises the
+ * spectral cotangent (m >= 1 halved, row N+1 dropped) and scales each latitude by w_j / (2 nlon). */
+int jgcm_trans_spherical_to_grid_adjoint(jgcm_mesh* mesh, const double* grid_bar, int nlev, double* spec_bar);
+int jgcm_trans_grid_to_spherical_adjoint(jgcm_mesh* mesh, const double* spec_bar, int nlev, double* grid_bar);
 /* Trans_Grid_To_Fourier!  Spectral_Spherical_Mesh.jl:295-330; writes fourier modes m = 0..N
  * of fft/nλ as complex double[nlev][nlat][N+1] (modes above N are not used downstream). */
 int jgcm_trans_grid_to_fourier(jgcm_mesh* mesh, const double* pfield, int nlev, double* fourier);

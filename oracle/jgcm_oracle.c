@@ -592,3 +592,78 @@ double om_area_weighted_global_mean(om_mesh* M, const double* g) {
 }
 
 #include "jgcm_oracle_models.inc"
+
+/* ---- adjoints of the two transforms (test infrastructure for the differentiation pattern) ------
+ * Written directly from the forward definitions on every latitude (no parity folding, no FFT):
+ *   S2G: g(lam_t, mu_j) = sum_m c_m Re( sum_n s_mn P_n^m(mu_j) e^{i m lam_t} ),  c_0 = 1, c_m = 2,
+ *        Im s_0n does not reach the grid (Spectral_Spherical_Mesh.jl:143-217);
+ *   G2S: s_mn = 1/2 sum_j w_j P_n^m(mu_j) (1/nlon) sum_t g e^{-i m lam_t}, n <= N, row N+1 = 0
+ *        (Spectral_Spherical_Mesh.jl:221-293). */
+void om_trans_spherical_to_grid_adjoint(om_mesh* M, const double* gbar, int nlev, double* sbar) {
+  int N = M->N, ns = M->ns, nlat = M->nlat, nlon = M->nlon;
+  memset(sbar, 0, 2 * sizeof(double) * (size_t)(N + 1) * (ns + 1) * nlev);
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(OMP_THREADS)
+#endif
+  for (int k = 0; k < nlev; k++) {
+    double* Gc = zalloc((size_t)(N + 1) * nlat);
+    double* Gs = zalloc((size_t)(N + 1) * nlat);
+    for (int j = 0; j < nlat; j++)
+      for (int m = 0; m <= N; m++) {
+        double c = 0.0, sn = 0.0;
+        for (int t = 0; t < nlon; t++) {
+          double a = 6.283185307179586476925287 * (double)(((long)m * t) % nlon) / (double)nlon;
+          double x = gbar[(size_t)t + (size_t)nlon * ((size_t)j + (size_t)nlat * k)];
+          c += x * cos(a);
+          sn += x * sin(a);
+        }
+        Gc[m + (size_t)(N + 1) * j] = c;
+        Gs[m + (size_t)(N + 1) * j] = sn;
+      }
+    for (int m = 0; m <= N; m++) {
+      double cm = m == 0 ? 1.0 : 2.0;
+      for (int n = m; n <= ns; n++) {
+        double re = 0.0, im = 0.0;
+        for (int j = 0; j < nlat; j++) {
+          double q = M->qnm[TIX(m, n, j)];
+          re += q * Gc[m + (size_t)(N + 1) * j];
+          im -= q * Gs[m + (size_t)(N + 1) * j];
+        }
+        sbar[SIX(m, n, k)] = cm * re;
+        sbar[SIX(m, n, k) + 1] = m == 0 ? 0.0 : cm * im;
+      }
+    }
+    free(Gc);
+    free(Gs);
+  }
+}
+
+void om_trans_grid_to_spherical_adjoint(om_mesh* M, const double* sbar, int nlev, double* gbar) {
+  int N = M->N, ns = M->ns, nlat = M->nlat, nlon = M->nlon;
+#ifdef _OPENMP
+#pragma omp parallel for collapse(2) num_threads(OMP_THREADS)
+#endif
+  for (int k = 0; k < nlev; k++)
+    for (int j = 0; j < nlat; j++) {
+      double* a_re = zalloc(N + 1);
+      double* a_im = zalloc(N + 1);
+      for (int m = 0; m <= N; m++)
+        for (int n = m; n <= N && n < ns; n++) {
+          double q = M->qnm[TIX(m, n, j)];
+          a_re[m] += q * sbar[SIX(m, n, k)];
+          a_im[m] += q * sbar[SIX(m, n, k) + 1];
+        }
+      double sc = M->wts[j] / (2.0 * nlon);
+      for (int t = 0; t < nlon; t++) {
+        double g = 0.0;
+        for (int m = 0; m <= N; m++) {
+          double a = 6.283185307179586476925287 * (double)(((long)m * t) % nlon) / (double)nlon;
+          g += a_re[m] * cos(a) - a_im[m] * sin(a);
+        }
+        gbar[(size_t)t + (size_t)nlon * ((size_t)j + (size_t)nlat * k)] = sc * g;
+      }
+      free(a_re);
+      free(a_im);
+    }
+}
+

@@ -58,6 +58,9 @@ void om_compute_gradients(om_mesh* m, const double* hs, int nlev, double* dlam, 
 void om_add_horizontal_advection(om_mesh* m, const double* hs, const double* u, const double* v, int nlev,
                                  double* dh);
 void om_apply_laplacian(om_mesh* m, double* spe, int nlev);
+/* adjoints of Trans_Spherical_To_Grid! and Trans_Grid_To_Spherical! (Euclidean inner products) */
+void om_trans_spherical_to_grid_adjoint(om_mesh* m, const double* grid_bar, int nlev, double* spec_bar);
+void om_trans_grid_to_spherical_adjoint(om_mesh* m, const double* spec_bar, int nlev, double* grid_bar);
 double om_area_weighted_global_mean(om_mesh* m, const double* grid);
 
 /* ---- models (Barotropic_Dynamics.jl, Shallow_Water_Dynamics.jl, Spectral_Dynamics.jl) ---- */

@@ -75,6 +75,8 @@ def lib():
             "om_spectral_initialize_fields": (I, [P, P, I]),
             "om_model_semi_implicit": (L, [P, C.c_char_p, P, L]),
             "om_hs_forcing": (None, [P, I, P, P, P, P, P, P, P, P, P]),
+            "om_trans_spherical_to_grid_adjoint": (None, [P, P, I, P]),
+            "om_trans_grid_to_spherical_adjoint": (None, [P, P, I, P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(_lib, name)
@@ -305,3 +307,16 @@ def HS_Forcing(model, dt, grid_u, grid_v, grid_p_half, grid_p_full, grid_t, grid
         _ptr(a)
     lib().om_hs_forcing(model._h, int(dt), *[_ptr(a) for a in ins], _ptr(grid_du), _ptr(grid_dv), _ptr(grid_t_eq),
                         _ptr(grid_dt))
+
+
+def Trans_Spherical_To_Grid_Adjoint(mesh, grid_bar, spec_bar):
+    """Adjoint of Trans_Spherical_To_Grid!: spec_bar = S2G^T grid_bar."""
+    nlev = _nlev_grid(mesh, grid_bar)
+    lib().om_trans_spherical_to_grid_adjoint(mesh._h, _ptr(np.asfortranarray(grid_bar)), nlev, _ptr(spec_bar))
+
+
+def Trans_Grid_To_Spherical_Adjoint(mesh, spec_bar, grid_bar):
+    """Adjoint of Trans_Grid_To_Spherical!: grid_bar = G2S^T spec_bar."""
+    nlev = _nlev_spec(mesh, spec_bar)
+    lib().om_trans_grid_to_spherical_adjoint(mesh._h, _ptr(np.asfortranarray(spec_bar)), nlev, _ptr(grid_bar))
+
