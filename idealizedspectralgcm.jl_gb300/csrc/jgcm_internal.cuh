@@ -203,6 +203,8 @@ struct jgcm_mesh {
   jgcm::TableStore<float> t32;
   jgcm::TcTables tc;
   unsigned int* d_status;  // device error bits of the tensor-core kernels (bounded waits that gave up)
+  int tune[4];             // tile overrides: [1] S2G columns, [2] G2S columns, [3] FFT columns per block (0 = default)
+  int tune_gen;            // bumped when the tiles change: captured graphs of the mesh's models are stale
   // workspace
   int Cmax;
   void* d_fbuf;       // Fourier buffer [m][j][c] complex T, c < Cmax
@@ -261,6 +263,8 @@ void tc_tables_free(jgcm_mesh* m);
 int launch_s2g_legendre_tc(jgcm_mesh* m, const S2GPlan& sp, void* fbuf, cudaStream_t st);
 int launch_g2s_legendre_tc(jgcm_mesh* m, const G2SPlan& gp, int Cin, cudaStream_t st, void* fbuf);
 int tc_status(jgcm_mesh* m);  // reads and clears the device error bits
+
+size_t simt_smem_need(const jgcm_mesh* m, int s2g, int g2s, int fft);
 
 // mesh.cu
 int mesh_build_tables(jgcm_mesh* m);

@@ -54,6 +54,7 @@ struct jgcm_model {
   void* fbuf;  // Fourier buffer of fcap columns
   int fcap;
   int hs_lanes;  // lanes per column of the Held-Suarez column kernel (1, 2 or 4)
+  int graph_gen;  // the mesh's tile generation the captured graphs were built with
   double cp_air;
   // time-levelled state (index by rotation)
   void *spe_vor[3], *spe_div[3], *spe_lnps[3], *spe_t[3];
@@ -1408,8 +1409,20 @@ void after_step(jgcm_model* md) {
 }
 
 // One steady step through a CUDA graph captured for the current rotation phase.
+void drop_graphs(jgcm_model* md) {
+  for (auto& g : md->graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
 int graph_step(jgcm_model* md) {
   jgcm_mesh* m = md->mesh;
+  if (md->graph_gen != m->tune_gen) {  // tiles changed since the capture
+    drop_graphs(md);
+    md->graph_gen = m->tune_gen;
+  }
   int ph = md->rot;
   if (!md->graph[ph]) {
     cudaGraph_t g;
@@ -2042,6 +2055,276 @@ extern "C" int jgcm_model_copy_member(jgcm_model* dst, int dst_member, jgcm_mode
     dst->steps_done = src->steps_done;
   }
   JG_CUDA(cudaStreamSynchronize(st));
+  return JGCM_OK;
+}
+
+
+// ------------------------------------------------------------------------------------------
+// Ensembles of uneven truncations in one graph launch per time window: each member-batched model
+// advances window / dt steady steps on its own branch of one captured CUDA graph (forked from and
+// joined back into the ensemble's stream), so the truncations run concurrently and one launch
+// advances them all.  A window graph is keyed by the models' time-level rotations at its start
+// (which repeat with period 3), captured when first needed and replayed afterwards.
+struct jgcm_ensemble {
+  std::vector<jgcm_model*> models;
+  std::vector<int> steps;  // steady steps per window of each model
+  std::vector<cudaStream_t> side;
+  cudaStream_t st;
+  cudaEvent_t fork, t0, t1;
+  std::vector<cudaEvent_t> join;
+  std::vector<std::pair<std::vector<int>, cudaGraphExec_t>> graphs;  // (rotations at start, graph)
+};
+
+namespace {
+std::vector<int> ensemble_key(const jgcm_ensemble* en) {  // rotations and tiles at the window start
+  std::vector<int> k;
+  for (auto* md : en->models) {
+    k.push_back(md->rot);
+    k.push_back(md->mesh->tune_gen);
+    k.push_back(md->hs_lanes);
+  }
+  return k;
+}
+
+int ensemble_capture(jgcm_ensemble* en, cudaGraphExec_t* out) {
+  struct Saved {
+    int rot, init_step, sw_adv_from_n, steps_done;
+  };
+  std::vector<Saved> saved;
+  for (auto* md : en->models) saved.push_back({md->rot, md->init_step, md->sw_adv_from_n, md->steps_done});
+  cudaGraph_t g;
+  JG_CUDA(cudaStreamBeginCapture(en->st, cudaStreamCaptureModeThreadLocal));
+  int s = JGCM_OK;
+  cudaError_t e = cudaEventRecord(en->fork, en->st);
+  for (size_t i = 0; i < en->models.size() && s == JGCM_OK && e == cudaSuccess; i++) {
+    e = cudaStreamWaitEvent(en->side[i], en->fork, 0);
+    for (int k = 0; k < en->steps[i] && s == JGCM_OK && e == cudaSuccess; k++) {
+      s = issue(en->models[i], en->side[i]);
+      after_step(en->models[i]);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(en->join[i], en->side[i]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(en->st, en->join[i], 0);
+  }
+  cudaError_t e2 = cudaStreamEndCapture(en->st, &g);
+  for (size_t i = 0; i < en->models.size(); i++) {  // the graph has not run yet
+    en->models[i]->rot = saved[i].rot;
+    en->models[i]->init_step = saved[i].init_step;
+    en->models[i]->sw_adv_from_n = saved[i].sw_adv_from_n;
+    en->models[i]->steps_done = saved[i].steps_done;
+  }
+  if (s != JGCM_OK || e != cudaSuccess || e2 != cudaSuccess) {
+    if (e2 == cudaSuccess) cudaGraphDestroy(g);
+    if (s != JGCM_OK) return s;
+    JG_CUDA(e != cudaSuccess ? e : e2);
+  }
+  cudaError_t e3 = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  JG_CUDA(e3);
+  return JGCM_OK;
+}
+
+int ensemble_graph(jgcm_ensemble* en, cudaGraphExec_t* out) {
+  const std::vector<int> key = ensemble_key(en);
+  for (auto& kv : en->graphs)
+    if (kv.first == key) {
+      *out = kv.second;
+      return JGCM_OK;
+    }
+  cudaGraphExec_t g = nullptr;
+  JG_TRY(ensemble_capture(en, &g));
+  en->graphs.push_back({key, g});
+  *out = g;
+  return JGCM_OK;
+}
+
+int ensemble_window(jgcm_ensemble* en) {
+  cudaGraphExec_t g;
+  JG_TRY(ensemble_graph(en, &g));
+  JG_CUDA(cudaGraphLaunch(g, en->st));
+  for (size_t i = 0; i < en->models.size(); i++)
+    for (int k = 0; k < en->steps[i]; k++) after_step(en->models[i]);
+  return JGCM_OK;
+}
+
+void ensemble_free(jgcm_ensemble* en) {
+  if (!en) return;
+  for (auto& kv : en->graphs)
+    if (kv.second) cudaGraphExecDestroy(kv.second);
+  for (auto s : en->side)
+    if (s) cudaStreamDestroy(s);
+  for (auto ev : en->join)
+    if (ev) cudaEventDestroy(ev);
+  if (en->fork) cudaEventDestroy(en->fork);
+  if (en->t0) cudaEventDestroy(en->t0);
+  if (en->t1) cudaEventDestroy(en->t1);
+  if (en->st) cudaStreamDestroy(en->st);
+  delete en;
+}
+}  // namespace
+
+extern "C" int jgcm_ensemble_create(jgcm_model* const* models, int nmodels, int window_seconds,
+                                    jgcm_ensemble** out) {
+  JG_ARG(models && out && nmodels >= 1 && nmodels <= 64, "need 1..64 models");
+  JG_ARG(window_seconds > 0, "window_seconds must be positive");
+  *out = nullptr;
+  for (int i = 0; i < nmodels; i++) {
+    JG_ARG(models[i], "model %d is NULL", i);
+    JG_ARG(window_seconds % models[i]->P.dt == 0, "window %d s is not a multiple of model %d's dt (%d s)",
+           window_seconds, i, models[i]->P.dt);
+    JG_ARG(!models[i]->init_step && !models[i]->sw_adv_from_n,
+           "model %d is still in its first step: step every model once before grouping", i);
+    for (int k = 0; k < i; k++) JG_ARG(models[k] != models[i], "model %d appears twice", i);
+    JG_ARG(models[i]->mesh->device == models[0]->mesh->device, "all models must live on one device");
+  }
+  jgcm_ensemble* en = new jgcm_ensemble();
+  auto fail = [&](cudaError_t e) -> int {
+    set_error("ensemble: %s", cudaGetErrorString(e));
+    ensemble_free(en);
+    return JGCM_E_CUDA;
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&en->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&en->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreate(&en->t0);
+  if (e == cudaSuccess) e = cudaEventCreate(&en->t1);
+  if (e != cudaSuccess) return fail(e);
+  for (int i = 0; i < nmodels; i++) {
+    en->models.push_back(models[i]);
+    en->steps.push_back(window_seconds / models[i]->P.dt);
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev = nullptr;
+    e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    en->side.push_back(s);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    en->join.push_back(ev);
+    if (e != cudaSuccess) return fail(e);
+  }
+  // work already queued on the models' own streams comes first
+  for (auto* md : en->models) {
+    e = cudaStreamSynchronize(md->mesh->stream);
+    if (e != cudaSuccess) return fail(e);
+  }
+  *out = en;
+  return JGCM_OK;
+}
+
+extern "C" int jgcm_ensemble_step(jgcm_ensemble* en, int nwindows) {
+  JG_ARG(en && nwindows >= 0, "bad arguments");
+  for (auto* md : en->models) JG_CUDA(cudaStreamSynchronize(md->mesh->stream));  // work queued on a model alone
+  for (int w = 0; w < nwindows; w++) JG_TRY(ensemble_window(en));
+  JG_CUDA(cudaStreamSynchronize(en->st));
+  return JGCM_OK;
+}
+
+extern "C" int jgcm_ensemble_time(jgcm_ensemble* en, int nwindows, float* ms) {
+  JG_ARG(en && ms && nwindows >= 1, "bad arguments");
+  for (auto* md : en->models) JG_CUDA(cudaStreamSynchronize(md->mesh->stream));
+  cudaGraphExec_t g;
+  JG_TRY(ensemble_graph(en, &g));  // the first window's graph is captured outside the timed region
+  JG_CUDA(cudaEventRecord(en->t0, en->st));
+  for (int w = 0; w < nwindows; w++) JG_TRY(ensemble_window(en));
+  JG_CUDA(cudaEventRecord(en->t1, en->st));
+  JG_CUDA(cudaEventSynchronize(en->t1));
+  JG_CUDA(cudaEventElapsedTime(ms, en->t0, en->t1));
+  return JGCM_OK;
+}
+
+extern "C" int jgcm_ensemble_destroy(jgcm_ensemble* en) {
+  if (!en) return JGCM_OK;
+  cudaStreamSynchronize(en->st);
+  ensemble_free(en);
+  return JGCM_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// Tiles and their autotuner.  Knobs: [0] lanes per column of the Held-Suarez column kernel
+// (model), [1] S2G columns, [2] G2S columns, [3] FFT columns per block of the SIMT transform
+// kernels (mesh: shared by the models of the mesh).  0 keeps the default.
+extern "C" int jgcm_model_get_tuning(jgcm_model* md, int* knobs, int n) {
+  JG_ARG(md && knobs && n >= 4, "need 4 knobs");
+  knobs[0] = md->hs_lanes;
+  for (int i = 1; i < 4; i++) knobs[i] = md->mesh->tune[i];
+  return JGCM_OK;
+}
+
+extern "C" int jgcm_model_set_tuning(jgcm_model* md, const int* knobs, int n) {
+  JG_ARG(md && knobs && n >= 4, "need 4 knobs");
+  jgcm_mesh* m = md->mesh;
+  const int lanes = knobs[0] > 0 ? knobs[0] : hs_lanes(m, md->ne, md->nd);
+  JG_ARG(lanes == 1 || lanes == 2 || lanes == 4, "lanes per column must be 1, 2 or 4");
+  for (int i = 1; i < 4; i++) JG_ARG(knobs[i] >= 0 && knobs[i] <= 256, "tile %d out of range", i);
+  int t[4] = {0, knobs[1], knobs[2], knobs[3]};
+  const int s2g = t[1] > 0 ? t[1] : (m->nh >= 256 ? 1 : 256 / m->nh);
+  const int g2s = t[2] > 0 ? t[2] : (m->nh >= 64 ? 4 : m->nh >= 32 ? 8 : 16);
+  const int fft = t[3] > 0 ? t[3] : (m->nlon >= 1024 ? 1 : 1024 / m->nlon);
+  JG_ARG(g2s % 4 == 0 || t[2] == 0, "G2S columns per block must be a multiple of 4");
+  JG_ARG(simt_smem_need(m, s2g, g2s, fft) <= kSmemBudget, "tiles need more than %zu bytes of shared memory",
+         kSmemBudget);
+  JG_CUDA(cudaStreamSynchronize(m->stream));
+  if (lanes != md->hs_lanes) {
+    md->hs_lanes = lanes;
+    drop_graphs(md);
+  }
+  bool changed = false;
+  for (int i = 1; i < 4; i++) changed = changed || m->tune[i] != t[i];
+  if (changed) {
+    for (int i = 1; i < 4; i++) m->tune[i] = t[i];
+    m->tune_gen++;
+  }
+  return JGCM_OK;
+}
+
+// Coordinate search over the knobs on a scratch copy of the model (its state is left untouched):
+// each candidate is timed with CUDA events over `nsteps` captured steps (after one untimed step
+// that captures the graphs); the fastest setting of each knob is kept before the next is tried.
+extern "C" int jgcm_model_autotune(jgcm_model* md, int nsteps, int* knobs_out, float* ms_out) {
+  JG_ARG(md && nsteps >= 1, "bad arguments");
+  jgcm_mesh* m = md->mesh;
+  jgcm_model* sc = nullptr;
+  JG_TRY(jgcm_model_create_members(m, &md->P, md->ne, &sc));
+  struct Guard {
+    jgcm_model* p;
+    ~Guard() { jgcm_model_destroy(p); }
+  } guard{sc};
+  sc->init_step = md->init_step;  // the scratch ensemble takes the model's time-step state
+  sc->sw_adv_from_n = md->sw_adv_from_n;
+  for (int e = 0; e < md->ne; e++) JG_TRY(jgcm_model_copy_member(sc, e, md, e));
+  if (sc->init_step || sc->sw_adv_from_n) JG_TRY(jgcm_model_step(sc, 1));
+  int cur[4];
+  JG_TRY(jgcm_model_get_tuning(md, cur, 4));
+  auto timed = [&](const int* k, float* ms) -> int {
+    JG_TRY(jgcm_model_set_tuning(sc, k, 4));
+    JG_TRY(jgcm_model_step(sc, 3));  // captures the three rotation phases
+    return jgcm_model_time_steps(sc, nsteps, ms);
+  };
+  float best = 0.f;
+  JG_TRY(timed(cur, &best));
+  const int d1 = m->nh >= 256 ? 1 : 256 / m->nh, d2 = m->nh >= 64 ? 4 : m->nh >= 32 ? 8 : 16,
+            d3 = m->nlon >= 1024 ? 1 : 1024 / m->nlon;
+  std::vector<std::vector<int>> cand = {
+      {1, 2, 4}, {std::max(1, d1 / 2), d1, 2 * d1, 4 * d1}, {4, 8, 16, 32}, {std::max(1, d3 / 2), d3, 2 * d3}};
+  if (md->P.kind != JGCM_HELD_SUAREZ) cand[0] = {cur[0]};
+  for (int knob = 0; knob < 4; knob++)
+    for (int v : cand[knob]) {
+      int k[4] = {cur[0], cur[1], cur[2], cur[3]};
+      k[knob] = v;
+      if (knob == 1 && v == d1) k[1] = 0;
+      if (knob == 2 && v == d2) k[2] = 0;
+      if (knob == 3 && v == d3) k[3] = 0;
+      if (k[knob] == cur[knob]) continue;
+      const int s2g = k[1] ? k[1] : d1, g2s = k[2] ? k[2] : d2, fft = k[3] ? k[3] : d3;
+      if (simt_smem_need(m, s2g, g2s, fft) > kSmemBudget) continue;
+      if (knob == 0 && (md->nd + v - 1) / v < 2) continue;
+      float ms = 0.f;
+      if (timed(k, &ms) != JGCM_OK) continue;
+      if (ms < best) {
+        best = ms;
+        for (int i = 0; i < 4; i++) cur[i] = k[i];
+      }
+    }
+  JG_TRY(jgcm_model_set_tuning(md, cur, 4));
+  if (knobs_out)
+    for (int i = 0; i < 4; i++) knobs_out[i] = cur[i];
+  if (ms_out) *ms_out = best;
   return JGCM_OK;
 }
 

@@ -16,6 +16,7 @@
 //                    Robert-Asselin filter and the shallow-water semi-implicit correction).
 // Spectral prologues build the inputs of the synthesis on the fly from neighbouring total
 // wavenumbers (gradient, Compute_Gradient_Cos! :655-692; ucos/vcos, :517-580).
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 #include <type_traits>
@@ -453,10 +454,17 @@ static int configure_smem() {
   return JGCM_OK;
 }
 
-static inline int s2g_ct(int nh) { return nh >= 256 ? 1 : 256 / nh; }
-// columns per FFT block: CT * nlon/4 butterflies per stage = 256 threads
-static inline int fft_ct(int nlon) { return nlon >= 1024 ? 1 : 1024 / nlon; }
-static inline int g2s_ct(int nh) { return nh >= 64 ? 4 : nh >= 32 ? 8 : 16; }
+// column tiles per block; a tuned value (jgcm_model_set_tuning / the autotuner) overrides the default
+static inline int s2g_ct(const jgcm_mesh* m) {
+  return m->tune[1] > 0 ? m->tune[1] : m->nh >= 256 ? 1 : 256 / m->nh;
+}
+static inline int g2s_ct(const jgcm_mesh* m) {
+  return m->tune[2] > 0 ? m->tune[2] : m->nh >= 64 ? 4 : m->nh >= 32 ? 8 : 16;
+}
+// columns per FFT block: CT * nlon/4 butterflies per stage = 256 threads by default
+static inline int fft_ct(const jgcm_mesh* m) {
+  return m->tune[3] > 0 ? m->tune[3] : m->nlon >= 1024 ? 1 : 1024 / m->nlon;
+}
 
 // Legendre synthesis then inverse FFT, with the Fourier coefficients staged in `fbuf`
 // ((N+1) x nlat x C complex T).
@@ -465,7 +473,7 @@ static int launch_s2g_into(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, 
   using V = V2<T>;
   JG_TRY(configure_smem<T>());
   Tables<T> tb = tables<T>(m);
-  const int nh = m->nh, ct = s2g_ct(nh);
+  const int nh = m->nh, ct = s2g_ct(m);
   if (std::is_same<T, float>::value && m->tc.on) {
     JG_TRY(launch_s2g_legendre_tc(m, sp, fbuf, st));
   } else {
@@ -475,7 +483,7 @@ static int launch_s2g_into(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, 
     mark(st);
     JG_CUDA(cudaGetLastError());
   }
-  const int fc = fft_ct(m->nlon);
+  const int fc = fft_ct(m);
   size_t sm2 = align16((size_t)(fc * m->nlon + m->nlon) * sizeof(T)) + (size_t)(m->N + 1) * fc * sizeof(V);
   dim3 g2((ip.C + fc - 1) / fc, m->nlat);
   k_ifft<T><<<g2, 256, sm2, st>>>(ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon, m->logn - 1, fc);
@@ -504,7 +512,7 @@ int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp, cudaStream_t st, void* fbuf
   }
   JG_ARG(fp.C <= cap && fp.C > 0, "bad FFT plan");
   Tables<T> tb = tables<T>(m);
-  const int fc = fft_ct(m->nlon);
+  const int fc = fft_ct(m);
   size_t sm = (size_t)(fc * m->nlon + m->nlon) * sizeof(T);
   dim3 g((fp.C + fc - 1) / fc, m->nlat);
   k_fft<T><<<g, 256, sm, st>>>(fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon, m->logn - 1, fc);
@@ -525,7 +533,7 @@ int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp, cudaStream_t 
   for (int i = 0; i < gp.ng; i++) adj = adj || gp.g[i].op == G2S_ADJ_S2G;
   if (std::is_same<T, float>::value && m->tc.on && !adj) return launch_g2s_legendre_tc(m, gp, fp.C, st, fbuf);
   Tables<T> tb = tables<T>(m);
-  const int nh = m->nh, ct = g2s_ct(nh);
+  const int nh = m->nh, ct = g2s_ct(m);
   size_t sm = (size_t)8 * ct * nh * sizeof(V);
   const size_t tab = (size_t)3 * (m->ns + 1) * nh * sizeof(T);
   const int stage = sm + tab <= kSmemBudget;
@@ -762,3 +770,15 @@ extern "C" int jgcm_trans_spherical_to_grid_noalloc(jgcm_mesh* m, const void* d_
   return is_fp64(m) ? launch_s2g_into<double>(m, sp, ip, st, (double2*)scratch)
                     : launch_s2g_into<float>(m, sp, ip, st, (float2*)scratch);
 }
+
+namespace jgcm {
+// shared memory of the SIMT transform kernels with tiles (s2g, g2s, fft); 0 = the mesh's current
+size_t simt_smem_need(const jgcm_mesh* m, int s2g, int g2s, int fft) {
+  const size_t ts = tsize(m), nh = m->nh, ns1 = m->ns + 1, nlon = m->nlon;
+  const size_t a = align16(ns1 * nh * ts) + ns1 * (size_t)s2g * 2 * ts;
+  const size_t b = 8 * (size_t)g2s * nh * 2 * ts;
+  const size_t c = align16(((size_t)fft * nlon + nlon) * ts) + (size_t)(m->N + 1) * fft * 2 * ts;
+  return std::max(a, std::max(b, c));
+}
+}  // namespace jgcm
+

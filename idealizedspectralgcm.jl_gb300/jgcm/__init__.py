@@ -84,6 +84,13 @@ def lib():
         "jgcm_model_create_members": (I, [P, P, I, PP]),
         "jgcm_model_members": (I, [P, C.POINTER(I)]),
         "jgcm_model_copy_member": (I, [P, I, P, I]),
+        "jgcm_model_get_tuning": (I, [P, C.POINTER(I), I]),
+        "jgcm_model_set_tuning": (I, [P, C.POINTER(I), I]),
+        "jgcm_model_autotune": (I, [P, I, C.POINTER(I), C.POINTER(C.c_float)]),
+        "jgcm_ensemble_create": (I, [C.POINTER(P), I, I, PP]),
+        "jgcm_ensemble_step": (I, [P, I]),
+        "jgcm_ensemble_time": (I, [P, I, C.POINTER(C.c_float)]),
+        "jgcm_ensemble_destroy": (I, [P]),
         "jgcm_model_destroy": (I, [P]),
         "jgcm_model_get_field": (I, [P, C.c_char_p, P, Lg, C.POINTER(Lg)]),
         "jgcm_model_set_field": (I, [P, C.c_char_p, P, Lg]),
@@ -428,3 +435,79 @@ def HS_Forcing(model, dt, grid_u, grid_v, grid_p_half, grid_p_full, grid_t, grid
         assert a.shape == ins[0].shape and a.dtype == np.float64, "output shape/dtype"
     _check(lib().jgcm_hs_forcing(model._h, int(dt), *[_ptr(a) for a in ins], _ptr(grid_du), _ptr(grid_dv),
                                  _ptr(grid_t_eq), _ptr(grid_dt)))
+
+
+class Ensemble:
+    """Models of uneven truncations / kinds advanced together: each window of `window_seconds` is
+    one CUDA-graph launch whose branches step every model concurrently (window_seconds a multiple
+    of every model's dt; every model past its first step)."""
+
+    def __init__(self, models, window_seconds):
+        self.models = list(models)
+        arr = (C.c_void_p * len(self.models))(*[m._h.value for m in self.models])
+        h = C.c_void_p()
+        _check(lib().jgcm_ensemble_create(arr, len(self.models), int(window_seconds), C.byref(h)))
+        self._h = h
+
+    def step(self, nwindows=1):
+        _check(lib().jgcm_ensemble_step(self._h, int(nwindows)))
+
+    def time_windows(self, nwindows):
+        """Advance nwindows windows and return their CUDA-event time in ms."""
+        ms = C.c_float()
+        _check(lib().jgcm_ensemble_time(self._h, int(nwindows), C.byref(ms)))
+        return float(ms.value)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().jgcm_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+TUNING_KNOBS = ("lanes_per_column", "s2g_columns", "g2s_columns", "fft_columns")
+
+
+def get_tuning(model):
+    k = (C.c_int * 4)()
+    _check(lib().jgcm_model_get_tuning(model._h, k, 4))
+    return dict(zip(TUNING_KNOBS, list(k)))
+
+
+def set_tuning(model, tuning):
+    k = (C.c_int * 4)(*[int(tuning.get(n, 0)) for n in TUNING_KNOBS])
+    _check(lib().jgcm_model_set_tuning(model._h, k, 4))
+
+
+def autotune(model, nsteps=24, cache=None):
+    """Pick the tiles of `model` (and its mesh) by timing candidates on a scratch copy; with a
+    `cache` path, results are stored in (and reused from) that JSON file, keyed by the workload
+    and the device."""
+    import json
+
+    m = model.mesh
+    dev = device_info()
+    key = (f"{model.params.get('kind')}:N{m.num_fourier}:{m.nlat}x{m.nlon}x{m.nd}:members{model.members}:"
+           f"prec{m.precision}:sm{dev['sm_count']}:cc{dev['cc'][0]}{dev['cc'][1]}")
+    table = {}
+    if cache and os.path.exists(cache):
+        with open(cache) as f:
+            table = json.load(f)
+    if key in table:
+        set_tuning(model, table[key]["tuning"])
+        return table[key]
+    k = (C.c_int * 4)()
+    ms = C.c_float()
+    _check(lib().jgcm_model_autotune(model._h, int(nsteps), k, C.byref(ms)))
+    entry = {"tuning": dict(zip(TUNING_KNOBS, list(k))), "ms_per_step": float(ms.value) / nsteps}
+    if cache:
+        table[key] = entry
+        with open(cache, "w") as f:
+            json.dump(table, f, indent=1, sort_keys=True)
+    return entry
+

@@ -153,6 +153,24 @@ int jgcm_model_members(jgcm_model* model, int* members);
  * time level of the prognostic state and the grid diagnostics.  A one-member dst also takes the
  * source's time-step state (init step); an ensemble dst must already share it. */
 int jgcm_model_copy_member(jgcm_model* dst, int dst_member, jgcm_model* src, int src_member);
+/* Tiles (no counterpart in the reference).  knobs[0]: lanes per column of the Held-Suarez column
+ * kernel (1, 2, 4; this model); knobs[1..3]: S2G, G2S and FFT columns per block of the SIMT
+ * transform kernels (the mesh: shared by its models).  0 = default.  The autotuner times candidate
+ * tiles on a scratch copy of the model (coordinate search, nsteps captured steps each), applies the
+ * fastest and returns it with its time per nsteps. */
+int jgcm_model_get_tuning(jgcm_model* model, int* knobs, int n);
+int jgcm_model_set_tuning(jgcm_model* model, const int* knobs, int n);
+int jgcm_model_autotune(jgcm_model* model, int nsteps, int* knobs, float* ms);
+/* Uneven ensembles (no counterpart in the reference): several (member-batched) models of
+ * different truncations or kinds advanced together, window_seconds of simulated time per window,
+ * each window one graph launch whose branches step the models concurrently (window_seconds a
+ * multiple of every model's dt; every model past its first step).  The models stay usable on
+ * their own between windows. */
+typedef struct jgcm_ensemble jgcm_ensemble;
+int jgcm_ensemble_create(jgcm_model* const* models, int nmodels, int window_seconds, jgcm_ensemble** out);
+int jgcm_ensemble_step(jgcm_ensemble* ensemble, int nwindows);
+int jgcm_ensemble_time(jgcm_ensemble* ensemble, int nwindows, float* ms); /* CUDA-event ms of nwindows */
+int jgcm_ensemble_destroy(jgcm_ensemble* ensemble);
 int jgcm_model_destroy(jgcm_model* model);
 /* Read / write one Dyn_Data field (Dyn_Data.jl:4-156) by its reference name with the
  * δ spelled "d": "spe_vor_c", "grid_u_p", "spe_dt", "grid_t_eq", "grid_p_full",

@@ -70,3 +70,85 @@ def test_ensemble_rejects_direct_field_access(jg):
     md = jg.Model(mesh, params)
     with pytest.raises(AssertionError):
         md.copy_member(1, ens, 0)  # member out of range
+
+
+def _ready(jg, name, prec, members, seed0):
+    params = configs.PARAMS[name]
+    mesh = configs.make_mesh(jg, name, precision=prec)
+    ens = jg.Model(mesh, params, members=members)
+    one = jg.Model(mesh, params)
+    for e in range(members):
+        _init(jg, params["kind"], mesh, one, seed0 + e)
+        ens.copy_member(e, one)
+    ens.step(1)  # the first (init) step runs eagerly
+    return mesh, ens
+
+
+def test_uneven_ensemble_one_graph_per_window(jg):
+    """HS T21L20 x3, HS T42L20 x2 and SW T85 x2 (dt 600 s, two steps per 1200 s window) advanced by
+    ensemble windows equal the same models advanced one by one."""
+    specs = [("hs_t21l20", "fp32", 3), ("hs_t42l20", "fp32", 2), ("sw_t85", "fp32", 2)]
+    a = [_ready(jg, n, p, e, configs.BASE_SEED + 10 * i) for i, (n, p, e) in enumerate(specs)]
+    b = [_ready(jg, n, p, e, configs.BASE_SEED + 10 * i) for i, (n, p, e) in enumerate(specs)]
+    ens = jg.Ensemble([m for _, m in a], 1200)
+    windows = 4
+    ens.step(windows - 1)
+    ms = ens.time_windows(1)
+    assert ms > 0
+    for (name, _, _), (_, md) in zip(specs, b):
+        md.step(windows * 1200 // configs.PARAMS[name]["dt"])
+    for (name, prec, E), (mesh_a, ma), (mesh_b, mb) in zip(specs, a, b):
+        kind = configs.PARAMS[name]["kind"]
+        x, y = jg.Model(mesh_a, configs.PARAMS[name]), jg.Model(mesh_b, configs.PARAMS[name])
+        for e in range(E):
+            x.copy_member(0, ma, e)
+            y.copy_member(0, mb, e)
+            for f in configs.PROGNOSTIC[kind]:
+                assert configs.rel_l2(x.get(f), y.get(f)) < 1e-12, (name, e, f)
+    ens.close()
+
+
+def test_uneven_ensemble_rejects_bad_windows(jg):
+    mesh, md = _ready(jg, "hs_t21l20", "fp32", 1, configs.BASE_SEED)
+    with pytest.raises(AssertionError):
+        jg.Ensemble([md], 1000)  # not a multiple of dt = 1200 s
+    fresh = jg.Model(mesh, configs.PARAMS["hs_t21l20"])
+    with pytest.raises(AssertionError):
+        jg.Ensemble([fresh], 1200)  # still in its first step
+
+
+def test_autotuner_keeps_results_and_caches(jg, tmp_path):
+    """The autotuner only changes tiles: the tuned model steps to the same state as an untuned twin
+    (FP64: identical arithmetic per column; the tile sizes only regroup the same sums), and a second
+    call is served from the JSON cache."""
+    name = "hs_t21l20"
+    params = configs.PARAMS[name]
+    mesh_a = configs.make_mesh(jg, name, precision="fp64")
+    mesh_b = configs.make_mesh(jg, name, precision="fp64")
+    a, b = jg.Model(mesh_a, params, members=2), jg.Model(mesh_b, params, members=2)
+    one = jg.Model(mesh_a, params)
+    for e in range(2):
+        configs.init_held_suarez(jg, mesh_a, one, seed=configs.BASE_SEED + e)
+        a.copy_member(e, one)
+    two = jg.Model(mesh_b, params)
+    for e in range(2):
+        configs.init_held_suarez(jg, mesh_b, two, seed=configs.BASE_SEED + e)
+        b.copy_member(e, two)
+    a.step(2)
+    b.step(2)
+    cache = str(tmp_path / "tiles.json")
+    first = jg.autotune(a, nsteps=4, cache=cache)
+    assert set(first["tuning"]) == set(jg.TUNING_KNOBS) and first["ms_per_step"] > 0
+    again = jg.autotune(a, nsteps=4, cache=cache)
+    assert again == first
+    assert jg.get_tuning(a)["lanes_per_column"] in (1, 2, 4)
+    a.step(6)
+    b.step(6)
+    x, y = jg.Model(mesh_a, params), jg.Model(mesh_b, params)
+    for e in range(2):
+        x.copy_member(0, a, e)
+        y.copy_member(0, b, e)
+        for f in configs.PROGNOSTIC["held_suarez"]:
+            assert configs.rel_l2(x.get(f), y.get(f)) < 1e-10, (e, f)
+    with pytest.raises(AssertionError):
+        jg.set_tuning(a, {"lanes_per_column": 3})
