@@ -2328,3 +2328,339 @@ extern "C" int jgcm_model_autotune(jgcm_model* md, int nsteps, int* knobs_out, f
   return JGCM_OK;
 }
 
+
+// ------------------------------------------------------------------------------------------
+// One semi-implicit step on its own, and its adjoint (the differentiation pattern; no counterpart in
+// the reference).  The step is Adjust_δlnps_δt_δdiv! + Implicit_Correction! (Semi_Implicit.jl:
+// 360-513), Compute_Spectral_Damping! and Filtered_Leapfrog! (Time_Integrator.jl:58-101) for one
+// model step: a linear map, per spectral mode (m,n), of the tendencies and the p and c time levels
+// to the n level and the filtered c level.  The adjoint reverses it mode by mode with the transposed
+// vertical operators, built once on the host in FP64 as matrices (Linear_Ps_T_δdiv!: d -> (δps,
+// δT); Linear_Geopot_δt!: δT -> Φ) from the same column functions as the wave matrices, and W_n^T.
+namespace {
+struct AdjMats {  // vertical operators A, row-major (A[k][c] at k*nd + c); matT applies A^T
+  double *Apt, *spt, *Ageo, *hk;
+};
+
+int adj_mats(jgcm_model* md, AdjMats* out) {
+  const int nd = md->nd;
+  std::vector<double> Apt((size_t)nd * nd), spt(nd), Ageo((size_t)nd * nd), hk(nd), e(nd), dtt(nd), geo(nd);
+  for (int c = 0; c < nd; c++) {
+    std::fill(e.begin(), e.end(), 0.0);
+    e[c] = 1.0;
+    double dps = 0.0;
+    lin_ps_t_col(md->vc, nd, md->P.kappa, e.data(), &dps, dtt.data());
+    spt[c] = dps;
+    // response of level k to a unit input at level c is A[k][c]; stored at [k][c] (row-major A), so
+    // that lane k reading M[c*nd + k] over c walks column k of A, i.e. row k of A^T
+    for (int k = 0; k < nd; k++) Apt[(size_t)k * nd + c] = dtt[k];
+    lin_geo_col(md->vc, nd, md->P.rdgas, e.data(), geo.data());
+    for (int k = 0; k < nd; k++) Ageo[(size_t)k * nd + c] = geo[k];
+  }
+  for (int k = 0; k < nd; k++) hk[k] = md->vc.h[k] * md->P.ps_ref;
+  double* d = nullptr;
+  JG_TRY(alloc((void**)&d, (2 * (size_t)nd * nd + 2 * nd) * 8));
+  out->Apt = d;
+  out->Ageo = d + (size_t)nd * nd;
+  out->spt = d + 2 * (size_t)nd * nd;
+  out->hk = out->spt + nd;
+  JG_CUDA(cudaMemcpy(out->Apt, Apt.data(), Apt.size() * 8, cudaMemcpyHostToDevice));
+  JG_CUDA(cudaMemcpy(out->Ageo, Ageo.data(), Ageo.size() * 8, cudaMemcpyHostToDevice));
+  JG_CUDA(cudaMemcpy(out->spt, spt.data(), nd * 8, cudaMemcpyHostToDevice));
+  JG_CUDA(cudaMemcpy(out->hk, hk.data(), nd * 8, cudaMemcpyHostToDevice));
+  return JGCM_OK;
+}
+
+// cotangents of the step's outputs -> cotangents of its inputs; arrays MNK, nd levels (lnps: 1)
+template <typename T>
+struct AdjArgs {
+  const V2<T>*vn_b, *vc_b, *dn_b, *dc_b, *tn_b, *tc_b, *ln_b, *lc_b;                 // outputs' cotangents
+  V2<T>*dvor_b, *ddiv_b, *dt_b, *dl_b, *vp_b, *vcin_b, *dp_b, *dcin_b, *tp_b, *tcin_b, *lp_b, *lcin_b;  // inputs'
+  const T *damping, *dfac;
+  const double *eig64, *W, *Apt, *spt, *Ageo, *hk;
+  const int2* pairs;
+  int npairs, nd, ns, N, init_step, dt;
+  double xi, ps_ref, robert;
+};
+
+// y = M^T x for row-major M: y_k = sum_c M[c][k] x_c at the lane's level k; lanes >= nd return 0
+template <typename R>
+__device__ __forceinline__ R matT(const double* M, R x, int lane, int nd) {
+  R y = 0;
+  for (int c = 0; c < nd; c++) {
+    R xc = __shfl_sync(FULL, x, c);
+    if (lane < nd) y += (R)M[(size_t)c * nd + lane] * xc;
+  }
+  return y;
+}
+
+template <typename R>
+__device__ __forceinline__ void lf_adj(int init, R Dt, R rob, R d, R f, R qnb, R qcb_out, R& dqb, R& qpb, R& qcb) {
+  const R qnt = qnb + rob * qcb_out;  // q_n feeds the filtered q_c
+  if (init) {  // dq' = (dq - qc d) f, qn = qc + Dt dq', qc' = (1 - r) qc + r qn
+    const R dqp = Dt * qnt;
+    dqb = f * dqp;
+    qcb = ((R)1 - rob) * qcb_out + qnt - d * f * dqp;
+    qpb = 0;
+  } else {  // dq' = (dq - qp d) f, qc'' = (1 - 2r) qc + r qp, qn = qp + 2 Dt dq', qc' = qc'' + r qn
+    const R dqp = (R)2 * Dt * qnt;
+    dqb = f * dqp;
+    qcb = ((R)1 - (R)2 * rob) * qcb_out;
+    qpb = rob * qcb_out + qnt - d * f * dqp;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_hs_implicit_adjoint(AdjArgs<T> a) {
+  using R = T;
+  const int lane = threadIdx.x & 31;
+  const int pid = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (pid >= a.npairs) return;  // whole warp
+  const int2 mn = a.pairs[pid];
+  const int m = mn.x, n = mn.y, nd = a.nd;
+  const bool act = lane < nd;
+  const size_t row = (size_t)m * (a.ns + 1) + n, s = row * nd + (act ? lane : 0);
+  auto ld = [&](const V2<T>* p, int comp) -> R { return act ? (R)(comp ? p[s].y : p[s].x) : (R)0; };
+  const R rob = (R)a.robert, Dt = (R)a.dt, d = (R)a.damping[row], f = (R)a.dfac[row], xi = (R)a.xi;
+  const R rpsr = (R)(1.0 / a.ps_ref), xipsr = (R)(a.xi / a.ps_ref), eig = (R)a.eig64[row];
+  for (int comp = 0; comp < 2; comp++) {  // real and imaginary parts are independent
+    R dvb, vpb, vcb, ddb2, dpb, dcb, dtb2, tpb, tcb;
+    lf_adj<R>(a.init_step, Dt, rob, d, f, ld(a.vn_b, comp), ld(a.vc_b, comp), dvb, vpb, vcb);
+    lf_adj<R>(a.init_step, Dt, rob, d, f, ld(a.dn_b, comp), ld(a.dc_b, comp), ddb2, dpb, dcb);
+    lf_adj<R>(a.init_step, Dt, rob, d, f, ld(a.tn_b, comp), ld(a.tc_b, comp), dtb2, tpb, tcb);
+    R dlb2 = 0, lpb = 0, lcb = 0;
+    {
+      const R lnb = comp ? (R)a.ln_b[row].y : (R)a.ln_b[row].x, lcbo = comp ? (R)a.lc_b[row].y : (R)a.lc_b[row].x;
+      lf_adj<R>(a.init_step, Dt, rob, (R)0, (R)1, lnb, lcbo, dlb2, lpb, lcb);
+    }
+    // dtt2 = dtt1 + xi dtmp_b, dl2 = dl1 + xi/ps_ref dps_b, (dps_b, dtmp_b) = LPT(ddiv2)
+    R dtt1b = dtb2, dl1b = dlb2;
+    const R dtmpb = xi * dtb2, dpsb = xipsr * dlb2;
+    R ddiv2b = ddb2 + matT<R>(a.Apt, dtmpb, lane, nd) + (act ? (R)a.spt[lane] * dpsb : (R)0);
+    // ddiv2 = W_n ddiv1 (n <= N)
+    R ddiv1b = ddiv2b;
+    if (n <= a.N) {
+      const double* W = a.W + (size_t)n * nd * nd;  // W[k][c] at c*nd + k: W^T[k][c] = W[c][k] at k*nd + c
+      R y = 0;
+      for (int c = 0; c < nd; c++) {
+        R xc = __shfl_sync(FULL, ddiv2b, c);
+        if (act) y += (R)W[(size_t)lane * nd + c] * xc;
+      }
+      ddiv1b = act ? y : (R)0;
+    }
+    // ddiv1 = ddiv - eig (A_geo t2 + hk l2)
+    const R gb = -eig * ddiv1b;
+    const R t2b = matT<R>(a.Ageo, gb, lane, nd);
+    R hdot = act ? (R)a.hk[lane] * ddiv1b : (R)0;
+    for (int o = 16; o > 0; o >>= 1) hdot += __shfl_xor_sync(FULL, hdot, o);
+    const R l2b = -eig * hdot;
+    // t2 = tp - tc + xi dtt1, l2 = lp - lc + xi dl1
+    tpb += t2b;
+    tcb -= t2b;
+    dtt1b += xi * t2b;
+    lpb += l2b;
+    lcb -= l2b;
+    dl1b += xi * l2b;
+    // dtt1 = dtt + dtmp_a, dl1 = dl + dps_a / ps_ref, (dps_a, dtmp_a) = LPT(div_p - div_c)
+    const R qb = matT<R>(a.Apt, dtt1b, lane, nd) + (act ? (R)a.spt[lane] * (rpsr * dl1b) : (R)0);
+    dpb += qb;
+    dcb -= qb;
+    auto st = [&](V2<T>* p, R v) {
+      if (act) {
+        if (comp) p[s].y = (T)v;
+        else p[s].x = (T)v;
+      }
+    };
+    st(a.dvor_b, dvb);
+    st(a.ddiv_b, ddiv1b);
+    st(a.dt_b, dtt1b);
+    st(a.vp_b, vpb);
+    st(a.vcin_b, vcb);
+    st(a.dp_b, dpb);
+    st(a.dcin_b, dcb);
+    st(a.tp_b, tpb);
+    st(a.tcin_b, tcb);
+    if (lane == 0) {
+      if (comp) {
+        a.dl_b[row].y = (T)dl1b;
+        a.lp_b[row].y = (T)lpb;
+        a.lcin_b[row].y = (T)lcb;
+      } else {
+        a.dl_b[row].x = (T)dl1b;
+        a.lp_b[row].x = (T)lpb;
+        a.lcin_b[row].x = (T)lcb;
+      }
+    }
+  }
+}
+
+// device buffers for the host-pointer entry points: 20 spectral fields (nd levels, lnps 1 level)
+struct SIBuffers {
+  void* f[20];
+  void* base;
+};
+int si_alloc(jgcm_model* md, SIBuffers* b) {
+  jgcm_mesh* m = md->mesh;
+  const size_t ts = tsize(m), S = spec_elems(m, md->nd) * 2 * ts, S1 = spec_elems(m, 1) * 2 * ts;
+  JG_TRY(alloc(&b->base, 20 * S));
+  for (int i = 0; i < 20; i++) b->f[i] = (char*)b->base + (size_t)i * S;
+  (void)S1;
+  return JGCM_OK;
+}
+// level count of field i in the input (12) / output (8) orders: lnps slots have one level
+int si_levels_in(const jgcm_model* md, int i) { return (i == 3 || i == 10 || i == 11) ? 1 : md->nd; }
+int si_levels_out(const jgcm_model* md, int i) { return (i == 6 || i == 7) ? 1 : md->nd; }
+
+template <typename T>
+ImplArgs<T> si_args(jgcm_model* md, void* const* in, void* const* out) {
+  using V = V2<T>;
+  jgcm_mesh* m = md->mesh;
+  ImplArgs<T> ia;
+  memset(&ia, 0, sizeof(ia));
+  ia.dvor = (const V*)in[0];
+  ia.ddiv = (const V*)in[1];
+  ia.dtend = (const V*)in[2];
+  ia.dlnps = (const V*)in[3];
+  ia.vor_p = (V*)in[4];
+  ia.vor_c = (V*)out[1];  // c level: read from the copy in the output slot, filtered in place
+  ia.vor_n = (V*)out[0];
+  ia.div_p = (V*)in[6];
+  ia.div_c = (V*)out[3];
+  ia.div_n = (V*)out[2];
+  ia.t_p = (V*)in[8];
+  ia.t_c = (V*)out[5];
+  ia.t_n = (V*)out[4];
+  ia.lnps_p = (V*)in[10];
+  ia.lnps_c = (V*)out[7];
+  ia.lnps_n = (V*)out[6];
+  ia.eig64 = m->t64.eig;
+  ia.damping = (const T*)md->damping;
+  ia.dfac = (const T*)md->dfac[md->init_step ? 0 : 1];
+  ia.W = md->d_W + (md->init_step ? 0 : (size_t)(m->N + 1) * md->nd * md->nd);
+  ia.pairs = md->d_pairs;
+  ia.npairs = md->npairs;
+  ia.nd = md->nd;
+  ia.L = md->nd;
+  ia.ne = 1;
+  ia.ns = m->ns;
+  ia.N = m->N;
+  ia.init_step = md->init_step;
+  ia.dt = md->P.dt;
+  ia.xi = md->init_step ? md->P.dt * md->P.implicit_coef : (2 * md->P.dt) * md->P.implicit_coef;
+  ia.ps_ref = md->P.ps_ref;
+  ia.kappa = md->P.kappa;
+  ia.rdgas = md->P.rdgas;
+  ia.robert = md->P.robert_coef;
+  return ia;
+}
+}  // namespace
+
+extern "C" int jgcm_model_semi_implicit_step(jgcm_model* md, const double* const* in, double* const* out) {
+  JG_ARG(md && in && out, "NULL argument");
+  JG_ARG(md->P.kind == JGCM_HELD_SUAREZ, "the semi-implicit step exists for Held-Suarez only");
+  JG_ARG(md->ne == 1, "one-member models only");
+  for (int i = 0; i < 12; i++) JG_ARG(in[i], "input %d is NULL", i);
+  for (int i = 0; i < 8; i++) JG_ARG(out[i], "output %d is NULL", i);
+  jgcm_mesh* m = md->mesh;
+  cudaStream_t st = m->stream;
+  SIBuffers b;
+  JG_TRY(si_alloc(md, &b));
+  struct Free {
+    void* p;
+    ~Free() { cudaFree(p); }
+  } fr{b.base};
+  void* din[12];
+  void* dout[8];
+  for (int i = 0; i < 12; i++) din[i] = b.f[i];
+  for (int i = 0; i < 8; i++) dout[i] = b.f[12 + i];
+  for (int i = 0; i < 12; i++) {
+    const size_t nn = 2 * spec_elems(m, si_levels_in(md, i));
+    JG_CUDA(cudaMemcpyAsync(m->d_stage, in[i], nn * 8, cudaMemcpyHostToDevice, st));
+    JG_TRY(spec_host_to_dev(m, m->d_stage, din[i], si_levels_in(md, i), st));
+  }
+  const size_t ts = tsize(m);
+  JG_CUDA(cudaMemcpyAsync(dout[1], din[5], spec_elems(m, md->nd) * 2 * ts, cudaMemcpyDeviceToDevice, st));
+  JG_CUDA(cudaMemcpyAsync(dout[3], din[7], spec_elems(m, md->nd) * 2 * ts, cudaMemcpyDeviceToDevice, st));
+  JG_CUDA(cudaMemcpyAsync(dout[5], din[9], spec_elems(m, md->nd) * 2 * ts, cudaMemcpyDeviceToDevice, st));
+  JG_CUDA(cudaMemcpyAsync(dout[7], din[11], spec_elems(m, 1) * 2 * ts, cudaMemcpyDeviceToDevice, st));
+  if (is_fp64(m))
+    k_hs_implicit<double, double><<<(md->npairs + 7) / 8, 256, 0, st>>>(si_args<double>(md, din, dout), md->d_vc);
+  else
+    k_hs_implicit<float, float><<<(md->npairs + 7) / 8, 256, 0, st>>>(si_args<float>(md, din, dout), md->d_vc);
+  JG_CUDA(cudaGetLastError());
+  for (int i = 0; i < 8; i++) {
+    const size_t nn = 2 * spec_elems(m, si_levels_out(md, i));
+    JG_TRY(spec_dev_to_host(m, dout[i], m->d_stage, si_levels_out(md, i), st));
+    JG_CUDA(cudaMemcpyAsync(out[i], m->d_stage, nn * 8, cudaMemcpyDeviceToHost, st));
+    JG_CUDA(cudaStreamSynchronize(st));
+  }
+  return JGCM_OK;
+}
+
+extern "C" int jgcm_model_semi_implicit_step_adjoint(jgcm_model* md, const double* const* out_bar,
+                                                     double* const* in_bar) {
+  JG_ARG(md && out_bar && in_bar, "NULL argument");
+  JG_ARG(md->P.kind == JGCM_HELD_SUAREZ, "the semi-implicit step exists for Held-Suarez only");
+  JG_ARG(md->ne == 1, "one-member models only");
+  for (int i = 0; i < 8; i++) JG_ARG(out_bar[i], "output cotangent %d is NULL", i);
+  for (int i = 0; i < 12; i++) JG_ARG(in_bar[i], "input cotangent %d is NULL", i);
+  jgcm_mesh* m = md->mesh;
+  cudaStream_t st = m->stream;
+  SIBuffers b;
+  JG_TRY(si_alloc(md, &b));
+  AdjMats am;
+  JG_TRY(adj_mats(md, &am));
+  struct Free {
+    void *p, *q;
+    ~Free() {
+      cudaFree(p);
+      cudaFree(q);
+    }
+  } fr{b.base, am.Apt};
+  void* dob[8];
+  void* dib[12];
+  for (int i = 0; i < 8; i++) dob[i] = b.f[i];
+  for (int i = 0; i < 12; i++) dib[i] = b.f[8 + i];
+  for (int i = 0; i < 8; i++) {
+    const size_t nn = 2 * spec_elems(m, si_levels_out(md, i));
+    JG_CUDA(cudaMemcpyAsync(m->d_stage, out_bar[i], nn * 8, cudaMemcpyHostToDevice, st));
+    JG_TRY(spec_host_to_dev(m, m->d_stage, dob[i], si_levels_out(md, i), st));
+  }
+  auto launch = [&](auto tag) {
+    using T = decltype(tag);
+    using V = V2<T>;
+    AdjArgs<T> a;
+    memset(&a, 0, sizeof(a));
+    a.vn_b = (const V*)dob[0]; a.vc_b = (const V*)dob[1]; a.dn_b = (const V*)dob[2]; a.dc_b = (const V*)dob[3];
+    a.tn_b = (const V*)dob[4]; a.tc_b = (const V*)dob[5]; a.ln_b = (const V*)dob[6]; a.lc_b = (const V*)dob[7];
+    a.dvor_b = (V*)dib[0]; a.ddiv_b = (V*)dib[1]; a.dt_b = (V*)dib[2]; a.dl_b = (V*)dib[3];
+    a.vp_b = (V*)dib[4]; a.vcin_b = (V*)dib[5]; a.dp_b = (V*)dib[6]; a.dcin_b = (V*)dib[7];
+    a.tp_b = (V*)dib[8]; a.tcin_b = (V*)dib[9]; a.lp_b = (V*)dib[10]; a.lcin_b = (V*)dib[11];
+    a.damping = (const T*)md->damping;
+    a.dfac = (const T*)md->dfac[md->init_step ? 0 : 1];
+    a.eig64 = m->t64.eig;
+    a.W = md->d_W + (md->init_step ? 0 : (size_t)(m->N + 1) * md->nd * md->nd);
+    a.Apt = am.Apt; a.spt = am.spt; a.Ageo = am.Ageo; a.hk = am.hk;
+    a.pairs = md->d_pairs;
+    a.npairs = md->npairs;
+    a.nd = md->nd;
+    a.ns = m->ns;
+    a.N = m->N;
+    a.init_step = md->init_step;
+    a.dt = md->P.dt;
+    a.xi = md->init_step ? md->P.dt * md->P.implicit_coef : (2 * md->P.dt) * md->P.implicit_coef;
+    a.ps_ref = md->P.ps_ref;
+    a.robert = md->P.robert_coef;
+    k_hs_implicit_adjoint<T><<<(md->npairs + 7) / 8, 256, 0, st>>>(a);
+  };
+  if (is_fp64(m)) launch(double());
+  else launch(float());
+  JG_CUDA(cudaGetLastError());
+  for (int i = 0; i < 12; i++) {
+    const size_t nn = 2 * spec_elems(m, si_levels_in(md, i));
+    JG_TRY(spec_dev_to_host(m, dib[i], m->d_stage, si_levels_in(md, i), st));
+    JG_CUDA(cudaMemcpyAsync(in_bar[i], m->d_stage, nn * 8, cudaMemcpyDeviceToHost, st));
+    JG_CUDA(cudaStreamSynchronize(st));
+  }
+  return JGCM_OK;
+}

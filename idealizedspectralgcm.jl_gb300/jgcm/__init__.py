@@ -84,6 +84,8 @@ def lib():
         "jgcm_model_create_members": (I, [P, P, I, PP]),
         "jgcm_model_members": (I, [P, C.POINTER(I)]),
         "jgcm_model_copy_member": (I, [P, I, P, I]),
+        "jgcm_model_semi_implicit_step": (I, [P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+        "jgcm_model_semi_implicit_step_adjoint": (I, [P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
         "jgcm_model_get_tuning": (I, [P, C.POINTER(I), I]),
         "jgcm_model_set_tuning": (I, [P, C.POINTER(I), I]),
         "jgcm_model_autotune": (I, [P, I, C.POINTER(I), C.POINTER(C.c_float)]),
@@ -510,4 +512,35 @@ def autotune(model, nsteps=24, cache=None):
         with open(cache, "w") as f:
             json.dump(table, f, indent=1, sort_keys=True)
     return entry
+
+
+SI_IN = ("dvor", "ddiv", "dt", "dlnps", "vor_p", "vor_c", "div_p", "div_c", "t_p", "t_c", "lnps_p", "lnps_c")
+SI_OUT = ("vor_n", "vor_c", "div_n", "div_c", "t_n", "t_c", "lnps_n", "lnps_c")
+
+
+def _si_arrays(model, names, source=None):
+    nd = model.mesh.nd
+    if source is None:
+        return [model.mesh.spectral(1 if k.startswith("lnps") or k == "dlnps" else nd) for k in names]
+    return [np.asfortranarray(source[k], dtype=np.complex128) for k in names]
+
+
+def Semi_Implicit_Step(model, inputs):
+    """One semi-implicit step on its own (Implicit_Correction! + Compute_Spectral_Damping! +
+    Filtered_Leapfrog! for the model's current step): dict of the SI_IN spectral arrays -> dict of
+    the SI_OUT arrays."""
+    ins, outs = _si_arrays(model, SI_IN, inputs), _si_arrays(model, SI_OUT)
+    pin = (C.c_void_p * 12)(*[a.ctypes.data for a in ins])
+    pout = (C.c_void_p * 8)(*[a.ctypes.data for a in outs])
+    _check(lib().jgcm_model_semi_implicit_step(model._h, pin, pout))
+    return dict(zip(SI_OUT, outs))
+
+
+def Semi_Implicit_Step_Adjoint(model, out_bar):
+    """Adjoint of Semi_Implicit_Step: cotangents of the SI_OUT arrays -> cotangents of SI_IN."""
+    obs, ibs = _si_arrays(model, SI_OUT, out_bar), _si_arrays(model, SI_IN)
+    pob = (C.c_void_p * 8)(*[a.ctypes.data for a in obs])
+    pib = (C.c_void_p * 12)(*[a.ctypes.data for a in ibs])
+    _check(lib().jgcm_model_semi_implicit_step_adjoint(model._h, pob, pib))
+    return dict(zip(SI_IN, ibs))
 

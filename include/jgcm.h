@@ -153,6 +153,14 @@ int jgcm_model_members(jgcm_model* model, int* members);
  * time level of the prognostic state and the grid diagnostics.  A one-member dst also takes the
  * source's time-step state (init step); an ensemble dst must already share it. */
 int jgcm_model_copy_member(jgcm_model* dst, int dst_member, jgcm_model* src, int src_member);
+/* One semi-implicit step on its own and its adjoint (Held-Suarez; no counterpart in the reference):
+ * Adjust_δlnps_δt_δdiv! + Implicit_Correction! (Semi_Implicit.jl:360-513) + Compute_Spectral_Damping!
+ * + Filtered_Leapfrog! (Time_Integrator.jl:58-101) for the model's current step (init step or not),
+ * a linear map.  in[12]: δvor, δdiv, δT, δlnps, vor_p, vor_c, div_p, div_c, T_p, T_c, lnps_p,
+ * lnps_c; out[8]: vor_n, vor_c (filtered), div_n, div_c, T_n, T_c, lnps_n, lnps_c.  Spectral host
+ * arrays [N+1, N+2, nd] (lnps: 1 level).  The adjoint maps cotangents of out to cotangents of in. */
+int jgcm_model_semi_implicit_step(jgcm_model* model, const double* const* in, double* const* out);
+int jgcm_model_semi_implicit_step_adjoint(jgcm_model* model, const double* const* out_bar, double* const* in_bar);
 /* Tiles (no counterpart in the reference).  knobs[0]: lanes per column of the Held-Suarez column
  * kernel (1, 2, 4; this model); knobs[1..3]: S2G, G2S and FFT columns per block of the SIMT
  * transform kernels (the mesh: shared by its models).  0 = default.  The autotuner times candidate

@@ -87,6 +87,7 @@ typedef struct {
 } om_params;
 
 om_model* om_model_create(om_mesh* mesh, const om_params* p);
+void om_semi_implicit_step(om_model* md, const double* const* in, double* const* out);
 void om_hs_forcing(om_model* md, int Dt, const double* u, const double* v, const double* p_half,
                    const double* p_full, const double* t, double* du, double* dv, double* t_eq, double* dtt);
 void om_model_destroy(om_model* md);

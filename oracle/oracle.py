@@ -75,6 +75,7 @@ def lib():
             "om_spectral_initialize_fields": (I, [P, P, I]),
             "om_model_semi_implicit": (L, [P, C.c_char_p, P, L]),
             "om_hs_forcing": (None, [P, I, P, P, P, P, P, P, P, P, P]),
+            "om_semi_implicit_step": (None, [P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
             "om_trans_spherical_to_grid_adjoint": (None, [P, P, I, P]),
             "om_trans_grid_to_spherical_adjoint": (None, [P, P, I, P]),
         }
@@ -319,4 +320,20 @@ def Trans_Grid_To_Spherical_Adjoint(mesh, spec_bar, grid_bar):
     """Adjoint of Trans_Grid_To_Spherical!: grid_bar = G2S^T spec_bar."""
     nlev = _nlev_spec(mesh, spec_bar)
     lib().om_trans_grid_to_spherical_adjoint(mesh._h, _ptr(np.asfortranarray(spec_bar)), nlev, _ptr(grid_bar))
+
+
+SI_IN = ("dvor", "ddiv", "dt", "dlnps", "vor_p", "vor_c", "div_p", "div_c", "t_p", "t_c", "lnps_p", "lnps_c")
+SI_OUT = ("vor_n", "vor_c", "div_n", "div_c", "t_n", "t_c", "lnps_n", "lnps_c")
+
+
+def Semi_Implicit_Step(model, inputs):
+    """One semi-implicit step (implicit correction + damping + filtered leapfrog): dict of the 12
+    SI_IN spectral arrays -> dict of the 8 SI_OUT arrays."""
+    ins = [np.asfortranarray(inputs[k], dtype=np.complex128) for k in SI_IN]
+    nd = model.mesh.nd
+    outs = [model.mesh.spectral(1 if k.startswith("lnps") else nd) for k in SI_OUT]
+    pin = (C.c_void_p * 12)(*[a.ctypes.data for a in ins])
+    pout = (C.c_void_p * 8)(*[a.ctypes.data for a in outs])
+    lib().om_semi_implicit_step(model._h, pin, pout)
+    return dict(zip(SI_OUT, outs))
 

@@ -94,3 +94,66 @@ def test_gpu_adjoints(jg, orc, case, prec, tol):
         orc.Trans_Grid_To_Spherical_Adjoint(om, s, b)
         assert configs.rel_l2(a, b) < tol
     _check_dot(jg, gm, nd, 1e-12 if prec == "fp64" else 1e-5)
+
+
+# ---- one semi-implicit step (implicit correction + damping + filtered leapfrog) ------------------
+_SCALE = {"dvor": 1e-10, "ddiv": 1e-10, "dt": 1e-5, "dlnps": 1e-9, "vor_p": 1e-5, "vor_c": 1e-5, "div_p": 1e-6,
+          "div_c": 1e-6, "t_p": 1.0, "t_c": 1.0, "lnps_p": 1e-3, "lnps_c": 1e-3}
+
+
+def _si_inputs(mesh, names, seed, scale=None):
+    rng = np.random.default_rng(seed)
+    out = {}
+    for i, k in enumerate(names):
+        nlev = 1 if k.startswith("lnps") or k == "dlnps" else mesh.nd
+        a = _spec(mesh, nlev, seed * 100 + i)
+        out[k] = np.asfortranarray(a * (scale[k] if scale else 1.0))
+    del rng
+    return out
+
+
+def _si_dot(a, b):
+    return sum(_sdot(a[k], b[k]) for k in a)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("init", [True, False])
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp32", 2e-5)])
+def test_gpu_semi_implicit_step_matches_oracle(jg, orc, init, prec, tol):
+    name = "hs_t21l10"
+    gm, om = configs.make_mesh(jg, name, precision=prec), configs.make_mesh(orc, name)
+    gmod, omod = jg.Model(gm, configs.PARAMS[name]), orc.Model(om, configs.PARAMS[name])
+    if not init:
+        gmod.update_init_step()
+        omod.update_init_step()
+    x = _si_inputs(om, jg.SI_IN, 3, _SCALE)
+    a, b = jg.Semi_Implicit_Step(gmod, x), orc.Semi_Implicit_Step(omod, x)
+    for k in jg.SI_OUT:
+        assert configs.rel_l2(a[k], b[k]) < tol, (k, configs.rel_l2(a[k], b[k]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("init", [True, False])
+def test_gpu_semi_implicit_step_adjoint(jg, init):
+    """<J x, y> = <x, J^T y> for the step's linear map J (FP64), and J^T y reproduces a central
+    finite difference of x -> <J x, y> in a few directions."""
+    name = "hs_t21l10"
+    gm = configs.make_mesh(jg, name, precision="fp64")
+    md = jg.Model(gm, configs.PARAMS[name])
+    if not init:
+        md.update_init_step()
+    x = _si_inputs(gm, jg.SI_IN, 5, _SCALE)
+    y = _si_inputs(gm, jg.SI_OUT, 6)
+    Jx = jg.Semi_Implicit_Step(md, x)
+    JTy = jg.Semi_Implicit_Step_Adjoint(md, y)
+    lhs, rhs = _si_dot(Jx, y), _si_dot(x, JTy)
+    assert abs(lhs - rhs) <= 1e-11 * (abs(lhs) + abs(rhs)), (lhs, rhs)
+    for k, (mm, n, lev) in [("ddiv", (1, 3, 2)), ("t_p", (0, 2, 5)), ("lnps_c", (2, 4, 0)), ("div_p", (4, 9, 7))]:
+        d = {kk: np.zeros_like(v) for kk, v in x.items()}
+        eps = 1e-3 * max(_SCALE[k], 1e-12)
+        d[k][mm, n, lev] = eps
+        plus = jg.Semi_Implicit_Step(md, {kk: x[kk] + d[kk] for kk in x})
+        minus = jg.Semi_Implicit_Step(md, {kk: x[kk] - d[kk] for kk in x})
+        fd = (_si_dot(plus, y) - _si_dot(minus, y)) / (2 * eps)
+        ad = JTy[k][mm, n, lev].real
+        assert abs(fd - ad) <= 1e-6 * max(abs(ad), 1e-30) + 1e-12 * abs(lhs) / eps, (k, fd, ad)
