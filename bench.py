@@ -454,6 +454,9 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "tf32x3", "bf16x3"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble and tensor-core side runs")
+    ap.add_argument("--ensemble-only", default=None, metavar="PRECISIONS",
+                    help="run only the batched-ensemble measurement for these precisions (comma list, e.g. "
+                         "fp32,tf32x3) over --steps days and print its JSON (for profiling the ensemble kernels)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, _ = dist_env()
@@ -464,6 +467,14 @@ def main():
     try:
         if args.impl == "reference":
             return run_reference(args)
+        if args.ensemble_only:
+            import jgcm
+            from jgcm import configs
+
+            jgcm.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+            res = ensemble_bench(jgcm, configs, args.ensemble_only.split(","), days=max(1, args.steps))
+            print(json.dumps({"ensemble": res}), flush=True)
+            return 0
         return run_jgcm(args)
     finally:
         if world > 1:
