@@ -118,6 +118,73 @@ __global__ void __launch_bounds__(256) k_s2g_legendre(S2GPlan plan, Tables<T> tb
   }
 }
 
+// ------------------------------------------------------------------------------------------
+// Per-element epilogue of the inverse FFT (value x at longitude t of latitude j, column k of
+// group g) and prologue of the forward FFT (the grid value to transform).
+template <typename T>
+__device__ __forceinline__ void ifft_store(const GridOutGroup& g, const Tables<T>& tb, int k, int j, int t, int nlat,
+                                           int nlon, T x) {
+  size_t idx = ((size_t)k * nlat + j) * nlon + t;
+  T* dst = (T*)g.dst;
+  switch (g.epi) {
+    case EPI_NONE:
+      dst[idx] = x;
+      break;
+    case EPI_DIVCOS:
+      dst[idx] = x / tb.cosj[j];
+      break;
+    case EPI_EXP2:
+      dst[idx] = x + (T)g.shift;
+      ((T*)g.dst2)[idx] = exp(x) * (T)exp(g.shift);
+      break;
+    case EPI_DIVCOS_MULPS:
+      dst[idx] = (x / tb.cosj[j]) * ((const T*)g.ps)[((size_t)k * nlat + j) * nlon + t];  // level k of ps
+      break;
+    case EPI_ADJ_G2S:
+      dst[idx] = x * (T)(tb.wts[j] / (2.0 * nlon));
+      break;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T fft_load(const FFTPlan& plan, const GridInGroup& g, int k, int j, int t, int nlat,
+                                      int nlon, T cj) {
+  T x = 0;
+  size_t idx = ((size_t)k * nlat + j) * nlon + t;
+  const T* s0 = (const T*)g.src;
+  switch (g.pro) {
+    case PRO_NONE:
+      x = s0[idx];
+      break;
+    case PRO_MULCOS:
+      x = s0[idx] * cj;
+      break;
+    case PRO_FLUXU: {  // (-kappa_m u + (vor + f) v) cos   (Shallow_Water_Dynamics.jl:129, Barotropic :28)
+      T u = s0[idx], v = ((const T*)g.s1)[idx], vor = ((const T*)g.s2)[idx];
+      T absvor = vor + ((const T*)plan.coriolis)[j];
+      x = ((-(T)plan.kappa_m) * u + absvor * v) * cj;
+    } break;
+    case PRO_FLUXV: {  // (-kappa_m v + (-(vor + f)) u) cos
+      T u = s0[idx], v = ((const T*)g.s1)[idx], vor = ((const T*)g.s2)[idx];
+      T absvor = vor + ((const T*)plan.coriolis)[j];
+      x = ((-(T)plan.kappa_m) * v + (-absvor) * u) * cj;
+    } break;
+    case PRO_KIN: {  // 0.5 (u^2 + v^2)
+      T u = s0[idx], v = ((const T*)g.s1)[idx];
+      x = (T)0.5 * (u * u + v * v);
+    } break;
+    case PRO_SWH: {  // -kappa_t (h - h_eq) - (u dlam_h + v dth_h) - h div
+      T h = s0[idx], u = ((const T*)g.s1)[idx], v = ((const T*)g.s2)[idx];
+      T dl = ((const T*)g.s3)[idx], dt = ((const T*)g.s4)[idx], dv = ((const T*)g.s5)[idx];
+      T heq = ((const T*)g.s6)[idx];
+      T d = (-(T)plan.kappa_t) * (h - heq);
+      d = d - (u * dl + v * dt);
+      x = d - h * dv;
+    } break;
+  }
+  return x;
+}
+
 // Fourier -> grid: inverse real FFT, one column per half-length (h = nlon/2) complex transform,
 // so rounding never leaks between columns of different magnitude.  grid (ceil(C/CT), nlat),
 // 256 threads.  Row x(λ_t) = Re g_0 + 2 Re sum_{m=1}^{N} g_m e^{imλ_t}, i.e. 2 nλ Re(ifft(g)) with
@@ -170,26 +237,7 @@ __global__ void __launch_bounds__(256) k_ifft(IFFTPlan plan, Tables<T> tb, const
     T x = (t & 1) ? im[cc * h + (t >> 1)] : re[cc * h + (t >> 1)];
     int k;
     const GridOutGroup& g = group_of(plan.g, plan.ng, c, &k);
-    size_t idx = ((size_t)k * nlat + j) * nlon + t;
-    T* dst = (T*)g.dst;
-    switch (g.epi) {
-      case EPI_NONE:
-        dst[idx] = x;
-        break;
-      case EPI_DIVCOS:
-        dst[idx] = x / tb.cosj[j];
-        break;
-      case EPI_EXP2:
-        dst[idx] = x + (T)g.shift;
-        ((T*)g.dst2)[idx] = exp(x) * (T)exp(g.shift);
-        break;
-      case EPI_DIVCOS_MULPS:
-        dst[idx] = (x / tb.cosj[j]) * ((const T*)g.ps)[((size_t)k * nlat + j) * nlon + t];  // level k of ps
-        break;
-      case EPI_ADJ_G2S:
-        dst[idx] = x * (T)(tb.wts[j] / (2.0 * nlon));
-        break;
-    }
+    ifft_store<T>(g, tb, k, j, t, nlat, nlon, x);
   }
 }
 
@@ -217,38 +265,7 @@ __global__ void __launch_bounds__(256) k_fft(FFTPlan plan, Tables<T> tb, V2<T>* 
     if (c < C) {
       int k;
       const GridInGroup& g = group_of(plan.g, plan.ng, c, &k);
-      size_t idx = ((size_t)k * nlat + j) * nlon + t;
-      const T* s0 = (const T*)g.src;
-      switch (g.pro) {
-        case PRO_NONE:
-          x = s0[idx];
-          break;
-        case PRO_MULCOS:
-          x = s0[idx] * cj;
-          break;
-        case PRO_FLUXU: {  // (-kappa_m u + (vor + f) v) cos   (Shallow_Water_Dynamics.jl:129, Barotropic :28)
-          T u = s0[idx], v = ((const T*)g.s1)[idx], vor = ((const T*)g.s2)[idx];
-          T absvor = vor + ((const T*)plan.coriolis)[j];
-          x = ((-(T)plan.kappa_m) * u + absvor * v) * cj;
-        } break;
-        case PRO_FLUXV: {  // (-kappa_m v + (-(vor + f)) u) cos
-          T u = s0[idx], v = ((const T*)g.s1)[idx], vor = ((const T*)g.s2)[idx];
-          T absvor = vor + ((const T*)plan.coriolis)[j];
-          x = ((-(T)plan.kappa_m) * v + (-absvor) * u) * cj;
-        } break;
-        case PRO_KIN: {  // 0.5 (u^2 + v^2)
-          T u = s0[idx], v = ((const T*)g.s1)[idx];
-          x = (T)0.5 * (u * u + v * v);
-        } break;
-        case PRO_SWH: {  // -kappa_t (h - h_eq) - (u dlam_h + v dth_h) - h div
-          T h = s0[idx], u = ((const T*)g.s1)[idx], v = ((const T*)g.s2)[idx];
-          T dl = ((const T*)g.s3)[idx], dt = ((const T*)g.s4)[idx], dv = ((const T*)g.s5)[idx];
-          T heq = ((const T*)g.s6)[idx];
-          T d = (-(T)plan.kappa_t) * (h - heq);
-          d = d - (u * dl + v * dt);
-          x = d - h * dv;
-        } break;
-      }
+      x = fft_load<T>(plan, g, k, j, t, nlat, nlon, cj);
     }
     int pos = brev(t >> 1, logh);
     if (t & 1)
@@ -271,6 +288,200 @@ __global__ void __launch_bounds__(256) k_fft(FFTPlan plan, Tables<T> tb, V2<T>* 
     o.x = (er + (tc * orr + ts * oi)) * scale;
     o.y = (ei + (tc * oi - ts * orr)) * scale;
     F[((size_t)mm * nlat + j) * C + c] = o;
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Warp-register FFTs (nlon = 64 V, V = 1..16): one warp per (column, latitude) row, the H = 32 V
+// complex points held V per lane (point i = lane + 32 r), radix-2 stages of half-size s >= 32
+// within a lane and s < 32 across lanes by shuffles: no block barrier inside the transform.  A
+// block stages the Fourier coefficients of its 8 columns once (coalesced) and its 8 warps transform
+// one column each.  Same arithmetic as k_ifft / k_fft (half-length complex transform of a real row).
+constexpr int FW_COLS = 8;  // columns (warps) per block
+
+// twiddle e^{SIGN 2πi t / nlon}, t < nlon/2, from the cos/sin table
+template <typename T, int SIGN>
+__device__ __forceinline__ void twiddle(const T* tw, int t, T& c, T& s) {
+  c = __ldg(tw + 2 * t);
+  s = (T)SIGN * __ldg(tw + 2 * t + 1);
+}
+
+// inverse: DIT on bit-reversed input -> natural order, twiddles e^{+2πi j/(2s)} = tw[j H / s]
+template <typename T, int V>
+__device__ __forceinline__ void warp_fft_dit(T (&re)[V], T (&im)[V], const T* tw, int lane) {
+  constexpr int H = 32 * V;
+#pragma unroll
+  for (int s = 1; s < 32; s <<= 1) {
+    const bool upper = (lane & s) != 0;
+    const int jj = lane & (s - 1);
+    T c, sn;
+    twiddle<T, 1>(tw, jj * (H / s), c, sn);
+#pragma unroll
+    for (int r = 0; r < V; r++) {
+      const T pr = __shfl_xor_sync(0xffffffffu, re[r], s), pi = __shfl_xor_sync(0xffffffffu, im[r], s);
+      // lower: a + w b (b = partner); upper: a' - w b' with a' = partner, b' = own
+      const T br = upper ? re[r] : pr, bi = upper ? im[r] : pi;
+      const T ar = upper ? pr : re[r], ai = upper ? pi : im[r];
+      const T tr = br * c - bi * sn, ti = br * sn + bi * c;
+      re[r] = upper ? ar - tr : ar + tr;
+      im[r] = upper ? ai - ti : ai + ti;
+    }
+  }
+#pragma unroll
+  for (int s = 32; s < H; s <<= 1) {
+    constexpr int dummy = 0;
+    (void)dummy;
+    const int sr = s / 32;
+#pragma unroll
+    for (int r = 0; r < V; r++) {
+      if ((r & sr) == 0) {
+        const int jj = (lane + 32 * r) & (s - 1);
+        T c, sn;
+        twiddle<T, 1>(tw, jj * (H / s), c, sn);
+        const T br = re[r + sr], bi = im[r + sr];
+        const T tr = br * c - bi * sn, ti = br * sn + bi * c;
+        re[r + sr] = re[r] - tr;
+        im[r + sr] = im[r] - ti;
+        re[r] = re[r] + tr;
+        im[r] = im[r] + ti;
+      }
+    }
+  }
+}
+
+// forward: DIF on natural input -> bit-reversed order, twiddles e^{-2πi j/(2s)}
+template <typename T, int V>
+__device__ __forceinline__ void warp_fft_dif(T (&re)[V], T (&im)[V], const T* tw, int lane) {
+  constexpr int H = 32 * V;
+#pragma unroll
+  for (int s = H / 2; s >= 32; s >>= 1) {
+    const int sr = s / 32;
+#pragma unroll
+    for (int r = 0; r < V; r++) {
+      if ((r & sr) == 0) {
+        const int jj = (lane + 32 * r) & (s - 1);
+        T c, sn;
+        twiddle<T, -1>(tw, jj * (H / s), c, sn);
+        const T ar = re[r], ai = im[r], br = re[r + sr], bi = im[r + sr];
+        re[r] = ar + br;
+        im[r] = ai + bi;
+        const T dr = ar - br, di = ai - bi;
+        re[r + sr] = dr * c - di * sn;
+        im[r + sr] = dr * sn + di * c;
+      }
+    }
+  }
+#pragma unroll
+  for (int s = 16; s >= 1; s >>= 1) {
+    const bool upper = (lane & s) != 0;
+    const int jj = lane & (s - 1);
+    T c, sn;
+    twiddle<T, -1>(tw, jj * (H / s), c, sn);
+#pragma unroll
+    for (int r = 0; r < V; r++) {
+      const T pr = __shfl_xor_sync(0xffffffffu, re[r], s), pi = __shfl_xor_sync(0xffffffffu, im[r], s);
+      // lower: a + b; upper: (a - b) w with a = partner, b = own
+      const T dr = pr - re[r], di = pi - im[r];
+      re[r] = upper ? dr * c - di * sn : re[r] + pr;
+      im[r] = upper ? dr * sn + di * c : im[r] + pi;
+    }
+  }
+}
+
+template <typename T, int V>
+__global__ void __launch_bounds__(256) k_ifft_w(IFFTPlan plan, Tables<T> tb, const V2<T>* __restrict__ F, int N,
+                                                int nlat, int nlon) {
+  using Vc = V2<T>;
+  constexpr int H = 32 * V, LOGH = (V == 1 ? 5 : V == 2 ? 6 : V == 4 ? 7 : V == 8 ? 8 : 9);
+  extern __shared__ __align__(16) unsigned char smem[];
+  Vc* G = (Vc*)smem;  // [N+1][FW_COLS]
+  const int j = blockIdx.y, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int C = plan.C, cbase = blockIdx.x * FW_COLS, c = cbase + w;
+  for (int i = threadIdx.x; i < (N + 1) * FW_COLS; i += blockDim.x) {
+    const int mm = i / FW_COLS, cc = i - mm * FW_COLS;
+    Vc g;
+    g.x = g.y = 0;
+    if (cbase + cc < C) g = F[((size_t)mm * nlat + j) * C + cbase + cc];
+    if (mm == 0) g.y = 0;  // only Re g_0 reaches the grid
+    G[i] = g;
+  }
+  __syncthreads();
+  if (c >= C) return;  // whole warp
+  T re[V], im[V];
+#pragma unroll
+  for (int r = 0; r < V; r++) {  // Z at bit-reversed position: element i holds Z[brev(i)]
+    const int mm = brev(lane + 32 * r, LOGH), q = H - mm;
+    Vc x, y;
+    x.x = x.y = y.x = y.y = 0;
+    if (mm <= N) x = G[mm * FW_COLS + w];
+    if (mm >= 1 && q <= N) y = G[q * FW_COLS + w];
+    const T er = x.x + y.x, ei = x.y - y.y;  // X[m] + conj X[h-m]
+    const T dr = x.x - y.x, di = x.y + y.y;  // X[m] - conj X[h-m]
+    T cs, sn;
+    twiddle<T, 1>(tb.tw, mm, cs, sn);
+    const T orr = dr * cs - di * sn, oi = dr * sn + di * cs;
+    re[r] = er - oi;
+    im[r] = ei + orr;
+  }
+  warp_fft_dit<T, V>(re, im, tb.tw, lane);
+  int k;
+  const GridOutGroup& g = group_of(plan.g, plan.ng, c, &k);
+#pragma unroll
+  for (int r = 0; r < V; r++) {  // z[i] = x[2i] + i x[2i+1]
+    const int i = lane + 32 * r;
+    ifft_store<T>(g, tb, k, j, 2 * i, nlat, nlon, re[r]);
+    ifft_store<T>(g, tb, k, j, 2 * i + 1, nlat, nlon, im[r]);
+  }
+}
+
+template <typename T, int V>
+__global__ void __launch_bounds__(256) k_fft_w(FFTPlan plan, Tables<T> tb, V2<T>* __restrict__ F, int N, int nlat,
+                                               int nlon) {
+  using Vc = V2<T>;
+  constexpr int H = 32 * V, LOGH = (V == 1 ? 5 : V == 2 ? 6 : V == 4 ? 7 : V == 8 ? 8 : 9);
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int j = blockIdx.y, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Vc* Z = (Vc*)smem + (size_t)w * H;  // this warp's spectrum, natural order
+  Vc* X = (Vc*)smem + (size_t)FW_COLS * H;  // [N+1][FW_COLS] results of the block
+  const int C = plan.C, cbase = blockIdx.x * FW_COLS, c = cbase + w;
+  if (c < C) {
+    int k;
+    const GridInGroup& g = group_of(plan.g, plan.ng, c, &k);
+    const T cj = tb.cosj[j];
+    T re[V], im[V];
+#pragma unroll
+    for (int r = 0; r < V; r++) {  // z[i] = x[2i] + i x[2i+1], natural order
+      const int i = lane + 32 * r;
+      re[r] = fft_load<T>(plan, g, k, j, 2 * i, nlat, nlon, cj);
+      im[r] = fft_load<T>(plan, g, k, j, 2 * i + 1, nlat, nlon, cj);
+    }
+    warp_fft_dif<T, V>(re, im, tb.tw, lane);
+#pragma unroll
+    for (int r = 0; r < V; r++) {
+      Vc z;
+      z.x = re[r];
+      z.y = im[r];
+      Z[brev(lane + 32 * r, LOGH)] = z;
+    }
+    __syncwarp();
+    const T scale = (T)(0.5 / nlon);
+    for (int mm = lane; mm <= N; mm += 32) {
+      const int q = (H - mm) & (H - 1);
+      const Vc zm = Z[mm], zq = Z[q];
+      const T er = zm.x + zq.x, ei = zm.y - zq.y;  // 2 E
+      const T orr = zm.y + zq.y, oi = zq.x - zm.x;  // 2 O
+      T tc, ts;
+      twiddle<T, 1>(tb.tw, mm, tc, ts);  // e^{-2πim/nλ} = tc - i ts
+      Vc o;
+      o.x = (er + (tc * orr + ts * oi)) * scale;
+      o.y = (ei + (tc * oi - ts * orr)) * scale;
+      X[mm * FW_COLS + w] = o;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < (N + 1) * FW_COLS; i += blockDim.x) {  // rows of 8 columns per m
+    const int mm = i / FW_COLS, cc = i - mm * FW_COLS;
+    if (cbase + cc < C) F[((size_t)mm * nlat + j) * C + cbase + cc] = X[i];
   }
 }
 
@@ -484,6 +695,21 @@ static int launch_s2g_into(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, 
     JG_CUDA(cudaGetLastError());
   }
   const int fc = fft_ct(m);
+  // the warp-register FFT wins in FP32; in FP64 the shared-memory radix-2 kernel is faster (measured)
+  if (std::is_same<T, float>::value && m->nlon >= 64 && m->nlon <= 1024 && m->tune[3] == 0) {
+    const size_t smw = (size_t)(m->N + 1) * FW_COLS * sizeof(V);
+    dim3 gw((ip.C + FW_COLS - 1) / FW_COLS, m->nlat);
+    switch (m->nlon) {
+      case 64: k_ifft_w<T, 1><<<gw, 256, smw, st>>>(ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon); break;
+      case 128: k_ifft_w<T, 2><<<gw, 256, smw, st>>>(ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon); break;
+      case 256: k_ifft_w<T, 4><<<gw, 256, smw, st>>>(ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon); break;
+      case 512: k_ifft_w<T, 8><<<gw, 256, smw, st>>>(ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon); break;
+      default: k_ifft_w<T, 16><<<gw, 256, smw, st>>>(ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon); break;
+    }
+    mark(st);
+    JG_CUDA(cudaGetLastError());
+    return JGCM_OK;
+  }
   size_t sm2 = align16((size_t)(fc * m->nlon + m->nlon) * sizeof(T)) + (size_t)(m->N + 1) * fc * sizeof(V);
   dim3 g2((ip.C + fc - 1) / fc, m->nlat);
   k_ifft<T><<<g2, 256, sm2, st>>>(ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon, m->logn - 1, fc);
@@ -513,6 +739,21 @@ int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp, cudaStream_t st, void* fbuf
   JG_ARG(fp.C <= cap && fp.C > 0, "bad FFT plan");
   Tables<T> tb = tables<T>(m);
   const int fc = fft_ct(m);
+  // forward: the warp-register FFT wins in FP32 from nlon = 128 on (measured)
+  if (std::is_same<T, float>::value && m->nlon >= 128 && m->nlon <= 1024 && m->tune[3] == 0) {
+    const size_t smw = ((size_t)FW_COLS * (m->nlon / 2) + (size_t)(m->N + 1) * FW_COLS) * sizeof(V);
+    dim3 gw((fp.C + FW_COLS - 1) / FW_COLS, m->nlat);
+    switch (m->nlon) {
+      case 64: k_fft_w<T, 1><<<gw, 256, smw, st>>>(fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon); break;
+      case 128: k_fft_w<T, 2><<<gw, 256, smw, st>>>(fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon); break;
+      case 256: k_fft_w<T, 4><<<gw, 256, smw, st>>>(fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon); break;
+      case 512: k_fft_w<T, 8><<<gw, 256, smw, st>>>(fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon); break;
+      default: k_fft_w<T, 16><<<gw, 256, smw, st>>>(fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon); break;
+    }
+    mark(st);
+    JG_CUDA(cudaGetLastError());
+    return JGCM_OK;
+  }
   size_t sm = (size_t)(fc * m->nlon + m->nlon) * sizeof(T);
   dim3 g((fp.C + fc - 1) / fc, m->nlat);
   k_fft<T><<<g, 256, sm, st>>>(fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon, m->logn - 1, fc);
