@@ -286,6 +286,7 @@ def ensemble_bench(jgcm, configs, precisions, days=2):
             one.close()
             spd = configs.STEPS_PER_DAY[name]
             ens.step(spd)
+            jgcm.autotune(ens, nsteps=8)
             t = sum(ens.time_steps(spd) for _ in range(days)) / 1000.0
             per[name] = {"member_sim_days_per_s": E * days / t, "ms_per_step": 1000.0 * t / (days * spd)}
             models.append(ens)
@@ -346,6 +347,8 @@ def run_jgcm(args):
     flush = L2Flush(local)
     for mdl in (modmx, mod64):
         mdl.step(spd * W)  # warm-up sim-days (the first step is the reference's init step)
+    # tiles chosen by the library's autotuner (timed on scratch copies; the models' states are untouched)
+    tiles = {"mixed": jgcm.autotune(modmx, nsteps=spd)["tuning"], "fp64": jgcm.autotune(mod64, nsteps=spd)["tuning"]}
     # ---- timed: mixed precision
     clocks = ClockSampler(local)
     barrier(world)
@@ -367,6 +370,7 @@ def run_jgcm(args):
         err[key] = configs.rel_l2(modmx.get(f), mod64.get(f))
     # ---- end to end through host buffers
     e2e_model = jgcm.Model(mmx, params)
+    jgcm.set_tuning(e2e_model, tiles["mixed"])
     host = {f: pinned_like(a) for f, a in init_state.items()}
     bytes_io = sum(a.nbytes for a, _ in host.values())
     for f, (a, _) in host.items():
@@ -426,7 +430,8 @@ def run_jgcm(args):
                                     "N(0,0.1^2) K grid noise",
                    "l2": "flushed (256 MiB write) before every timed sim-day; working set ~20 MB is otherwise "
                          "L2-resident within a day", "parallelism": f"replicas x{world}",
-                   "ms_per_model_step": 1000.0 * t_mx / (K * spd)},
+                   "ms_per_model_step": 1000.0 * t_mx / (K * spd),
+                   "tiles": {"chosen_by": "jgcm.autotune (coordinate search, CUDA-event timed)", **tiles}},
         "fp64": {"value": value64, "unit": "sim-days/s", "ms_per_step": 1000.0 * t_64 / K},
         "speedup_vs_fp64": value / value64,
         "error_vs_fp64": {"after_sim_days": round(days_done, 3), **{k: v for k, v in err.items()}},
