@@ -392,7 +392,8 @@ __global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertC
   }
 }
 
-// lanes per column for a launch: S = 4 for small grids (latency), 1 for large ensembles
+// lanes per column for a launch: S = 4 for small grids (latency), 1 for large ensembles; the
+// autotuner may pick 8
 inline int hs_lanes(const jgcm_mesh* m, int ne, int nd) {
   const size_t cols = (size_t)ne * m->nlat * m->nlon;
   int S = cols >= 65536 ? 1 : cols >= 32768 ? 2 : 4;
@@ -406,7 +407,8 @@ int launch_hs_column(const HSColArgs<T>& a, const jgcm_mesh* m, int ne, int S, c
   dim3 g((m->nlon + cpb - 1) / cpb, m->nlat, ne);
   if (S == 1) k_hs_column<T, 1><<<g, HS_CT, 0, st>>>(a, vc);
   else if (S == 2) k_hs_column<T, 2><<<g, HS_CT, 0, st>>>(a, vc);
-  else k_hs_column<T, 4><<<g, HS_CT, 0, st>>>(a, vc);
+  else if (S == 4) k_hs_column<T, 4><<<g, HS_CT, 0, st>>>(a, vc);
+  else k_hs_column<T, 8><<<g, HS_CT, 0, st>>>(a, vc);
   return JGCM_OK;
 }
 
@@ -952,10 +954,11 @@ int build_wave(jgcm_model* md) {
   return JGCM_OK;
 }
 
-// FP64 block partials per member: the column kernel folds 2 sums over its (nlon/(64/S)) x nlat blocks,
+// FP64 block partials per member: the column kernel folds 2 sums over its (nlon/(64/S)) x nlat blocks
+// (S <= 8),
 // the fixer kernel 3 sums over (nlon/32) x nlat blocks
 size_t partial_stride(const jgcm_mesh* m) {
-  size_t a = (size_t)2 * ((m->nlon + HS_CT / 4 - 1) / (HS_CT / 4)) * m->nlat;
+  size_t a = (size_t)2 * ((m->nlon + HS_CT / 8 - 1) / (HS_CT / 8)) * m->nlat;
   size_t b = (size_t)3 * ((m->nlon + 31) / 32) * m->nlat;
   return a > b ? a : b;
 }
@@ -2250,7 +2253,7 @@ extern "C" int jgcm_model_set_tuning(jgcm_model* md, const int* knobs, int n) {
   JG_ARG(md && knobs && n >= 4, "need 4 knobs");
   jgcm_mesh* m = md->mesh;
   const int lanes = knobs[0] > 0 ? knobs[0] : hs_lanes(m, md->ne, md->nd);
-  JG_ARG(lanes == 1 || lanes == 2 || lanes == 4, "lanes per column must be 1, 2 or 4");
+  JG_ARG(lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8, "lanes per column must be 1, 2, 4 or 8");
   for (int i = 1; i < 4; i++) JG_ARG(knobs[i] >= 0 && knobs[i] <= 256, "tile %d out of range", i);
   int t[4] = {0, knobs[1], knobs[2], knobs[3]};
   const int s2g = t[1] > 0 ? t[1] : (m->nh >= 256 ? 1 : 256 / m->nh);
@@ -2301,7 +2304,7 @@ extern "C" int jgcm_model_autotune(jgcm_model* md, int nsteps, int* knobs_out, f
   const int d1 = m->nh >= 256 ? 1 : 256 / m->nh, d2 = m->nh >= 64 ? 4 : m->nh >= 32 ? 8 : 16,
             d3 = m->nlon >= 1024 ? 1 : 1024 / m->nlon;
   std::vector<std::vector<int>> cand = {
-      {1, 2, 4}, {std::max(1, d1 / 2), d1, 2 * d1, 4 * d1}, {4, 8, 16, 32}, {std::max(1, d3 / 2), d3, 2 * d3}};
+      {1, 2, 4, 8}, {std::max(1, d1 / 2), d1, 2 * d1, 4 * d1}, {4, 8, 16, 32}, {std::max(1, d3 / 2), d3, 2 * d3}};
   if (md->P.kind != JGCM_HELD_SUAREZ) cand[0] = {cur[0]};
   for (int knob = 0; knob < 4; knob++)
     for (int v : cand[knob]) {

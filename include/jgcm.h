@@ -162,7 +162,7 @@ int jgcm_model_copy_member(jgcm_model* dst, int dst_member, jgcm_model* src, int
 int jgcm_model_semi_implicit_step(jgcm_model* model, const double* const* in, double* const* out);
 int jgcm_model_semi_implicit_step_adjoint(jgcm_model* model, const double* const* out_bar, double* const* in_bar);
 /* Tiles (no counterpart in the reference).  knobs[0]: lanes per column of the Held-Suarez column
- * kernel (1, 2, 4; this model); knobs[1..3]: S2G, G2S and FFT columns per block of the SIMT
+ * kernel (1, 2, 4, 8; this model); knobs[1..3]: S2G, G2S and FFT columns per block of the SIMT
  * transform kernels (the mesh: shared by its models).  0 = default.  The autotuner times candidate
  * tiles on a scratch copy of the model (coordinate search, nsteps captured steps each), applies the
  * fastest and returns it with its time per nsteps. */

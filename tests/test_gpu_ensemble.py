@@ -141,7 +141,7 @@ def test_autotuner_keeps_results_and_caches(jg, tmp_path):
     assert set(first["tuning"]) == set(jg.TUNING_KNOBS) and first["ms_per_step"] > 0
     again = jg.autotune(a, nsteps=4, cache=cache)
     assert again == first
-    assert jg.get_tuning(a)["lanes_per_column"] in (1, 2, 4)
+    assert jg.get_tuning(a)["lanes_per_column"] in (1, 2, 4, 8)
     a.step(6)
     b.step(6)
     x, y = jg.Model(mesh_a, params), jg.Model(mesh_b, params)
