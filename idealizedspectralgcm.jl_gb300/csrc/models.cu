@@ -55,6 +55,11 @@ struct jgcm_model {
   int fcap;
   int hs_lanes;  // lanes per column of the Held-Suarez column kernel (1, 2 or 4)
   int graph_gen;  // the mesh's tile generation the captured graphs were built with
+  // Held-Suarez: the gradients of ln ps and T of the current level are already in g_dlps ...
+  // g_dtT (computed at the end of the previous step, concurrently with the fixers)
+  int grad_ready;
+  cudaStream_t side;        // second branch of a step (the gradients next to the fixers)
+  cudaEvent_t ev_fork, ev_join;
   double cp_air;
   // time-levelled state (index by rotation)
   void *spe_vor[3], *spe_div[3], *spe_lnps[3], *spe_t[3];
@@ -248,7 +253,9 @@ __global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertC
   const T ln_pref = (T)11.512925464970229;  // ln 1e5 (HS_Forcing.jl:49 p_ref)
   const T tDt = (T)a.Dt;
   const T ps = act ? a.ps_c[c1] : (T)1, psp = act ? a.ps_p[c1] : (T)0;
-  const T dlps = act ? a.dlps[c1] : (T)0, dtps = act ? a.dtps[c1] : (T)0, gs = act ? a.geopots[c1] : (T)0;
+  // ∇ps / cos θ = (∇ ln ps / cos θ) ps (Spectral_Dynamics.jl:259-264)
+  const T dlps = act ? a.dlps[c1] * ps : (T)0, dtps = act ? a.dtps[c1] * ps : (T)0;
+  const T gs = act ? a.geopots[c1] : (T)0;
   // ---- pressure variables from ps_c (Pressure_Variables!, Press_And_Geopot.jl:36-67)
   const T lnps = log(ps);
   // ---- pass 1: Compute_Geopotential! (Press_And_Geopot.jl:71-111) on T - T0_k with T0_k the level's
@@ -917,6 +924,9 @@ void model_free(jgcm_model* md) {
   for (auto p : ps)
     if (p) cudaFree(p);
   delete[] md->div_mat;
+  if (md->ev_fork) cudaEventDestroy(md->ev_fork);
+  if (md->ev_join) cudaEventDestroy(md->ev_join);
+  if (md->side) cudaStreamDestroy(md->side);
   if (md->ev0) cudaEventDestroy(md->ev0);
   if (md->ev1) cudaEventDestroy(md->ev1);
   delete md;
@@ -1023,6 +1033,9 @@ int model_alloc(jgcm_model* md) {
   JG_CUDA(cudaGetLastError());
   JG_CUDA(cudaEventCreate(&md->ev0));
   JG_CUDA(cudaEventCreate(&md->ev1));
+  JG_CUDA(cudaEventCreateWithFlags(&md->ev_fork, cudaEventDisableTiming));
+  JG_CUDA(cudaEventCreateWithFlags(&md->ev_join, cudaEventDisableTiming));
+  JG_CUDA(cudaStreamCreateWithFlags(&md->side, cudaStreamNonBlocking));
   md->div_mat = new double[nd * nd]();
   vertical_setup(md);
   JG_TRY(alloc((void**)&md->d_vc, sizeof(VertCoef)));
@@ -1199,29 +1212,39 @@ int step_shallow_water(jgcm_model* md, cudaStream_t st) {
 }
 
 // Atmosphere_Update! (Spectral_Dynamics.jl:470-490) for Held-Suarez.
+// Gradients (cos θ ∇ / cos θ) of ln ps and T of time level `lev` into g_dlps, g_dtps, g_dlT, g_dtT
+// (Compute_Gradients!, Spectral_Spherical_Mesh.jl:721-741).  They read no (0,0) spectral mode (its
+// coefficients m/a and (n-1) ε_n/a vanish), so they may run while the fixers adjust those modes.
+template <typename T>
+int issue_hs_grad(jgcm_model* md, int lev, cudaStream_t st) {
+  const int L = md->L, E = md->ne;
+  S2GPlan sp;
+  memset(&sp, 0, sizeof(sp));
+  sp.ng = 4;
+  sp.C = 2 * E + 2 * L;
+  sp.g[0] = sg(S2G_DLAM, md->spe_lnps[lev], nullptr, E, 0);
+  sp.g[1] = sg(S2G_DTH, md->spe_lnps[lev], nullptr, E, E);
+  sp.g[2] = sg(S2G_DLAM, md->spe_t[lev], nullptr, L, 2 * E);
+  sp.g[3] = sg(S2G_DTH, md->spe_t[lev], nullptr, L, 2 * E + L);
+  IFFTPlan ip;
+  memset(&ip, 0, sizeof(ip));
+  ip.ng = 4;
+  ip.C = 2 * E + 2 * L;
+  ip.g[0] = og(EPI_DIVCOS, md->g_dlps, E, 0);
+  ip.g[1] = og(EPI_DIVCOS, md->g_dtps, E, E);
+  ip.g[2] = og(EPI_DIVCOS, md->g_dlT, L, 2 * E);
+  ip.g[3] = og(EPI_DIVCOS, md->g_dtT, L, 2 * E + L);
+  return launch_s2g<T>(md->mesh, sp, ip, st, md->fbuf, md->fcap);
+}
+
 template <typename T>
 int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   jgcm_mesh* m = md->mesh;
   const int nd = md->nd, L = md->L, E = md->ne, p = lvl(md, 0), c = lvl(md, 1), n = lvl(md, 2);
   const int Dt = md->init_step ? md->P.dt : 2 * md->P.dt;
-  // 1. gradients of lnps_c (-> ∇ps = ∇lnps * ps) and of T_c
-  S2GPlan sp;
-  memset(&sp, 0, sizeof(sp));
-  sp.ng = 4;
-  sp.C = 2 * E + 2 * L;
-  sp.g[0] = sg(S2G_DLAM, md->spe_lnps[c], nullptr, E, 0);
-  sp.g[1] = sg(S2G_DTH, md->spe_lnps[c], nullptr, E, E);
-  sp.g[2] = sg(S2G_DLAM, md->spe_t[c], nullptr, L, 2 * E);
-  sp.g[3] = sg(S2G_DTH, md->spe_t[c], nullptr, L, 2 * E + L);
-  IFFTPlan ip;
-  memset(&ip, 0, sizeof(ip));
-  ip.ng = 4;
-  ip.C = 2 * E + 2 * L;
-  ip.g[0] = og(EPI_DIVCOS_MULPS, md->g_dlps, E, 0, nullptr, md->grid_ps[c]);
-  ip.g[1] = og(EPI_DIVCOS_MULPS, md->g_dtps, E, E, nullptr, md->grid_ps[c]);
-  ip.g[2] = og(EPI_DIVCOS, md->g_dlT, L, 2 * E);
-  ip.g[3] = og(EPI_DIVCOS, md->g_dtT, L, 2 * E + L);
-  JG_TRY(launch_s2g<T>(m, sp, ip, st, md->fbuf, md->fcap));
+  // 1. gradients of lnps_c and T_c, unless the previous step left them (∇ps = ∇lnps ps is formed in
+  //    the column kernel)
+  if (!md->grad_ready) JG_TRY(issue_hs_grad<T>(md, c, st));
   // 2. physics + grid dynamics (one warp per column)
   Tables<T> tb = tables<T>(m);
   HSColArgs<T> a;
@@ -1375,6 +1398,13 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ca.do_energy = md->P.do_energy_correction;
   ca.cp = md->cp_air;
   ca.grav = md->P.grav;
+  // the fixers (this branch) and the next step's gradients of the new level (second branch)
+  const bool serial = g_marker != nullptr;  // per-kernel timing: one stream, launches in order
+  cudaStream_t br = serial ? st : md->side;
+  if (!serial) {
+    JG_CUDA(cudaEventRecord(md->ev_fork, st));
+    JG_CUDA(cudaStreamWaitEvent(br, md->ev_fork, 0));
+  }
   k_hs_corr_reduce<T><<<dim3((m->nlon + 31) / 32, m->nlat, E), 256, 0, st>>>(ca, md->d_vc);
   mark(st);
   JG_CUDA(cudaGetLastError());
@@ -1385,6 +1415,11 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
                                                   (size_t)nd * G1, G1);
   mark(st);
   JG_CUDA(cudaGetLastError());
+  JG_TRY(issue_hs_grad<T>(md, n, br));
+  if (!serial) {
+    JG_CUDA(cudaEventRecord(md->ev_join, br));
+    JG_CUDA(cudaStreamWaitEvent(st, md->ev_join, 0));
+  }
   return JGCM_OK;
 }
 
@@ -1405,6 +1440,7 @@ int issue(jgcm_model* md, cudaStream_t st) {
 }
 
 void after_step(jgcm_model* md) {
+  md->grad_ready = md->P.kind == JGCM_HELD_SUAREZ;
   md->rot = (md->rot + 1) % 3;
   md->init_step = 0;
   md->sw_adv_from_n = 0;
@@ -1447,7 +1483,7 @@ int graph_step(jgcm_model* md) {
 }
 
 int model_step(jgcm_model* md) {
-  if (md->init_step || md->sw_adv_from_n) {
+  if (md->init_step || md->sw_adv_from_n || (md->P.kind == JGCM_HELD_SUAREZ && !md->grad_ready)) {
     JG_TRY(issue(md, md->mesh->stream));
     after_step(md);
     return JGCM_OK;
@@ -1600,9 +1636,9 @@ extern "C" int jgcm_model_launches_per_step(jgcm_model* md, int* launches) {
 
 extern "C" int jgcm_model_kernel_name(jgcm_model* md, int slot, char* buf, int cap) {
   JG_ARG(md && buf && cap > 0, "bad arguments");
-  static const char* hs[] = {"s2g_legendre(grad lnps,T)", "ifft(grad lnps,T)", "hs_column", "fft(tendencies)",
-                             "g2s_legendre(vor,div,T,lnps)", "hs_implicit", "s2g_legendre(vor,div,u,v,T,lnps)",
-                             "ifft(vor,div,u,v,T,lnps)", "hs_corr_reduce", "hs_corr_apply"};
+  static const char* hs[] = {"hs_column", "fft(tendencies)", "g2s_legendre(vor,div,T,lnps)", "hs_implicit",
+                             "s2g_legendre(vor,div,u,v,T,lnps)", "ifft(vor,div,u,v,T,lnps)", "hs_corr_reduce",
+                             "hs_corr_apply", "s2g_legendre(grad lnps,T)", "ifft(grad lnps,T)"};
   static const char* bt[] = {"fft(flux)", "g2s_legendre(vor+leapfrog)", "s2g_legendre(vor,u,v)", "ifft(vor,u,v)"};
   static const char* sw[] = {"s2g_legendre(grad h)", "ifft(grad h)", "fft(fluxes,kin,dh)",
                              "g2s_legendre(vor,div,h+implicit+leapfrog)", "s2g_legendre(vor,div,h,u,v)",
@@ -1629,7 +1665,7 @@ extern "C" int jgcm_model_kernel_times(jgcm_model* md, int nsteps, float* ms, in
   jgcm_mesh* m = md->mesh;
   const int L = launches_per_step(md);
   JG_ARG(cap >= L, "buffer too small");
-  if (md->init_step) JG_TRY(model_step(md));
+  if (md->init_step || (md->P.kind == JGCM_HELD_SUAREZ && !md->grad_ready)) JG_TRY(model_step(md));
   std::vector<cudaEvent_t> ev((size_t)nsteps * L + 1);
   for (auto& e : ev) JG_CUDA(cudaEventCreate(&e));
   Marker mk{ev.data() + 1, 0, nsteps * L};
@@ -1675,9 +1711,16 @@ extern "C" int jgcm_model_kernel_times(jgcm_model* md, int nsteps, float* ms, in
 extern "C" int jgcm_model_time_steps(jgcm_model* md, int nsteps, float* ms) {
   JG_ARG(md && ms && nsteps > 0, "bad arguments");
   jgcm_mesh* m = md->mesh;
-  if (md->init_step) JG_TRY(model_step(md));
-  // make sure every phase is captured before timing
-  for (int s = 0; s < 3 && md->steps_done < 4; s++) JG_TRY(model_step(md));
+  while (md->init_step || md->sw_adv_from_n || (md->P.kind == JGCM_HELD_SUAREZ && !md->grad_ready))
+    JG_TRY(model_step(md));
+  // capture every rotation phase before timing (after a tile change the graphs are rebuilt)
+  auto captured = [&]() {
+    if (md->graph_gen != m->tune_gen) return false;
+    for (auto g : md->graph)
+      if (!g) return false;
+    return true;
+  };
+  for (int s = 0; s < 3 && !captured(); s++) JG_TRY(graph_step(md));
   JG_CUDA(cudaStreamSynchronize(m->stream));
   JG_CUDA(cudaEventRecord(md->ev0, m->stream));
   for (int s = 0; s < nsteps; s++) JG_TRY(graph_step(md));
@@ -1741,6 +1784,7 @@ extern "C" int jgcm_model_set_field(jgcm_model* md, const char* name, const doub
   else
     JG_TRY(grid_host_to_dev(m, m->d_stage, f.ptr, n, st));
   if (!strcmp(name, "spe_lnps_n")) md->sw_adv_from_n = 1;
+  md->grad_ready = 0;  // the gradients of the current level are recomputed by the next step
   JG_CUDA(cudaStreamSynchronize(st));
   return JGCM_OK;
 }
@@ -2052,6 +2096,7 @@ extern "C" int jgcm_model_copy_member(jgcm_model* dst, int dst_member, jgcm_mode
   JG_TRY(grid(dst->grid_lnps, src->grid_lnps, 1));
   JG_TRY(grid(dst->grid_geopots, src->grid_geopots, 1));
   JG_TRY(grid(dst->grid_h_eq, src->grid_h_eq, 1));
+  dst->grad_ready = 0;
   if (dst->ne == 1) {  // a one-member model takes the source's time-step state
     dst->init_step = src->init_step;
     dst->sw_adv_from_n = src->sw_adv_from_n;
@@ -2091,10 +2136,11 @@ std::vector<int> ensemble_key(const jgcm_ensemble* en) {  // rotations and tiles
 
 int ensemble_capture(jgcm_ensemble* en, cudaGraphExec_t* out) {
   struct Saved {
-    int rot, init_step, sw_adv_from_n, steps_done;
+    int rot, init_step, sw_adv_from_n, steps_done, grad_ready;
   };
   std::vector<Saved> saved;
-  for (auto* md : en->models) saved.push_back({md->rot, md->init_step, md->sw_adv_from_n, md->steps_done});
+  for (auto* md : en->models)
+    saved.push_back({md->rot, md->init_step, md->sw_adv_from_n, md->steps_done, md->grad_ready});
   cudaGraph_t g;
   JG_CUDA(cudaStreamBeginCapture(en->st, cudaStreamCaptureModeThreadLocal));
   int s = JGCM_OK;
@@ -2114,6 +2160,7 @@ int ensemble_capture(jgcm_ensemble* en, cudaGraphExec_t* out) {
     en->models[i]->init_step = saved[i].init_step;
     en->models[i]->sw_adv_from_n = saved[i].sw_adv_from_n;
     en->models[i]->steps_done = saved[i].steps_done;
+    en->models[i]->grad_ready = saved[i].grad_ready;
   }
   if (s != JGCM_OK || e != cudaSuccess || e2 != cudaSuccess) {
     if (e2 == cudaSuccess) cudaGraphDestroy(g);
@@ -2141,6 +2188,12 @@ int ensemble_graph(jgcm_ensemble* en, cudaGraphExec_t* out) {
 }
 
 int ensemble_window(jgcm_ensemble* en) {
+  for (auto* md : en->models)  // window graphs start from ready gradients
+    if (md->P.kind == JGCM_HELD_SUAREZ && !md->grad_ready) {
+      JG_TRY(is_fp64(md->mesh) ? issue_hs_grad<double>(md, lvl(md, 1), en->st)
+                               : issue_hs_grad<float>(md, lvl(md, 1), en->st));
+      md->grad_ready = 1;
+    }
   cudaGraphExec_t g;
   JG_TRY(ensemble_graph(en, &g));
   JG_CUDA(cudaGraphLaunch(g, en->st));
