@@ -303,21 +303,26 @@ def ensemble_bench(jgcm, configs, precisions, days=2):
     return out
 
 
-def tensor_core_modes(jgcm, configs, mod64, days):
+def tensor_core_modes(jgcm, configs, days):
     """HS T42L20 with the Legendre contractions on the tensor cores (TF32x3, BF16x3): sim-days/s and
-    the error against the FP64 path after the same days from the same state."""
+    the error against an FP64 GPU twin stepped the same days from the same state."""
     out = {}
     spd = configs.STEPS_PER_DAY[WORKLOAD]
     params = configs.PARAMS[WORKLOAD]
+    m64 = configs.make_mesh(jgcm, WORKLOAD, precision="fp64")
+    ref = jgcm.Model(m64, params)
+    configs.init_held_suarez(jgcm, m64, ref)
+    ref.step(spd * days)
     for prec in ("tf32x3", "bf16x3"):
         m = configs.make_mesh(jgcm, WORKLOAD, precision=prec)
         md = jgcm.Model(m, params)
         configs.init_held_suarez(jgcm, m, md)
         md.step(spd * days)
-        err = {k: configs.rel_l2(md.get(f), mod64.get(f))
+        err = {k: configs.rel_l2(md.get(f), ref.get(f))
                for k, f in (("T", "grid_t_c"), ("u", "grid_u_c"), ("v", "grid_v_c"), ("ps", "grid_ps_c"))}
+        jgcm.autotune(md, nsteps=spd)
         ms = md.time_steps(spd)
-        out[prec] = {"value": 1000.0 / ms, "unit": "sim-days/s", "error_vs_fp64_same_days": err}
+        out[prec] = {"value": 1000.0 / ms, "unit": "sim-days/s", "after_sim_days": days, "error_vs_fp64": err}
     return out
 
 
@@ -414,7 +419,7 @@ def run_jgcm(args):
     if not args.no_ensemble and world == 1:
         try:
             # error of the tensor-core modes after the same W + K days as the FP64 run
-            extra["tensor_core_modes"] = tensor_core_modes(jgcm, configs, mod64, days_done)
+            extra["tensor_core_modes"] = tensor_core_modes(jgcm, configs, days_done)
             extra["ensemble"] = ensemble_bench(jgcm, configs, ["fp32", "tf32x3"])
         except Exception as e:
             extra["ensemble_error"] = str(e)

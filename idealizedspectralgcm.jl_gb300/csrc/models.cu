@@ -60,6 +60,11 @@ struct jgcm_model {
   int grad_ready;
   cudaStream_t side;        // second branch of a step (the gradients next to the fixers)
   cudaEvent_t ev_fork, ev_join;
+  // on-device diagnostics (Output_Manager.jl:81-107): FP64 sums after every step of the zonal means
+  // of T, T_eq, u, v ([4][ne][nd][nlat]) and of ps ([ne][nlat][nlon]), and the number of steps summed
+  double* diag;
+  int diag_on;
+  long diag_steps;
   double cp_air;
   // time-levelled state (index by rotation)
   void *spe_vor[3], *spe_div[3], *spe_lnps[3], *spe_t[3];
@@ -920,7 +925,7 @@ void model_free(jgcm_model* md) {
                 md->spe_zero, md->spe_dvor, md->spe_ddiv, md->spe_dlnps, md->spe_dt, md->g_dlps, md->g_dtps,
                 md->g_dlT, md->g_dtT, md->g_ducos, md->g_dvcos, md->g_dt, md->g_energy, md->g_dlnps, md->g_diag,
                 md->coriolis, md->damping, md->dfac[0], md->dfac[1], md->d_W, md->d_pairs, md->d_partials,
-                md->d_scalars, md->d_counter, md->d_vc, md->fbuf};
+                md->d_scalars, md->d_counter, md->d_vc, md->fbuf, md->diag};
   for (auto p : ps)
     if (p) cudaFree(p);
   delete[] md->div_mat;
@@ -1212,6 +1217,53 @@ int step_shallow_water(jgcm_model* md, cudaStream_t st) {
 }
 
 // Atmosphere_Update! (Spectral_Dynamics.jl:470-490) for Held-Suarez.
+// Zonal means of T, T_eq, u, v added to the FP64 sums (Zonal_Mean, Output_Manager.jl:81-107):
+// block (latitude j, level k, member e), threads over longitude, fixed-order FP64 reduction.
+template <typename T>
+__global__ void k_diag_zonal(const T* t, const T* t_eq, const T* u, const T* v, double* sums, int nd, int nlat,
+                             int nlon, int ne) {
+  const int j = blockIdx.x, k = blockIdx.y, e = blockIdx.z;
+  const size_t G = (size_t)nlat * nlon, row = ((size_t)e * nd + k) * G + (size_t)j * nlon;
+  __shared__ double red[4][4];
+  double acc[4] = {0, 0, 0, 0};
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) {
+    acc[0] += (double)t[row + i];
+    acc[1] += (double)t_eq[row + i];
+    acc[2] += (double)u[row + i];
+    acc[3] += (double)v[row + i];
+  }
+  for (int f = 0; f < 4; f++) acc[f] = warp_sum(acc[f]);
+  if ((threadIdx.x & 31) == 0)
+    for (int f = 0; f < 4; f++) red[f][threadIdx.x >> 5] = acc[f];
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    const int f = threadIdx.x;
+    double tot = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += red[f][w];
+    sums[(((size_t)f * ne + e) * nd + k) * nlat + j] += tot / nlon;
+  }
+}
+template <typename T>
+__global__ void k_diag_ps(const T* ps, double* sums, size_t n) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+    sums[q] += (double)ps[q];
+}
+
+template <typename T>
+int issue_diag(jgcm_model* md, int lev, cudaStream_t st) {
+  jgcm_mesh* m = md->mesh;
+  const int nd = md->nd, E = md->ne;
+  k_diag_zonal<T><<<dim3(m->nlat, nd, E), 128, 0, st>>>((const T*)md->grid_t[lev], (const T*)md->grid_t_eq,
+                                                         (const T*)md->grid_u[lev], (const T*)md->grid_v[lev],
+                                                         md->diag, nd, m->nlat, m->nlon, E);
+  JG_CUDA(cudaGetLastError());
+  const size_t nps = grid_elems(m, E);
+  k_diag_ps<T><<<(int)std::min<size_t>((nps + 255) / 256, 1024), 256, 0, st>>>(
+      (const T*)md->grid_ps[lev], md->diag + (size_t)4 * E * nd * m->nlat, nps);
+  JG_CUDA(cudaGetLastError());
+  return JGCM_OK;
+}
+
 // Gradients (cos θ ∇ / cos θ) of ln ps and T of time level `lev` into g_dlps, g_dtps, g_dlT, g_dtT
 // (Compute_Gradients!, Spectral_Spherical_Mesh.jl:721-741).  They read no (0,0) spectral mode (its
 // coefficients m/a and (n-1) ε_n/a vanish), so they may run while the fixers adjust those modes.
@@ -1416,6 +1468,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   mark(st);
   JG_CUDA(cudaGetLastError());
   JG_TRY(issue_hs_grad<T>(md, n, br));
+  if (md->diag_on && !serial) JG_TRY(issue_diag<T>(md, n, st));  // the new state, after the fixers
   if (!serial) {
     JG_CUDA(cudaEventRecord(md->ev_join, br));
     JG_CUDA(cudaStreamWaitEvent(st, md->ev_join, 0));
@@ -1441,6 +1494,7 @@ int issue(jgcm_model* md, cudaStream_t st) {
 
 void after_step(jgcm_model* md) {
   md->grad_ready = md->P.kind == JGCM_HELD_SUAREZ;
+  if (md->diag_on) md->diag_steps++;
   md->rot = (md->rot + 1) % 3;
   md->init_step = 0;
   md->sw_adv_from_n = 0;
@@ -1666,6 +1720,12 @@ extern "C" int jgcm_model_kernel_times(jgcm_model* md, int nsteps, float* ms, in
   const int L = launches_per_step(md);
   JG_ARG(cap >= L, "buffer too small");
   if (md->init_step || (md->P.kind == JGCM_HELD_SUAREZ && !md->grad_ready)) JG_TRY(model_step(md));
+  struct DiagOff {  // the timed steps run without the diagnostics' reductions (and are not summed)
+    jgcm_model* md;
+    int saved;
+    ~DiagOff() { md->diag_on = saved; }
+  } diag_off{md, md->diag_on};
+  md->diag_on = 0;
   std::vector<cudaEvent_t> ev((size_t)nsteps * L + 1);
   for (auto& e : ev) JG_CUDA(cudaEventCreate(&e));
   Marker mk{ev.data() + 1, 0, nsteps * L};
@@ -2720,3 +2780,51 @@ extern "C" int jgcm_model_semi_implicit_step_adjoint(jgcm_model* md, const doubl
   }
   return JGCM_OK;
 }
+
+// ------------------------------------------------------------------------------------------
+// On-device diagnostics (the reductions of Output_Manager.jl:81-145; its file output and plots stay
+// with the host).  Held-Suarez only.
+extern "C" int jgcm_model_diagnostics(jgcm_model* md, int on) {
+  JG_ARG(md, "NULL model");
+  JG_ARG(md->P.kind == JGCM_HELD_SUAREZ, "diagnostics are kept for Held-Suarez models");
+  jgcm_mesh* m = md->mesh;
+  const size_t n = (size_t)4 * md->ne * md->nd * m->nlat + grid_elems(m, md->ne);
+  JG_CUDA(cudaStreamSynchronize(m->stream));
+  if (on) {
+    if (!md->diag) JG_TRY(alloc((void**)&md->diag, n * 8));
+    JG_CUDA(cudaMemset(md->diag, 0, n * 8));
+    md->diag_steps = 0;
+  }
+  if ((on != 0) != (md->diag_on != 0)) drop_graphs(md);  // the step graphs gain / lose the reduction
+  md->diag_on = on != 0;
+  return JGCM_OK;
+}
+
+// Means over the steps summed since jgcm_model_diagnostics(model, 1): "t_zonal_mean",
+// "t_eq_zonal_mean", "u_zonal_mean", "v_zonal_mean" ([nθ, nd, members], column-major) and
+// "ps_mean" ([nλ, nθ, members]); `steps` returns the number of steps summed.
+extern "C" int jgcm_model_read_diagnostics(jgcm_model* md, const char* name, double* out, long cap, long* count,
+                                           long* steps) {
+  JG_ARG(md && name, "NULL argument");
+  JG_ARG(md->diag, "diagnostics were never started");
+  jgcm_mesh* m = md->mesh;
+  const std::string nm(name);
+  const char* names[4] = {"t_zonal_mean", "t_eq_zonal_mean", "u_zonal_mean", "v_zonal_mean"};
+  int f = -1;
+  for (int i = 0; i < 4; i++)
+    if (nm == names[i]) f = i;
+  JG_ARG(f >= 0 || nm == "ps_mean", "unknown diagnostic '%s'", name);
+  const size_t nz = (size_t)md->ne * md->nd * m->nlat;
+  const size_t n = f >= 0 ? nz : grid_elems(m, md->ne);
+  if (count) *count = (long)n;
+  if (steps) *steps = md->diag_steps;
+  if (!out) return JGCM_OK;
+  JG_ARG(cap >= (long)n, "buffer too small");
+  JG_CUDA(cudaStreamSynchronize(m->stream));
+  const double* src = md->diag + (f >= 0 ? (size_t)f * nz : 4 * nz);
+  JG_CUDA(cudaMemcpy(out, src, n * 8, cudaMemcpyDeviceToHost));  // [e][k][j] / [e][j][i]: Julia order
+  const double sc = md->diag_steps > 0 ? 1.0 / (double)md->diag_steps : 0.0;
+  for (size_t q = 0; q < n; q++) out[q] *= sc;
+  return JGCM_OK;
+}
+

@@ -86,6 +86,8 @@ def lib():
         "jgcm_model_copy_member": (I, [P, I, P, I]),
         "jgcm_model_semi_implicit_step": (I, [P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
         "jgcm_model_semi_implicit_step_adjoint": (I, [P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+        "jgcm_model_diagnostics": (I, [P, I]),
+        "jgcm_model_read_diagnostics": (I, [P, C.c_char_p, P, Lg, C.POINTER(Lg), C.POINTER(Lg)]),
         "jgcm_model_get_tuning": (I, [P, C.POINTER(I), I]),
         "jgcm_model_set_tuning": (I, [P, C.POINTER(I), I]),
         "jgcm_model_autotune": (I, [P, I, C.POINTER(I), C.POINTER(C.c_float)]),
@@ -327,6 +329,24 @@ class Model:
         h = C.c_void_p()
         _check(lib().jgcm_model_create_members(mesh._h, C.byref(p), self.members, C.byref(h)))
         self._h = h
+
+    def diagnostics(self, on=True):
+        """Start (zeroing the sums) or stop the on-device diagnostics (Held-Suarez): after every step
+        the zonal means of T, T_eq, u, v and the ps field are added to FP64 sums."""
+        _check(lib().jgcm_model_diagnostics(self._h, int(bool(on))))
+
+    def read_diagnostics(self, name):
+        """Mean over the summed steps of 't_zonal_mean', 't_eq_zonal_mean', 'u_zonal_mean',
+        'v_zonal_mean' ([nθ, nd] per member) or 'ps_mean' ([nλ, nθ] per member), and the step count."""
+        n, steps = C.c_long(), C.c_long()
+        _check(lib().jgcm_model_read_diagnostics(self._h, name.encode(), None, 0, C.byref(n), C.byref(steps)))
+        out = np.zeros(n.value)
+        _check(lib().jgcm_model_read_diagnostics(self._h, name.encode(), _ptr(out), n.value, C.byref(n),
+                                                 C.byref(steps)))
+        m = self.mesh
+        shape = (m.nlon, m.nlat, self.members) if name == "ps_mean" else (m.nlat, m.nd, self.members)
+        out = out.reshape(shape, order="F")
+        return (out[..., 0] if self.members == 1 else out), int(steps.value)
 
     def copy_member(self, member: int, src: "Model", src_member: int = 0):
         """Member `member` of this model <- member `src_member` of `src` (same mesh and kind)."""

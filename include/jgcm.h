@@ -161,6 +161,14 @@ int jgcm_model_copy_member(jgcm_model* dst, int dst_member, jgcm_model* src, int
  * arrays [N+1, N+2, nd] (lnps: 1 level).  The adjoint maps cotangents of out to cotangents of in. */
 int jgcm_model_semi_implicit_step(jgcm_model* model, const double* const* in, double* const* out);
 int jgcm_model_semi_implicit_step_adjoint(jgcm_model* model, const double* const* out_bar, double* const* in_bar);
+/* On-device diagnostics (Held-Suarez): the reductions of Update_Output! (Output_Manager.jl:81-107)
+ * as FP64 sums after every step — zonal means of T, T_eq, u, v and the ps field.  on = 1 zeroes
+ * the sums and starts; on = 0 stops.  read returns the mean over the summed steps of
+ * "t_zonal_mean", "t_eq_zonal_mean", "u_zonal_mean", "v_zonal_mean" ([nθ, nd, members]) or
+ * "ps_mean" ([nλ, nθ, members]) and, in *steps, how many steps were summed. */
+int jgcm_model_diagnostics(jgcm_model* model, int on);
+int jgcm_model_read_diagnostics(jgcm_model* model, const char* name, double* out, long cap, long* count,
+                                long* steps);
 /* Tiles (no counterpart in the reference).  knobs[0]: lanes per column of the Held-Suarez column
  * kernel (1, 2, 4, 8; this model); knobs[1..3]: S2G, G2S and FFT columns per block of the SIMT
  * transform kernels (the mesh: shared by its models).  0 = default.  The autotuner times candidate

@@ -173,3 +173,38 @@ def test_hs_forcing_entry_point(jg, orc, prec, tol):
         assert configs.rel_l2(a, b) < tol, (name, configs.rel_l2(a, b))
     with pytest.raises(AssertionError):
         jg.HS_Forcing(gmod, 0, *ins, *[np.zeros_like(ins[0]) for _ in range(4)])
+
+
+@pytest.mark.parametrize("members", [1, 2])
+def test_on_device_zonal_mean_diagnostics(jg, members):
+    """Update_Output! (Output_Manager.jl:81-107) as on-device FP64 sums: the means over the steps
+    equal the zonal means of the fields read back after every step."""
+    name = "hs_t21l10"
+    gm = configs.make_mesh(jg, name, precision="fp64")
+    params = configs.PARAMS[name]
+    md = jg.Model(gm, params, members=members)
+    one = jg.Model(gm, params)
+    for e in range(members):
+        configs.init_held_suarez(jg, gm, one, seed=configs.BASE_SEED + e)
+        md.copy_member(e, one)
+    md.step(2)
+    md.diagnostics(True)
+    want = {k: 0.0 for k in ("t_zonal_mean", "t_eq_zonal_mean", "u_zonal_mean", "v_zonal_mean", "ps_mean")}
+    nsteps = 6
+    reader = jg.Model(gm, params)
+    for _ in range(nsteps):
+        md.step(1)
+        for e in range(members):
+            reader.copy_member(0, md, e)
+            for key, field in (("t_zonal_mean", "grid_t_c"), ("t_eq_zonal_mean", "grid_t_eq"),
+                               ("u_zonal_mean", "grid_u_c"), ("v_zonal_mean", "grid_v_c")):
+                z = reader.get(field).mean(axis=0)
+                want[key] = want[key] + (z if members == 1 else np.stack([z if i == e else 0 * z
+                                                                          for i in range(members)], -1))
+            ps = reader.get("grid_ps_c")[:, :, 0]
+            want["ps_mean"] = want["ps_mean"] + (ps if members == 1 else np.stack([ps if i == e else 0 * ps
+                                                                                  for i in range(members)], -1))
+    for key, w in want.items():
+        got, steps = md.read_diagnostics(key)
+        assert steps == nsteps
+        assert configs.rel_l2(got, w / nsteps) < 1e-12, key
