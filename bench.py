@@ -13,7 +13,9 @@ value      sim-days/s of the mixed-precision path (FP32 state, transforms and te
 e2e        the same through the C ABI with host (pinned) buffers: per sim-day the prognostic state is
            uploaded, 72 steps run, and the state is read back; wall-clock.
 fp64       the FP64 GPU path on the same workload, same timing; error_vs_fp64 = relative L2 of
-           T, u, v, ps between the two paths after the same number of days.
+           T, u, v, ps of a mixed-precision twin against an FP64 twin stepped the same days from
+           the same state (tensor_core_modes: the same for TF32x3 / BF16x3, with their speed).
+tiles      both timed paths run the tiles the library's autotuner picks at start-up.
 roofline   the dominant kernel of the mixed step (largest summed CUDA-event time), its algorithmic
            bytes per launch / its mean launch time, against the measured HBM copy bandwidth.
 cpu_baseline  the FP64 C oracle (a restatement of the reference on the host) timed on a bounded sample.
@@ -303,9 +305,10 @@ def ensemble_bench(jgcm, configs, precisions, days=2):
     return out
 
 
-def tensor_core_modes(jgcm, configs, days):
-    """HS T42L20 with the Legendre contractions on the tensor cores (TF32x3, BF16x3): sim-days/s and
-    the error against an FP64 GPU twin stepped the same days from the same state."""
+def precision_modes(jgcm, configs, days, timed=("tf32x3", "bf16x3")):
+    """HS T42L20 in each mixed mode (FP32 SIMT; TF32x3 and BF16x3: the Legendre contractions on the
+    tensor cores): the relative L2 error against an FP64 GPU twin stepped the same days from the same
+    state, and for the tensor-core modes their tuned sim-days/s."""
     out = {}
     spd = configs.STEPS_PER_DAY[WORKLOAD]
     params = configs.PARAMS[WORKLOAD]
@@ -313,16 +316,17 @@ def tensor_core_modes(jgcm, configs, days):
     ref = jgcm.Model(m64, params)
     configs.init_held_suarez(jgcm, m64, ref)
     ref.step(spd * days)
-    for prec in ("tf32x3", "bf16x3"):
+    for prec in ("fp32",) + tuple(timed):
         m = configs.make_mesh(jgcm, WORKLOAD, precision=prec)
         md = jgcm.Model(m, params)
         configs.init_held_suarez(jgcm, m, md)
         md.step(spd * days)
         err = {k: configs.rel_l2(md.get(f), ref.get(f))
                for k, f in (("T", "grid_t_c"), ("u", "grid_u_c"), ("v", "grid_v_c"), ("ps", "grid_ps_c"))}
-        jgcm.autotune(md, nsteps=spd)
-        ms = md.time_steps(spd)
-        out[prec] = {"value": 1000.0 / ms, "unit": "sim-days/s", "after_sim_days": days, "error_vs_fp64": err}
+        out[prec] = {"after_sim_days": days, "error_vs_fp64": err}
+        if prec in timed:
+            jgcm.autotune(md, nsteps=spd)
+            out[prec].update({"value": 1000.0 / md.time_steps(spd), "unit": "sim-days/s"})
     return out
 
 
@@ -370,9 +374,9 @@ def run_jgcm(args):
         flush()
         ms_64.append(mod64.time_steps(spd))
     days_done = W + K
-    err = {}
-    for key, f in (("T", "grid_t_c"), ("u", "grid_u_c"), ("v", "grid_v_c"), ("ps", "grid_ps_c")):
-        err[key] = configs.rel_l2(modmx.get(f), mod64.get(f))
+    modes = precision_modes(jgcm, configs, days_done, timed=() if (args.no_ensemble or world > 1)
+                            else ("tf32x3", "bf16x3"))
+    err = modes["fp32"]["error_vs_fp64"]
     # ---- end to end through host buffers
     e2e_model = jgcm.Model(mmx, params)
     jgcm.set_tuning(e2e_model, tiles["mixed"])
@@ -419,7 +423,7 @@ def run_jgcm(args):
     if not args.no_ensemble and world == 1:
         try:
             # error of the tensor-core modes after the same W + K days as the FP64 run
-            extra["tensor_core_modes"] = tensor_core_modes(jgcm, configs, days_done)
+            extra["tensor_core_modes"] = {k: v for k, v in modes.items() if k != "fp32"}
             extra["ensemble"] = ensemble_bench(jgcm, configs, ["fp32", "tf32x3"])
         except Exception as e:
             extra["ensemble_error"] = str(e)
