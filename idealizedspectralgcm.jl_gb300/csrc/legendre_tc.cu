@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(256) k_s2g_tc(S2GPlan plan, Tables<float> tb, 
   if (tid == 0) bulk_load(Bhi, timg + toff[m], (uint32_t)(2 * opB), &bar[0]);
   // prologue: X[row][r] for n = m + r, split into hi / lo
   const size_t mrow = (size_t)m * (ns + 1);
-  // U items per thread per round: all their loads are issued before any shared-memory store
+  // U items per thread per pass: all their loads are issued before any shared-memory store
   constexpr int U = 4;
   for (int base = tid; base < Kp * 64; base += U * blockDim.x) {
     float2 x[U];
@@ -451,7 +451,7 @@ __global__ void __launch_bounds__(256) k_g2s_tc(G2SPlan plan, Tables<float> tb, 
     for (int chunk = 0; chunk < nch && ok; chunk++) {
       if (tid == 0) bulk_load(Bhi, img + (size_t)chunk * 2 * opB, (uint32_t)(2 * opB), &bar[0]);
       // A[row][kappa]: the folded inputs of this channel's contraction
-      constexpr int U = 8;  // items per thread per round: loads first, then the stores
+      constexpr int U = 8;  // items per thread per pass: loads first, then the stores
       for (int base = tid; base < KC * 64; base += U * blockDim.x) {
         float2 xs[U], ys[U];
 #pragma unroll
