@@ -468,6 +468,10 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "tf32x3", "bf16x3"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble and tensor-core side runs")
+    ap.add_argument("--profile", action="store_true",
+                    help="only the mixed-precision headline model: --warmup then --steps sim-days with the tiles of "
+                         "--tiles (no autotuning, no other model), a short launch sequence for ncu")
+    ap.add_argument("--tiles", default="4,4,4,0", help="lanes per column, S2G, G2S, FFT columns per block (--profile)")
     ap.add_argument("--ensemble-only", default=None, metavar="PRECISIONS",
                     help="run only the batched-ensemble measurement for these precisions (comma list, e.g. "
                          "fp32,tf32x3) over --steps days and print its JSON (for profiling the ensemble kernels)")
@@ -481,6 +485,21 @@ def main():
     try:
         if args.impl == "reference":
             return run_reference(args)
+        if args.profile:
+            import jgcm
+            from jgcm import configs
+
+            jgcm.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+            spd = configs.STEPS_PER_DAY[WORKLOAD]
+            m = configs.make_mesh(jgcm, WORKLOAD, precision=args.precision)
+            md = jgcm.Model(m, configs.PARAMS[WORKLOAD])
+            configs.init_held_suarez(jgcm, m, md)
+            jgcm.set_tuning(md, dict(zip(jgcm.TUNING_KNOBS, [int(x) for x in args.tiles.split(",")])))
+            md.step(spd * args.warmup)
+            ms = [md.time_steps(spd) for _ in range(args.steps)]
+            print(json.dumps({"profile": WORKLOAD, "precision": args.precision, "tiles": args.tiles,
+                              "ms_per_sim_day": ms}), flush=True)
+            return 0
         if args.ensemble_only:
             import jgcm
             from jgcm import configs

@@ -32,6 +32,7 @@ int d2h(jgcm_mesh* m, double* dst, const double* src, size_t n) {
 int finish(jgcm_mesh* m) {
   JG_CUDA(cudaStreamSynchronize(m->stream));
   JG_CUDA(cudaGetLastError());
+  if (m->tc.on) JG_TRY(tc_status(m));  // a tensor-core kernel whose bounded wait gave up
   return JGCM_OK;
 }
 

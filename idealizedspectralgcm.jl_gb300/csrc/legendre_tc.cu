@@ -118,9 +118,9 @@ __device__ __forceinline__ void bar_init(uint64_t* bar) {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 // bounded wait for the phase with the given parity; true when it completed
-__device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity, int max_polls = 1 << 20) {
   uint32_t done = 0;
-  for (int it = 0; it < (1 << 20) && !done; it++) {
+  for (int it = 0; it < max_polls && !done; it++) {
     asm volatile(
         "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
         : "=r"(done)
@@ -727,6 +727,19 @@ int launch_g2s_legendre_tc(jgcm_mesh* m, const G2SPlan& gp, int Cin, cudaStream_
                                      : g2s_tc<tc::BF16x3>(m, gp, Cin, st, fbuf);
 }
 
+// Self-test of the failure path: one CTA waits (with a short poll bound) on an mbarrier phase that
+// nothing completes, records the give-up in the status word exactly as the Legendre kernels do and
+// returns; no copy or MMA is in flight, so the context stays usable.
+namespace tc {
+__global__ void k_bounded_wait_selftest(unsigned* status) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    bar_init(&bar);
+    if (!bar_wait(&bar, 0, 4096)) atomicOr(status, ST_TABLE_WAIT);  // phase 0 never completes
+  }
+}
+}  // namespace tc
+
 int tc_status(jgcm_mesh* m) {
   unsigned s = 0;
   JG_CUDA(cudaMemcpy(&s, m->d_status, sizeof(s), cudaMemcpyDeviceToHost));
@@ -740,3 +753,11 @@ int tc_status(jgcm_mesh* m) {
 }
 
 }  // namespace jgcm
+
+extern "C" int jgcm_selftest_bounded_wait(jgcm_mesh* m) {
+  JG_ARG(m, "mesh is NULL");
+  jgcm::tc::k_bounded_wait_selftest<<<1, 32, 0, m->stream>>>(m->d_status);
+  JG_CUDA(cudaGetLastError());
+  JG_CUDA(cudaStreamSynchronize(m->stream));
+  return jgcm::tc_status(m);
+}

@@ -1662,6 +1662,7 @@ extern "C" int jgcm_model_step(jgcm_model* md, int nsteps) {
   JG_ARG(md && nsteps >= 0, "bad arguments");
   for (int s = 0; s < nsteps; s++) JG_TRY(model_step(md));
   JG_CUDA(cudaStreamSynchronize(md->mesh->stream));
+  if (md->mesh->tc.on) JG_TRY(tc_status(md->mesh));  // a tensor-core kernel whose bounded wait gave up
   return JGCM_OK;
 }
 

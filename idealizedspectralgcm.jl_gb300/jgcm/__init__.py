@@ -109,6 +109,7 @@ def lib():
         "jgcm_model_kernel_times": (I, [P, I, C.POINTER(C.c_float), I, C.POINTER(I)]),
         "jgcm_model_kernel_name": (I, [P, I, C.c_char_p, I]),
         "jgcm_set_device": (I, [I]),
+        "jgcm_selftest_bounded_wait": (I, [P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

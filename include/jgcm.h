@@ -227,6 +227,11 @@ int jgcm_model_kernel_times(jgcm_model* model, int nsteps, float* ms, int cap, i
 int jgcm_model_kernel_name(jgcm_model* model, int slot, char* buf, int cap);
 /* Select the CUDA device used by subsequently created meshes on this thread. */
 int jgcm_set_device(int device);
+/* Failure-path self-test (no counterpart in the reference): a kernel waits, with a short poll
+ * bound, on a barrier phase nothing completes, sets the mesh's status bit and
+ * returns; the call then reports it like a Legendre kernel that gave up (JGCM_E_CUDA with a message)
+ * and clears it.  The mesh stays usable. */
+int jgcm_selftest_bounded_wait(jgcm_mesh* mesh);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop
