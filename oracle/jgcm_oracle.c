@@ -667,3 +667,4 @@ void om_trans_grid_to_spherical_adjoint(om_mesh* M, const double* sbar, int nlev
     }
 }
 
+#include "jgcm_oracle_adjoint.inc"

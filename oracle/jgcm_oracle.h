@@ -104,6 +104,24 @@ int om_spectral_initialize_fields(om_model* md, const double* grid_t_pert, int v
 /* Semi_Implicit.jl: copy out "div_mat" (nd*nd), "h" (nd), "wave_matrix" (nd*nd*(N+1)) */
 long om_model_semi_implicit(om_model* md, const char* name, double* out, long cap);
 
+/* ---- reverse mode (the reference has none; test infrastructure for the adjoint kernels) ---- */
+/* pressure variables of grid_ps_c (call after setting grid_ps_c by om_model_field) */
+void om_model_sync_pressure(om_model* md);
+/* set the init-step flag and rebuild the wave matrices for it */
+int om_model_set_init_step(om_model* md, int flag);
+/* adjoints of Vor_Div_From_Grid_UV!, UV_Grid_From_Vor_Div!, Compute_Gradients! (outputs overwritten) */
+void om_vor_div_from_grid_uv_adjoint(om_mesh* m, const double* vor_bar, const double* div_bar, int nlev,
+                                     double* u_bar, double* v_bar);
+void om_uv_grid_from_vor_div_adjoint(om_mesh* m, const double* u_bar, const double* v_bar, int nlev,
+                                     double* vor_bar, double* div_bar);
+void om_compute_gradients_adjoint(om_mesh* m, const double* dlam_bar, const double* dth_bar, int nlev,
+                                  double* hs_bar);
+/* adjoint of one Held-Suarez step from the model's state X_s: xbar[18] (cotangents of X_{s+1} in,
+ * of X_s out; order spe_vor_c spe_vor_p spe_div_c spe_div_p spe_lnps_c spe_lnps_p spe_t_c spe_t_p
+ * grid_u_c grid_u_p grid_v_c grid_v_p grid_ps_c grid_ps_p grid_t_c grid_t_p grid_vor grid_div);
+ * pbar[5] += cotangents of k_f, k_a, k_s, dT_y, dtheta_z */
+int om_hs_step_adjoint(om_model* md, double* const* xbar, double* pbar);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,7 +25,7 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libjgcm_oracle.so")
-_SOURCES = ["jgcm_oracle.c", "jgcm_oracle_models.inc", "jgcm_oracle.h"]
+_SOURCES = ["jgcm_oracle.c", "jgcm_oracle_models.inc", "jgcm_oracle_adjoint.inc", "jgcm_oracle.h"]
 
 
 def build(force: bool = False) -> str:
@@ -78,6 +78,12 @@ def lib():
             "om_semi_implicit_step": (None, [P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
             "om_trans_spherical_to_grid_adjoint": (None, [P, P, I, P]),
             "om_trans_grid_to_spherical_adjoint": (None, [P, P, I, P]),
+            "om_model_sync_pressure": (None, [P]),
+            "om_model_set_init_step": (I, [P, I]),
+            "om_vor_div_from_grid_uv_adjoint": (None, [P, P, P, I, P, P]),
+            "om_uv_grid_from_vor_div_adjoint": (None, [P, P, P, I, P, P]),
+            "om_compute_gradients_adjoint": (None, [P, P, P, I, P]),
+            "om_hs_step_adjoint": (I, [P, C.POINTER(C.c_void_p), P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(_lib, name)
@@ -337,3 +343,90 @@ def Semi_Implicit_Step(model, inputs):
     lib().om_semi_implicit_step(model._h, pin, pout)
     return dict(zip(SI_OUT, outs))
 
+
+# ---- reverse mode of the Held-Suarez step (the reference has none) --------------------------------
+STATE_FIELDS = ("spe_vor_c", "spe_vor_p", "spe_div_c", "spe_div_p", "spe_lnps_c", "spe_lnps_p", "spe_t_c",
+                "spe_t_p", "grid_u_c", "grid_u_p", "grid_v_c", "grid_v_p", "grid_ps_c", "grid_ps_p", "grid_t_c",
+                "grid_t_p", "grid_vor", "grid_div")
+HS_PARAMS = ("k_f", "k_a", "k_s", "dT_y", "dtheta_z")
+
+
+def get_state(model):
+    """The 18 fields one Held-Suarez step reads and writes, with the init-step flag."""
+    return {k: model.get(k) for k in STATE_FIELDS}, model.init_step
+
+
+def set_state(model, state):
+    fields, init = state
+    for k in STATE_FIELDS:
+        model.set(k, fields[k])
+    lib().om_model_sync_pressure(model._h)
+    if model.init_step != init:
+        lib().om_model_set_init_step(model._h, int(init))
+
+
+def set_init_step(model, flag):
+    lib().om_model_set_init_step(model._h, int(flag))
+
+
+def HS_Step_Adjoint(model, xbar, pbar=None):
+    """Cotangents of X_{s+1} (dict over STATE_FIELDS) -> cotangents of X_s (the model's state) and
+    of the HS parameters (array over HS_PARAMS, accumulated into `pbar`)."""
+    arrs = [np.array(xbar[k], dtype=model.get(k).dtype, order="F", copy=True) for k in STATE_FIELDS]
+    pb = np.zeros(5) if pbar is None else pbar
+    ptrs = (C.c_void_p * 18)(*[a.ctypes.data for a in arrs])
+    assert lib().om_hs_step_adjoint(model._h, ptrs, _ptr(pb)) == 0
+    return dict(zip(STATE_FIELDS, arrs)), pb
+
+
+def Vor_Div_From_Grid_UV_Adjoint(mesh, vor_bar, div_bar, u_bar, v_bar):
+    n = _nlev_spec(mesh, vor_bar)
+    lib().om_vor_div_from_grid_uv_adjoint(mesh._h, _ptr(np.asfortranarray(vor_bar)), _ptr(np.asfortranarray(div_bar)),
+                                          n, _ptr(u_bar), _ptr(v_bar))
+
+
+def UV_Grid_From_Vor_Div_Adjoint(mesh, u_bar, v_bar, vor_bar, div_bar):
+    n = _nlev_grid(mesh, u_bar)
+    lib().om_uv_grid_from_vor_div_adjoint(mesh._h, _ptr(np.asfortranarray(u_bar)), _ptr(np.asfortranarray(v_bar)),
+                                          n, _ptr(vor_bar), _ptr(div_bar))
+
+
+def Compute_Gradients_Adjoint(mesh, dlam_bar, dth_bar, hs_bar):
+    n = _nlev_grid(mesh, dlam_bar)
+    lib().om_compute_gradients_adjoint(mesh._h, _ptr(np.asfortranarray(dlam_bar)), _ptr(np.asfortranarray(dth_bar)),
+                                       n, _ptr(hs_bar))
+
+
+def hs_loss(mesh, grid_t, t_target):
+    """sum_{i,j,k} w_j (T - T_target)^2 / (2 nlon nd): the area-weighted mean squared difference
+    (sum_j w_j = 2), and its gradient with respect to grid T."""
+    w = mesh.wts[None, :, None]
+    d = grid_t - t_target
+    norm = 2.0 * mesh.nlon * grid_t.shape[2]
+    return float(np.sum(w * d * d) / norm), np.asfortranarray(2.0 * w * d / norm)
+
+
+def HS_Gradient(model, nsteps, t_target):
+    """Loss of the grid temperature after `nsteps` Held-Suarez steps from the model's state, and its
+    gradient with respect to the initial spectral temperature T0 (the state's spe_t_c = spe_t_p = T0,
+    grid_t_c = grid_t_p = S2G(T0), as Spectral_Initialize_Fields! leaves them) and the five HS
+    parameters, by the step adjoint over all steps (every state kept: the CPU check needs no
+    checkpointing).  The model is left at the final state."""
+    states = []
+    for _ in range(nsteps):
+        states.append(get_state(model))
+        model.step(1)
+    loss, tbar = hs_loss(model.mesh, model.get("grid_t_c"), t_target)
+    final = get_state(model)
+    xbar = {k: np.zeros_like(v) for k, v in final[0].items()}
+    xbar["grid_t_c"] = tbar
+    pbar = np.zeros(5)
+    for st in reversed(states):
+        set_state(model, st)
+        xbar, pbar = HS_Step_Adjoint(model, xbar, pbar)
+    set_state(model, final)
+    m = model.mesh
+    g = np.asfortranarray(xbar["grid_t_c"] + xbar["grid_t_p"])
+    s = m.spectral(m.nd)
+    Trans_Spherical_To_Grid_Adjoint(m, g, s)
+    return loss, np.asfortranarray(xbar["spe_t_c"] + xbar["spe_t_p"] + s), pbar
