@@ -246,6 +246,9 @@ int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp, cudaStream_t 
                int cap = 0);
 template <typename T>
 int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp, cudaStream_t st, void* fbuf = nullptr, int cap = 0);
+// the inverse FFT of Fourier coefficients already staged in fbuf ((N+1) x nlat x ip.C)
+template <typename T>
+int launch_ifft_only(jgcm_mesh* m, const IFFTPlan& ip, cudaStream_t st, void* fbuf = nullptr, int cap = 0);
 int spec_host_to_dev(jgcm_mesh* m, const double* d_host_layout, void* d_native, int L, cudaStream_t st);
 int spec_dev_to_host(jgcm_mesh* m, const void* d_native, double* d_host_layout, int L, cudaStream_t st);
 int grid_host_to_dev(jgcm_mesh* m, const double* d_src, void* d_native, size_t n, cudaStream_t st);

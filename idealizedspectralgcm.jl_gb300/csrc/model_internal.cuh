@@ -1,0 +1,85 @@
+// model_internal.cuh -- the device-resident model (Dyn_Data + Semi_Implicit_Solver state) shared by
+// the time stepping (models.cu) and the reverse sweep (hs_adjoint.cu).
+#pragma once
+#include "jgcm_internal.cuh"
+
+namespace jgcm {
+constexpr unsigned FULL = 0xffffffffu;
+constexpr double kLnPsRef = 11.512925464970229;  // ln 1e5
+
+struct VertCoef {  // Vert_Coordinate (even_sigma) and the semi-implicit reference column
+  double ak[JGCM_MAX_ND + 1], bk[JGCM_MAX_ND + 1], dak[JGCM_MAX_ND], dbk[JGCM_MAX_ND];
+  double dp_ref[JGCM_MAX_ND], rdp_ref[JGCM_MAX_ND], lnph_ref[JGCM_MAX_ND + 1], lnpf_ref[JGCM_MAX_ND],
+      t_ref[JGCM_MAX_ND], h[JGCM_MAX_ND];
+  // sigma coordinates (a_k = 0): with p = b ps, ln p_{k+1/2} = lb[k+1] + ln ps and
+  // ln p_k = cf[k] + ln ps (Simmons-Burridge, Press_And_Geopot.jl:46-60, zero top), so every
+  // log-pressure difference is a per-level constant and p_k = sf[k] ps
+  double lb[JGCM_MAX_ND + 1];  // ln b_k (k >= 1)
+  double cf[JGCM_MAX_ND];      // ln p_k - ln ps
+  double sf[JGCM_MAX_ND];      // exp(cf) = p_k / ps
+  double dlp_p[JGCM_MAX_ND];   // ln p_{k+1/2} - ln p_k
+  double dlp_m[JGCM_MAX_ND];   // ln p_k - ln p_{k-1/2}   (k >= 1)
+  double dlp[JGCM_MAX_ND];     // ln p_{k+1/2} - ln p_{k-1/2}   (k >= 1)
+};
+}  // namespace jgcm
+
+struct jgcm_model {
+  jgcm_mesh* mesh;
+  jgcm_params P;
+  int nd, init_step, rot, sw_adv_from_n, steps_done;
+  // ensemble members advanced together: every field holds ne members, member-major (grid level
+  // index e*nd + k, spectral innermost index e*nd + k), so a transform sees L = ne*nd columns
+  int ne, L;
+  void* fbuf;  // Fourier buffer of fcap columns
+  int fcap;
+  int hs_lanes;  // lanes per column of the Held-Suarez column kernel (1, 2 or 4)
+  int graph_gen;  // the mesh's tile generation the captured graphs were built with
+  // Held-Suarez: the gradients of ln ps and T of the current level are already in g_dlps ...
+  // g_dtT (computed at the end of the previous step, concurrently with the fixers)
+  int grad_ready;
+  cudaStream_t side;        // second branch of a step (the gradients next to the fixers)
+  cudaEvent_t ev_fork, ev_join;
+  // on-device diagnostics (Output_Manager.jl:81-107): FP64 sums after every step of the zonal means
+  // of T, T_eq, u, v ([4][ne][nd][nlat]) and of ps ([ne][nlat][nlon]), and the number of steps summed
+  double* diag;
+  int diag_on;
+  long diag_steps;
+  double cp_air;
+  // time-levelled state (index by rotation)
+  void *spe_vor[3], *spe_div[3], *spe_lnps[3], *spe_t[3];
+  void *grid_u[3], *grid_v[3], *grid_ps[3], *grid_t[3];
+  // single-level state and diagnostics
+  void *grid_vor, *grid_div, *grid_lnps, *grid_t_eq, *grid_geopots, *grid_h_eq, *spe_zero;
+  // tendencies and scratch
+  void *spe_dvor, *spe_ddiv, *spe_dlnps, *spe_dt;
+  void *g_dlps, *g_dtps, *g_dlT, *g_dtT, *g_ducos, *g_dvcos, *g_dt, *g_energy, *g_dlnps, *g_diag;
+  void *coriolis, *damping;  // [nlat], [m][n] in T
+  void* dfac[2];             // [m][n] in T: 1/(1 + Δt d) (init step), 1/(1 + 2Δt d) (afterwards)
+  // FP64 semi-implicit data
+  jgcm::VertCoef vc;
+  jgcm::VertCoef* d_vc;  // device copy read by the column and semi-implicit kernels
+  double* div_mat;  // host nd*nd column-major
+  double* d_W;      // device [2][N+1][nd][nd] (transposed: [c][r])
+  int2* d_pairs;    // (m, n) pairs with n >= m
+  int npairs;
+  double *d_partials, *d_scalars;
+  unsigned* d_counter;
+  cudaGraphExec_t graph[3];
+  cudaEvent_t ev0, ev1;
+};
+
+
+namespace jgcm {
+inline int lvl(const jgcm_model* md, int which) { return (md->rot + which) % 3; }  // 0 = p, 1 = c, 2 = n
+
+// models.cu services used by the reverse sweep
+int dev_alloc(void** p, size_t bytes);  // cudaMalloc + zero fill
+int hs_grad(jgcm_model* md, int lev, cudaStream_t st);  // gradients of ln ps and T of level `lev`
+// transposed semi-implicit step (Semi_Implicit.jl:360-513 + Time_Integrator.jl:58-101) on device
+// buffers: obar[8] = cotangents of vor_n, vor_c', div_n, div_c', T_n, T_c', lnps_n, lnps_c';
+// ibar[12] = cotangents of dvor, ddiv, dT, dlnps, vor_p, vor_c, div_p, div_c, T_p, T_c, lnps_p,
+// lnps_c (written for n >= m); `mats` from si_adjoint_mats (freed by the caller with cudaFree)
+int si_adjoint_mats(jgcm_model* md, double** mats);
+int si_adjoint_launch(jgcm_model* md, const void* const* obar, void* const* ibar, const double* mats,
+                      cudaStream_t st);
+}  // namespace jgcm

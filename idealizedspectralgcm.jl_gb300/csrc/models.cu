@@ -22,78 +22,14 @@
 
 using namespace jgcm;
 
-namespace {
-constexpr unsigned FULL = 0xffffffffu;
+#include "model_internal.cuh"
 
+namespace {
 template <typename T>
 using V2 = typename C2<T>::t;
-
-struct VertCoef {  // Vert_Coordinate (even_sigma) and the semi-implicit reference column
-  double ak[JGCM_MAX_ND + 1], bk[JGCM_MAX_ND + 1], dak[JGCM_MAX_ND], dbk[JGCM_MAX_ND];
-  double dp_ref[JGCM_MAX_ND], rdp_ref[JGCM_MAX_ND], lnph_ref[JGCM_MAX_ND + 1], lnpf_ref[JGCM_MAX_ND],
-      t_ref[JGCM_MAX_ND], h[JGCM_MAX_ND];
-  // sigma coordinates (a_k = 0): with p = b ps, ln p_{k+1/2} = lb[k+1] + ln ps and
-  // ln p_k = cf[k] + ln ps (Simmons-Burridge, Press_And_Geopot.jl:46-60, zero top), so every
-  // log-pressure difference is a per-level constant and p_k = sf[k] ps
-  double lb[JGCM_MAX_ND + 1];  // ln b_k (k >= 1)
-  double cf[JGCM_MAX_ND];      // ln p_k - ln ps
-  double sf[JGCM_MAX_ND];      // exp(cf) = p_k / ps
-  double dlp_p[JGCM_MAX_ND];   // ln p_{k+1/2} - ln p_k
-  double dlp_m[JGCM_MAX_ND];   // ln p_k - ln p_{k-1/2}   (k >= 1)
-  double dlp[JGCM_MAX_ND];     // ln p_{k+1/2} - ln p_{k-1/2}   (k >= 1)
-};
 }  // namespace
 
-struct jgcm_model {
-  jgcm_mesh* mesh;
-  jgcm_params P;
-  int nd, init_step, rot, sw_adv_from_n, steps_done;
-  // ensemble members advanced together: every field holds ne members, member-major (grid level
-  // index e*nd + k, spectral innermost index e*nd + k), so a transform sees L = ne*nd columns
-  int ne, L;
-  void* fbuf;  // Fourier buffer of fcap columns
-  int fcap;
-  int hs_lanes;  // lanes per column of the Held-Suarez column kernel (1, 2 or 4)
-  int graph_gen;  // the mesh's tile generation the captured graphs were built with
-  // Held-Suarez: the gradients of ln ps and T of the current level are already in g_dlps ...
-  // g_dtT (computed at the end of the previous step, concurrently with the fixers)
-  int grad_ready;
-  cudaStream_t side;        // second branch of a step (the gradients next to the fixers)
-  cudaEvent_t ev_fork, ev_join;
-  // on-device diagnostics (Output_Manager.jl:81-107): FP64 sums after every step of the zonal means
-  // of T, T_eq, u, v ([4][ne][nd][nlat]) and of ps ([ne][nlat][nlon]), and the number of steps summed
-  double* diag;
-  int diag_on;
-  long diag_steps;
-  double cp_air;
-  // time-levelled state (index by rotation)
-  void *spe_vor[3], *spe_div[3], *spe_lnps[3], *spe_t[3];
-  void *grid_u[3], *grid_v[3], *grid_ps[3], *grid_t[3];
-  // single-level state and diagnostics
-  void *grid_vor, *grid_div, *grid_lnps, *grid_t_eq, *grid_geopots, *grid_h_eq, *spe_zero;
-  // tendencies and scratch
-  void *spe_dvor, *spe_ddiv, *spe_dlnps, *spe_dt;
-  void *g_dlps, *g_dtps, *g_dlT, *g_dtT, *g_ducos, *g_dvcos, *g_dt, *g_energy, *g_dlnps, *g_diag;
-  void *coriolis, *damping;  // [nlat], [m][n] in T
-  void* dfac[2];             // [m][n] in T: 1/(1 + Δt d) (init step), 1/(1 + 2Δt d) (afterwards)
-  // FP64 semi-implicit data
-  VertCoef vc;
-  VertCoef* d_vc;  // device copy read by the column and semi-implicit kernels
-  double* div_mat;  // host nd*nd column-major
-  double* d_W;      // device [2][N+1][nd][nd] (transposed: [c][r])
-  int2* d_pairs;    // (m, n) pairs with n >= m
-  int npairs;
-  double *d_partials, *d_scalars;
-  unsigned* d_counter;
-  cudaGraphExec_t graph[3];
-  cudaEvent_t ev0, ev1;
-};
-
 namespace {
-
-int lvl(const jgcm_model* md, int which) { return (md->rot + which) % 3; }  // 0 = p, 1 = c, 2 = n
-
-constexpr double kLnPsRef = 11.512925464970229;  // ln 1e5
 
 // ------------------------------------------------------------------------------------------
 // warp scans over levels (lanes >= nd hold zero)
@@ -1672,6 +1608,16 @@ extern "C" int jgcm_model_init_step(jgcm_model* md, int* init_step) {
   return JGCM_OK;
 }
 
+// Sets the init-step flag (Get_Δt: Δt on the first step, 2Δt afterwards): restarting a run from a
+// stored first state.  The device holds the wave matrices of both flags.
+extern "C" int jgcm_model_set_init_step(jgcm_model* md, int init_step) {
+  JG_ARG(md, "NULL model");
+  JG_CUDA(cudaStreamSynchronize(md->mesh->stream));
+  md->init_step = init_step != 0;
+  md->grad_ready = 0;
+  return JGCM_OK;
+}
+
 extern "C" int jgcm_model_update_init_step(jgcm_model* md) {
   JG_ARG(md, "NULL argument");
   JG_ARG(md->init_step, "Update_Init_Step!: the model is not in its init step (@assert(integrator.init_step))");
@@ -2671,6 +2617,62 @@ ImplArgs<T> si_args(jgcm_model* md, void* const* in, void* const* out) {
   return ia;
 }
 }  // namespace
+
+namespace jgcm {
+int dev_alloc(void** p, size_t bytes) { return alloc(p, bytes); }
+
+int hs_grad(jgcm_model* md, int lev, cudaStream_t st) {
+  return is_fp64(md->mesh) ? issue_hs_grad<double>(md, lev, st) : issue_hs_grad<float>(md, lev, st);
+}
+
+int si_adjoint_mats(jgcm_model* md, double** mats) {
+  AdjMats am;
+  JG_TRY(adj_mats(md, &am));
+  *mats = am.Apt;  // one allocation: Apt, Ageo, spt, hk
+  return JGCM_OK;
+}
+
+int si_adjoint_launch(jgcm_model* md, const void* const* obar, void* const* ibar, const double* mats,
+                      cudaStream_t st) {
+  jgcm_mesh* m = md->mesh;
+  const int nd = md->nd;
+  auto launch = [&](auto tag) {
+    using T = decltype(tag);
+    using V = V2<T>;
+    AdjArgs<T> a;
+    memset(&a, 0, sizeof(a));
+    a.vn_b = (const V*)obar[0]; a.vc_b = (const V*)obar[1]; a.dn_b = (const V*)obar[2]; a.dc_b = (const V*)obar[3];
+    a.tn_b = (const V*)obar[4]; a.tc_b = (const V*)obar[5]; a.ln_b = (const V*)obar[6]; a.lc_b = (const V*)obar[7];
+    a.dvor_b = (V*)ibar[0]; a.ddiv_b = (V*)ibar[1]; a.dt_b = (V*)ibar[2]; a.dl_b = (V*)ibar[3];
+    a.vp_b = (V*)ibar[4]; a.vcin_b = (V*)ibar[5]; a.dp_b = (V*)ibar[6]; a.dcin_b = (V*)ibar[7];
+    a.tp_b = (V*)ibar[8]; a.tcin_b = (V*)ibar[9]; a.lp_b = (V*)ibar[10]; a.lcin_b = (V*)ibar[11];
+    a.damping = (const T*)md->damping;
+    a.dfac = (const T*)md->dfac[md->init_step ? 0 : 1];
+    a.eig64 = m->t64.eig;
+    a.W = md->d_W + (md->init_step ? 0 : (size_t)(m->N + 1) * nd * nd);
+    a.Apt = mats;
+    a.Ageo = mats + (size_t)nd * nd;
+    a.spt = mats + 2 * (size_t)nd * nd;
+    a.hk = a.spt + nd;
+    a.pairs = md->d_pairs;
+    a.npairs = md->npairs;
+    a.nd = nd;
+    a.ns = m->ns;
+    a.N = m->N;
+    a.init_step = md->init_step;
+    a.dt = md->P.dt;
+    a.xi = md->init_step ? md->P.dt * md->P.implicit_coef : (2 * md->P.dt) * md->P.implicit_coef;
+    a.ps_ref = md->P.ps_ref;
+    a.robert = md->P.robert_coef;
+    k_hs_implicit_adjoint<T><<<(md->npairs + 7) / 8, 256, 0, st>>>(a);
+  };
+  if (is_fp64(m)) launch(double());
+  else launch(float());
+  mark(st);
+  JG_CUDA(cudaGetLastError());
+  return JGCM_OK;
+}
+}  // namespace jgcm
 
 extern "C" int jgcm_model_semi_implicit_step(jgcm_model* md, const double* const* in, double* const* out) {
   JG_ARG(md && in && out, "NULL argument");

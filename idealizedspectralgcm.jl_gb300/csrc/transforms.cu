@@ -677,6 +677,9 @@ static inline int fft_ct(const jgcm_mesh* m) {
   return m->tune[3] > 0 ? m->tune[3] : m->nlon >= 1024 ? 1 : 1024 / m->nlon;
 }
 
+template <typename T>
+static int launch_ifft_stage(jgcm_mesh* m, const IFFTPlan& ip, cudaStream_t st, V2<T>* fbuf);
+
 // Legendre synthesis then inverse FFT, with the Fourier coefficients staged in `fbuf`
 // ((N+1) x nlat x C complex T).
 template <typename T>
@@ -694,6 +697,14 @@ static int launch_s2g_into(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, 
     mark(st);
     JG_CUDA(cudaGetLastError());
   }
+  return launch_ifft_stage<T>(m, ip, st, fbuf);
+}
+
+// The inverse FFT stage alone (Fourier coefficients already in `fbuf`).
+template <typename T>
+static int launch_ifft_stage(jgcm_mesh* m, const IFFTPlan& ip, cudaStream_t st, V2<T>* fbuf) {
+  using V = V2<T>;
+  Tables<T> tb = tables<T>(m);
   const int fc = fft_ct(m);
   // the warp-register FFT wins in FP32; in FP64 the shared-memory radix-2 kernel is faster (measured)
   if (std::is_same<T, float>::value && m->nlon >= 64 && m->nlon <= 1024 && m->tune[3] == 0) {
@@ -726,6 +737,17 @@ int launch_s2g(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, cudaStream_t
   }
   JG_ARG(sp.C == ip.C && sp.C <= cap && sp.C > 0, "bad S2G plan");
   return launch_s2g_into<T>(m, sp, ip, st, (V2<T>*)fbuf);
+}
+
+template <typename T>
+int launch_ifft_only(jgcm_mesh* m, const IFFTPlan& ip, cudaStream_t st, void* fbuf, int cap) {
+  JG_TRY(configure_smem<T>());
+  if (!fbuf) {
+    fbuf = m->d_fbuf;
+    cap = m->Cmax;
+  }
+  JG_ARG(ip.C <= cap && ip.C > 0, "bad inverse FFT plan");
+  return launch_ifft_stage<T>(m, ip, st, (V2<T>*)fbuf);
 }
 
 template <typename T>
@@ -790,6 +812,8 @@ template int launch_s2g<float>(jgcm_mesh*, const S2GPlan&, const IFFTPlan&, cuda
 template int launch_s2g<double>(jgcm_mesh*, const S2GPlan&, const IFFTPlan&, cudaStream_t, void*, int);
 template int launch_g2s<float>(jgcm_mesh*, const FFTPlan&, const G2SPlan&, cudaStream_t, void*, int);
 template int launch_g2s<double>(jgcm_mesh*, const FFTPlan&, const G2SPlan&, cudaStream_t, void*, int);
+template int launch_ifft_only<float>(jgcm_mesh*, const IFFTPlan&, cudaStream_t, void*, int);
+template int launch_ifft_only<double>(jgcm_mesh*, const IFFTPlan&, cudaStream_t, void*, int);
 template int launch_fft_only<float>(jgcm_mesh*, const FFTPlan&, cudaStream_t, void*, int);
 template int launch_fft_only<double>(jgcm_mesh*, const FFTPlan&, cudaStream_t, void*, int);
 

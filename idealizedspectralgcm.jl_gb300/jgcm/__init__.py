@@ -86,6 +86,8 @@ def lib():
         "jgcm_model_copy_member": (I, [P, I, P, I]),
         "jgcm_model_semi_implicit_step": (I, [P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
         "jgcm_model_semi_implicit_step_adjoint": (I, [P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+        "jgcm_model_step_adjoint": (I, [P, C.POINTER(C.c_void_p), P]),
+        "jgcm_model_hs_gradient": (I, [P, I, I, P, P, P, P]),
         "jgcm_model_diagnostics": (I, [P, I]),
         "jgcm_model_read_diagnostics": (I, [P, C.c_char_p, P, Lg, C.POINTER(Lg), C.POINTER(Lg)]),
         "jgcm_model_get_tuning": (I, [P, C.POINTER(I), I]),
@@ -101,6 +103,7 @@ def lib():
         "jgcm_model_step": (I, [P, I]),
         "jgcm_model_init_step": (I, [P, C.POINTER(I)]),
         "jgcm_model_update_init_step": (I, [P]),
+        "jgcm_model_set_init_step": (I, [P, I]),
         "jgcm_spectral_initialize_fields": (I, [P, P, I]),
         "jgcm_model_semi_implicit": (I, [P, C.c_char_p, P, Lg, C.POINTER(Lg)]),
         "jgcm_hs_forcing": (I, [P, I, P, P, P, P, P, P, P, P, P]),
@@ -395,6 +398,10 @@ class Model:
     def step(self, nsteps=1):
         _check(lib().jgcm_model_step(self._h, int(nsteps)))
 
+    def set_init_step(self, flag=True):
+        """Make the next step a first step (Δt) or a leapfrog step (2Δt)."""
+        _check(lib().jgcm_model_set_init_step(self._h, int(bool(flag))))
+
     def update_init_step(self):
         """Update_Init_Step! (Time_Integrator.jl:40-43): leave the forward init-step mode."""
         _check(lib().jgcm_model_update_init_step(self._h))
@@ -564,4 +571,48 @@ def Semi_Implicit_Step_Adjoint(model, out_bar):
     pib = (C.c_void_p * 12)(*[a.ctypes.data for a in ibs])
     _check(lib().jgcm_model_semi_implicit_step_adjoint(model._h, pob, pib))
     return dict(zip(SI_IN, ibs))
+
+
+# ---- reverse mode of the Held-Suarez step -------------------------------------------------------
+STATE_FIELDS = ("spe_vor_c", "spe_vor_p", "spe_div_c", "spe_div_p", "spe_lnps_c", "spe_lnps_p", "spe_t_c",
+                "spe_t_p", "grid_u_c", "grid_u_p", "grid_v_c", "grid_v_p", "grid_ps_c", "grid_ps_p", "grid_t_c",
+                "grid_t_p", "grid_vor", "grid_div")
+HS_PARAMS = ("k_f", "k_a", "k_s", "dT_y", "dtheta_z")
+
+
+def HS_Step_Adjoint(model, xbar, pbar=None):
+    """Adjoint of one Held-Suarez step from the model's current state X_s: cotangents of X_{s+1}
+    (dict over STATE_FIELDS, reference layout) -> cotangents of X_s, and the cotangents of the
+    HS parameters (HS_PARAMS order) accumulated into ``pbar``.  The model stays at X_s."""
+    m = model.mesh
+    arrs = []
+    for k in STATE_FIELDS:
+        nlev = 1 if k in ("spe_lnps_c", "spe_lnps_p", "grid_ps_c", "grid_ps_p") else m.nd
+        if k.startswith("spe_"):
+            a = np.array(xbar[k], dtype=np.complex128, order="F", copy=True).reshape(
+                (m.num_fourier + 1, m.num_spherical + 1, nlev), order="F")
+        else:
+            a = np.array(xbar[k], dtype=np.float64, order="F", copy=True).reshape((m.nlon, m.nlat, nlev), order="F")
+        arrs.append(np.asfortranarray(a))
+    pb = np.zeros(5) if pbar is None else pbar
+    ptrs = (C.c_void_p * 18)(*[a.ctypes.data for a in arrs])
+    _check(lib().jgcm_model_step_adjoint(model._h, ptrs, _ptr(pb)))
+    return dict(zip(STATE_FIELDS, arrs)), pb
+
+
+def HS_Gradient(model, nsteps, t_target, checkpoint_every=8):
+    """Loss sum w_j (T - t_target)^2 / (2 nlon nd) of the grid temperature after ``nsteps`` steps from
+    the model's state, with its gradient with respect to the initial spectral temperature (array
+    [N+1, N+2, nd]) and the HS parameters (HS_PARAMS order): the discrete adjoint run backwards
+    with a recomputation checkpoint every ``checkpoint_every`` steps.  The model ends at the final
+    state."""
+    m = model.mesh
+    tgt = np.asfortranarray(t_target, dtype=np.float64)
+    assert tgt.shape == (m.nlon, m.nlat, m.nd)
+    loss = C.c_double()
+    g = m.spectral(m.nd)
+    gp = np.zeros(5)
+    _check(lib().jgcm_model_hs_gradient(model._h, int(nsteps), int(checkpoint_every), _ptr(tgt), C.byref(loss),
+                                        _ptr(g), _ptr(gp)))
+    return loss.value, g, gp
 

@@ -161,6 +161,24 @@ int jgcm_model_copy_member(jgcm_model* dst, int dst_member, jgcm_model* src, int
  * arrays [N+1, N+2, nd] (lnps: 1 level).  The adjoint maps cotangents of out to cotangents of in. */
 int jgcm_model_semi_implicit_step(jgcm_model* model, const double* const* in, double* const* out);
 int jgcm_model_semi_implicit_step_adjoint(jgcm_model* model, const double* const* out_bar, double* const* in_bar);
+/* Reverse mode of one whole Held-Suarez step (Atmosphere_Update!, Spectral_Dynamics.jl:206-365 +
+ * 452-490 with HS_Forcing.jl and Compute_Corrections!; no counterpart in the reference) from the
+ * model's current state X_s.  state_bar[18] holds host arrays (reference layout) of the cotangents
+ * of X_{s+1} on entry and receives those of X_s, in the order spe_vor_c, spe_vor_p, spe_div_c,
+ * spe_div_p, spe_lnps_c, spe_lnps_p, spe_t_c, spe_t_p, grid_u_c, grid_u_p, grid_v_c, grid_v_p,
+ * grid_ps_c, grid_ps_p, grid_t_c, grid_t_p, grid_vor, grid_div; param_bar[5] (nullable) is
+ * incremented by the cotangents of k_f, k_a, k_s, dT_y, dtheta_z.  The model is left at X_s.
+ * One-member models, nd <= 32, diagnostics off. */
+int jgcm_model_step_adjoint(jgcm_model* model, double* const* state_bar, double* param_bar);
+/* Loss J = sum_{i,j,k} w_j (T - t_target)^2 / (2 nlon nd) of the grid temperature after nsteps
+ * steps from the model's current state, and its gradient with respect to the initial spectral
+ * temperature T0 (the state's spe_t_c = spe_t_p = T0 and grid_t_c = grid_t_p = S2G(T0), as
+ * Spectral_Initialize_Fields! leaves them; host array [N+1, N+2, nd]) and to k_f, k_a, k_s, dT_y,
+ * dtheta_z (grad_params[5]).  The reverse sweep recomputes each segment of checkpoint_every steps
+ * from its stored state.  t_target: host grid [nlon, nlat, nd].  Outputs are nullable.  The
+ * model is left at the final state. */
+int jgcm_model_hs_gradient(jgcm_model* model, int nsteps, int checkpoint_every, const double* t_target,
+                           double* loss, double* grad_spe_t0, double* grad_params);
 /* On-device diagnostics (Held-Suarez): the reductions of Update_Output! (Output_Manager.jl:81-107)
  * as FP64 sums after every step — zonal means of T, T_eq, u, v and the ps field.  on = 1 zeroes
  * the sums and starts; on = 0 stops.  read returns the mean over the summed steps of
@@ -202,6 +220,9 @@ int jgcm_model_init_step(jgcm_model* model, int* init_step);
 /* Update_Init_Step!  Time_Integrator.jl:40-43 / Semi_Implicit.jl:182-188: leave the forward
  * init-step mode without stepping (e.g. when restarting from a saved leapfrog state). */
 int jgcm_model_update_init_step(jgcm_model* model);
+/* Set the init-step flag (1: the next step is a first step with Δt, Time_Integrator.jl:40-56), e.g.
+ * to restart from a stored first state.  No counterpart in the reference. */
+int jgcm_model_set_init_step(jgcm_model* model, int init_step);
 /* HS_Forcing!  HS_Forcing.jl:1-130 (Rayleigh_Damping! :101-130, energy-conserving heating :21-26,
  * Newtonian_Damping! :37-97) on host arrays in the reference layout: u, v, t, p_full, du, dv,
  * t_eq, dt are [nλ,nθ,nd], p_half is [nλ,nθ,nd+1]; Δt in seconds as Get_Δt returns it.  The

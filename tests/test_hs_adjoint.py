@@ -124,3 +124,78 @@ def test_oracle_gradient_matches_finite_differences(orc):
             vals.append(orc.hs_loss(mesh, m2.get("grid_t_c"), tgt)[0])
         fd = (vals[0] - vals[1]) / (2 * h)
         assert abs(fd - gp[i]) <= 1e-6 * abs(gp[i]), (p, fd, gp[i])
+
+
+# ---- GPU ----------------------------------------------------------------------------------------
+def _gpu_twin(jg, orc, prec, fields, init):
+    gm = configs.make_mesh(jg, NAME, precision=prec)
+    gmod = jg.Model(gm, configs.PARAMS[NAME])
+    for k in orc.STATE_FIELDS:
+        gmod.set(k, fields[k])
+    if not init:
+        gmod.update_init_step()
+    return gm, gmod
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("init", [False, True])
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("fp32", 2e-4)])
+def test_gpu_step_adjoint_matches_oracle(jg, orc, init, prec, tol):
+    mesh, md = _developed_state(orc)
+    fields, _ = orc.get_state(md)
+    orc.set_state(md, (fields, init))
+    rng = np.random.default_rng(21)
+    ybar = {k: _rand_like(rng, v, 1.0 / _rms(v)) for k, v in fields.items()}
+    xb_o, pb_o = orc.HS_Step_Adjoint(md, ybar)
+    gm, gmod = _gpu_twin(jg, orc, prec, fields, init)
+    xb_g, pb_g = jg.HS_Step_Adjoint(gmod, ybar)
+    for k in orc.STATE_FIELDS:
+        err = configs.rel_l2(xb_g[k], xb_o[k])
+        assert err < tol, (k, err)
+    for i, p in enumerate(orc.HS_PARAMS):
+        assert abs(pb_g[i] - pb_o[i]) <= tol * abs(pb_o[i]) + 1e-30, (p, pb_g[i], pb_o[i])
+    # the model is left at X_s: the step adjoint again gives the same cotangents
+    xb_g2, _ = jg.HS_Step_Adjoint(gmod, ybar)
+    for k in orc.STATE_FIELDS:
+        assert configs.rel_l2(xb_g2[k], xb_g[k]) < 1e-12, k
+
+
+def _gpu_loss_t0(jg, gmod, S0, d, gd, eps, nsteps, tgt, init=True):
+    f = S0
+    for k in jg.STATE_FIELDS:
+        v = f[k]
+        if k in ("spe_t_c", "spe_t_p"):
+            v = v + eps * d
+        elif k in ("grid_t_c", "grid_t_p"):
+            v = v + eps * gd
+        gmod.set(k, np.asfortranarray(v))
+    gmod.set_init_step(init)
+    gmod.step(nsteps)
+    w = gmod.mesh.wts[None, :, None]
+    diff = gmod.get("grid_t_c") - tgt
+    return float(np.sum(w * diff * diff) / (2.0 * gmod.mesh.nlon * gmod.mesh.nd))
+
+
+@pytest.mark.gpu
+def test_gpu_gradient_matches_oracle_and_finite_differences(jg, orc):
+    """8 steps with a checkpoint every 3 (segments of 3, 3, 2), FP64: the library's gradient equals
+    the oracle's, and central differences of the library's own forward model."""
+    nsteps, ck = 8, 3
+    mesh, md, S0, tgt = _gradient_case(orc)
+    loss_o, gT_o, gp_o = orc.HS_Gradient(md, nsteps, tgt)
+    gm, gmod = _gpu_twin(jg, orc, "fp64", S0[0], True)
+    loss_g, gT_g, gp_g = jg.HS_Gradient(gmod, nsteps, tgt, checkpoint_every=ck)
+    assert abs(loss_g - loss_o) <= 1e-11 * loss_o, (loss_g, loss_o)
+    assert configs.rel_l2(gT_g, gT_o) < 1e-9, configs.rel_l2(gT_g, gT_o)
+    for i, p in enumerate(orc.HS_PARAMS):
+        assert abs(gp_g[i] - gp_o[i]) <= 1e-9 * abs(gp_o[i]), (p, gp_g[i], gp_o[i])
+    # the model was left at the final state
+    assert configs.rel_l2(gmod.get("grid_t_c"), md.get("grid_t_c")) < 1e-11
+    d = _t0_direction(mesh, orc)
+    gd = mesh.grid(mesh.nd)
+    orc.Trans_Spherical_To_Grid(mesh, d, gd)
+    eps = 1e-4
+    fd = (_gpu_loss_t0(jg, gmod, S0[0], d, gd, eps, nsteps, tgt)
+          - _gpu_loss_t0(jg, gmod, S0[0], d, gd, -eps, nsteps, tgt)) / (2 * eps)
+    ad = float(np.sum((gT_g.conj() * d).real))
+    assert abs(fd - ad) <= 1e-6 * abs(ad), (fd, ad)
