@@ -1102,7 +1102,8 @@ extern "C" int jgcm_model_step_adjoint(jgcm_model* md, double* const* state_bar,
   JG_TRY(adjoint_step_any(md, &w, &x1, &bi, &bo));
   JG_TRY(bars_d2h(md, &bo, state_bar));
   double pb[5];
-  JG_CUDA(cudaMemcpy(pb, w.pbar, sizeof(pb), cudaMemcpyDeviceToHost));
+  JG_CUDA(cudaMemcpyAsync(pb, w.pbar, sizeof(pb), cudaMemcpyDeviceToHost, st));
+  JG_CUDA(cudaStreamSynchronize(st));
   if (param_bar)
     for (int i = 0; i < 5; i++) param_bar[i] += pb[i];
   if (m->tc.on) JG_TRY(tc_status(m));
@@ -1165,7 +1166,10 @@ extern "C" int jgcm_model_hs_gradient(jgcm_model* md, int nsteps, int checkpoint
                                          m->nlon, nd, part);
     k_fold_scalar<<<1, 256, 0, st>>>(part, nbl, w.sc + SC_LOSS);
     JG_CUDA(cudaGetLastError());
-    if (loss) JG_CUDA(cudaMemcpy(loss, w.sc + SC_LOSS, 8, cudaMemcpyDeviceToHost));
+    if (loss) {  // the mesh stream does not synchronise with the legacy default stream
+      JG_CUDA(cudaMemcpyAsync(loss, w.sc + SC_LOSS, 8, cudaMemcpyDeviceToHost, st));
+      JG_CUDA(cudaStreamSynchronize(st));
+    }
   }
   // reverse sweep: each segment is recomputed from its checkpoint, then reversed step by step
   StateBuf* xin = &bi;
@@ -1219,6 +1223,15 @@ extern "C" int jgcm_model_hs_gradient(jgcm_model* md, int nsteps, int checkpoint
     JG_CUDA(cudaGetLastError());
     JG_TRY(spec_dev_to_host(m, w.nb_t, m->d_stage, nd, st));
     JG_CUDA(cudaMemcpyAsync(grad_spe_t0, m->d_stage, SLn * 8, cudaMemcpyDeviceToHost, st));
+    JG_CUDA(cudaStreamSynchronize(st));
+    // T0 lives where the analysis puts it: row N+1 zero (Trans_Grid_To_Spherical!).  That row is
+    // outside the semi-implicit solve (n > N skips W_n) and an explicit gravity-wave mode of the
+    // step grows there by orders of magnitude per step; it is not part of the control.
+    for (int k = 0; k < nd; k++)
+      for (int mm = 0; mm <= m->N; mm++) {
+        const size_t h = 2 * ((size_t)mm + (size_t)(m->N + 1) * ((size_t)m->ns + (size_t)(m->ns + 1) * k));
+        grad_spe_t0[h] = grad_spe_t0[h + 1] = 0.0;
+      }
     (void)ts;
   }
   if (grad_params) JG_CUDA(cudaMemcpyAsync(grad_params, w.pbar, 5 * 8, cudaMemcpyDeviceToHost, st));

@@ -603,7 +603,8 @@ def HS_Step_Adjoint(model, xbar, pbar=None):
 def HS_Gradient(model, nsteps, t_target, checkpoint_every=8):
     """Loss sum w_j (T - t_target)^2 / (2 nlon nd) of the grid temperature after ``nsteps`` steps from
     the model's state, with its gradient with respect to the initial spectral temperature (array
-    [N+1, N+2, nd]) and the HS parameters (HS_PARAMS order): the discrete adjoint run backwards
+    [N+1, N+2, nd]; row N+1, zero in every analysed field, is not part of the control and returns 0)
+    and the HS parameters (HS_PARAMS order): the discrete adjoint run backwards
     with a recomputation checkpoint every ``checkpoint_every`` steps.  The model ends at the final
     state."""
     m = model.mesh

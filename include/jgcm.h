@@ -173,7 +173,8 @@ int jgcm_model_step_adjoint(jgcm_model* model, double* const* state_bar, double*
 /* Loss J = sum_{i,j,k} w_j (T - t_target)^2 / (2 nlon nd) of the grid temperature after nsteps
  * steps from the model's current state, and its gradient with respect to the initial spectral
  * temperature T0 (the state's spe_t_c = spe_t_p = T0 and grid_t_c = grid_t_p = S2G(T0), as
- * Spectral_Initialize_Fields! leaves them; host array [N+1, N+2, nd]) and to k_f, k_a, k_s, dT_y,
+ * Spectral_Initialize_Fields! leaves them; host array [N+1, N+2, nd]; T0 has row N+1 = 0 like every
+ * analysis output, so that row of the gradient is returned as 0) and to k_f, k_a, k_s, dT_y,
  * dtheta_z (grad_params[5]).  The reverse sweep recomputes each segment of checkpoint_every steps
  * from its stored state.  t_target: host grid [nlon, nlat, nd].  Outputs are nullable.  The
  * model is left at the final state. */

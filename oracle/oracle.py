@@ -409,7 +409,7 @@ def hs_loss(mesh, grid_t, t_target):
 def HS_Gradient(model, nsteps, t_target):
     """Loss of the grid temperature after `nsteps` Held-Suarez steps from the model's state, and its
     gradient with respect to the initial spectral temperature T0 (the state's spe_t_c = spe_t_p = T0,
-    grid_t_c = grid_t_p = S2G(T0), as Spectral_Initialize_Fields! leaves them) and the five HS
+    grid_t_c = grid_t_p = S2G(T0), as Spectral_Initialize_Fields! leaves them, row N+1 = 0) and the five HS
     parameters, by the step adjoint over all steps (every state kept: the CPU check needs no
     checkpointing).  The model is left at the final state."""
     states = []
@@ -429,4 +429,6 @@ def HS_Gradient(model, nsteps, t_target):
     g = np.asfortranarray(xbar["grid_t_c"] + xbar["grid_t_p"])
     s = m.spectral(m.nd)
     Trans_Spherical_To_Grid_Adjoint(m, g, s)
-    return loss, np.asfortranarray(xbar["spe_t_c"] + xbar["spe_t_p"] + s), pbar
+    g = np.asfortranarray(xbar["spe_t_c"] + xbar["spe_t_p"] + s)
+    g[:, -1, :] = 0  # T0 has row N+1 = 0 (an analysis output); that row is not part of the control
+    return loss, g, pbar

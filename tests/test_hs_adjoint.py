@@ -86,6 +86,7 @@ def _t0_direction(mesh, orc_or_jg, seed=3):
         d[m, :m, :] = 0
     d[0] = d[0].real
     d /= (1.0 + np.arange(S1))[None, :, None] ** 2
+    d[:, -1, :] = 0  # row N+1: zero in every analysed field (not part of the control)
     return np.asfortranarray(d)
 
 
@@ -199,3 +200,50 @@ def test_gpu_gradient_matches_oracle_and_finite_differences(jg, orc):
           - _gpu_loss_t0(jg, gmod, S0[0], d, gd, -eps, nsteps, tgt)) / (2 * eps)
     ad = float(np.sum((gT_g.conj() * d).real))
     assert abs(fd - ad) <= 1e-6 * abs(ad), (fd, ad)
+
+
+@pytest.mark.gpu
+def test_gpu_gradient_one_day_t42l20():
+    """The configuration of the adjoint benchmark: Held-Suarez T42L20, 72 steps from the seeded
+    initial state, a checkpoint every 8.  FP64 against central differences (T0 direction and the five
+    parameters, eps 1e-4 relative); the mixed-precision gradient against the FP64 one."""
+    import jgcm
+
+    name, nsteps = "hs_t42l20", 72
+    grads = {}
+    for prec in ("fp64", "fp32"):
+        mesh = configs.make_mesh(jgcm, name, precision=prec)
+        md = jgcm.Model(mesh, configs.PARAMS[name])
+        configs.init_held_suarez(jgcm, mesh, md)
+        if prec == "fp64":
+            ref = {k: md.get(k) for k in jgcm.STATE_FIELDS}
+            tgt = np.asfortranarray(ref["grid_t_c"] + np.random.default_rng(5).standard_normal(ref["grid_t_c"].shape))
+        for k in jgcm.STATE_FIELDS:
+            md.set(k, ref[k])
+        md.set_init_step(True)
+        grads[prec] = jgcm.HS_Gradient(md, nsteps, tgt, checkpoint_every=8)
+        if prec != "fp64":
+            continue
+        loss, gT, gp = grads[prec]
+        d = _t0_direction(mesh, None)
+        gd = mesh.grid(mesh.nd)
+        jgcm.Trans_Spherical_To_Grid(mesh, d, gd)
+        eps = 1e-4
+        fd = (_gpu_loss_t0(jgcm, md, ref, d, gd, eps, nsteps, tgt)
+              - _gpu_loss_t0(jgcm, md, ref, d, gd, -eps, nsteps, tgt)) / (2 * eps)
+        ad = float(np.sum((gT.conj() * d).real))
+        assert abs(fd - ad) <= 1e-6 * abs(ad), (fd, ad)
+        for i, p in enumerate(jgcm.HS_PARAMS):
+            h = eps * configs.PARAMS[name][p]
+            vals = []
+            for sg in (1, -1):
+                P = dict(configs.PARAMS[name])
+                P[p] += sg * h
+                m2 = jgcm.Model(mesh, P)
+                vals.append(_gpu_loss_t0(jgcm, m2, ref, d, gd, 0.0, nsteps, tgt))
+            f = (vals[0] - vals[1]) / (2 * h)
+            assert abs(f - gp[i]) <= 1e-6 * abs(gp[i]), (p, f, gp[i])
+    (l64, g64, p64), (l32, g32, p32) = grads["fp64"], grads["fp32"]
+    assert abs(l32 - l64) <= 1e-4 * l64
+    assert configs.rel_l2(g32, g64) < 1e-3, configs.rel_l2(g32, g64)
+    assert np.all(np.abs(p32 - p64) <= 1e-3 * np.abs(p64))
