@@ -18,6 +18,8 @@ fp64       the FP64 GPU path on the same workload, same timing; error_vs_fp64 = 
 tiles      both timed paths run the tiles the library's autotuner picks at start-up.
 roofline   the dominant kernel of the mixed step (largest summed CUDA-event time), its algorithmic
            bytes per launch / its mean launch time, against the measured HBM copy bandwidth.
+adjoint    the one-day gradient (HS T42L20, 72 steps, checkpoint every 8) in both paths: ms per
+           gradient and the mixed gradient's error against the FP64 one.
 cpu_baseline  the FP64 C oracle (a restatement of the reference on the host) timed on a bounded sample.
 --impl reference  times that oracle on all host threads on the same workload (the reference itself is
            Julia and Julia is not installed on the GPU hosts).
@@ -330,6 +332,42 @@ def precision_modes(jgcm, configs, days, timed=("tf32x3", "bf16x3")):
     return out
 
 
+def adjoint_bench(jgcm, configs, nsteps=72, checkpoint=8):
+    """Gradient of the one-day loss (the adjoint configuration: HS T42L20, 72 steps, a checkpoint every
+    8) in the mixed and FP64 paths: wall-clock per gradient (forward sweep, loss, recomputation and
+    reverse sweep, host-timed after a warm-up) and the mixed gradient's error against the FP64 one."""
+    import numpy as np
+
+    out = {"workload": f"HS T42L20, {nsteps} steps from the seeded initial state, checkpoint every {checkpoint}; "
+                       "loss = area-weighted mean squared difference of the final grid T from a seeded target",
+           "gradient_of": "initial spectral T and k_f, k_a, k_s, dT_y, dtheta_z"}
+    grads, ref = {}, None
+    for prec in ("fp64", "fp32"):
+        m = configs.make_mesh(jgcm, WORKLOAD, precision=prec)
+        md = jgcm.Model(m, configs.PARAMS[WORKLOAD])
+        configs.init_held_suarez(jgcm, m, md)
+        if ref is None:
+            ref = {k: md.get(k) for k in jgcm.STATE_FIELDS}
+            tgt = np.asfortranarray(ref["grid_t_c"] + np.random.default_rng(5).standard_normal(ref["grid_t_c"].shape))
+        times = []
+        for i in range(4):
+            for k in jgcm.STATE_FIELDS:
+                md.set(k, ref[k])
+            md.set_init_step(True)
+            jgcm.lib().jgcm_mesh_synchronize(m._h)
+            t0 = time.perf_counter()
+            grads[prec] = jgcm.HS_Gradient(md, nsteps, tgt, checkpoint_every=checkpoint)
+            if i:
+                times.append(time.perf_counter() - t0)
+        out[prec] = {"ms_per_gradient": 1e3 * min(times), "loss": grads[prec][0]}
+        md.close()
+    (l64, g64, p64), (l32, g32, p32) = grads["fp64"], grads["fp32"]
+    out["fp32_vs_fp64"] = {"loss_rel": abs(l32 - l64) / l64,
+                           "grad_T0_rel_l2": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64)),
+                           "grad_params_max_rel": float(np.max(np.abs(p32 - p64) / np.abs(p64)))}
+    return out
+
+
 def run_jgcm(args):
     import numpy as np
 
@@ -427,6 +465,11 @@ def run_jgcm(args):
             extra["ensemble"] = ensemble_bench(jgcm, configs, ["fp32", "tf32x3"])
         except Exception as e:
             extra["ensemble_error"] = str(e)
+    if not args.no_adjoint and world == 1:
+        try:
+            extra["adjoint"] = adjoint_bench(jgcm, configs)
+        except Exception as e:
+            extra["adjoint_error"] = str(e)
     line = {
         "metric": METRIC, "value": value, "unit": "sim-days/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": 1000.0 * t_mx / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -468,6 +511,7 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "tf32x3", "bf16x3"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble and tensor-core side runs")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the one-day gradient timing")
     ap.add_argument("--profile", action="store_true",
                     help="only the mixed-precision headline model: --warmup then --steps sim-days with the tiles of "
                          "--tiles (no autotuning, no other model), a short launch sequence for ncu")

@@ -17,6 +17,8 @@
 // In sigma coordinates (a_k = 0) every log-pressure difference is a per-level constant, so the
 // dynamics depend on ps only through grad ln ps; only the Newtonian relaxation (T_eq(p)) and the
 // fixers see ps itself.  FP64 folds of block partials keep every global sum deterministic.
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -153,12 +155,11 @@ struct FixArgs {
   double cp, grav;
 };
 
+// one thread per grid point: block partials of the sum of the grid temperature cotangent
 template <typename T>
 __global__ void __launch_bounds__(256) k_fix1(FixArgs a) {
-  const int G = a.nlat * a.nlon, c = blockIdx.x * blockDim.x + threadIdx.x;
-  double s = 0.0;
-  if (c < G)
-    for (int k = 0; k < a.nd; k++) s += (double)((const T*)a.bt)[c + (size_t)G * k];
+  const size_t n = (size_t)a.nlat * a.nlon * a.nd, i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double s = i < n ? (double)((const T*)a.bt)[i] : 0.0;
   s = block_sum(s);
   if (threadIdx.x == 0) a.part[blockIdx.x] = s;
 }
@@ -181,29 +182,34 @@ __global__ void __launch_bounds__(256) k_fold1(FixArgs a, int nb) {
   }
 }
 
-// energy fixer reversed: en_n = |u_n|^2/2 + cp T_n weighted by dp(ps_n2); partials of ps_n2_bar ps_n
+// energy fixer reversed: en_n = |u_n|^2/2 + cp T_n weighted by dp(ps_n2); a warp per column, a lane
+// per level; block partials of ps_n2_bar ps_n
 template <typename T>
 __global__ void __launch_bounds__(256) k_fix2(FixArgs a) {
-  const int G = a.nlat * a.nlon, c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int G = a.nlat * a.nlon, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * 8 + (threadIdx.x >> 5), k = lane;
+  const bool colv = c < G, act = colv && k < a.nd;
+  const int j = colv ? c / a.nlon : 0;
+  const double factor = a.sc[SC_FACTOR], corr = a.sc[SC_CORR], En_bar = a.sc[SC_EN_BAR];
+  const double Wc = a.wts[j] / (2.0 * a.nlon);
+  const double ps2 = colv ? (double)((const T*)a.ps_n2)[c] : 0.0;
+  double acc = 0.0;
+  if (act && a.do_energy) {
+    const size_t x = c + (size_t)G * k;
+    const double u = ((const T*)a.u_n)[x], v = ((const T*)a.v_n)[x], t = (double)((const T*)a.t_n2)[x] - corr;
+    const double en = 0.5 * (u * u + v * v) + a.cp * t;
+    const double eb = En_bar * Wc * (a.vc->dak[k] + a.vc->dbk[k] * ps2) / a.grav;
+    ((T*)a.bu)[x] = (T)((double)((T*)a.bu)[x] + eb * u);
+    ((T*)a.bv)[x] = (T)((double)((T*)a.bv)[x] + eb * v);
+    ((T*)a.bt)[x] = (T)((double)((T*)a.bt)[x] + a.cp * eb);
+    acc = en * a.vc->dbk[k];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
   double s = 0.0;
-  if (c < G) {
-    const int j = c / a.nlon;
-    const double factor = a.sc[SC_FACTOR], corr = a.sc[SC_CORR], En_bar = a.sc[SC_EN_BAR];
-    const double Wc = a.wts[j] / (2.0 * a.nlon);
-    const double ps2 = (double)((const T*)a.ps_n2)[c];
+  if (colv && lane == 0) {
     double bps = (double)((T*)a.bps)[c];
     if (a.do_energy) {
-      double acc = 0.0;
-      for (int k = 0; k < a.nd; k++) {
-        const size_t x = c + (size_t)G * k;
-        const double u = ((const T*)a.u_n)[x], v = ((const T*)a.v_n)[x], t = (double)((const T*)a.t_n2)[x] - corr;
-        const double en = 0.5 * (u * u + v * v) + a.cp * t;
-        const double eb = En_bar * Wc * (a.vc->dak[k] + a.vc->dbk[k] * ps2) / a.grav;
-        ((T*)a.bu)[x] = (T)((double)((T*)a.bu)[x] + eb * u);
-        ((T*)a.bv)[x] = (T)((double)((T*)a.bv)[x] + eb * v);
-        ((T*)a.bt)[x] = (T)((double)((T*)a.bt)[x] + a.cp * eb);
-        acc += en * a.vc->dbk[k];
-      }
       bps += En_bar * Wc / a.grav * acc;
       ((T*)a.bps)[c] = (T)bps;
     }
@@ -229,22 +235,23 @@ __global__ void __launch_bounds__(256) k_fold2(FixArgs a, int nb) {
   }
 }
 
-// mass fixer reversed and exp(ln ps); u, v cotangents divided by cos (inputs of S2G^T of ucos, vcos)
+// mass fixer reversed and exp(ln ps); u, v cotangents divided by cos (inputs of S2G^T of ucos,
+// vcos); one thread per grid point
 template <typename T>
 __global__ void __launch_bounds__(256) k_fix3(FixArgs a) {
-  const int G = a.nlat * a.nlon, c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= G) return;
-  const int j = c / a.nlon;
-  const double factor = a.sc[SC_FACTOR];
-  const double ps_n = (double)((const T*)a.ps_n2)[c] / factor;
-  double bps = (double)((const T*)a.bps)[c];
-  if (a.do_mass) bps = bps * factor + a.sc[SC_MN_BAR] * a.wts[j] / (2.0 * a.nlon);
-  ((T*)a.g_lnps)[c] = (T)(bps * ps_n);
+  const int G = a.nlat * a.nlon;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)G * a.nd) return;
+  const int c = (int)(i % G), j = c / a.nlon;
   const T cj = ((const T*)a.cosj)[j];
-  for (int k = 0; k < a.nd; k++) {
-    const size_t x = c + (size_t)G * k;
-    ((T*)a.g_uc)[x] = ((const T*)a.bu)[x] / cj;
-    ((T*)a.g_vc)[x] = ((const T*)a.bv)[x] / cj;
+  ((T*)a.g_uc)[i] = ((const T*)a.bu)[i] / cj;
+  ((T*)a.g_vc)[i] = ((const T*)a.bv)[i] / cj;
+  if (i < (size_t)G) {
+    const double factor = a.sc[SC_FACTOR];
+    const double ps_n = (double)((const T*)a.ps_n2)[c] / factor;
+    double bps = (double)((const T*)a.bps)[c];
+    if (a.do_mass) bps = bps * factor + a.sc[SC_MN_BAR] * a.wts[j] / (2.0 * a.nlon);
+    ((T*)a.g_lnps)[c] = (T)(bps * ps_n);
   }
 }
 
@@ -422,6 +429,10 @@ __global__ void __launch_bounds__(256) k_alpha_adjoint(const V2<T>* __restrict__
 }
 
 // ---- the column kernel --------------------------------------------------------------------------
+// Arithmetic in the state precision R = T (the mixed path's FP32 column, as its forward column
+// kernel; FP64 on the FP64 path); per-column sums of the parameter cotangents go to FP64 block
+// partials.  Divisions by constants are host-side reciprocals, and T_eq's power and logarithm come
+// from one ln ps per column: ln(p_k / p0) = cf_k + ln ps - ln p0, (p_k/p0)^kappa = exp(kappa ln).
 template <typename T>
 struct ColAdjArgs {
   const T *u, *v, *t, *vor, *div, *up, *vp, *tp, *ps, *psp;  // X_s
@@ -435,36 +446,44 @@ struct ColAdjArgs {
   const double* sc;
   double* ppart;  // [5][nblocks]
   int nd, nlat, nlon, Dt;
-  double sigma_b, k_f, k_a, k_s, dT_y, dtheta_z, kappa, rdgas, cp, grav;
+  // HS_Forcing.jl constants (per second): k_v = kvc max(0, sigma - sigma_b),
+  // k_t = ka + ktc max(0, sigma - sigma_b) cos^4
+  double sigma_b, kvc, ka, ktc, inv_1msb, inv_day, dT_y, dtheta_z, kappa, ln_p0;
+  double rdgas, cp, inv_cp, inv_grav;
 };
 
-__device__ __forceinline__ double up1(double x, int lane) {  // value of lane - 1 (0 for lane 0)
-  double y = __shfl_up_sync(FULL, x, 1);
-  return lane == 0 ? 0.0 : y;
+template <typename R>
+__device__ __forceinline__ R up1(R x, int lane) {  // value of lane - 1 (0 for lane 0)
+  R y = __shfl_up_sync(FULL, x, 1);
+  return lane == 0 ? (R)0 : y;
 }
-__device__ __forceinline__ double dn1(double x, int lane) {  // value of lane + 1 (0 for lane 31)
-  double y = __shfl_down_sync(FULL, x, 1);
-  return lane == 31 ? 0.0 : y;
+template <typename R>
+__device__ __forceinline__ R dn1(R x, int lane) {  // value of lane + 1 (0 for lane 31)
+  R y = __shfl_down_sync(FULL, x, 1);
+  return lane == 31 ? (R)0 : y;
 }
-__device__ __forceinline__ double wsum(double x) {
+template <typename R>
+__device__ __forceinline__ R wsum(R x) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
   return x;
 }
-__device__ __forceinline__ double scan_excl(double x, int lane) {  // sum over lanes < lane
-  double s = x;
+template <typename R>
+__device__ __forceinline__ R scan_excl(R x, int lane) {  // sum over lanes < lane
+  R s = x;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    double y = __shfl_up_sync(FULL, s, o);
+    R y = __shfl_up_sync(FULL, s, o);
     if (lane >= o) s += y;
   }
   return s - x;
 }
-__device__ __forceinline__ double rscan_excl(double x, int lane) {  // sum over lanes > lane
-  double s = x;
+template <typename R>
+__device__ __forceinline__ R rscan_excl(R x, int lane) {  // sum over lanes > lane
+  R s = x;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    double y = __shfl_down_sync(FULL, s, o);
+    R y = __shfl_down_sync(FULL, s, o);
     if (lane + o < 32) s += y;
   }
   return s - x;
@@ -472,6 +491,7 @@ __device__ __forceinline__ double rscan_excl(double x, int lane) {  // sum over 
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_hs_column_adjoint(ColAdjArgs<T> a, const VertCoef* __restrict__ vcp) {
+  using R = T;
   __shared__ double pw[8][5];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int G = a.nlat * a.nlon, nd = a.nd;
@@ -482,134 +502,142 @@ __global__ void __launch_bounds__(256) k_hs_column_adjoint(ColAdjArgs<T> a, cons
   const VertCoef& vc = *vcp;
   const int j = colv ? col / a.nlon : 0;
   const size_t x = (size_t)(colv ? col : 0) + (size_t)G * (act ? k : 0);
-  auto ld = [&](const T* p) -> double { return act ? (double)p[x] : 0.0; };
-  const double u = ld(a.u), v = ld(a.v), t = ld(a.t), vor = ld(a.vor), div = ld(a.div);
-  const double tl = ld(a.tl), tt = ld(a.tt), up = ld(a.up), vp = ld(a.vp), tp = ld(a.tp);
-  const double DU = ld(a.DU), DV = ld(a.DV), DT = ld(a.DT), EN = ld(a.EN);
+  auto ld = [&](const T* p) -> R { return act ? (R)p[x] : (R)0; };
+  const R u = ld(a.u), v = ld(a.v), t = ld(a.t), vor = ld(a.vor), div = ld(a.div);
+  const R tl = ld(a.tl), tt = ld(a.tt), up = ld(a.up), vp = ld(a.vp), tp = ld(a.tp);
+  const R DU = ld(a.DU), DV = ld(a.DV), DT = ld(a.DT), EN = ld(a.EN);
   const size_t c1 = colv ? col : 0;
-  const double ps = a.ps[c1], psp = a.psp[c1], gl = a.gl[c1], gt = a.gt[c1], DLN = colv ? (double)a.DLN[c1] : 0.0;
-  const double R = a.rdgas, kap = a.rdgas / a.cp;
+  const R ps = a.ps[c1], psp = a.psp[c1], gl = a.gl[c1], gt = a.gt[c1];
+  const R DLN = colv ? (R)a.DLN[c1] : (R)0;
+  const R Rg = (R)a.rdgas, kap = (R)a.kappa;
   // vertical constants; lanes >= nd carry zeros (dbk = 1 keeps the divisions finite)
-  const double bk = act ? vc.bk[k] : 0.0, bk1 = act ? vc.bk[k + 1] : 0.0, dbk = act ? vc.dbk[k] : 1.0;
-  const double dlp_p = act ? vc.dlp_p[k] : 0.0, dlp_m = (act && k >= 1) ? vc.dlp_m[k] : 0.0;
-  const double dlp = (act && k >= 1) ? vc.dlp[k] : 0.0, sf = act ? vc.sf[k] : 1.0;
-  const double X1 = (bk * dlp_m + bk1 * dlp_p) / dbk;  // x1 ps (Four_In_One!)
+  const R bk = act ? (R)vc.bk[k] : (R)0, bk1 = act ? (R)vc.bk[k + 1] : (R)0, dbk = act ? (R)vc.dbk[k] : (R)1;
+  const R rdbk = (R)1 / dbk;
+  const R dlp_p = act ? (R)vc.dlp_p[k] : (R)0, dlp_m = (act && k >= 1) ? (R)vc.dlp_m[k] : (R)0;
+  const R dlp = (act && k >= 1) ? (R)vc.dlp[k] : (R)0, sf = act ? (R)vc.sf[k] : (R)1;
+  const R cf = act ? (R)vc.cf[k] : (R)0;
+  const R X1 = (bk * dlp_m + bk1 * dlp_p) * rdbk;  // x1 ps (Four_In_One!)
   // ---- forward of the column: Four_In_One! with the mass fluxes scaled by 1/ps ----
-  const double gu = u * gl + v * gt;
-  const double q = act ? dbk * (div + gu) : 0.0;  // dmean / ps
-  const double Tex = scan_excl(q, lane);          // dmean_tot before level k, / ps
-  const double Ttot = wsum(q);
-  const double x5 = -(Tex * dlp + q * dlp_p) / dbk + X1 * gu;
-  const double Mt = (act && k >= 1) ? (-Tex + Ttot * bk) : 0.0;  // M_half[k] / ps (k = 1..nd-1)
-  const double Mn = dn1(Mt, lane);                                // every lane takes part in the shuffle
-  const double Mb = (k + 1 < nd) ? Mn : 0.0;                       // M_half[k+1] / ps
-  const double dbk_m1 = up1(dbk, lane);
-  const double al = (act && k >= 1) ? dbk_m1 / (dbk_m1 + dbk) : 0.0;
+  const R gu = u * gl + v * gt;
+  const R q = act ? dbk * (div + gu) : (R)0;  // dmean / ps
+  const R Tex = scan_excl(q, lane);           // dmean_tot before level k, / ps
+  const R Ttot = wsum(q);
+  const R x5 = -(Tex * dlp + q * dlp_p) * rdbk + X1 * gu;
+  const R Mt = (act && k >= 1) ? (-Tex + Ttot * bk) : (R)0;  // M_half[k] / ps (k = 1..nd-1)
+  const R Mn = dn1(Mt, lane);                                 // every lane takes part in the shuffle
+  const R Mb = (k + 1 < nd) ? Mn : (R)0;                      // M_half[k+1] / ps
+  const R dbk_m1 = up1(dbk, lane);
+  const R al = (act && k >= 1) ? dbk_m1 / (dbk_m1 + dbk) : (R)0;
   // ---- cotangents ----
-  double bu = act ? (double)a.seed_u[x] : 0.0, bv = act ? (double)a.seed_v[x] : 0.0;
-  double bt = act ? (double)a.seed_t[x] : 0.0;
+  R bu = act ? (R)a.seed_u[x] : (R)0, bv = act ? (R)a.seed_v[x] : (R)0;
+  R bt = act ? (R)a.seed_t[x] : (R)0;
   // absolute-vorticity fluxes: du += (vor + f) v, dv -= (vor + f) u
-  const double av = vor + (double)a.coriolis[j];
-  const double bvor = DU * v - DV * u;
+  const R av = vor + (R)a.coriolis[j];
+  const R bvor = DU * v - DV * u;
   bv += DU * av;
   bu -= DV * av;
   // horizontal advection of T: dT -= u dT/dlam + v dT/dth
   bu -= DT * tl;
   bv -= DT * tt;
-  const double btl = -DT * u, btt = -DT * v;
+  const R btl = -DT * u, btt = -DT * v;
   // vertical advection (Vert_Advection!, dz = dp = dbk ps, w = M_half): flux_k = w_k r_int_k
-  double Mbar = 0.0;
-  auto vadv = [&](double r, double Rb, double& rb) {
-    const double r_m1 = up1(r, lane);
-    const double rint = (k >= 1) ? r_m1 + (r - r_m1) * al : 0.0;
-    const double qq = Rb / dbk;
-    const double qq_m1 = up1(qq, lane);
-    const double fb = (act && k >= 1) ? qq - qq_m1 : 0.0;  // flux_k enters rdt_k (+) and rdt_{k-1} (-)
+  R Mbar = 0;
+  auto vadv = [&](R r, R Rb, R& rb) {
+    const R r_m1 = up1(r, lane);
+    const R rint = (k >= 1) ? r_m1 + (r - r_m1) * al : (R)0;
+    const R qq = Rb * rdbk;
+    const R qq_m1 = up1(qq, lane);
+    const R fb = (act && k >= 1) ? qq - qq_m1 : (R)0;  // flux_k enters rdt_k (+) and rdt_{k-1} (-)
     rb += qq * (Mb - Mt);
-    Mbar += -qq * r + ((k >= 1) ? qq_m1 * r_m1 : 0.0);
+    Mbar += -qq * r + ((k >= 1) ? qq_m1 * r_m1 : (R)0);
     Mbar += fb * rint;
     rb += fb * Mt * al;
-    rb += dn1(fb * Mt * (1.0 - al), lane);  // r_{k-1} share of flux_k, from lane k + 1's view
+    rb += dn1(fb * Mt * ((R)1 - al), lane);  // r_{k-1} share of flux_k, from lane k + 1's view
   };
   vadv(u, DU, bu);
   vadv(v, DV, bv);
   vadv(t, DT, bt);
   // dlnps = dps / ps = -dmean_tot / ps
-  double Tbar_tot = -DLN;
+  R Tbar_tot = -DLN;
   // energy = geopotential + |u|^2 / 2: Phi_k = R (t_k dlp_p_k + sum_{l > k} t_l dlp_l)
   bu += EN * u;
   bv += EN * v;
-  bt += R * (EN * dlp_p + dlp * scan_excl(EN, lane));
+  bt += Rg * (EN * dlp_p + dlp * scan_excl(EN, lane));
   // Four_In_One! reversed: M_half[k] = -tot_k + tot_nd b_k
-  double Tbar = (act && k >= 1) ? -Mbar : 0.0;
-  Tbar_tot += wsum((act && k >= 1) ? Mbar * bk : 0.0);
+  R Tbar = (act && k >= 1) ? -Mbar : (R)0;
+  Tbar_tot += wsum((act && k >= 1) ? Mbar * bk : (R)0);
   bt += kap * x5 * DT;
-  const double bx5 = kap * t * DT;
-  if (k >= 1) Tbar -= bx5 * dlp / dbk;
-  double qbar = -bx5 * dlp_p / dbk;
-  double gub = bx5 * X1;
-  bt -= R * X1 * (gl * DU + gt * DV);
-  double glb = -R * t * X1 * DU, gtb = -R * t * X1 * DV;
-  qbar += rscan_excl(act ? Tbar : 0.0, lane) + Tbar_tot;  // tot_k = sum_{l < k} dmean_l
-  const double bdiv = qbar * dbk;
+  const R bx5 = kap * t * DT;
+  if (k >= 1) Tbar -= bx5 * dlp * rdbk;
+  R qbar = -bx5 * dlp_p * rdbk;
+  R gub = bx5 * X1;
+  bt -= Rg * X1 * (gl * DU + gt * DV);
+  R glb = -Rg * t * X1 * DU, gtb = -Rg * t * X1 * DV;
+  qbar += rscan_excl(act ? Tbar : (R)0, lane) + Tbar_tot;  // tot_k = sum_{l < k} dmean_l
+  const R bdiv = qbar * dbk;
   gub += qbar * dbk;
   bu += gub * gl;
   bv += gub * gt;
   glb += gub * u;
   gtb += gub * v;
   // ---- HS_Forcing! of the p level and the energy integral of Compute_Corrections_Init ----
-  const double day = 86400.0, t_zero = 315.0, t_strat = 200.0, p_ref = 1.0e5, sb = a.sigma_b;
-  const double kf = a.k_f / day, ka = a.k_a / day, ks = a.k_s / day;
-  const double sj = (double)a.sinj[j], s2 = sj * sj, c2 = 1.0 - s2, c4 = c2 * c2;
-  const double Ep_bar = a.sc[SC_EP_BAR], mpsp_bar = a.sc[SC_MPSP_BAR], Wc = a.wts[j] / (2.0 * a.nlon);
-  const int Dt = a.Dt;
-  double bup = 0.0, bvp = 0.0, btp = 0.0, bps_l = 0.0, bpsp_l = 0.0;
-  double pb0 = 0.0, pb1 = 0.0, pb2 = 0.0, pb3 = 0.0, pb4 = 0.0;
+  const R t_zero = 315, t_strat = 200, sb = (R)a.sigma_b;
+  const R sj = a.sinj[j], s2 = sj * sj, c2 = (R)1 - s2, c4 = c2 * c2;
+  const R Ep_bar = (R)a.sc[SC_EP_BAR], Wc = (R)(a.wts[j] / (2.0 * a.nlon));
+  const R Dt = (R)a.Dt, icp = (R)a.inv_cp, ig = (R)a.inv_grav;
+  const R lps = log(ps) - (R)a.ln_p0;  // one logarithm per column
+  R bup = 0, bvp = 0, btp = 0, bps_l = 0, bpsp_l = 0;
+  R pb0 = 0, pb1 = 0, pb2 = 0, pb3 = 0, pb4 = 0;
   if (act) {
-    const double s = sf - sb, sp = s > 0.0 ? s : 0.0;  // sigma = p_k / ps
-    const double kv = kf / (1.0 - sb) * sp;
-    const double duf = -kv * up, dvf = -kv * vp;
-    const double pn = sf * ps / p_ref, lpn = log(pn), pk = pow(pn, a.kappa);
-    const double te = (t_zero - a.dT_y * s2 - a.dtheta_z * c2 * lpn) * pk;
-    const double teq = te > t_strat ? te : t_strat;
-    const double kt = ka + (ks - ka) / (1.0 - sb) * sp * c4;
-    const double fr = -((up + 0.5 * duf * Dt) * duf + (vp + 0.5 * dvf * Dt) * dvf) / a.cp;
-    const double dTf = fr - kt * (tp - teq);
-    const double aa = up + Dt * duf, bb = vp + Dt * dvf;
-    const double enp = 0.5 * (aa * aa + bb * bb) + a.cp * (tp + Dt * dTf);
-    bpsp_l = Ep_bar * Wc / a.grav * enp * dbk;
-    const double eb = Ep_bar * Wc * (vc.dak[k] + dbk * psp) / a.grav;
-    const double ba = eb * aa, bbv = eb * bb;
-    btp += a.cp * eb;
-    double bdTf = DT + a.cp * Dt * eb;
-    double bduf = DU + Dt * ba;
-    double bdvf = DV + Dt * bbv;
+    const R s = sf - sb, sp = s > (R)0 ? s : (R)0;  // sigma = p_k / ps
+    const R kv = (R)a.kvc * sp;
+    const R duf = -kv * up, dvf = -kv * vp;
+    const R lpn = cf + lps;                  // ln(p_k / p0)
+    const R pk = exp(kap * lpn);             // (p_k / p0)^kappa
+    const R pn = sf * ps * (R)1.0e-5;        // p_k / p0
+    const R tpot = t_zero - (R)a.dT_y * s2 - (R)a.dtheta_z * c2 * lpn;
+    const R te = tpot * pk;
+    const R teq = te > t_strat ? te : t_strat;
+    const R kt = (R)a.ka + (R)a.ktc * sp * c4;
+    const R fr = -((up + (R)0.5 * duf * Dt) * duf + (vp + (R)0.5 * dvf * Dt) * dvf) * icp;
+    const R dTf = fr - kt * (tp - teq);
+    const R aa = up + Dt * duf, bb = vp + Dt * dvf;
+    const R enp = (R)0.5 * (aa * aa + bb * bb) + (R)a.cp * (tp + Dt * dTf);
+    bpsp_l = Ep_bar * Wc * ig * enp * dbk;
+    const R eb = Ep_bar * Wc * ((R)vc.dak[k] + dbk * psp) * ig;
+    const R ba = eb * aa, bbv = eb * bb;
+    btp += (R)a.cp * eb;
+    R bdTf = DT + (R)a.cp * Dt * eb;
+    R bduf = DU + Dt * ba;
+    R bdvf = DV + Dt * bbv;
     bup += ba;
     bvp += bbv;
-    const double bkt = -bdTf * (tp - teq);
+    const R bkt = -bdTf * (tp - teq);
     btp -= kt * bdTf;
-    const double bteq = kt * bdTf;
-    bduf -= bdTf * (up + duf * Dt) / a.cp;
-    bup -= bdTf * duf / a.cp;
-    bdvf -= bdTf * (vp + dvf * Dt) / a.cp;
-    bvp -= bdTf * dvf / a.cp;
-    const double bkv = -bduf * up - bdvf * vp;
+    const R bteq = kt * bdTf;
+    bduf -= bdTf * (up + duf * Dt) * icp;
+    bup -= bdTf * duf * icp;
+    bdvf -= bdTf * (vp + dvf * Dt) * icp;
+    bvp -= bdTf * dvf * icp;
+    const R bkv = -bduf * up - bdvf * vp;
     bup -= kv * bduf;
     bvp -= kv * bdvf;
-    pb0 = bkv * sp / (1.0 - sb) / day;
-    pb1 = bkt * (1.0 - sp * c4 / (1.0 - sb)) / day;
-    pb2 = bkt * sp * c4 / (1.0 - sb) / day;
-    const double bte = te > t_strat ? bteq : 0.0;
+    const R spn = sp * (R)a.inv_1msb;
+    pb0 = bkv * spn * (R)a.inv_day;
+    pb1 = bkt * ((R)1 - spn * c4) * (R)a.inv_day;
+    pb2 = bkt * spn * c4 * (R)a.inv_day;
+    const R bte = te > t_strat ? bteq : (R)0;
     pb3 = -s2 * pk * bte;
     pb4 = -c2 * lpn * pk * bte;
-    const double dte = -a.dtheta_z * c2 / pn * pk + (t_zero - a.dT_y * s2 - a.dtheta_z * c2 * lpn) * a.kappa * pk / pn;
-    bps_l = bte * dte * sf / p_ref;
+    // d te / d pn = (pk / pn) (kappa tpot - dtheta_z cos^2); pn = sf ps / p0
+    const R dte = pk / pn * (kap * tpot - (R)a.dtheta_z * c2);
+    bps_l = bte * dte * sf * (R)1.0e-5;
   }
-  const double glb_c = wsum(act ? glb : 0.0), gtb_c = wsum(act ? gtb : 0.0);
-  const double bps_c = wsum(bps_l), bpsp_c = wsum(bpsp_l);
-  const double p0 = wsum(pb0), p1 = wsum(pb1), p2 = wsum(pb2), p3 = wsum(pb3), p4 = wsum(pb4);
+  const R glb_c = wsum(act ? glb : (R)0), gtb_c = wsum(act ? gtb : (R)0);
+  const R bps_c = wsum(bps_l), bpsp_c = wsum(bpsp_l);
+  const R p0 = wsum(pb0), p1 = wsum(pb1), p2 = wsum(pb2), p3 = wsum(pb3), p4 = wsum(pb4);
   if (act) {
-    const T cj = a.cosj[j];
+    const R rc = (R)1 / (R)a.cosj[j];
     a.bu[x] = (T)bu;
     a.bv[x] = (T)bv;
     a.bt[x] = (T)bt;
@@ -618,37 +646,36 @@ __global__ void __launch_bounds__(256) k_hs_column_adjoint(ColAdjArgs<T> a, cons
     a.btp[x] = (T)btp;
     a.bvor[x] = (T)bvor;
     a.bdiv[x] = (T)bdiv;
-    a.btl[x] = (T)(btl / (double)cj);
-    a.btt[x] = (T)(btt / (double)cj);
+    a.btl[x] = (T)(btl * rc);
+    a.btt[x] = (T)(btt * rc);
   }
   if (colv && lane == 0) {
-    const double cj = (double)a.cosj[j];
-    a.bps[col] = (T)((double)a.seed_ps[col] + bps_c);
-    a.bpsp[col] = (T)(bpsp_c + mpsp_bar * Wc);
-    a.bgl[col] = (T)(glb_c / cj);
-    a.bgt[col] = (T)(gtb_c / cj);
+    const R rc = (R)1 / (R)a.cosj[j];
+    a.bps[col] = (T)((R)a.seed_ps[col] + bps_c);
+    a.bpsp[col] = (T)(bpsp_c + (R)a.sc[SC_MPSP_BAR] * Wc);
+    a.bgl[col] = (T)(glb_c * rc);
+    a.bgt[col] = (T)(gtb_c * rc);
   }
   if (lane == 0) {
-    pw[wid][0] = colv ? p0 : 0.0;
-    pw[wid][1] = colv ? p1 : 0.0;
-    pw[wid][2] = colv ? p2 : 0.0;
-    pw[wid][3] = colv ? p3 : 0.0;
-    pw[wid][4] = colv ? p4 : 0.0;
+    pw[wid][0] = colv ? (double)p0 : 0.0;
+    pw[wid][1] = colv ? (double)p1 : 0.0;
+    pw[wid][2] = colv ? (double)p2 : 0.0;
+    pw[wid][3] = colv ? (double)p3 : 0.0;
+    pw[wid][4] = colv ? (double)p4 : 0.0;
   }
   __syncthreads();
   if (threadIdx.x < 5) {
-    double s = 0.0;
-    for (int w = 0; w < 8; w++) s += pw[w][threadIdx.x];
-    a.ppart[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = s;
+    double sum = 0.0;
+    for (int w = 0; w < 8; w++) sum += pw[w][threadIdx.x];
+    a.ppart[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = sum;
   }
 }
 
+// one block per parameter
 __global__ void k_fold_params(const double* __restrict__ part, int nb, double* __restrict__ pbar) {
-  for (int v = 0; v < 5; v++) {
-    double s = fold_partials(part + (size_t)v * nb, nb);
-    if (threadIdx.x == 0) pbar[v] += s;
-    __syncthreads();
-  }
+  const int v = blockIdx.x;
+  double s = fold_partials(part + (size_t)v * nb, nb);
+  if (threadIdx.x == 0) pbar[v] += s;
 }
 
 // loss = sum w_j (T - T_target)^2 / (2 nlon nd) and its grid cotangent
@@ -704,11 +731,12 @@ int work_alloc(jgcm_model* md, AdjWork* w) {
   const size_t S1 = spec_elems(m, 1) * 2 * ts, SL = spec_elems(m, nd) * 2 * ts;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const int G = m->nlat * m->nlon;
-  w->nb_col = (G + 255) / 256;  // one thread per column
+  w->nb_col = (int)((grid_elems(m, nd) + 255) / 256);  // block partials: a thread per grid point
   w->nb_adj = (G + 7) / 8;      // one warp per column
   const size_t gtot = 4 * al(G1) + 8 * al(GL);
   const size_t stot = 4 * al(S1) + 15 * al(SL);
-  const size_t dtot = al(SC_N * 8) + al((size_t)(w->nb_col + 8) * 8) + al((size_t)5 * w->nb_adj * 8) + al(5 * 8);
+  const size_t dtot = al(SC_N * 8) + al((size_t)(std::max(w->nb_col, w->nb_adj) + 8) * 8) +
+                      al((size_t)5 * w->nb_adj * 8) + al(5 * 8);
   JG_TRY(dev_alloc(&w->base, gtot + stot + dtot));
   char* p = (char*)w->base;
   auto take = [&](size_t b) {
@@ -748,7 +776,7 @@ int work_alloc(jgcm_model* md, AdjWork* w) {
   w->s_tl = take(SL);
   w->s_tt = take(SL);
   w->sc = (double*)take(SC_N * 8);
-  w->part = (double*)take((size_t)(w->nb_col + 8) * 8);
+  w->part = (double*)take((size_t)(std::max(w->nb_col, w->nb_adj) + 8) * 8);
   w->ppart = (double*)take((size_t)5 * w->nb_adj * 8);
   w->pbar = (double*)take(5 * 8);
   JG_TRY(si_adjoint_mats(md, &w->mats));
@@ -838,12 +866,12 @@ int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x1, StateBuf* xin, 
   fa.do_energy = md->P.do_energy_correction;
   fa.cp = md->cp_air;
   fa.grav = md->P.grav;
-  const int nbc = w->nb_col;
-  k_fix1<T><<<nbc, 256, 0, st>>>(fa);
-  k_fold1<T><<<1, 256, 0, st>>>(fa, nbc);
-  k_fix2<T><<<nbc, 256, 0, st>>>(fa);
-  k_fold2<T><<<1, 256, 0, st>>>(fa, nbc);
-  k_fix3<T><<<nbc, 256, 0, st>>>(fa);
+  const int nbp = (int)((grid_elems(m, nd) + 255) / 256);  // a thread per grid point
+  k_fix1<T><<<nbp, 256, 0, st>>>(fa);
+  k_fold1<T><<<1, 256, 0, st>>>(fa, nbp);
+  k_fix2<T><<<w->nb_adj, 256, 0, st>>>(fa);  // a warp per column
+  k_fold2<T><<<1, 256, 0, st>>>(fa, w->nb_adj);
+  k_fix3<T><<<nbp, 256, 0, st>>>(fa);
   JG_CUDA(cudaGetLastError());
   // 2. syntheses of the new level reversed: ln ps, T, vor, div, u cos, v cos
   {
@@ -976,18 +1004,25 @@ int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x1, StateBuf* xin, 
   ca.nlat = nlat;
   ca.nlon = nlon;
   ca.Dt = md->init_step ? md->P.dt : 2 * md->P.dt;
-  ca.sigma_b = md->P.sigma_b;
-  ca.k_f = md->P.k_f;
-  ca.k_a = md->P.k_a;
-  ca.k_s = md->P.k_s;
-  ca.dT_y = md->P.dT_y;
-  ca.dtheta_z = md->P.dtheta_z;
-  ca.kappa = md->P.kappa;
-  ca.rdgas = md->P.rdgas;
-  ca.cp = md->cp_air;
-  ca.grav = md->P.grav;
+  {
+    const double day = 86400.0, sb = md->P.sigma_b;
+    ca.sigma_b = sb;
+    ca.kvc = md->P.k_f / day / (1.0 - sb);
+    ca.ka = md->P.k_a / day;
+    ca.ktc = (md->P.k_s - md->P.k_a) / day / (1.0 - sb);
+    ca.inv_1msb = 1.0 / (1.0 - sb);
+    ca.inv_day = 1.0 / day;
+    ca.dT_y = md->P.dT_y;
+    ca.dtheta_z = md->P.dtheta_z;
+    ca.kappa = md->P.kappa;
+    ca.ln_p0 = std::log(1.0e5);
+    ca.rdgas = md->P.rdgas;
+    ca.cp = md->cp_air;
+    ca.inv_cp = 1.0 / md->cp_air;
+    ca.inv_grav = 1.0 / md->P.grav;
+  }
   k_hs_column_adjoint<T><<<w->nb_adj, 256, 0, st>>>(ca, md->d_vc);
-  k_fold_params<<<1, 256, 0, st>>>(w->ppart, w->nb_adj, w->pbar);
+  k_fold_params<<<5, 256, 0, st>>>(w->ppart, w->nb_adj, w->pbar);
   JG_CUDA(cudaGetLastError());
   // 6. the gradients' syntheses reversed, then Compute_Gradient_Cos! transposed
   {
@@ -1146,7 +1181,7 @@ extern "C" int jgcm_model_hs_gradient(jgcm_model* md, int nsteps, int checkpoint
   // forward sweep with checkpoints
   for (int s = 0; s < nsteps; s++) {
     if (s % K == 0) JG_TRY(state_save(md, &ck[s / K], st));
-    JG_TRY(jgcm_model_step(md, 1));
+    JG_TRY(model_step_async(md));
   }
   JG_TRY(state_save(md, &fin, st));
   // loss and the cotangent of the final grid temperature
@@ -1179,7 +1214,7 @@ extern "C" int jgcm_model_hs_gradient(jgcm_model* md, int nsteps, int checkpoint
     JG_TRY(state_load(md, &ck[g], st));
     for (int s = s0; s < s1; s++) {
       JG_TRY(state_save(md, &seg[s - s0], st));
-      JG_TRY(jgcm_model_step(md, 1));
+      JG_TRY(model_step_async(md));
       JG_TRY(save_scalars(md, d_scal + 4 * (s - s0), st));
     }
     JG_TRY(state_save(md, &seg[s1 - s0], st));

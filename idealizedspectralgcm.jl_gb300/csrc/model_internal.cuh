@@ -75,6 +75,7 @@ inline int lvl(const jgcm_model* md, int which) { return (md->rot + which) % 3; 
 // models.cu services used by the reverse sweep
 int dev_alloc(void** p, size_t bytes);  // cudaMalloc + zero fill
 int hs_grad(jgcm_model* md, int lev, cudaStream_t st);  // gradients of ln ps and T of level `lev`
+int model_step_async(jgcm_model* md);  // one step enqueued on the mesh stream, no synchronisation
 // transposed semi-implicit step (Semi_Implicit.jl:360-513 + Time_Integrator.jl:58-101) on device
 // buffers: obar[8] = cotangents of vor_n, vor_c', div_n, div_c', T_n, T_c', lnps_n, lnps_c';
 // ibar[12] = cotangents of dvor, ddiv, dT, dlnps, vor_p, vor_c, div_p, div_c, T_p, T_c, lnps_p,

@@ -2621,6 +2621,8 @@ ImplArgs<T> si_args(jgcm_model* md, void* const* in, void* const* out) {
 namespace jgcm {
 int dev_alloc(void** p, size_t bytes) { return alloc(p, bytes); }
 
+int model_step_async(jgcm_model* md) { return model_step(md); }
+
 int hs_grad(jgcm_model* md, int lev, cudaStream_t st) {
   return is_fp64(md->mesh) ? issue_hs_grad<double>(md, lev, st) : issue_hs_grad<float>(md, lev, st);
 }

@@ -17,6 +17,7 @@ Reported:
   * wall-clock of one gradient (forward sweep + loss + reverse sweep with recomputation).
 
   python tests/hs_adjoint_config.py [--steps 72] [--checkpoint 8] [--no-oracle] [--out adj.json]
+  python tests/hs_adjoint_config.py --profile fp32 --steps 8      (two gradients only, for ncu)
 """
 from __future__ import annotations
 
@@ -53,12 +54,28 @@ def main():
     ap.add_argument("--eps", type=float, default=1e-6)
     ap.add_argument("--no-oracle", action="store_true")
     ap.add_argument("--out", default=None)
+    ap.add_argument("--profile", default=None, metavar="PRECISION",
+                    help="only two gradients in this precision (a short launch sequence for ncu)")
     args = ap.parse_args()
     import __graft_entry__
 
     __graft_entry__.build()
     import jgcm
     from jgcm import configs
+
+    if args.profile:
+        mesh = configs.make_mesh(jgcm, NAME, precision=args.profile)
+        md = jgcm.Model(mesh, configs.PARAMS[NAME])
+        configs.init_held_suarez(jgcm, mesh, md)
+        S0 = {k: md.get(k) for k in jgcm.STATE_FIELDS}
+        tgt = np.asfortranarray(S0["grid_t_c"] + np.random.default_rng(5).standard_normal(S0["grid_t_c"].shape))
+        for _ in range(2):
+            for k in jgcm.STATE_FIELDS:
+                md.set(k, S0[k])
+            md.set_init_step(True)
+            loss, _, _ = jgcm.HS_Gradient(md, args.steps, tgt, checkpoint_every=args.checkpoint)
+        print(json.dumps({"profile": NAME, "precision": args.profile, "steps": args.steps, "loss": loss}))
+        return
 
     nsteps, ck = args.steps, args.checkpoint
     rep = {"workload": f"Held-Suarez T42L20, {nsteps} steps of dt 1200 s, checkpoint every {ck}; loss = area-weighted "
