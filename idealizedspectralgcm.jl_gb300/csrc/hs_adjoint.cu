@@ -85,16 +85,51 @@ int state_alloc(jgcm_model* md, StateBuf* b) {
   return JGCM_OK;
 }
 
+// The 18 fields copied by one launch (a block row per field, 16-byte words; every field's size is
+// a multiple of 16 bytes: 8-byte complex floats x an even count, or 4-byte reals x nlon (even)).
+struct CopyList {
+  const uint4* src[NSTATE];
+  uint4* dst[NSTATE];
+  size_t n16[NSTATE];
+};
+
+__global__ void __launch_bounds__(256) k_copy_fields(CopyList c) {
+  const int f = blockIdx.y;
+  const uint4* __restrict__ s = c.src[f];
+  uint4* __restrict__ d = c.dst[f];
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < c.n16[f]; i += (size_t)gridDim.x * blockDim.x)
+    d[i] = s[i];
+}
+
+int copy_fields(jgcm_model* md, void* const* dst, const void* const* src, cudaStream_t st) {
+  CopyList c;
+  size_t mx = 0;
+  for (int i = 0; i < NSTATE; i++) {
+    const size_t b = st_bytes(md, i);
+    JG_ARG(b % 16 == 0, "state field %d is not a whole number of 16-byte words", i);
+    c.src[i] = (const uint4*)src[i];
+    c.dst[i] = (uint4*)dst[i];
+    c.n16[i] = b / 16;
+    mx = c.n16[i] > mx ? c.n16[i] : mx;
+  }
+  const int bx = (int)std::min<size_t>((mx + 255) / 256, 64);
+  k_copy_fields<<<dim3(bx, NSTATE), 256, 0, st>>>(c);
+  JG_CUDA(cudaGetLastError());
+  return JGCM_OK;
+}
+
 int state_save(jgcm_model* md, StateBuf* b, cudaStream_t st) {
-  for (int i = 0; i < NSTATE; i++)
-    JG_CUDA(cudaMemcpyAsync(b->f[i], model_slot(md, i), st_bytes(md, i), cudaMemcpyDeviceToDevice, st));
+  const void* src[NSTATE];
+  for (int i = 0; i < NSTATE; i++) src[i] = model_slot(md, i);
+  JG_TRY(copy_fields(md, b->f, src, st));
   b->init = md->init_step;
   return JGCM_OK;
 }
 
 int state_load(jgcm_model* md, const StateBuf* b, cudaStream_t st) {
-  for (int i = 0; i < NSTATE; i++)
-    JG_CUDA(cudaMemcpyAsync(model_slot(md, i), b->f[i], st_bytes(md, i), cudaMemcpyDeviceToDevice, st));
+  void* dst[NSTATE];
+  for (int i = 0; i < NSTATE; i++) dst[i] = model_slot(md, i);
+  JG_TRY(copy_fields(md, dst, b->f, st));
   md->init_step = b->init;
   md->grad_ready = 0;  // the next step recomputes the gradients of the loaded c level
   return JGCM_OK;
