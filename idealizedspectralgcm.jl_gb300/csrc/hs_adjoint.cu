@@ -1135,12 +1135,12 @@ int bars_d2h(jgcm_model* md, const StateBuf* b, double* const* host) {
   return JGCM_OK;
 }
 
-struct Scope {  // frees device allocations on every return path
+struct Scope {  // frees device allocations on every return path (holds copies of the handles)
   std::vector<void*> p;
-  std::vector<AdjWork*> w;
+  std::vector<AdjWork> w;
   ~Scope() {
     for (void* q : p) cudaFree(q);
-    for (AdjWork* a : w) work_free(a);
+    for (AdjWork& a : w) work_free(&a);
   }
 };
 
@@ -1160,7 +1160,7 @@ extern "C" int jgcm_model_step_adjoint(jgcm_model* md, double* const* state_bar,
   }
   AdjWork w;
   JG_TRY(work_alloc(md, &w));
-  sc.w.push_back(&w);
+  sc.w.push_back(w);
   JG_TRY(state_save(md, &x0, st));
   JG_TRY(jgcm_model_step(md, 1));
   JG_TRY(state_save(md, &x1, st));
@@ -1204,7 +1204,7 @@ extern "C" int jgcm_model_hs_gradient(jgcm_model* md, int nsteps, int checkpoint
   JG_TRY(nb(&bo));
   AdjWork w;
   JG_TRY(work_alloc(md, &w));
-  sc.w.push_back(&w);
+  sc.w.push_back(w);
   double *d_tgt = nullptr, *d_scal = nullptr;
   const size_t GL = grid_elems(m, nd);
   JG_TRY(dev_alloc((void**)&d_tgt, GL * 8));
