@@ -205,6 +205,8 @@ struct jgcm_mesh {
   unsigned int* d_status;  // device error bits of the tensor-core kernels (bounded waits that gave up)
   int tune[4];             // tile overrides: [1] S2G columns, [2] G2S columns, [3] FFT columns per block (0 = default)
   int tune_gen;            // bumped when the tiles change: captured graphs of the mesh's models are stale
+  int simt_legendre;       // tensor-core precision modes: 1 = run the Legendre contractions on the FP32
+                           // SIMT kernels instead (chosen by the autotuner where they are faster)
   // workspace
   int Cmax;
   void* d_fbuf;       // Fourier buffer [m][j][c] complex T, c < Cmax

@@ -2306,6 +2306,7 @@ extern "C" int jgcm_model_get_tuning(jgcm_model* md, int* knobs, int n) {
   JG_ARG(md && knobs && n >= 4, "need 4 knobs");
   knobs[0] = md->hs_lanes;
   for (int i = 1; i < 4; i++) knobs[i] = md->mesh->tune[i];
+  if (n >= 5) knobs[4] = md->mesh->simt_legendre;
   return JGCM_OK;
 }
 
@@ -2327,10 +2328,16 @@ extern "C" int jgcm_model_set_tuning(jgcm_model* md, const int* knobs, int n) {
     md->hs_lanes = lanes;
     drop_graphs(md);
   }
-  bool changed = false;
+  int simt = m->simt_legendre;
+  if (n >= 5) {
+    JG_ARG(knobs[4] == 0 || knobs[4] == 1, "Legendre engine knob must be 0 (tensor cores) or 1 (SIMT)");
+    simt = m->tc.on ? knobs[4] : 0;  // meaningful for the tensor-core precision modes only
+  }
+  bool changed = simt != m->simt_legendre;
   for (int i = 1; i < 4; i++) changed = changed || m->tune[i] != t[i];
   if (changed) {
     for (int i = 1; i < 4; i++) m->tune[i] = t[i];
+    m->simt_legendre = simt;
     m->tune_gen++;
   }
   return JGCM_OK;
@@ -2352,10 +2359,10 @@ extern "C" int jgcm_model_autotune(jgcm_model* md, int nsteps, int* knobs_out, f
   sc->sw_adv_from_n = md->sw_adv_from_n;
   for (int e = 0; e < md->ne; e++) JG_TRY(jgcm_model_copy_member(sc, e, md, e));
   if (sc->init_step || sc->sw_adv_from_n) JG_TRY(jgcm_model_step(sc, 1));
-  int cur[4];
-  JG_TRY(jgcm_model_get_tuning(md, cur, 4));
+  int cur[5];
+  JG_TRY(jgcm_model_get_tuning(md, cur, 5));
   auto timed = [&](const int* k, float* ms) -> int {
-    JG_TRY(jgcm_model_set_tuning(sc, k, 4));
+    JG_TRY(jgcm_model_set_tuning(sc, k, 5));
     JG_TRY(jgcm_model_step(sc, 3));  // captures the three rotation phases
     return jgcm_model_time_steps(sc, nsteps, ms);
   };
@@ -2364,11 +2371,13 @@ extern "C" int jgcm_model_autotune(jgcm_model* md, int nsteps, int* knobs_out, f
   const int d1 = m->nh >= 256 ? 1 : 256 / m->nh, d2 = m->nh >= 64 ? 4 : m->nh >= 32 ? 8 : 16,
             d3 = m->nlon >= 1024 ? 1 : 1024 / m->nlon;
   std::vector<std::vector<int>> cand = {
-      {1, 2, 4, 8}, {std::max(1, d1 / 2), d1, 2 * d1, 4 * d1}, {4, 8, 16, 32}, {std::max(1, d3 / 2), d3, 2 * d3}};
+      {1, 2, 4, 8}, {std::max(1, d1 / 2), d1, 2 * d1, 4 * d1}, {4, 8, 16, 32}, {std::max(1, d3 / 2), d3, 2 * d3},
+      {0, 1}};
   if (md->P.kind != JGCM_HELD_SUAREZ) cand[0] = {cur[0]};
-  for (int knob = 0; knob < 4; knob++)
+  if (!m->tc.on) cand[4] = {cur[4]};  // the Legendre engine: tensor cores or SIMT (tensor-core modes)
+  for (int knob = 0; knob < 5; knob++)
     for (int v : cand[knob]) {
-      int k[4] = {cur[0], cur[1], cur[2], cur[3]};
+      int k[5] = {cur[0], cur[1], cur[2], cur[3], cur[4]};
       k[knob] = v;
       if (knob == 1 && v == d1) k[1] = 0;
       if (knob == 2 && v == d2) k[2] = 0;
@@ -2381,12 +2390,12 @@ extern "C" int jgcm_model_autotune(jgcm_model* md, int nsteps, int* knobs_out, f
       if (timed(k, &ms) != JGCM_OK) continue;
       if (ms < best) {
         best = ms;
-        for (int i = 0; i < 4; i++) cur[i] = k[i];
+        for (int i = 0; i < 5; i++) cur[i] = k[i];
       }
     }
-  JG_TRY(jgcm_model_set_tuning(md, cur, 4));
+  JG_TRY(jgcm_model_set_tuning(md, cur, 5));
   if (knobs_out)
-    for (int i = 0; i < 4; i++) knobs_out[i] = cur[i];
+    for (int i = 0; i < 5; i++) knobs_out[i] = cur[i];
   if (ms_out) *ms_out = best;
   return JGCM_OK;
 }

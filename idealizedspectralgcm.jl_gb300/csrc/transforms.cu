@@ -688,7 +688,7 @@ static int launch_s2g_into(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, 
   JG_TRY(configure_smem<T>());
   Tables<T> tb = tables<T>(m);
   const int nh = m->nh, ct = s2g_ct(m);
-  if (std::is_same<T, float>::value && m->tc.on) {
+  if (std::is_same<T, float>::value && m->tc.on && !m->simt_legendre) {
     JG_TRY(launch_s2g_legendre_tc(m, sp, fbuf, st));
   } else {
     size_t sm1 = align16((size_t)(m->ns + 1) * nh * sizeof(T)) + (size_t)(m->ns + 1) * ct * sizeof(V);
@@ -794,7 +794,8 @@ int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp, cudaStream_t 
   JG_TRY(launch_fft_only<T>(m, fp, st, fbuf, cap));
   bool adj = false;
   for (int i = 0; i < gp.ng; i++) adj = adj || gp.g[i].op == G2S_ADJ_S2G;
-  if (std::is_same<T, float>::value && m->tc.on && !adj) return launch_g2s_legendre_tc(m, gp, fp.C, st, fbuf);
+  if (std::is_same<T, float>::value && m->tc.on && !adj && !m->simt_legendre)
+    return launch_g2s_legendre_tc(m, gp, fp.C, st, fbuf);
   Tables<T> tb = tables<T>(m);
   const int nh = m->nh, ct = g2s_ct(m);
   size_t sm = (size_t)8 * ct * nh * sizeof(V);

@@ -500,18 +500,18 @@ class Ensemble:
             pass
 
 
-TUNING_KNOBS = ("lanes_per_column", "s2g_columns", "g2s_columns", "fft_columns")
+TUNING_KNOBS = ("lanes_per_column", "s2g_columns", "g2s_columns", "fft_columns", "simt_legendre")
 
 
 def get_tuning(model):
-    k = (C.c_int * 4)()
-    _check(lib().jgcm_model_get_tuning(model._h, k, 4))
+    k = (C.c_int * 5)()
+    _check(lib().jgcm_model_get_tuning(model._h, k, 5))
     return dict(zip(TUNING_KNOBS, list(k)))
 
 
 def set_tuning(model, tuning):
-    k = (C.c_int * 4)(*[int(tuning.get(n, 0)) for n in TUNING_KNOBS])
-    _check(lib().jgcm_model_set_tuning(model._h, k, 4))
+    k = (C.c_int * 5)(*[int(tuning.get(n, 0)) for n in TUNING_KNOBS])
+    _check(lib().jgcm_model_set_tuning(model._h, k, 5))
 
 
 def autotune(model, nsteps=24, cache=None):
@@ -531,7 +531,7 @@ def autotune(model, nsteps=24, cache=None):
     if key in table:
         set_tuning(model, table[key]["tuning"])
         return table[key]
-    k = (C.c_int * 4)()
+    k = (C.c_int * 5)()
     ms = C.c_float()
     _check(lib().jgcm_model_autotune(model._h, int(nsteps), k, C.byref(ms)))
     entry = {"tuning": dict(zip(TUNING_KNOBS, list(k))), "ms_per_step": float(ms.value) / nsteps}

@@ -152,3 +152,37 @@ def test_autotuner_keeps_results_and_caches(jg, tmp_path):
             assert configs.rel_l2(x.get(f), y.get(f)) < 1e-10, (e, f)
     with pytest.raises(AssertionError):
         jg.set_tuning(a, {"lanes_per_column": 3})
+
+
+@pytest.mark.gpu
+def test_legendre_engine_knob(jg):
+    """A tensor-core mesh can run its Legendre contractions on the FP32 SIMT kernels (the autotuner's
+    fifth knob): the step then equals the FP32 mesh's step, and switching back reproduces the
+    tensor-core result; on an FP32 mesh the knob has nothing to switch and stays 0."""
+    name = "hs_t21l20"
+    params = configs.PARAMS[name]
+    m32 = configs.make_mesh(jg, name, precision="fp32")
+    mtc = configs.make_mesh(jg, name, precision="tf32x3")
+    r32, rtc = jg.Model(m32, params), jg.Model(mtc, params)
+    configs.init_held_suarez(jg, m32, r32)
+    start = {f: r32.get(f) for f in jg.STATE_FIELDS}  # everything a step reads
+    for f, v in start.items():
+        rtc.set(f, v)
+    r32.step(4)
+    rtc.step(4)
+    tc_result = rtc.get("grid_t_c")
+    simt = jg.Model(mtc, params)
+    for f, v in start.items():
+        simt.set(f, v)
+    jg.set_tuning(simt, {"simt_legendre": 1})
+    assert jg.get_tuning(simt)["simt_legendre"] == 1
+    simt.step(4)
+    assert configs.rel_l2(simt.get("grid_t_c"), r32.get("grid_t_c")) < 1e-12
+    back = jg.Model(mtc, params)
+    for f, v in start.items():
+        back.set(f, v)
+    jg.set_tuning(back, {"simt_legendre": 0})
+    back.step(4)
+    assert configs.rel_l2(back.get("grid_t_c"), tc_result) < 1e-12
+    jg.set_tuning(r32, {"simt_legendre": 1})
+    assert jg.get_tuning(r32)["simt_legendre"] == 0
