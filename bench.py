@@ -290,9 +290,10 @@ def ensemble_bench(jgcm, configs, precisions, days=2):
             one.close()
             spd = configs.STEPS_PER_DAY[name]
             ens.step(spd)
-            jgcm.autotune(ens, nsteps=8)
+            tuned = jgcm.autotune(ens, nsteps=8)["tuning"]
             t = sum(ens.time_steps(spd) for _ in range(days)) / 1000.0
-            per[name] = {"member_sim_days_per_s": E * days / t, "ms_per_step": 1000.0 * t / (days * spd)}
+            per[name] = {"member_sim_days_per_s": E * days / t, "ms_per_step": 1000.0 * t / (days * spd),
+                         "tuning": tuned}
             models.append(ens)
             owned.append(m)
         group = jgcm.Ensemble(models, 1200)
