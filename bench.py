@@ -10,8 +10,9 @@ dry dynamical core (128 x 64 Gaussian grid, 20 sigma levels), the reference's he
 value      sim-days/s of the mixed-precision path (FP32 state, transforms and tendencies; FP64 wave-
            matrix solve and global sums), device-resident, CUDA-event timed over K sim-days, L2 flushed
            (256 MiB write) before every timed sim-day.
-e2e        the same through the C ABI with host (pinned) buffers: per sim-day the prognostic state is
-           uploaded, 72 steps run, and the state is read back; wall-clock.
+e2e        the same through the C ABI with host (pinned) buffers: per sim-day the whole state (one packed
+           FP64 buffer of the 18 state arrays, reference layout) is uploaded, 72 steps run, and the
+           state is read back into the same buffer; wall-clock.
 fp64       the FP64 GPU path on the same workload, same timing; error_vs_fp64 = relative L2 of
            T, u, v, ps of a mixed-precision twin against an FP64 twin stepped the same days from
            the same state (tensor_core_modes: the same for TF32x3 / BF16x3, with their speed).
@@ -419,24 +420,22 @@ def run_jgcm(args):
     modes = precision_modes(jgcm, configs, days_done, timed=() if (args.no_ensemble or world > 1)
                             else ("tf32x3", "bf16x3"))
     err = modes["fp32"]["error_vs_fp64"]
-    # ---- end to end through host buffers
+    # ---- end to end through host buffers: the whole state in one pinned FP64 buffer (reference layout)
     e2e_model = jgcm.Model(mmx, params)
     jgcm.set_tuning(e2e_model, tiles["mixed"])
-    host = {f: pinned_like(a) for f, a in init_state.items()}
-    bytes_io = sum(a.nbytes for a, _ in host.values())
-    for f, (a, _) in host.items():
-        e2e_model.set(f, a)
+    buf, _keep = pinned_like(jgcm.pack_state(mmx, {f: init_state[f] for f in jgcm.STATE_FIELDS}))
+    bytes_io = buf.nbytes
+    e2e_model.set_state(buf)
     e2e_model.step(1)  # the init step; every timed sim-day below restarts from host state
+    e2e_model.get_state(out=buf)
     t_e2e = 0.0
     ne2e = max(1, K)
     for _ in range(ne2e):
         flush()
         t0 = time.perf_counter()
-        for f, (a, _) in host.items():
-            e2e_model.set(f, a)
+        e2e_model.set_state(buf)
         e2e_model.step(spd)
-        for f, (a, _) in host.items():
-            a[...] = e2e_model.get(f)
+        e2e_model.get_state(out=buf)
         t_e2e += time.perf_counter() - t0
     # ---- per-kernel times and the roofline of the dominant kernel
     kt = modmx.kernel_times(spd)

@@ -29,117 +29,6 @@ using namespace jgcm;
 
 namespace {
 
-constexpr int NSTATE = 18;
-
-// ---- state buffers ----------------------------------------------------------------------------
-// field i of the state: 0 spe_vor_c, 1 spe_vor_p, 2 spe_div_c, 3 spe_div_p, 4 spe_lnps_c,
-// 5 spe_lnps_p, 6 spe_t_c, 7 spe_t_p, 8 grid_u_c, 9 grid_u_p, 10 grid_v_c, 11 grid_v_p,
-// 12 grid_ps_c, 13 grid_ps_p, 14 grid_t_c, 15 grid_t_p, 16 grid_vor, 17 grid_div
-bool st_spec(int i) { return i < 8; }
-int st_levels(const jgcm_model* md, int i) { return (i == 4 || i == 5 || i == 12 || i == 13) ? 1 : md->nd; }
-size_t st_bytes(const jgcm_model* md, int i) {
-  const jgcm_mesh* m = md->mesh;
-  const size_t ts = tsize(m);
-  return st_spec(i) ? spec_elems(m, st_levels(md, i)) * 2 * ts : grid_elems(m, st_levels(md, i)) * ts;
-}
-void* model_slot(jgcm_model* md, int i) {
-  const int p = lvl(md, 0), c = lvl(md, 1);
-  switch (i) {
-    case 0: return md->spe_vor[c];
-    case 1: return md->spe_vor[p];
-    case 2: return md->spe_div[c];
-    case 3: return md->spe_div[p];
-    case 4: return md->spe_lnps[c];
-    case 5: return md->spe_lnps[p];
-    case 6: return md->spe_t[c];
-    case 7: return md->spe_t[p];
-    case 8: return md->grid_u[c];
-    case 9: return md->grid_u[p];
-    case 10: return md->grid_v[c];
-    case 11: return md->grid_v[p];
-    case 12: return md->grid_ps[c];
-    case 13: return md->grid_ps[p];
-    case 14: return md->grid_t[c];
-    case 15: return md->grid_t[p];
-    case 16: return md->grid_vor;
-    default: return md->grid_div;
-  }
-}
-
-struct StateBuf {
-  void* f[NSTATE];
-  void* base;
-  int init;
-};
-
-int state_alloc(jgcm_model* md, StateBuf* b) {
-  size_t tot = 0;
-  for (int i = 0; i < NSTATE; i++) tot += (st_bytes(md, i) + 255) & ~(size_t)255;
-  JG_TRY(dev_alloc(&b->base, tot));
-  size_t off = 0;
-  for (int i = 0; i < NSTATE; i++) {
-    b->f[i] = (char*)b->base + off;
-    off += (st_bytes(md, i) + 255) & ~(size_t)255;
-  }
-  b->init = 0;
-  return JGCM_OK;
-}
-
-// The 18 fields copied by one launch (a block row per field, 16-byte words; every field's size is
-// a multiple of 16 bytes: 8-byte complex floats x an even count, or 4-byte reals x nlon (even)).
-struct CopyList {
-  const uint4* src[NSTATE];
-  uint4* dst[NSTATE];
-  size_t n16[NSTATE];
-};
-
-__global__ void __launch_bounds__(256) k_copy_fields(CopyList c) {
-  const int f = blockIdx.y;
-  const uint4* __restrict__ s = c.src[f];
-  uint4* __restrict__ d = c.dst[f];
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < c.n16[f]; i += (size_t)gridDim.x * blockDim.x)
-    d[i] = s[i];
-}
-
-int copy_fields(jgcm_model* md, void* const* dst, const void* const* src, cudaStream_t st) {
-  CopyList c;
-  size_t mx = 0;
-  for (int i = 0; i < NSTATE; i++) {
-    const size_t b = st_bytes(md, i);
-    JG_ARG(b % 16 == 0, "state field %d is not a whole number of 16-byte words", i);
-    c.src[i] = (const uint4*)src[i];
-    c.dst[i] = (uint4*)dst[i];
-    c.n16[i] = b / 16;
-    mx = c.n16[i] > mx ? c.n16[i] : mx;
-  }
-  const int bx = (int)std::min<size_t>((mx + 255) / 256, 64);
-  k_copy_fields<<<dim3(bx, NSTATE), 256, 0, st>>>(c);
-  JG_CUDA(cudaGetLastError());
-  return JGCM_OK;
-}
-
-int state_save(jgcm_model* md, StateBuf* b, cudaStream_t st) {
-  const void* src[NSTATE];
-  for (int i = 0; i < NSTATE; i++) src[i] = model_slot(md, i);
-  JG_TRY(copy_fields(md, b->f, src, st));
-  b->init = md->init_step;
-  return JGCM_OK;
-}
-
-int state_load(jgcm_model* md, const StateBuf* b, cudaStream_t st) {
-  void* dst[NSTATE];
-  for (int i = 0; i < NSTATE; i++) dst[i] = model_slot(md, i);
-  JG_TRY(copy_fields(md, dst, b->f, st));
-  md->init_step = b->init;
-  md->grad_ready = 0;  // the next step recomputes the gradients of the loaded c level
-  return JGCM_OK;
-}
-
-int state_zero(jgcm_model* md, StateBuf* b, cudaStream_t st) {
-  for (int i = 0; i < NSTATE; i++) JG_CUDA(cudaMemsetAsync(b->f[i], 0, st_bytes(md, i), st));
-  return JGCM_OK;
-}
-
 // ---- deterministic FP64 reductions --------------------------------------------------------------
 // Sum over the block in a fixed order; the result is valid in thread 0.
 __device__ double block_sum(double v) {

@@ -64,6 +64,7 @@ struct jgcm_model {
   int npairs;
   double *d_partials, *d_scalars;
   unsigned* d_counter;
+  double* state_stage;  // FP64 staging of the packed host state (jgcm_model_set_state / get_state)
   cudaGraphExec_t graph[3];
   cudaEvent_t ev0, ev1;
 };
@@ -71,6 +72,26 @@ struct jgcm_model {
 
 namespace jgcm {
 inline int lvl(const jgcm_model* md, int which) { return (md->rot + which) % 3; }  // 0 = p, 1 = c, 2 = n
+
+// state.cu: the 18 arrays one Held-Suarez step reads and writes, in this order:
+//   0 spe_vor_c, 1 spe_vor_p, 2 spe_div_c, 3 spe_div_p, 4 spe_lnps_c, 5 spe_lnps_p, 6 spe_t_c,
+//   7 spe_t_p, 8 grid_u_c, 9 grid_u_p, 10 grid_v_c, 11 grid_v_p, 12 grid_ps_c, 13 grid_ps_p,
+//   14 grid_t_c, 15 grid_t_p, 16 grid_vor, 17 grid_div
+constexpr int NSTATE = 18;
+struct StateBuf {  // a device copy of the state
+  void* f[NSTATE];
+  void* base;
+  int init;  // the init-step flag of the copied state
+};
+bool st_spec(int i);
+int st_levels(const jgcm_model* md, int i);
+size_t st_bytes(const jgcm_model* md, int i);
+void* model_slot(jgcm_model* md, int i);  // field i of the model's current state
+int state_alloc(jgcm_model* md, StateBuf* b);
+int state_save(jgcm_model* md, StateBuf* b, cudaStream_t st);        // model -> b (one launch)
+int state_load(jgcm_model* md, const StateBuf* b, cudaStream_t st);  // b -> model (one launch)
+int state_zero(jgcm_model* md, StateBuf* b, cudaStream_t st);
+int copy_fields(jgcm_model* md, void* const* dst, const void* const* src, cudaStream_t st);
 
 // models.cu services used by the reverse sweep
 int dev_alloc(void** p, size_t bytes);  // cudaMalloc + zero fill

@@ -86,6 +86,9 @@ def lib():
         "jgcm_model_copy_member": (I, [P, I, P, I]),
         "jgcm_model_semi_implicit_step": (I, [P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
         "jgcm_model_semi_implicit_step_adjoint": (I, [P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+        "jgcm_model_state_size": (I, [P, C.POINTER(Lg)]),
+        "jgcm_model_set_state": (I, [P, P]),
+        "jgcm_model_get_state": (I, [P, P]),
         "jgcm_model_step_adjoint": (I, [P, C.POINTER(C.c_void_p), P]),
         "jgcm_model_hs_gradient": (I, [P, I, I, P, P, P, P]),
         "jgcm_model_diagnostics": (I, [P, I]),
@@ -398,6 +401,27 @@ class Model:
     def step(self, nsteps=1):
         _check(lib().jgcm_model_step(self._h, int(nsteps)))
 
+    # ---- the whole state of a Held-Suarez step in one transfer (STATE_FIELDS, packed) ----
+    def state_size(self):
+        n = C.c_long()
+        _check(lib().jgcm_model_state_size(self._h, C.byref(n)))
+        return int(n.value)
+
+    def set_state(self, packed):
+        """Load the 18 STATE_FIELDS from one FP64 buffer (``pack_state``); pinned memory makes the
+        host-to-device copy fastest."""
+        a = np.asarray(packed)
+        assert a.dtype == np.float64 and a.size == self.state_size() and a.flags.c_contiguous
+        _check(lib().jgcm_model_set_state(self._h, a.ctypes.data_as(C.c_void_p)))
+
+    def get_state(self, out=None):
+        """The 18 STATE_FIELDS in one FP64 buffer (``unpack_state`` splits it)."""
+        n = self.state_size()
+        a = np.empty(n) if out is None else out
+        assert a.dtype == np.float64 and a.size == n and a.flags.c_contiguous
+        _check(lib().jgcm_model_get_state(self._h, a.ctypes.data_as(C.c_void_p)))
+        return a
+
     def set_init_step(self, flag=True):
         """Make the next step a first step (Δt) or a leapfrog step (2Δt)."""
         _check(lib().jgcm_model_set_init_step(self._h, int(bool(flag))))
@@ -578,6 +602,38 @@ STATE_FIELDS = ("spe_vor_c", "spe_vor_p", "spe_div_c", "spe_div_p", "spe_lnps_c"
                 "spe_t_p", "grid_u_c", "grid_u_p", "grid_v_c", "grid_v_p", "grid_ps_c", "grid_ps_p", "grid_t_c",
                 "grid_t_p", "grid_vor", "grid_div")
 HS_PARAMS = ("k_f", "k_a", "k_s", "dT_y", "dtheta_z")
+
+
+def _state_shapes(mesh):
+    N1, S1 = mesh.num_fourier + 1, mesh.num_spherical + 1
+    out = []
+    for k in STATE_FIELDS:
+        nlev = 1 if k in ("spe_lnps_c", "spe_lnps_p", "grid_ps_c", "grid_ps_p") else mesh.nd
+        out.append((k, (N1, S1, nlev), np.complex128) if k.startswith("spe_") else
+                   (k, (mesh.nlon, mesh.nlat, nlev), np.float64))
+    return out
+
+
+def pack_state(mesh, fields, out=None):
+    """dict over STATE_FIELDS (reference layout) -> one FP64 buffer for Model.set_state."""
+    parts = [np.asarray(fields[k], dtype=dt).reshape(shp, order="F").ravel(order="F")
+             for k, shp, dt in _state_shapes(mesh)]
+    flat = [p.view(np.float64) if p.dtype == np.complex128 else p for p in parts]
+    if out is None:
+        return np.concatenate(flat)
+    np.concatenate(flat, out=out)
+    return out
+
+
+def unpack_state(mesh, packed):
+    """One FP64 buffer from Model.get_state -> dict over STATE_FIELDS (reference layout)."""
+    out, off = {}, 0
+    for k, shp, dt in _state_shapes(mesh):
+        n = int(np.prod(shp)) * (2 if dt == np.complex128 else 1)
+        v = np.asarray(packed[off:off + n])
+        out[k] = np.asfortranarray((v.view(np.complex128) if dt == np.complex128 else v).reshape(shp, order="F"))
+        off += n
+    return out
 
 
 def HS_Step_Adjoint(model, xbar, pbar=None):

@@ -161,6 +161,14 @@ int jgcm_model_copy_member(jgcm_model* dst, int dst_member, jgcm_model* src, int
  * arrays [N+1, N+2, nd] (lnps: 1 level).  The adjoint maps cotangents of out to cotangents of in. */
 int jgcm_model_semi_implicit_step(jgcm_model* model, const double* const* in, double* const* out);
 int jgcm_model_semi_implicit_step_adjoint(jgcm_model* model, const double* const* out_bar, double* const* in_bar);
+/* The whole state of a Held-Suarez step in one transfer (no counterpart in the reference, which keeps
+ * Dyn_Data on the host): the 18 arrays in the order of jgcm_model_step_adjoint below, each in the
+ * reference host layout (FP64; spectral complex interleaved), back to back in one host buffer of
+ * *ndoubles doubles.  One host<->device copy and one layout-conversion launch each way; a restart
+ * from host state, or a read-out of it, costs one call instead of one per field.  One-member models. */
+int jgcm_model_state_size(jgcm_model* model, long* ndoubles);
+int jgcm_model_set_state(jgcm_model* model, const double* packed);
+int jgcm_model_get_state(jgcm_model* model, double* packed);
 /* Reverse mode of one whole Held-Suarez step (Atmosphere_Update!, Spectral_Dynamics.jl:206-365 +
  * 452-490 with HS_Forcing.jl and Compute_Corrections!; no counterpart in the reference) from the
  * model's current state X_s.  state_bar[18] holds host arrays (reference layout) of the cotangents

@@ -208,3 +208,31 @@ def test_on_device_zonal_mean_diagnostics(jg, members):
         got, steps = md.read_diagnostics(key)
         assert steps == nsteps
         assert configs.rel_l2(got, w / nsteps) < 1e-12, key
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_packed_state_transfer(jg, prec):
+    """jgcm_model_get_state / set_state move the 18 state arrays in one buffer: the packed read equals
+    the per-field reads, and a model loaded from it steps exactly like one loaded field by field."""
+    name = "hs_t21l10"
+    mesh = configs.make_mesh(jg, name, precision=prec)
+    a = jg.Model(mesh, configs.PARAMS[name])
+    configs.init_held_suarez(jg, mesh, a)
+    a.step(2)
+    fields = {k: a.get(k) for k in jg.STATE_FIELDS}
+    packed = a.get_state()
+    assert packed.size == a.state_size()
+    back = jg.unpack_state(mesh, packed)
+    for k in jg.STATE_FIELDS:
+        assert np.array_equal(back[k], fields[k]), k
+    assert np.array_equal(jg.pack_state(mesh, fields), packed)
+    b, c = jg.Model(mesh, configs.PARAMS[name]), jg.Model(mesh, configs.PARAMS[name])
+    b.set_state(packed)
+    for k in jg.STATE_FIELDS:
+        c.set(k, fields[k])
+    for mdl in (b, c):
+        mdl.update_init_step()
+        mdl.step(3)
+    for k in jg.STATE_FIELDS:
+        assert np.array_equal(b.get(k), c.get(k)), k

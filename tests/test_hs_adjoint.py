@@ -247,3 +247,27 @@ def test_gpu_gradient_one_day_t42l20():
     assert abs(l32 - l64) <= 1e-4 * l64
     assert configs.rel_l2(g32, g64) < 1e-3, configs.rel_l2(g32, g64)
     assert np.all(np.abs(p32 - p64) <= 1e-3 * np.abs(p64))
+
+
+def test_packed_state_layout_round_trip():
+    """pack_state / unpack_state (host side of jgcm_model_set_state / get_state): the 18 arrays back
+    to back in STATE_FIELDS order, each in the reference layout; no GPU needed."""
+    import types
+
+    import jgcm
+
+    mesh = types.SimpleNamespace(num_fourier=5, num_spherical=6, nlon=16, nlat=8, nd=3)
+    rng = np.random.default_rng(0)
+    fields = {}
+    for k in jgcm.STATE_FIELDS:
+        nlev = 1 if k in ("spe_lnps_c", "spe_lnps_p", "grid_ps_c", "grid_ps_p") else 3
+        if k.startswith("spe_"):
+            fields[k] = np.asfortranarray(rng.standard_normal((6, 7, nlev)) + 1j * rng.standard_normal((6, 7, nlev)))
+        else:
+            fields[k] = np.asfortranarray(rng.standard_normal((16, 8, nlev)))
+    packed = jgcm.pack_state(mesh, fields)
+    assert packed.size == 2 * 6 * 7 * (3 * 6 + 2) + 16 * 8 * (3 * 8 + 2)
+    assert np.array_equal(packed[:2 * 6 * 7 * 3].view(np.complex128), fields["spe_vor_c"].ravel(order="F"))
+    back = jgcm.unpack_state(mesh, packed)
+    for k in jgcm.STATE_FIELDS:
+        assert np.array_equal(back[k], fields[k]), k
