@@ -13,6 +13,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <utility>
 
 #include "jgcm.h"
 
@@ -231,6 +232,32 @@ struct Marker {
 extern thread_local Marker* g_marker;
 inline void mark(cudaStream_t st) {
   if (g_marker && g_marker->n < g_marker->cap) cudaEventRecord(g_marker->ev[g_marker->n++], st);
+}
+
+// Programmatic dependent launch.  The kernels of a model step start with pdl_wait() (griddepcontrol.wait:
+// returns once the preceding grid on the stream has completed and its writes are visible; a no-op
+// for an ordinary launch), and launch_pdl() launches them with the programmatic-serialization
+// attribute: the next grid is launched as the blocks of its predecessor exit, without waiting for
+// the whole grid's completion, in streams and in captured graphs (HS T42L20 FP32 step: 78.3 -> 75.3
+// us).  An explicit griddepcontrol.launch_dependents at the start of every block, which lets the
+// next grid's blocks occupy the SMs while this one runs, measured 10 % slower and is not used.
+// Set JGCM_PDL=0 to launch them ordinarily.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+extern int g_pdl;
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = g_pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
 }
 
 inline bool is_fp64(const jgcm_mesh* m) { return m->precision == JGCM_FP64; }

@@ -230,6 +230,7 @@ template <class P>
 __global__ void __launch_bounds__(256) k_s2g_tc(S2GPlan plan, Tables<float> tb, const unsigned char* __restrict__ timg,
                                                 const long long* __restrict__ toff, float2* __restrict__ F, int ns,
                                                 int nlat, unsigned* status) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using E = typename P::E;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t bar[2];
@@ -405,6 +406,7 @@ __global__ void __launch_bounds__(256) k_g2s_tc(G2SPlan plan, Tables<float> tb, 
                                                 const long long* __restrict__ off_a, const float2* __restrict__ F,
                                                 int ns, int nlat, int Cin, int KC, int NpM, int nchan,
                                                 unsigned* status) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using E = typename P::E;
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t bar[2];
@@ -691,8 +693,8 @@ static int s2g_tc(jgcm_mesh* m, const S2GPlan& sp, void* fbuf, cudaStream_t st) 
   int tiles = 0;
   for (int i = 0; i < sp.ng; i++) tiles += (sp.g[i].L + 63) / 64;
   dim3 g(tiles, m->N + 1);
-  tc::k_s2g_tc<P><<<g, 256, t.smem_s2g, st>>>(sp, tables<float>(m), t.s2g, t.s2g_off, (float2*)fbuf, m->ns, m->nlat,
-                                              m->d_status);
+  JG_CUDA(launch_pdl(tc::k_s2g_tc<P>, g, 256, t.smem_s2g, st, sp, tables<float>(m), t.s2g, t.s2g_off, (float2*)fbuf, m->ns, m->nlat,
+                                              m->d_status));
   mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;
@@ -710,9 +712,9 @@ static int g2s_tc(jgcm_mesh* m, const G2SPlan& gp, int Cin, cudaStream_t st, voi
   int tiles = 0;
   for (int i = 0; i < gp.ng; i++) tiles += (gp.g[i].L + 63) / 64;
   dim3 g(tiles, m->N + 1);
-  tc::k_g2s_tc<P><<<g, 256, t.smem_g2s, st>>>(gp, tables<float>(m), t.g2s_p, t.g2s_p_off, t.g2s_a, t.g2s_a_off,
+  JG_CUDA(launch_pdl(tc::k_g2s_tc<P>, g, 256, t.smem_g2s, st, gp, tables<float>(m), t.g2s_p, t.g2s_p_off, t.g2s_a, t.g2s_a_off,
                                               (const float2*)fbuf, m->ns, m->nlat, Cin, t.KC, t.NpM, nchan,
-                                              m->d_status);
+                                              m->d_status));
   mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;

@@ -173,6 +173,7 @@ __device__ __forceinline__ R seg_excl_suffix(R x, int s) {  // sum over the lane
 
 template <typename T, int S>
 __global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertCoef* __restrict__ vcp) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const VertCoef& vc = *vcp;
   __shared__ double red[2][HS_CT / 32];
   const int nd = a.nd, nlon = a.nlon, nlat = a.nlat;
@@ -353,10 +354,10 @@ template <typename T>
 int launch_hs_column(const HSColArgs<T>& a, const jgcm_mesh* m, int ne, int S, const VertCoef* vc, cudaStream_t st) {
   const int cpb = HS_CT / S;  // columns per block
   dim3 g((m->nlon + cpb - 1) / cpb, m->nlat, ne);
-  if (S == 1) k_hs_column<T, 1><<<g, HS_CT, 0, st>>>(a, vc);
-  else if (S == 2) k_hs_column<T, 2><<<g, HS_CT, 0, st>>>(a, vc);
-  else if (S == 4) k_hs_column<T, 4><<<g, HS_CT, 0, st>>>(a, vc);
-  else k_hs_column<T, 8><<<g, HS_CT, 0, st>>>(a, vc);
+  if (S == 1) JG_CUDA(launch_pdl(k_hs_column<T, 1>, g, HS_CT, 0, st, a, vc));
+  else if (S == 2) JG_CUDA(launch_pdl(k_hs_column<T, 2>, g, HS_CT, 0, st, a, vc));
+  else if (S == 4) JG_CUDA(launch_pdl(k_hs_column<T, 4>, g, HS_CT, 0, st, a, vc));
+  else JG_CUDA(launch_pdl(k_hs_column<T, 8>, g, HS_CT, 0, st, a, vc));
   return JGCM_OK;
 }
 
@@ -429,6 +430,7 @@ __device__ __forceinline__ void lf(int init, int Dt, R rob, R d, R f, R& dq, R q
 // R is the precision of the vertical algebra (FP64 on the FP64 path; selectable on the FP32 path).
 template <typename T, typename R>
 __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCoef* __restrict__ vcp) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const VertCoef& vc = *vcp;
   using C = CX<R>;
   const int lane = threadIdx.x & 31;
@@ -541,6 +543,7 @@ struct CorrArgs {
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const VertCoef* __restrict__ vcp) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const VertCoef& vc = *vcp;
   // block = 32 consecutive columns of one latitude row x 8 level groups: warp ks reads levels
   // ks, ks + 8, ... of the 32 columns (coalesced rows); column partial sums in the state precision,
@@ -615,6 +618,7 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
 
 template <typename T>
 __global__ void k_hs_corr_apply(T* t_n, T* ps_n, const double* scalars, size_t memL, size_t mem1) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const int e = blockIdx.y;  // member: ps *= factor, T += correction
   const T factor = (T)scalars[4 * e + 2], corr = (T)scalars[4 * e + 3];
   T* t = t_n + (size_t)e * memL;
@@ -1159,6 +1163,7 @@ int step_shallow_water(jgcm_model* md, cudaStream_t st) {
 template <typename T>
 __global__ void k_diag_zonal(const T* t, const T* t_eq, const T* u, const T* v, double* sums, int nd, int nlat,
                              int nlon, int ne) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const int j = blockIdx.x, k = blockIdx.y, e = blockIdx.z;
   const size_t G = (size_t)nlat * nlon, row = ((size_t)e * nd + k) * G + (size_t)j * nlon;
   __shared__ double red[4][4];
@@ -1182,6 +1187,7 @@ __global__ void k_diag_zonal(const T* t, const T* t_eq, const T* u, const T* v, 
 }
 template <typename T>
 __global__ void k_diag_ps(const T* ps, double* sums, size_t n) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
     sums[q] += (double)ps[q];
 }
@@ -1190,13 +1196,13 @@ template <typename T>
 int issue_diag(jgcm_model* md, int lev, cudaStream_t st) {
   jgcm_mesh* m = md->mesh;
   const int nd = md->nd, E = md->ne;
-  k_diag_zonal<T><<<dim3(m->nlat, nd, E), 128, 0, st>>>((const T*)md->grid_t[lev], (const T*)md->grid_t_eq,
+  JG_CUDA(launch_pdl(k_diag_zonal<T>, dim3(m->nlat, nd, E), 128, 0, st, (const T*)md->grid_t[lev], (const T*)md->grid_t_eq,
                                                          (const T*)md->grid_u[lev], (const T*)md->grid_v[lev],
-                                                         md->diag, nd, m->nlat, m->nlon, E);
+                                                         md->diag, nd, m->nlat, m->nlon, E));
   JG_CUDA(cudaGetLastError());
   const size_t nps = grid_elems(m, E);
-  k_diag_ps<T><<<(int)std::min<size_t>((nps + 255) / 256, 1024), 256, 0, st>>>(
-      (const T*)md->grid_ps[lev], md->diag + (size_t)4 * E * nd * m->nlat, nps);
+  JG_CUDA(launch_pdl(k_diag_ps<T>, (int)std::min<size_t>((nps + 255) / 256, 1024), 256, 0, st, 
+      (const T*)md->grid_ps[lev], md->diag + (size_t)4 * E * nd * m->nlat, nps));
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;
 }
@@ -1337,7 +1343,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ia.robert = md->P.robert_coef;
   // vertical algebra in the state precision (FP64 algebra on the FP32 path measured no more
   // accurate: its error is set by FP32 storage); the wave-matrix solve is FP64 in both
-  k_hs_implicit<T, T><<<dim3((md->npairs + 7) / 8, E), 256, 0, st>>>(ia, md->d_vc);
+  JG_CUDA(launch_pdl(k_hs_implicit<T, T>, dim3((md->npairs + 7) / 8, E), 256, 0, st, ia, md->d_vc));
   mark(st);
   JG_CUDA(cudaGetLastError());
   // 5. back to the grid: vor, div, u, v, T, lnps (+ ps = exp(lnps))
@@ -1394,14 +1400,14 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
     JG_CUDA(cudaEventRecord(md->ev_fork, st));
     JG_CUDA(cudaStreamWaitEvent(br, md->ev_fork, 0));
   }
-  k_hs_corr_reduce<T><<<dim3((m->nlon + 31) / 32, m->nlat, E), 256, 0, st>>>(ca, md->d_vc);
+  JG_CUDA(launch_pdl(k_hs_corr_reduce<T>, dim3((m->nlon + 31) / 32, m->nlat, E), 256, 0, st, ca, md->d_vc));
   mark(st);
   JG_CUDA(cudaGetLastError());
   const size_t G1 = grid_elems(m, 1);
   int nb = (int)(((size_t)nd * G1 + 255) / 256);
   if (nb * E > 8 * 152) nb = (8 * 152 + E - 1) / E;
-  k_hs_corr_apply<T><<<dim3(nb, E), 256, 0, st>>>((T*)md->grid_t[n], (T*)md->grid_ps[n], md->d_scalars,
-                                                  (size_t)nd * G1, G1);
+  JG_CUDA(launch_pdl(k_hs_corr_apply<T>, dim3(nb, E), 256, 0, st, (T*)md->grid_t[n], (T*)md->grid_ps[n], md->d_scalars,
+                                                  (size_t)nd * G1, G1));
   mark(st);
   JG_CUDA(cudaGetLastError());
   JG_TRY(issue_hs_grad<T>(md, n, br));

@@ -16,6 +16,7 @@
 //                    Robert-Asselin filter and the shallow-water semi-implicit correction).
 // Spectral prologues build the inputs of the synthesis on the fly from neighbouring total
 // wavenumbers (gradient, Compute_Gradient_Cos! :655-692; ucos/vcos, :517-580).
+#include <cstdlib>
 #include <algorithm>
 #include <cmath>
 #include <mutex>
@@ -25,6 +26,12 @@
 #include "transform_ops.cuh"
 
 namespace jgcm {
+
+// programmatic dependent launch of the step kernels (JGCM_PDL=0 turns it off)
+int g_pdl = [] {
+  const char* e = std::getenv("JGCM_PDL");
+  return (e && e[0] == '0') ? 0 : 1;
+}();
 
 __host__ __device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 __device__ __forceinline__ int brev(int x, int logn) { return (int)(__brev((unsigned)x) >> (32 - logn)); }
@@ -63,6 +70,7 @@ __device__ __forceinline__ void fft_stages(T* re, T* im, const T* tw, int nrow, 
 template <typename T>
 __global__ void __launch_bounds__(256) k_s2g_legendre(S2GPlan plan, Tables<T> tb, V2<T>* __restrict__ F, int ns,
                                                       int nlat, int CT) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using V = V2<T>;
   extern __shared__ __align__(16) unsigned char smem[];
   const int m = blockIdx.y;
@@ -194,6 +202,7 @@ __device__ __forceinline__ T fft_load(const FFTPlan& plan, const GridInGroup& g,
 template <typename T>
 __global__ void __launch_bounds__(256) k_ifft(IFFTPlan plan, Tables<T> tb, const V2<T>* __restrict__ F, int N,
                                               int nlat, int nlon, int logh, int CT) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using V = V2<T>;
   extern __shared__ __align__(16) unsigned char smem[];
   const int h = nlon >> 1;
@@ -247,6 +256,7 @@ __global__ void __launch_bounds__(256) k_ifft(IFFTPlan plan, Tables<T> tb, const
 template <typename T>
 __global__ void __launch_bounds__(256) k_fft(FFTPlan plan, Tables<T> tb, V2<T>* __restrict__ F, int N, int nlat,
                                              int nlon, int logh, int CT) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using V = V2<T>;
   extern __shared__ __align__(16) unsigned char smem[];
   const int h = nlon >> 1;
@@ -391,6 +401,7 @@ __device__ __forceinline__ void warp_fft_dif(T (&re)[V], T (&im)[V], const T* tw
 template <typename T, int V>
 __global__ void __launch_bounds__(256) k_ifft_w(IFFTPlan plan, Tables<T> tb, const V2<T>* __restrict__ F, int N,
                                                 int nlat, int nlon) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using Vc = V2<T>;
   constexpr int H = 32 * V, LOGH = (V == 1 ? 5 : V == 2 ? 6 : V == 4 ? 7 : V == 8 ? 8 : 9);
   extern __shared__ __align__(16) unsigned char smem[];
@@ -437,6 +448,7 @@ __global__ void __launch_bounds__(256) k_ifft_w(IFFTPlan plan, Tables<T> tb, con
 template <typename T, int V>
 __global__ void __launch_bounds__(256) k_fft_w(FFTPlan plan, Tables<T> tb, V2<T>* __restrict__ F, int N, int nlat,
                                                int nlon) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using Vc = V2<T>;
   constexpr int H = 32 * V, LOGH = (V == 1 ? 5 : V == 2 ? 6 : V == 4 ? 7 : V == 8 ? 8 : 9);
   extern __shared__ __align__(16) unsigned char smem[];
@@ -491,6 +503,7 @@ __global__ void __launch_bounds__(256) k_fft_w(FFTPlan plan, Tables<T> tb, V2<T>
 template <typename T>
 __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb, const V2<T>* __restrict__ F,
                                                       int ns, int nlat, int Cin, int CT, int stage) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using V = V2<T>;
   extern __shared__ __align__(16) unsigned char smem[];
   const int m = blockIdx.y;
@@ -693,7 +706,7 @@ static int launch_s2g_into(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, 
   } else {
     size_t sm1 = align16((size_t)(m->ns + 1) * nh * sizeof(T)) + (size_t)(m->ns + 1) * ct * sizeof(V);
     dim3 g1((sp.C + ct - 1) / ct, m->N + 1);
-    k_s2g_legendre<T><<<g1, 256, sm1, st>>>(sp, tb, fbuf, m->ns, m->nlat, ct);
+    JG_CUDA(launch_pdl(k_s2g_legendre<T>, g1, 256, sm1, st, sp, tb, fbuf, m->ns, m->nlat, ct));
     mark(st);
     JG_CUDA(cudaGetLastError());
   }
@@ -711,11 +724,11 @@ static int launch_ifft_stage(jgcm_mesh* m, const IFFTPlan& ip, cudaStream_t st, 
     const size_t smw = (size_t)(m->N + 1) * FW_COLS * sizeof(V);
     dim3 gw((ip.C + FW_COLS - 1) / FW_COLS, m->nlat);
     switch (m->nlon) {
-      case 64: k_ifft_w<T, 1><<<gw, 256, smw, st>>>(ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon); break;
-      case 128: k_ifft_w<T, 2><<<gw, 256, smw, st>>>(ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon); break;
-      case 256: k_ifft_w<T, 4><<<gw, 256, smw, st>>>(ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon); break;
-      case 512: k_ifft_w<T, 8><<<gw, 256, smw, st>>>(ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon); break;
-      default: k_ifft_w<T, 16><<<gw, 256, smw, st>>>(ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon); break;
+      case 64: JG_CUDA(launch_pdl(k_ifft_w<T, 1>, gw, 256, smw, st, ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon)); break;
+      case 128: JG_CUDA(launch_pdl(k_ifft_w<T, 2>, gw, 256, smw, st, ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon)); break;
+      case 256: JG_CUDA(launch_pdl(k_ifft_w<T, 4>, gw, 256, smw, st, ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon)); break;
+      case 512: JG_CUDA(launch_pdl(k_ifft_w<T, 8>, gw, 256, smw, st, ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon)); break;
+      default: JG_CUDA(launch_pdl(k_ifft_w<T, 16>, gw, 256, smw, st, ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon)); break;
     }
     mark(st);
     JG_CUDA(cudaGetLastError());
@@ -723,7 +736,7 @@ static int launch_ifft_stage(jgcm_mesh* m, const IFFTPlan& ip, cudaStream_t st, 
   }
   size_t sm2 = align16((size_t)(fc * m->nlon + m->nlon) * sizeof(T)) + (size_t)(m->N + 1) * fc * sizeof(V);
   dim3 g2((ip.C + fc - 1) / fc, m->nlat);
-  k_ifft<T><<<g2, 256, sm2, st>>>(ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon, m->logn - 1, fc);
+  JG_CUDA(launch_pdl(k_ifft<T>, g2, 256, sm2, st, ip, tb, (const V*)fbuf, m->N, m->nlat, m->nlon, m->logn - 1, fc));
   mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;
@@ -766,11 +779,11 @@ int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp, cudaStream_t st, void* fbuf
     const size_t smw = ((size_t)FW_COLS * (m->nlon / 2) + (size_t)(m->N + 1) * FW_COLS) * sizeof(V);
     dim3 gw((fp.C + FW_COLS - 1) / FW_COLS, m->nlat);
     switch (m->nlon) {
-      case 64: k_fft_w<T, 1><<<gw, 256, smw, st>>>(fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon); break;
-      case 128: k_fft_w<T, 2><<<gw, 256, smw, st>>>(fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon); break;
-      case 256: k_fft_w<T, 4><<<gw, 256, smw, st>>>(fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon); break;
-      case 512: k_fft_w<T, 8><<<gw, 256, smw, st>>>(fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon); break;
-      default: k_fft_w<T, 16><<<gw, 256, smw, st>>>(fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon); break;
+      case 64: JG_CUDA(launch_pdl(k_fft_w<T, 1>, gw, 256, smw, st, fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon)); break;
+      case 128: JG_CUDA(launch_pdl(k_fft_w<T, 2>, gw, 256, smw, st, fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon)); break;
+      case 256: JG_CUDA(launch_pdl(k_fft_w<T, 4>, gw, 256, smw, st, fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon)); break;
+      case 512: JG_CUDA(launch_pdl(k_fft_w<T, 8>, gw, 256, smw, st, fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon)); break;
+      default: JG_CUDA(launch_pdl(k_fft_w<T, 16>, gw, 256, smw, st, fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon)); break;
     }
     mark(st);
     JG_CUDA(cudaGetLastError());
@@ -778,7 +791,7 @@ int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp, cudaStream_t st, void* fbuf
   }
   size_t sm = (size_t)(fc * m->nlon + m->nlon) * sizeof(T);
   dim3 g((fp.C + fc - 1) / fc, m->nlat);
-  k_fft<T><<<g, 256, sm, st>>>(fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon, m->logn - 1, fc);
+  JG_CUDA(launch_pdl(k_fft<T>, g, 256, sm, st, fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon, m->logn - 1, fc));
   mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;
@@ -803,7 +816,7 @@ int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp, cudaStream_t 
   const int stage = sm + tab <= kSmemBudget;
   if (stage) sm += tab;
   dim3 g((gp.C + ct - 1) / ct, m->N + 1);
-  k_g2s_legendre<T><<<g, 256, sm, st>>>(gp, tb, (const V*)fbuf, m->ns, m->nlat, fp.C, ct, stage);
+  JG_CUDA(launch_pdl(k_g2s_legendre<T>, g, 256, sm, st, gp, tb, (const V*)fbuf, m->ns, m->nlat, fp.C, ct, stage));
   mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;
