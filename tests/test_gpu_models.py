@@ -236,3 +236,29 @@ def test_packed_state_transfer(jg, prec):
         mdl.step(3)
     for k in jg.STATE_FIELDS:
         assert np.array_equal(b.get(k), c.get(k)), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_gpu_rh4_phase_speed_and_steady_zonal_flow(jg, prec):
+    """The analytic checks of the oracle on the library: the Rossby-Haurwitz wave 4 moves at the
+    analytic speed (Barotropic T42), and Williamson test case 2 stays steady (shallow water T42)."""
+    from test_oracle import (SW_TC2, init_sw_steady_zonal_flow, rh4_analytic_speed, rh4_phase_speed,
+                             sw_tc2_params)
+
+    name = "barotropic_t42"
+    M = configs.make_mesh(jg, name, precision=prec)
+    md = jg.Model(M, configs.PARAMS[name])
+    nu = rh4_phase_speed(jg, M, md)
+    ref = rh4_analytic_speed(configs.PARAMS[name]["omega"])
+    assert abs(nu - ref) / ref < 1e-3, (nu, ref)
+    g = SW_TC2
+    M2 = jg.Spectral_Spherical_Mesh(g["num_fourier"], g["num_fourier"] + 1, g["nlat"], g["nlon"], 1, g["radius"],
+                                    precision=prec)
+    sw = jg.Model(M2, sw_tc2_params())
+    h0 = init_sw_steady_zonal_flow(jg, M2, sw)
+    u0 = sw.get("grid_u_c")
+    sw.step(72)
+    tol = 1e-8 if prec == "fp64" else 1e-4
+    assert np.abs(sw.get("grid_ps_c") - h0).max() / (h0.max() - h0.min()) < tol
+    assert np.abs(sw.get("grid_u_c") - u0).max() / np.abs(u0).max() < tol
