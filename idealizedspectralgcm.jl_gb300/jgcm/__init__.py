@@ -355,6 +355,19 @@ class Model:
         out = out.reshape(shape, order="F")
         return (out[..., 0] if self.members == 1 else out), int(steps.value)
 
+    DIAGNOSTICS = ("t_zonal_mean", "t_eq_zonal_mean", "u_zonal_mean", "v_zonal_mean", "ps_mean")
+
+    def write_diagnostics(self, path):
+        """Write the current diagnostic means to ``path`` (raw little-endian FP64, the arrays back to
+        back in Julia column-major order: read in Julia with ``read!(io, Array{Float64}(undef,
+        shape...))``) and ``path + ".json"`` (names, shapes, byte offsets, steps summed, mesh), the
+        output of Output_Manager.jl:81-145 without its plots."""
+        return write_arrays(path, {k: self.read_diagnostics(k)[0] for k in self.DIAGNOSTICS},
+                            {"steps": self.read_diagnostics("ps_mean")[1], "members": self.members,
+                             "mesh": {"num_fourier": self.mesh.num_fourier, "nlat": self.mesh.nlat,
+                                      "nlon": self.mesh.nlon, "nd": self.mesh.nd},
+                             "latitudes_deg": [float(x) for x in np.degrees(np.arcsin(self.mesh.sinth))]})
+
     def copy_member(self, member: int, src: "Model", src_member: int = 0):
         """Member `member` of this model <- member `src_member` of `src` (same mesh and kind)."""
         _check(lib().jgcm_model_copy_member(self._h, int(member), src._h, int(src_member)))
@@ -525,6 +538,40 @@ class Ensemble:
 
 
 TUNING_KNOBS = ("lanes_per_column", "s2g_columns", "g2s_columns", "fft_columns", "simt_legendre")
+
+
+def write_arrays(path, arrays, meta=None):
+    """Raw FP64 dump: ``path`` holds the arrays back to back (Fortran order, little-endian),
+    ``path + ".json"`` their names, shapes and byte offsets plus ``meta``.  Returns the header."""
+    import json
+
+    header = {"format": "raw float64 little-endian, column-major arrays back to back", "arrays": []}
+    off = 0
+    with open(path, "wb") as f:
+        for name, a in arrays.items():
+            a = np.asarray(a, dtype="<f8")
+            f.write(np.asfortranarray(a).tobytes(order="F"))
+            header["arrays"].append({"name": name, "shape": list(a.shape), "offset_bytes": off})
+            off += a.nbytes
+    header.update(meta or {})
+    with open(path + ".json", "w") as f:
+        json.dump(header, f, indent=1)
+    return header
+
+
+def read_arrays(path):
+    """Inverse of write_arrays: dict name -> array, and the header."""
+    import json
+
+    with open(path + ".json") as f:
+        header = json.load(f)
+    raw = np.fromfile(path, dtype="<f8")
+    out = {}
+    for e in header["arrays"]:
+        n = int(np.prod(e["shape"]))
+        o = e["offset_bytes"] // 8
+        out[e["name"]] = raw[o:o + n].reshape(e["shape"], order="F")
+    return out, header
 
 
 def get_tuning(model):

@@ -176,7 +176,7 @@ def test_hs_forcing_entry_point(jg, orc, prec, tol):
 
 
 @pytest.mark.parametrize("members", [1, 2])
-def test_on_device_zonal_mean_diagnostics(jg, members):
+def test_on_device_zonal_mean_diagnostics(jg, members, tmp_path):
     """Update_Output! (Output_Manager.jl:81-107) as on-device FP64 sums: the means over the steps
     equal the zonal means of the fields read back after every step."""
     name = "hs_t21l10"
@@ -208,6 +208,13 @@ def test_on_device_zonal_mean_diagnostics(jg, members):
         got, steps = md.read_diagnostics(key)
         assert steps == nsteps
         assert configs.rel_l2(got, w / nsteps) < 1e-12, key
+    # the file dump (raw FP64 + JSON header) holds the same means
+    path = str(tmp_path / "diag.bin")
+    head = md.write_diagnostics(path)
+    back, _ = jg.read_arrays(path)
+    assert head["steps"] == nsteps
+    for key in want:
+        assert np.array_equal(back[key], md.read_diagnostics(key)[0]), key
 
 
 @pytest.mark.gpu

@@ -271,3 +271,19 @@ def test_packed_state_layout_round_trip():
     back = jgcm.unpack_state(mesh, packed)
     for k in jgcm.STATE_FIELDS:
         assert np.array_equal(back[k], fields[k]), k
+
+
+def test_raw_array_dump_round_trip(tmp_path):
+    """write_arrays / read_arrays (the diagnostics dump): Fortran-order FP64 arrays back to back."""
+    import jgcm
+
+    rng = np.random.default_rng(1)
+    arrays = {"t_zonal_mean": rng.standard_normal((8, 3)), "ps_mean": rng.standard_normal((16, 8))}
+    path = str(tmp_path / "diag.bin")
+    head = jgcm.write_arrays(path, arrays, {"steps": 12})
+    back, head2 = jgcm.read_arrays(path)
+    assert head2 == head and head["steps"] == 12
+    for k, v in arrays.items():
+        assert np.array_equal(back[k], v)
+    raw = np.fromfile(path, dtype="<f8")
+    assert np.array_equal(raw[:24], arrays["t_zonal_mean"].ravel(order="F"))
