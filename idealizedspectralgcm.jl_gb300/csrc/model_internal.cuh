@@ -65,7 +65,9 @@ struct jgcm_model {
   double *d_partials, *d_scalars;
   unsigned* d_counter;
   double* state_stage;  // FP64 staging of the packed host state (jgcm_model_set_state / get_state)
-  cudaGraphExec_t graph[3];
+  cudaGraphExec_t graph[3];   // one steady step, per rotation phase
+  cudaGraphExec_t graph3[3];  // three steady steps (a whole rotation), per starting phase
+  cudaGraphExec_t graph24[3]; // twenty-four steady steps (eight rotations), per starting phase
   cudaEvent_t ev0, ev1;
 };
 

@@ -861,6 +861,8 @@ void model_free(jgcm_model* md) {
     for (auto p : ps)
       if (p) cudaFree(p);
     if (md->graph[i]) cudaGraphExecDestroy(md->graph[i]);
+    if (md->graph3[i]) cudaGraphExecDestroy(md->graph3[i]);
+    if (md->graph24[i]) cudaGraphExecDestroy(md->graph24[i]);
   }
   void* ps[] = {md->grid_vor, md->grid_div, md->grid_lnps, md->grid_t_eq, md->grid_geopots, md->grid_h_eq,
                 md->spe_zero, md->spe_dvor, md->spe_ddiv, md->spe_dlnps, md->spe_dt, md->g_dlps, md->g_dtps,
@@ -1451,6 +1453,16 @@ void drop_graphs(jgcm_model* md) {
       cudaGraphExecDestroy(g);
       g = nullptr;
     }
+  for (auto& g : md->graph3)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  for (auto& g : md->graph24)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
 }
 
 int graph_step(jgcm_model* md) {
@@ -1478,6 +1490,54 @@ int graph_step(jgcm_model* md) {
   after_step(md);
   return JGCM_OK;
 }
+
+// K steady steps through one CUDA graph (K a multiple of 3: whole time-level rotations): fewer graph
+// launches, and the step boundaries inside become ordinary (programmatic) kernel edges.
+bool steady(const jgcm_model* md) {
+  return !(md->init_step || md->sw_adv_from_n || (md->P.kind == JGCM_HELD_SUAREZ && !md->grad_ready));
+}
+
+int graph_steps(jgcm_model* md, int K, cudaGraphExec_t* slots) {
+  jgcm_mesh* m = md->mesh;
+  if (md->graph_gen != m->tune_gen) {
+    drop_graphs(md);
+    md->graph_gen = m->tune_gen;
+  }
+  const int ph = md->rot;
+  if (!slots[ph]) {
+    // capture: the host-side bookkeeping of the three steps is replayed below, so restore it after
+    const int rot = md->rot, gr = md->grad_ready, init = md->init_step, adv = md->sw_adv_from_n;
+    const int done = md->steps_done;
+    const long dsteps = md->diag_steps;
+    cudaGraph_t g;
+    JG_CUDA(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+    int s = JGCM_OK;
+    for (int k = 0; k < K && s == JGCM_OK; k++) {
+      s = issue(md, m->stream);
+      after_step(md);
+    }
+    cudaError_t e = cudaStreamEndCapture(m->stream, &g);
+    md->rot = rot;
+    md->grad_ready = gr;
+    md->init_step = init;
+    md->sw_adv_from_n = adv;
+    md->steps_done = done;
+    md->diag_steps = dsteps;
+    if (s != JGCM_OK) {
+      if (e == cudaSuccess) cudaGraphDestroy(g);
+      return s;
+    }
+    JG_CUDA(e);
+    cudaError_t e2 = cudaGraphInstantiate(&slots[ph], g, 0);
+    cudaGraphDestroy(g);
+    JG_CUDA(e2);
+  }
+  JG_CUDA(cudaGraphLaunch(slots[ph], m->stream));
+  for (int k = 0; k < K; k++) after_step(md);
+  return JGCM_OK;
+}
+int graph_step3(jgcm_model* md) { return graph_steps(md, 3, md->graph3); }
+int graph_step24(jgcm_model* md) { return graph_steps(md, 24, md->graph24); }
 
 int model_step(jgcm_model* md) {
   if (md->init_step || md->sw_adv_from_n || (md->P.kind == JGCM_HELD_SUAREZ && !md->grad_ready)) {
@@ -1603,7 +1663,18 @@ extern "C" int jgcm_model_destroy(jgcm_model* md) {
 
 extern "C" int jgcm_model_step(jgcm_model* md, int nsteps) {
   JG_ARG(md && nsteps >= 0, "bad arguments");
-  for (int s = 0; s < nsteps; s++) JG_TRY(model_step(md));
+  for (int s = 0; s < nsteps;) {
+    if (nsteps - s >= 24 && steady(md)) {
+      JG_TRY(graph_step24(md));
+      s += 24;
+    } else if (nsteps - s >= 3 && steady(md)) {
+      JG_TRY(graph_step3(md));
+      s += 3;
+    } else {
+      JG_TRY(model_step(md));
+      s++;
+    }
+  }
   JG_CUDA(cudaStreamSynchronize(md->mesh->stream));
   if (md->mesh->tc.on) JG_TRY(tc_status(md->mesh));  // a tensor-core kernel whose bounded wait gave up
   return JGCM_OK;
@@ -1732,12 +1803,32 @@ extern "C" int jgcm_model_time_steps(jgcm_model* md, int nsteps, float* ms) {
     if (md->graph_gen != m->tune_gen) return false;
     for (auto g : md->graph)
       if (!g) return false;
+    for (auto g : md->graph3)
+      if (!g) return false;
+    if (nsteps >= 24)
+      for (auto g : md->graph24)
+        if (!g) return false;
     return true;
   };
-  for (int s = 0; s < 3 && !captured(); s++) JG_TRY(graph_step(md));
+  for (int s = 0; s < 3 && !captured(); s++) {
+    JG_TRY(graph_step(md));
+    JG_TRY(graph_step3(md));
+    if (nsteps >= 24) JG_TRY(graph_step24(md));
+  }
   JG_CUDA(cudaStreamSynchronize(m->stream));
   JG_CUDA(cudaEventRecord(md->ev0, m->stream));
-  for (int s = 0; s < nsteps; s++) JG_TRY(graph_step(md));
+  for (int s = 0; s < nsteps;) {
+    if (nsteps - s >= 24) {
+      JG_TRY(graph_step24(md));
+      s += 24;
+    } else if (nsteps - s >= 3) {
+      JG_TRY(graph_step3(md));
+      s += 3;
+    } else {
+      JG_TRY(graph_step(md));
+      s++;
+    }
+  }
   JG_CUDA(cudaEventRecord(md->ev1, m->stream));
   JG_CUDA(cudaEventSynchronize(md->ev1));
   JG_CUDA(cudaEventElapsedTime(ms, md->ev0, md->ev1));
