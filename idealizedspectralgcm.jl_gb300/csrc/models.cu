@@ -2515,7 +2515,8 @@ extern "C" int jgcm_model_autotune(jgcm_model* md, int nsteps, int* knobs_out, f
       {0, 1}};
   if (md->P.kind != JGCM_HELD_SUAREZ) cand[0] = {cur[0]};
   if (!m->tc.on) cand[4] = {cur[4]};  // the Legendre engine: tensor cores or SIMT (tensor-core modes)
-  for (int knob = 0; knob < 5; knob++)
+  // the Legendre engine first: the SIMT tiles searched next only matter once the engine is known
+  for (int knob : {4, 0, 1, 2, 3})
     for (int v : cand[knob]) {
       int k[5] = {cur[0], cur[1], cur[2], cur[3], cur[4]};
       k[knob] = v;
