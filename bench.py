@@ -295,6 +295,19 @@ def ensemble_bench(jgcm, configs, precisions, days=2):
             t = sum(ens.time_steps(spd) for _ in range(days)) / 1000.0
             per[name] = {"member_sim_days_per_s": E * days / t, "ms_per_step": 1000.0 * t / (days * spd),
                          "tuning": tuned}
+            if params["kind"] == "held_suarez":
+                # the dominant kernel at ensemble scale: E members' algorithmic bytes per launch over
+                # its CUDA-event launch time (eager steps), against the measured HBM copy bandwidth
+                kt = ens.kernel_times(spd)
+                dom = max(kt, key=kt.get)
+                g = configs.GRIDS[name]
+                alg = E * algorithmic_bytes(dom, g["num_fourier"], g["nlat"], g["nlon"], g["nd"],
+                                            8 if prec == "fp64" else 4)
+                peak, kind = measured_peaks()
+                ach = alg / (kt[dom] * 1e-3) / 1e9
+                per[name]["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak,
+                                         "unit": "GB/s", "frac": ach / peak, "peak_kind": kind,
+                                         "algorithmic_bytes": alg, "launch_ms": kt[dom]}
             models.append(ens)
             owned.append(m)
         group = jgcm.Ensemble(models, 1200)

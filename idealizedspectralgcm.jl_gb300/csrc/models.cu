@@ -173,10 +173,30 @@ __device__ __forceinline__ R seg_excl_suffix(R x, int s) {  // sum over the lane
 
 template <typename T, int S>
 __global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertCoef* __restrict__ vcp) {
-  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const VertCoef& vc = *vcp;
   __shared__ double red[2][HS_CT / 32];
+  // the vertical coefficients in the state precision, staged once per block (constants: staged
+  // before the dependency wait; on the FP32 path this also keeps the FP64 -> FP32 conversions out of
+  // the level loops)
+  __shared__ T s_dak[JGCM_MAX_ND], s_dbk[JGCM_MAX_ND], s_bk[JGCM_MAX_ND + 1], s_cf[JGCM_MAX_ND],
+      s_dlpp[JGCM_MAX_ND], s_dlpm[JGCM_MAX_ND], s_dlp[JGCM_MAX_ND], s_sf[JGCM_MAX_ND];
+  __shared__ T s_lb1;
   const int nd = a.nd, nlon = a.nlon, nlat = a.nlat;
+  for (int q = threadIdx.x; q <= nd; q += blockDim.x) {
+    s_bk[q] = (T)vc.bk[q];
+    if (q < nd) {
+      s_dak[q] = (T)vc.dak[q];
+      s_dbk[q] = (T)vc.dbk[q];
+      s_cf[q] = (T)vc.cf[q];
+      s_dlpp[q] = (T)vc.dlp_p[q];
+      s_dlpm[q] = (T)vc.dlp_m[q];
+      s_dlp[q] = (T)vc.dlp[q];
+      s_sf[q] = (T)vc.sf[q];
+    }
+  }
+  if (threadIdx.x == 0) s_lb1 = (T)vc.lb[1];
+  __syncthreads();
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const int seg = threadIdx.x % S, i = blockIdx.x * (HS_CT / S) + threadIdx.x / S, j = blockIdx.y, e = blockIdx.z;
   const int len = (nd + S - 1) / S, k0 = min(nd, seg * len), k1 = min(nd, k0 + len);
   const bool act = i < nlon;
@@ -210,9 +230,9 @@ __global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertC
     for (int k = k0; k < k1; k++) {
       const size_t x = (size_t)k * G;
       const T t = t_c[x], u = u_c[x], v = v_c[x], dvg = dvgp[x];
-      const T dlnp = k == 0 ? (T)vc.lb[1] + lnps : (T)vc.dlp[k];
+      const T dlnp = k == 0 ? s_lb1 + lnps : s_dlp[k];
       termS += R * (t - (T)a.t_spec[e * nd + k].x) * dlnp;
-      dmeanS += dvg * ((T)vc.dak[k] + (T)vc.dbk[k] * ps) + (T)vc.dbk[k] * (u * dlps + v * dtps);
+      dmeanS += dvg * (s_dak[k] + s_dbk[k] * ps) + s_dbk[k] * (u * dlps + v * dtps);
     }
   const T tot = seg_sum<S>(dmeanS);
   T rs = seg_excl_suffix<S>(termS, seg);  // sum_{r >= k1} R (T_r - T0_r) dlnp_r
@@ -222,8 +242,8 @@ __global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertC
       const size_t x = (size_t)k * G;
       const T t = t_c[x], u = u_c[x], v = v_c[x];
       const T tdev = t - (T)a.t_spec[e * nd + k].x;
-      const T dlnp = k == 0 ? (T)vc.lb[1] + lnps : (T)vc.dlp[k];
-      a.energy[cL + x] = gs + rs + R * tdev * (T)vc.dlp_p[k] + (T)0.5 * (u * u + v * v);
+      const T dlnp = k == 0 ? s_lb1 + lnps : s_dlp[k];
+      a.energy[cL + x] = gs + rs + R * tdev * s_dlpp[k] + (T)0.5 * (u * u + v * v);
       rs += R * tdev * dlnp;
     }
   // ---- pass 2, top-down within the segment
@@ -231,11 +251,11 @@ __global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertC
   if (act && k0 < k1) {
     T incl = incl0, Mlo = 0, flu = 0, flv = 0, flt = 0;  // M and the advective fluxes at k0-1/2
     T u = u_c[(size_t)k0 * G], v = v_c[(size_t)k0 * G], t = t_c[(size_t)k0 * G];
-    T dp = (T)vc.dak[k0] + (T)vc.dbk[k0] * ps;
+    T dp = s_dak[k0] + s_dbk[k0] * ps;
     if (k0 > 0) {  // the level above the segment: M_{k0-1/2} and its fluxes
       const size_t x = (size_t)(k0 - 1) * G;
-      const T um = u_c[x], vm = v_c[x], tm = t_c[x], dpm = (T)vc.dak[k0 - 1] + (T)vc.dbk[k0 - 1] * ps;
-      Mlo = -incl0 + tot * (T)vc.bk[k0];
+      const T um = u_c[x], vm = v_c[x], tm = t_c[x], dpm = s_dak[k0 - 1] + s_dbk[k0 - 1] * ps;
+      Mlo = -incl0 + tot * s_bk[k0];
       const T w = dpm / (dpm + dp);
       flu = Mlo * (um + (u - um) * w);
       flv = Mlo * (vm + (v - vm) * w);
@@ -251,15 +271,15 @@ __global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertC
         u1 = u_c[x + G];
         v1 = v_c[x + G];
         t1 = t_c[x + G];
-        dp1 = (T)vc.dak[k + 1] + (T)vc.dbk[k + 1] * ps;
+        dp1 = s_dak[k + 1] + s_dbk[k + 1] * ps;
       }
       const T rdp = (T)1 / dp;
-      const T lnpf = (T)vc.cf[k] + lnps;
-      const T dlnp_p = (T)vc.dlp_p[k];                 // ln p_{k+1/2} - ln p_k
-      const T dlnp_m = k == 0 ? lnpf : (T)vc.dlp_m[k];  // ln p_k - ln p_{k-1/2} (ln p_{1/2} = 0)
-      const T dlnp = k == 0 ? (T)vc.lb[1] + lnps : (T)vc.dlp[k];
+      const T lnpf = s_cf[k] + lnps;
+      const T dlnp_p = s_dlpp[k];                 // ln p_{k+1/2} - ln p_k
+      const T dlnp_m = k == 0 ? lnpf : s_dlpm[k];  // ln p_k - ln p_{k-1/2} (ln p_{1/2} = 0)
+      const T dlnp = k == 0 ? s_lb1 + lnps : s_dlp[k];
       // HS_Forcing! on the previous level (sigma = p_k / ps = sf[k])
-      const T sg = (T)vc.sf[k] - sb;
+      const T sg = s_sf[k] - sb;
       const T smax = sg > (T)0 ? sg : (T)0;
       const T k_v = kv0 * smax;
       T du = -k_v * up, dv = -k_v * vp;
@@ -271,20 +291,20 @@ __global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertC
       // Compute_Corrections_Init: column energy integral with ps_p in the state precision
       {
         const T ua = up + tDt * du, va = vp + tDt * dv;
-        col_e += ((T)0.5 * (ua * ua + va * va) + cp * (tp + tDt * dt)) * ((T)vc.dak[k] + (T)vc.dbk[k] * psp);
+        col_e += ((T)0.5 * (ua * ua + va * va) + cp * (tp + tDt * dt)) * (s_dak[k] + s_dbk[k] * psp);
       }
       // Four_In_One! (Spectral_Dynamics.jl:88-183)
-      const T x1 = ((T)vc.bk[k] * dlnp_m + (T)vc.bk[k + 1] * dlnp_p) * rdp;
+      const T x1 = (s_bk[k] * dlnp_m + s_bk[k + 1] * dlnp_p) * rdp;
       const T dlnp_dl = x1 * dlps, dlnp_dt = x1 * dtps;
       du = du - R * t * dlnp_dl;
       dv = dv - R * t * dlnp_dt;
-      const T dmean = dvg * dp + (T)vc.dbk[k] * (u * dlps + v * dtps);
+      const T dmean = dvg * dp + s_dbk[k] * (u * dlps + v * dtps);
       const T excl = incl;
       incl += dmean;
       const T x5 = -(excl * dlnp + dmean * dlnp_p) * rdp + u * dlnp_dl + v * dlnp_dt;
       dt = dt + kap * t * x5;
       // M_{k+1/2} = -sum_{r<=k} D_r + B_{k+1/2} sum_r D_r, zero at the surface
-      const T Mhi = below ? -incl + tot * (T)vc.bk[k + 1] : (T)0;
+      const T Mhi = below ? -incl + tot * s_bk[k + 1] : (T)0;
       // Vert_Advection! (second_centered_wts): flux at k+1/2 with weight dp_k / (dp_k + dp_{k+1})
       const T w1 = dp / (dp + dp1);
       const T fhu = below ? Mhi * (u + (u1 - u) * w1) : (T)0;
@@ -549,6 +569,12 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   // ks, ks + 8, ... of the 32 columns (coalesced rows); column partial sums in the state precision,
   // folded across level groups and columns in FP64 in a fixed order
   constexpr int KS = 8;
+  __shared__ T s_dak[JGCM_MAX_ND], s_dbk[JGCM_MAX_ND];  // the layer coefficients in the state precision
+  for (int q = threadIdx.x; q < a.nd; q += blockDim.x) {
+    s_dak[q] = (T)vc.dak[q];
+    s_dbk[q] = (T)vc.dbk[q];
+  }
+  __syncthreads();
   const int i = blockIdx.x * 32 + (threadIdx.x & 31), ks = threadIdx.x >> 5, j = blockIdx.y, nd = a.nd;
   const int e = blockIdx.z;  // member
   const bool act = i < a.nlon;
@@ -562,8 +588,8 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
       size_t x = offL + (size_t)k * G + col;
       T u = a.u_n[x], v = a.v_n[x], t = a.t_n[x];
       T E = (T)0.5 * (u * u + v * v) + cp * t;
-      ea += E * (T)vc.dak[k];
-      eb += E * (T)vc.dbk[k];
+      ea += E * s_dak[k];
+      eb += E * s_dbk[k];
     }
   }
   part[0][ks][threadIdx.x & 31] = ea;
