@@ -405,25 +405,49 @@ struct CX {
 };
 
 // Linear_Ps_T_δdiv! (Semi_Implicit.jl:271-341) for one (m,n) column held one level per lane.
+// The semi-implicit kernel's per-level reference-column constants in the vertical-algebra precision R,
+// staged once per block (the same FP64 expressions, rounded once instead of in every warp)
 template <typename R>
-__device__ __forceinline__ void linear_ps_t(const VertCoef& vc, int lane, int nd, R kappa, CX<R> d, CX<R>& dps,
+struct VertR {
+  R dpr[JGCM_MAX_ND], rdpr[JGCM_MAX_ND], dlnp[JGCM_MAX_ND], dlnpp[JGCM_MAX_ND], tref[JGCM_MAX_ND],
+      bk1[JGCM_MAX_ND], tdh[JGCM_MAX_ND], dh[JGCM_MAX_ND], df[JGCM_MAX_ND], hk[JGCM_MAX_ND];
+};
+
+template <typename R>
+__device__ __forceinline__ void stage_vert(const VertCoef& vc, int nd, double ps_ref, VertR<R>& v) {
+  for (int k = threadIdx.x; k < nd; k += blockDim.x) {
+    v.dpr[k] = (R)vc.dp_ref[k];
+    v.rdpr[k] = (R)vc.rdp_ref[k];
+    v.dlnp[k] = (R)(vc.lnph_ref[k + 1] - vc.lnph_ref[k]);
+    v.dlnpp[k] = (R)(vc.lnph_ref[k + 1] - vc.lnpf_ref[k]);
+    v.tref[k] = (R)vc.t_ref[k];
+    v.bk1[k] = (R)vc.bk[k + 1];
+    v.tdh[k] = k + 1 <= nd - 1 ? (R)(vc.t_ref[k + 1] - vc.t_ref[k]) : (R)0;
+    v.dh[k] = (R)(vc.lnph_ref[k + 1] - vc.lnph_ref[k]);
+    v.df[k] = (R)(vc.lnph_ref[k + 1] - vc.lnpf_ref[k]);
+    v.hk[k] = (R)(vc.h[k] * ps_ref);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void linear_ps_t(const VertR<R>& vr, int lane, int nd, R kappa, CX<R> d, CX<R>& dps,
                                             CX<R>& dtt) {
   const bool act = lane < nd;
   const int k = act ? lane : 0;
-  const R dpr = (R)vc.dp_ref[k], rdpr = (R)vc.rdp_ref[k];
+  const R dpr = vr.dpr[k], rdpr = vr.rdpr[k];
   CX<R> dm = {act ? d.x * dpr : (R)0, act ? d.y * dpr : (R)0};
   R ix = scan_incl<R>(dm.x, lane), iy = scan_incl<R>(dm.y, lane);
   R tx = __shfl_sync(FULL, ix, nd - 1), ty = __shfl_sync(FULL, iy, nd - 1);
   R ex = shfl_up1(ix, lane, (R)0), ey = shfl_up1(iy, lane, (R)0);
-  R dlnp = (R)(vc.lnph_ref[k + 1] - vc.lnph_ref[k]), dlnp_p = (R)(vc.lnph_ref[k + 1] - vc.lnpf_ref[k]);
-  R c = -kappa * (R)vc.t_ref[k];
+  R dlnp = vr.dlnp[k], dlnp_p = vr.dlnpp[k];
+  R c = -kappa * vr.tref[k];
   dtt.x = c * (ex * dlnp + dm.x * dlnp_p) * rdpr;
   dtt.y = c * (ey * dlnp + dm.y * dlnp_p) * rdpr;
   // M_{k+1/2} (k <= nd-2) and the centred vertical-advection term with (t_ref[k] - t_ref[k-1])
   const bool inner = lane + 1 <= nd - 1;
-  R bk1 = (R)vc.bk[k + 1];
+  R bk1 = vr.bk1[k];
   R mhx = inner ? -ix + tx * bk1 : (R)0, mhy = inner ? -iy + ty * bk1 : (R)0;
-  R tdh = inner ? (R)(vc.t_ref[k + 1] - vc.t_ref[k]) : (R)0;
+  R tdh = inner ? vr.tdh[k] : (R)0;
   R mdhx = mhx * tdh, mdhy = mhy * tdh;  // Mdt_{k+1/2}
   R mdlx = shfl_up1(mdhx, lane, (R)0), mdly = shfl_up1(mdhy, lane, (R)0);
   dtt.x = dtt.x - (R)0.5 * (mdhx + mdlx) * rdpr;
@@ -450,8 +474,11 @@ __device__ __forceinline__ void lf(int init, int Dt, R rob, R d, R f, R& dq, R q
 // R is the precision of the vertical algebra (FP64 on the FP64 path; selectable on the FP32 path).
 template <typename T, typename R>
 __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCoef* __restrict__ vcp) {
-  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const VertCoef& vc = *vcp;
+  __shared__ VertR<R> vr;
+  stage_vert<R>(vc, a.nd, a.ps_ref, vr);  // constants: staged before the dependency wait
+  __syncthreads();
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using C = CX<R>;
   const int lane = threadIdx.x & 31;
   const int pid = blockIdx.x * 8 + (threadIdx.x >> 5);
@@ -475,7 +502,7 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCo
   const R kap = (R)a.kappa, Rg = (R)a.rdgas;
   // Adjust_δlnps_δt_δdiv! :360-404
   C dps, dtmp;
-  linear_ps_t<R>(vc, lane, nd, kap, C{divp.x - divc.x, divp.y - divc.y}, dps, dtmp);
+  linear_ps_t<R>(vr, lane, nd, kap, C{divp.x - divc.x, divp.y - divc.y}, dps, dtmp);
   dtt.x = dtt.x + dtmp.x;
   dtt.y = dtt.y + dtmp.y;
   dl.x = dl.x + dps.x * rpsr;
@@ -483,13 +510,13 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCo
   C t2 = {tp.x - tc.x + xi * dtt.x, tp.y - tc.y + xi * dtt.y};
   C l2 = {lp.x - lc.x + xi * dl.x, lp.y - lc.y + xi * dl.y};
   // Linear_Geopot_δt! :213-241
-  R dh = (R)(vc.lnph_ref[k + 1] - vc.lnph_ref[k]);
+  R dh = vr.dh[k];
   R tmx = act ? Rg * (t2.x * dh) : (R)0, tmy = act ? Rg * (t2.y * dh) : (R)0;
   R rx = rscan_incl<R>(tmx, lane), ry = rscan_incl<R>(tmy, lane);
   R hx = shfl_dn1(rx, lane, nd, (R)0), hy = shfl_dn1(ry, lane, nd, (R)0);  // Φ_{k+1/2}
-  R df = (R)(vc.lnph_ref[k + 1] - vc.lnpf_ref[k]);
+  R df = vr.df[k];
   R gx = hx + Rg * (t2.x * df), gy = hy + Rg * (t2.y * df);
-  R hk = (R)(vc.h[k] * a.ps_ref);
+  R hk = vr.hk[k];
   ddiv.x = ddiv.x - eig * (gx + hk * l2.x);
   ddiv.y = ddiv.y - eig * (gy + hk * l2.y);
   // wave-matrix solve in FP64, n <= N only (Implicit_Correction! :486-497)
@@ -511,7 +538,7 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCo
     ddiv.x = act ? (R)sx : (R)0;
     ddiv.y = act ? (R)sy : (R)0;
   }
-  linear_ps_t<R>(vc, lane, nd, kap, ddiv, dps, dtmp);
+  linear_ps_t<R>(vr, lane, nd, kap, ddiv, dps, dtmp);
   dtt.x = dtt.x + xi * dtmp.x;
   dtt.y = dtt.y + xi * dtmp.y;
   dl.x = dl.x + xipsr * dps.x;
