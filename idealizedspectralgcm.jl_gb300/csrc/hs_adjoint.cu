@@ -1069,6 +1069,70 @@ extern "C" int jgcm_model_step_adjoint(jgcm_model* md, double* const* state_bar,
   return JGCM_OK;
 }
 
+namespace {
+// The workspace of the checkpointed gradient, kept in the model between calls with the same step
+// count and checkpoint interval (allocation, and the host build of the transposed vertical
+// operators, would otherwise dominate short windows).
+struct AdjContext {
+  int nsteps = 0, K = 0, nbl = 0;
+  std::vector<StateBuf> ck, seg;
+  StateBuf fin{}, bi{}, bo{};
+  AdjWork w{};
+  bool has_w = false;
+  std::vector<void*> bufs;  // every StateBuf base and scratch array
+  double *d_tgt = nullptr, *d_scal = nullptr, *part = nullptr;
+};
+
+void ctx_free(AdjContext* c) {
+  if (!c) return;
+  for (void* p : c->bufs) cudaFree(p);
+  if (c->has_w) work_free(&c->w);
+  delete c;
+}
+
+int ctx_create(jgcm_model* md, int nsteps, int K, AdjContext** out) {
+  jgcm_mesh* m = md->mesh;
+  AdjContext* c = new AdjContext();
+  c->nsteps = nsteps;
+  c->K = K;
+  const int nseg = (nsteps + K - 1) / K, segl = K < nsteps ? K : nsteps;
+  c->ck.resize(nseg);
+  c->seg.resize(segl + 1);
+  auto fail = [&](int st) {
+    ctx_free(c);
+    return st;
+  };
+  auto nb = [&](StateBuf* b) -> int {
+    const int st = state_alloc(md, b);
+    if (st == JGCM_OK) c->bufs.push_back(b->base);
+    return st;
+  };
+  for (auto& b : c->ck)
+    if (int st = nb(&b)) return fail(st);
+  for (auto& b : c->seg)
+    if (int st = nb(&b)) return fail(st);
+  for (StateBuf* b : {&c->fin, &c->bi, &c->bo})
+    if (int st = nb(b)) return fail(st);
+  if (int st = work_alloc(md, &c->w)) return fail(st);
+  c->has_w = true;
+  const size_t GL = grid_elems(m, md->nd);
+  c->nbl = (int)((GL + 255) / 256);
+  void** scratch[] = {(void**)&c->d_tgt, (void**)&c->d_scal, (void**)&c->part};
+  const size_t bytes[] = {GL * 8, (size_t)segl * 4 * 8, (size_t)c->nbl * 8};
+  for (int i = 0; i < 3; i++) {
+    if (int st = dev_alloc(scratch[i], bytes[i])) return fail(st);
+    c->bufs.push_back(*scratch[i]);
+  }
+  *out = c;
+  return JGCM_OK;
+}
+}  // namespace
+
+void jgcm::adj_context_free(jgcm_model* md) {
+  ctx_free((AdjContext*)md->adj);
+  md->adj = nullptr;
+}
+
 extern "C" int jgcm_model_hs_gradient(jgcm_model* md, int nsteps, int checkpoint_every, const double* t_target,
                                       double* loss, double* grad_spe_t0, double* grad_params) {
   JG_TRY(check_model(md));
@@ -1077,29 +1141,18 @@ extern "C" int jgcm_model_hs_gradient(jgcm_model* md, int nsteps, int checkpoint
   jgcm_mesh* m = md->mesh;
   cudaStream_t st = m->stream;
   const int nd = md->nd, K = checkpoint_every, nseg = (nsteps + K - 1) / K;
-  const int segl = K < nsteps ? K : nsteps;
-  Scope sc;
-  std::vector<StateBuf> ck(nseg), seg(segl + 1);
-  StateBuf fin, bi, bo;
-  auto nb = [&](StateBuf* b) -> int {
-    JG_TRY(state_alloc(md, b));
-    sc.p.push_back(b->base);
-    return JGCM_OK;
-  };
-  for (auto& b : ck) JG_TRY(nb(&b));
-  for (auto& b : seg) JG_TRY(nb(&b));
-  JG_TRY(nb(&fin));
-  JG_TRY(nb(&bi));
-  JG_TRY(nb(&bo));
-  AdjWork w;
-  JG_TRY(work_alloc(md, &w));
-  sc.w.push_back(w);
-  double *d_tgt = nullptr, *d_scal = nullptr;
+  AdjContext* ctx = (AdjContext*)md->adj;
+  if (!ctx || ctx->nsteps != nsteps || ctx->K != K) {
+    jgcm::adj_context_free(md);
+    JG_TRY(ctx_create(md, nsteps, K, &ctx));
+    md->adj = ctx;
+  }
+  std::vector<StateBuf>& ck = ctx->ck;
+  std::vector<StateBuf>& seg = ctx->seg;
+  StateBuf &fin = ctx->fin, &bi = ctx->bi, &bo = ctx->bo;
+  AdjWork& w = ctx->w;
+  double *d_tgt = ctx->d_tgt, *d_scal = ctx->d_scal;
   const size_t GL = grid_elems(m, nd);
-  JG_TRY(dev_alloc((void**)&d_tgt, GL * 8));
-  sc.p.push_back(d_tgt);
-  JG_TRY(dev_alloc((void**)&d_scal, (size_t)segl * 4 * 8));
-  sc.p.push_back(d_scal);
   // the target, FP64: the reference layout [i][j][k] (i fastest) is the device grid layout [k][j][i]
   JG_CUDA(cudaMemcpyAsync(d_tgt, t_target, GL * 8, cudaMemcpyHostToDevice, st));
   // forward sweep with checkpoints
@@ -1113,10 +1166,8 @@ extern "C" int jgcm_model_hs_gradient(jgcm_model* md, int nsteps, int checkpoint
   JG_TRY(state_zero(md, &bo, st));
   JG_CUDA(cudaMemsetAsync(w.pbar, 0, 5 * 8, st));
   {
-    const int nbl = (int)((GL + 255) / 256);
-    double* part = nullptr;
-    JG_TRY(dev_alloc((void**)&part, (size_t)nbl * 8));
-    sc.p.push_back(part);
+    const int nbl = ctx->nbl;
+    double* part = ctx->part;
     if (is_fp64(m))
       k_loss<double><<<nbl, 256, 0, st>>>((const double*)fin.f[14], d_tgt, (double*)bi.f[14], m->d_wts, m->nlat,
                                           m->nlon, nd, part);

@@ -65,6 +65,7 @@ struct jgcm_model {
   double *d_partials, *d_scalars;
   unsigned* d_counter;
   double* state_stage;  // FP64 staging of the packed host state (jgcm_model_set_state / get_state)
+  void* adj;            // workspace of jgcm_model_hs_gradient, kept between calls (hs_adjoint.cu)
   cudaGraphExec_t graph[3];   // one steady step, per rotation phase
   cudaGraphExec_t graph3[3];  // three steady steps (a whole rotation), per starting phase
   cudaGraphExec_t graph24[3]; // twenty-four steady steps (eight rotations), per starting phase
@@ -94,6 +95,8 @@ int state_save(jgcm_model* md, StateBuf* b, cudaStream_t st);        // model ->
 int state_load(jgcm_model* md, const StateBuf* b, cudaStream_t st);  // b -> model (one launch)
 int state_zero(jgcm_model* md, StateBuf* b, cudaStream_t st);
 int copy_fields(jgcm_model* md, void* const* dst, const void* const* src, cudaStream_t st);
+
+void adj_context_free(jgcm_model* md);  // hs_adjoint.cu: the cached gradient workspace
 
 // models.cu services used by the reverse sweep
 int dev_alloc(void** p, size_t bytes);  // cudaMalloc + zero fill

@@ -907,6 +907,7 @@ int alloc(void** p, size_t bytes) {
 
 void model_free(jgcm_model* md) {
   if (!md) return;
+  adj_context_free(md);
   if (md->state_stage) cudaFree(md->state_stage);
   for (int i = 0; i < 3; i++) {
     void* ps[] = {md->spe_vor[i], md->spe_div[i], md->spe_lnps[i], md->spe_t[i],
