@@ -82,6 +82,7 @@ struct FixArgs {
 // one thread per grid point: block partials of the sum of the grid temperature cotangent
 template <typename T>
 __global__ void __launch_bounds__(256) k_fix1(FixArgs a) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const size_t n = (size_t)a.nlat * a.nlon * a.nd, i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   double s = i < n ? (double)((const T*)a.bt)[i] : 0.0;
   s = block_sum(s);
@@ -90,6 +91,7 @@ __global__ void __launch_bounds__(256) k_fix1(FixArgs a) {
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_fold1(FixArgs a, int nb) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using V = V2<T>;
   double s = fold_partials(a.part, nb);
   if (threadIdx.x == 0) {
@@ -110,6 +112,7 @@ __global__ void __launch_bounds__(256) k_fold1(FixArgs a, int nb) {
 // per level; block partials of ps_n2_bar ps_n
 template <typename T>
 __global__ void __launch_bounds__(256) k_fix2(FixArgs a) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const int G = a.nlat * a.nlon, lane = threadIdx.x & 31;
   const int c = blockIdx.x * 8 + (threadIdx.x >> 5), k = lane;
   const bool colv = c < G, act = colv && k < a.nd;
@@ -145,6 +148,7 @@ __global__ void __launch_bounds__(256) k_fix2(FixArgs a) {
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_fold2(FixArgs a, int nb) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using V = V2<T>;
   double s = fold_partials(a.part, nb);
   if (threadIdx.x == 0) {
@@ -163,6 +167,7 @@ __global__ void __launch_bounds__(256) k_fold2(FixArgs a, int nb) {
 // vcos); one thread per grid point
 template <typename T>
 __global__ void __launch_bounds__(256) k_fix3(FixArgs a) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const int G = a.nlat * a.nlon;
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (size_t)G * a.nd) return;
@@ -192,6 +197,7 @@ struct NbarArgs {
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_nbar(NbarArgs<T> a, Tables<T> tb) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using V = V2<T>;
   const size_t total = (size_t)(a.N + 1) * (a.ns + 1) * a.nd;
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -254,6 +260,7 @@ __global__ void __launch_bounds__(256) k_nbar(NbarArgs<T> a, Tables<T> tb) {
 // E = -eig ddiv_bar (the -Laplacian of the energy analysis, transposed)
 template <typename T>
 __global__ void k_neg_lap(const V2<T>* __restrict__ in, V2<T>* __restrict__ out, Tables<T> tb, int N, int ns, int L) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const size_t total = (size_t)(N + 1) * (ns + 1) * L;
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= total) return;
@@ -268,6 +275,7 @@ __global__ void k_neg_lap(const V2<T>* __restrict__ in, V2<T>* __restrict__ out,
 template <typename T>
 __global__ void k_grad_adjoint(const V2<T>* __restrict__ sl, const V2<T>* __restrict__ stt, V2<T>* __restrict__ out,
                                Tables<T> tb, int N, int ns, int L) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using V = V2<T>;
   const size_t total = (size_t)(N + 1) * (ns + 1) * L;
   const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -308,6 +316,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_alpha_adjoint(const V2<T>* __restrict__ bvor, const V2<T>* __restrict__ bdiv,
                                                        V2<T>* __restrict__ F, Tables<T> tb, int N, int ns, int nlat,
                                                        int nlon, int nd) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using V = V2<T>;
   const int m = blockIdx.y, nh = nlat >> 1;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -415,6 +424,7 @@ __device__ __forceinline__ R rscan_excl(R x, int lane) {  // sum over lanes > la
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_hs_column_adjoint(ColAdjArgs<T> a, const VertCoef* __restrict__ vcp) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using R = T;
   __shared__ double pw[8][5];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -597,6 +607,7 @@ __global__ void __launch_bounds__(256) k_hs_column_adjoint(ColAdjArgs<T> a, cons
 
 // one block per parameter
 __global__ void k_fold_params(const double* __restrict__ part, int nb, double* __restrict__ pbar) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const int v = blockIdx.x;
   double s = fold_partials(part + (size_t)v * nb, nb);
   if (threadIdx.x == 0) pbar[v] += s;
@@ -607,6 +618,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) k_loss(const T* __restrict__ t, const double* __restrict__ tgt, T* __restrict__ bar,
                                               const double* __restrict__ wts, int nlat, int nlon, int nd,
                                               double* __restrict__ part) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const size_t n = (size_t)nlat * nlon * nd;
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   double s = 0.0;
@@ -622,12 +634,14 @@ __global__ void __launch_bounds__(256) k_loss(const T* __restrict__ t, const dou
 }
 
 __global__ void k_fold_scalar(const double* __restrict__ part, int nb, double* __restrict__ out) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   double s = fold_partials(part, nb);
   if (threadIdx.x == 0) *out = s;
 }
 
 template <typename T>
 __global__ void k_add2(const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ out, size_t n) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = a[i] + b[i];
 }
@@ -791,11 +805,11 @@ int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x1, StateBuf* xin, 
   fa.cp = md->cp_air;
   fa.grav = md->P.grav;
   const int nbp = (int)((grid_elems(m, nd) + 255) / 256);  // a thread per grid point
-  k_fix1<T><<<nbp, 256, 0, st>>>(fa);
-  k_fold1<T><<<1, 256, 0, st>>>(fa, nbp);
+  JG_CUDA(launch_pdl(k_fix1<T>, nbp, 256, 0, st, fa));
+  JG_CUDA(launch_pdl(k_fold1<T>, 1, 256, 0, st, fa, nbp));
   k_fix2<T><<<w->nb_adj, 256, 0, st>>>(fa);  // a warp per column
-  k_fold2<T><<<1, 256, 0, st>>>(fa, w->nb_adj);
-  k_fix3<T><<<nbp, 256, 0, st>>>(fa);
+  JG_CUDA(launch_pdl(k_fold2<T>, 1, 256, 0, st, fa, w->nb_adj));
+  JG_CUDA(launch_pdl(k_fix3<T>, nbp, 256, 0, st, fa));
   JG_CUDA(cudaGetLastError());
   // 2. syntheses of the new level reversed: ln ps, T, vor, div, u cos, v cos
   {
@@ -835,7 +849,7 @@ int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x1, StateBuf* xin, 
   na.nd = nd;
   const size_t SL = spec_elems(m, nd);
   const int nbs = (int)((SL + 255) / 256);
-  k_nbar<T><<<nbs, 256, 0, st>>>(na, tb);
+  JG_CUDA(launch_pdl(k_nbar<T>, nbs, 256, 0, st, na, tb));
   JG_CUDA(cudaGetLastError());
   // 3. implicit correction + damping + filtered leapfrog reversed
   {
@@ -845,7 +859,7 @@ int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x1, StateBuf* xin, 
     JG_TRY(si_adjoint_launch(md, ob, ib, w->mats, st));
   }
   // 4. analyses of the tendencies reversed: dT, dlnps, energy (-eig ddiv_bar) ...
-  k_neg_lap<T><<<nbs, 256, 0, st>>>((const V*)w->b_ddiv, (V*)w->e_spec, tb, N, ns, nd);
+  JG_CUDA(launch_pdl(k_neg_lap<T>, nbs, 256, 0, st, (const V*)w->b_ddiv, (V*)w->e_spec, tb, N, ns, nd));
   JG_CUDA(cudaGetLastError());
   {
     S2GPlan sp;
@@ -865,8 +879,8 @@ int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x1, StateBuf* xin, 
   // ... and the alpha operators (vor, div from u cos, v cos) -> du, dv
   {
     dim3 ga((m->nh * nd + 255) / 256, N + 1);
-    k_alpha_adjoint<T><<<ga, 256, 0, st>>>((const V*)w->b_dvor, (const V*)w->b_ddiv, (V*)md->fbuf, tb, N, ns, nlat,
-                                            nlon, nd);
+    JG_CUDA(launch_pdl(k_alpha_adjoint<T>, ga, 256, 0, st, (const V*)w->b_dvor, (const V*)w->b_ddiv, (V*)md->fbuf, tb, N, ns, nlat,
+                                            nlon, nd));
     JG_CUDA(cudaGetLastError());
     IFFTPlan ip;
     memset(&ip, 0, sizeof(ip));
@@ -946,7 +960,7 @@ int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x1, StateBuf* xin, 
     ca.inv_grav = 1.0 / md->P.grav;
   }
   k_hs_column_adjoint<T><<<w->nb_adj, 256, 0, st>>>(ca, md->d_vc);
-  k_fold_params<<<5, 256, 0, st>>>(w->ppart, w->nb_adj, w->pbar);
+  JG_CUDA(launch_pdl(k_fold_params, 5, 256, 0, st, w->ppart, w->nb_adj, w->pbar));
   JG_CUDA(cudaGetLastError());
   // 6. the gradients' syntheses reversed, then Compute_Gradient_Cos! transposed
   {
@@ -967,9 +981,9 @@ int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x1, StateBuf* xin, 
     JG_TRY(launch_g2s<T>(m, fp, gp, st, md->fbuf, md->fcap));
   }
   const size_t S1 = spec_elems(m, 1);
-  k_grad_adjoint<T><<<(int)((S1 + 255) / 256), 256, 0, st>>>((const V*)w->s_gl, (const V*)w->s_gt, (V*)xout->f[4], tb,
-                                                             N, ns, 1);
-  k_grad_adjoint<T><<<nbs, 256, 0, st>>>((const V*)w->s_tl, (const V*)w->s_tt, (V*)xout->f[6], tb, N, ns, nd);
+  JG_CUDA(launch_pdl(k_grad_adjoint<T>, (int)((S1 + 255) / 256), 256, 0, st, (const V*)w->s_gl, (const V*)w->s_gt, (V*)xout->f[4], tb,
+                                                             N, ns, 1));
+  JG_CUDA(launch_pdl(k_grad_adjoint<T>, nbs, 256, 0, st, (const V*)w->s_tl, (const V*)w->s_tt, (V*)xout->f[6], tb, N, ns, nd));
   JG_CUDA(cudaGetLastError());
   (void)G;
   return JGCM_OK;
@@ -1169,12 +1183,12 @@ extern "C" int jgcm_model_hs_gradient(jgcm_model* md, int nsteps, int checkpoint
     const int nbl = ctx->nbl;
     double* part = ctx->part;
     if (is_fp64(m))
-      k_loss<double><<<nbl, 256, 0, st>>>((const double*)fin.f[14], d_tgt, (double*)bi.f[14], m->d_wts, m->nlat,
-                                          m->nlon, nd, part);
+      JG_CUDA(launch_pdl(k_loss<double>, nbl, 256, 0, st, (const double*)fin.f[14], d_tgt, (double*)bi.f[14], m->d_wts, m->nlat,
+                                          m->nlon, nd, part));
     else
-      k_loss<float><<<nbl, 256, 0, st>>>((const float*)fin.f[14], d_tgt, (float*)bi.f[14], m->d_wts, m->nlat,
-                                         m->nlon, nd, part);
-    k_fold_scalar<<<1, 256, 0, st>>>(part, nbl, w.sc + SC_LOSS);
+      JG_CUDA(launch_pdl(k_loss<float>, nbl, 256, 0, st, (const float*)fin.f[14], d_tgt, (float*)bi.f[14], m->d_wts, m->nlat,
+                                         m->nlon, nd, part));
+    JG_CUDA(launch_pdl(k_fold_scalar, 1, 256, 0, st, part, nbl, w.sc + SC_LOSS));
     JG_CUDA(cudaGetLastError());
     if (loss) {  // the mesh stream does not synchronise with the legacy default stream
       JG_CUDA(cudaMemcpyAsync(loss, w.sc + SC_LOSS, 8, cudaMemcpyDeviceToHost, st));
@@ -1208,9 +1222,9 @@ extern "C" int jgcm_model_hs_gradient(jgcm_model* md, int nsteps, int checkpoint
     void* gsum = w.g_du;  // free scratch: nd grid levels
     const int nbl = (int)((GL + 255) / 256);
     if (is_fp64(m))
-      k_add2<double><<<nbl, 256, 0, st>>>((const double*)xin->f[14], (const double*)xin->f[15], (double*)gsum, GL);
+      JG_CUDA(launch_pdl(k_add2<double>, nbl, 256, 0, st, (const double*)xin->f[14], (const double*)xin->f[15], (double*)gsum, GL));
     else
-      k_add2<float><<<nbl, 256, 0, st>>>((const float*)xin->f[14], (const float*)xin->f[15], (float*)gsum, GL);
+      JG_CUDA(launch_pdl(k_add2<float>, nbl, 256, 0, st, (const float*)xin->f[14], (const float*)xin->f[15], (float*)gsum, GL));
     FFTPlan fp;
     memset(&fp, 0, sizeof(fp));
     G2SPlan gp;
@@ -1224,11 +1238,11 @@ extern "C" int jgcm_model_hs_gradient(jgcm_model* md, int nsteps, int checkpoint
     const size_t SLn = spec_elems(m, nd) * 2;  // reals
     const int nbs = (int)((SLn + 255) / 256);
     if (is_fp64(m)) {
-      k_add2<double><<<nbs, 256, 0, st>>>((const double*)xin->f[6], (const double*)xin->f[7], (double*)w.nb_t, SLn);
-      k_add2<double><<<nbs, 256, 0, st>>>((const double*)w.nb_t, (const double*)w.a_t, (double*)w.nb_t, SLn);
+      JG_CUDA(launch_pdl(k_add2<double>, nbs, 256, 0, st, (const double*)xin->f[6], (const double*)xin->f[7], (double*)w.nb_t, SLn));
+      JG_CUDA(launch_pdl(k_add2<double>, nbs, 256, 0, st, (const double*)w.nb_t, (const double*)w.a_t, (double*)w.nb_t, SLn));
     } else {
-      k_add2<float><<<nbs, 256, 0, st>>>((const float*)xin->f[6], (const float*)xin->f[7], (float*)w.nb_t, SLn);
-      k_add2<float><<<nbs, 256, 0, st>>>((const float*)w.nb_t, (const float*)w.a_t, (float*)w.nb_t, SLn);
+      JG_CUDA(launch_pdl(k_add2<float>, nbs, 256, 0, st, (const float*)xin->f[6], (const float*)xin->f[7], (float*)w.nb_t, SLn));
+      JG_CUDA(launch_pdl(k_add2<float>, nbs, 256, 0, st, (const float*)w.nb_t, (const float*)w.a_t, (float*)w.nb_t, SLn));
     }
     JG_CUDA(cudaGetLastError());
     JG_TRY(spec_dev_to_host(m, w.nb_t, m->d_stage, nd, st));

@@ -2679,6 +2679,7 @@ __device__ __forceinline__ void lf_adj(int init, R Dt, R rob, R d, R f, R qnb, R
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_hs_implicit_adjoint(AdjArgs<T> a) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using R = T;
   const int lane = threadIdx.x & 31;
   const int pid = blockIdx.x * 8 + (threadIdx.x >> 5);
@@ -2842,7 +2843,7 @@ int si_adjoint_launch(jgcm_model* md, const void* const* obar, void* const* ibar
                       cudaStream_t st) {
   jgcm_mesh* m = md->mesh;
   const int nd = md->nd;
-  auto launch = [&](auto tag) {
+  auto launch = [&](auto tag) -> cudaError_t {
     using T = decltype(tag);
     using V = V2<T>;
     AdjArgs<T> a;
@@ -2870,12 +2871,10 @@ int si_adjoint_launch(jgcm_model* md, const void* const* obar, void* const* ibar
     a.xi = md->init_step ? md->P.dt * md->P.implicit_coef : (2 * md->P.dt) * md->P.implicit_coef;
     a.ps_ref = md->P.ps_ref;
     a.robert = md->P.robert_coef;
-    k_hs_implicit_adjoint<T><<<(md->npairs + 7) / 8, 256, 0, st>>>(a);
+    return launch_pdl(k_hs_implicit_adjoint<T>, dim3((md->npairs + 7) / 8), dim3(256), 0, st, a);
   };
-  if (is_fp64(m)) launch(double());
-  else launch(float());
+  JG_CUDA(is_fp64(m) ? launch(double()) : launch(float()));
   mark(st);
-  JG_CUDA(cudaGetLastError());
   return JGCM_OK;
 }
 }  // namespace jgcm

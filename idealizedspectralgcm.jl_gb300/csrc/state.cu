@@ -20,6 +20,7 @@ struct CopyList {
 };
 
 __global__ void __launch_bounds__(256) k_copy_fields(CopyList c) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const int f = blockIdx.y;
   const uint4* __restrict__ s = c.src[f];
   uint4* __restrict__ d = c.dst[f];
@@ -174,7 +175,7 @@ int copy_fields(jgcm_model* md, void* const* dst, const void* const* src, cudaSt
     mx = c.n16[i] > mx ? c.n16[i] : mx;
   }
   const int bx = (int)std::min<size_t>((mx + 255) / 256, 64);
-  k_copy_fields<<<dim3(bx, NSTATE), 256, 0, st>>>(c);
+  JG_CUDA(launch_pdl(k_copy_fields, dim3(bx, NSTATE), 256, 0, st, c));
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;
 }
