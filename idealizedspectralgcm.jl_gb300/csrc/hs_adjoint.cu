@@ -651,6 +651,8 @@ struct AdjWork {
   void* base;
   // grid (T): lnps bar, u/cos, v/cos, du, dv, dT, energy, dlnps, gl, gt, tl, tt
   void *g_l, *g_uc, *g_vc, *g_du, *g_dv, *g_dT, *g_en, *g_dln, *g_gl, *g_gt, *g_tl, *g_tt;
+  // grid (T): the gradients of ln ps and T of X_s (forward values: Compute_Gradients!)
+  void *x_gl, *x_gt, *x_tl, *x_tt;
   // spectral (T2): S2G^T results, new-level cotangents, tendency cotangents, E, gradient S2G^T
   void *a_l, *a_t, *a_vor, *a_div, *a_uc, *a_vc, *nb_vor, *nb_div, *nb_t, *nb_l;
   void *b_dvor, *b_ddiv, *b_dt, *b_dl, *e_spec, *s_gl, *s_gt, *s_tl, *s_tt;
@@ -671,7 +673,7 @@ int work_alloc(jgcm_model* md, AdjWork* w) {
   const int G = m->nlat * m->nlon;
   w->nb_col = (int)((grid_elems(m, nd) + 255) / 256);  // block partials: a thread per grid point
   w->nb_adj = (G + 7) / 8;      // one warp per column
-  const size_t gtot = 4 * al(G1) + 8 * al(GL);
+  const size_t gtot = 6 * al(G1) + 10 * al(GL);
   const size_t stot = 4 * al(S1) + 15 * al(SL);
   const size_t dtot = al(SC_N * 8) + al((size_t)(std::max(w->nb_col, w->nb_adj) + 8) * 8) +
                       al((size_t)5 * w->nb_adj * 8) + al(5 * 8);
@@ -694,6 +696,10 @@ int work_alloc(jgcm_model* md, AdjWork* w) {
   w->g_en = take(GL);
   w->g_tl = take(GL);
   w->g_tt = take(GL);
+  w->x_gl = take(G1);
+  w->x_gt = take(G1);
+  w->x_tl = take(GL);
+  w->x_tt = take(GL);
   w->a_l = take(S1);
   w->nb_l = take(S1);
   w->b_dl = take(S1);
@@ -766,11 +772,13 @@ GridOutGroup gout(int epi, void* dst, int L, int col0) {
   return g;
 }
 
-// One adjoint step.  The model holds X_s (its init flag selects Δt or 2Δt); x1 is X_{s+1}; w->sc
-// holds the step's forward scalars; xin holds the cotangents of X_{s+1} (its grid u_c, v_c, t_c,
-// ps_c are updated in place), xout receives those of X_s; w->pbar accumulates.
+// One adjoint step.  x0 is X_s (init: the step's init flag, Δt or 2Δt), x1 is X_{s+1}; w->sc holds
+// the step's forward scalars; xin holds the cotangents of X_{s+1} (its grid u_c, v_c, t_c, ps_c are
+// updated in place), xout receives those of X_s; w->pbar accumulates.  Reads no model state slot,
+// so a step is capturable once per (segment slot, buffer parity) and replayed.
 template <typename T>
-int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x1, StateBuf* xin, StateBuf* xout) {
+int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x0, const StateBuf* x1, StateBuf* xin, StateBuf* xout,
+                 int init) {
   using V = V2<T>;
   jgcm_mesh* m = md->mesh;
   cudaStream_t st = m->stream;
@@ -856,7 +864,7 @@ int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x1, StateBuf* xin, 
     const void* ob[8] = {w->nb_vor, xin->f[1], w->nb_div, xin->f[3], w->nb_t, xin->f[7], w->nb_l, xin->f[5]};
     void* ib[12] = {w->b_dvor, w->b_ddiv, w->b_dt, w->b_dl, xout->f[1], xout->f[0],
                     xout->f[3], xout->f[2], xout->f[7], xout->f[6], xout->f[5], xout->f[4]};
-    JG_TRY(si_adjoint_launch(md, ob, ib, w->mats, st));
+    JG_TRY(si_adjoint_launch(md, ob, ib, w->mats, init, st));
   }
   // 4. analyses of the tendencies reversed: dT, dlnps, energy (-eig ddiv_bar) ...
   JG_CUDA(launch_pdl(k_neg_lap<T>, nbs, 256, 0, st, (const V*)w->b_ddiv, (V*)w->e_spec, tb, N, ns, nd));
@@ -890,25 +898,46 @@ int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x1, StateBuf* xin, 
     ip.g[1] = gout(EPI_NONE, w->g_dv, nd, nd);
     JG_TRY(launch_ifft_only<T>(m, ip, st, md->fbuf, md->fcap));
   }
-  // 5. columns: gradients of ln ps and T of X_s first (into the model's gradient buffers)
-  JG_TRY(hs_grad(md, lvl(md, 1), st));
+  // 5. columns: the gradients of ln ps and T of X_s first (Compute_Gradients!: DLAM / DTH prologues,
+  //    / cos epilogue)
+  {
+    S2GPlan sp;
+    memset(&sp, 0, sizeof(sp));
+    IFFTPlan ip;
+    memset(&ip, 0, sizeof(ip));
+    sp.ng = ip.ng = 4;
+    sp.C = ip.C = 2 + 2 * nd;
+    const int ops[4] = {S2G_DLAM, S2G_DTH, S2G_DLAM, S2G_DTH};
+    const void* src[4] = {x0->f[4], x0->f[4], x0->f[6], x0->f[6]};
+    void* dst[4] = {w->x_gl, w->x_gt, w->x_tl, w->x_tt};
+    for (int i = 0, col = 0; i < 4; i++) {
+      const int L = i < 2 ? 1 : nd;
+      memset(&sp.g[i], 0, sizeof(sp.g[i]));
+      sp.g[i].a = src[i];
+      sp.g[i].op = ops[i];
+      sp.g[i].L = L;
+      sp.g[i].col0 = col;
+      ip.g[i] = gout(EPI_DIVCOS, dst[i], L, col);
+      col += L;
+    }
+    JG_TRY(launch_s2g<T>(m, sp, ip, st, md->fbuf, md->fcap));
+  }
   ColAdjArgs<T> ca;
   memset(&ca, 0, sizeof(ca));
-  const int p = lvl(md, 0), c = lvl(md, 1);
-  ca.u = (const T*)md->grid_u[c];
-  ca.v = (const T*)md->grid_v[c];
-  ca.t = (const T*)md->grid_t[c];
-  ca.vor = (const T*)md->grid_vor;
-  ca.div = (const T*)md->grid_div;
-  ca.up = (const T*)md->grid_u[p];
-  ca.vp = (const T*)md->grid_v[p];
-  ca.tp = (const T*)md->grid_t[p];
-  ca.ps = (const T*)md->grid_ps[c];
-  ca.psp = (const T*)md->grid_ps[p];
-  ca.gl = (const T*)md->g_dlps;
-  ca.gt = (const T*)md->g_dtps;
-  ca.tl = (const T*)md->g_dlT;
-  ca.tt = (const T*)md->g_dtT;
+  ca.u = (const T*)x0->f[8];
+  ca.v = (const T*)x0->f[10];
+  ca.t = (const T*)x0->f[14];
+  ca.vor = (const T*)x0->f[16];
+  ca.div = (const T*)x0->f[17];
+  ca.up = (const T*)x0->f[9];
+  ca.vp = (const T*)x0->f[11];
+  ca.tp = (const T*)x0->f[15];
+  ca.ps = (const T*)x0->f[12];
+  ca.psp = (const T*)x0->f[13];
+  ca.gl = (const T*)w->x_gl;
+  ca.gt = (const T*)w->x_gt;
+  ca.tl = (const T*)w->x_tl;
+  ca.tt = (const T*)w->x_tt;
   ca.DU = (const T*)w->g_du;
   ca.DV = (const T*)w->g_dv;
   ca.DT = (const T*)w->g_dT;
@@ -941,7 +970,7 @@ int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x1, StateBuf* xin, 
   ca.nd = nd;
   ca.nlat = nlat;
   ca.nlon = nlon;
-  ca.Dt = md->init_step ? md->P.dt : 2 * md->P.dt;
+  ca.Dt = init ? md->P.dt : 2 * md->P.dt;
   {
     const double day = 86400.0, sb = md->P.sigma_b;
     ca.sigma_b = sb;
@@ -989,8 +1018,10 @@ int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x1, StateBuf* xin, 
   return JGCM_OK;
 }
 
-int adjoint_step_any(jgcm_model* md, AdjWork* w, const StateBuf* x1, StateBuf* xin, StateBuf* xout) {
-  return is_fp64(md->mesh) ? adjoint_step<double>(md, w, x1, xin, xout) : adjoint_step<float>(md, w, x1, xin, xout);
+int adjoint_step_any(jgcm_model* md, AdjWork* w, const StateBuf* x0, const StateBuf* x1, StateBuf* xin,
+                     StateBuf* xout, int init) {
+  return is_fp64(md->mesh) ? adjoint_step<double>(md, w, x0, x1, xin, xout, init)
+                           : adjoint_step<float>(md, w, x0, x1, xin, xout, init);
 }
 
 // forward scalars of the step just taken: mean_ps_p, mean_energy_p, factor, correction
@@ -1072,7 +1103,7 @@ extern "C" int jgcm_model_step_adjoint(jgcm_model* md, double* const* state_bar,
   JG_TRY(bars_h2d(md, state_bar, &bi));
   JG_TRY(state_zero(md, &bo, st));
   JG_CUDA(cudaMemsetAsync(w.pbar, 0, 5 * 8, st));
-  JG_TRY(adjoint_step_any(md, &w, &x1, &bi, &bo));
+  JG_TRY(adjoint_step_any(md, &w, &x0, &x1, &bi, &bo, x0.init));
   JG_TRY(bars_d2h(md, &bo, state_bar));
   double pb[5];
   JG_CUDA(cudaMemcpyAsync(pb, w.pbar, sizeof(pb), cudaMemcpyDeviceToHost, st));
@@ -1088,7 +1119,8 @@ namespace {
 // count and checkpoint interval (allocation, and the host build of the transposed vertical
 // operators, would otherwise dominate short windows).
 struct AdjContext {
-  int nsteps = 0, K = 0, nbl = 0;
+  int nsteps = 0, K = 0, nbl = 0, tune_gen = -1;
+  std::vector<std::pair<int, cudaGraphExec_t>> graphs;  // reverse steps: key (slot, init, parity)
   std::vector<StateBuf> ck, seg;
   StateBuf fin{}, bi{}, bo{};
   AdjWork w{};
@@ -1099,6 +1131,8 @@ struct AdjContext {
 
 void ctx_free(AdjContext* c) {
   if (!c) return;
+  for (auto& kv : c->graphs)
+    if (kv.second) cudaGraphExecDestroy(kv.second);
   for (void* p : c->bufs) cudaFree(p);
   if (c->has_w) work_free(&c->w);
   delete c;
@@ -1140,6 +1174,37 @@ int ctx_create(jgcm_model* md, int nsteps, int K, AdjContext** out) {
   *out = c;
   return JGCM_OK;
 }
+// The reverse step of segment slot j: the step's forward scalars copied into the work scalars, then
+// adjoint_step from seg[j] (X_s) and seg[j+1] (X_{s+1}) between the two cotangent buffers (bi -> bo
+// when in_bi, else bo -> bi), captured once and replayed in every segment.
+int ctx_step_graph(jgcm_model* md, AdjContext* c, int j, int init, bool in_bi, cudaGraphExec_t* out) {
+  const int key = (j * 2 + (init ? 1 : 0)) * 2 + (in_bi ? 1 : 0);
+  for (auto& kv : c->graphs)
+    if (kv.first == key) {
+      *out = kv.second;
+      return JGCM_OK;
+    }
+  cudaStream_t st = md->mesh->stream;
+  StateBuf* xin = in_bi ? &c->bi : &c->bo;
+  StateBuf* xout = in_bi ? &c->bo : &c->bi;
+  cudaGraph_t g;
+  JG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaMemcpyAsync(c->w.sc, c->d_scal + 4 * j, 4 * 8, cudaMemcpyDeviceToDevice, st);
+  int s = e == cudaSuccess ? adjoint_step_any(md, &c->w, &c->seg[j], &c->seg[j + 1], xin, xout, init) : JGCM_OK;
+  cudaError_t e2 = cudaStreamEndCapture(st, &g);
+  if (s != JGCM_OK || e != cudaSuccess || e2 != cudaSuccess) {
+    if (e2 == cudaSuccess) cudaGraphDestroy(g);
+    if (s != JGCM_OK) return s;
+    JG_CUDA(e != cudaSuccess ? e : e2);
+  }
+  cudaGraphExec_t ge = nullptr;
+  cudaError_t e3 = cudaGraphInstantiate(&ge, g, 0);
+  cudaGraphDestroy(g);
+  JG_CUDA(e3);
+  c->graphs.push_back({key, ge});
+  *out = ge;
+  return JGCM_OK;
+}
 }  // namespace
 
 void jgcm::adj_context_free(jgcm_model* md) {
@@ -1160,6 +1225,12 @@ extern "C" int jgcm_model_hs_gradient(jgcm_model* md, int nsteps, int checkpoint
     jgcm::adj_context_free(md);
     JG_TRY(ctx_create(md, nsteps, K, &ctx));
     md->adj = ctx;
+  }
+  if (ctx->tune_gen != m->tune_gen) {  // tiles or Legendre engine changed since the capture
+    for (auto& kv : ctx->graphs)
+      if (kv.second) cudaGraphExecDestroy(kv.second);
+    ctx->graphs.clear();
+    ctx->tune_gen = m->tune_gen;
   }
   std::vector<StateBuf>& ck = ctx->ck;
   std::vector<StateBuf>& seg = ctx->seg;
@@ -1207,10 +1278,11 @@ extern "C" int jgcm_model_hs_gradient(jgcm_model* md, int nsteps, int checkpoint
       JG_TRY(save_scalars(md, d_scal + 4 * (s - s0), st));
     }
     JG_TRY(state_save(md, &seg[s1 - s0], st));
-    for (int s = s1 - 1; s >= s0; s--) {
-      JG_TRY(state_load(md, &seg[s - s0], st));
-      JG_CUDA(cudaMemcpyAsync(w.sc, d_scal + 4 * (s - s0), 4 * 8, cudaMemcpyDeviceToDevice, st));
-      JG_TRY(adjoint_step_any(md, &w, &seg[s - s0 + 1], xin, xout));
+    for (int s = s1 - 1; s >= s0; s--) {  // one captured graph per (slot, init flag, buffer parity)
+      const int j = s - s0;
+      cudaGraphExec_t ge = nullptr;
+      JG_TRY(ctx_step_graph(md, ctx, j, seg[j].init, xin == &bi, &ge));
+      JG_CUDA(cudaGraphLaunch(ge, st));
       StateBuf* t = xin;
       xin = xout;
       xout = t;

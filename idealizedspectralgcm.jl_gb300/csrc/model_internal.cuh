@@ -105,8 +105,9 @@ int model_step_async(jgcm_model* md);  // one step enqueued on the mesh stream, 
 // transposed semi-implicit step (Semi_Implicit.jl:360-513 + Time_Integrator.jl:58-101) on device
 // buffers: obar[8] = cotangents of vor_n, vor_c', div_n, div_c', T_n, T_c', lnps_n, lnps_c';
 // ibar[12] = cotangents of dvor, ddiv, dT, dlnps, vor_p, vor_c, div_p, div_c, T_p, T_c, lnps_p,
-// lnps_c (written for n >= m); `mats` from si_adjoint_mats (freed by the caller with cudaFree)
+// lnps_c (written for n >= m); `mats` from si_adjoint_mats (freed by the caller with cudaFree);
+// init: the step's init flag (Δt or 2Δt coefficients)
 int si_adjoint_mats(jgcm_model* md, double** mats);
-int si_adjoint_launch(jgcm_model* md, const void* const* obar, void* const* ibar, const double* mats,
+int si_adjoint_launch(jgcm_model* md, const void* const* obar, void* const* ibar, const double* mats, int init,
                       cudaStream_t st);
 }  // namespace jgcm

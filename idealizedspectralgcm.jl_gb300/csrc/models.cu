@@ -2839,7 +2839,7 @@ int si_adjoint_mats(jgcm_model* md, double** mats) {
   return JGCM_OK;
 }
 
-int si_adjoint_launch(jgcm_model* md, const void* const* obar, void* const* ibar, const double* mats,
+int si_adjoint_launch(jgcm_model* md, const void* const* obar, void* const* ibar, const double* mats, int init,
                       cudaStream_t st) {
   jgcm_mesh* m = md->mesh;
   const int nd = md->nd;
@@ -2854,9 +2854,9 @@ int si_adjoint_launch(jgcm_model* md, const void* const* obar, void* const* ibar
     a.vp_b = (V*)ibar[4]; a.vcin_b = (V*)ibar[5]; a.dp_b = (V*)ibar[6]; a.dcin_b = (V*)ibar[7];
     a.tp_b = (V*)ibar[8]; a.tcin_b = (V*)ibar[9]; a.lp_b = (V*)ibar[10]; a.lcin_b = (V*)ibar[11];
     a.damping = (const T*)md->damping;
-    a.dfac = (const T*)md->dfac[md->init_step ? 0 : 1];
+    a.dfac = (const T*)md->dfac[init ? 0 : 1];
     a.eig64 = m->t64.eig;
-    a.W = md->d_W + (md->init_step ? 0 : (size_t)(m->N + 1) * nd * nd);
+    a.W = md->d_W + (init ? 0 : (size_t)(m->N + 1) * nd * nd);
     a.Apt = mats;
     a.Ageo = mats + (size_t)nd * nd;
     a.spt = mats + 2 * (size_t)nd * nd;
@@ -2866,9 +2866,9 @@ int si_adjoint_launch(jgcm_model* md, const void* const* obar, void* const* ibar
     a.nd = nd;
     a.ns = m->ns;
     a.N = m->N;
-    a.init_step = md->init_step;
+    a.init_step = init;
     a.dt = md->P.dt;
-    a.xi = md->init_step ? md->P.dt * md->P.implicit_coef : (2 * md->P.dt) * md->P.implicit_coef;
+    a.xi = init ? md->P.dt * md->P.implicit_coef : (2 * md->P.dt) * md->P.implicit_coef;
     a.ps_ref = md->P.ps_ref;
     a.robert = md->P.robert_coef;
     return launch_pdl(k_hs_implicit_adjoint<T>, dim3((md->npairs + 7) / 8), dim3(256), 0, st, a);
