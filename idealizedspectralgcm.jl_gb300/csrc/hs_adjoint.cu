@@ -109,38 +109,40 @@ __global__ void __launch_bounds__(256) k_fold1(FixArgs a, int nb) {
 }
 
 // energy fixer reversed: en_n = |u_n|^2/2 + cp T_n weighted by dp(ps_n2); a warp per column, a lane
-// per level; block partials of ps_n2_bar ps_n
+// per level, arithmetic in the state precision; block partials of ps_n2_bar ps_n in FP64
 template <typename T>
 __global__ void __launch_bounds__(256) k_fix2(FixArgs a) {
   pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
+  using R = T;
   const int G = a.nlat * a.nlon, lane = threadIdx.x & 31;
   const int c = blockIdx.x * 8 + (threadIdx.x >> 5), k = lane;
   const bool colv = c < G, act = colv && k < a.nd;
   const int j = colv ? c / a.nlon : 0;
-  const double factor = a.sc[SC_FACTOR], corr = a.sc[SC_CORR], En_bar = a.sc[SC_EN_BAR];
-  const double Wc = a.wts[j] / (2.0 * a.nlon);
-  const double ps2 = colv ? (double)((const T*)a.ps_n2)[c] : 0.0;
-  double acc = 0.0;
+  const R factor = (R)a.sc[SC_FACTOR], corr = (R)a.sc[SC_CORR], En_bar = (R)a.sc[SC_EN_BAR];
+  const R Wc = (R)(a.wts[j] / (2.0 * a.nlon)), cp = (R)a.cp, ig = (R)(1.0 / a.grav);
+  const R ps2 = colv ? (R)((const T*)a.ps_n2)[c] : (R)0;
+  R acc = 0;
   if (act && a.do_energy) {
     const size_t x = c + (size_t)G * k;
-    const double u = ((const T*)a.u_n)[x], v = ((const T*)a.v_n)[x], t = (double)((const T*)a.t_n2)[x] - corr;
-    const double en = 0.5 * (u * u + v * v) + a.cp * t;
-    const double eb = En_bar * Wc * (a.vc->dak[k] + a.vc->dbk[k] * ps2) / a.grav;
-    ((T*)a.bu)[x] = (T)((double)((T*)a.bu)[x] + eb * u);
-    ((T*)a.bv)[x] = (T)((double)((T*)a.bv)[x] + eb * v);
-    ((T*)a.bt)[x] = (T)((double)((T*)a.bt)[x] + a.cp * eb);
-    acc = en * a.vc->dbk[k];
+    const R u = ((const T*)a.u_n)[x], v = ((const T*)a.v_n)[x], t = ((const T*)a.t_n2)[x] - corr;
+    const R dbk = (R)a.vc->dbk[k];
+    const R en = (R)0.5 * (u * u + v * v) + cp * t;
+    const R eb = En_bar * Wc * ((R)a.vc->dak[k] + dbk * ps2) * ig;
+    ((T*)a.bu)[x] = ((T*)a.bu)[x] + eb * u;
+    ((T*)a.bv)[x] = ((T*)a.bv)[x] + eb * v;
+    ((T*)a.bt)[x] = ((T*)a.bt)[x] + cp * eb;
+    acc = en * dbk;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
   double s = 0.0;
   if (colv && lane == 0) {
-    double bps = (double)((T*)a.bps)[c];
+    R bps = ((T*)a.bps)[c];
     if (a.do_energy) {
-      bps += En_bar * Wc / a.grav * acc;
-      ((T*)a.bps)[c] = (T)bps;
+      bps += En_bar * Wc * ig * acc;
+      ((T*)a.bps)[c] = bps;
     }
-    s = bps * (ps2 / factor);
+    s = (double)bps * ((double)ps2 / (double)factor);
   }
   s = block_sum(s);
   if (threadIdx.x == 0) a.part[blockIdx.x] = s;

@@ -2606,8 +2606,40 @@ extern "C" int jgcm_model_autotune(jgcm_model* md, int nsteps, int* knobs_out, f
 // δT); Linear_Geopot_δt!: δT -> Φ) from the same column functions as the wave matrices, and W_n^T.
 namespace {
 struct AdjMats {  // vertical operators A, row-major (A[k][c] at k*nd + c); matT applies A^T
-  double *Apt, *spt, *Ageo, *hk;
+  double *Apt, *spt, *Ageo, *hk;  // FP64 (the FP64 path)
+  float *Aptf, *sptf, *Ageof, *hkf;  // the same rounded to FP32 (the mixed path: no conversions per use)
 };
+
+// the operators of the state precision T within one allocation made by adj_mats
+template <typename T>
+struct AdjMatsT;
+template <>
+struct AdjMatsT<double> {
+  static void get(const AdjMats& m, const double** Apt, const double** spt, const double** Ageo, const double** hk) {
+    *Apt = m.Apt, *spt = m.spt, *Ageo = m.Ageo, *hk = m.hk;
+  }
+};
+template <>
+struct AdjMatsT<float> {
+  static void get(const AdjMats& m, const float** Apt, const float** spt, const float** Ageo, const float** hk) {
+    *Apt = m.Aptf, *spt = m.sptf, *Ageo = m.Ageof, *hk = m.hkf;
+  }
+};
+
+AdjMats adj_mats_view(double* d, int nd) {  // the pointers of an adj_mats allocation
+  AdjMats a;
+  const size_t n2 = (size_t)nd * nd;
+  a.Apt = d;
+  a.Ageo = d + n2;
+  a.spt = d + 2 * n2;
+  a.hk = a.spt + nd;
+  float* f = (float*)(d + 2 * n2 + 2 * nd);
+  a.Aptf = f;
+  a.Ageof = f + n2;
+  a.sptf = f + 2 * n2;
+  a.hkf = a.sptf + nd;
+  return a;
+}
 
 int adj_mats(jgcm_model* md, AdjMats* out) {
   const int nd = md->nd;
@@ -2625,16 +2657,19 @@ int adj_mats(jgcm_model* md, AdjMats* out) {
     for (int k = 0; k < nd; k++) Ageo[(size_t)k * nd + c] = geo[k];
   }
   for (int k = 0; k < nd; k++) hk[k] = md->vc.h[k] * md->P.ps_ref;
+  const size_t nall = 2 * (size_t)nd * nd + 2 * nd;
+  std::vector<double> host(nall);
+  std::copy(Apt.begin(), Apt.end(), host.begin());
+  std::copy(Ageo.begin(), Ageo.end(), host.begin() + (size_t)nd * nd);
+  std::copy(spt.begin(), spt.end(), host.begin() + 2 * (size_t)nd * nd);
+  std::copy(hk.begin(), hk.end(), host.begin() + 2 * (size_t)nd * nd + nd);
+  std::vector<float> hostf(nall);
+  for (size_t i = 0; i < nall; i++) hostf[i] = (float)host[i];
   double* d = nullptr;
-  JG_TRY(alloc((void**)&d, (2 * (size_t)nd * nd + 2 * nd) * 8));
-  out->Apt = d;
-  out->Ageo = d + (size_t)nd * nd;
-  out->spt = d + 2 * (size_t)nd * nd;
-  out->hk = out->spt + nd;
-  JG_CUDA(cudaMemcpy(out->Apt, Apt.data(), Apt.size() * 8, cudaMemcpyHostToDevice));
-  JG_CUDA(cudaMemcpy(out->Ageo, Ageo.data(), Ageo.size() * 8, cudaMemcpyHostToDevice));
-  JG_CUDA(cudaMemcpy(out->spt, spt.data(), nd * 8, cudaMemcpyHostToDevice));
-  JG_CUDA(cudaMemcpy(out->hk, hk.data(), nd * 8, cudaMemcpyHostToDevice));
+  JG_TRY(alloc((void**)&d, nall * 8 + nall * 4));
+  *out = adj_mats_view(d, nd);
+  JG_CUDA(cudaMemcpy(d, host.data(), nall * 8, cudaMemcpyHostToDevice));
+  JG_CUDA(cudaMemcpy(out->Aptf, hostf.data(), nall * 4, cudaMemcpyHostToDevice));
   return JGCM_OK;
 }
 
@@ -2644,15 +2679,16 @@ struct AdjArgs {
   const V2<T>*vn_b, *vc_b, *dn_b, *dc_b, *tn_b, *tc_b, *ln_b, *lc_b;                 // outputs' cotangents
   V2<T>*dvor_b, *ddiv_b, *dt_b, *dl_b, *vp_b, *vcin_b, *dp_b, *dcin_b, *tp_b, *tcin_b, *lp_b, *lcin_b;  // inputs'
   const T *damping, *dfac;
-  const double *eig64, *W, *Apt, *spt, *Ageo, *hk;
+  const double *eig64, *W;
+  const T *Apt, *spt, *Ageo, *hk;  // vertical operators in the state precision
   const int2* pairs;
   int npairs, nd, ns, N, init_step, dt;
   double xi, ps_ref, robert;
 };
 
 // y = M^T x for row-major M: y_k = sum_c M[c][k] x_c at the lane's level k; lanes >= nd return 0
-template <typename R>
-__device__ __forceinline__ R matT(const double* M, R x, int lane, int nd) {
+template <typename R, typename E>
+__device__ __forceinline__ R matT(const E* M, R x, int lane, int nd) {
   R y = 0;
   for (int c = 0; c < nd; c++) {
     R xc = __shfl_sync(FULL, x, c);
@@ -2857,10 +2893,7 @@ int si_adjoint_launch(jgcm_model* md, const void* const* obar, void* const* ibar
     a.dfac = (const T*)md->dfac[init ? 0 : 1];
     a.eig64 = m->t64.eig;
     a.W = md->d_W + (init ? 0 : (size_t)(m->N + 1) * nd * nd);
-    a.Apt = mats;
-    a.Ageo = mats + (size_t)nd * nd;
-    a.spt = mats + 2 * (size_t)nd * nd;
-    a.hk = a.spt + nd;
+    AdjMatsT<T>::get(adj_mats_view(const_cast<double*>(mats), nd), &a.Apt, &a.spt, &a.Ageo, &a.hk);
     a.pairs = md->d_pairs;
     a.npairs = md->npairs;
     a.nd = nd;
@@ -2964,7 +2997,7 @@ extern "C" int jgcm_model_semi_implicit_step_adjoint(jgcm_model* md, const doubl
     a.dfac = (const T*)md->dfac[md->init_step ? 0 : 1];
     a.eig64 = m->t64.eig;
     a.W = md->d_W + (md->init_step ? 0 : (size_t)(m->N + 1) * md->nd * md->nd);
-    a.Apt = am.Apt; a.spt = am.spt; a.Ageo = am.Ageo; a.hk = am.hk;
+    AdjMatsT<T>::get(am, &a.Apt, &a.spt, &a.Ageo, &a.hk);
     a.pairs = md->d_pairs;
     a.npairs = md->npairs;
     a.nd = md->nd;
