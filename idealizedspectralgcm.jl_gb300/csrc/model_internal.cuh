@@ -34,6 +34,8 @@ struct jgcm_model {
   int fcap;
   int hs_lanes;  // lanes per column of the Held-Suarez column kernel (1, 2 or 4)
   int graph_gen;  // the mesh's tile generation the captured graphs were built with
+  // sigma half-level coefficients b_k given at creation (Vert_Coordinate's bk); empty = even_sigma
+  std::vector<double> vert_bk;
   // Held-Suarez: the gradients of ln ps and T of the current level are already in g_dlps ...
   // g_dtT (computed at the end of the previous step, concurrently with the fixers)
   int grad_ready;

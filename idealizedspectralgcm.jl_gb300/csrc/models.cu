@@ -812,6 +812,54 @@ void lin_geo_col(const VertCoef& vc, int nd, double R, const double* dtt, double
   for (int k = 0; k < nd; k++) geo[k] = gh[k + 1] + R * (dtt[k] * (vc.lnph_ref[k + 1] - vc.lnpf_ref[k]));
 }
 
+// Compute_Vert_Coord (Vert_Coordinate.jl:61-87) for the sigma options, zero top (the constructor's
+// default, :44): a_k = 0 and b_k from
+//   even_sigma    LinRange(0, 1, nd+1)                                    (Compute_Even_Sigma, :112-117)
+//   uneven_sigma  b = exp(-(surf_res z + (1 - surf_res) z^exponent) scale_heights), z = 1 - k/nd,
+//                 b_nd = 1, b_0 = 0 (Compute_Uneven_Sigma, :120-141, following its docstring: the
+//                 reference's branch (:69-70) passes undefined a, b and its code flips the sign of
+//                 the exponent, which gives b > 1 above the surface)
+//   mcm, v197     the fixed 14- and 18-level tables of Compute_Old_Model_Sigma / Compute_V197_Sigma
+//                 (:143-165)
+// "hybrid" (:71-76, a_k != 0) does not run in the reference (Compute_Uneven_Sigma called without nd)
+// and is not supported: the column kernels use ln p = ln b_k + ln ps.
+int vert_coord_table(int nd, const std::string& opt, double scale_heights, double surf_res, double exponent,
+                     double* ak, double* bk) {
+  static const double kMcm[15] = {0.0, 0.03, 0.0707, 0.1311, 0.2102, 0.3036, 0.4062, 0.5138,
+                                  0.6226, 0.7284, 0.8255, 0.9066, 0.9640, 0.9933, 1.0};
+  static const double kV197[19] = {0.0, 0.0089163, 0.0342936, 0.0740741, 0.1262002, 0.1886145, 0.2592592,
+                                   0.3360768, 0.4170096, 0.5000000, 0.5829904, 0.6639231, 0.7407407,
+                                   0.8113854, 0.8737997, 0.9259259, 0.9657064, 0.9910837, 1.0};
+  for (int k = 0; k <= nd; k++) ak[k] = 0.0;
+  if (opt == "even_sigma") {
+    for (int k = 0; k <= nd; k++) {
+      double t = (double)k / (double)nd;
+      bk[k] = (1 - t) * 0.0 + t * 1.0;
+    }
+  } else if (opt == "uneven_sigma") {
+    for (int k = 0; k <= nd; k++) {
+      double t = (double)k / (double)nd, z = (1 - t) * 1.0 + t * 0.0;  // LinRange(1, 0, nd+1)
+      bk[k] = std::exp(-(surf_res * z + (1.0 - surf_res) * std::pow(z, exponent)) * scale_heights);
+    }
+    bk[nd] = 1.0;
+    bk[0] = 0.0;
+  } else if (opt == "mcm" || opt == "v197") {
+    const int need = opt == "mcm" ? 14 : 18;
+    if (nd != need) {
+      set_error("%s has %d levels", opt.c_str(), need);
+      return JGCM_E_ARG;
+    }
+    memcpy(bk, opt == "mcm" ? kMcm : kV197, (size_t)(nd + 1) * sizeof(double));
+  } else if (opt == "hybrid") {
+    set_error("hybrid coordinates (a_k != 0) are not supported");
+    return JGCM_E_ARG;
+  } else {
+    set_error("Compute_Vert_Coord: %s is not a valid value for option", opt.c_str());
+    return JGCM_E_ARG;
+  }
+  return JGCM_OK;
+}
+
 void vertical_setup(jgcm_model* md) {
   int nd = md->nd;
   VertCoef& vc = md->vc;
@@ -819,7 +867,7 @@ void vertical_setup(jgcm_model* md) {
   for (int k = 0; k <= nd; k++) {
     double t = (double)k / (double)nd;
     vc.ak[k] = 0.0;
-    vc.bk[k] = (1 - t) * 0.0 + t * 1.0;
+    vc.bk[k] = md->vert_bk.empty() ? (1 - t) * 0.0 + t * 1.0 : md->vert_bk[k];
   }
   for (int k = 0; k < nd; k++) {
     vc.dak[k] = vc.ak[k + 1] - vc.ak[k];
@@ -1677,7 +1725,26 @@ extern "C" int jgcm_model_create(jgcm_mesh* mesh, const jgcm_params* params, jgc
 
 extern "C" int jgcm_model_create_members(jgcm_mesh* mesh, const jgcm_params* params, int members,
                                          jgcm_model** out) {
+  return jgcm_model_create_vert(mesh, params, members, nullptr, nullptr, out);
+}
+
+extern "C" int jgcm_vert_coord(int nd, const char* option, double scale_heights, double surf_res, double exponent,
+                               double* ak, double* bk) {
+  JG_ARG(option && ak && bk, "NULL argument");
+  JG_ARG(nd >= 1 && nd <= JGCM_MAX_ND, "nd out of range");
+  return vert_coord_table(nd, option, scale_heights, surf_res, exponent, ak, bk);
+}
+
+extern "C" int jgcm_model_create_vert(jgcm_mesh* mesh, const jgcm_params* params, int members, const double* ak,
+                                      const double* bk, jgcm_model** out) {
   JG_ARG(mesh && params && out, "NULL argument");
+  JG_ARG((ak == nullptr) == (bk == nullptr), "ak and bk are given together");
+  if (bk) {
+    const int nd = mesh->nd;
+    for (int k = 0; k <= nd; k++) JG_ARG(ak[k] == 0.0, "hybrid coordinates (a_k != 0) are not supported");
+    JG_ARG(bk[0] == 0.0 && bk[nd] == 1.0, "sigma coordinates need b_0 = 0 (zero top) and b_nd = 1");
+    for (int k = 0; k < nd; k++) JG_ARG(bk[k + 1] > bk[k], "b_k must increase downwards");
+  }
   *out = nullptr;
   JG_ARG(members >= 1 && members <= 65535, "members must be in [1, 65535]");
   JG_ARG(params->kind >= JGCM_BAROTROPIC && params->kind <= JGCM_HELD_SUAREZ, "unknown model kind");
@@ -1696,6 +1763,7 @@ extern "C" int jgcm_model_create_members(jgcm_mesh* mesh, const jgcm_params* par
   md->init_step = 1;
   md->sw_adv_from_n = 1;
   md->cp_air = params->rdgas / params->kappa;
+  if (bk) md->vert_bk.assign(bk, bk + mesh->nd + 1);
   int s = model_alloc(md);
   if (s != JGCM_OK) {
     model_free(md);
@@ -2544,7 +2612,7 @@ extern "C" int jgcm_model_autotune(jgcm_model* md, int nsteps, int* knobs_out, f
   JG_ARG(md && nsteps >= 1, "bad arguments");
   jgcm_mesh* m = md->mesh;
   jgcm_model* sc = nullptr;
-  JG_TRY(jgcm_model_create_members(m, &md->P, md->ne, &sc));
+  JG_TRY(jgcm_model_create_vert(m, &md->P, md->ne, md->vc.ak, md->vc.bk, &sc));
   struct Guard {
     jgcm_model* p;
     ~Guard() { jgcm_model_destroy(p); }

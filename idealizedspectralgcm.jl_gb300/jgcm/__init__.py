@@ -29,7 +29,7 @@ __all__ = [
     "FP64", "FP32", "TF32X3", "BF16X3", "JGCMError", "Spectral_Spherical_Mesh", "Trans_Spherical_To_Grid",
     "Trans_Grid_To_Spherical", "Trans_Grid_To_Fourier", "Vor_Div_From_Grid_UV", "UV_Grid_From_Vor_Div",
     "Compute_Gradients", "Add_Horizontal_Advection", "Apply_Laplacian", "Area_Weighted_Global_Mean", "Model",
-    "lib", "lib_path",
+    "Compute_Vert_Coord", "lib", "lib_path",
 ]
 
 FP64, FP32, TF32X3, BF16X3 = 0, 1, 2, 3
@@ -82,6 +82,8 @@ def lib():
         "jgcm_area_weighted_global_mean": (I, [P, P, C.POINTER(D)]),
         "jgcm_model_create": (I, [P, P, PP]),
         "jgcm_model_create_members": (I, [P, P, I, PP]),
+        "jgcm_vert_coord": (I, [I, C.c_char_p, D, D, D, P, P]),
+        "jgcm_model_create_vert": (I, [P, P, I, P, P, PP]),
         "jgcm_model_members": (I, [P, C.POINTER(I)]),
         "jgcm_model_copy_member": (I, [P, I, P, I]),
         "jgcm_model_semi_implicit_step": (I, [P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
@@ -309,6 +311,18 @@ class _Params(C.Structure):
 KINDS = {"barotropic": 0, "shallow_water": 1, "held_suarez": 2}
 
 
+def Compute_Vert_Coord(nd, vert_coord_option, scale_heights=4.0, surf_res=1.0, exponent=2.5):
+    """Vert_Coordinate.jl:61-87: the half-level coefficients (ak, bk), nd+1 each, top first, zero top.
+
+    Options: "even_sigma", "uneven_sigma" (built as Compute_Uneven_Sigma's docstring states; the
+    reference's own branch does not run), "mcm" (nd 14), "v197" (nd 18).  "hybrid" raises: its
+    reference branch does not run and a_k != 0 is not supported."""
+    ak, bk = np.zeros(nd + 1), np.zeros(nd + 1)
+    _check(lib().jgcm_vert_coord(int(nd), vert_coord_option.encode(), float(scale_heights), float(surf_res),
+                                 float(exponent), _ptr(ak), _ptr(bk)))
+    return ak, bk
+
+
 class Model:
     """Dyn_Data + Filtered_Leapfrog (+ Semi_Implicit_Solver) on the GPU.
 
@@ -320,12 +334,24 @@ class Model:
 
     ``members`` > 1 makes an ensemble: that many independent members advanced together by the
     same kernels.  Members are loaded and read with ``copy_member`` through one-member models.
+
+    ``vert_coord`` is Vert_Coordinate's option (``"even_sigma"``, the reference drivers' choice,
+    ``"uneven_sigma"``, ``"mcm"``, ``"v197"``; see ``Compute_Vert_Coord``) or a pair (ak, bk) of
+    sigma half-level coefficients.
     """
 
-    def __init__(self, mesh: Spectral_Spherical_Mesh, params: dict, members: int = 1):
+    def __init__(self, mesh: Spectral_Spherical_Mesh, params: dict, members: int = 1,
+                 vert_coord="even_sigma", **vert_options):
         self.mesh = mesh
         self.params = dict(params)
         self.members = int(members)
+        if isinstance(vert_coord, str):
+            ak, bk = Compute_Vert_Coord(mesh.nd, vert_coord, **vert_options)
+        else:
+            ak, bk = (np.ascontiguousarray(x, dtype=np.float64) for x in vert_coord)
+            if ak.shape != (mesh.nd + 1,) or bk.shape != (mesh.nd + 1,):
+                raise ValueError("ak and bk need nd + 1 values each")
+        self.ak, self.bk = ak, bk
         p = _Params()
         for name, _ in _Params._fields_:
             if name == "kind":
@@ -334,7 +360,7 @@ class Model:
                 setattr(p, name, params[name])
         self._p = p
         h = C.c_void_p()
-        _check(lib().jgcm_model_create_members(mesh._h, C.byref(p), self.members, C.byref(h)))
+        _check(lib().jgcm_model_create_vert(mesh._h, C.byref(p), self.members, _ptr(ak), _ptr(bk), C.byref(h)))
         self._h = h
 
     def diagnostics(self, on=True):

@@ -32,6 +32,9 @@ GRIDS = {
     "hs_t42l20": dict(num_fourier=42, nlat=64, nlon=128, nd=20, radius=6371000.0),
     "hs_t21l20": dict(num_fourier=21, nlat=32, nlon=64, nd=20, radius=6371000.0),
     "hs_t21l10": dict(num_fourier=21, nlat=32, nlon=64, nd=10, radius=6371000.0),
+    # the level counts of Vert_Coordinate's fixed sigma tables (mcm: 14, v197: 18)
+    "hs_t21l14": dict(num_fourier=21, nlat=32, nlon=64, nd=14, radius=6371000.0),
+    "hs_t21l18": dict(num_fourier=21, nlat=32, nlon=64, nd=18, radius=6371000.0),
 }
 
 _COMMON = dict(robert_coef=0.04, damping_order=4, omega=7.292e-5, grav=9.80, rdgas=287.04, kappa=2.0 / 7.0,
@@ -48,6 +51,11 @@ PARAMS = {
 }
 PARAMS["hs_t21l20"] = dict(PARAMS["hs_t42l20"])
 PARAMS["hs_t21l10"] = dict(PARAMS["hs_t42l20"])
+PARAMS["hs_t21l14"] = dict(PARAMS["hs_t42l20"])
+PARAMS["hs_t21l18"] = dict(PARAMS["hs_t42l20"])
+
+# Vert_Coordinate options with the grid whose level count each one needs
+VERT_COORD_CASES = [("hs_t21l14", "mcm"), ("hs_t21l18", "v197"), ("hs_t21l20", "uneven_sigma")]
 
 STEPS_PER_DAY = {k: DAY // v["dt"] for k, v in PARAMS.items()}
 

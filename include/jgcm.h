@@ -149,6 +149,20 @@ int jgcm_model_create(jgcm_mesh* mesh, const jgcm_params* params, jgcm_model** o
  * and copied in; their fields are read by copying a member out into a one-member model. */
 int jgcm_model_create_members(jgcm_mesh* mesh, const jgcm_params* params, int members, jgcm_model** out);
 int jgcm_model_members(jgcm_model* model, int* members);
+/* Vert_Coordinate's Compute_Vert_Coord (Atmos_Spectral/Vert_Coordinate.jl:61-87), host FP64:
+ * half-level coefficients ak[nd+1], bk[nd+1] (p_{k+1/2} = ak + bk ps, top first) for option
+ * "even_sigma", "uneven_sigma" (scale_heights, surf_res, exponent: the reference's defaults are
+ * 4, 1, 2.5; built as Compute_Uneven_Sigma's docstring states, :120-141 — the reference's code
+ * for that branch does not run), "mcm" (nd 14) or "v197" (nd 18); always zero top (the
+ * constructor's default, :44).  "hybrid" (a_k != 0; :71-76, which does not run in the reference)
+ * returns JGCM_E_ARG. */
+int jgcm_vert_coord(int nd, const char* option, double scale_heights, double surf_res, double exponent,
+                    double* ak, double* bk);
+/* jgcm_model_create_members on the vertical coordinate ak, bk (each nd+1; NULL, NULL = even_sigma,
+ * the reference drivers' choice, Spectral_Dynamics.jl:513): sigma coordinates only (ak = 0,
+ * bk[0] = 0, bk[nd] = 1, increasing), else JGCM_E_ARG. */
+int jgcm_model_create_vert(jgcm_mesh* mesh, const jgcm_params* params, int members, const double* ak,
+                           const double* bk, jgcm_model** out);
 /* Copy member src_member of src into member dst_member of dst (same mesh and model kind): every
  * time level of the prognostic state and the grid diagnostics.  A one-member dst also takes the
  * source's time-step state (init step); an ensemble dst must already share it. */

@@ -87,6 +87,9 @@ typedef struct {
 } om_params;
 
 om_model* om_model_create(om_mesh* mesh, const om_params* p);
+om_model* om_model_create_vert(om_mesh* mesh, const om_params* p, const double* bk);
+int om_vert_coord(int nd, const char* option, double scale_heights, double surf_res, double exponent, double* ak,
+                  double* bk);
 void om_semi_implicit_step(om_model* md, const double* const* in, double* const* out);
 void om_hs_forcing(om_model* md, int Dt, const double* u, const double* v, const double* p_half,
                    const double* p_full, const double* t, double* du, double* dv, double* t_eq, double* dtt);

@@ -67,6 +67,8 @@ def lib():
             "om_apply_laplacian": (None, [P, P, I]),
             "om_area_weighted_global_mean": (D, [P, P]),
             "om_model_create": (P, [P, P]),
+            "om_model_create_vert": (P, [P, P, P]),
+            "om_vert_coord": (I, [I, C.c_char_p, D, D, D, P, P]),
             "om_model_destroy": (None, [P]),
             "om_model_field": (L, [P, C.c_char_p, P, L, I]),
             "om_model_init_step": (I, [P]),
@@ -232,12 +234,28 @@ class _Params(C.Structure):
 KINDS = {"barotropic": 0, "shallow_water": 1, "held_suarez": 2}
 
 
-class Model:
-    """Dyn_Data + Filtered_Leapfrog (+ Semi_Implicit_Solver for Held-Suarez) on the oracle."""
+def Compute_Vert_Coord(nd, vert_coord_option, scale_heights=4.0, surf_res=1.0, exponent=2.5):
+    """Vert_Coordinate.jl:61-87 (zero top): (ak, bk), nd+1 each."""
+    ak, bk = np.zeros(nd + 1), np.zeros(nd + 1)
+    if lib().om_vert_coord(int(nd), vert_coord_option.encode(), float(scale_heights), float(surf_res),
+                           float(exponent), ak.ctypes.data_as(C.c_void_p), bk.ctypes.data_as(C.c_void_p)):
+        raise AssertionError(f"Compute_Vert_Coord: {vert_coord_option!r} with nd = {nd} is not supported")
+    return ak, bk
 
-    def __init__(self, mesh, params: dict):
+
+class Model:
+    """Dyn_Data + Filtered_Leapfrog (+ Semi_Implicit_Solver for Held-Suarez) on the oracle.
+
+    ``vert_coord``: a Vert_Coordinate option (see ``Compute_Vert_Coord``) or a pair (ak, bk)."""
+
+    def __init__(self, mesh, params: dict, vert_coord="even_sigma", **vert_options):
         self.mesh = mesh
         self.params = dict(params)
+        if isinstance(vert_coord, str):
+            vert_coord = Compute_Vert_Coord(mesh.nd, vert_coord, **vert_options)
+        self.ak, self.bk = (np.ascontiguousarray(x, dtype=np.float64) for x in vert_coord)
+        if np.any(self.ak != 0):
+            raise AssertionError("hybrid coordinates (a_k != 0) are not supported")
         p = _Params()
         for name, _ in _Params._fields_:
             if name == "kind":
@@ -245,7 +263,7 @@ class Model:
             elif name in params:
                 setattr(p, name, params[name])
         self._p = p
-        self._h = lib().om_model_create(mesh._h, C.byref(p))
+        self._h = lib().om_model_create_vert(mesh._h, C.byref(p), self.bk.ctypes.data_as(C.c_void_p))
         if not self._h:
             raise AssertionError("model creation failed")
 

@@ -4,6 +4,7 @@ import os
 import re
 import subprocess
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -61,3 +62,15 @@ def test_argument_errors_are_assertions(jg):
         jg.Spectral_Spherical_Mesh(21, 22, 31, 64, 3, 1.0)
     with pytest.raises(AssertionError):
         jg.Spectral_Spherical_Mesh(21, 22, 32, 40, 3, 1.0)  # nlon not a power of two
+
+
+def test_vert_coord_tables_match_the_oracle(jg, orc):
+    """jgcm_vert_coord is host code: it runs without a device and equals the oracle's tables."""
+    for nd, opt, kw in ((20, "even_sigma", {}), (20, "uneven_sigma", {}), (14, "mcm", {}), (18, "v197", {}),
+                        (24, "uneven_sigma", dict(scale_heights=5.0, surf_res=0.2, exponent=2.0))):
+        ag, bg = jg.Compute_Vert_Coord(nd, opt, **kw)
+        ao, bo = orc.Compute_Vert_Coord(nd, opt, **kw)
+        assert np.array_equal(ag, ao) and np.allclose(bg, bo, rtol=2e-16, atol=0), opt
+    for nd, opt in ((20, "mcm"), (20, "hybrid"), (20, "sigma")):
+        with pytest.raises(AssertionError):
+            jg.Compute_Vert_Coord(nd, opt)

@@ -111,6 +111,38 @@ def test_held_suarez_steps(jg, orc, name, prec, tol):
         assert configs.rel_l2(gmod.get(f), omod.get(f)) < tol, f
 
 
+@pytest.mark.parametrize("name,option", configs.VERT_COORD_CASES)
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("fp32", 1e-3)])
+def test_held_suarez_vert_coords(jg, orc, name, option, prec, tol):
+    """Held-Suarez on Vert_Coordinate's other sigma options (mcm, v197, uneven_sigma): the
+    semi-implicit matrices and the steps from a developed state equal the oracle's."""
+    params = configs.PARAMS[name]
+    gm, om = configs.make_mesh(jg, name, precision=prec), configs.make_mesh(orc, name)
+    gmod, omod = jg.Model(gm, params, vert_coord=option), orc.Model(om, params, vert_coord=option)
+    assert np.array_equal(gmod.bk, omod.bk)
+    if prec == "fp64":
+        assert configs.rel_l2(gmod.semi_implicit("div_mat"), omod.semi_implicit("div_mat")) < 1e-13
+        assert configs.rel_l2(gmod.semi_implicit("wave_matrix"), omod.semi_implicit("wave_matrix")) < 1e-12
+    omod.spectral_initialize_fields(configs.hs_temperature_noise(om), True)
+    configs.add_hs_flow(orc, om, omod)
+    configs.copy_state(omod, gmod, "held_suarez")
+    for n in (1, 1, 2):
+        gmod.step(n)
+        omod.step(n)
+        _compare(gmod, omod, "held_suarez", tol)
+    for f in ("grid_t_eq", "grid_p_full", "grid_p_half"):
+        assert configs.rel_l2(gmod.get(f), omod.get(f)) < tol, f
+
+
+def test_held_suarez_refuses_hybrid_coordinates(jg):
+    gm = configs.make_mesh(jg, "hs_t21l10", precision="fp32")
+    ak, bk = np.linspace(0.0, 1.0e3, 11), np.linspace(0.0, 1.0, 11)
+    with pytest.raises(AssertionError):
+        jg.Model(gm, configs.PARAMS["hs_t21l10"], vert_coord=(ak, bk))
+    with pytest.raises(AssertionError):
+        jg.Model(gm, configs.PARAMS["hs_t21l10"], vert_coord="hybrid")
+
+
 def test_held_suarez_restart_steady_step(jg, orc):
     """A state saved after the init step continues identically once Update_Init_Step! is applied."""
     gm, om, gmod, omod = _hs_developed(jg, orc, "hs_t42l20", "fp64")

@@ -203,6 +203,32 @@ def test_gpu_gradient_matches_oracle_and_finite_differences(jg, orc):
 
 
 @pytest.mark.gpu
+def test_gpu_gradient_on_v197_levels_matches_oracle(jg, orc):
+    """The gradient on Vert_Coordinate's 18-level v197 sigma table (6 steps, checkpoint every 4)
+    equals the oracle's: the reverse column, fixers and semi-implicit transposes take the level
+    coefficients from the model."""
+    name, nsteps, ck = "hs_t21l18", 6, 4
+    mesh = configs.make_mesh(orc, name)
+    md = orc.Model(mesh, configs.PARAMS[name], vert_coord="v197")
+    configs.init_held_suarez(orc, mesh, md)
+    configs.add_hs_flow(orc, mesh, md)
+    orc.set_state(md, orc.get_state(md))
+    S0 = orc.get_state(md)[0]
+    tgt = np.asfortranarray(S0["grid_t_c"] + np.random.default_rng(5).standard_normal(S0["grid_t_c"].shape))
+    loss_o, gT_o, gp_o = orc.HS_Gradient(md, nsteps, tgt)
+    gm = configs.make_mesh(jg, name, precision="fp64")
+    gmod = jg.Model(gm, configs.PARAMS[name], vert_coord="v197")
+    for k in orc.STATE_FIELDS:
+        gmod.set(k, S0[k])
+    gmod.set_init_step(True)
+    loss_g, gT_g, gp_g = jg.HS_Gradient(gmod, nsteps, tgt, checkpoint_every=ck)
+    assert abs(loss_g - loss_o) <= 1e-11 * loss_o, (loss_g, loss_o)
+    assert configs.rel_l2(gT_g, gT_o) < 1e-9, configs.rel_l2(gT_g, gT_o)
+    for i, p in enumerate(orc.HS_PARAMS):
+        assert abs(gp_g[i] - gp_o[i]) <= 1e-9 * abs(gp_o[i]), (p, gp_g[i], gp_o[i])
+
+
+@pytest.mark.gpu
 def test_gpu_gradient_one_day_t42l20():
     """The configuration of the adjoint benchmark: Held-Suarez T42L20, 72 steps from the seeded
     initial state, a checkpoint every 8.  FP64 against central differences (T0 direction and the five

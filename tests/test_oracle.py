@@ -203,6 +203,46 @@ def test_hs_mass_fixer_and_step_finite(orc):
     assert np.isfinite(md.get("grid_t_c")).all()
 
 
+def test_vert_coord_tables(orc):
+    """Compute_Vert_Coord (Vert_Coordinate.jl:61-87), zero top: even_sigma is LinRange(0, 1);
+    uneven_sigma with surf_res = 1 is exp(-scale_heights (1 - k/nd)) inside, and with surf_res < 1
+    stays increasing; the v197 table is symmetric about 1/2 (b_k + b_{nd-k} = 1 to its 7 printed decimals); mcm and v197 need
+    their own level counts; hybrid (a_k != 0, a branch that does not run in the reference) is
+    refused."""
+    ak, bk = orc.Compute_Vert_Coord(20, "even_sigma")
+    assert np.all(ak == 0) and np.allclose(bk, np.linspace(0, 1, 21), rtol=0, atol=1e-15)
+    ak, bk = orc.Compute_Vert_Coord(20, "uneven_sigma")
+    k = np.arange(1, 20)
+    assert np.all(ak == 0) and bk[0] == 0 and bk[20] == 1
+    assert np.allclose(bk[1:20], np.exp(-4.0 * (1.0 - k / 20.0)), rtol=1e-15, atol=0)
+    _, bk = orc.Compute_Vert_Coord(24, "uneven_sigma", scale_heights=5.0, surf_res=0.2, exponent=2.0)
+    assert np.all(np.diff(bk) > 0) and bk[0] == 0 and bk[24] == 1
+    _, b197 = orc.Compute_Vert_Coord(18, "v197")
+    assert np.allclose(b197 + b197[::-1], 1.0, rtol=0, atol=1.5e-7) and np.all(np.diff(b197) > 0)
+    _, bmcm = orc.Compute_Vert_Coord(14, "mcm")
+    assert bmcm[0] == 0 and bmcm[14] == 1 and np.all(np.diff(bmcm) > 0)
+    for nd, opt in ((20, "mcm"), (20, "v197"), (20, "hybrid"), (20, "sigma")):
+        with pytest.raises(AssertionError):
+            orc.Compute_Vert_Coord(nd, opt)
+
+
+@pytest.mark.parametrize("name,option", configs.VERT_COORD_CASES)
+def test_hs_vert_coords_mass_fixer_and_step_finite(orc, name, option):
+    """Held-Suarez on the other sigma coordinates: the mass fixer holds the area-mean surface
+    pressure and the state stays finite; the half-level pressures are b_k ps."""
+    M = configs.make_mesh(orc, name)
+    md = orc.Model(M, configs.PARAMS[name], vert_coord=option)
+    md.spectral_initialize_fields(configs.hs_temperature_noise(M), True)
+    ps0 = orc.Area_Weighted_Global_Mean(M, md.get("grid_ps_c"))
+    md.step(6)
+    ps1 = orc.Area_Weighted_Global_Mean(M, md.get("grid_ps_c"))
+    assert abs(ps1 - ps0) / ps0 < 1e-13
+    assert np.isfinite(md.get("grid_t_c")).all() and np.isfinite(md.get("spe_div_c")).all()
+    ph = md.get("grid_p_half")
+    ps = md.get("grid_ps_c")
+    assert np.allclose(ph, ps[:, :, :1] * md.bk[None, None, :], rtol=1e-14, atol=0)
+
+
 def test_barotropic_rh4_is_steady_pattern(orc):
     """The Rossby-Haurwitz wave 4 keeps its shape (it is an exact solution of the barotropic
     vorticity equation; damping and noise perturb it only slightly over 2 days)."""
