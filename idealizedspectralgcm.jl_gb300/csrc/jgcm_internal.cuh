@@ -107,11 +107,26 @@ struct TableStore {
 // column range [col0, col0+L) to one field (one column per level).
 // S2G_ADJ_G2S: input of the adjoint of the analysis (m >= 1 halved, row N+1 dropped)
 enum S2GOp { S2G_PLAIN = 0, S2G_DLAM = 1, S2G_DTH = 2, S2G_UCOS = 3, S2G_VCOS = 4, S2G_ADJ_G2S = 5 };
+// A plan scalar in the kernel's precision: FP64 fields keep the host's values and FP32 kernels read
+// the FP32 copies the launchers fill in (every FP64 -> FP32 conversion, like every FP64 operation,
+// runs on the FP64 pipe, at 1/64 of the FP32 rate on this part).
+template <typename T>
+__host__ __device__ __forceinline__ T pick(double d, float f);
+template <>
+__host__ __device__ __forceinline__ float pick<float>(double, float f) {
+  return f;
+}
+template <>
+__host__ __device__ __forceinline__ double pick<double>(double d, float) {
+  return d;
+}
+
 struct S2GGroup {
   const void* a;  // spectral field (MNK, L levels)
   const void* b;  // second field (UCOS/VCOS: divergence; a = vorticity)
   double shift;   // PLAIN: subtracted from the real part of mode (0,0) before the synthesis
-  int op, L, col0, pad;
+  float shiftf;   // its FP32 copy (filled by the launchers, as every *f field below)
+  int op, L, col0;
 };
 struct S2GPlan {
   int ng, C;
@@ -125,6 +140,8 @@ struct GridOutGroup {
   void* dst2;      // EPI_EXP2: exp(x)
   const void* ps;  // EPI_DIVCOS_MULPS: surface pressure grid [nlat][nlon]
   double shift;    // EPI_EXP2: x is ln(ps) - shift: dst = x + shift, dst2 = exp(x) exp(shift)
+  double eshift;   // exp(shift)
+  float shiftf, eshiftf;
   int epi, L, col0, pad;
 };
 struct IFFTPlan {
@@ -146,6 +163,7 @@ struct GridInGroup {
 struct FFTPlan {
   int ng, C;
   double kappa_m, kappa_t;
+  float kappa_mf, kappa_tf;
   const void* coriolis;  // [nlat] in T
   GridInGroup g[JGCM_MAX_GROUPS];
 };
@@ -157,6 +175,7 @@ struct StepParams {
   int init_step;
   int dt;
   double robert, implicit_coef, h0;
+  float robertf, implicit_coeff, h0f;
   const void* damping;  // [m][n] in T
 };
 struct SpecOutGroup {
@@ -167,6 +186,7 @@ struct SpecOutGroup {
   const void* qc[3];  // BARO/SW: current level (vor, div, h) -- updated in place by the RA filter
   const void* qp[3];  // BARO/SW: previous level
   double scale;       // ADJ_S2G: nlon
+  float scalef;
   int op, L, col0;
   int colA, colB, colE, colH;  // Fourier-buffer base columns of the input slots (-1 = unused)
 };

@@ -97,9 +97,21 @@ __device__ bool grid_reduce_last(const double* vals, double* partials, unsigned*
   // the block's row), then warps and the block combine in a fixed order: deterministic
   double s[NV];
   for (int v = 0; v < NV; v++) s[v] = 0.0;
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-    const double w = wts[b / gridDim.x];
-    for (int v = 0; v < NV; v++) s[v] += __ldcg(partials + (size_t)v * nb + b) * w;
+  constexpr int U = 8;  // loads in flight per thread; the additions keep their order
+  for (int b0 = threadIdx.x; b0 < nb; b0 += U * blockDim.x) {
+    double pv[U][NV], wv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int b = b0 + u * (int)blockDim.x;
+      wv[u] = b < nb ? wts[b / gridDim.x] : 0.0;
+#pragma unroll
+      for (int v = 0; v < NV; v++) pv[u][v] = b < nb ? __ldcg(partials + (size_t)v * nb + b) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++)
+      if (b0 + u * (int)blockDim.x < nb)
+#pragma unroll
+        for (int v = 0; v < NV; v++) s[v] += pv[u][v] * wv[u];
   }
   for (int v = 0; v < NV; v++) s[v] = warp_sum(s[v]);
   const int nw = (blockDim.x + 31) >> 5;
@@ -138,7 +150,26 @@ struct HSColArgs {
   size_t pstride;
   int nd, nlat, nlon, Dt;
   double sigma_b, k_f, k_a, k_s, dT_y, dtheta_z, kappa, rdgas, cp, grav;
+  // the physics constants in T, formed on the host with the kernel's own T arithmetic (no FP64 ->
+  // FP32 conversion per thread: those run on the FP64 pipe)
+  T sb, R, kap, cp_t, kv0, ka, ks, kt0, dTy, dthz, kappa_t;
 };
+
+template <typename T>
+void hs_col_consts(HSColArgs<T>& a) {
+  const T day = (T)86400;
+  a.sb = (T)a.sigma_b;
+  a.R = (T)a.rdgas;
+  a.cp_t = (T)a.cp;
+  a.kap = a.R / a.cp_t;
+  a.kv0 = ((T)a.k_f / day) / ((T)1.0 - a.sb);
+  a.ka = (T)a.k_a / day;
+  a.ks = (T)a.k_s / day;
+  a.kt0 = (a.ks - a.ka) / ((T)1.0 - a.sb);
+  a.dTy = (T)a.dT_y;
+  a.dthz = (T)a.dtheta_z;
+  a.kappa_t = (T)a.kappa;
+}
 
 // S lanes per column (S = 1, 2, 4): lane s walks levels [s*len, s*len + len), len = ceil(nd/S); the
 // running sums that couple the levels (the geopotential from below, the mass-divergence prefix and
@@ -207,11 +238,9 @@ __global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertC
   const T* __restrict__ v_c = a.v_c + cL;
   const T* __restrict__ t_c = a.t_c + cL;
   const T* __restrict__ dvgp = a.div + cL;
-  const T day = (T)86400;
   const T sj = a.sinj[j], s2 = sj * sj, c2 = (T)1.0 - s2, c4 = c2 * c2, cj = a.cosj[j], fj = a.coriolis[j];
-  const T sb = (T)a.sigma_b, R = (T)a.rdgas, kap = (T)a.rdgas / (T)a.cp, cp = (T)a.cp;
-  const T kv0 = ((T)a.k_f / day) / ((T)1.0 - sb);
-  const T ka = (T)a.k_a / day, ks = (T)a.k_s / day, kt0 = (ks - ka) / ((T)1.0 - sb);
+  const T sb = a.sb, R = a.R, kap = a.kap, cp = a.cp_t;
+  const T kv0 = a.kv0, ka = a.ka, kt0 = a.kt0;
   const T ln_pref = (T)11.512925464970229;  // ln 1e5 (HS_Forcing.jl:49 p_ref)
   const T tDt = (T)a.Dt;
   const T ps = act ? a.ps_c[c1] : (T)1, psp = act ? a.ps_p[c1] : (T)0;
@@ -285,7 +314,7 @@ __global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertC
       T du = -k_v * up, dv = -k_v * vp;
       T dt = -((up + (T)0.5 * du * tDt) * du + (vp + (T)0.5 * dv * tDt) * dv) / cp;
       const T lpn = lnpf - ln_pref;  // ln(p / p_ref)
-      T teq = ((T)315.0 - (T)a.dT_y * s2 - (T)a.dtheta_z * c2 * lpn) * exp((T)a.kappa * lpn);
+      T teq = ((T)315.0 - a.dTy * s2 - a.dthz * c2 * lpn) * exp(a.kappa_t * lpn);
       teq = teq > (T)200.0 ? teq : (T)200.0;
       dt = dt - (ka + kt0 * smax * c4) * (tp - teq);
       // Compute_Corrections_Init: column energy integral with ps_p in the state precision
@@ -339,9 +368,14 @@ __global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertC
     accp = (double)psp;
     acce = (double)col_e;
   }
-  // ---- block partials for mean_ps_p and mean_energy_p (fixed order), then the member's fold
-  accp = warp_sum(accp);
-  acce = warp_sum(acce);
+  // ---- block partials for mean_ps_p and mean_energy_p (fixed order), then the member's fold;
+  // only lanes with seg = 0 hold values, so the butterfly stops at offset S (the skipped levels
+  // would add exact zeros)
+#pragma unroll
+  for (int o = 16; o >= S; o >>= 1) {
+    accp += __shfl_xor_sync(FULL, accp, o);
+    acce += __shfl_xor_sync(FULL, acce, o);
+  }
   if ((threadIdx.x & 31) == 0) {
     red[0][threadIdx.x >> 5] = accp;
     red[1][threadIdx.x >> 5] = acce;
@@ -397,7 +431,22 @@ struct ImplArgs {
   const int2* pairs;
   int npairs, nd, L, ne, ns, N, init_step, dt;  // spectral innermost index e*nd + k of L = ne*nd
   double xi, ps_ref, kappa, rdgas, robert;
+  // the same scalars rounded to T on the host (no FP64 division or conversion per thread), and the
+  // Laplacian eigenvalues in T
+  const T* eig_t;
+  T xi_t, rpsr_t, xipsr_t, kap_t, rg_t, rob_t;
 };
+
+template <typename T>
+void impl_consts(ImplArgs<T>& a, const T* eig_t) {
+  a.eig_t = eig_t;
+  a.xi_t = (T)a.xi;
+  a.rpsr_t = (T)(1.0 / a.ps_ref);
+  a.xipsr_t = (T)(a.xi / a.ps_ref);
+  a.kap_t = (T)a.kappa;
+  a.rg_t = (T)a.rdgas;
+  a.rob_t = (T)a.robert;
+}
 
 template <typename R>
 struct CX {
@@ -481,7 +530,7 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCo
   pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using C = CX<R>;
   const int lane = threadIdx.x & 31;
-  const int pid = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int pid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);  // one (m, n) mode per warp
   if (pid >= a.npairs) return;  // whole warp exits together
   const int2 mn = a.pairs[pid];
   const int m = mn.x, n = mn.y, nd = a.nd, e = blockIdx.y;
@@ -498,8 +547,8 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCo
   C divp = ld(a.div_p), divc = ld(a.div_c), tp = ld(a.t_p), tc = ld(a.t_c), vorp = ld(a.vor_p), vorc = ld(a.vor_c);
   V2<T> l0 = a.dlnps[s1], lp0 = a.lnps_p[s1], lc0 = a.lnps_c[s1];
   C dl = {(R)l0.x, (R)l0.y}, lp = {(R)lp0.x, (R)lp0.y}, lc = {(R)lc0.x, (R)lc0.y};
-  const R xi = (R)a.xi, rpsr = (R)(1.0 / a.ps_ref), xipsr = (R)(a.xi / a.ps_ref), eig = (R)a.eig64[row];
-  const R kap = (R)a.kappa, Rg = (R)a.rdgas;
+  const R xi = (R)a.xi_t, rpsr = (R)a.rpsr_t, xipsr = (R)a.xipsr_t, eig = (R)a.eig_t[row];
+  const R kap = (R)a.kap_t, Rg = (R)a.rg_t;
   // Adjust_δlnps_δt_δdiv! :360-404
   C dps, dtmp;
   linear_ps_t<R>(vr, lane, nd, kap, C{divp.x - divc.x, divp.y - divc.y}, dps, dtmp);
@@ -544,7 +593,7 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCo
   dl.x = dl.x + xipsr * dps.x;
   dl.y = dl.y + xipsr * dps.y;
   // damping + leapfrog
-  const R d = (R)a.damping[row], f = (R)a.dfac[row], rob = (R)a.robert;
+  const R d = (R)a.damping[row], f = (R)a.dfac[row], rob = (R)a.rob_t;
   const int ini = a.init_step, Dt = a.dt;
   if (act) {
     C vn, dn, tn;
@@ -582,6 +631,7 @@ struct CorrArgs {
   V2<T>*lnps_n, *t_spec_n;
   const double* wts;
   double *partials, *scalars;  // per member as in HSColArgs
+  T* scal_t;                   // per member: factor and correction rounded to T (for k_hs_corr_apply)
   unsigned* counter;
   size_t pstride;
   int nd, nlat, nlon, do_mass, do_energy;
@@ -622,20 +672,26 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   part[0][ks][threadIdx.x & 31] = ea;
   part[1][ks][threadIdx.x & 31] = eb;
   __syncthreads();
-  double vals[3] = {0, 0, 0};
-  if (ks == 0) {
-    const int c = threadIdx.x;
-    double sa = 0.0, sb = 0.0;
-    for (int q = 0; q < KS; q++) {
-      sa += (double)part[0][q][c];
-      sb += (double)part[1][q][c];
+  // the column's level groups folded in the state precision (as the column integrals themselves);
+  // the three sums over the block's columns in FP64, one warp each (FP64 runs at 1/64 of the FP32
+  // rate: spread over three SM sub-partitions instead of one)
+  __shared__ double wsum[3];
+  if (ks < 3) {
+    const int c = threadIdx.x & 31;
+    const T ps = act ? a.ps_n[off1 + col] : (T)0;
+    double x;
+    if (ks == 0) {
+      x = (double)ps;
+    } else {
+      T sq = 0;
+      for (int q = 0; q < KS; q++) sq += part[ks - 1][q][c];
+      x = ks == 1 ? (double)sq : (double)sq * (double)ps;
     }
-    const double ps = act ? (double)a.ps_n[off1 + col] : 0.0;
-    sb *= ps;
-    vals[0] = warp_sum(ps);
-    vals[1] = warp_sum(sa);
-    vals[2] = warp_sum(sb);
+    x = warp_sum(x);
+    if (c == 0) wsum[ks] = x;
   }
+  __syncthreads();
+  double vals[3] = {wsum[0], wsum[1], wsum[2]};
   double tot3[3];
   __shared__ double fc[2];
   double* scal = a.scalars + 4 * e;
@@ -658,6 +714,8 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
       }
       scal[2] = factor;
       scal[3] = corr;
+      a.scal_t[2 * e] = (T)factor;
+      a.scal_t[2 * e + 1] = (T)corr;
       fc[1] = corr;
     }
     __syncthreads();
@@ -670,10 +728,10 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
 }
 
 template <typename T>
-__global__ void k_hs_corr_apply(T* t_n, T* ps_n, const double* scalars, size_t memL, size_t mem1) {
+__global__ void k_hs_corr_apply(T* t_n, T* ps_n, const T* scal_t, size_t memL, size_t mem1) {
   pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const int e = blockIdx.y;  // member: ps *= factor, T += correction
-  const T factor = (T)scalars[4 * e + 2], corr = (T)scalars[4 * e + 3];
+  const T factor = scal_t[2 * e], corr = scal_t[2 * e + 1];
   T* t = t_n + (size_t)e * memL;
   T* ps = ps_n + (size_t)e * mem1;
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < memL; q += (size_t)gridDim.x * blockDim.x) {
@@ -1060,7 +1118,8 @@ int model_alloc(jgcm_model* md) {
   JG_TRY(alloc((void**)&md->d_pairs, pairs.size() * sizeof(int2)));
   JG_CUDA(cudaMemcpy(md->d_pairs, pairs.data(), pairs.size() * sizeof(int2), cudaMemcpyHostToDevice));
   JG_TRY(alloc((void**)&md->d_partials, (size_t)ne * partial_stride(m) * 8));
-  JG_TRY(alloc((void**)&md->d_scalars, (size_t)4 * ne * 8));
+  // 4 FP64 scalars per member, then each member's factor and correction in the state precision
+  JG_TRY(alloc((void**)&md->d_scalars, (size_t)6 * ne * 8));
   JG_TRY(alloc((void**)&md->d_counter, (size_t)ne * sizeof(unsigned)));
   int nt = (N + 1) * (ns + 1);
   JG_TRY(alloc(&md->dfac[0], (size_t)nt * ts));
@@ -1392,6 +1451,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   a.cp = md->cp_air;
   a.grav = md->P.grav;
   a.pstride = partial_stride(m);
+  hs_col_consts<T>(a);
   JG_TRY(launch_hs_column<T>(a, m, E, md->hs_lanes, md->d_vc, st));
   mark(st);
   JG_CUDA(cudaGetLastError());
@@ -1445,9 +1505,11 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ia.kappa = md->P.kappa;
   ia.rdgas = md->P.rdgas;
   ia.robert = md->P.robert_coef;
+  impl_consts<T>(ia, tables<T>(md->mesh).eig);
   // vertical algebra in the state precision (FP64 algebra on the FP32 path measured no more
   // accurate: its error is set by FP32 storage); the wave-matrix solve is FP64 in both
-  JG_CUDA(launch_pdl(k_hs_implicit<T, T>, dim3((md->npairs + 7) / 8, E), 256, 0, st, ia, md->d_vc));
+  // 4 modes per block: (N+1)(N+2)/2 + N+1 modes at T42 make 248 blocks, every SM's FP64 units busy
+  JG_CUDA(launch_pdl(k_hs_implicit<T, T>, dim3((md->npairs + 3) / 4, E), 128, 0, st, ia, md->d_vc));
   mark(st);
   JG_CUDA(cudaGetLastError());
   // 5. back to the grid: vor, div, u, v, T, lnps (+ ps = exp(lnps))
@@ -1488,6 +1550,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ca.wts = m->d_wts;
   ca.partials = md->d_partials;
   ca.scalars = md->d_scalars;
+  ca.scal_t = (T*)(md->d_scalars + 4 * E);
   ca.counter = md->d_counter;
   ca.nd = nd;
   ca.pstride = partial_stride(m);
@@ -1510,8 +1573,8 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   const size_t G1 = grid_elems(m, 1);
   int nb = (int)(((size_t)nd * G1 + 255) / 256);
   if (nb * E > 8 * 152) nb = (8 * 152 + E - 1) / E;
-  JG_CUDA(launch_pdl(k_hs_corr_apply<T>, dim3(nb, E), 256, 0, st, (T*)md->grid_t[n], (T*)md->grid_ps[n], md->d_scalars,
-                                                  (size_t)nd * G1, G1));
+  JG_CUDA(launch_pdl(k_hs_corr_apply<T>, dim3(nb, E), 256, 0, st, (T*)md->grid_t[n], (T*)md->grid_ps[n],
+                     (const T*)(md->d_scalars + 4 * E), (size_t)nd * G1, G1));
   mark(st);
   JG_CUDA(cudaGetLastError());
   JG_TRY(issue_hs_grad<T>(md, n, br));
@@ -2923,6 +2986,7 @@ ImplArgs<T> si_args(jgcm_model* md, void* const* in, void* const* out) {
   ia.kappa = md->P.kappa;
   ia.rdgas = md->P.rdgas;
   ia.robert = md->P.robert_coef;
+  impl_consts<T>(ia, tables<T>(md->mesh).eig);
   return ia;
 }
 }  // namespace

@@ -22,7 +22,7 @@ __device__ __forceinline__ const G& group_of(const G* g, int ng, int c, int* k) 
 // Fused spectral time stepping used by the G2S epilogues (Time_Integrator.jl:58-101).
 template <typename T>
 __device__ __forceinline__ void damp_leapfrog(const StepParams& sp, T d, T& dq, T qp, T& qc, T& qn) {
-  const T r = (T)sp.robert;
+  const T r = pick<T>(sp.robert, sp.robertf);
   const int Dt = sp.dt;
   if (sp.init_step) {
     dq = (dq - qc * d) / ((T)1.0 + (T)Dt * d);
@@ -60,7 +60,7 @@ __device__ __forceinline__ V2<T> s2g_input(const S2GGroup& g, const Tables<T>& t
   switch (g.op) {
     case S2G_PLAIN:
       x = a[(mrow + n) * L + k];
-      if (m == 0 && n == 0) x.x = x.x - (T)g.shift;
+      if (m == 0 && n == 0) x.x = x.x - pick<T>(g.shift, g.shiftf);
       break;
     case S2G_ADJ_G2S:  // the synthesis weights every m >= 1 twice; the analysis never sees row N+1
       if (n < ns) {
@@ -174,13 +174,13 @@ __device__ __forceinline__ void g2s_store(const G2SPlan& plan, const SpecOutGrou
       ddiv.x = ddiv.x - eig * (kin.x + hc.x);
       ddiv.y = ddiv.y - eig * (kin.y + hc.y);
       // Implicit_Correction! (SW) :25-54
-      const T h0 = (T)plan.sp.h0;
-      const T Dt = plan.sp.init_step ? (T)plan.sp.dt : (T)(2.0 * plan.sp.dt);
+      const T h0 = pick<T>(plan.sp.h0, plan.sp.h0f);
+      const T Dt = plan.sp.init_step ? (T)plan.sp.dt : (T)(2 * plan.sp.dt);
       ddiv.x = ddiv.x + eig * (hc.x - hp.x);
       ddiv.y = ddiv.y + eig * (hc.y - hp.y);
       dh.x = dh.x + h0 * (dc.x - dp.x);
       dh.y = dh.y + h0 * (dc.y - dp.y);
-      const T mu = (T)plan.sp.implicit_coef * Dt, mu2 = mu * mu;
+      const T mu = pick<T>(plan.sp.implicit_coef, plan.sp.implicit_coeff) * Dt, mu2 = mu * mu;
       const T den = (T)1.0 - mu2 * eig * h0;
       ddiv.x = (ddiv.x - mu * eig * dh.x) / den;
       ddiv.y = (ddiv.y - mu * eig * dh.y) / den;

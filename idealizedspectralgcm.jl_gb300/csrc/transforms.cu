@@ -142,14 +142,14 @@ __device__ __forceinline__ void ifft_store(const GridOutGroup& g, const Tables<T
       dst[idx] = x / tb.cosj[j];
       break;
     case EPI_EXP2:
-      dst[idx] = x + (T)g.shift;
-      ((T*)g.dst2)[idx] = exp(x) * (T)exp(g.shift);
+      dst[idx] = x + pick<T>(g.shift, g.shiftf);
+      ((T*)g.dst2)[idx] = exp(x) * pick<T>(g.eshift, g.eshiftf);
       break;
     case EPI_DIVCOS_MULPS:
       dst[idx] = (x / tb.cosj[j]) * ((const T*)g.ps)[((size_t)k * nlat + j) * nlon + t];  // level k of ps
       break;
     case EPI_ADJ_G2S:
-      dst[idx] = x * (T)(tb.wts[j] / (2.0 * nlon));
+      dst[idx] = x * (tb.wts[j] / (T)(2 * nlon));
       break;
   }
 }
@@ -170,12 +170,12 @@ __device__ __forceinline__ T fft_load(const FFTPlan& plan, const GridInGroup& g,
     case PRO_FLUXU: {  // (-kappa_m u + (vor + f) v) cos   (Shallow_Water_Dynamics.jl:129, Barotropic :28)
       T u = s0[idx], v = ((const T*)g.s1)[idx], vor = ((const T*)g.s2)[idx];
       T absvor = vor + ((const T*)plan.coriolis)[j];
-      x = ((-(T)plan.kappa_m) * u + absvor * v) * cj;
+      x = ((-pick<T>(plan.kappa_m, plan.kappa_mf)) * u + absvor * v) * cj;
     } break;
     case PRO_FLUXV: {  // (-kappa_m v + (-(vor + f)) u) cos
       T u = s0[idx], v = ((const T*)g.s1)[idx], vor = ((const T*)g.s2)[idx];
       T absvor = vor + ((const T*)plan.coriolis)[j];
-      x = ((-(T)plan.kappa_m) * v + (-absvor) * u) * cj;
+      x = ((-pick<T>(plan.kappa_m, plan.kappa_mf)) * v + (-absvor) * u) * cj;
     } break;
     case PRO_KIN: {  // 0.5 (u^2 + v^2)
       T u = s0[idx], v = ((const T*)g.s1)[idx];
@@ -185,7 +185,7 @@ __device__ __forceinline__ T fft_load(const FFTPlan& plan, const GridInGroup& g,
       T h = s0[idx], u = ((const T*)g.s1)[idx], v = ((const T*)g.s2)[idx];
       T dl = ((const T*)g.s3)[idx], dt = ((const T*)g.s4)[idx], dv = ((const T*)g.s5)[idx];
       T heq = ((const T*)g.s6)[idx];
-      T d = (-(T)plan.kappa_t) * (h - heq);
+      T d = (-pick<T>(plan.kappa_t, plan.kappa_tf)) * (h - heq);
       d = d - (u * dl + v * dt);
       x = d - h * dv;
     } break;
@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(256) k_fft(FFTPlan plan, Tables<T> tb, V2<T>* 
   }
   __syncthreads();
   fft_stages<T, -1>(re, im, tw, CT, h, logh);
-  const T scale = (T)(0.5 / nlon);
+  const T scale = (T)0.5 / (T)nlon;  // nlon is a power of two: exact
   for (int i = threadIdx.x; i < (N + 1) * ncol; i += blockDim.x) {
     int mm = i / ncol, cc = i - mm * ncol, c = cbase + cc;
     if (c >= C) continue;
@@ -476,7 +476,7 @@ __global__ void __launch_bounds__(256) k_fft_w(FFTPlan plan, Tables<T> tb, V2<T>
       Z[brev(lane + 32 * r, LOGH)] = z;
     }
     __syncwarp();
-    const T scale = (T)(0.5 / nlon);
+    const T scale = (T)0.5 / (T)nlon;  // nlon is a power of two: exact
     for (int mm = lane; mm <= N; mm += 32) {
       const int q = (H - mm) & (H - 1);
       const Vc zm = Z[mm], zq = Z[q];
@@ -626,7 +626,7 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
       si += __shfl_xor_sync(qmask, si, 1);
       sr += __shfl_xor_sync(qmask, sr, 2);
       si += __shfl_xor_sync(qmask, si, 2);
-      const T sc = (T)((m == 0 ? 1.0 : 2.0) * g.scale);  // scale = nlon (the FFT returned fft / nlon)
+      const T sc = (m == 0 ? (T)1 : (T)2) * pick<T>(g.scale, g.scalef);  // scale = nlon (the FFT returned fft / nlon)
       V o;
       o.x = sr * sc;
       o.y = si * sc;
@@ -690,14 +690,46 @@ static inline int fft_ct(const jgcm_mesh* m) {
   return m->tune[3] > 0 ? m->tune[3] : m->nlon >= 1024 ? 1 : 1024 / m->nlon;
 }
 
+// The plans' FP32 copies of their FP64 scalars (pick<T> in the kernels), filled here so that
+// every plan builder stays in FP64.
+static S2GPlan with_f32(const S2GPlan& p) {
+  S2GPlan q = p;
+  for (int i = 0; i < q.ng; i++) q.g[i].shiftf = (float)q.g[i].shift;
+  return q;
+}
+static IFFTPlan with_f32(const IFFTPlan& p) {
+  IFFTPlan q = p;
+  for (int i = 0; i < q.ng; i++) {
+    q.g[i].eshift = std::exp(q.g[i].shift);
+    q.g[i].shiftf = (float)q.g[i].shift;
+    q.g[i].eshiftf = (float)q.g[i].eshift;
+  }
+  return q;
+}
+static FFTPlan with_f32(const FFTPlan& p) {
+  FFTPlan q = p;
+  q.kappa_mf = (float)q.kappa_m;
+  q.kappa_tf = (float)q.kappa_t;
+  return q;
+}
+static G2SPlan with_f32(const G2SPlan& p) {
+  G2SPlan q = p;
+  q.sp.robertf = (float)q.sp.robert;
+  q.sp.implicit_coeff = (float)q.sp.implicit_coef;
+  q.sp.h0f = (float)q.sp.h0;
+  for (int i = 0; i < q.ng; i++) q.g[i].scalef = (float)q.g[i].scale;
+  return q;
+}
+
 template <typename T>
 static int launch_ifft_stage(jgcm_mesh* m, const IFFTPlan& ip, cudaStream_t st, V2<T>* fbuf);
 
 // Legendre synthesis then inverse FFT, with the Fourier coefficients staged in `fbuf`
 // ((N+1) x nlat x C complex T).
 template <typename T>
-static int launch_s2g_into(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, cudaStream_t st, V2<T>* fbuf) {
+static int launch_s2g_into(jgcm_mesh* m, const S2GPlan& sp0, const IFFTPlan& ip, cudaStream_t st, V2<T>* fbuf) {
   using V = V2<T>;
+  const S2GPlan sp = with_f32(sp0);
   JG_TRY(configure_smem<T>());
   Tables<T> tb = tables<T>(m);
   const int nh = m->nh, ct = s2g_ct(m);
@@ -715,8 +747,9 @@ static int launch_s2g_into(jgcm_mesh* m, const S2GPlan& sp, const IFFTPlan& ip, 
 
 // The inverse FFT stage alone (Fourier coefficients already in `fbuf`).
 template <typename T>
-static int launch_ifft_stage(jgcm_mesh* m, const IFFTPlan& ip, cudaStream_t st, V2<T>* fbuf) {
+static int launch_ifft_stage(jgcm_mesh* m, const IFFTPlan& ip0, cudaStream_t st, V2<T>* fbuf) {
   using V = V2<T>;
+  const IFFTPlan ip = with_f32(ip0);
   Tables<T> tb = tables<T>(m);
   const int fc = fft_ct(m);
   // the warp-register FFT wins in FP32; in FP64 the shared-memory radix-2 kernel is faster (measured)
@@ -764,8 +797,9 @@ int launch_ifft_only(jgcm_mesh* m, const IFFTPlan& ip, cudaStream_t st, void* fb
 }
 
 template <typename T>
-int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp, cudaStream_t st, void* fbuf, int cap) {
+int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp0, cudaStream_t st, void* fbuf, int cap) {
   using V = V2<T>;
+  const FFTPlan fp = with_f32(fp0);
   JG_TRY(configure_smem<T>());
   if (!fbuf) {
     fbuf = m->d_fbuf;
@@ -798,8 +832,9 @@ int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp, cudaStream_t st, void* fbuf
 }
 
 template <typename T>
-int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp, cudaStream_t st, void* fbuf, int cap) {
+int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp0, cudaStream_t st, void* fbuf, int cap) {
   using V = V2<T>;
+  const G2SPlan gp = with_f32(gp0);
   if (!fbuf) {
     fbuf = m->d_fbuf;
     cap = m->Cmax;
