@@ -13,6 +13,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 #include <utility>
 
 #include "jgcm.h"
@@ -240,6 +241,7 @@ struct jgcm_mesh {
   int refs;           // 1 for the caller's handle + 1 per live model built on the mesh
   int device;         // CUDA device the mesh lives on
   std::string name;
+  std::vector<float> twf_host;  // the FP32 twiddle table (cos, sin of 2π t / nlon, t < nlon/2) on the host
 };
 
 namespace jgcm {

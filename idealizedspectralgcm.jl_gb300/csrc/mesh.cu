@@ -204,6 +204,8 @@ int mesh_build_tables(jgcm_mesh* m) {
   k_derive1<<<(n1 + 127) / 128, 128, 0, st>>>(nlat, nlon, m->d_sinth, m->d_costh, m->t64.cosj, m->t64.sinj, m->t64.tw,
                                               m->t32.cosj, m->t32.sinj, m->t32.tw);
   JG_CUDA(cudaGetLastError());
+  m->twf_host.assign(nlon, 0.0f);
+  JG_CUDA(cudaMemcpyAsync(m->twf_host.data(), m->t32.tw, (size_t)nlon * sizeof(float), cudaMemcpyDeviceToHost, st));
   int h_status = 0;
   JG_CUDA(cudaMemcpyAsync(&h_status, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
   JG_CUDA(cudaStreamSynchronize(st));

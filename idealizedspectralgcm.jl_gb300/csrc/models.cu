@@ -76,8 +76,10 @@ __device__ __forceinline__ T shfl_dn1(T x, int lane, int nd, T fill) {
 // Deterministic grid-wide FP64 reduction over a (x = column chunk, y = latitude) grid.  Thread 0
 // of every block passes its NV block sums; the last block to finish (atomic ticket) folds the
 // partials in a fixed order, sum_j w_j sum_b partial[v][j][b], and returns true with the NV
-// totals in out[] (valid in every thread of that block).  All other blocks return false.
-template <int NV>
+// totals in out[] (valid in every thread of that block).  All other blocks return false.  U
+// partials per thread are loaded before they are added (in their fixed order): latency hidden when
+// a thread folds many partials, at U * NV * 2 registers of the whole kernel.
+template <int NV, int U = 1>
 __device__ bool grid_reduce_last(const double* vals, double* partials, unsigned* counter, const double* wts,
                                  double* out) {
   __shared__ bool am_last;
@@ -97,7 +99,6 @@ __device__ bool grid_reduce_last(const double* vals, double* partials, unsigned*
   // the block's row), then warps and the block combine in a fixed order: deterministic
   double s[NV];
   for (int v = 0; v < NV; v++) s[v] = 0.0;
-  constexpr int U = 8;  // loads in flight per thread; the additions keep their order
   for (int b0 = threadIdx.x; b0 < nb; b0 += U * blockDim.x) {
     double pv[U][NV], wv[U];
 #pragma unroll
@@ -389,7 +390,8 @@ __global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertC
     }
   double tot2[2];
   double* scal = a.scalars + 4 * e;
-  if (grid_reduce_last<2>(vals, a.partials + e * a.pstride, a.counter + e, a.wts, tot2) && threadIdx.x == 0) {
+  // 64 threads fold (nlon / (64 / S)) x nlat partials (512 at T42 with S = 4): 8 loads in flight each
+  if (grid_reduce_last<2, 8>(vals, a.partials + e * a.pstride, a.counter + e, a.wts, tot2) && threadIdx.x == 0) {
     scal[0] = tot2[0] / (2.0 * nlon);           // mean_ps_p   (Area_Weighted_Global_Mean)
     scal[1] = tot2[1] / (2.0 * nlon) / a.grav;  // mean_energy_p (Mass_Weighted_Global_Integral)
   }
@@ -661,6 +663,7 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   T ea = 0, eb = 0;
   if (act) {
     const T cp = (T)a.cp;
+#pragma unroll 4  // nd <= 32: every level's loads in flight together
     for (int k = ks; k < nd; k += KS) {
       size_t x = offL + (size_t)k * G + col;
       T u = a.u_n[x], v = a.v_n[x], t = a.t_n[x];
@@ -2640,7 +2643,7 @@ extern "C" int jgcm_model_set_tuning(jgcm_model* md, const int* knobs, int n) {
   jgcm_mesh* m = md->mesh;
   const int lanes = knobs[0] > 0 ? knobs[0] : hs_lanes(m, md->ne, md->nd);
   JG_ARG(lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8, "lanes per column must be 1, 2, 4 or 8");
-  for (int i = 1; i < 4; i++) JG_ARG(knobs[i] >= 0 && knobs[i] <= 256, "tile %d out of range", i);
+  for (int i = 1; i < 4; i++) JG_ARG(knobs[i] >= (i == 3 ? -1 : 0) && knobs[i] <= 256, "tile %d out of range", i);
   int t[4] = {0, knobs[1], knobs[2], knobs[3]};
   const int s2g = t[1] > 0 ? t[1] : (m->nh >= 256 ? 1 : 256 / m->nh);
   const int g2s = t[2] > 0 ? t[2] : (m->nh >= 64 ? 4 : m->nh >= 32 ? 8 : 16);

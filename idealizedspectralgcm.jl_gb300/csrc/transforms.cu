@@ -497,6 +497,190 @@ __global__ void __launch_bounds__(256) k_fft_w(FFTPlan plan, Tables<T> tb, V2<T>
   }
 }
 
+// ------------------------------------------------------------------------------------------
+// Row-per-thread real FFTs (FP32, nlon = 64 or 128) for transforms with many (column, latitude) rows
+// (member ensembles).  Each thread transforms one row in registers: the H = nlon/2 point complex
+// transform as radix-2 stages unrolled at compile time, with the twiddles passed as a kernel
+// parameter and read at compile-time indices (constant-bank operands: no loads, shuffles or block
+// barriers in the transform).  A warp's 32 rows pass through padded shared memory, so that every
+// global read and write is a coalesced row (grid) or a run of 32 consecutive columns (Fourier).
+// Same arithmetic as k_fft_w / k_ifft_w: the half-length complex transform of the real row.
+template <int NLON>
+struct RowTwiddles {
+  float c[NLON / 2], s[NLON / 2];  // cos, sin of 2π t / nlon
+};
+constexpr int RF_WARPS = 4;               // warps per block, 32 rows each
+constexpr size_t kRowsMin = 152 * 4 * 32;  // rows from which the row-per-thread kernels are used
+
+__host__ __device__ constexpr int brev_c(int x, int bits) {
+  int r = 0;
+  for (int b = 0; b < bits; b++) r |= ((x >> b) & 1) << (bits - 1 - b);
+  return r;
+}
+
+template <int NLON>
+__global__ void __launch_bounds__(32 * RF_WARPS) k_fft_rows(FFTPlan plan, Tables<float> tb, RowTwiddles<NLON> tw,
+                                                            float2* __restrict__ F, int N, int nlat) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
+  constexpr int H = NLON / 2, P = NLON + 1, LOGH = NLON == 64 ? 5 : 6;
+  extern __shared__ float rsm[];
+  const int j = blockIdx.y, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int C = plan.C, c0 = (blockIdx.x * RF_WARPS + w) * 32;
+  if (c0 >= C) return;  // whole warp; no block barrier follows
+  float* S = rsm + (size_t)w * 32 * P;
+  const int nr = min(32, C - c0);
+  const float cj = tb.cosj[j];
+  // row r = column c0 + r, lanes along longitude (coalesced); 16 rows' loads are issued before any
+  // of them is stored, so their latencies overlap
+  constexpr int RB = 16;
+#pragma unroll
+  for (int rb = 0; rb < 32; rb += RB) {
+    float v[RB][NLON / 32];
+#pragma unroll
+    for (int rr = 0; rr < RB; rr++) {
+#pragma unroll
+      for (int q = 0; q < NLON / 32; q++) v[rr][q] = 0.f;
+      if (rb + rr < nr) {
+        int k;
+        const GridInGroup& g = group_of(plan.g, plan.ng, c0 + rb + rr, &k);
+#pragma unroll
+        for (int q = 0; q < NLON / 32; q++) v[rr][q] = fft_load<float>(plan, g, k, j, lane + 32 * q, nlat, NLON, cj);
+      }
+    }
+#pragma unroll
+    for (int rr = 0; rr < RB; rr++)
+#pragma unroll
+      for (int q = 0; q < NLON / 32; q++) S[(rb + rr) * P + lane + 32 * q] = v[rr][q];
+  }
+  __syncwarp();
+  if (lane >= nr) return;
+  float re[H], im[H];  // z[i] = x[2i] + i x[2i+1], natural order
+#pragma unroll
+  for (int i = 0; i < H; i++) {
+    re[i] = S[lane * P + 2 * i];
+    im[i] = S[lane * P + 2 * i + 1];
+  }
+  // decimation in frequency, w = e^{-2πi jj/(2s)} = tw[jj nlon/(2s)]: bit-reversed output
+#pragma unroll
+  for (int s = H / 2; s >= 1; s >>= 1) {
+#pragma unroll
+    for (int b = 0; b < H; b += 2 * s) {
+#pragma unroll
+      for (int jj = 0; jj < s; jj++) {
+        const int i0 = b + jj, i1 = i0 + s, t = jj * (NLON / (2 * s));
+        const float ar = re[i0], ai = im[i0], br = re[i1], bi = im[i1];
+        re[i0] = ar + br;
+        im[i0] = ai + bi;
+        const float dr = ar - br, di = ai - bi;
+        re[i1] = dr * tw.c[t] + di * tw.s[t];
+        im[i1] = di * tw.c[t] - dr * tw.s[t];
+      }
+    }
+  }
+  // X[m] = (E_m + e^{-2πim/nλ} O_m) / nλ for m <= N, from Z[m] and Z[H - m]
+  const float scale = 0.5f / (float)NLON;
+  const int c = c0 + lane;
+#pragma unroll
+  for (int mm = 0; mm < H; mm++) {
+    if (mm <= N) {
+      const int zi = brev_c(mm, LOGH), qi = brev_c((H - mm) & (H - 1), LOGH);
+      const float er = re[zi] + re[qi], ei = im[zi] - im[qi];  // 2 E
+      const float orr = im[zi] + im[qi], oi = re[qi] - re[zi];  // 2 O
+      const float tc = tw.c[mm], ts = tw.s[mm];
+      float2 o;
+      o.x = (er + (tc * orr + ts * oi)) * scale;
+      o.y = (ei + (tc * oi - ts * orr)) * scale;
+      F[((size_t)mm * nlat + j) * C + c] = o;
+    }
+  }
+}
+
+template <int NLON>
+__global__ void __launch_bounds__(32 * RF_WARPS) k_ifft_rows(IFFTPlan plan, Tables<float> tb, RowTwiddles<NLON> tw,
+                                                             const float2* __restrict__ F, int N, int nlat) {
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
+  constexpr int H = NLON / 2, P = NLON + 1, LOGH = NLON == 64 ? 5 : 6;
+  extern __shared__ float rsm[];
+  const int j = blockIdx.y, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int C = plan.C, c0 = (blockIdx.x * RF_WARPS + w) * 32;
+  if (c0 >= C) return;  // whole warp; no block barrier follows
+  float* S = rsm + (size_t)w * 32 * P;
+  const int nr = min(32, C - c0);
+  if (lane < nr) {
+    const int c = c0 + lane;
+    auto X = [&](int mm) -> float2 {  // coefficient m of this column (Re only for m = 0), 0 above N
+      float2 x = make_float2(0.f, 0.f);
+      if (mm <= N) x = F[((size_t)mm * nlat + j) * C + c];
+      if (mm == 0) x.y = 0.f;
+      return x;
+    };
+    // Z[m] = (X[m] + conj X[H-m]) + i e^{2πim/nλ} (X[m] - conj X[H-m]), placed bit-reversed
+    float re[H], im[H];
+#pragma unroll
+    for (int mm = 0; mm < H; mm++) {
+      const float2 x = X(mm);
+      const float2 y = mm >= 1 ? X(H - mm) : make_float2(0.f, 0.f);
+      const float er = x.x + y.x, ei = x.y - y.y, dr = x.x - y.x, di = x.y + y.y;
+      const float cs = tw.c[mm], sn = tw.s[mm];
+      const float orr = dr * cs - di * sn, oi = dr * sn + di * cs;
+      re[brev_c(mm, LOGH)] = er - oi;
+      im[brev_c(mm, LOGH)] = ei + orr;
+    }
+    // decimation in time, w = e^{+2πi jj/(2s)}: natural output
+#pragma unroll
+    for (int s = 1; s < H; s <<= 1) {
+#pragma unroll
+      for (int b = 0; b < H; b += 2 * s) {
+#pragma unroll
+        for (int jj = 0; jj < s; jj++) {
+          const int i0 = b + jj, i1 = i0 + s, t = jj * (NLON / (2 * s));
+          const float br = re[i1], bi = im[i1];
+          const float tr = br * tw.c[t] - bi * tw.s[t], ti = br * tw.s[t] + bi * tw.c[t];
+          re[i1] = re[i0] - tr;
+          im[i1] = im[i0] - ti;
+          re[i0] = re[i0] + tr;
+          im[i0] = im[i0] + ti;
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < H; i++) {  // x[2i] = Re z[i], x[2i+1] = Im z[i]
+      S[lane * P + 2 * i] = re[i];
+      S[lane * P + 2 * i + 1] = im[i];
+    }
+  }
+  __syncwarp();
+#pragma unroll 4
+  for (int r = 0; r < 32; r++) {  // row r = column c0 + r, lanes along longitude (coalesced)
+    if (r < nr) {
+      int k;
+      const GridOutGroup& g = group_of(plan.g, plan.ng, c0 + r, &k);
+#pragma unroll
+      for (int q = 0; q < NLON / 32; q++)
+        ifft_store<float>(g, tb, k, j, lane + 32 * q, nlat, NLON, S[r * P + lane + 32 * q]);
+    }
+  }
+}
+
+template <int NLON>
+RowTwiddles<NLON> row_twiddles(const jgcm_mesh* m) {
+  RowTwiddles<NLON> t;
+  for (int q = 0; q < NLON / 2; q++) {
+    t.c[q] = m->twf_host[2 * q];
+    t.s[q] = m->twf_host[2 * q + 1];
+  }
+  return t;
+}
+
+// FFT tile knob: 0 = by size (nlon 64 rows one per thread from kRowsMin rows on; at nlon 128 the
+// thread holds 64 complex points and its 164-254 registers cost more occupancy than the warp FFT's
+// shuffles, measured), -1 = rows per thread always (nlon 64 and 128)
+static inline bool use_row_fft(const jgcm_mesh* m, int C) {
+  if (m->tune[3] == -1) return m->nlon == 64 || m->nlon == 128;
+  return m->tune[3] == 0 && m->nlon == 64 && (size_t)C * m->nlat >= kRowsMin;
+}
+static inline size_t row_fft_smem(const jgcm_mesh* m) { return (size_t)RF_WARPS * 32 * (m->nlon + 1) * sizeof(float); }
+
 // Fourier -> spectral: Gaussian quadrature per m.  grid (ceil(Cout/CT), N+1), 256 threads.
 // Shared memory holds, for 4 input slots, the hemisphere-symmetric and -antisymmetric
 // combinations g(mu_j) +/- g(-mu_j) of the tile's columns.
@@ -674,6 +858,12 @@ static int configure_smem() {
   JG_CUDA(cudaFuncSetAttribute(k_ifft<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   JG_CUDA(cudaFuncSetAttribute(k_fft<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   JG_CUDA(cudaFuncSetAttribute(k_g2s_legendre<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  if (idx == 0) {
+    JG_CUDA(cudaFuncSetAttribute(k_fft_rows<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    JG_CUDA(cudaFuncSetAttribute(k_fft_rows<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    JG_CUDA(cudaFuncSetAttribute(k_ifft_rows<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    JG_CUDA(cudaFuncSetAttribute(k_ifft_rows<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  }
   g_smem_configured[idx] = 1;
   return JGCM_OK;
 }
@@ -752,6 +942,18 @@ static int launch_ifft_stage(jgcm_mesh* m, const IFFTPlan& ip0, cudaStream_t st,
   const IFFTPlan ip = with_f32(ip0);
   Tables<T> tb = tables<T>(m);
   const int fc = fft_ct(m);
+  if (std::is_same<T, float>::value && use_row_fft(m, ip.C)) {  // many rows: a row per thread
+    dim3 gr((ip.C + 32 * RF_WARPS - 1) / (32 * RF_WARPS), m->nlat);
+    const Tables<float> tf = tables<float>(m);
+    const float2* Ff = (const float2*)fbuf;
+    if (m->nlon == 64)
+      JG_CUDA(launch_pdl(k_ifft_rows<64>, gr, 32 * RF_WARPS, row_fft_smem(m), st, ip, tf, row_twiddles<64>(m), Ff, m->N, m->nlat));
+    else
+      JG_CUDA(launch_pdl(k_ifft_rows<128>, gr, 32 * RF_WARPS, row_fft_smem(m), st, ip, tf, row_twiddles<128>(m), Ff, m->N, m->nlat));
+    mark(st);
+    JG_CUDA(cudaGetLastError());
+    return JGCM_OK;
+  }
   // the warp-register FFT wins in FP32; in FP64 the shared-memory radix-2 kernel is faster (measured)
   if (std::is_same<T, float>::value && m->nlon >= 64 && m->nlon <= 1024 && m->tune[3] == 0) {
     const size_t smw = (size_t)(m->N + 1) * FW_COLS * sizeof(V);
@@ -808,6 +1010,18 @@ int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp0, cudaStream_t st, void* fbu
   JG_ARG(fp.C <= cap && fp.C > 0, "bad FFT plan");
   Tables<T> tb = tables<T>(m);
   const int fc = fft_ct(m);
+  if (std::is_same<T, float>::value && use_row_fft(m, fp.C)) {  // many rows: a row per thread
+    dim3 gr((fp.C + 32 * RF_WARPS - 1) / (32 * RF_WARPS), m->nlat);
+    const Tables<float> tf = tables<float>(m);
+    float2* Ff = (float2*)fbuf;
+    if (m->nlon == 64)
+      JG_CUDA(launch_pdl(k_fft_rows<64>, gr, 32 * RF_WARPS, row_fft_smem(m), st, fp, tf, row_twiddles<64>(m), Ff, m->N, m->nlat));
+    else
+      JG_CUDA(launch_pdl(k_fft_rows<128>, gr, 32 * RF_WARPS, row_fft_smem(m), st, fp, tf, row_twiddles<128>(m), Ff, m->N, m->nlat));
+    mark(st);
+    JG_CUDA(cudaGetLastError());
+    return JGCM_OK;
+  }
   // forward: the warp-register FFT wins in FP32 from nlon = 128 on (measured)
   if (std::is_same<T, float>::value && m->nlon >= 128 && m->nlon <= 1024 && m->tune[3] == 0) {
     const size_t smw = ((size_t)FW_COLS * (m->nlon / 2) + (size_t)(m->N + 1) * FW_COLS) * sizeof(V);

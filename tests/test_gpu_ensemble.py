@@ -61,6 +61,39 @@ def test_ensemble_matches_members(jg, name, prec, members, steps):
     print(name, prec, members, "worst", worst)
 
 
+@pytest.mark.parametrize("name,members", [("hs_t21l20", 16), ("hs_t42l20", 8)])
+def test_large_fp32_ensemble_matches_oracle(jg, orc, name, members):
+    """Member-batched FP32 steps at scale (T21: enough members that every zonal FFT runs one row
+    per thread, k_fft_rows / k_ifft_rows): the first and last members, stepped from a developed
+    flow, equal the oracle's steps (the FP32 step tolerance of the single-member parity tests)."""
+    params = configs.PARAMS[name]
+    gm, om = configs.make_mesh(jg, name, precision="fp32"), configs.make_mesh(orc, name)
+    ens = jg.Model(gm, params, members=members)
+    refs = {}
+    for e in range(members):
+        omod = orc.Model(om, params)
+        configs.init_held_suarez(orc, om, omod, seed=configs.BASE_SEED + e)
+        configs.add_hs_flow(orc, om, omod)
+        one = jg.Model(gm, params)
+        configs.copy_state(omod, one, "held_suarez")
+        ens.copy_member(e, one)
+        if e in (0, members - 1):
+            refs[e] = omod
+    ens.step(1)
+    ens.step(3)
+    for omod in refs.values():
+        omod.step(4)
+    out = jg.Model(gm, params)
+    for e, omod in refs.items():
+        out.copy_member(0, ens, e)
+        for f in configs.PROGNOSTIC["held_suarez"]:
+            den = np.linalg.norm(omod.get(f).ravel())
+            if f.startswith("spe_div") or f == "grid_div":
+                den = max(den, np.linalg.norm(omod.get(f.replace("div", "vor")).ravel()))
+            err = float(np.linalg.norm((out.get(f) - omod.get(f)).ravel()) / den)
+            assert err < 1e-3, (e, f, err)
+
+
 def test_ensemble_rejects_direct_field_access(jg):
     params = configs.PARAMS["hs_t21l20"]
     mesh = configs.make_mesh(jg, "hs_t21l20", precision="fp32")

@@ -82,6 +82,36 @@ def test_grid_to_spherical(jg, orc, case, prec):
             assert np.all(a[mm, :mm, :] == 0)
 
 
+@pytest.mark.parametrize("prec", ["fp32", "tf32x3"])
+@pytest.mark.parametrize("name", ["hs_t21l20", "hs_t42l20"])
+def test_row_per_thread_ffts(jg, orc, name, prec):
+    """The row-per-thread FFT kernels (k_fft_rows / k_ifft_rows, nlon 64 and 128; chosen by size for
+    member ensembles) forced on through the FFT tile knob of a model on the mesh."""
+    g = configs.GRIDS[name]
+    N, nlat, nlon, nd = g["num_fourier"], g["nlat"], g["nlon"], g["nd"]
+    gm, om = _meshes(jg, orc, N, nlat, nlon, nd, prec)
+    md = jg.Model(gm, configs.PARAMS[name])
+    jg.set_tuning(md, dict(jg.get_tuning(md), fft_columns=-1))
+    s = _spec(om, nd, 17)
+    a, b = gm.grid(nd), om.grid(nd)
+    jg.Trans_Spherical_To_Grid(gm, s, a)
+    orc.Trans_Spherical_To_Grid(om, s, b)
+    assert configs.rel_l2(a, b) < TOL[prec]
+    gr = _grid(om, nd, 19)
+    a, b = gm.spectral(nd), om.spectral(nd)
+    jg.Trans_Grid_To_Spherical(gm, gr, a)
+    orc.Trans_Grid_To_Spherical(om, gr, b)
+    assert configs.rel_l2(a, b) < TOL[prec]
+    f = np.zeros((N + 1, nlat, nd), dtype=np.complex128, order="F")
+    jg.Trans_Grid_To_Fourier(gm, gr, f)
+    ref = np.zeros((nlon, nlat, nd), dtype=np.complex128, order="F")
+    orc.Trans_Grid_To_Fourier(om, gr, ref)
+    assert configs.rel_l2(f, ref[: N + 1]) < TOL[prec]
+    err = (np.linalg.norm((f - ref[: N + 1]).reshape(-1, nd), axis=0)
+           / np.linalg.norm(ref[: N + 1].reshape(-1, nd), axis=0))
+    assert err.max() < 4 * TOL[prec], err.max()  # every level, not only the whole
+
+
 @pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("case", CASES[:2])
 def test_grid_to_fourier(jg, orc, case, prec):
