@@ -531,7 +531,11 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="only the mixed-precision headline model: --warmup then --steps sim-days with the tiles of "
                          "--tiles (no autotuning, no other model), a short launch sequence for ncu")
-    ap.add_argument("--tiles", default="4,4,4,0", help="lanes per column, S2G, G2S, FFT columns per block (--profile)")
+    ap.add_argument("--tiles", default="4,4,4,0",
+                    help="lanes per column, S2G, G2S, FFT columns per block, or 'auto' for the autotuner (--profile)")
+    ap.add_argument("--profile-members", type=int, default=1, metavar="E",
+                    help="--profile: E member-batched members (seeds base + e); after the timing, one eager "
+                         "step runs inside a CUDA profiler range (ncu --profile-from-start off captures it)")
     ap.add_argument("--ensemble-only", default=None, metavar="PRECISIONS",
                     help="run only the batched-ensemble measurement for these precisions (comma list, e.g. "
                          "fp32,tf32x3) over --steps days and print its JSON (for profiling the ensemble kernels)")
@@ -550,15 +554,34 @@ def main():
             from jgcm import configs
 
             jgcm.set_device(int(os.environ.get("LOCAL_RANK", 0)))
-            spd = configs.STEPS_PER_DAY[WORKLOAD]
-            m = configs.make_mesh(jgcm, WORKLOAD, precision=args.precision)
-            md = jgcm.Model(m, configs.PARAMS[WORKLOAD])
-            configs.init_held_suarez(jgcm, m, md)
-            jgcm.set_tuning(md, dict(zip(jgcm.TUNING_KNOBS, [int(x) for x in args.tiles.split(",")])))
+            name = WORKLOAD if args.profile_members == 1 else "hs_t21l20"
+            spd = configs.STEPS_PER_DAY[name]
+            m = configs.make_mesh(jgcm, name, precision=args.precision)
+            E = args.profile_members
+            md = jgcm.Model(m, configs.PARAMS[name], members=E)
+            if E == 1:
+                configs.init_held_suarez(jgcm, m, md)
+            else:
+                one = jgcm.Model(m, configs.PARAMS[name])
+                for e in range(E):
+                    configs.init_held_suarez(jgcm, m, one, seed=configs.BASE_SEED + e)
+                    md.copy_member(e, one)
+                one.close()
+            md.step(1)
+            if args.tiles == "auto":
+                jgcm.autotune(md, nsteps=8)
+            else:
+                jgcm.set_tuning(md, dict(zip(jgcm.TUNING_KNOBS, [int(x) for x in args.tiles.split(",")])))
             md.step(spd * args.warmup)
             ms = [md.time_steps(spd) for _ in range(args.steps)]
-            print(json.dumps({"profile": WORKLOAD, "precision": args.precision, "tiles": args.tiles,
-                              "ms_per_sim_day": ms}), flush=True)
+            import ctypes
+
+            cuda = ctypes.CDLL("libcuda.so.1")
+            cuda.cuProfilerStart()
+            kt = md.kernel_times(1)  # one eager step, its kernels serialised
+            cuda.cuProfilerStop()
+            print(json.dumps({"profile": name, "members": E, "precision": args.precision,
+                              "tuning": jgcm.get_tuning(md), "ms_per_sim_day": ms, "kernel_ms": kt}), flush=True)
             return 0
         if args.ensemble_only:
             import jgcm
