@@ -574,16 +574,20 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCo
   if (n <= a.N) {
     const double* W = a.W + (size_t)n * nd * nd;
     const double bxl = (double)ddiv.x, byl = (double)ddiv.y;
-    double wv[32];  // row k of W_n, fetched up front (independent loads in flight together)
-#pragma unroll
-    for (int c = 0; c < 32; c++) wv[c] = (act && c < nd) ? W[(size_t)c * nd + k] : 0.0;
     double sx = 0, sy = 0;
+    // row k of W_n in chunks of 8 (8 loads in flight; the whole row would hold 64 registers and
+    // cost the kernel occupancy it needs to overlap its FP32 scans with other warps' FP64 products)
+    for (int c0 = 0; c0 < nd; c0 += 8) {  // nd is warp-uniform
+      double wv[8];
 #pragma unroll
-    for (int c = 0; c < 32; c++) {
-      if (c < nd) {  // nd is warp-uniform
-        double bx = __shfl_sync(FULL, bxl, c), by = __shfl_sync(FULL, byl, c);
-        sx = sx + wv[c] * bx;
-        sy = sy + wv[c] * by;
+      for (int cc = 0; cc < 8; cc++) wv[cc] = (act && c0 + cc < nd) ? W[(size_t)(c0 + cc) * nd + k] : 0.0;
+#pragma unroll
+      for (int cc = 0; cc < 8; cc++) {
+        if (c0 + cc < nd) {
+          double bx = __shfl_sync(FULL, bxl, c0 + cc), by = __shfl_sync(FULL, byl, c0 + cc);
+          sx = sx + wv[cc] * bx;
+          sy = sy + wv[cc] * by;
+        }
       }
     }
     ddiv.x = act ? (R)sx : (R)0;
