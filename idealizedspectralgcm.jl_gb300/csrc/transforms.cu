@@ -596,7 +596,7 @@ __global__ void __launch_bounds__(32 * RF_WARPS) k_fft_rows(FFTPlan plan, Tables
 }
 
 template <int NLON>
-__global__ void __launch_bounds__(32 * RF_WARPS) k_ifft_rows(IFFTPlan plan, Tables<float> tb, RowTwiddles<NLON> tw,
+__global__ void __launch_bounds__(32 * RF_WARPS, NLON == 64 ? 6 : 1) k_ifft_rows(IFFTPlan plan, Tables<float> tb, RowTwiddles<NLON> tw,
                                                              const float2* __restrict__ F, int N, int nlat) {
   pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   constexpr int H = NLON / 2, P = NLON + 1, LOGH = NLON == 64 ? 5 : 6;
@@ -614,17 +614,22 @@ __global__ void __launch_bounds__(32 * RF_WARPS) k_ifft_rows(IFFTPlan plan, Tabl
       if (mm == 0) x.y = 0.f;
       return x;
     };
-    // Z[m] = (X[m] + conj X[H-m]) + i e^{2πim/nλ} (X[m] - conj X[H-m]), placed bit-reversed
+    // Z[m] = (X[m] + conj X[H-m]) + i e^{2πim/nλ} (X[m] - conj X[H-m]), placed bit-reversed; Z[m]
+    // and Z[H-m] from the same pair, each coefficient loaded once (short live ranges)
     float re[H], im[H];
-#pragma unroll
-    for (int mm = 0; mm < H; mm++) {
-      const float2 x = X(mm);
-      const float2 y = mm >= 1 ? X(H - mm) : make_float2(0.f, 0.f);
+    auto zput = [&](int mm, float2 x, float2 y) {
       const float er = x.x + y.x, ei = x.y - y.y, dr = x.x - y.x, di = x.y + y.y;
       const float cs = tw.c[mm], sn = tw.s[mm];
       const float orr = dr * cs - di * sn, oi = dr * sn + di * cs;
       re[brev_c(mm, LOGH)] = er - oi;
       im[brev_c(mm, LOGH)] = ei + orr;
+    };
+    zput(0, X(0), make_float2(0.f, 0.f));
+#pragma unroll
+    for (int mm = 1; mm <= H / 2; mm++) {
+      const float2 a = X(mm), b = X(H - mm);
+      zput(mm, a, b);
+      if (mm < H / 2) zput(H - mm, b, a);
     }
     // decimation in time, w = e^{+2πi jj/(2s)}: natural output
 #pragma unroll
