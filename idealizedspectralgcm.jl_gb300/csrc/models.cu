@@ -76,7 +76,7 @@ __device__ __forceinline__ T shfl_dn1(T x, int lane, int nd, T fill) {
 // Deterministic grid-wide FP64 reduction over a (x = column chunk, y = latitude) grid.  Thread 0
 // of every block passes its NV block sums; the last block to finish (atomic ticket) folds the
 // partials in a fixed order, sum_j w_j sum_b partial[v][j][b], and returns true with the NV
-// totals in out[] (valid in every thread of that block).  All other blocks return false.  U
+// totals in out[] of its thread 0.  All other blocks return false.  U
 // partials per thread are loaded before they are added (in their fixed order): latency hidden when
 // a thread folds many partials, at U * NV * 2 registers of the whole kernel.
 template <int NV, int U = 1>
@@ -119,12 +119,14 @@ __device__ bool grid_reduce_last(const double* vals, double* partials, unsigned*
   if ((threadIdx.x & 31) == 0)
     for (int v = 0; v < NV; v++) red[v][threadIdx.x >> 5] = s[v];
   __syncthreads();
-  for (int v = 0; v < NV; v++) {
-    double t = 0.0;
-    for (int q = 0; q < nw; q++) t += red[v][q];
-    out[v] = t;
+  if (threadIdx.x == 0) {  // the caller reads the totals in thread 0 (FP64 work on one warp only)
+    for (int v = 0; v < NV; v++) {
+      double t = 0.0;
+      for (int q = 0; q < nw; q++) t += red[v][q];
+      out[v] = t;
+    }
+    *counter = 0u;
   }
-  if (threadIdx.x == 0) *counter = 0u;
   return true;
 }
 
@@ -151,6 +153,7 @@ struct HSColArgs {
   size_t pstride;
   int nd, nlat, nlon, Dt;
   double sigma_b, k_f, k_a, k_s, dT_y, dtheta_z, kappa, rdgas, cp, grav;
+  double inv_2n;  // 1 / (2 nlon), exact (nlon is a power of two)
   // the physics constants in T, formed on the host with the kernel's own T arithmetic (no FP64 ->
   // FP32 conversion per thread: those run on the FP64 pipe)
   T sb, R, kap, cp_t, kv0, ka, ks, kt0, dTy, dthz, kappa_t;
@@ -392,8 +395,8 @@ __global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertC
   double* scal = a.scalars + 4 * e;
   // 64 threads fold (nlon / (64 / S)) x nlat partials (512 at T42 with S = 4): 8 loads in flight each
   if (grid_reduce_last<2, 8>(vals, a.partials + e * a.pstride, a.counter + e, a.wts, tot2) && threadIdx.x == 0) {
-    scal[0] = tot2[0] / (2.0 * nlon);           // mean_ps_p   (Area_Weighted_Global_Mean)
-    scal[1] = tot2[1] / (2.0 * nlon) / a.grav;  // mean_energy_p (Mass_Weighted_Global_Integral)
+    scal[0] = tot2[0] * a.inv_2n;           // mean_ps_p   (Area_Weighted_Global_Mean)
+    scal[1] = tot2[1] * a.inv_2n / a.grav;  // mean_energy_p (Mass_Weighted_Global_Integral)
   }
 }
 
@@ -642,6 +645,7 @@ struct CorrArgs {
   size_t pstride;
   int nd, nlat, nlon, do_mass, do_energy;
   double cp, grav;
+  double inv_2n;  // 1 / (2 nlon), exact (nlon is a power of two)
 };
 
 template <typename T>
@@ -704,11 +708,11 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   double* scal = a.scalars + 4 * e;
   if (grid_reduce_last<3>(vals, a.partials + e * a.pstride, a.counter + e, a.wts, tot3)) {
     if (threadIdx.x == 0) {
-      double two_n = 2.0 * a.nlon;
+      const double inv_2n = a.inv_2n;
       double mean_ps_p = scal[0], mean_energy_p = scal[1];
       double factor = 1.0, corr = 0.0;
       if (a.do_mass) {
-        double mean_ps_n = tot3[0] / two_n;
+        double mean_ps_n = tot3[0] * inv_2n;
         factor = mean_ps_p / mean_ps_n;
         V2<T> l = a.lnps_n[e];  // spe_lnps_n[1,1,1] += log(factor)  (P_00 = 1)
         l.x = (T)((double)l.x + log(factor));
@@ -716,7 +720,7 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
       }
       if (a.do_energy) {
         // Δp_k = Δa_k + Δb_k (factor ps_n): the mass correction enters linearly
-        double mean_energy_n = (tot3[1] + factor * tot3[2]) / two_n / a.grav;
+        double mean_energy_n = (tot3[1] + factor * tot3[2]) * inv_2n / a.grav;
         corr = a.grav * (mean_energy_p - mean_energy_n) / (a.cp * mean_ps_p);
       }
       scal[2] = factor;
@@ -1457,6 +1461,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   a.rdgas = md->P.rdgas;
   a.cp = md->cp_air;
   a.grav = md->P.grav;
+  a.inv_2n = 0.5 / m->nlon;
   a.pstride = partial_stride(m);
   hs_col_consts<T>(a);
   JG_TRY(launch_hs_column<T>(a, m, E, md->hs_lanes, md->d_vc, st));
@@ -1567,6 +1572,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ca.do_energy = md->P.do_energy_correction;
   ca.cp = md->cp_air;
   ca.grav = md->P.grav;
+  ca.inv_2n = 0.5 / m->nlon;
   // the fixers (this branch) and the next step's gradients of the new level (second branch)
   const bool serial = g_marker != nullptr;  // per-kernel timing: one stream, launches in order
   cudaStream_t br = serial ? st : md->side;
