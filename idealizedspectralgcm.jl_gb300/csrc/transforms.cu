@@ -689,7 +689,10 @@ static inline size_t row_fft_smem(const jgcm_mesh* m) { return (size_t)RF_WARPS 
 // Fourier -> spectral: Gaussian quadrature per m.  grid (ceil(Cout/CT), N+1), 256 threads.
 // Shared memory holds, for 4 input slots, the hemisphere-symmetric and -antisymmetric
 // combinations g(mu_j) +/- g(-mu_j) of the tile's columns.
-template <typename T>
+// QL lanes per output (4: a quad splits the latitude sum and combines it with two shuffles, for
+// launches too small to fill the device; 1: a lane sums its output alone, half the instructions per
+// output, for launches with many outputs).
+template <typename T, int QL>
 __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb, const V2<T>* __restrict__ F,
                                                       int ns, int nlat, int Cin, int CT, int stage) {
   pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
@@ -742,11 +745,17 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
     A[(slot * nh + jh) * CT + cl] = a;
   }
   __syncthreads();
-  // each output is summed by a quad of threads (latitudes jh = q, q+4, ...), then combined with two
-  // masked shuffles; quads never straddle loop iterations (blockDim is a multiple of 4)
-  const unsigned qmask = 0xFu << (threadIdx.x & 28);
-  for (int i = threadIdx.x; i < K * CT * 4; i += blockDim.x) {
-    const int q = i & 3, o = i >> 2;
+  // each output is summed by QL threads (latitudes jh = q, q+QL, ...), then combined with masked
+  // shuffles; the QL lanes never straddle loop iterations (blockDim is a multiple of 4)
+  const unsigned qmask = QL == 4 ? 0xFu << (threadIdx.x & 28) : 0u;
+  auto qsum = [&](T& x) {
+    if (QL == 4) {
+      x += __shfl_xor_sync(qmask, x, 1);
+      x += __shfl_xor_sync(qmask, x, 2);
+    }
+  };
+  for (int i = threadIdx.x; i < K * CT * QL; i += blockDim.x) {
+    const int q = i & (QL - 1), o = i / QL;
     int r = o / CT, cl = o - r * CT, n = m + r, c = cbase + cl;
     if (c >= C) continue;  // whole quad
     int k;
@@ -760,16 +769,14 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
       const V* src = (even ? S : A) + slot * nh * CT + cl;
       T sr = 0, si = 0;
 #pragma unroll 4
-      for (int jh = q; jh < nh; jh += 4) {
+      for (int jh = q; jh < nh; jh += QL) {
         T w = pw[jh];
         V x = src[jh * CT];
         sr += x.x * w;
         si += x.y * w;
       }
-      sr += __shfl_xor_sync(qmask, sr, 1);
-      si += __shfl_xor_sync(qmask, si, 1);
-      sr += __shfl_xor_sync(qmask, sr, 2);
-      si += __shfl_xor_sync(qmask, si, 2);
+      qsum(sr);
+      qsum(si);
       V o;
       o.x = (n == ns) ? (T)0 : sr * (T)0.5;
       o.y = (n == ns) ? (T)0 : si * (T)0.5;
@@ -781,7 +788,7 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
       const V* sb = (even ? A : S) + slotB * nh * CT + cl;
       T ar = 0, ai = 0, br = 0, bi = 0;
 #pragma unroll 4
-      for (int jh = q; jh < nh; jh += 4) {
+      for (int jh = q; jh < nh; jh += QL) {
         T wa = ca[jh], wb = cb[jh];
         V xa = sa[jh * CT], xb = sb[jh * CT];
         ar += (-xa.y) * wa;
@@ -790,10 +797,8 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
         bi += xb.y * wb;
       }
       T xr = ar + sign * br, xi = ai + sign * bi;
-      xr += __shfl_xor_sync(qmask, xr, 1);
-      xi += __shfl_xor_sync(qmask, xi, 1);
-      xr += __shfl_xor_sync(qmask, xr, 2);
-      xi += __shfl_xor_sync(qmask, xi, 2);
+      qsum(xr);
+      qsum(xi);
       V o;
       o.x = (n == ns) ? (T)0 : xr;
       o.y = (n == ns) ? (T)0 : xi;
@@ -805,16 +810,14 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
       const T* p = tb.P + (mrow + n) * nh;
       T sr = 0, si = 0;
 #pragma unroll 4
-      for (int jh = q; jh < nh; jh += 4) {
+      for (int jh = q; jh < nh; jh += QL) {
         T w = p[jh];
         V x = src[jh * CT];
         sr += x.x * w;
         si += x.y * w;
       }
-      sr += __shfl_xor_sync(qmask, sr, 1);
-      si += __shfl_xor_sync(qmask, si, 1);
-      sr += __shfl_xor_sync(qmask, sr, 2);
-      si += __shfl_xor_sync(qmask, si, 2);
+      qsum(sr);
+      qsum(si);
       const T sc = (m == 0 ? (T)1 : (T)2) * pick<T>(g.scale, g.scalef);  // scale = nlon (the FFT returned fft / nlon)
       V o;
       o.x = sr * sc;
@@ -862,7 +865,8 @@ static int configure_smem() {
   JG_CUDA(cudaFuncSetAttribute(k_s2g_legendre<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   JG_CUDA(cudaFuncSetAttribute(k_ifft<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   JG_CUDA(cudaFuncSetAttribute(k_fft<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  JG_CUDA(cudaFuncSetAttribute(k_g2s_legendre<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  JG_CUDA(cudaFuncSetAttribute(k_g2s_legendre<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  JG_CUDA(cudaFuncSetAttribute(k_g2s_legendre<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   if (idx == 0) {
     JG_CUDA(cudaFuncSetAttribute(k_fft_rows<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     JG_CUDA(cudaFuncSetAttribute(k_fft_rows<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
@@ -1070,7 +1074,12 @@ int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp0, cudaStream_t
   const int stage = sm + tab <= kSmemBudget;
   if (stage) sm += tab;
   dim3 g((gp.C + ct - 1) / ct, m->N + 1);
-  JG_CUDA(launch_pdl(k_g2s_legendre<T>, g, 256, sm, st, gp, tb, (const V*)fbuf, m->ns, m->nlat, fp.C, ct, stage));
+  // one lane per output once the launch has outputs for every thread the device holds
+  const size_t outputs = (size_t)gp.C * (m->N + 1) * (m->N + 2) / 2;
+  if (outputs >= (size_t)152 * 2048)
+    JG_CUDA(launch_pdl(k_g2s_legendre<T, 1>, g, 256, sm, st, gp, tb, (const V*)fbuf, m->ns, m->nlat, fp.C, ct, stage));
+  else
+    JG_CUDA(launch_pdl(k_g2s_legendre<T, 4>, g, 256, sm, st, gp, tb, (const V*)fbuf, m->ns, m->nlat, fp.C, ct, stage));
   mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;

@@ -61,11 +61,12 @@ def test_ensemble_matches_members(jg, name, prec, members, steps):
     print(name, prec, members, "worst", worst)
 
 
-@pytest.mark.parametrize("name,members", [("hs_t21l20", 16), ("hs_t42l20", 8)])
+@pytest.mark.parametrize("name,members", [("hs_t21l20", 24), ("hs_t42l20", 8)])
 def test_large_fp32_ensemble_matches_oracle(jg, orc, name, members):
-    """Member-batched FP32 steps at scale (T21: enough members that every zonal FFT runs one row
-    per thread, k_fft_rows / k_ifft_rows): the first and last members, stepped from a developed
-    flow, equal the oracle's steps (the FP32 step tolerance of the single-member parity tests)."""
+    """Member-batched FP32 steps at scale: enough members that the analysis runs one lane per
+    output (k_g2s_legendre<T, 1>) and, at T21, every zonal FFT one row per thread (k_fft_rows /
+    k_ifft_rows).  The first and last members, stepped from a developed flow, equal the oracle's
+    steps (the FP32 step tolerance of the single-member parity tests)."""
     params = configs.PARAMS[name]
     gm, om = configs.make_mesh(jg, name, precision="fp32"), configs.make_mesh(orc, name)
     ens = jg.Model(gm, params, members=members)
