@@ -518,7 +518,9 @@ __host__ __device__ constexpr int brev_c(int x, int bits) {
   return r;
 }
 
-template <int NLON>
+// PLAIN: every group of the plan reads its field as it is (PRO_NONE): the prologue switch, inlined
+// for each of a warp's 32 rows, leaves the instruction stream
+template <int NLON, bool PLAIN>
 __global__ void __launch_bounds__(32 * RF_WARPS) k_fft_rows(FFTPlan plan, Tables<float> tb, RowTwiddles<NLON> tw,
                                                             float2* __restrict__ F, int N, int nlat) {
   pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
@@ -544,7 +546,9 @@ __global__ void __launch_bounds__(32 * RF_WARPS) k_fft_rows(FFTPlan plan, Tables
         int k;
         const GridInGroup& g = group_of(plan.g, plan.ng, c0 + rb + rr, &k);
 #pragma unroll
-        for (int q = 0; q < NLON / 32; q++) v[rr][q] = fft_load<float>(plan, g, k, j, lane + 32 * q, nlat, NLON, cj);
+        for (int q = 0; q < NLON / 32; q++)
+          v[rr][q] = PLAIN ? ((const float*)g.src)[((size_t)k * nlat + j) * NLON + lane + 32 * q]
+                           : fft_load<float>(plan, g, k, j, lane + 32 * q, nlat, NLON, cj);
       }
     }
 #pragma unroll
@@ -868,8 +872,10 @@ static int configure_smem() {
   JG_CUDA(cudaFuncSetAttribute(k_g2s_legendre<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   JG_CUDA(cudaFuncSetAttribute(k_g2s_legendre<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   if (idx == 0) {
-    JG_CUDA(cudaFuncSetAttribute(k_fft_rows<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    JG_CUDA(cudaFuncSetAttribute(k_fft_rows<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    JG_CUDA(cudaFuncSetAttribute(k_fft_rows<64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    JG_CUDA(cudaFuncSetAttribute(k_fft_rows<64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    JG_CUDA(cudaFuncSetAttribute(k_fft_rows<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    JG_CUDA(cudaFuncSetAttribute(k_fft_rows<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     JG_CUDA(cudaFuncSetAttribute(k_ifft_rows<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
     JG_CUDA(cudaFuncSetAttribute(k_ifft_rows<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   }
@@ -1023,10 +1029,17 @@ int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp0, cudaStream_t st, void* fbu
     dim3 gr((fp.C + 32 * RF_WARPS - 1) / (32 * RF_WARPS), m->nlat);
     const Tables<float> tf = tables<float>(m);
     float2* Ff = (float2*)fbuf;
-    if (m->nlon == 64)
-      JG_CUDA(launch_pdl(k_fft_rows<64>, gr, 32 * RF_WARPS, row_fft_smem(m), st, fp, tf, row_twiddles<64>(m), Ff, m->N, m->nlat));
+    bool plain = true;
+    for (int i = 0; i < fp.ng; i++) plain = plain && fp.g[i].pro == PRO_NONE;
+    const size_t sm = row_fft_smem(m);
+    if (m->nlon == 64 && plain)
+      JG_CUDA(launch_pdl(k_fft_rows<64, true>, gr, 32 * RF_WARPS, sm, st, fp, tf, row_twiddles<64>(m), Ff, m->N, m->nlat));
+    else if (m->nlon == 64)
+      JG_CUDA(launch_pdl(k_fft_rows<64, false>, gr, 32 * RF_WARPS, sm, st, fp, tf, row_twiddles<64>(m), Ff, m->N, m->nlat));
+    else if (plain)
+      JG_CUDA(launch_pdl(k_fft_rows<128, true>, gr, 32 * RF_WARPS, sm, st, fp, tf, row_twiddles<128>(m), Ff, m->N, m->nlat));
     else
-      JG_CUDA(launch_pdl(k_fft_rows<128>, gr, 32 * RF_WARPS, row_fft_smem(m), st, fp, tf, row_twiddles<128>(m), Ff, m->N, m->nlat));
+      JG_CUDA(launch_pdl(k_fft_rows<128, false>, gr, 32 * RF_WARPS, sm, st, fp, tf, row_twiddles<128>(m), Ff, m->N, m->nlat));
     mark(st);
     JG_CUDA(cudaGetLastError());
     return JGCM_OK;
