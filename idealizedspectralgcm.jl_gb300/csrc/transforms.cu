@@ -445,7 +445,7 @@ __global__ void __launch_bounds__(256) k_ifft_w(IFFTPlan plan, Tables<T> tb, con
   }
 }
 
-template <typename T, int V>
+template <typename T, int V, bool PLAIN>
 __global__ void __launch_bounds__(256) k_fft_w(FFTPlan plan, Tables<T> tb, V2<T>* __restrict__ F, int N, int nlat,
                                                int nlon) {
   pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
@@ -464,8 +464,14 @@ __global__ void __launch_bounds__(256) k_fft_w(FFTPlan plan, Tables<T> tb, V2<T>
 #pragma unroll
     for (int r = 0; r < V; r++) {  // z[i] = x[2i] + i x[2i+1], natural order
       const int i = lane + 32 * r;
-      re[r] = fft_load<T>(plan, g, k, j, 2 * i, nlat, nlon, cj);
-      im[r] = fft_load<T>(plan, g, k, j, 2 * i + 1, nlat, nlon, cj);
+      if (PLAIN) {  // every group reads its field as it is (k_fft_rows' PLAIN)
+        const T* src = (const T*)g.src + ((size_t)k * nlat + j) * nlon;
+        re[r] = src[2 * i];
+        im[r] = src[2 * i + 1];
+      } else {
+        re[r] = fft_load<T>(plan, g, k, j, 2 * i, nlat, nlon, cj);
+        im[r] = fft_load<T>(plan, g, k, j, 2 * i + 1, nlat, nlon, cj);
+      }
     }
     warp_fft_dif<T, V>(re, im, tb.tw, lane);
 #pragma unroll
@@ -659,7 +665,7 @@ __global__ void __launch_bounds__(32 * RF_WARPS, NLON == 64 ? 6 : 1) k_ifft_rows
     }
   }
   __syncwarp();
-#pragma unroll 4
+#pragma unroll 1  // stores need no unrolling to overlap; one copy of the epilogue switch in the code
   for (int r = 0; r < 32; r++) {  // row r = column c0 + r, lanes along longitude (coalesced)
     if (r < nr) {
       int k;
@@ -1048,13 +1054,19 @@ int launch_fft_only(jgcm_mesh* m, const FFTPlan& fp0, cudaStream_t st, void* fbu
   if (std::is_same<T, float>::value && m->nlon >= 128 && m->nlon <= 1024 && m->tune[3] == 0) {
     const size_t smw = ((size_t)FW_COLS * (m->nlon / 2) + (size_t)(m->N + 1) * FW_COLS) * sizeof(V);
     dim3 gw((fp.C + FW_COLS - 1) / FW_COLS, m->nlat);
+    bool plain = true;
+    for (int i = 0; i < fp.ng; i++) plain = plain && fp.g[i].pro == PRO_NONE;
+#define JG_FFT_W(VV)                                                                                               \
+  (plain ? launch_pdl(k_fft_w<T, VV, true>, gw, 256, smw, st, fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon)            \
+         : launch_pdl(k_fft_w<T, VV, false>, gw, 256, smw, st, fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon))
     switch (m->nlon) {
-      case 64: JG_CUDA(launch_pdl(k_fft_w<T, 1>, gw, 256, smw, st, fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon)); break;
-      case 128: JG_CUDA(launch_pdl(k_fft_w<T, 2>, gw, 256, smw, st, fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon)); break;
-      case 256: JG_CUDA(launch_pdl(k_fft_w<T, 4>, gw, 256, smw, st, fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon)); break;
-      case 512: JG_CUDA(launch_pdl(k_fft_w<T, 8>, gw, 256, smw, st, fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon)); break;
-      default: JG_CUDA(launch_pdl(k_fft_w<T, 16>, gw, 256, smw, st, fp, tb, (V*)fbuf, m->N, m->nlat, m->nlon)); break;
+      case 64: JG_CUDA(JG_FFT_W(1)); break;
+      case 128: JG_CUDA(JG_FFT_W(2)); break;
+      case 256: JG_CUDA(JG_FFT_W(4)); break;
+      case 512: JG_CUDA(JG_FFT_W(8)); break;
+      default: JG_CUDA(JG_FFT_W(16)); break;
     }
+#undef JG_FFT_W
     mark(st);
     JG_CUDA(cudaGetLastError());
     return JGCM_OK;
