@@ -687,12 +687,13 @@ RowTwiddles<NLON> row_twiddles(const jgcm_mesh* m) {
   return t;
 }
 
-// FFT tile knob: 0 = by size (nlon 64 rows one per thread from kRowsMin rows on; at nlon 128 the
-// thread holds 64 complex points and its 164-254 registers cost more occupancy than the warp FFT's
-// shuffles, measured), -1 = rows per thread always (nlon 64 and 128)
-static inline bool use_row_fft(const jgcm_mesh* m, int C) {
+// FFT tile knob: 0 = by size, from kRowsMin rows on: nlon 64 both ways, nlon 128 the inverse only
+// (its thread holds 64 complex points in 158 registers and still beats the warp FFT, 135 -> 107 us
+// at T42 x 32 members; the forward one at 165 registers does not, 80 -> 190 us, measured);
+// -1 = rows per thread always (nlon 64 and 128)
+static inline bool use_row_fft(const jgcm_mesh* m, int C, bool inverse = false) {
   if (m->tune[3] == -1) return m->nlon == 64 || m->nlon == 128;
-  return m->tune[3] == 0 && m->nlon == 64 && (size_t)C * m->nlat >= kRowsMin;
+  return m->tune[3] == 0 && (m->nlon == 64 || (inverse && m->nlon == 128)) && (size_t)C * m->nlat >= kRowsMin;
 }
 static inline size_t row_fft_smem(const jgcm_mesh* m) { return (size_t)RF_WARPS * 32 * (m->nlon + 1) * sizeof(float); }
 
@@ -963,7 +964,7 @@ static int launch_ifft_stage(jgcm_mesh* m, const IFFTPlan& ip0, cudaStream_t st,
   const IFFTPlan ip = with_f32(ip0);
   Tables<T> tb = tables<T>(m);
   const int fc = fft_ct(m);
-  if (std::is_same<T, float>::value && use_row_fft(m, ip.C)) {  // many rows: a row per thread
+  if (std::is_same<T, float>::value && use_row_fft(m, ip.C, true)) {  // many rows: a row per thread
     dim3 gr((ip.C + 32 * RF_WARPS - 1) / (32 * RF_WARPS), m->nlat);
     const Tables<float> tf = tables<float>(m);
     const float2* Ff = (const float2*)fbuf;

@@ -213,7 +213,7 @@ int jgcm_model_read_diagnostics(jgcm_model* model, const char* name, double* out
 /* Tiles (no counterpart in the reference).  knobs[0]: lanes per column of the Held-Suarez column
  * kernel (1, 2, 4, 8; this model); knobs[1..3]: S2G, G2S and FFT columns per block of the SIMT
  * transform kernels (the mesh: shared by its models).  0 = default; knobs[3] = -1 puts FP32 rows of
- * nlon 64 or 128 one per thread whatever their number (by default: nlon 64 from 19456 rows on).  knobs[4] (read and written when
+ * nlon 64 or 128 one per thread whatever their number (by default from 19456 rows on: nlon 64, and the inverse at nlon 128).  knobs[4] (read and written when
  * n >= 5): the Legendre engine of a tensor-core precision mode (0 tcgen05, 1 the FP32 SIMT
  * kernels; the mesh).  The autotuner times candidates on a scratch copy of the model (coordinate
  * search, nsteps captured steps each), applies the fastest and returns it (knobs[5]) with its time
