@@ -526,7 +526,10 @@ __device__ __forceinline__ void lf(int init, int Dt, R rob, R d, R f, R& dq, R q
 }
 
 // R is the precision of the vertical algebra (FP64 on the FP64 path; selectable on the FP32 path).
-template <typename T, typename R>
+// DENSE: the FP64 wave-matrix products of the block's modes are spread over all its threads, one
+// (mode, component, row) output each, instead of one mode per warp, whose 32 - nd idle lanes the
+// FP64 pipe executes all the same (for launches with many modes: member ensembles).
+template <typename T, typename R, bool DENSE = false>
 __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCoef* __restrict__ vcp) {
   const VertCoef& vc = *vcp;
   __shared__ VertR<R> vr;
@@ -535,9 +538,11 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCo
   pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using C = CX<R>;
   const int lane = threadIdx.x & 31;
-  const int pid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);  // one (m, n) mode per warp
-  if (pid >= a.npairs) return;  // whole warp exits together
-  const int2 mn = a.pairs[pid];
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int pid = blockIdx.x * nw + w;  // one (m, n) mode per warp
+  const bool live = pid < a.npairs;     // warp-uniform
+  if (!DENSE && !live) return;          // whole warp exits together (no block barrier follows)
+  const int2 mn = live ? a.pairs[pid] : make_int2(0, 0);  // DENSE: a spare warp only meets the barriers
   const int m = mn.x, n = mn.y, nd = a.nd, e = blockIdx.y;
   const bool act = lane < nd;
   const int k = act ? lane : 0;
@@ -574,7 +579,37 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCo
   ddiv.x = ddiv.x - eig * (gx + hk * l2.x);
   ddiv.y = ddiv.y - eig * (gy + hk * l2.y);
   // wave-matrix solve in FP64, n <= N only (Implicit_Correction! :486-497)
-  if (n <= a.N) {
+  if (DENSE) {
+    __shared__ double s_b[8][2][JGCM_MAX_ND], s_o[8][2][JGCM_MAX_ND];
+    if (act) {
+      s_b[w][0][k] = (double)ddiv.x;
+      s_b[w][1][k] = (double)ddiv.y;
+    }
+    __syncthreads();
+    // outputs o = (mode, component, row); the block's first output rotates with the block so that
+    // the remainder past a multiple of the block size falls on every warp in turn
+    const int nout = nw * 2 * nd, o0 = (int)((blockIdx.x * 32u) % (unsigned)blockDim.x);
+    for (int t = threadIdx.x; t < nout; t += blockDim.x) {
+      const int o = (t + o0) % nout;
+      const int wq = o / (2 * nd), rem = o - wq * 2 * nd, cq = rem / nd, rw = rem - cq * nd;
+      const int pq = blockIdx.x * nw + wq;
+      if (pq < a.npairs) {
+        const int nq = a.pairs[pq].y;
+        if (nq <= a.N) {
+          const double* W = a.W + (size_t)nq * nd * nd;
+          double acc = 0;  // the same products in the same order as the per-warp form below
+#pragma unroll 4
+          for (int c = 0; c < nd; c++) acc = acc + W[(size_t)c * nd + rw] * s_b[wq][cq][c];
+          s_o[wq][cq][rw] = acc;
+        }
+      }
+    }
+    __syncthreads();
+    if (n <= a.N) {
+      ddiv.x = act ? (R)s_o[w][0][k] : (R)0;
+      ddiv.y = act ? (R)s_o[w][1][k] : (R)0;
+    }
+  } else if (n <= a.N) {
     const double* W = a.W + (size_t)n * nd * nd;
     const double bxl = (double)ddiv.x, byl = (double)ddiv.y;
     double sx = 0, sy = 0;
@@ -604,7 +639,7 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCo
   // damping + leapfrog
   const R d = (R)a.damping[row], f = (R)a.dfac[row], rob = (R)a.rob_t;
   const int ini = a.init_step, Dt = a.dt;
-  if (act) {
+  if (live && act) {
     C vn, dn, tn;
     lf<R>(ini, Dt, rob, d, f, dvor.x, vorp.x, vorc.x, vn.x);
     lf<R>(ini, Dt, rob, d, f, dvor.y, vorp.y, vorc.y, vn.y);
@@ -620,7 +655,7 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCo
     o.x = (T)tn.x; o.y = (T)tn.y; a.t_n[s] = o;
     o.x = (T)tc.x; o.y = (T)tc.y; a.t_c[s] = o;
   }
-  if (lane == 0) {  // lnps: leapfrog without damping (d = 0, f = 1)
+  if (live && lane == 0) {  // lnps: leapfrog without damping (d = 0, f = 1)
     C ln;
     lf<R>(ini, Dt, rob, (R)0, (R)1, dl.x, lp.x, lc.x, ln.x);
     lf<R>(ini, Dt, rob, (R)0, (R)1, dl.y, lp.y, lc.y, ln.y);
@@ -1520,8 +1555,12 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   impl_consts<T>(ia, tables<T>(md->mesh).eig);
   // vertical algebra in the state precision (FP64 algebra on the FP32 path measured no more
   // accurate: its error is set by FP32 storage); the wave-matrix solve is FP64 in both
-  // 4 modes per block: (N+1)(N+2)/2 + N+1 modes at T42 make 248 blocks, every SM's FP64 units busy
-  JG_CUDA(launch_pdl(k_hs_implicit<T, T>, dim3((md->npairs + 3) / 4, E), 128, 0, st, ia, md->d_vc));
+  // 4 modes per block: (N+1)(N+2)/2 + N+1 modes at T42 make 248 blocks, every SM's FP64 units busy;
+  // member ensembles (from 4 members) spread the FP64 products densely over each block
+  if (E >= 4)
+    JG_CUDA(launch_pdl(k_hs_implicit<T, T, true>, dim3((md->npairs + 3) / 4, E), 128, 0, st, ia, md->d_vc));
+  else
+    JG_CUDA(launch_pdl(k_hs_implicit<T, T>, dim3((md->npairs + 3) / 4, E), 128, 0, st, ia, md->d_vc));
   mark(st);
   JG_CUDA(cudaGetLastError());
   // 5. back to the grid: vor, div, u, v, T, lnps (+ ps = exp(lnps))
