@@ -240,6 +240,7 @@ struct jgcm_mesh {
   unsigned int* d_counter;
   int refs;           // 1 for the caller's handle + 1 per live model built on the mesh
   int device;         // CUDA device the mesh lives on
+  int sm_count;       // its SMs (152 on GB300): the size thresholds of the kernel choices
   std::string name;
   std::vector<float> twf_host;  // the FP32 twiddle table (cos, sin of 2π t / nlon, t < nlon/2) on the host
 };

@@ -314,6 +314,9 @@ extern "C" int jgcm_mesh_create(int num_fourier, int num_spherical, int nlat, in
     return JGCM_OK;
   };
   MCHK(cuda(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking), "cudaStreamCreate"));
+  int dev = 0;
+  MCHK(cuda(cudaGetDevice(&dev), "cudaGetDevice"));
+  MCHK(cuda(cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute"));
   size_t T3 = (size_t)(m->N + 1) * (m->ns + 1) * nlat;
   MCHK(cuda(cudaMalloc(&m->d_sinth, nlat * 8), "alloc"));
   MCHK(cuda(cudaMalloc(&m->d_wts, nlat * 8), "alloc"));

@@ -1624,7 +1624,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   JG_CUDA(cudaGetLastError());
   const size_t G1 = grid_elems(m, 1);
   int nb = (int)(((size_t)nd * G1 + 255) / 256);
-  if (nb * E > 8 * 152) nb = (8 * 152 + E - 1) / E;
+  if (nb * E > 8 * m->sm_count) nb = (8 * m->sm_count + E - 1) / E;
   JG_CUDA(launch_pdl(k_hs_corr_apply<T>, dim3(nb, E), 256, 0, st, (T*)md->grid_t[n], (T*)md->grid_ps[n],
                      (const T*)(md->d_scalars + 4 * E), (size_t)nd * G1, G1));
   mark(st);
@@ -2248,7 +2248,7 @@ extern "C" int jgcm_hs_forcing(jgcm_model* md, int Dt, const double* grid_u, con
   a.kappa = md->P.kappa;
   a.cp = md->cp_air;
   if (st == JGCM_OK) {
-    int nb = (int)std::min<size_t>((n + 255) / 256, 4 * 152);
+    int nb = (int)std::min<size_t>((n + 255) / 256, 4 * (size_t)m->sm_count);
     if (is_fp64(m)) k_hs_forcing<double><<<nb, 256, 0, m->stream>>>(a);
     else k_hs_forcing<float><<<nb, 256, 0, m->stream>>>(a);
     mark(m->stream);

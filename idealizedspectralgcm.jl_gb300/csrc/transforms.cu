@@ -516,7 +516,8 @@ struct RowTwiddles {
   float c[NLON / 2], s[NLON / 2];  // cos, sin of 2π t / nlon
 };
 constexpr int RF_WARPS = 4;               // warps per block, 32 rows each
-constexpr size_t kRowsMin = 152 * 4 * 32;  // rows from which the row-per-thread kernels are used
+// rows from which the row-per-thread kernels are used: 128 per SM (4 warps), 19456 on GB300
+static inline size_t rows_min(const jgcm_mesh* m) { return (size_t)m->sm_count * 4 * 32; }
 
 __host__ __device__ constexpr int brev_c(int x, int bits) {
   int r = 0;
@@ -687,13 +688,13 @@ RowTwiddles<NLON> row_twiddles(const jgcm_mesh* m) {
   return t;
 }
 
-// FFT tile knob: 0 = by size, from kRowsMin rows on: nlon 64 both ways, nlon 128 the inverse only
+// FFT tile knob: 0 = by size, from rows_min rows on: nlon 64 both ways, nlon 128 the inverse only
 // (its thread holds 64 complex points in 158 registers and still beats the warp FFT, 135 -> 107 us
 // at T42 x 32 members; the forward one at 165 registers does not, 80 -> 190 us, measured);
 // -1 = rows per thread always (nlon 64 and 128)
 static inline bool use_row_fft(const jgcm_mesh* m, int C, bool inverse = false) {
   if (m->tune[3] == -1) return m->nlon == 64 || m->nlon == 128;
-  return m->tune[3] == 0 && (m->nlon == 64 || (inverse && m->nlon == 128)) && (size_t)C * m->nlat >= kRowsMin;
+  return m->tune[3] == 0 && (m->nlon == 64 || (inverse && m->nlon == 128)) && (size_t)C * m->nlat >= rows_min(m);
 }
 static inline size_t row_fft_smem(const jgcm_mesh* m) { return (size_t)RF_WARPS * 32 * (m->nlon + 1) * sizeof(float); }
 
@@ -1102,7 +1103,7 @@ int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp0, cudaStream_t
   dim3 g((gp.C + ct - 1) / ct, m->N + 1);
   // one lane per output once the launch has outputs for every thread the device holds
   const size_t outputs = (size_t)gp.C * (m->N + 1) * (m->N + 2) / 2;
-  if (outputs >= (size_t)152 * 2048)
+  if (outputs >= (size_t)m->sm_count * 2048)
     JG_CUDA(launch_pdl(k_g2s_legendre<T, 1>, g, 256, sm, st, gp, tb, (const V*)fbuf, m->ns, m->nlat, fp.C, ct, stage));
   else
     JG_CUDA(launch_pdl(k_g2s_legendre<T, 4>, g, 256, sm, st, gp, tb, (const V*)fbuf, m->ns, m->nlat, fp.C, ct, stage));
