@@ -701,6 +701,17 @@ static inline size_t row_fft_smem(const jgcm_mesh* m) { return (size_t)RF_WARPS 
 // Fourier -> spectral: Gaussian quadrature per m.  grid (ceil(Cout/CT), N+1), 256 threads.
 // Shared memory holds, for 4 input slots, the hemisphere-symmetric and -antisymmetric
 // combinations g(mu_j) +/- g(-mu_j) of the tile's columns.
+// four consecutive table weights in one 16-byte load (the address is 16-byte aligned: nh is a
+// multiple of 4 and the tables start aligned)
+__device__ __forceinline__ void ld4(const float* p, float (&w)[4]) {
+  const float4 v = *reinterpret_cast<const float4*>(p);
+  w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+}
+__device__ __forceinline__ void ld4(const double* p, double (&w)[4]) {
+  const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+  w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
+}
+
 // QL lanes per output (4: a quad splits the latitude sum and combines it with two shuffles, for
 // launches too small to fill the device; 1: a lane sums its output alone, half the instructions per
 // output, for launches with many outputs).
@@ -780,12 +791,25 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
     auto plain = [&](int slot) -> V {
       const V* src = (even ? S : A) + slot * nh * CT + cl;
       T sr = 0, si = 0;
+      if (QL == 1) {  // a lane walks every latitude: weights four at a time, same order of sums
+        for (int jh = 0; jh < nh; jh += 4) {
+          T w[4];
+          ld4(pw + jh, w);
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const V x = src[(jh + u) * CT];
+            sr += x.x * w[u];
+            si += x.y * w[u];
+          }
+        }
+      } else {
 #pragma unroll 4
-      for (int jh = q; jh < nh; jh += QL) {
-        T w = pw[jh];
-        V x = src[jh * CT];
-        sr += x.x * w;
-        si += x.y * w;
+        for (int jh = q; jh < nh; jh += QL) {
+          T w = pw[jh];
+          V x = src[jh * CT];
+          sr += x.x * w;
+          si += x.y * w;
+        }
       }
       qsum(sr);
       qsum(si);
@@ -799,14 +823,30 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
       const V* sa = (even ? S : A) + slotA * nh * CT + cl;
       const V* sb = (even ? A : S) + slotB * nh * CT + cl;
       T ar = 0, ai = 0, br = 0, bi = 0;
+      if (QL == 1) {  // weights four at a time, same order of sums
+        for (int jh = 0; jh < nh; jh += 4) {
+          T wa[4], wb[4];
+          ld4(ca + jh, wa);
+          ld4(cb + jh, wb);
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const V xa = sa[(jh + u) * CT], xb = sb[(jh + u) * CT];
+            ar += (-xa.y) * wa[u];
+            ai += xa.x * wa[u];
+            br += xb.x * wb[u];
+            bi += xb.y * wb[u];
+          }
+        }
+      } else {
 #pragma unroll 4
-      for (int jh = q; jh < nh; jh += QL) {
-        T wa = ca[jh], wb = cb[jh];
-        V xa = sa[jh * CT], xb = sb[jh * CT];
-        ar += (-xa.y) * wa;
-        ai += xa.x * wa;
-        br += xb.x * wb;
-        bi += xb.y * wb;
+        for (int jh = q; jh < nh; jh += QL) {
+          T wa = ca[jh], wb = cb[jh];
+          V xa = sa[jh * CT], xb = sb[jh * CT];
+          ar += (-xa.y) * wa;
+          ai += xa.x * wa;
+          br += xb.x * wb;
+          bi += xb.y * wb;
+        }
       }
       T xr = ar + sign * br, xi = ai + sign * bi;
       qsum(xr);
@@ -1103,7 +1143,7 @@ int launch_g2s(jgcm_mesh* m, const FFTPlan& fp, const G2SPlan& gp0, cudaStream_t
   dim3 g((gp.C + ct - 1) / ct, m->N + 1);
   // one lane per output once the launch has outputs for every thread the device holds
   const size_t outputs = (size_t)gp.C * (m->N + 1) * (m->N + 2) / 2;
-  if (outputs >= (size_t)m->sm_count * 2048)
+  if (outputs >= (size_t)m->sm_count * 2048 && nh % 4 == 0)
     JG_CUDA(launch_pdl(k_g2s_legendre<T, 1>, g, 256, sm, st, gp, tb, (const V*)fbuf, m->ns, m->nlat, fp.C, ct, stage));
   else
     JG_CUDA(launch_pdl(k_g2s_legendre<T, 4>, g, 256, sm, st, gp, tb, (const V*)fbuf, m->ns, m->nlat, fp.C, ct, stage));
