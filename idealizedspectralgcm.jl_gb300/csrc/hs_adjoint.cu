@@ -77,6 +77,8 @@ struct FixArgs {
   const VertCoef* vc;
   int nd, nlat, nlon, do_mass, do_energy;
   double cp, grav;
+  double inv_2n, ig;  // 1 / (2 nlon) (exact: nlon is a power of two), 1 / grav
+  float cpf, igf;     // cp and 1 / grav rounded to FP32 on the host
 };
 
 // one thread per grid point: block partials of the sum of the grid temperature cotangent
@@ -108,35 +110,42 @@ __global__ void __launch_bounds__(256) k_fold1(FixArgs a, int nb) {
   }
 }
 
-// energy fixer reversed: en_n = |u_n|^2/2 + cp T_n weighted by dp(ps_n2); a warp per column, a lane
-// per level, arithmetic in the state precision; block partials of ps_n2_bar ps_n in FP64
+// energy fixer reversed: en_n = |u_n|^2/2 + cp T_n weighted by dp(ps_n2); one thread per column
+// (consecutive longitudes: every level read and write is a coalesced row), arithmetic in the state
+// precision with the layer coefficients staged per block; block partials of ps_n2_bar ps_n in FP64
 template <typename T>
 __global__ void __launch_bounds__(256) k_fix2(FixArgs a) {
-  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using R = T;
-  const int G = a.nlat * a.nlon, lane = threadIdx.x & 31;
-  const int c = blockIdx.x * 8 + (threadIdx.x >> 5), k = lane;
-  const bool colv = c < G, act = colv && k < a.nd;
+  __shared__ R s_dak[JGCM_MAX_ND], s_dbk[JGCM_MAX_ND];
+  for (int q = threadIdx.x; q < a.nd; q += blockDim.x) {
+    s_dak[q] = (R)a.vc->dak[q];
+    s_dbk[q] = (R)a.vc->dbk[q];
+  }
+  __syncthreads();
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
+  const int G = a.nlat * a.nlon, c = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool colv = c < G;
   const int j = colv ? c / a.nlon : 0;
   const R factor = (R)a.sc[SC_FACTOR], corr = (R)a.sc[SC_CORR], En_bar = (R)a.sc[SC_EN_BAR];
-  const R Wc = (R)(a.wts[j] / (2.0 * a.nlon)), cp = (R)a.cp, ig = (R)(1.0 / a.grav);
+  const R Wc = (R)(a.wts[j] * a.inv_2n), cp = pick<R>(a.cp, a.cpf), ig = pick<R>(a.ig, a.igf);
   const R ps2 = colv ? (R)((const T*)a.ps_n2)[c] : (R)0;
   R acc = 0;
-  if (act && a.do_energy) {
-    const size_t x = c + (size_t)G * k;
-    const R u = ((const T*)a.u_n)[x], v = ((const T*)a.v_n)[x], t = ((const T*)a.t_n2)[x] - corr;
-    const R dbk = (R)a.vc->dbk[k];
-    const R en = (R)0.5 * (u * u + v * v) + cp * t;
-    const R eb = En_bar * Wc * ((R)a.vc->dak[k] + dbk * ps2) * ig;
-    ((T*)a.bu)[x] = ((T*)a.bu)[x] + eb * u;
-    ((T*)a.bv)[x] = ((T*)a.bv)[x] + eb * v;
-    ((T*)a.bt)[x] = ((T*)a.bt)[x] + cp * eb;
-    acc = en * dbk;
+  if (colv && a.do_energy) {
+#pragma unroll 4
+    for (int k = 0; k < a.nd; k++) {
+      const size_t x = c + (size_t)G * k;
+      const R u = ((const T*)a.u_n)[x], v = ((const T*)a.v_n)[x], t = ((const T*)a.t_n2)[x] - corr;
+      const R dbk = s_dbk[k];
+      const R en = (R)0.5 * (u * u + v * v) + cp * t;
+      const R eb = En_bar * Wc * (s_dak[k] + dbk * ps2) * ig;
+      ((T*)a.bu)[x] = ((T*)a.bu)[x] + eb * u;
+      ((T*)a.bv)[x] = ((T*)a.bv)[x] + eb * v;
+      ((T*)a.bt)[x] = ((T*)a.bt)[x] + cp * eb;
+      acc += en * dbk;
+    }
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
   double s = 0.0;
-  if (colv && lane == 0) {
+  if (colv) {
     R bps = ((T*)a.bps)[c];
     if (a.do_energy) {
       bps += En_bar * Wc * ig * acc;
@@ -181,7 +190,7 @@ __global__ void __launch_bounds__(256) k_fix3(FixArgs a) {
     const double factor = a.sc[SC_FACTOR];
     const double ps_n = (double)((const T*)a.ps_n2)[c] / factor;
     double bps = (double)((const T*)a.bps)[c];
-    if (a.do_mass) bps = bps * factor + a.sc[SC_MN_BAR] * a.wts[j] / (2.0 * a.nlon);
+    if (a.do_mass) bps = bps * factor + a.sc[SC_MN_BAR] * a.wts[j] * a.inv_2n;
     ((T*)a.g_lnps)[c] = (T)(bps * ps_n);
   }
 }
@@ -345,7 +354,7 @@ __global__ void __launch_bounds__(256) k_alpha_adjoint(const V2<T>* __restrict__
     vbb[0] += cb * db.x;  // +CB div_bar
     vbb[1] += cb * db.y;
   }
-  const T sc = tb.cosj[jh] / (T)((m == 0 ? 1.0 : 2.0) * nlon);
+  const T sc = tb.cosj[jh] / ((m == 0 ? (T)1 : (T)2) * (T)nlon);  // exact in T: no FP64 per thread
   const int C = 2 * nd;
   const int jn = nlat - 1 - jh;
   V us, un, vs, vn;
@@ -385,7 +394,21 @@ struct ColAdjArgs {
   // k_t = ka + ktc max(0, sigma - sigma_b) cos^4
   double sigma_b, kvc, ka, ktc, inv_1msb, inv_day, dT_y, dtheta_z, kappa, ln_p0;
   double rdgas, cp, inv_cp, inv_grav;
+  double inv_2n;  // 1 / (2 nlon), exact (nlon is a power of two)
+  // the same constants rounded to T on the host (an FP64 -> FP32 conversion per thread would run on
+  // the FP64 pipe)
+  T sigma_b_t, kvc_t, ka_t, ktc_t, inv_1msb_t, inv_day_t, dT_y_t, dtheta_z_t, kappa_t, ln_p0_t;
+  T rdgas_t, cp_t, inv_cp_t, inv_grav_t;
 };
+
+template <typename T>
+void col_adj_consts(ColAdjArgs<T>& a) {
+  a.sigma_b_t = (T)a.sigma_b; a.kvc_t = (T)a.kvc; a.ka_t = (T)a.ka; a.ktc_t = (T)a.ktc;
+  a.inv_1msb_t = (T)a.inv_1msb; a.inv_day_t = (T)a.inv_day; a.dT_y_t = (T)a.dT_y;
+  a.dtheta_z_t = (T)a.dtheta_z; a.kappa_t = (T)a.kappa; a.ln_p0_t = (T)a.ln_p0;
+  a.rdgas_t = (T)a.rdgas; a.cp_t = (T)a.cp; a.inv_cp_t = (T)a.inv_cp; a.inv_grav_t = (T)a.inv_grav;
+  a.inv_2n = 0.5 / a.nlon;
+}
 
 template <typename R>
 __device__ __forceinline__ R up1(R x, int lane) {  // value of lane - 1 (0 for lane 0)
@@ -445,7 +468,7 @@ __global__ void __launch_bounds__(256) k_hs_column_adjoint(ColAdjArgs<T> a, cons
   const size_t c1 = colv ? col : 0;
   const R ps = a.ps[c1], psp = a.psp[c1], gl = a.gl[c1], gt = a.gt[c1];
   const R DLN = colv ? (R)a.DLN[c1] : (R)0;
-  const R Rg = (R)a.rdgas, kap = (R)a.kappa;
+  const R Rg = (R)a.rdgas_t, kap = (R)a.kappa_t;
   // vertical constants; lanes >= nd carry zeros (dbk = 1 keeps the divisions finite)
   const R bk = act ? (R)vc.bk[k] : (R)0, bk1 = act ? (R)vc.bk[k + 1] : (R)0, dbk = act ? (R)vc.dbk[k] : (R)1;
   const R rdbk = (R)1 / dbk;
@@ -517,33 +540,33 @@ __global__ void __launch_bounds__(256) k_hs_column_adjoint(ColAdjArgs<T> a, cons
   glb += gub * u;
   gtb += gub * v;
   // ---- HS_Forcing! of the p level and the energy integral of Compute_Corrections_Init ----
-  const R t_zero = 315, t_strat = 200, sb = (R)a.sigma_b;
+  const R t_zero = 315, t_strat = 200, sb = (R)a.sigma_b_t;
   const R sj = a.sinj[j], s2 = sj * sj, c2 = (R)1 - s2, c4 = c2 * c2;
-  const R Ep_bar = (R)a.sc[SC_EP_BAR], Wc = (R)(a.wts[j] / (2.0 * a.nlon));
-  const R Dt = (R)a.Dt, icp = (R)a.inv_cp, ig = (R)a.inv_grav;
-  const R lps = log(ps) - (R)a.ln_p0;  // one logarithm per column
+  const R Ep_bar = (R)a.sc[SC_EP_BAR], Wc = (R)(a.wts[j] * a.inv_2n);
+  const R Dt = (R)a.Dt, icp = (R)a.inv_cp_t, ig = (R)a.inv_grav_t;
+  const R lps = log(ps) - (R)a.ln_p0_t;  // one logarithm per column
   R bup = 0, bvp = 0, btp = 0, bps_l = 0, bpsp_l = 0;
   R pb0 = 0, pb1 = 0, pb2 = 0, pb3 = 0, pb4 = 0;
   if (act) {
     const R s = sf - sb, sp = s > (R)0 ? s : (R)0;  // sigma = p_k / ps
-    const R kv = (R)a.kvc * sp;
+    const R kv = (R)a.kvc_t * sp;
     const R duf = -kv * up, dvf = -kv * vp;
     const R lpn = cf + lps;                  // ln(p_k / p0)
     const R pk = exp(kap * lpn);             // (p_k / p0)^kappa
     const R pn = sf * ps * (R)1.0e-5;        // p_k / p0
-    const R tpot = t_zero - (R)a.dT_y * s2 - (R)a.dtheta_z * c2 * lpn;
+    const R tpot = t_zero - (R)a.dT_y_t * s2 - (R)a.dtheta_z_t * c2 * lpn;
     const R te = tpot * pk;
     const R teq = te > t_strat ? te : t_strat;
-    const R kt = (R)a.ka + (R)a.ktc * sp * c4;
+    const R kt = (R)a.ka_t + (R)a.ktc_t * sp * c4;
     const R fr = -((up + (R)0.5 * duf * Dt) * duf + (vp + (R)0.5 * dvf * Dt) * dvf) * icp;
     const R dTf = fr - kt * (tp - teq);
     const R aa = up + Dt * duf, bb = vp + Dt * dvf;
-    const R enp = (R)0.5 * (aa * aa + bb * bb) + (R)a.cp * (tp + Dt * dTf);
+    const R enp = (R)0.5 * (aa * aa + bb * bb) + (R)a.cp_t * (tp + Dt * dTf);
     bpsp_l = Ep_bar * Wc * ig * enp * dbk;
     const R eb = Ep_bar * Wc * ((R)vc.dak[k] + dbk * psp) * ig;
     const R ba = eb * aa, bbv = eb * bb;
-    btp += (R)a.cp * eb;
-    R bdTf = DT + (R)a.cp * Dt * eb;
+    btp += (R)a.cp_t * eb;
+    R bdTf = DT + (R)a.cp_t * Dt * eb;
     R bduf = DU + Dt * ba;
     R bdvf = DV + Dt * bbv;
     bup += ba;
@@ -558,15 +581,15 @@ __global__ void __launch_bounds__(256) k_hs_column_adjoint(ColAdjArgs<T> a, cons
     const R bkv = -bduf * up - bdvf * vp;
     bup -= kv * bduf;
     bvp -= kv * bdvf;
-    const R spn = sp * (R)a.inv_1msb;
-    pb0 = bkv * spn * (R)a.inv_day;
-    pb1 = bkt * ((R)1 - spn * c4) * (R)a.inv_day;
-    pb2 = bkt * spn * c4 * (R)a.inv_day;
+    const R spn = sp * (R)a.inv_1msb_t;
+    pb0 = bkv * spn * (R)a.inv_day_t;
+    pb1 = bkt * ((R)1 - spn * c4) * (R)a.inv_day_t;
+    pb2 = bkt * spn * c4 * (R)a.inv_day_t;
     const R bte = te > t_strat ? bteq : (R)0;
     pb3 = -s2 * pk * bte;
     pb4 = -c2 * lpn * pk * bte;
     // d te / d pn = (pk / pn) (kappa tpot - dtheta_z cos^2); pn = sf ps / p0
-    const R dte = pk / pn * (kap * tpot - (R)a.dtheta_z * c2);
+    const R dte = pk / pn * (kap * tpot - (R)a.dtheta_z_t * c2);
     bps_l = bte * dte * sf * (R)1.0e-5;
   }
   const R glb_c = wsum(act ? glb : (R)0), gtb_c = wsum(act ? gtb : (R)0);
@@ -814,11 +837,16 @@ int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x0, const StateBuf*
   fa.do_energy = md->P.do_energy_correction;
   fa.cp = md->cp_air;
   fa.grav = md->P.grav;
+  fa.inv_2n = 0.5 / nlon;
+  fa.ig = 1.0 / md->P.grav;
+  fa.cpf = (float)md->cp_air;
+  fa.igf = (float)(1.0 / md->P.grav);
   const int nbp = (int)((grid_elems(m, nd) + 255) / 256);  // a thread per grid point
+  const int nbc = (G + 255) / 256;                          // a thread per column
   JG_CUDA(launch_pdl(k_fix1<T>, nbp, 256, 0, st, fa));
   JG_CUDA(launch_pdl(k_fold1<T>, 1, 256, 0, st, fa, nbp));
-  k_fix2<T><<<w->nb_adj, 256, 0, st>>>(fa);  // a warp per column
-  JG_CUDA(launch_pdl(k_fold2<T>, 1, 256, 0, st, fa, w->nb_adj));
+  JG_CUDA(launch_pdl(k_fix2<T>, nbc, 256, 0, st, fa));
+  JG_CUDA(launch_pdl(k_fold2<T>, 1, 256, 0, st, fa, nbc));
   JG_CUDA(launch_pdl(k_fix3<T>, nbp, 256, 0, st, fa));
   JG_CUDA(cudaGetLastError());
   // 2. syntheses of the new level reversed: ln ps, T, vor, div, u cos, v cos
@@ -989,6 +1017,7 @@ int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x0, const StateBuf*
     ca.cp = md->cp_air;
     ca.inv_cp = 1.0 / md->cp_air;
     ca.inv_grav = 1.0 / md->P.grav;
+    col_adj_consts<T>(ca);
   }
   k_hs_column_adjoint<T><<<w->nb_adj, 256, 0, st>>>(ca, md->d_vc);
   JG_CUDA(launch_pdl(k_fold_params, 5, 256, 0, st, w->ppart, w->nb_adj, w->pbar));
