@@ -110,29 +110,33 @@ __global__ void __launch_bounds__(256) k_fold1(FixArgs a, int nb) {
   }
 }
 
-// energy fixer reversed: en_n = |u_n|^2/2 + cp T_n weighted by dp(ps_n2); one thread per column
-// (consecutive longitudes: every level read and write is a coalesced row), arithmetic in the state
-// precision with the layer coefficients staged per block; block partials of ps_n2_bar ps_n in FP64
+// energy fixer reversed: en_n = |u_n|^2/2 + cp T_n weighted by dp(ps_n2).  Block = 32 consecutive
+// columns of one latitude row x 8 level groups (warp g takes levels g, g+8, ...: every read and write
+// a coalesced row), arithmetic in the state precision with the layer coefficients staged per block;
+// the column sums fold over the level groups in a fixed order; block partials of ps_n2_bar ps_n in
+// FP64.
 template <typename T>
 __global__ void __launch_bounds__(256) k_fix2(FixArgs a) {
   using R = T;
-  __shared__ R s_dak[JGCM_MAX_ND], s_dbk[JGCM_MAX_ND];
+  constexpr int KS = 8;
+  __shared__ R s_dak[JGCM_MAX_ND], s_dbk[JGCM_MAX_ND], s_acc[KS][32];
   for (int q = threadIdx.x; q < a.nd; q += blockDim.x) {
     s_dak[q] = (R)a.vc->dak[q];
     s_dbk[q] = (R)a.vc->dbk[q];
   }
   __syncthreads();
   pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
-  const int G = a.nlat * a.nlon, c = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool colv = c < G;
-  const int j = colv ? c / a.nlon : 0;
+  const int G = a.nlat * a.nlon, lane = threadIdx.x & 31, ks = threadIdx.x >> 5, j = blockIdx.y;
+  const int i = blockIdx.x * 32 + lane;
+  const bool act = i < a.nlon;
+  const int c = j * a.nlon + (act ? i : 0);
   const R factor = (R)a.sc[SC_FACTOR], corr = (R)a.sc[SC_CORR], En_bar = (R)a.sc[SC_EN_BAR];
   const R Wc = (R)(a.wts[j] * a.inv_2n), cp = pick<R>(a.cp, a.cpf), ig = pick<R>(a.ig, a.igf);
-  const R ps2 = colv ? (R)((const T*)a.ps_n2)[c] : (R)0;
+  const R ps2 = act ? (R)((const T*)a.ps_n2)[c] : (R)0;
   R acc = 0;
-  if (colv && a.do_energy) {
-#pragma unroll 4
-    for (int k = 0; k < a.nd; k++) {
+  if (act && a.do_energy) {
+#pragma unroll 4  // nd <= 32: every level's loads in flight together
+    for (int k = ks; k < a.nd; k += KS) {
       const size_t x = c + (size_t)G * k;
       const R u = ((const T*)a.u_n)[x], v = ((const T*)a.v_n)[x], t = ((const T*)a.t_n2)[x] - corr;
       const R dbk = s_dbk[k];
@@ -144,17 +148,21 @@ __global__ void __launch_bounds__(256) k_fix2(FixArgs a) {
       acc += en * dbk;
     }
   }
+  s_acc[ks][lane] = acc;
+  __syncthreads();
   double s = 0.0;
-  if (colv) {
+  if (ks == 0 && act) {
+    R tot = 0;
+    for (int q = 0; q < KS; q++) tot += s_acc[q][lane];
     R bps = ((T*)a.bps)[c];
     if (a.do_energy) {
-      bps += En_bar * Wc * ig * acc;
+      bps += En_bar * Wc * ig * tot;
       ((T*)a.bps)[c] = bps;
     }
     s = (double)bps * ((double)ps2 / (double)factor);
   }
   s = block_sum(s);
-  if (threadIdx.x == 0) a.part[blockIdx.x] = s;
+  if (threadIdx.x == 0) a.part[blockIdx.y * gridDim.x + blockIdx.x] = s;
 }
 
 template <typename T>
@@ -842,11 +850,11 @@ int adjoint_step(jgcm_model* md, AdjWork* w, const StateBuf* x0, const StateBuf*
   fa.cpf = (float)md->cp_air;
   fa.igf = (float)(1.0 / md->P.grav);
   const int nbp = (int)((grid_elems(m, nd) + 255) / 256);  // a thread per grid point
-  const int nbc = (G + 255) / 256;                          // a thread per column
+  const dim3 gf2((nlon + 31) / 32, nlat);                   // 32 columns x 8 level groups
   JG_CUDA(launch_pdl(k_fix1<T>, nbp, 256, 0, st, fa));
   JG_CUDA(launch_pdl(k_fold1<T>, 1, 256, 0, st, fa, nbp));
-  JG_CUDA(launch_pdl(k_fix2<T>, nbc, 256, 0, st, fa));
-  JG_CUDA(launch_pdl(k_fold2<T>, 1, 256, 0, st, fa, nbc));
+  JG_CUDA(launch_pdl(k_fix2<T>, gf2, 256, 0, st, fa));
+  JG_CUDA(launch_pdl(k_fold2<T>, 1, 256, 0, st, fa, (int)(gf2.x * gf2.y)));
   JG_CUDA(launch_pdl(k_fix3<T>, nbp, 256, 0, st, fa));
   JG_CUDA(cudaGetLastError());
   // 2. syntheses of the new level reversed: ln ps, T, vor, div, u cos, v cos
