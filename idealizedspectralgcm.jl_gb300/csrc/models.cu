@@ -2867,7 +2867,20 @@ struct AdjArgs {
   const int2* pairs;
   int npairs, nd, ns, N, init_step, dt;
   double xi, ps_ref, robert;
+  // the scalars rounded to T on the host (no FP64 division or conversion per thread) and the
+  // Laplacian eigenvalues in T
+  const T* eig_t;
+  T xi_t, rpsr_t, xipsr_t, rob_t;
 };
+
+template <typename T>
+void adj_consts(AdjArgs<T>& a, const T* eig_t) {
+  a.eig_t = eig_t;
+  a.xi_t = (T)a.xi;
+  a.rpsr_t = (T)(1.0 / a.ps_ref);
+  a.xipsr_t = (T)(a.xi / a.ps_ref);
+  a.rob_t = (T)a.robert;
+}
 
 // y = M^T x for row-major M: y_k = sum_c M[c][k] x_c at the lane's level k; lanes >= nd return 0
 template <typename R, typename E>
@@ -2908,8 +2921,8 @@ __global__ void __launch_bounds__(256) k_hs_implicit_adjoint(AdjArgs<T> a) {
   const bool act = lane < nd;
   const size_t row = (size_t)m * (a.ns + 1) + n, s = row * nd + (act ? lane : 0);
   auto ld = [&](const V2<T>* p, int comp) -> R { return act ? (R)(comp ? p[s].y : p[s].x) : (R)0; };
-  const R rob = (R)a.robert, Dt = (R)a.dt, d = (R)a.damping[row], f = (R)a.dfac[row], xi = (R)a.xi;
-  const R rpsr = (R)(1.0 / a.ps_ref), xipsr = (R)(a.xi / a.ps_ref), eig = (R)a.eig64[row];
+  const R rob = (R)a.rob_t, Dt = (R)a.dt, d = (R)a.damping[row], f = (R)a.dfac[row], xi = (R)a.xi_t;
+  const R rpsr = (R)a.rpsr_t, xipsr = (R)a.xipsr_t, eig = (R)a.eig_t[row];
   for (int comp = 0; comp < 2; comp++) {  // real and imaginary parts are independent
     R dvb, vpb, vcb, ddb2, dpb, dcb, dtb2, tpb, tcb;
     lf_adj<R>(a.init_step, Dt, rob, d, f, ld(a.vn_b, comp), ld(a.vc_b, comp), dvb, vpb, vcb);
@@ -3088,6 +3101,7 @@ int si_adjoint_launch(jgcm_model* md, const void* const* obar, void* const* ibar
     a.xi = init ? md->P.dt * md->P.implicit_coef : (2 * md->P.dt) * md->P.implicit_coef;
     a.ps_ref = md->P.ps_ref;
     a.robert = md->P.robert_coef;
+    adj_consts<T>(a, tables<T>(m).eig);
     return launch_pdl(k_hs_implicit_adjoint<T>, dim3((md->npairs + 7) / 8), dim3(256), 0, st, a);
   };
   JG_CUDA(is_fp64(m) ? launch(double()) : launch(float()));
@@ -3192,6 +3206,7 @@ extern "C" int jgcm_model_semi_implicit_step_adjoint(jgcm_model* md, const doubl
     a.xi = md->init_step ? md->P.dt * md->P.implicit_coef : (2 * md->P.dt) * md->P.implicit_coef;
     a.ps_ref = md->P.ps_ref;
     a.robert = md->P.robert_coef;
+    adj_consts<T>(a, tables<T>(m).eig);
     k_hs_implicit_adjoint<T><<<(md->npairs + 7) / 8, 256, 0, st>>>(a);
   };
   if (is_fp64(m)) launch(double());
