@@ -681,6 +681,7 @@ struct CorrArgs {
   int nd, nlat, nlon, do_mass, do_energy;
   double cp, grav;
   double inv_2n;  // 1 / (2 nlon), exact (nlon is a power of two)
+  T cp_t;         // cp rounded to T on the host
 };
 
 template <typename T>
@@ -705,7 +706,7 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   __shared__ T part[2][KS][32];
   T ea = 0, eb = 0;
   if (act) {
-    const T cp = (T)a.cp;
+    const T cp = a.cp_t;
 #pragma unroll 4  // nd <= 32: every level's loads in flight together
     for (int k = ks; k < nd; k += KS) {
       size_t x = offL + (size_t)k * G + col;
@@ -742,25 +743,34 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   __shared__ double fc[2];
   double* scal = a.scalars + 4 * e;
   if (grid_reduce_last<3>(vals, a.partials + e * a.pstride, a.counter + e, a.wts, tot3)) {
+    // the mass factor first; then its logarithm (warp 0) and the energy correction (warp 1) side by
+    // side, each a chain of FP64 operations on its own sub-partition
+    __shared__ double s_tot[3];
     if (threadIdx.x == 0) {
-      const double inv_2n = a.inv_2n;
-      double mean_ps_p = scal[0], mean_energy_p = scal[1];
-      double factor = 1.0, corr = 0.0;
-      if (a.do_mass) {
-        double mean_ps_n = tot3[0] * inv_2n;
-        factor = mean_ps_p / mean_ps_n;
-        V2<T> l = a.lnps_n[e];  // spe_lnps_n[1,1,1] += log(factor)  (P_00 = 1)
-        l.x = (T)((double)l.x + log(factor));
-        a.lnps_n[e] = l;
-      }
+      double factor = 1.0;
+      if (a.do_mass) factor = scal[0] / (tot3[0] * a.inv_2n);  // mean_ps_p / mean_ps_n
+      fc[0] = factor;
+      s_tot[1] = tot3[1];
+      s_tot[2] = tot3[2];
+      scal[2] = factor;
+      a.scal_t[2 * e] = (T)factor;
+    }
+    __syncthreads();
+    const double factor = fc[0];
+    if (threadIdx.x == 0 && a.do_mass) {
+      V2<T> l = a.lnps_n[e];  // spe_lnps_n[1,1,1] += log(factor)  (P_00 = 1)
+      l.x = (T)((double)l.x + log(factor));
+      a.lnps_n[e] = l;
+    }
+    if (threadIdx.x == 32) {
+      double corr = 0.0;
       if (a.do_energy) {
         // Δp_k = Δa_k + Δb_k (factor ps_n): the mass correction enters linearly
-        double mean_energy_n = (tot3[1] + factor * tot3[2]) * inv_2n / a.grav;
+        const double mean_ps_p = scal[0], mean_energy_p = scal[1];
+        const double mean_energy_n = (s_tot[1] + factor * s_tot[2]) * a.inv_2n / a.grav;
         corr = a.grav * (mean_energy_p - mean_energy_n) / (a.cp * mean_ps_p);
       }
-      scal[2] = factor;
       scal[3] = corr;
-      a.scal_t[2 * e] = (T)factor;
       a.scal_t[2 * e + 1] = (T)corr;
       fc[1] = corr;
     }
@@ -1612,6 +1622,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ca.cp = md->cp_air;
   ca.grav = md->P.grav;
   ca.inv_2n = 0.5 / m->nlon;
+  ca.cp_t = (T)md->cp_air;
   // the fixers (this branch) and the next step's gradients of the new level (second branch)
   const bool serial = g_marker != nullptr;  // per-kernel timing: one stream, launches in order
   cudaStream_t br = serial ? st : md->side;
