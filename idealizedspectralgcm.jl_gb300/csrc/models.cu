@@ -119,12 +119,15 @@ __device__ bool grid_reduce_last(const double* vals, double* partials, unsigned*
   if ((threadIdx.x & 31) == 0)
     for (int v = 0; v < NV; v++) red[v][threadIdx.x >> 5] = s[v];
   __syncthreads();
-  if (threadIdx.x == 0) {  // the caller reads the totals in thread 0 (FP64 work on one warp only)
-    for (int v = 0; v < NV; v++) {
-      double t = 0.0;
-      for (int q = 0; q < nw; q++) t += red[v][q];
-      out[v] = t;
-    }
+  __shared__ double tot[NV];
+  if (threadIdx.x < NV) {  // one lane per total: the NV folds side by side, each in its fixed order
+    double t = 0.0;
+    for (int q = 0; q < nw; q++) t += red[threadIdx.x][q];
+    tot[threadIdx.x] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {  // the caller reads the totals in thread 0
+    for (int v = 0; v < NV; v++) out[v] = tot[v];
     *counter = 0u;
   }
   return true;
