@@ -73,30 +73,15 @@ __device__ __forceinline__ T shfl_dn1(T x, int lane, int nd, T fill) {
   return lane + 1 >= nd ? fill : y;
 }
 
-// Deterministic grid-wide FP64 reduction over a (x = column chunk, y = latitude) grid.  Thread 0
-// of every block passes its NV block sums; the last block to finish (atomic ticket) folds the
-// partials in a fixed order, sum_j w_j sum_b partial[v][j][b], and returns true with the NV
-// totals in out[] of its thread 0.  All other blocks return false.  U
-// partials per thread are loaded before they are added (in their fixed order): latency hidden when
-// a thread folds many partials, at U * NV * 2 registers of the whole kernel.
+// Block-wide deterministic fold of the FP64 partials of a (gx = column chunk, y = latitude) grid of
+// nb blocks, sum_j w_j sum_b partial[v][j][b] (v < NV): every thread of the block calls it; each
+// folds a fixed strided subset (weighted by the latitude of the block's row), then warps and lanes
+// combine in a fixed order.  The NV totals land in out[] of thread 0.  U partials per thread are
+// loaded before they are added (in their fixed order): latency hidden when a thread folds many
+// partials, at U * NV * 2 registers of the whole kernel.
 template <int NV, int U = 1>
-__device__ bool grid_reduce_last(const double* vals, double* partials, unsigned* counter, const double* wts,
-                                 double* out) {
-  __shared__ bool am_last;
+__device__ void fold_weighted(const double* partials, int nb, int gx, const double* wts, double* out) {
   __shared__ double red[NV][32];
-  const int nb = gridDim.x * gridDim.y;
-  const int bid = blockIdx.y * gridDim.x + blockIdx.x;
-  if (threadIdx.x == 0) {
-    for (int v = 0; v < NV; v++) partials[(size_t)v * nb + bid] = vals[v];
-    __threadfence();
-    unsigned t = atomicAdd(counter, 1u);
-    am_last = (t == (unsigned)nb - 1);
-  }
-  __syncthreads();
-  if (!am_last) return false;
-  __threadfence();
-  // every thread folds a fixed strided subset of the block partials (weighted by the latitude of
-  // the block's row), then warps and the block combine in a fixed order: deterministic
   double s[NV];
   for (int v = 0; v < NV; v++) s[v] = 0.0;
   for (int b0 = threadIdx.x; b0 < nb; b0 += U * blockDim.x) {
@@ -104,7 +89,7 @@ __device__ bool grid_reduce_last(const double* vals, double* partials, unsigned*
 #pragma unroll
     for (int u = 0; u < U; u++) {
       const int b = b0 + u * (int)blockDim.x;
-      wv[u] = b < nb ? wts[b / gridDim.x] : 0.0;
+      wv[u] = b < nb ? wts[b / gx] : 0.0;
 #pragma unroll
       for (int v = 0; v < NV; v++) pv[u][v] = b < nb ? __ldcg(partials + (size_t)v * nb + b) : 0.0;
     }
@@ -126,10 +111,31 @@ __device__ bool grid_reduce_last(const double* vals, double* partials, unsigned*
     tot[threadIdx.x] = t;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {  // the caller reads the totals in thread 0
+  if (threadIdx.x == 0)
     for (int v = 0; v < NV; v++) out[v] = tot[v];
-    *counter = 0u;
+}
+
+// Deterministic grid-wide FP64 reduction over a (x = column chunk, y = latitude) grid.  Thread 0
+// of every block passes its NV block sums; the last block to finish (atomic ticket) folds the
+// partials (fold_weighted) and returns true with the NV totals in out[] of its thread 0.  All other
+// blocks return false.
+template <int NV, int U = 1>
+__device__ bool grid_reduce_last(const double* vals, double* partials, unsigned* counter, const double* wts,
+                                 double* out) {
+  __shared__ bool am_last;
+  const int nb = gridDim.x * gridDim.y;
+  const int bid = blockIdx.y * gridDim.x + blockIdx.x;
+  if (threadIdx.x == 0) {
+    for (int v = 0; v < NV; v++) partials[(size_t)v * nb + bid] = vals[v];
+    __threadfence();
+    unsigned t = atomicAdd(counter, 1u);
+    am_last = (t == (unsigned)nb - 1);
   }
+  __syncthreads();
+  if (!am_last) return false;
+  __threadfence();
+  fold_weighted<NV, U>(partials, nb, gridDim.x, wts, out);
+  if (threadIdx.x == 0) *counter = 0u;
   return true;
 }
 
@@ -151,8 +157,7 @@ struct HSColArgs {
   T *ducos, *dvcos, *dtg, *energy, *dlnps, *t_eq;
   const V2<T>* t_spec;  // spe_t_c: its (0,0) modes are the level means of T
   const double* wts;
-  double *partials, *scalars;  // per member: partials + e * pstride, scalars + 4 e
-  unsigned* counter;          // per member: counter + e
+  double* partials;  // per member: partials + e * pstride (the block partials of mean ps_p, energy_p)
   size_t pstride;
   int nd, nlat, nlon, Dt;
   double sigma_b, k_f, k_a, k_s, dT_y, dtheta_z, kappa, rdgas, cp, grav;
@@ -394,12 +399,13 @@ __global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertC
       vals[0] += red[0][q];
       vals[1] += red[1][q];
     }
-  double tot2[2];
-  double* scal = a.scalars + 4 * e;
-  // 64 threads fold (nlon / (64 / S)) x nlat partials (512 at T42 with S = 4): 8 loads in flight each
-  if (grid_reduce_last<2, 8>(vals, a.partials + e * a.pstride, a.counter + e, a.wts, tot2) && threadIdx.x == 0) {
-    scal[0] = tot2[0] * a.inv_2n;           // mean_ps_p   (Area_Weighted_Global_Mean)
-    scal[1] = tot2[1] * a.inv_2n / a.grav;  // mean_energy_p (Mass_Weighted_Global_Integral)
+  // the block partials only: the fixer reduction, their one consumer, folds them (its last block), so
+  // no grid-wide fold sits at this kernel's end
+  if (threadIdx.x == 0) {
+    const int nb = gridDim.x * gridDim.y, bid = blockIdx.y * gridDim.x + blockIdx.x;
+    double* p = a.partials + e * a.pstride;
+    p[bid] = vals[0];
+    p[(size_t)nb + bid] = vals[1];
   }
 }
 
@@ -677,10 +683,15 @@ struct CorrArgs {
   const T *u_n, *v_n, *t_n, *ps_n;
   V2<T>*lnps_n, *t_spec_n;
   const double* wts;
-  double *partials, *scalars;  // per member as in HSColArgs
+  double *partials, *scalars;  // per member: partials + e * pstride, scalars + 4 e
   T* scal_t;                   // per member: factor and correction rounded to T (for k_hs_corr_apply)
   unsigned* counter;
   size_t pstride;
+  // the column kernel's block partials (mean ps and column energy of the previous level) at the
+  // start of the member's region, its grid (col_gx x nlat blocks); this kernel's own partials at
+  // col_off
+  int col_gx, col_nb;
+  size_t col_off;
   int nd, nlat, nlon, do_mass, do_energy;
   double cp, grav;
   double inv_2n;  // 1 / (2 nlon), exact (nlon is a power of two)
@@ -745,11 +756,17 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   double tot3[3];
   __shared__ double fc[2];
   double* scal = a.scalars + 4 * e;
-  if (grid_reduce_last<3>(vals, a.partials + e * a.pstride, a.counter + e, a.wts, tot3)) {
+  if (grid_reduce_last<3>(vals, a.partials + e * a.pstride + a.col_off, a.counter + e, a.wts, tot3)) {
+    // Compute_Corrections_Init: the previous level's mean ps and energy from the column kernel's
+    // partials (64-thread blocks of (nlon / (64 / S)) x nlat: 512 at T42 with S = 4)
+    double totc[2];
+    fold_weighted<2, 2>(a.partials + e * a.pstride, a.col_nb, a.col_gx, a.wts, totc);
     // the mass factor first; then its logarithm (warp 0) and the energy correction (warp 1) side by
     // side, each a chain of FP64 operations on its own sub-partition
     __shared__ double s_tot[3];
     if (threadIdx.x == 0) {
+      scal[0] = totc[0] * a.inv_2n;           // mean_ps_p   (Area_Weighted_Global_Mean)
+      scal[1] = totc[1] * a.inv_2n / a.grav;  // mean_energy_p (Mass_Weighted_Global_Integral)
       double factor = 1.0;
       if (a.do_mass) factor = scal[0] / (tot3[0] * a.inv_2n);  // mean_ps_p / mean_ps_n
       fc[0] = factor;
@@ -1131,14 +1148,11 @@ int build_wave(jgcm_model* md) {
   return JGCM_OK;
 }
 
-// FP64 block partials per member: the column kernel folds 2 sums over its (nlon/(64/S)) x nlat blocks
-// (S <= 8),
-// the fixer kernel 3 sums over (nlon/32) x nlat blocks
-size_t partial_stride(const jgcm_mesh* m) {
-  size_t a = (size_t)2 * ((m->nlon + HS_CT / 8 - 1) / (HS_CT / 8)) * m->nlat;
-  size_t b = (size_t)3 * ((m->nlon + 31) / 32) * m->nlat;
-  return a > b ? a : b;
-}
+// FP64 block partials per member: the column kernel's 2 sums over its (nlon/(64/S)) x nlat blocks
+// (S <= 8) first, then the fixer kernel's 3 sums over (nlon/32) x nlat blocks (both live until the
+// fixer's last block has folded them)
+size_t col_partials(const jgcm_mesh* m) { return (size_t)2 * ((m->nlon + HS_CT / 8 - 1) / (HS_CT / 8)) * m->nlat; }
+size_t partial_stride(const jgcm_mesh* m) { return col_partials(m) + (size_t)3 * ((m->nlon + 31) / 32) * m->nlat; }
 
 int model_alloc(jgcm_model* md) {
   jgcm_mesh* m = md->mesh;
@@ -1493,8 +1507,6 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   a.t_spec = (const V2<T>*)md->spe_t[c];
   a.wts = m->d_wts;
   a.partials = md->d_partials;
-  a.scalars = md->d_scalars;
-  a.counter = md->d_counter;
   a.nd = nd;
   a.nlat = m->nlat;
   a.nlon = m->nlon;
@@ -1618,6 +1630,9 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ca.counter = md->d_counter;
   ca.nd = nd;
   ca.pstride = partial_stride(m);
+  ca.col_gx = (m->nlon + HS_CT / md->hs_lanes - 1) / (HS_CT / md->hs_lanes);
+  ca.col_nb = ca.col_gx * m->nlat;
+  ca.col_off = col_partials(m);
   ca.nlat = m->nlat;
   ca.nlon = m->nlon;
   ca.do_mass = md->P.do_mass_correction;

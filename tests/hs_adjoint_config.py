@@ -9,8 +9,8 @@ the initial spectral temperature and to k_f, k_a, k_s, dT_y, dtheta_z.
 
 Reported:
   * the FP64 GPU gradient against central finite differences of the FP64 GPU forward model
-    (eps = 1e-6, relative for the parameters, and 1e-4 where the difference at 1e-6 is at the
-    rounding level of the loss; one seeded direction for T0, row N+1 left out: that row is zero in
+    (eps = 1e-6, relative for the parameters, and 1e-4 and 1e-3 where the difference at 1e-6 is at
+    the rounding level of the loss; one seeded direction for T0, row N+1 left out: that row is zero in
     every analysed field and not part of the control);
   * the FP64 GPU gradient against the FP64 oracle's gradient (the C restatement, every state kept);
   * the mixed-precision (FP32) gradient against the FP64 gradient;
@@ -142,7 +142,7 @@ def main():
             fdrep = {"T0_direction": {"fd": fd, "adjoint": ad, "rel_err": abs(fd - ad) / abs(ad)}}
             for i, p in enumerate(jgcm.HS_PARAMS):
                 fdrep[p] = {"adjoint": float(gp[i])}
-                for e in (eps, 1e-4):  # 1e-4: truncation O(e^2) still far below, rounding 100x smaller
+                for e in (eps, 1e-4, 1e-3):  # larger steps: truncation O(e^2) still far below, rounding smaller
                     h = e * configs.PARAMS[NAME][p]
                     vals = []
                     for sg in (1, -1):
