@@ -214,8 +214,10 @@ __device__ __forceinline__ R seg_excl_suffix(R x, int s) {  // sum over the lane
   return incl - x;
 }
 
+// FP32: at most 72 registers (14 blocks of 64 threads per SM): at ensemble scale the kernel streams
+// and its time follows occupancy (at 77 registers, allocated as 80, 12 blocks: 97 -> 109 us, measured)
 template <typename T, int S>
-__global__ void __launch_bounds__(HS_CT) k_hs_column(HSColArgs<T> a, const VertCoef* __restrict__ vcp) {
+__global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HSColArgs<T> a, const VertCoef* __restrict__ vcp) {
   const VertCoef& vc = *vcp;
   __shared__ double red[2][HS_CT / 32];
   // the vertical coefficients in the state precision, staged once per block (constants: staged
