@@ -12,7 +12,7 @@ value      sim-days/s of the mixed-precision path (FP32 state, transforms and te
            (256 MiB write) before every timed sim-day.
 e2e        the same through the C ABI with host (pinned) buffers: per sim-day the whole state (one packed
            FP64 buffer of the 18 state arrays, reference layout) is uploaded, 72 steps run, and the
-           state is read back into the same buffer; wall-clock.
+           state is read back into the same buffer; wall-clock.  fp64.e2e: the FP64 path the same way.
 fp64       the FP64 GPU path on the same workload, same timing; error_vs_fp64 = relative L2 of
            T, u, v, ps of a mixed-precision twin against an FP64 twin stepped the same days from
            the same state (tensor_core_modes: the same for TF32x3 / BF16x3, with their speed).
@@ -21,6 +21,16 @@ roofline   the dominant kernel of the mixed step (largest summed CUDA-event time
            bytes per launch / its mean launch time, against the measured HBM copy bandwidth.
 adjoint    the one-day gradient (HS T42L20, 72 steps, checkpoint every 8) in both paths: ms per
            gradient and the mixed gradient's error against the FP64 one.
+config1    Barotropic T42 (128x64, 1 level) in FP64, 480 steps of 1800 s (10 days) from the Rossby-Haurwitz
+           wave 4 + seeded noise: sim-days/s, whole-step roofline, end-state error against the FP64 oracle.
+config2    Shallow water T85 (256x128), 864 steps of 600 s (6 days) from the unstable jet + seeded bump, in
+           FP32 and split-BF16 (BF16x3): sim-days/s, whole-step roofline, per-field error against the FP64
+           oracle at day 6.
+config4    The batched ensemble as stated: 128 x HS T21L20, 32 x HS T42L20, 8 x SW T85 in split-BF16 with
+           tiles from the autotuner, 30 simulated days per member in one graph launch per 24 windows:
+           ensemble sim-days/s, and the first and last member of each truncation against the FP64 oracle
+           (and against an FP64 GPU twin) after the 30 days.
+the benchmark spec the last key: the headline figures in one short object (the driver keeps the tail of stdout).
 cpu_baseline  the FP64 C oracle (a restatement of the reference on the host) timed on a bounded sample.
 --impl reference  times that oracle on all host threads on the same workload (the reference itself is
            Julia and Julia is not installed on the GPU hosts).
@@ -205,6 +215,102 @@ def profile_traffic(kernel: str):
         return None
 
 
+def step_bytes(kind: str, N: int, nlat: int, nlon: int, nd: int, esize: int) -> float:
+    """Algorithmic bytes of one model step from its transform counts: every transform reads its input
+    and writes its output once, (#S2G + #G2S)(G + 2S) + #alpha (2G + 2S) reals of esize bytes per level
+    (G = nlon nlat grid points, S = (N+1)(N+2) spectral reals).  Barotropic_Dynamics!: 3 S2G (vorticity,
+    u, v) and the alpha pair of Vor_Div_From_Grid_UV!; Shallow_Water_Dynamics!: 7 S2G (two gradients,
+    vor, div, h, u, v), 2 G2S (kinetic energy, h tendency) and the alpha pair."""
+    G, S = nlon * nlat, (N + 1) * (N + 2)
+    n_s2g, n_g2s, n_alpha = {"barotropic": (3, 0, 2), "shallow_water": (7, 2, 2)}[kind]
+    return float(esize * nd * ((n_s2g + n_g2s) * (G + 2 * S) + n_alpha * (2 * G + 2 * S)))
+
+
+def oracle_job(job):
+    """One FP64 oracle run in a worker process (started with the spawn method): build the workload's
+    initial state exactly as the GPU side does for it (configs.init_*), step it, return the prognostic
+    fields.  job = (workload, init, seed, nsteps, threads)."""
+    name, init, seed, nsteps, threads = job
+    for pth in (PKG, os.path.join(ROOT, "oracle")):
+        if pth not in sys.path:
+            sys.path.insert(0, pth)
+    import oracle
+    from jgcm import configs
+
+    oracle.set_threads(threads)
+    m = configs.make_mesh(oracle, name)
+    md = oracle.Model(m, configs.PARAMS[name])
+    if init == "rh4":
+        configs.init_barotropic_rh4(oracle, m, md, seed=seed)
+    elif init == "jet":
+        configs.init_shallow_water_jet(oracle, m, md, seed=seed)
+    else:
+        configs.init_held_suarez(oracle, m, md, seed=seed)
+    t0 = time.perf_counter()
+    md.step(nsteps)
+    kind = configs.PARAMS[name]["kind"]
+    return {"fields": {f: md.get(f) for f in configs.PROGNOSTIC[kind]}, "seconds": time.perf_counter() - t0}
+
+
+def field_errors(gpu, ref, kind):
+    """Relative L2 error per prognostic field (divergence against the vorticity scale, a wind component
+    against the wind), as the parity tests measure it."""
+    import numpy as np
+
+    scale = {"spe_div_c": ("spe_vor_c",), "spe_div_p": ("spe_vor_p",), "grid_div": ("grid_vor",),
+             "grid_u_c": ("grid_u_c", "grid_v_c"), "grid_v_c": ("grid_u_c", "grid_v_c")}
+    out = {}
+    for f, b in ref.items():
+        den = np.linalg.norm(b.ravel())
+        if f in scale and all(g in ref for g in scale[f]):
+            den = max(den, math.sqrt(sum(np.linalg.norm(ref[g].ravel()) ** 2 for g in scale[f])))
+        out[f] = float(np.linalg.norm((gpu[f] - b).ravel()) / (den if den > 0 else 1.0))
+    return out
+
+
+def whole_step_roofline(kind, name, prec, ms_per_step, kt):
+    """Whole-step HBM roofline of a one-layer model (step_bytes / step time) and its longest kernel."""
+    from jgcm import configs
+
+    g = configs.GRIDS[name]
+    alg = step_bytes(kind, g["num_fourier"], g["nlat"], g["nlon"], g["nd"], 8 if prec == "fp64" else 4)
+    peak, pk = measured_peaks()
+    ach = alg / (ms_per_step * 1e-3) / 1e9
+    dom = max(kt, key=kt.get)
+    return {"bound": "hbm", "kernel": "whole step", "achieved": ach, "peak": peak, "unit": "GB/s",
+            "frac": ach / peak, "peak_kind": pk, "algorithmic_bytes_per_step": alg,
+            "longest_kernel": dom, "longest_kernel_share": kt[dom] / sum(kt.values())}
+
+
+def one_layer_bench(jgcm, configs, name, init, prec, nsteps):
+    """A one-layer workload (barotropic or shallow water) on the GPU: the final prognostic fields of
+    exactly nsteps steps from the seeded initial state (the first is the reference's forward step),
+    and, on a twin with the autotuner's tiles, the CUDA-event time of nsteps - 1 steady steps (graph
+    capture before timing steps the twin further), its per-kernel times and the whole-step roofline."""
+    params = configs.PARAMS[name]
+    kind = params["kind"]
+    init_fn = configs.init_barotropic_rh4 if init == "rh4" else configs.init_shallow_water_jet
+    m = configs.make_mesh(jgcm, name, precision=prec)
+    tm = jgcm.Model(m, params)
+    init_fn(jgcm, m, tm)
+    tm.step(1)
+    tuned = jgcm.autotune(tm, nsteps=24)["tuning"]
+    ms = tm.time_steps(nsteps - 1)
+    kt = tm.kernel_times(8)
+    tm.close()
+    md = jgcm.Model(m, params)
+    init_fn(jgcm, m, md)
+    md.step(nsteps)
+    fields = {f: md.get(f) for f in configs.PROGNOSTIC[kind]}
+    md.close()
+    per_step = ms / (nsteps - 1)
+    spd = configs.DAY / params["dt"]
+    out = {"precision": prec, "steps": nsteps, "sim_days": nsteps * params["dt"] / configs.DAY,
+           "sim_days_per_s": 1000.0 / (per_step * spd), "ms_per_step": per_step, "tuning": tuned,
+           "roofline": whole_step_roofline(kind, name, prec, per_step, kt)}
+    return out, fields
+
+
 # ------------------------------------------------------------------------------------------------
 def cpu_baseline(seconds_target: float = 12.0):
     """The FP64 C oracle on the host cores: bounded sample of the same workload."""
@@ -322,6 +428,69 @@ def ensemble_bench(jgcm, configs, precisions, days=2):
     return out
 
 
+def config4_bench(jgcm, configs, prec="bf16x3", days=30):
+    """The batched-ensemble configuration as stated: 128 x HS T21L20, 32 x HS T42L20 and 8 x SW T85 (each
+    member seeded base + e), Legendre contractions in split-BF16 (prec), tiles from the autotuner, `days`
+    simulated days per member.  Every model takes its first window's steps on its own (the first step is
+    the reference's forward step), then all three advance together by 1200 s windows, 24 windows per
+    graph launch, CUDA-event timed.  The first and last member of each truncation start from the FP64 GPU
+    initial state (equal to the oracle's to 1e-12) and are returned with an FP64 GPU twin stepped the same
+    days, for the comparison against the FP64 oracle.  Returns (result, {(name, e): (member, fp64 twin)})."""
+    win = 1200
+    wpd = configs.DAY // win
+    nwin = wpd * days
+    chunk = 24
+    pre = chunk  # windows each model takes on its own first: the first step and the rest of one chunk
+    out = {"precision": prec, "members": {n: e for n, e in ENSEMBLE}, "days": days, "window_seconds": win,
+           "windows_per_graph_launch": chunk}
+    models, meshes, twins, per = [], [], {}, {}
+    for name, E in ENSEMBLE:
+        params = configs.PARAMS[name]
+        kind = params["kind"]
+        init = configs.init_held_suarez if kind == "held_suarez" else configs.init_shallow_water_jet
+        steps_per_win = win // params["dt"]
+        m = configs.make_mesh(jgcm, name, precision=prec)
+        m64 = configs.make_mesh(jgcm, name, precision="fp64")
+        ens = jgcm.Model(m, params, members=E)
+        one = jgcm.Model(m, params)
+        for e in range(E):
+            if e in (0, E - 1):
+                ref = jgcm.Model(m64, params)
+                init(jgcm, m64, ref, seed=configs.BASE_SEED + e)
+                configs.copy_state(ref, one, kind)
+                twins[(name, e)] = ref
+            else:
+                init(jgcm, m, one, seed=configs.BASE_SEED + e)
+            ens.copy_member(e, one)
+        one.close()
+        ens.step(1)
+        per[name] = {"tuning": jgcm.autotune(ens, nsteps=8)["tuning"]}
+        ens.step(pre * steps_per_win - 1)
+        models.append(ens)
+        meshes += [m, m64]
+    group = jgcm.Ensemble(models, win)
+    ms = group.time_windows(nwin - pre)
+    group.close()
+    timed_days = (nwin - pre) * win / configs.DAY
+    out.update({"ensemble_sim_days_per_s": timed_days / (ms / 1000.0), "ms_per_window": ms / (nwin - pre),
+                "timed_sim_days": timed_days, "per_truncation": per})
+    states = {}
+    for (name, E), ens in zip(ENSEMBLE, models):
+        params = configs.PARAMS[name]
+        kind = params["kind"]
+        reader = jgcm.Model(ens.mesh, params)
+        for e in (0, E - 1):
+            reader.copy_member(0, ens, e)
+            twin = twins[(name, e)]
+            twin.step(days * configs.DAY // params["dt"])
+            states[(name, e)] = ({f: reader.get(f) for f in configs.PROGNOSTIC[kind]},
+                                 {f: twin.get(f) for f in configs.PROGNOSTIC[kind]})
+            twin.close()
+        reader.close()
+        ens.close()
+    return out, states
+
+
 def precision_modes(jgcm, configs, days, timed=("tf32x3", "bf16x3")):
     """HS T42L20 in each mixed mode (FP32 SIMT; TF32x3 and BF16x3: the Legendre contractions on the
     tensor cores): the relative L2 error against an FP64 GPU twin stepped the same days from the same
@@ -386,6 +555,49 @@ def adjoint_bench(jgcm, configs, nsteps=72, checkpoint=8):
     return out
 
 
+def e2e_days(jgcm, mesh, params, tiles, init_state, ndays, flush):
+    """End-to-end sim-days through the C ABI with host buffers: per sim-day, upload the whole state
+    (jgcm_model_set_state: one pinned FP64 buffer of the 18 state arrays, reference layout), run 72
+    steps, read it back into the same buffer (jgcm_model_get_state); wall-clock.  The first step (the
+    reference's forward step) runs untimed; every timed day restarts from the host state."""
+    spd = configs_steps_per_day(params)
+    md = jgcm.Model(mesh, params)
+    jgcm.set_tuning(md, tiles)
+    buf, _keep = pinned_like(jgcm.pack_state(mesh, {f: init_state[f] for f in jgcm.STATE_FIELDS}))
+    md.set_state(buf)
+    md.step(1)
+    md.get_state(out=buf)
+    t = 0.0
+    for _ in range(ndays):
+        flush()
+        t0 = time.perf_counter()
+        md.set_state(buf)
+        md.step(spd)
+        md.get_state(out=buf)
+        t += time.perf_counter() - t0
+    md.close()
+    return t, ndays, buf.nbytes
+
+
+def configs_steps_per_day(params):
+    return 86400 // params["dt"]
+
+
+def oracle_checks(jobs, log_prefix="oracle checks"):
+    """Run the FP64 oracle jobs (the checker of the error figures) in spawned worker processes after
+    the GPU work, on the host's cores; returns {job: result}."""
+    import multiprocessing as mp
+
+    cores = os.cpu_count() or 1
+    workers = max(1, min(len(jobs), 4, cores))
+    threads = max(1, cores // workers)
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(workers) as pool:
+        res = pool.map(oracle_job, [j + (threads,) for j in jobs], chunksize=1)
+    log(f"{log_prefix}: {len(jobs)} runs on {workers} x {threads} threads in {time.perf_counter() - t0:.1f} s")
+    return dict(zip(jobs, res))
+
+
 def run_jgcm(args):
     import numpy as np
 
@@ -434,22 +646,8 @@ def run_jgcm(args):
                             else ("tf32x3", "bf16x3"))
     err = modes["fp32"]["error_vs_fp64"]
     # ---- end to end through host buffers: the whole state in one pinned FP64 buffer (reference layout)
-    e2e_model = jgcm.Model(mmx, params)
-    jgcm.set_tuning(e2e_model, tiles["mixed"])
-    buf, _keep = pinned_like(jgcm.pack_state(mmx, {f: init_state[f] for f in jgcm.STATE_FIELDS}))
-    bytes_io = buf.nbytes
-    e2e_model.set_state(buf)
-    e2e_model.step(1)  # the init step; every timed sim-day below restarts from host state
-    e2e_model.get_state(out=buf)
-    t_e2e = 0.0
-    ne2e = max(1, K)
-    for _ in range(ne2e):
-        flush()
-        t0 = time.perf_counter()
-        e2e_model.set_state(buf)
-        e2e_model.step(spd)
-        e2e_model.get_state(out=buf)
-        t_e2e += time.perf_counter() - t0
+    t_e2e, ne2e, bytes_io = e2e_days(jgcm, mmx, params, tiles["mixed"], init_state, max(1, K), flush)
+    t_e2e64, _, _ = e2e_days(jgcm, m64, params, tiles["fp64"], init_state, max(1, K), flush)
     # ---- per-kernel times and the roofline of the dominant kernel
     kt = modmx.kernel_times(spd)
     esize = 8 if args.precision == "fp64" else 4
@@ -486,6 +684,11 @@ def run_jgcm(args):
             extra["adjoint"] = adjoint_bench(jgcm, configs)
         except Exception as e:
             extra["adjoint_error"] = str(e)
+    if not args.no_configs and world == 1:
+        try:
+            extra.update(config_legs(jgcm, configs, args))
+        except Exception as e:
+            extra["configs_error"] = f"{type(e).__name__}: {e}"
     line = {
         "metric": METRIC, "value": value, "unit": "sim-days/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": 1000.0 * t_mx / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -500,7 +703,9 @@ def run_jgcm(args):
                          "L2-resident within a day", "parallelism": f"replicas x{world}",
                    "ms_per_model_step": 1000.0 * t_mx / (K * spd),
                    "tiles": {"chosen_by": "jgcm.autotune (coordinate search, CUDA-event timed)", **tiles}},
-        "fp64": {"value": value64, "unit": "sim-days/s", "ms_per_step": 1000.0 * t_64 / K},
+        "fp64": {"value": value64, "unit": "sim-days/s", "ms_per_step": 1000.0 * t_64 / K,
+                 "e2e": {"value": world * ne2e / t_e2e64, "unit": "sim-days/s", "h2d_bytes_per_step": bytes_io,
+                         "d2h_bytes_per_step": bytes_io}},
         "speedup_vs_fp64": value / value64,
         "error_vs_fp64": {"after_sim_days": round(days_done, 3), **{k: v for k, v in err.items()}},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -514,8 +719,86 @@ def run_jgcm(args):
         "clocks": clk,
         **extra,
     }
+    line["north_star"] = north_star_summary(line)
     print(json.dumps(line), flush=True)
     return 0
+
+
+def north_star_summary(line):
+    """The headline figures in one short object, printed last (the end of stdout is what survives in a
+    truncated log): mixed vs FP64 sim-days/s and their errors, e2e, tensor-core modes, configs 1, 2, 4."""
+    r = lambda x, n=4: None if x is None else float(f"{x:.{n}g}")  # noqa: E731
+    ns = {"mixed_sim_days_per_s": r(line["value"]), "fp64_sim_days_per_s": r(line["fp64"]["value"]),
+          "speedup_vs_fp64": r(line["speedup_vs_fp64"], 3),
+          "error_vs_fp64": {k: r(v, 2) for k, v in line["error_vs_fp64"].items()},
+          "e2e_mixed": r(line["e2e"]["value"]), "e2e_fp64": r(line["fp64"]["e2e"]["value"]),
+          "roofline_frac": r(line["roofline"]["frac"], 3)}
+    tc = line.get("tensor_core_modes") or {}
+    ns["tensor_core_sim_days_per_s"] = {k: r(v.get("value")) for k, v in tc.items()}
+    c1 = line.get("config1")
+    if c1:
+        ns["config1_barotropic_t42_fp64"] = {"sim_days_per_s": r(c1["sim_days_per_s"]),
+                                             "max_error_vs_oracle": r(c1.get("max_error_vs_oracle"), 2)}
+    c2 = line.get("config2")
+    if c2:
+        ns["config2_sw_t85"] = {p: {"sim_days_per_s": r(v["sim_days_per_s"]),
+                                    "max_error_vs_oracle": r(v.get("max_error_vs_oracle"), 2)}
+                                for p, v in c2.items() if isinstance(v, dict) and "sim_days_per_s" in v}
+    c4 = line.get("config4")
+    if c4:
+        ns["config4_ensemble_bf16x3"] = {"ensemble_sim_days_per_s": r(c4["ensemble_sim_days_per_s"]),
+                                         "days": c4["days"]}
+    adj = line.get("adjoint")
+    if adj:
+        ns["adjoint_ms_per_gradient"] = {"fp32": r(adj["fp32"]["ms_per_gradient"]),
+                                         "fp64": r(adj["fp64"]["ms_per_gradient"])}
+    return ns
+
+
+def config_legs(jgcm, configs, args):
+    """Configs 1, 2 and 4 on the GPU, then their errors against the FP64 oracle (the checker, run in
+    worker processes after the GPU work)."""
+    base = configs.BASE_SEED
+    out = {}
+    c1, f1 = one_layer_bench(jgcm, configs, "barotropic_t42", "rh4", "fp64", 480)
+    out["config1"] = dict(c1, workload="Barotropic T42 (128x64, 1 level), RH wave 4 + seeded noise, dt 1800 s, "
+                                       "480 steps (10 days), FP64")
+    c2 = {"workload": "Shallow water T85 (256x128), unstable jet + seeded bump, dt 600 s, 864 steps (6 days)"}
+    f2 = {}
+    for prec in ("fp32", "bf16x3"):
+        c2[prec], f2[prec] = one_layer_bench(jgcm, configs, "sw_t85", "jet", prec, 864)
+    out["config2"] = c2
+    c4, st4 = config4_bench(jgcm, configs, days=args.ensemble_days)
+    out["config4"] = c4
+    if args.no_oracle_checks:
+        return out
+    jobs = [("barotropic_t42", "rh4", base, 480), ("sw_t85", "jet", base, 864)]
+    for (name, e) in st4:
+        kind = configs.PARAMS[name]["kind"]
+        jobs.append((name, "hs" if kind == "held_suarez" else "jet", base + e,
+                     args.ensemble_days * configs.DAY // configs.PARAMS[name]["dt"]))
+    jobs.sort(key=lambda j: -j[3] * (20 if j[0] == "hs_t42l20" else 4 if j[0] == "hs_t21l20" else 1))
+    res = oracle_checks(jobs)
+    ref = res[("barotropic_t42", "rh4", base, 480)]["fields"]
+    e1 = field_errors(f1, ref, "barotropic")
+    out["config1"]["error_vs_oracle"] = e1
+    out["config1"]["max_error_vs_oracle"] = max(e1.values())
+    ref = res[("sw_t85", "jet", base, 864)]["fields"]
+    for prec in ("fp32", "bf16x3"):
+        e2 = field_errors(f2[prec], ref, "shallow_water")
+        c2[prec]["error_vs_oracle_day6"] = e2
+        c2[prec]["max_error_vs_oracle"] = max(e2.values())
+    errs = {}
+    for (name, e), (member, twin) in st4.items():
+        kind = configs.PARAMS[name]["kind"]
+        job = next(j for j in jobs if j[0] == name and j[2] == base + e)
+        ref = res[job]["fields"]
+        errs[f"{name}[{e}]"] = {"bf16x3_vs_oracle": field_errors(member, ref, kind),
+                               "fp64_gpu_vs_oracle": field_errors(twin, ref, kind),
+                               "bf16x3_vs_fp64_gpu": field_errors(member, twin, kind)}
+    c4["errors_after_days"] = {"days": args.ensemble_days, "members": errs}
+    out["oracle_check_seconds"] = {f"{j[0]}:{j[2]}": round(v["seconds"], 2) for j, v in res.items()}
+    return out
 
 
 def main():
@@ -528,6 +811,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble and tensor-core side runs")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the one-day gradient timing")
+    ap.add_argument("--no-configs", action="store_true", help="skip configs 1, 2 and 4 (barotropic T42, SW T85, "
+                                                              "the 30-day split-BF16 ensemble)")
+    ap.add_argument("--no-oracle-checks", action="store_true",
+                    help="configs 1, 2, 4 without their errors against the FP64 oracle")
+    ap.add_argument("--ensemble-days", type=int, default=30, help="simulated days per member of config 4")
     ap.add_argument("--profile", action="store_true",
                     help="only the mixed-precision headline model: --warmup then --steps sim-days with the tiles of "
                          "--tiles (no autotuning, no other model), a short launch sequence for ncu")

@@ -203,16 +203,10 @@ extern "C" int jgcm_trans_grid_to_spherical_adjoint(jgcm_mesh* m, const double* 
 
 extern "C" int jgcm_trans_grid_to_fourier(jgcm_mesh* m, const double* pfield, int nlev, double* fourier) {
   JG_TRY(check_nlev(m, nlev));
-  size_t ng = grid_elems(m, nlev), nf = 2 * (size_t)(m->N + 1) * m->nlat * nlev;
+  size_t ng = grid_elems(m, nlev), nf = 2 * ng;  // complex [nlev][nlat][nlon]: staging slots 1 and 2
   JG_TRY(h2d(m, slot(m, 0), pfield, ng));
   JG_TRY(grid_host_to_dev(m, slot(m, 0), m->d_grid[0], ng, m->stream));
-  FFTPlan fp;
-  memset(&fp, 0, sizeof(fp));
-  fp.ng = 1;
-  fp.C = nlev;
-  fp.g[0] = in_group(PRO_NONE, m->d_grid[0], nlev, 0);
-  JG_TRY(is_fp64(m) ? launch_fft_only<double>(m, fp, m->stream) : launch_fft_only<float>(m, fp, m->stream));
-  JG_TRY(fourier_dev_to_host(m, nlev, slot(m, 1), m->stream));
+  JG_TRY(fourier_full_to_host(m, m->d_grid[0], nlev, slot(m, 1), m->stream));
   JG_TRY(d2h(m, fourier, slot(m, 1), nf));
   return finish(m);
 }

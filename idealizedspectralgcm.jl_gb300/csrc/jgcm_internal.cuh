@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+#include <mutex>
 #include <string>
 #include <vector>
 #include <utility>
@@ -20,6 +22,7 @@
 
 #define JGCM_MAX_GROUPS 8
 #define JGCM_MAX_ND 64
+#define JGCM_MAX_DEVICES 64
 
 namespace jgcm {
 
@@ -62,6 +65,27 @@ void set_error(const char* fmt, ...);
       return JGCM_E_ARG;                \
     }                                   \
   } while (0)
+
+// One-time set-up that has to be repeated on every CUDA device: cudaFuncSetAttribute (the dynamic
+// shared-memory cap of a kernel) applies only to the device current when it is called.  run() calls
+// `f` once per device, with that device current; callers on several threads serialise on the mutex,
+// and a device already set up costs one atomic load.
+struct PerDeviceOnce {
+  std::atomic<bool> done[JGCM_MAX_DEVICES] = {};
+  std::mutex mu;
+  template <class F>
+  int run(F&& f) {
+    int dev = 0;
+    JG_CUDA(cudaGetDevice(&dev));
+    JG_ARG(dev >= 0 && dev < JGCM_MAX_DEVICES, "device index %d out of range", dev);
+    if (done[dev].load(std::memory_order_acquire)) return JGCM_OK;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done[dev].load(std::memory_order_relaxed)) return JGCM_OK;
+    JG_TRY(f());
+    done[dev].store(true, std::memory_order_release);
+    return JGCM_OK;
+  }
+};
 
 template <typename T>
 struct C2;
@@ -306,6 +330,8 @@ int spec_dev_to_host(jgcm_mesh* m, const void* d_native, double* d_host_layout, 
 int grid_host_to_dev(jgcm_mesh* m, const double* d_src, void* d_native, size_t n, cudaStream_t st);
 int grid_dev_to_host(jgcm_mesh* m, const void* d_native, double* d_dst, size_t n, cudaStream_t st);
 int fourier_dev_to_host(jgcm_mesh* m, int L, double* d_dst, cudaStream_t st);
+// all nλ modes of fft/nλ of L device grid levels, FP64 host layout [L][nlat][nlon] complex
+int fourier_full_to_host(jgcm_mesh* m, const void* d_grid, int L, double* d_dst, cudaStream_t st);
 int apply_laplacian(jgcm_mesh* m, void* d_spec, int L, cudaStream_t st);
 int area_mean(jgcm_mesh* m, const void* d_grid, double* d_out, cudaStream_t st);
 template <typename T>

@@ -674,16 +674,16 @@ int tc_tables_build(jgcm_mesh* m) {
   return JGCM_OK;
 }
 
-static int g_tc_smem_set[2] = {0, 0};
+static PerDeviceOnce g_tc_smem_set[2];  // [0] TF32x3, [1] BF16x3
 
 template <class P>
 static int tc_configure() {
   const int idx = sizeof(typename P::E) == 4 ? 0 : 1;
-  if (g_tc_smem_set[idx]) return JGCM_OK;
-  JG_CUDA(cudaFuncSetAttribute(tc::k_s2g_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget));
-  JG_CUDA(cudaFuncSetAttribute(tc::k_g2s_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget));
-  g_tc_smem_set[idx] = 1;
-  return JGCM_OK;
+  return g_tc_smem_set[idx].run([]() -> int {
+    JG_CUDA(cudaFuncSetAttribute(tc::k_s2g_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget));
+    JG_CUDA(cudaFuncSetAttribute(tc::k_g2s_tc<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget));
+    return JGCM_OK;
+  });
 }
 
 template <class P>
@@ -760,6 +760,9 @@ extern "C" int jgcm_selftest_bounded_wait(jgcm_mesh* m) {
   JG_ARG(m, "mesh is NULL");
   jgcm::tc::k_bounded_wait_selftest<<<1, 32, 0, m->stream>>>(m->d_status);
   JG_CUDA(cudaGetLastError());
+  // on a tensor-core mesh the give-up is reported the way an asynchronous call's is: by
+  // jgcm_mesh_synchronize
+  if (m->tc.on) return jgcm_mesh_synchronize(m);
   JG_CUDA(cudaStreamSynchronize(m->stream));
   return jgcm::tc_status(m);
 }

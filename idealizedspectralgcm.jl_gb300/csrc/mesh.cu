@@ -373,9 +373,13 @@ extern "C" int jgcm_mesh_destroy(jgcm_mesh* m) {
 
 extern "C" int jgcm_mesh_precision(const jgcm_mesh* m) { return m ? m->precision : JGCM_E_ARG; }
 
+// Also reports what the asynchronous entry points cannot: a tensor-core Legendre kernel whose bounded
+// wait gave up since the last check (its output is then not a transform; JGCM_E_CUDA with a message,
+// and the status is cleared).
 extern "C" int jgcm_mesh_synchronize(jgcm_mesh* m) {
   JG_ARG(m, "mesh is NULL");
   JG_CUDA(cudaStreamSynchronize(m->stream));
+  if (m->tc.on) JG_TRY(jgcm::tc_status(m));
   return JGCM_OK;
 }
 

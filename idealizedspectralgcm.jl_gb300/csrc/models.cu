@@ -2754,8 +2754,9 @@ extern "C" int jgcm_model_set_tuning(jgcm_model* md, const int* knobs, int n) {
 // Coordinate search over the knobs on a scratch copy of the model (its state is left untouched):
 // each candidate is timed with CUDA events over `nsteps` captured steps (after one untimed step
 // that captures the graphs); the fastest setting of each knob is kept before the next is tried.
-extern "C" int jgcm_model_autotune(jgcm_model* md, int nsteps, int* knobs_out, float* ms_out) {
+extern "C" int jgcm_model_autotune(jgcm_model* md, int nsteps, int* knobs_out, int n, float* ms_out) {
   JG_ARG(md && nsteps >= 1, "bad arguments");
+  JG_ARG(knobs_out == nullptr || n >= 4, "knobs_out holds %d ints, need at least 4", n);
   jgcm_mesh* m = md->mesh;
   jgcm_model* sc = nullptr;
   JG_TRY(jgcm_model_create_vert(m, &md->P, md->ne, md->vc.ak, md->vc.bk, &sc));
@@ -2804,7 +2805,7 @@ extern "C" int jgcm_model_autotune(jgcm_model* md, int nsteps, int* knobs_out, f
     }
   JG_TRY(jgcm_model_set_tuning(md, cur, 5));
   if (knobs_out)
-    for (int i = 0; i < 5; i++) knobs_out[i] = cur[i];
+    for (int i = 0; i < std::min(n, 5); i++) knobs_out[i] = cur[i];
   if (ms_out) *ms_out = best;
   return JGCM_OK;
 }

@@ -301,6 +301,60 @@ __global__ void __launch_bounds__(256) k_fft(FFTPlan plan, Tables<T> tb, V2<T>* 
   }
 }
 
+// Grid -> Fourier as Trans_Grid_To_Fourier! returns it (Spectral_Spherical_Mesh.jl:295-330): fft/nλ of
+// every row, all nλ modes, written straight into the FP64 host layout out[k][j][i] (complex
+// interleaved, i fastest: Julia's Array{ComplexF64,3}(nλ, nθ, L)).  Modes m < h as k_fft forms them,
+// the Nyquist mode X[h] = Re Z[0] - Im Z[0], and the modes above h by the Hermitian symmetry of a
+// real row, X[nλ - m] = conj X[m].  Same shared-memory transform and block shape as k_fft; this
+// serves the entry point only (the model steps read modes m <= N from k_fft and its variants).
+template <typename T>
+__global__ void __launch_bounds__(256) k_fourier_full(const T* __restrict__ grid, Tables<T> tb,
+                                                      double* __restrict__ out, int C, int nlat, int nlon,
+                                                      int logh, int CT) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int h = nlon >> 1;
+  T* re = (T*)smem;
+  T* im = re + CT * h;
+  T* tw = im + CT * h;
+  const int j = blockIdx.y;
+  const int cbase = blockIdx.x * CT;
+  for (int i = threadIdx.x; i < nlon; i += blockDim.x) tw[i] = tb.tw[i];
+  for (int i = threadIdx.x; i < CT * nlon; i += blockDim.x) {
+    int cc = i / nlon, t = i - cc * nlon, c = cbase + cc;
+    T x = c < C ? grid[((size_t)c * nlat + j) * nlon + t] : (T)0;
+    int pos = brev(t >> 1, logh);
+    if (t & 1)
+      im[cc * h + pos] = x;
+    else
+      re[cc * h + pos] = x;
+  }
+  __syncthreads();
+  fft_stages<T, -1>(re, im, tw, CT, h, logh);
+  const T scale = (T)0.5 / (T)nlon;  // nlon is a power of two: exact
+  for (int i = threadIdx.x; i < CT * nlon; i += blockDim.x) {
+    int cc = i / nlon, t = i - cc * nlon, c = cbase + cc;
+    if (c >= C) continue;
+    const int mm = t <= h ? t : nlon - t;
+    T xr, xi;
+    if (mm == h) {
+      xr = (re[cc * h] - im[cc * h]) * (scale + scale);
+      xi = 0;
+    } else {
+      int q = (h - mm) & (h - 1);
+      T zr = re[cc * h + mm], zi = im[cc * h + mm], qr = re[cc * h + q], qi = im[cc * h + q];
+      T er = zr + qr, ei = zi - qi;   // 2 E
+      T orr = zi + qi, oi = qr - zr;  // 2 O
+      T tc = tw[2 * mm], ts = tw[2 * mm + 1];
+      xr = (er + (tc * orr + ts * oi)) * scale;
+      xi = (ei + (tc * oi - ts * orr)) * scale;
+    }
+    if (t > h) xi = -xi;
+    const size_t o = (((size_t)c * nlat + j) * nlon + t) * 2;
+    out[o] = (double)xr;
+    out[o + 1] = (double)xi;
+  }
+}
+
 // ------------------------------------------------------------------------------------------
 // Warp-register FFTs (nlon = 64 V, V = 1..16): one warp per (column, latitude) row, the H = 32 V
 // complex points held V per lane (point i = lane + 32 r), radix-2 stages of half-size s >= 32
@@ -907,28 +961,29 @@ __global__ void __launch_bounds__(256) k_g2s_legendre(G2SPlan plan, Tables<T> tb
 }
 
 // ------------------------------------------------------------------------------------------
-static int g_smem_configured[2] = {0, 0};
+static PerDeviceOnce g_smem_configured[2];  // [0] FP32 kernels, [1] FP64 kernels
 
 template <typename T>
 static int configure_smem() {
-  int idx = sizeof(T) == 8 ? 1 : 0;
-  if (g_smem_configured[idx]) return JGCM_OK;
-  const int big = (int)kSmemBudget;
-  JG_CUDA(cudaFuncSetAttribute(k_s2g_legendre<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  JG_CUDA(cudaFuncSetAttribute(k_ifft<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  JG_CUDA(cudaFuncSetAttribute(k_fft<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  JG_CUDA(cudaFuncSetAttribute(k_g2s_legendre<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  JG_CUDA(cudaFuncSetAttribute(k_g2s_legendre<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  if (idx == 0) {
-    JG_CUDA(cudaFuncSetAttribute(k_fft_rows<64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    JG_CUDA(cudaFuncSetAttribute(k_fft_rows<64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    JG_CUDA(cudaFuncSetAttribute(k_fft_rows<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    JG_CUDA(cudaFuncSetAttribute(k_fft_rows<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    JG_CUDA(cudaFuncSetAttribute(k_ifft_rows<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-    JG_CUDA(cudaFuncSetAttribute(k_ifft_rows<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  }
-  g_smem_configured[idx] = 1;
-  return JGCM_OK;
+  const int idx = sizeof(T) == 8 ? 1 : 0;
+  return g_smem_configured[idx].run([idx]() -> int {
+    const int big = (int)kSmemBudget;
+    JG_CUDA(cudaFuncSetAttribute(k_s2g_legendre<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    JG_CUDA(cudaFuncSetAttribute(k_ifft<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    JG_CUDA(cudaFuncSetAttribute(k_fft<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    JG_CUDA(cudaFuncSetAttribute(k_fourier_full<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    JG_CUDA(cudaFuncSetAttribute(k_g2s_legendre<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    JG_CUDA(cudaFuncSetAttribute(k_g2s_legendre<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    if (idx == 0) {
+      JG_CUDA(cudaFuncSetAttribute(k_fft_rows<64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+      JG_CUDA(cudaFuncSetAttribute(k_fft_rows<64, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+      JG_CUDA(cudaFuncSetAttribute(k_fft_rows<128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+      JG_CUDA(cudaFuncSetAttribute(k_fft_rows<128, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+      JG_CUDA(cudaFuncSetAttribute(k_ifft_rows<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+      JG_CUDA(cudaFuncSetAttribute(k_ifft_rows<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+    }
+    return JGCM_OK;
+  });
 }
 
 // column tiles per block; a tuned value (jgcm_model_set_tuning / the autotuner) overrides the default
@@ -1253,6 +1308,26 @@ int fourier_dev_to_host(jgcm_mesh* m, int L, double* dst, cudaStream_t st) {
     k_fourier_d2h<double><<<nblk(n), 256, 0, st>>>((const double2*)m->d_fbuf, dst, m->N, m->nlat, L);
   else
     k_fourier_d2h<float><<<nblk(n), 256, 0, st>>>((const float2*)m->d_fbuf, dst, m->N, m->nlat, L);
+  JG_CUDA(cudaGetLastError());
+  return JGCM_OK;
+}
+
+// Trans_Grid_To_Fourier!: every mode of fft/nλ of the L device grid levels at d_grid, FP64 host layout.
+int fourier_full_to_host(jgcm_mesh* m, const void* d_grid, int L, double* d_dst, cudaStream_t st) {
+  const int fc = fft_ct(m);
+  const size_t sm = (size_t)(fc * m->nlon + m->nlon) * tsize(m);
+  JG_ARG(sm <= kSmemBudget, "FFT tile needs %zu bytes of shared memory", sm);
+  dim3 g((L + fc - 1) / fc, m->nlat);
+  if (is_fp64(m)) {
+    JG_TRY(configure_smem<double>());
+    k_fourier_full<double><<<g, 256, sm, st>>>((const double*)d_grid, tables<double>(m), d_dst, L, m->nlat,
+                                               m->nlon, m->logn - 1, fc);
+  } else {
+    JG_TRY(configure_smem<float>());
+    k_fourier_full<float><<<g, 256, sm, st>>>((const float*)d_grid, tables<float>(m), d_dst, L, m->nlat, m->nlon,
+                                              m->logn - 1, fc);
+  }
+  mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;
 }

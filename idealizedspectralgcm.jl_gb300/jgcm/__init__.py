@@ -97,7 +97,7 @@ def lib():
         "jgcm_model_read_diagnostics": (I, [P, C.c_char_p, P, Lg, C.POINTER(Lg), C.POINTER(Lg)]),
         "jgcm_model_get_tuning": (I, [P, C.POINTER(I), I]),
         "jgcm_model_set_tuning": (I, [P, C.POINTER(I), I]),
-        "jgcm_model_autotune": (I, [P, I, C.POINTER(I), C.POINTER(C.c_float)]),
+        "jgcm_model_autotune": (I, [P, I, C.POINTER(I), I, C.POINTER(C.c_float)]),
         "jgcm_ensemble_create": (I, [C.POINTER(P), I, I, PP]),
         "jgcm_ensemble_step": (I, [P, I]),
         "jgcm_ensemble_time": (I, [P, I, C.POINTER(C.c_float)]),
@@ -249,9 +249,11 @@ def Trans_Grid_To_Spherical_Adjoint(mesh, spec_bar, grid_bar):
 
 
 def Trans_Grid_To_Fourier(mesh, pfield, fourier):
-    """Spectral_Spherical_Mesh.jl:295-330.  ``fourier`` is complex128[N+1, nθ, nlev] (modes 0..N)."""
+    """Spectral_Spherical_Mesh.jl:295-330: ``fourier`` (complex128[nλ, nθ, nlev], the reference's
+    ``fourier_g``) receives fft(pfield, 1) / nλ, every mode."""
     n = _nlev_grid(mesh, pfield)
-    assert fourier.dtype == np.complex128 and fourier.shape == (mesh.num_fourier + 1, mesh.nlat, n)
+    assert fourier.dtype == np.complex128 and fourier.shape == (mesh.nlon, mesh.nlat, n)
+    assert fourier.flags.f_contiguous
     _check(lib().jgcm_trans_grid_to_fourier(mesh._h, _ptr(pfield), n, _ptr(fourier)))
 
 
@@ -630,7 +632,7 @@ def autotune(model, nsteps=24, cache=None):
         return table[key]
     k = (C.c_int * 5)()
     ms = C.c_float()
-    _check(lib().jgcm_model_autotune(model._h, int(nsteps), k, C.byref(ms)))
+    _check(lib().jgcm_model_autotune(model._h, int(nsteps), k, 5, C.byref(ms)))
     entry = {"tuning": dict(zip(TUNING_KNOBS, list(k))), "ms_per_step": float(ms.value) / nsteps}
     if cache:
         table[key] = entry

@@ -32,6 +32,9 @@ GRIDS = {
     "hs_t42l20": dict(num_fourier=42, nlat=64, nlon=128, nd=20, radius=6371000.0),
     "hs_t21l20": dict(num_fourier=21, nlat=32, nlon=64, nd=20, radius=6371000.0),
     "hs_t21l10": dict(num_fourier=21, nlat=32, nlon=64, nd=10, radius=6371000.0),
+    # the reference experiments' own grids (exp/Barotropic/Barotropic.jl:7-11, exp/Shallow_Water/SW.jl:7-12)
+    "barotropic_t85_ref": dict(num_fourier=85, nlat=128, nlon=256, nd=1, radius=6371.2e3),
+    "sw_t85_ref": dict(num_fourier=85, nlat=128, nlon=256, nd=1, radius=6371.0e3),
     # the level counts of Vert_Coordinate's fixed sigma tables (mcm: 14, v197: 18)
     "hs_t21l14": dict(num_fourier=21, nlat=32, nlon=64, nd=14, radius=6371000.0),
     "hs_t21l18": dict(num_fourier=21, nlat=32, nlon=64, nd=18, radius=6371000.0),
@@ -49,6 +52,11 @@ PARAMS = {
     "hs_t42l20": dict(_COMMON, kind="held_suarez", damping_coef=1.15741e-4, implicit_coef=0.5, dt=1200,
                       do_mass_correction=1, do_energy_correction=1),
 }
+# exp/Barotropic/Barotropic.jl:26-35 and exp/Shallow_Water/SW.jl:13-25,41-50 (h_0 = 3e4, friction and
+# thermal relaxation times 20 and 10 days)
+PARAMS["barotropic_t85_ref"] = dict(PARAMS["barotropic_t42"])
+PARAMS["sw_t85_ref"] = dict(_COMMON, kind="shallow_water", damping_coef=1.0e-4, implicit_coef=0.5, dt=1200,
+                            h0=3.0e4, kappa_m=1.0 / (20.0 * DAY), kappa_t=1.0 / (10.0 * DAY))
 PARAMS["hs_t21l20"] = dict(PARAMS["hs_t42l20"])
 PARAMS["hs_t21l10"] = dict(PARAMS["hs_t42l20"])
 PARAMS["hs_t21l14"] = dict(PARAMS["hs_t42l20"])
@@ -188,6 +196,69 @@ def init_shallow_water_jet(backend, mesh, model, seed=BASE_SEED, grav=9.80):
     model.set("grid_vor", gvor)
     model.set("grid_div", gdiv)
     model.set("grid_lnps", h)
+
+
+def init_barotropic_reference(backend, mesh, model):
+    """The reference barotropic experiment's initial state (exp/Barotropic/Barotropic.jl:43-62): the
+    zonal wind u = 25 cosθ - 30 cos³θ + 300 sin²θ cos⁶θ, v = 0, its vorticity and divergence (spectral
+    and on the grid), then an m = 4 vorticity bump A/2 cosθ exp(-((θ-θ0)/θw)²) cos(4λ) (A = 8e-5,
+    θ0 = 45°, θw = 15°) added on the grid and analysed back into the spectral vorticity.  As in the
+    reference, grid u, v keep the unperturbed wind and every other field starts at zero."""
+    cos, sin = mesh.costh, mesh.sinth
+    lat, lon = mesh.latc, mesh.lonc
+    u = mesh.grid(1)
+    u[:, :, 0] = (25.0 * cos - 30.0 * cos ** 3 + 300.0 * sin ** 2 * cos ** 6)[None, :]
+    v = mesh.grid(1)
+    vor, div = mesh.spectral(1), mesh.spectral(1)
+    backend.Vor_Div_From_Grid_UV(mesh, u, v, vor, div)
+    gvor, gdiv = mesh.grid(1), mesh.grid(1)
+    backend.Trans_Spherical_To_Grid(mesh, vor, gvor)
+    backend.Trans_Spherical_To_Grid(mesh, div, gdiv)
+    m, th0, thw, A = 4.0, 45.0 * math.pi / 180.0, 15.0 * math.pi / 180.0, 8.0e-5
+    gvor[:, :, 0] += (A / 2.0 * cos[None, :] * np.exp(-((lat[None, :] - th0) / thw) ** 2)
+                      * np.cos(m * lon[:, None]))
+    backend.Trans_Grid_To_Spherical(mesh, gvor, vor)
+    model.set("grid_u_c", u)
+    model.set("grid_v_c", v)
+    model.set("spe_vor_c", vor)
+    model.set("grid_vor", gvor)
+    return vor
+
+
+def sw_reference_h_eq(mesh, h_0=3.0e4, h_amp=2.0e4, h_lon=math.pi / 2, h_lat=25.0 * math.pi / 180.0,
+                      h_width=15.0 * math.pi / 180.0, h_itcz=1.0e5, itcz_width=4.0 * math.pi / 180.0):
+    """The relaxation height of the reference shallow-water experiment (exp/Shallow_Water/SW.jl:69-80):
+    h_0 + a Gaussian mound at (90°E, 25°N) + an equatorial ITCZ ridge, [nλ, nθ, 1]."""
+    lat, lon = mesh.latc, mesh.lonc
+    d2 = (lat / itcz_width) ** 2
+    x2 = ((lon[:, None] - h_lon) / (2.0 * h_width)) ** 2
+    y2 = ((lat[None, :] - h_lat) / h_width) ** 2
+    return np.asfortranarray((h_0 + h_amp * np.exp(-(x2 + y2)) + h_itcz * np.exp(-d2)[None, :])[:, :, None])
+
+
+def init_shallow_water_reference(backend, mesh, model, h_0=3.0e4):
+    """The reference shallow-water experiment's initial state (exp/Shallow_Water/SW.jl:57-80): at rest,
+    h = h_0 seeded into grid_lnps and analysed into spe_lnps_c, h_eq for Shallow_Water_Physics!.  The
+    dynamics read h from grid_ps_c, which stays zero (and spe_lnps_p stays zero), so the first step
+    sees h = 0 on the grid: the reference's own quirk, kept."""
+    u, v = mesh.grid(1), mesh.grid(1)
+    vor, div = mesh.spectral(1), mesh.spectral(1)
+    backend.Vor_Div_From_Grid_UV(mesh, u, v, vor, div)
+    gvor, gdiv = mesh.grid(1), mesh.grid(1)
+    backend.Trans_Spherical_To_Grid(mesh, vor, gvor)
+    backend.Trans_Spherical_To_Grid(mesh, div, gdiv)
+    gh = np.asfortranarray(np.full((mesh.nlon, mesh.nlat, 1), h_0))
+    sh = mesh.spectral(1)
+    backend.Trans_Grid_To_Spherical(mesh, gh, sh)
+    model.set("grid_u_c", u)
+    model.set("grid_v_c", v)
+    model.set("spe_vor_c", vor)
+    model.set("spe_div_c", div)
+    model.set("grid_vor", gvor)
+    model.set("grid_div", gdiv)
+    model.set("grid_lnps", gh)
+    model.set("spe_lnps_c", sh)
+    model.set("grid_h_eq", sw_reference_h_eq(mesh, h_0=h_0))
 
 
 def hs_temperature_noise(mesh, seed=BASE_SEED, amplitude=0.1):

@@ -4,7 +4,7 @@
  * Drop-in for the Atmos_Spectral hot path of CliMA/IdealizedSpectralGCM.jl (module JGCM).
  * Every entry point below replaces one Julia method of the reference; the comment above
  * each cites the file:line of the method it replaces.  A Julia host binds these with
- * `ccall` (the shim is shown in INTEGRATION.md); the tests bind them with ctypes.
+ * `ccall`; the tests bind them with ctypes.
  *
  * Conventions
  *  - Every function returns an int status: JGCM_OK (0) or a negative JGCM_E_* code.
@@ -66,7 +66,10 @@ int jgcm_mesh_precision(const jgcm_mesh* mesh);
  * "epsilon","coef_uvm","coef_uvc","coef_uvp","coef_dlam","coef_dthm","coef_dthp",
  * "laplacian_eig" ([N+2][N+1]).  Writes *count = element count; out may be NULL to query. */
 int jgcm_mesh_table(jgcm_mesh* mesh, const char* name, double* out, long cap, long* count);
-/* Block until all work queued on the mesh stream is done. */
+/* Block until all work queued on the mesh stream is done.  On a tensor-core mesh (JGCM_TF32X3,
+ * JGCM_BF16X3) it also reports a Legendre kernel whose bounded wait gave up since the last check
+ * (JGCM_E_CUDA, message in jgcm_last_error; the status is cleared): the only report the
+ * asynchronous entry points (jgcm_trans_spherical_to_grid_noalloc) give of that failure. */
 int jgcm_mesh_synchronize(jgcm_mesh* mesh);
 
 /* Trans_Spherical_To_Grid!  Spectral_Spherical_Mesh.jl:143-217 */
@@ -81,8 +84,10 @@ int jgcm_trans_grid_to_spherical(jgcm_mesh* mesh, const double* pfield, int nlev
  * spectral cotangent (m >= 1 halved, row N+1 dropped) and scales each latitude by w_j / (2 nlon). */
 int jgcm_trans_spherical_to_grid_adjoint(jgcm_mesh* mesh, const double* grid_bar, int nlev, double* spec_bar);
 int jgcm_trans_grid_to_spherical_adjoint(jgcm_mesh* mesh, const double* spec_bar, int nlev, double* grid_bar);
-/* Trans_Grid_To_Fourier!  Spectral_Spherical_Mesh.jl:295-330; writes fourier modes m = 0..N
- * of fft/nλ as complex double[nlev][nlat][N+1] (modes above N are not used downstream). */
+/* Trans_Grid_To_Fourier!  Spectral_Spherical_Mesh.jl:295-330; fourier is the reference's
+ * fourier_g, Array{ComplexF64,3}(nλ, nθ, nlev): fft(pfield, 1) / nλ, every mode m = 0..nλ-1
+ * (complex double[nlev][nlat][nlon], re/im interleaved, m fastest; modes above nλ/2 are the complex
+ * conjugates of modes nλ - m, as for any real row). */
 int jgcm_trans_grid_to_fourier(jgcm_mesh* mesh, const double* pfield, int nlev, double* fourier);
 /* Vor_Div_From_Grid_UV!  Spectral_Spherical_Mesh.jl:349-393 (+ Compute_Alpha_Operator! :424-459) */
 int jgcm_vor_div_from_grid_uv(jgcm_mesh* mesh, const double* grid_u, const double* grid_v, int nlev,
@@ -114,7 +119,10 @@ int jgcm_area_weighted_global_mean(jgcm_mesh* mesh, const double* grid, double* 
  * (N+1) * nlat * nlev complex values must fit: larger sizes return JGCM_E_ARG with a message.
  * The first call on a device resolves that array's address (set-up), so make it before any
  * stream capture.  All calls share the array: calls that overlap on the GPU (different streams,
- * meshes or threads without ordering) race; nothing in it needs clearing between calls. */
+ * meshes or threads without ordering) race.  A successful call writes every scratch element it
+ * reads, so nothing needs clearing between calls.  On a tensor-core mesh a Legendre kernel whose
+ * bounded wait gave up leaves the scratch (and so d_grid) stale; the call, being asynchronous,
+ * cannot say so: jgcm_mesh_synchronize on the mesh reports it. */
 int jgcm_trans_spherical_to_grid_noalloc(jgcm_mesh* mesh, const void* d_snm, int nlev, void* d_grid,
                                          void* stream);
 
@@ -216,11 +224,11 @@ int jgcm_model_read_diagnostics(jgcm_model* model, const char* name, double* out
  * nlon 64 or 128 one per thread whatever their number (by default from 19456 rows on: nlon 64, and the inverse at nlon 128).  knobs[4] (read and written when
  * n >= 5): the Legendre engine of a tensor-core precision mode (0 tcgen05, 1 the FP32 SIMT
  * kernels; the mesh).  The autotuner times candidates on a scratch copy of the model (coordinate
- * search, nsteps captured steps each), applies the fastest and returns it (knobs[5]) with its time
- * per nsteps. */
+ * search, nsteps captured steps each), applies the fastest, writes it to knobs (nullable; the first
+ * min(n, 5) knobs, n >= 4, like jgcm_model_get_tuning) and its time per nsteps to ms (nullable). */
 int jgcm_model_get_tuning(jgcm_model* model, int* knobs, int n);
 int jgcm_model_set_tuning(jgcm_model* model, const int* knobs, int n);
-int jgcm_model_autotune(jgcm_model* model, int nsteps, int* knobs, float* ms);
+int jgcm_model_autotune(jgcm_model* model, int nsteps, int* knobs, int n, float* ms);
 /* Uneven ensembles (no counterpart in the reference): several (member-batched) models of
  * different truncations or kinds advanced together, window_seconds of simulated time per window,
  * each window one graph launch whose branches step the models concurrently (window_seconds a

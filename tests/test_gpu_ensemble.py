@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 from jgcm import configs
+from test_gpu_models import MIXED_TOL, _compare
 
 pytestmark = pytest.mark.gpu
 
@@ -87,12 +88,7 @@ def test_large_fp32_ensemble_matches_oracle(jg, orc, name, members):
     out = jg.Model(gm, params)
     for e, omod in refs.items():
         out.copy_member(0, ens, e)
-        for f in configs.PROGNOSTIC["held_suarez"]:
-            den = np.linalg.norm(omod.get(f).ravel())
-            if f.startswith("spe_div") or f == "grid_div":
-                den = max(den, np.linalg.norm(omod.get(f.replace("div", "vor")).ravel()))
-            err = float(np.linalg.norm((out.get(f) - omod.get(f)).ravel()) / den)
-            assert err < 1e-3, (e, f, err)
+        _compare(out, omod, "held_suarez", MIXED_TOL["fp32"])
 
 
 def test_ensemble_rejects_direct_field_access(jg):
@@ -186,6 +182,14 @@ def test_autotuner_keeps_results_and_caches(jg, tmp_path):
             assert configs.rel_l2(x.get(f), y.get(f)) < 1e-10, (e, f)
     with pytest.raises(AssertionError):
         jg.set_tuning(a, {"lanes_per_column": 3})
+    # the C ABI writes no more knobs than the caller's buffer holds (n = 4 of the 5)
+    import ctypes as C
+    buf = (C.c_int * 6)(*([-7] * 6))
+    ms = C.c_float()
+    assert jg.lib().jgcm_model_autotune(a._h, 2, buf, 4, C.byref(ms)) == 0
+    assert list(buf)[4:] == [-7, -7] and ms.value > 0
+    assert list(buf)[:4] == [jg.get_tuning(a)[k] for k in jg.TUNING_KNOBS[:4]]
+    assert jg.lib().jgcm_model_autotune(a._h, 2, buf, 3, C.byref(ms)) == -1  # fewer than 4: refused
 
 
 @pytest.mark.gpu

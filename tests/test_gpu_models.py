@@ -2,8 +2,9 @@
 
 The GPU model is loaded with the oracle's state (copy_state), both advance the same steps,
 and every prognostic field is compared by relative L2.  Tolerances: FP64 path 1e-10 after a
-few steps (summation order differs; HS's chaotic growth is slow over a few steps), FP32 path
-5e-5.  The barotropic T42 workload runs its full 480 steps (10 days) in FP64.
+few steps (summation order differs; HS's chaotic growth is slow over a few steps); the one-layer
+models' FP32 path 5e-5; Held-Suarez's mixed modes per field (MIXED_TOL).  The barotropic T42
+workload runs its full 480 steps (10 days) in FP64.
 """
 import numpy as np
 import pytest
@@ -21,21 +22,36 @@ def _pair(jg, orc, name, prec):
 
 
 # divergence can be pure roundoff (a resting or non-divergent start), so its error is measured
-# against the scale of the companion vorticity field
-_SCALE = {"spe_div_c": "spe_vor_c", "spe_div_p": "spe_vor_p", "grid_div": "grid_vor"}
+# against the scale of the companion vorticity field; a wind component's against the wind (u, v)
+_SCALE = {"spe_div_c": ("spe_vor_c",), "spe_div_p": ("spe_vor_p",), "grid_div": ("grid_vor",),
+          "grid_u_c": ("grid_u_c", "grid_v_c"), "grid_v_c": ("grid_u_c", "grid_v_c")}
+
+# Per-field step tolerances of the mixed modes after a few steps from a developed flow (relative L2).
+# Thermodynamic fields (T, ln ps / ps, the shallow-water height) are transformed and stepped with no
+# cancellation and stay near FP32 rounding (measured <= 1e-6); the dynamics (vorticity, divergence,
+# winds) carry the FP32 conditioning of the divergence tendency, a Laplacian of an energy whose
+# dynamically active part is ~1e-3 of its size (measured <= 5e-5).  BF16x3 splits each operand into
+# two 8-bit-mantissa halves (~16 bits kept, against FP32's 24), so its bounds are wider.
+_THERMO = ("spe_t_c", "spe_t_p", "grid_t_c", "grid_t_p", "spe_lnps_c", "grid_ps_c", "grid_ps_p")
+MIXED_TOL = {"fp32": {"default": 2e-4, **{f: 5e-6 for f in _THERMO}},
+             "tf32x3": {"default": 2e-4, **{f: 5e-6 for f in _THERMO}},
+             "bf16x3": {"default": 5e-4, **{f: 2e-5 for f in _THERMO}}}
 
 
 def _compare(gmod, omod, kind, tol):
+    """Relative L2 error of every prognostic field; `tol` is a bound for all of them or a dict of
+    per-field bounds with a "default"."""
     errs = {}
     for f in configs.PROGNOSTIC[kind]:
         a, b = gmod.get(f), omod.get(f)
         den = np.linalg.norm(b.ravel())
         if f in _SCALE:
-            den = max(den, np.linalg.norm(omod.get(_SCALE[f]).ravel()))
+            den = max(den, np.sqrt(sum(np.linalg.norm(omod.get(g).ravel()) ** 2 for g in _SCALE[f])))
         errs[f] = float(np.linalg.norm((a - b).ravel()) / (den if den > 0 else 1.0))
     print(kind, {k: f"{v:.2e}" for k, v in errs.items()})
-    bad = {k: v for k, v in errs.items() if not v < tol}
-    assert not bad, f"fields above {tol}: {bad}"
+    bound = (lambda f: tol.get(f, tol["default"])) if isinstance(tol, dict) else (lambda f: tol)
+    bad = {k: (v, bound(k)) for k, v in errs.items() if not v < bound(k)}
+    assert not bad, f"fields above their bounds (error, bound): {bad}"
     return errs
 
 
@@ -97,22 +113,23 @@ def _hs_developed(jg, orc, name, prec):
 
 
 @pytest.mark.parametrize("name,prec,tol", [("hs_t21l10", "fp64", 1e-10), ("hs_t42l20", "fp64", 1e-10),
-                                           ("hs_t21l10", "fp32", 1e-3), ("hs_t42l20", "fp32", 1e-3)])
+                                           ("hs_t21l10", "fp32", MIXED_TOL["fp32"]),
+                                           ("hs_t42l20", "fp32", MIXED_TOL["fp32"])])
 def test_held_suarez_steps(jg, orc, name, prec, tol):
-    """FP32 tolerance: the divergence tendency is the Laplacian of an energy field of ~1e5 m^2/s^2
-    whose dynamically active part is ~1e2, so FP32 storage bounds the divergence (and the divergent
-    wind) near 1e-4 relative per step; vorticity, T and ps stay near 1e-6 (printed by _compare)."""
+    """FP32 tolerances (MIXED_TOL): the divergence tendency is the Laplacian of an energy field of
+    ~1e5 m^2/s^2 whose dynamically active part is ~1e2, so FP32 bounds the divergence (and the
+    divergent wind) near 1e-5..1e-4 relative; T and ps stay near 1e-7 (printed by _compare)."""
     gm, om, gmod, omod = _hs_developed(jg, orc, name, prec)
     for n in (1, 1, 2):
         gmod.step(n)
         omod.step(n)
         _compare(gmod, omod, "held_suarez", tol)
     for f in ("grid_t_eq", "grid_p_full", "grid_p_half", "grid_z_full"):
-        assert configs.rel_l2(gmod.get(f), omod.get(f)) < tol, f
+        assert configs.rel_l2(gmod.get(f), omod.get(f)) < (tol if prec == "fp64" else 1e-5), f
 
 
 @pytest.mark.parametrize("name,option", configs.VERT_COORD_CASES)
-@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("fp32", 1e-3)])
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("fp32", MIXED_TOL["fp32"])])
 def test_held_suarez_vert_coords(jg, orc, name, option, prec, tol):
     """Held-Suarez on Vert_Coordinate's other sigma options (mcm, v197, uneven_sigma): the
     semi-implicit matrices and the steps from a developed state equal the oracle's."""
@@ -131,7 +148,7 @@ def test_held_suarez_vert_coords(jg, orc, name, option, prec, tol):
         omod.step(n)
         _compare(gmod, omod, "held_suarez", tol)
     for f in ("grid_t_eq", "grid_p_full", "grid_p_half"):
-        assert configs.rel_l2(gmod.get(f), omod.get(f)) < tol, f
+        assert configs.rel_l2(gmod.get(f), omod.get(f)) < (tol if prec == "fp64" else 1e-5), f
 
 
 def test_held_suarez_refuses_hybrid_coordinates(jg):
