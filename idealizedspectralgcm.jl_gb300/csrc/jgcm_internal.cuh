@@ -131,7 +131,9 @@ struct TableStore {
 // Transform plans.  A launch processes a batch of columns; each group maps a contiguous
 // column range [col0, col0+L) to one field (one column per level).
 // S2G_ADJ_G2S: input of the adjoint of the analysis (m >= 1 halved, row N+1 dropped)
-enum S2GOp { S2G_PLAIN = 0, S2G_DLAM = 1, S2G_DTH = 2, S2G_UCOS = 3, S2G_VCOS = 4, S2G_ADJ_G2S = 5 };
+// S2G_ANOM: the field without the real part of its (0,0) mode (P_00 = 1: each level's anomaly about
+// its area mean), so its FP32 rounding scales with the anomaly, not with the mean
+enum S2GOp { S2G_PLAIN = 0, S2G_DLAM = 1, S2G_DTH = 2, S2G_UCOS = 3, S2G_VCOS = 4, S2G_ADJ_G2S = 5, S2G_ANOM = 6 };
 // A plan scalar in the kernel's precision: FP64 fields keep the host's values and FP32 kernels read
 // the FP32 copies the launchers fill in (every FP64 -> FP32 conversion, like every FP64 operation,
 // runs on the FP64 pipe, at 1/64 of the FP32 rate on this part).

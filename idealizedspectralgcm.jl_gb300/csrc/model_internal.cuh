@@ -55,6 +55,8 @@ struct jgcm_model {
   // tendencies and scratch
   void *spe_dvor, *spe_ddiv, *spe_dlnps, *spe_dt;
   void *g_dlps, *g_dtps, *g_dlT, *g_dtT, *g_ducos, *g_dvcos, *g_dt, *g_energy, *g_dlnps, *g_diag;
+  void* g_tdev;  // FP32 path: the temperature of the level the next column kernel reads, less its level
+                 // means (synthesised from spectral T without its (0,0) modes; written with the gradients)
   void *coriolis, *damping;  // [nlat], [m][n] in T
   void* dfac[2];             // [m][n] in T: 1/(1 + Δt d) (init step), 1/(1 + 2Δt d) (afterwards)
   // FP64 semi-implicit data

@@ -154,6 +154,7 @@ template <typename T>
 struct HSColArgs {
   const T *u_p, *v_p, *t_p, *ps_p, *ps_c, *u_c, *v_c, *t_c, *div, *vor, *dlps, *dtps, *dlT, *dtT, *geopots, *coriolis,
       *sinj, *cosj;
+  const T* tdev;  // T_c less its level means, synthesised as such (FP32 path); NULL: T_c - T0_k here
   T *ducos, *dvcos, *dtg, *energy, *dlnps, *t_eq;
   const V2<T>* t_spec;  // spe_t_c: its (0,0) modes are the level means of T
   const double* wts;
@@ -266,15 +267,20 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
   // ---- pass 1: Compute_Geopotential! (Press_And_Geopot.jl:71-111) on T - T0_k with T0_k the level's
   // area mean (spectral mode (0,0)): the T0 part is a per-level constant (dlnp_r, r >= 1, and dlnp_p
   // do not vary horizontally), so it only moves the (0,0) mode of the energy, which the Laplacian
-  // annihilates, while the rounding of the sum shrinks with |T - T0|.  Also the column sum of the
-  // mass divergence D_k.
+  // annihilates, while the rounding of the sum shrinks with |T - T0|.  On the FP32 path T - T0_k is
+  // read as synthesised without the (0,0) modes (a.tdev): T itself, stored in FP32 at ~264 K, keeps
+  // only ~3e-5 K of it, and that rounding, through the Laplacian of the energy, set the divergence's
+  // error (day-1 u, v errors against the FP64 oracle 8e-5, 5e-4 with T_c - T0_k formed here).  Also
+  // the column sum of the mass divergence D_k.
+  const T* __restrict__ tdev = a.tdev ? a.tdev + cL : nullptr;
   T termS = 0, dmeanS = 0;
   if (act)
     for (int k = k0; k < k1; k++) {
       const size_t x = (size_t)k * G;
-      const T t = t_c[x], u = u_c[x], v = v_c[x], dvg = dvgp[x];
+      const T u = u_c[x], v = v_c[x], dvg = dvgp[x];
+      const T td = tdev ? tdev[x] : t_c[x] - (T)a.t_spec[e * nd + k].x;
       const T dlnp = k == 0 ? s_lb1 + lnps : s_dlp[k];
-      termS += R * (t - (T)a.t_spec[e * nd + k].x) * dlnp;
+      termS += R * td * dlnp;
       dmeanS += dvg * (s_dak[k] + s_dbk[k] * ps) + s_dbk[k] * (u * dlps + v * dtps);
     }
   const T tot = seg_sum<S>(dmeanS);
@@ -283,11 +289,11 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
   if (act)
     for (int k = k1 - 1; k >= k0; k--) {  // the energy Φ + |u|^2/2, bottom-up within the segment
       const size_t x = (size_t)k * G;
-      const T t = t_c[x], u = u_c[x], v = v_c[x];
-      const T tdev = t - (T)a.t_spec[e * nd + k].x;
+      const T u = u_c[x], v = v_c[x];
+      const T td = tdev ? tdev[x] : t_c[x] - (T)a.t_spec[e * nd + k].x;
       const T dlnp = k == 0 ? s_lb1 + lnps : s_dlp[k];
-      a.energy[cL + x] = gs + rs + R * tdev * s_dlpp[k] + (T)0.5 * (u * u + v * v);
-      rs += R * tdev * dlnp;
+      a.energy[cL + x] = gs + rs + R * td * s_dlpp[k] + (T)0.5 * (u * u + v * v);
+      rs += R * td * dlnp;
     }
   // ---- pass 2, top-down within the segment
   T col_e = 0;
@@ -1105,7 +1111,7 @@ void model_free(jgcm_model* md) {
   void* ps[] = {md->grid_vor, md->grid_div, md->grid_lnps, md->grid_t_eq, md->grid_geopots, md->grid_h_eq,
                 md->spe_zero, md->spe_dvor, md->spe_ddiv, md->spe_dlnps, md->spe_dt, md->g_dlps, md->g_dtps,
                 md->g_dlT, md->g_dtT, md->g_ducos, md->g_dvcos, md->g_dt, md->g_energy, md->g_dlnps, md->g_diag,
-                md->coriolis, md->damping, md->dfac[0], md->dfac[1], md->d_W, md->d_pairs, md->d_partials,
+                md->g_tdev, md->coriolis, md->damping, md->dfac[0], md->dfac[1], md->d_W, md->d_pairs, md->d_partials,
                 md->d_scalars, md->d_counter, md->d_vc, md->fbuf, md->diag};
   for (auto p : ps)
     if (p) cudaFree(p);
@@ -1175,7 +1181,7 @@ int model_alloc(jgcm_model* md) {
     JG_TRY(alloc(&md->grid_t[i], G));
   }
   void** gnd[] = {&md->grid_vor, &md->grid_div, &md->grid_t_eq, &md->g_dlT, &md->g_dtT, &md->g_ducos, &md->g_dvcos,
-                  &md->g_dt, &md->g_energy};
+                  &md->g_dt, &md->g_energy, &md->g_tdev};
   for (auto p : gnd) JG_TRY(alloc(p, G));
   void** g1[] = {&md->grid_lnps, &md->grid_geopots, &md->grid_h_eq, &md->g_dlps, &md->g_dtps, &md->g_dlnps};
   for (auto p : g1) JG_TRY(alloc(p, G1));
@@ -1453,20 +1459,24 @@ int issue_hs_grad(jgcm_model* md, int lev, cudaStream_t st) {
   const int L = md->L, E = md->ne;
   S2GPlan sp;
   memset(&sp, 0, sizeof(sp));
-  sp.ng = 4;
-  sp.C = 2 * E + 2 * L;
+  // FP32: also T less its level means for the next column kernel's geopotential (S2G_ANOM)
+  const bool anom = std::is_same<T, float>::value;
+  sp.ng = anom ? 5 : 4;
+  sp.C = 2 * E + (anom ? 3 : 2) * L;
   sp.g[0] = sg(S2G_DLAM, md->spe_lnps[lev], nullptr, E, 0);
   sp.g[1] = sg(S2G_DTH, md->spe_lnps[lev], nullptr, E, E);
   sp.g[2] = sg(S2G_DLAM, md->spe_t[lev], nullptr, L, 2 * E);
   sp.g[3] = sg(S2G_DTH, md->spe_t[lev], nullptr, L, 2 * E + L);
+  if (anom) sp.g[4] = sg(S2G_ANOM, md->spe_t[lev], nullptr, L, 2 * E + 2 * L);
   IFFTPlan ip;
   memset(&ip, 0, sizeof(ip));
-  ip.ng = 4;
-  ip.C = 2 * E + 2 * L;
+  ip.ng = sp.ng;
+  ip.C = sp.C;
   ip.g[0] = og(EPI_DIVCOS, md->g_dlps, E, 0);
   ip.g[1] = og(EPI_DIVCOS, md->g_dtps, E, E);
   ip.g[2] = og(EPI_DIVCOS, md->g_dlT, L, 2 * E);
   ip.g[3] = og(EPI_DIVCOS, md->g_dtT, L, 2 * E + L);
+  if (anom) ip.g[4] = og(EPI_NONE, md->g_tdev, L, 2 * E + 2 * L);
   return launch_s2g<T>(md->mesh, sp, ip, st, md->fbuf, md->fcap);
 }
 
@@ -1490,6 +1500,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   a.u_c = (const T*)md->grid_u[c];
   a.v_c = (const T*)md->grid_v[c];
   a.t_c = (const T*)md->grid_t[c];
+  a.tdev = std::is_same<T, float>::value ? (const T*)md->g_tdev : nullptr;
   a.div = (const T*)md->grid_div;
   a.vor = (const T*)md->grid_vor;
   a.dlps = (const T*)md->g_dlps;
@@ -2295,6 +2306,39 @@ extern "C" int jgcm_hs_forcing(jgcm_model* md, int Dt, const double* grid_u, con
 }
 
 // Spectral_Initialize_Fields! (Spectral_Dynamics.jl:372-449) on the device.
+namespace {
+// The mixed precisions form the initial state in FP64 (a scratch FP64 mesh and one-member model of
+// the same grid, coordinate and parameters) and round it into the model: an FP32 analysis of the
+// isothermal 264 K temperature and of ln ps (~11.5) leaves their FP32 rounding (~1e-5 K) in every
+// n > 0 mode, where the reference's state holds only the seeded perturbation (0.1 K noise, so a
+// 1e-4 relative error before the first step).
+int initialize_fields_fp64(jgcm_model* md, const double* grid_t_pert, int vorticity_seed) {
+  jgcm_mesh* m = md->mesh;
+  jgcm_mesh* m64 = nullptr;
+  JG_TRY(jgcm_mesh_create(m->N, m->ns, m->nlat, m->nlon, m->nd, m->radius, JGCM_FP64, &m64));
+  jgcm_model* t64 = nullptr;
+  int st = jgcm_model_create_vert(m64, &md->P, 1, md->vc.ak, md->vc.bk, &t64);
+  static const char* names[] = {"grid_t_c", "grid_t_p", "grid_lnps", "grid_ps_c", "grid_ps_p", "spe_vor_c",
+                                "spe_vor_p", "spe_div_c", "spe_div_p", "spe_t_c", "spe_t_p", "spe_lnps_c",
+                                "spe_lnps_p", "grid_u_c", "grid_u_p", "grid_v_c", "grid_v_p", "grid_vor", "grid_div"};
+  std::vector<double> buf;
+  auto move = [&](jgcm_model* dst, jgcm_model* src, const char* nm) -> int {
+    long cnt = 0;
+    JG_TRY(jgcm_model_get_field(src, nm, nullptr, 0, &cnt));
+    buf.resize((size_t)cnt);
+    JG_TRY(jgcm_model_get_field(src, nm, buf.data(), cnt, &cnt));
+    return jgcm_model_set_field(dst, nm, buf.data(), cnt);
+  };
+  if (st == JGCM_OK) st = move(t64, md, "grid_geopots");  // the surface geopotential the init reads
+  if (st == JGCM_OK) st = jgcm_spectral_initialize_fields(t64, grid_t_pert, vorticity_seed);
+  for (const char* nm : names)
+    if (st == JGCM_OK) st = move(md, t64, nm);
+  if (t64) jgcm_model_destroy(t64);
+  jgcm_mesh_destroy(m64);
+  return st;
+}
+}  // namespace
+
 extern "C" int jgcm_spectral_initialize_fields(jgcm_model* md, const double* grid_t_pert, int vorticity_seed) {
   JG_ARG(md, "NULL model");
   JG_ARG(md->ne == 1, "initialise one-member models and copy them into the ensemble (jgcm_model_copy_member)");
@@ -2302,6 +2346,7 @@ extern "C" int jgcm_spectral_initialize_fields(jgcm_model* md, const double* gri
   const int nd = md->nd, N = m->N, ns = m->ns;
   const size_t G = grid_elems(m, 1);
   JG_ARG(N >= 5 && ns >= 9 || !vorticity_seed, "the vorticity seed needs num_fourier >= 5");
+  if (!is_fp64(m)) return initialize_fields_fp64(md, grid_t_pert, vorticity_seed);
   // host-side grid fields (FP64), uploaded through set_field
   std::vector<double> gt(G * nd), geo(G), lnps(G), ps(G), spv(2 * spec_elems(m, nd), 0.0);
   long cnt = 0;

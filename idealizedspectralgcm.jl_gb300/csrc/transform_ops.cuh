@@ -62,6 +62,10 @@ __device__ __forceinline__ V2<T> s2g_input(const S2GGroup& g, const Tables<T>& t
       x = a[(mrow + n) * L + k];
       if (m == 0 && n == 0) x.x = x.x - pick<T>(g.shift, g.shiftf);
       break;
+    case S2G_ANOM:
+      x = a[(mrow + n) * L + k];
+      if (m == 0 && n == 0) x.x = 0;
+      break;
     case S2G_ADJ_G2S:  // the synthesis weights every m >= 1 twice; the analysis never sees row N+1
       if (n < ns) {
         x = a[(mrow + n) * L + k];

@@ -44,6 +44,16 @@ void om_set_threads(int n) { g_threads = n; }
 
 static double* zalloc(size_t n) { return (double*)calloc(n ? n : 1, sizeof(double)); }
 
+/* FP32 emulation switches (jgcm_oracle.h); 0 = the FP64 restatement of the reference */
+static int g_f32 = 0;
+void om_set_f32(int mask) { g_f32 = mask; }
+static inline double r32(double x) { return (double)(float)x; }
+/* a + b c rounded once to float: b, c are floats, so their product is exact in double */
+static inline double fma32(double a, double b, double c) { return r32(a + r32(b) * r32(c)); }
+static void r32_arr(double* a, size_t n) {
+  for (size_t i = 0; i < n; i++) a[i] = r32(a[i]);
+}
+
 #define TIX(m, n, j) ((size_t)(m) + (size_t)(N + 1) * ((size_t)(n) + (size_t)(ns + 1) * (size_t)(j)))
 #define SIX(m, n, k) (2 * ((size_t)(m) + (size_t)(N + 1) * ((size_t)(n) + (size_t)(ns + 1) * (size_t)(k))))
 #define GIX(i, j, k) ((size_t)(i) + (size_t)nlon * ((size_t)(j) + (size_t)nlat * (size_t)(k)))
@@ -124,8 +134,13 @@ int om_compute_legendre(int N, int ns, const double* sinth, int nlat, double* qn
 /* ------------------------------------------------------------------------------------------ */
 /* FFT (stand-in for FFTW.jl fft/ifft, unpinned third-party boundary): radix-2 for powers of  */
 /* two, plain DFT otherwise.  sign=-1 forward (fft), +1 backward (unnormalised ifft).         */
+static void fft_inplace_f32(const om_mesh* M, double* re, double* im, int sign);
 static void fft_inplace(const om_mesh* M, double* re, double* im, int sign) {
   int n = M->nlon;
+  if (M->pow2 && (g_f32 & (sign < 0 ? OM_F32_FFT_FWD : OM_F32_FFT_INV))) {
+    fft_inplace_f32(M, re, im, sign);
+    return;
+  }
   if (M->pow2) {
     for (int i = 0; i < n; i++) {
       int r = M->bitrev[i];
@@ -166,6 +181,36 @@ static void fft_inplace(const om_mesh* M, double* re, double* im, int sign) {
     free(ore);
     free(oim);
   }
+}
+
+/* The radix-2 FFT above in FP32 arithmetic (FP32 emulation, not the reference's FP64). */
+static void fft_inplace_f32(const om_mesh* M, double* re, double* im, int sign) {
+  int n = M->nlon;
+  float* a = (float*)calloc((size_t)n, sizeof(float));
+  float* b = (float*)calloc((size_t)n, sizeof(float));
+  for (int i = 0; i < n; i++) {
+    a[M->bitrev[i]] = (float)re[i];
+    b[M->bitrev[i]] = (float)im[i];
+  }
+  for (int len = 2; len <= n; len <<= 1) {
+    int half = len >> 1, step = n / len;
+    for (int i = 0; i < n; i += len)
+      for (int k = 0; k < half; k++) {
+        float wr = (float)M->tw[2 * (k * step)], wi = (float)(sign * M->tw[2 * (k * step) + 1]);
+        float xr = a[i + k + half], xi = b[i + k + half];
+        float tr = xr * wr - xi * wi, ti = xr * wi + xi * wr;
+        a[i + k + half] = a[i + k] - tr;
+        b[i + k + half] = b[i + k] - ti;
+        a[i + k] = a[i + k] + tr;
+        b[i + k] = b[i + k] + ti;
+      }
+  }
+  for (int i = 0; i < n; i++) {
+    re[i] = a[i];
+    im[i] = b[i];
+  }
+  free(a);
+  free(b);
 }
 
 /* ------------------------------------------------------------------------------------------ */
@@ -298,8 +343,13 @@ void om_trans_spherical_to_grid(om_mesh* M, const double* snm, int nlev, double*
         for (int j = 0; j < nh; j++) {
           double q = M->qnm[TIX(m, n, j)];
           double* d = &s[2 * ((size_t)(off + j) + (size_t)nlat * k)];
-          d[0] = d[0] + q * sr;
-          d[1] = d[1] + q * si;
+          if (g_f32 & OM_F32_SYNTHESIS) {
+            d[0] = fma32(d[0], q, sr);
+            d[1] = fma32(d[1], q, si);
+          } else {
+            d[0] = d[0] + q * sr;
+            d[1] = d[1] + q * si;
+          }
         }
       }
     }
@@ -311,6 +361,10 @@ void om_trans_spherical_to_grid(om_mesh* M, const double* snm, int nlev, double*
         (&FG(m, j, k))[1] = e[1] + o[1];
         (&FG(m, nlat - 1 - j, k))[0] = e[0] - o[0];
         (&FG(m, nlat - 1 - j, k))[1] = e[1] - o[1];
+        if (g_f32 & OM_F32_SYNTHESIS) {
+          r32_arr(&FG(m, j, k), 2);
+          r32_arr(&FG(m, nlat - 1 - j, k), 2);
+        }
       }
     free(s);
   }
@@ -332,6 +386,8 @@ void om_trans_spherical_to_grid(om_mesh* M, const double* snm, int nlev, double*
     }
     fft_inplace(M, re, im, +1);
     for (int i = 0; i < nlon; i++) pfield[GIX(i, j, k)] = 2.0 * nlon * (re[i] / nlon);
+    if (g_f32 & OM_F32_FFT_INV)
+      for (int i = 0; i < nlon; i++) pfield[GIX(i, j, k)] = r32(pfield[GIX(i, j, k)]);
     free(re);
     free(im);
   }
@@ -355,6 +411,8 @@ void om_trans_grid_to_fourier(om_mesh* M, const double* pfield, int nlev, double
       fourier[2 * GIX(i, j, k)] = re[i] / nlon;
       fourier[2 * GIX(i, j, k) + 1] = im[i] / nlon;
     }
+    if (g_f32 & OM_F32_FFT_FWD)
+      for (int i = 0; i < nlon; i++) r32_arr(&fourier[2 * GIX(i, j, k)], 2);
     free(re);
     free(im);
   }
@@ -379,8 +437,13 @@ void om_trans_grid_to_spherical(om_mesh* M, const double* pfield, int nlev, doub
           double q = M->qwg[TIX(m, n, j)];
           double cr = even ? a[0] + b[0] : a[0] - b[0];
           double ci = even ? a[1] + b[1] : a[1] - b[1];
-          sr = sr + cr * q;
-          si = si + ci * q;
+          if (g_f32 & OM_F32_ANALYSIS) {
+            sr = fma32(sr, r32(cr), q);
+            si = fma32(si, r32(ci), q);
+          } else {
+            sr = sr + cr * q;
+            si = si + ci * q;
+          }
         }
         snm[SIX(m, n, k)] = sr / 2.0;
         snm[SIX(m, n, k) + 1] = si / 2.0;
@@ -407,13 +470,21 @@ static void alpha_operator(om_mesh* M, const double* fa, const double* fb, doubl
           const double* B = &fb[2 * GIX(m, j, k)];
           double ca = M->coef_alp_a[TIX(m, n, j)], cb = M->coef_alp_b[TIX(m, n, j)];
           /* (imag(A') + real(A') im) = i*A  */
-          ar = ar + (-A[1]) * ca;
-          ai = ai + A[0] * ca;
-          br = br + B[0] * cb;
-          bi = bi + B[1] * cb;
+          if (g_f32 & OM_F32_ANALYSIS) {
+            ar = fma32(ar, -A[1], ca);
+            ai = fma32(ai, A[0], ca);
+            br = fma32(br, B[0], cb);
+            bi = fma32(bi, B[1], cb);
+          } else {
+            ar = ar + (-A[1]) * ca;
+            ai = ai + A[0] * ca;
+            br = br + B[0] * cb;
+            bi = bi + B[1] * cb;
+          }
         }
         alpha[SIX(m, n, k)] = c * (ar + isign * br);
         alpha[SIX(m, n, k) + 1] = c * (ai + isign * bi);
+        if (g_f32 & OM_F32_ANALYSIS) r32_arr(&alpha[SIX(m, n, k)], 2);
       }
 }
 

@@ -43,6 +43,25 @@ void om_mesh_destroy(om_mesh* m);
  * "coef_dthm","coef_dthp","laplacian_eig"); returns element count or -1 */
 long om_mesh_table(const om_mesh* m, const char* name, double* out, long cap);
 void om_set_threads(int nthreads);
+/* FP32 emulation for error bisection (all off by default: the oracle is FP64).  Each bit runs one
+ * stage of the mixed-precision GPU path in FP32 arithmetic (every operation rounded to float, the
+ * Legendre sums as fused multiply-adds) or rounds one stage's outputs to float:
+ *   1 forward FFT, 2 analysis Legendre sums (grid->spectral, alpha operator), 4 synthesis Legendre
+ *   sums (spectral->grid), 8 inverse FFT, 16 Held-Suarez grid stage (the column computations'
+ *   outputs: tendencies and the energy field, and the grid state), 32 Held-Suarez spectral stage
+ *   (the analysed tendencies and the state after the semi-implicit leapfrog).  With any bit set the
+ *   energy field is analysed relative to each level's first point, as the GPU sums its geopotential
+ *   on T - T0_k (a per-level constant the Laplacian annihilates). */
+#define OM_F32_FFT_FWD 1
+#define OM_F32_ANALYSIS 2
+#define OM_F32_SYNTHESIS 4
+#define OM_F32_FFT_INV 8
+#define OM_F32_GRID 16
+#define OM_F32_SPECTRAL 32
+/* 64: the geopotential reads the temperature synthesised without its (0,0) modes, with the level
+ * constants added back exactly (the GPU's FP32 formulation), instead of grid T (stored in FP32) */
+#define OM_F32_TANOM 64
+void om_set_f32(int mask);
 
 /* Spectral_Spherical_Mesh.jl transforms; nlev = third dimension (nd or 1) */
 void om_trans_spherical_to_grid(om_mesh* m, const double* snm, int nlev, double* grid);

@@ -57,6 +57,7 @@ def lib():
             "om_mesh_destroy": (None, [P]),
             "om_mesh_table": (L, [P, C.c_char_p, P, L]),
             "om_set_threads": (None, [I]),
+            "om_set_f32": (None, [I]),
             "om_trans_spherical_to_grid": (None, [P, P, I, P]),
             "om_trans_grid_to_spherical": (None, [P, P, I, P]),
             "om_trans_grid_to_fourier": (None, [P, P, I, P]),
@@ -96,6 +97,15 @@ def lib():
 
 def set_threads(n: int) -> None:
     lib().om_set_threads(int(n))
+
+
+# FP32 emulation switches for error bisection (jgcm_oracle.h); 0 = the FP64 restatement
+F32_STAGES = {"fft_fwd": 1, "analysis": 2, "synthesis": 4, "fft_inv": 8, "grid": 16, "spectral": 32}
+F32_TANOM = 64  # the geopotential on T synthesised without its level means (the GPU's FP32 formulation)
+
+
+def set_f32(mask: int) -> None:
+    lib().om_set_f32(int(mask))
 
 
 def _ptr(a: np.ndarray):

@@ -10,7 +10,7 @@ and prints, per checkpoint day, the relative L2 difference of every prognostic g
 (T, u, v, ps) and of the zonal means of T and u (a climatological measure that stays meaningful
 after the flow becomes chaotic).  Writes one JSON document to stdout (and to --out if given).
 
-  python tests/error_growth.py --days 1 10 100 [--out results.json] [--threads N]
+  python tests/measure/error_growth.py --days 1 10 100 [--out results.json] [--threads N]
 """
 from __future__ import annotations
 
@@ -20,7 +20,7 @@ import os
 import sys
 import time
 
-ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path[:0] = [os.path.join(ROOT, "idealizedspectralgcm.jl_gb300"), os.path.join(ROOT, "oracle"), ROOT]
 
 import numpy as np  # noqa: E402

@@ -16,8 +16,8 @@ Reported:
   * the mixed-precision (FP32) gradient against the FP64 gradient;
   * wall-clock of one gradient (forward sweep + loss + reverse sweep with recomputation).
 
-  python tests/hs_adjoint_config.py [--steps 72] [--checkpoint 8] [--no-oracle] [--out adj.json]
-  python tests/hs_adjoint_config.py --profile fp32 --steps 8      (two gradients only, for ncu)
+  python tests/measure/hs_adjoint_config.py [--steps 72] [--checkpoint 8] [--no-oracle] [--out adj.json]
+  python tests/measure/hs_adjoint_config.py --profile fp32 --steps 8      (two gradients only, for ncu)
 """
 from __future__ import annotations
 
@@ -27,7 +27,7 @@ import os
 import sys
 import time
 
-ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path[:0] = [os.path.join(ROOT, "idealizedspectralgcm.jl_gb300"), os.path.join(ROOT, "oracle"), ROOT]
 
 import numpy as np  # noqa: E402

@@ -9,7 +9,7 @@ in the mixed (FP32) and FP64 paths, and reports the features the reference's fig
 zonal-mean jet maximum and where it sits, the near-surface equatorial temperature and the
 equatorial tropopause minimum, plus the relative L2 difference between the two paths' climatologies.
 
-  python tests/hs_climatology.py [--days 1200] [--spinup 200] [--out clim.json]
+  python tests/measure/hs_climatology.py [--days 1200] [--spinup 200] [--out clim.json]
 """
 from __future__ import annotations
 
@@ -19,7 +19,7 @@ import os
 import sys
 import time
 
-ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path[:0] = [os.path.join(ROOT, "idealizedspectralgcm.jl_gb300"), ROOT]
 
 import numpy as np  # noqa: E402
