@@ -195,6 +195,15 @@ def algorithmic_bytes(name: str, N: int, nlat: int, nlon: int, nd: int, esize: i
     return float(table[name])
 
 
+def step_roofline(kt, N, nlat, nlon, nd, esize, s_per_step, peak):
+    """The whole model step against the HBM roofline: the algorithmic bytes of its launches (one of
+    each kernel of the step, the table of algorithmic_bytes) per measured step time."""
+    alg = sum(algorithmic_bytes(k, N, nlat, nlon, nd, esize) for k in kt)
+    ach = alg / s_per_step / 1e9
+    return {"algorithmic_bytes": alg, "ms_per_step": 1e3 * s_per_step, "achieved": ach, "unit": "GB/s",
+            "frac": ach / peak}
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -717,7 +726,8 @@ def run_jgcm(args):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "algorithmic_bytes": alg,
                      "launch_ms": kt[dom], "traffic": profile_traffic(dom),
-                     "step_kernels_ms": {k: round(v, 5) for k, v in kt.items()}},
+                     "step_kernels_ms": {k: round(v, 5) for k, v in kt.items()},
+                     "whole_step": step_roofline(kt, N, nlat, nlon, nd, esize, t_mx / (K * spd), peak)},
         "cpu_baseline": base,
         "e2e": {"value": world * ne2e / t_e2e, "unit": "sim-days/s", "h2d_bytes_per_step": bytes_io,
                 "d2h_bytes_per_step": bytes_io},
@@ -738,7 +748,8 @@ def north_star_summary(line):
           "speedup_vs_fp64": r(line["speedup_vs_fp64"], 3),
           "error_vs_fp64": {k: r(v, 2) for k, v in line["error_vs_fp64"].items()},
           "e2e_mixed": r(line["e2e"]["value"]), "e2e_fp64": r(line["fp64"]["e2e"]["value"]),
-          "roofline_frac": r(line["roofline"]["frac"], 3)}
+          "roofline_frac": r(line["roofline"]["frac"], 3),
+          "whole_step_roofline_frac": r(line["roofline"]["whole_step"]["frac"], 3)}
     tc = line.get("tensor_core_modes") or {}
     ns["tensor_core_sim_days_per_s"] = {k: r(v.get("value")) for k, v in tc.items()}
     c1 = line.get("config1")

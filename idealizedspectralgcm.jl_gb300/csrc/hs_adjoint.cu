@@ -1076,6 +1076,8 @@ int check_model(jgcm_model* md) {
   JG_ARG(md->ne == 1, "one-member models only");
   JG_ARG(md->nd <= 32, "the column adjoint holds one level per lane: nd <= 32");
   JG_ARG(!md->diag_on, "switch the on-device diagnostics off before differentiating");
+  // the reverse column kernel reads the sigma coordinates' per-level log-pressure constants
+  JG_ARG(!md->vc.hybrid, "the step adjoint is built for sigma coordinates (a_k = 0), not hybrid ones");
   return JGCM_OK;
 }
 

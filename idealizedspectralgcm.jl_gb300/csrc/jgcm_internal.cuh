@@ -161,11 +161,13 @@ struct S2GPlan {
 };
 
 // EPI_ADJ_G2S: x w_j / (2 nlon), the output scaling of the adjoint of the analysis
-enum GridEpi { EPI_NONE = 0, EPI_DIVCOS = 1, EPI_EXP2 = 2, EPI_DIVCOS_MULPS = 3, EPI_ADJ_G2S = 4 };
+// EPI_ANOM: x synthesised from an S2G_ANOM group (the field less its level means): dst = x + the level
+// mean (the real part of the group's spectral (0,0) mode, P_00 = 1), dst2 = x
+enum GridEpi { EPI_NONE = 0, EPI_DIVCOS = 1, EPI_EXP2 = 2, EPI_DIVCOS_MULPS = 3, EPI_ADJ_G2S = 4, EPI_ANOM = 5 };
 struct GridOutGroup {
   void* dst;
-  void* dst2;      // EPI_EXP2: exp(x)
-  const void* ps;  // EPI_DIVCOS_MULPS: surface pressure grid [nlat][nlon]
+  void* dst2;      // EPI_EXP2: exp(x); EPI_ANOM: x
+  const void* ps;  // EPI_DIVCOS_MULPS: surface pressure grid [nlat][nlon]; EPI_ANOM: the spectral field
   double shift;    // EPI_EXP2: x is ln(ps) - shift: dst = x + shift, dst2 = exp(x) exp(shift)
   double eshift;   // exp(shift)
   float shiftf, eshiftf;

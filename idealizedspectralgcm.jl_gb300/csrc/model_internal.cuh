@@ -14,6 +14,7 @@ struct VertCoef {  // Vert_Coordinate (even_sigma) and the semi-implicit referen
   // sigma coordinates (a_k = 0): with p = b ps, ln p_{k+1/2} = lb[k+1] + ln ps and
   // ln p_k = cf[k] + ln ps (Simmons-Burridge, Press_And_Geopot.jl:46-60, zero top), so every
   // log-pressure difference is a per-level constant and p_k = sf[k] ps
+  int hybrid;                  // some a_k != 0: the log pressures vary per column (the sigma tables below unused)
   double lb[JGCM_MAX_ND + 1];  // ln b_k (k >= 1)
   double cf[JGCM_MAX_ND];      // ln p_k - ln ps
   double sf[JGCM_MAX_ND];      // exp(cf) = p_k / ps
@@ -34,8 +35,8 @@ struct jgcm_model {
   int fcap;
   int hs_lanes;  // lanes per column of the Held-Suarez column kernel (1, 2 or 4)
   int graph_gen;  // the mesh's tile generation the captured graphs were built with
-  // sigma half-level coefficients b_k given at creation (Vert_Coordinate's bk); empty = even_sigma
-  std::vector<double> vert_bk;
+  // half-level coefficients a_k, b_k given at creation (Vert_Coordinate's ak, bk); empty = even_sigma
+  std::vector<double> vert_ak, vert_bk;
   // Held-Suarez: the gradients of ln ps and T of the current level are already in g_dlps ...
   // g_dtT (computed at the end of the previous step, concurrently with the fixers)
   int grad_ready;

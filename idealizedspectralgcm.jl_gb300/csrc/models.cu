@@ -155,6 +155,7 @@ struct HSColArgs {
   const T *u_p, *v_p, *t_p, *ps_p, *ps_c, *u_c, *v_c, *t_c, *div, *vor, *dlps, *dtps, *dlT, *dtT, *geopots, *coriolis,
       *sinj, *cosj;
   const T* tdev;  // T_c less its level means, synthesised as such (FP32 path); NULL: T_c - T0_k here
+  int has_dak;    // some a_k differs between levels (hybrid coordinates): the energy sums need sum_k T_k Δa_k
   T *ducos, *dvcos, *dtg, *energy, *dlnps, *t_eq;
   const V2<T>* t_spec;  // spe_t_c: its (0,0) modes are the level means of T
   const double* wts;
@@ -217,7 +218,12 @@ __device__ __forceinline__ R seg_excl_suffix(R x, int s) {  // sum over the lane
 
 // FP32: at most 72 registers (14 blocks of 64 threads per SM): at ensemble scale the kernel streams
 // and its time follows occupancy (at 77 registers, allocated as 80, 12 blocks: 97 -> 109 us, measured)
-template <typename T, int S>
+// HYB (hybrid coordinates, a_k != 0): the log pressures of Pressure_Variables! (Press_And_Geopot.jl:
+// 36-67, Simmons-Burridge, zero top) are formed per column and level from p_{k+1/2} = a_k + b_k ps:
+// D_k = ln(p_{k+1/2} / p_{k-1/2}) = log1p(Δp_k / p_{k-1/2}) (no difference of two large logarithms),
+// ln p_{k+1/2} - ln p_k = 1 - p_{k-1/2} D_k / Δp_k, ln p_k - ln p_{k-1/2} = D_k - that; the top level
+// has ln p_1 = ln p_{3/2} - 1.  Sigma coordinates read the same quantities as per-level constants.
+template <typename T, int S, bool HYB>
 __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HSColArgs<T> a, const VertCoef* __restrict__ vcp) {
   const VertCoef& vc = *vcp;
   __shared__ double red[2][HS_CT / 32];
@@ -227,10 +233,15 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
   __shared__ T s_dak[JGCM_MAX_ND], s_dbk[JGCM_MAX_ND], s_bk[JGCM_MAX_ND + 1], s_cf[JGCM_MAX_ND],
       s_dlpp[JGCM_MAX_ND], s_dlpm[JGCM_MAX_ND], s_dlp[JGCM_MAX_ND], s_sf[JGCM_MAX_ND];
   __shared__ T s_lb1;
+  __shared__ T s_ak[JGCM_MAX_ND + 1];  // hybrid coordinates: a_k in the state precision
+  __shared__ double s_dak64[JGCM_MAX_ND], s_dbk64[JGCM_MAX_ND];  // FP64 layer coefficients: the energy integral
   const int nd = a.nd, nlon = a.nlon, nlat = a.nlat;
   for (int q = threadIdx.x; q <= nd; q += blockDim.x) {
     s_bk[q] = (T)vc.bk[q];
+    s_ak[q] = (T)vc.ak[q];
     if (q < nd) {
+      s_dak64[q] = vc.dak[q];
+      s_dbk64[q] = vc.dbk[q];
       s_dak[q] = (T)vc.dak[q];
       s_dbk[q] = (T)vc.dbk[q];
       s_cf[q] = (T)vc.cf[q];
@@ -264,6 +275,30 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
   const T gs = act ? a.geopots[c1] : (T)0;
   // ---- pressure variables from ps_c (Pressure_Variables!, Press_And_Geopot.jl:36-67)
   const T lnps = log(ps);
+  // the level's log-pressure differences: dlnp = ln p_{k+1/2} - ln p_{k-1/2} (k = 0: ln p_{3/2}),
+  // dlpp = ln p_{k+1/2} - ln p_k, dlpm = ln p_k - ln p_{k-1/2} (k = 0: ln p_1), lnpf = ln p_k
+  auto logs = [&](int k, T& dlnp, T& dlpp, T& dlpm, T& lnpf) {
+    if constexpr (HYB) {
+      const T plo = s_ak[k] + s_bk[k] * ps, phi = s_ak[k + 1] + s_bk[k + 1] * ps, dpk = phi - plo;
+      const T lph = log(phi);
+      if (k == 0) {
+        dlnp = lph;
+        dlpp = (T)1;
+        lnpf = lph - (T)1;
+        dlpm = lnpf;
+      } else {
+        dlnp = log1p(dpk / plo);
+        dlpp = (T)1 - plo * dlnp / dpk;
+        dlpm = dlnp - dlpp;
+        lnpf = lph - dlpp;
+      }
+    } else {
+      dlnp = k == 0 ? s_lb1 + lnps : s_dlp[k];
+      dlpp = s_dlpp[k];
+      lnpf = s_cf[k] + lnps;
+      dlpm = k == 0 ? lnpf : s_dlpm[k];
+    }
+  };
   // ---- pass 1: Compute_Geopotential! (Press_And_Geopot.jl:71-111) on T - T0_k with T0_k the level's
   // area mean (spectral mode (0,0)): the T0 part is a per-level constant (dlnp_r, r >= 1, and dlnp_p
   // do not vary horizontally), so it only moves the (0,0) mode of the energy, which the Laplacian
@@ -272,31 +307,50 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
   // only ~3e-5 K of it, and that rounding, through the Laplacian of the energy, set the divergence's
   // error (day-1 u, v errors against the FP64 oracle 8e-5, 5e-4 with T_c - T0_k formed here).  Also
   // the column sum of the mass divergence D_k.
+  // Hybrid coordinates: dlnp_k and dlpp_k follow ps, so the T0 part is no per-level constant there;
+  // it is summed on its own (rs0) and added back, keeping the anomaly sum's conditioning.
   const T* __restrict__ tdev = a.tdev ? a.tdev + cL : nullptr;
-  T termS = 0, dmeanS = 0;
+  T termS = 0, term0S = 0, dmeanS = 0;
   if (act)
     for (int k = k0; k < k1; k++) {
       const size_t x = (size_t)k * G;
       const T u = u_c[x], v = v_c[x], dvg = dvgp[x];
-      const T td = tdev ? tdev[x] : t_c[x] - (T)a.t_spec[e * nd + k].x;
-      const T dlnp = k == 0 ? s_lb1 + lnps : s_dlp[k];
+      const T t0 = (T)a.t_spec[e * nd + k].x;
+      const T td = tdev ? tdev[x] : t_c[x] - t0;
+      T dlnp, dlpp, dlpm, lnpf;
+      logs(k, dlnp, dlpp, dlpm, lnpf);
       termS += R * td * dlnp;
+      if constexpr (HYB) term0S += R * t0 * dlnp;
       dmeanS += dvg * (s_dak[k] + s_dbk[k] * ps) + s_dbk[k] * (u * dlps + v * dtps);
     }
   const T tot = seg_sum<S>(dmeanS);
   T rs = seg_excl_suffix<S>(termS, seg);  // sum_{r >= k1} R (T_r - T0_r) dlnp_r
+  T rs0 = (T)0;
+  if constexpr (HYB) rs0 = seg_excl_suffix<S>(term0S, seg);  // sum_{r >= k1} R T0_r dlnp_r
   const T incl0 = seg_excl_prefix<S>(dmeanS, seg);  // sum_{r < k0} D_r
   if (act)
     for (int k = k1 - 1; k >= k0; k--) {  // the energy Φ + |u|^2/2, bottom-up within the segment
       const size_t x = (size_t)k * G;
       const T u = u_c[x], v = v_c[x];
-      const T td = tdev ? tdev[x] : t_c[x] - (T)a.t_spec[e * nd + k].x;
-      const T dlnp = k == 0 ? s_lb1 + lnps : s_dlp[k];
-      a.energy[cL + x] = gs + rs + R * td * s_dlpp[k] + (T)0.5 * (u * u + v * v);
+      const T t0 = (T)a.t_spec[e * nd + k].x;
+      const T td = tdev ? tdev[x] : t_c[x] - t0;
+      T dlnp, dlpp, dlpm, lnpf;
+      logs(k, dlnp, dlpp, dlpm, lnpf);
+      T en = gs + rs + R * td * dlpp + (T)0.5 * (u * u + v * v);
+      if constexpr (HYB) {
+        en += rs0 + R * t0 * dlpp;
+        rs0 += R * t0 * dlnp;
+      }
+      a.energy[cL + x] = en;
       rs += R * td * dlnp;
     }
   // ---- pass 2, top-down within the segment
+  // the column's energy integral (Compute_Corrections_Init): its kinetic part in the state precision,
+  // its c_p T part (~99 % of it) as FP64 sums of the exact products T_k Δa_k and T_k Δb_k (on the FP32
+  // path the state precision's rounding of c_p T, the same at nearly every point of a near-uniform
+  // temperature, biased the energy correction by up to 1e-6 K per step)
   T col_e = 0;
+  double col_ta = 0, col_tb = 0;
   if (act && k0 < k1) {
     T incl = incl0, Mlo = 0, flu = 0, flv = 0, flt = 0;  // M and the advective fluxes at k0-1/2
     T u = u_c[(size_t)k0 * G], v = v_c[(size_t)k0 * G], t = t_c[(size_t)k0 * G];
@@ -323,12 +377,12 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
         dp1 = s_dak[k + 1] + s_dbk[k + 1] * ps;
       }
       const T rdp = (T)1 / dp;
-      const T lnpf = s_cf[k] + lnps;
-      const T dlnp_p = s_dlpp[k];                 // ln p_{k+1/2} - ln p_k
-      const T dlnp_m = k == 0 ? lnpf : s_dlpm[k];  // ln p_k - ln p_{k-1/2} (ln p_{1/2} = 0)
-      const T dlnp = k == 0 ? s_lb1 + lnps : s_dlp[k];
-      // HS_Forcing! on the previous level (sigma = p_k / ps = sf[k])
-      const T sg = s_sf[k] - sb;
+      T dlnp, dlnp_p, dlnp_m, lnpf;  // ln p_{k+1/2} - ln p_k, ln p_k - ln p_{k-1/2} (ln p_{1/2} = 0)
+      logs(k, dlnp, dlnp_p, dlnp_m, lnpf);
+      // HS_Forcing! on the previous level (sigma = p_k / ps: sf[k] in sigma coordinates)
+      T sg;
+      if constexpr (HYB) sg = exp(lnpf) / ps - sb;
+      else sg = s_sf[k] - sb;
       const T smax = sg > (T)0 ? sg : (T)0;
       const T k_v = kv0 * smax;
       T du = -k_v * up, dv = -k_v * vp;
@@ -337,10 +391,14 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
       T teq = ((T)315.0 - a.dTy * s2 - a.dthz * c2 * lpn) * exp(a.kappa_t * lpn);
       teq = teq > (T)200.0 ? teq : (T)200.0;
       dt = dt - (ka + kt0 * smax * c4) * (tp - teq);
-      // Compute_Corrections_Init: column energy integral with ps_p in the state precision
+      // Compute_Corrections_Init: column energy integral with ps_p
       {
         const T ua = up + tDt * du, va = vp + tDt * dv;
-        col_e += ((T)0.5 * (ua * ua + va * va) + cp * (tp + tDt * dt)) * (s_dak[k] + s_dbk[k] * psp);
+        const T te = tp + tDt * dt;
+        col_e += ((T)0.5 * (ua * ua + va * va)) * (s_dak[k] + s_dbk[k] * psp);
+        const double ted = (double)te;
+        if (a.has_dak) col_ta += ted * s_dak64[k];
+        col_tb += ted * s_dbk64[k];
       }
       // Four_In_One! (Spectral_Dynamics.jl:88-183)
       const T x1 = (s_bk[k] * dlnp_m + s_bk[k + 1] * dlnp_p) * rdp;
@@ -381,12 +439,13 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
       dp = dp1;
     }
   }
-  col_e = seg_sum<S>(col_e);
+  double col_ed = (double)col_e + a.cp * (col_ta + col_tb * (double)psp);
+  col_ed = seg_sum<S>(col_ed);
   double accp = 0.0, acce = 0.0;
   if (act && seg == 0) {
     a.dlnps[c1] = (-tot) / ps;  // grid_δlnps = grid_δps / ps (Spectral_Dynamics.jl:279)
     accp = (double)psp;
-    acce = (double)col_e;
+    acce = col_ed;
   }
   // ---- block partials for mean_ps_p and mean_energy_p (fixed order), then the member's fold;
   // only lanes with seg = 0 hold values, so the butterfly stops at offset S (the skipped levels
@@ -426,15 +485,20 @@ inline int hs_lanes(const jgcm_mesh* m, int ne, int nd) {
   return S;
 }
 
-template <typename T>
-int launch_hs_column(const HSColArgs<T>& a, const jgcm_mesh* m, int ne, int S, const VertCoef* vc, cudaStream_t st) {
+template <typename T, bool HYB>
+int launch_hs_column_v(const HSColArgs<T>& a, const jgcm_mesh* m, int ne, int S, const VertCoef* vc, cudaStream_t st) {
   const int cpb = HS_CT / S;  // columns per block
   dim3 g((m->nlon + cpb - 1) / cpb, m->nlat, ne);
-  if (S == 1) JG_CUDA(launch_pdl(k_hs_column<T, 1>, g, HS_CT, 0, st, a, vc));
-  else if (S == 2) JG_CUDA(launch_pdl(k_hs_column<T, 2>, g, HS_CT, 0, st, a, vc));
-  else if (S == 4) JG_CUDA(launch_pdl(k_hs_column<T, 4>, g, HS_CT, 0, st, a, vc));
-  else JG_CUDA(launch_pdl(k_hs_column<T, 8>, g, HS_CT, 0, st, a, vc));
+  if (S == 1) JG_CUDA(launch_pdl(k_hs_column<T, 1, HYB>, g, HS_CT, 0, st, a, vc));
+  else if (S == 2) JG_CUDA(launch_pdl(k_hs_column<T, 2, HYB>, g, HS_CT, 0, st, a, vc));
+  else if (S == 4) JG_CUDA(launch_pdl(k_hs_column<T, 4, HYB>, g, HS_CT, 0, st, a, vc));
+  else JG_CUDA(launch_pdl(k_hs_column<T, 8, HYB>, g, HS_CT, 0, st, a, vc));
   return JGCM_OK;
+}
+template <typename T>
+int launch_hs_column(const HSColArgs<T>& a, const jgcm_mesh* m, int ne, int S, const VertCoef* vc, bool hybrid,
+                     cudaStream_t st) {
+  return hybrid ? launch_hs_column_v<T, true>(a, m, ne, S, vc, st) : launch_hs_column_v<T, false>(a, m, ne, S, vc, st);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -701,6 +765,7 @@ struct CorrArgs {
   int col_gx, col_nb;
   size_t col_off;
   int nd, nlat, nlon, do_mass, do_energy;
+  int has_dak;  // some a_k differs between levels: the energy sums need sum_k T_k Δa_k
   double cp, grav;
   double inv_2n;  // 1 / (2 nlon), exact (nlon is a power of two)
   T cp_t;         // cp rounded to T on the host
@@ -715,9 +780,12 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   // folded across level groups and columns in FP64 in a fixed order
   constexpr int KS = 8;
   __shared__ T s_dak[JGCM_MAX_ND], s_dbk[JGCM_MAX_ND];  // the layer coefficients in the state precision
+  __shared__ double s_dak64[JGCM_MAX_ND], s_dbk64[JGCM_MAX_ND];  // and in FP64 (the c_p T sums)
   for (int q = threadIdx.x; q < a.nd; q += blockDim.x) {
     s_dak[q] = (T)vc.dak[q];
     s_dbk[q] = (T)vc.dbk[q];
+    s_dak64[q] = vc.dak[q];
+    s_dbk64[q] = vc.dbk[q];
   }
   __syncthreads();
   const int i = blockIdx.x * 32 + (threadIdx.x & 31), ks = threadIdx.x >> 5, j = blockIdx.y, nd = a.nd;
@@ -725,25 +793,30 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   const bool act = i < a.nlon;
   const size_t G = (size_t)a.nlat * a.nlon, col = (size_t)j * a.nlon + (act ? i : 0);
   const size_t offL = (size_t)e * nd * G, off1 = (size_t)e * G;
-  __shared__ T part[2][KS][32];
+  // the energy integrals sum_k E_k Δa_k, sum_k E_k Δb_k (E = |u|^2/2 + c_p T): the kinetic part in the
+  // state precision, the c_p T part (~99 %) as FP64 sums of the exact products T_k Δa_k, T_k Δb_k (the
+  // state precision's rounding of c_p T biased the energy correction by up to 1e-6 K per step)
+  __shared__ double part[2][KS][32];
   T ea = 0, eb = 0;
+  double ta = 0, tb = 0;
   if (act) {
-    const T cp = a.cp_t;
 #pragma unroll 4  // nd <= 32: every level's loads in flight together
     for (int k = ks; k < nd; k += KS) {
       size_t x = offL + (size_t)k * G + col;
-      T u = a.u_n[x], v = a.v_n[x], t = a.t_n[x];
-      T E = (T)0.5 * (u * u + v * v) + cp * t;
-      ea += E * s_dak[k];
-      eb += E * s_dbk[k];
+      T u = a.u_n[x], v = a.v_n[x];
+      const double t = (double)a.t_n[x];
+      T K = (T)0.5 * (u * u + v * v);
+      ea += K * s_dak[k];
+      eb += K * s_dbk[k];
+      if (a.has_dak) ta += t * s_dak64[k];
+      tb += t * s_dbk64[k];
     }
   }
-  part[0][ks][threadIdx.x & 31] = ea;
-  part[1][ks][threadIdx.x & 31] = eb;
+  part[0][ks][threadIdx.x & 31] = (double)ea + a.cp * ta;
+  part[1][ks][threadIdx.x & 31] = (double)eb + a.cp * tb;
   __syncthreads();
-  // the column's level groups folded in the state precision (as the column integrals themselves);
-  // the three sums over the block's columns in FP64, one warp each (FP64 runs at 1/64 of the FP32
-  // rate: spread over three SM sub-partitions instead of one)
+  // the column's level groups and the three sums over the block's columns in FP64, one warp each
+  // (FP64 runs at 1/64 of the FP32 rate: spread over three SM sub-partitions instead of one)
   __shared__ double wsum[3];
   if (ks < 3) {
     const int c = threadIdx.x & 31;
@@ -752,9 +825,9 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
     if (ks == 0) {
       x = (double)ps;
     } else {
-      T sq = 0;
+      double sq = 0;
       for (int q = 0; q < KS; q++) sq += part[ks - 1][q][c];
-      x = ks == 1 ? (double)sq : (double)sq * (double)ps;
+      x = ks == 1 ? sq : sq * (double)ps;
     }
     x = warp_sum(x);
     if (c == 0) wsum[ks] = x;
@@ -963,8 +1036,13 @@ void lin_geo_col(const VertCoef& vc, int nd, double R, const double* dtt, double
 //                 the exponent, which gives b > 1 above the surface)
 //   mcm, v197     the fixed 14- and 18-level tables of Compute_Old_Model_Sigma / Compute_V197_Sigma
 //                 (:143-165)
-// "hybrid" (:71-76, a_k != 0) does not run in the reference (Compute_Uneven_Sigma called without nd)
-// and is not supported: the column kernels use ln p = ln b_k + ln ps.
+//   hybrid        (:71-76, built as its code means it: the branch does not run in the reference,
+//                 Compute_Uneven_Sigma and Transition being called without nd) uneven sigma levels s_k
+//                 (zero_top false) serve as pressure levels p_ref s_k above s = p_press and as sigma
+//                 levels below s = p_sigma, blended by Transition (:93-110, sin^2 between):
+//                 a_k = p_ref s_k (1 - trans_k), b_k = s_k trans_k, with the constructor's defaults
+//                 p_ref = 101325, p_press = 0.1, p_sigma = 0.3 (:44-46); top half level zero, as the
+//                 zero_top pressure variables assume
 int vert_coord_table(int nd, const std::string& opt, double scale_heights, double surf_res, double exponent,
                      double* ak, double* bk) {
   static const double kMcm[15] = {0.0, 0.03, 0.0707, 0.1311, 0.2102, 0.3036, 0.4062, 0.5138,
@@ -993,8 +1071,15 @@ int vert_coord_table(int nd, const std::string& opt, double scale_heights, doubl
     }
     memcpy(bk, opt == "mcm" ? kMcm : kV197, (size_t)(nd + 1) * sizeof(double));
   } else if (opt == "hybrid") {
-    set_error("hybrid coordinates (a_k != 0) are not supported");
-    return JGCM_E_ARG;
+    const double p_ref = 101325.0, p_press = 0.1, p_sigma = 0.3, pi = 3.14159265358979323846;
+    for (int k = 0; k <= nd; k++) {
+      double t = (double)k / (double)nd, z = (1 - t) * 1.0 + t * 0.0;  // LinRange(1, 0, nd+1)
+      double sg = k == nd ? 1.0 : std::exp(-(surf_res * z + (1.0 - surf_res) * std::pow(z, exponent)) * scale_heights);
+      double tr = sg <= p_press ? 0.0 : sg >= p_sigma ? 1.0 : std::pow(std::sin(0.5 * pi * (sg - p_press) / (p_sigma - p_press)), 2);
+      ak[k] = p_ref * sg * (1.0 - tr);
+      bk[k] = sg * tr;
+    }
+    ak[0] = bk[0] = 0.0;
   } else {
     set_error("Compute_Vert_Coord: %s is not a valid value for option", opt.c_str());
     return JGCM_E_ARG;
@@ -1008,15 +1093,17 @@ void vertical_setup(jgcm_model* md) {
   memset(&vc, 0, sizeof(vc));
   for (int k = 0; k <= nd; k++) {
     double t = (double)k / (double)nd;
-    vc.ak[k] = 0.0;
+    vc.ak[k] = md->vert_ak.empty() ? 0.0 : md->vert_ak[k];
     vc.bk[k] = md->vert_bk.empty() ? (1 - t) * 0.0 + t * 1.0 : md->vert_bk[k];
+    if (vc.ak[k] != 0.0) vc.hybrid = 1;
   }
   for (int k = 0; k < nd; k++) {
     vc.dak[k] = vc.ak[k + 1] - vc.ak[k];
     vc.dbk[k] = vc.bk[k + 1] - vc.bk[k];
   }
-  for (int k = 1; k <= nd; k++) vc.lb[k] = std::log(vc.bk[k]);
-  for (int k = 0; k < nd; k++) {
+  // sigma coordinates: every log-pressure difference is a per-level constant (formed here in FP64)
+  for (int k = 1; k <= nd && !vc.hybrid; k++) vc.lb[k] = std::log(vc.bk[k]);
+  for (int k = 0; k < nd && !vc.hybrid; k++) {
     vc.cf[k] = (k == 0) ? vc.lb[1] - 1.0
                         : vc.lb[k + 1] + vc.bk[k] * (vc.lb[k + 1] - vc.lb[k]) / vc.dbk[k] - 1.0;
     vc.sf[k] = std::exp(vc.cf[k]);
@@ -1455,12 +1542,13 @@ int issue_diag(jgcm_model* md, int lev, cudaStream_t st) {
 // (Compute_Gradients!, Spectral_Spherical_Mesh.jl:721-741).  They read no (0,0) spectral mode (its
 // coefficients m/a and (n-1) ε_n/a vanish), so they may run while the fixers adjust those modes.
 template <typename T>
-int issue_hs_grad(jgcm_model* md, int lev, cudaStream_t st) {
+int issue_hs_grad(jgcm_model* md, int lev, cudaStream_t st, bool with_anom = true) {
   const int L = md->L, E = md->ne;
   S2GPlan sp;
   memset(&sp, 0, sizeof(sp));
-  // FP32: also T less its level means for the next column kernel's geopotential (S2G_ANOM)
-  const bool anom = std::is_same<T, float>::value;
+  // FP32: also T less its level means for the column kernel's geopotential (S2G_ANOM), unless the
+  // step's own synthesis of the level wrote it (EPI_ANOM)
+  const bool anom = std::is_same<T, float>::value && with_anom;
   sp.ng = anom ? 5 : 4;
   sp.C = 2 * E + (anom ? 3 : 2) * L;
   sp.g[0] = sg(S2G_DLAM, md->spe_lnps[lev], nullptr, E, 0);
@@ -1478,6 +1566,13 @@ int issue_hs_grad(jgcm_model* md, int lev, cudaStream_t st) {
   ip.g[3] = og(EPI_DIVCOS, md->g_dtT, L, 2 * E + L);
   if (anom) ip.g[4] = og(EPI_NONE, md->g_tdev, L, 2 * E + 2 * L);
   return launch_s2g<T>(md->mesh, sp, ip, st, md->fbuf, md->fcap);
+}
+
+// whether the vertical coordinate has Δa_k != 0 (hybrid): the energy integrals then need sum_k T_k Δa_k
+inline int has_dak(const jgcm_model* md) {
+  for (int k = 0; k < md->nd; k++)
+    if (md->vc.dak[k] != 0.0) return 1;
+  return 0;
 }
 
 template <typename T>
@@ -1501,6 +1596,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   a.v_c = (const T*)md->grid_v[c];
   a.t_c = (const T*)md->grid_t[c];
   a.tdev = std::is_same<T, float>::value ? (const T*)md->g_tdev : nullptr;
+  a.has_dak = has_dak(md);
   a.div = (const T*)md->grid_div;
   a.vor = (const T*)md->grid_vor;
   a.dlps = (const T*)md->g_dlps;
@@ -1537,7 +1633,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   a.inv_2n = 0.5 / m->nlon;
   a.pstride = partial_stride(m);
   hs_col_consts<T>(a);
-  JG_TRY(launch_hs_column<T>(a, m, E, md->hs_lanes, md->d_vc, st));
+  JG_TRY(launch_hs_column<T>(a, m, E, md->hs_lanes, md->d_vc, md->vc.hybrid, st));
   mark(st);
   JG_CUDA(cudaGetLastError());
   // 3. forward transforms: δu cos, δv cos, δT, energy, δlnps -> vor/div tendencies (alpha
@@ -1610,7 +1706,10 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   s2.g[1] = sg(S2G_PLAIN, md->spe_div[n], nullptr, L, L);
   s2.g[2] = sg(S2G_UCOS, md->spe_vor[n], md->spe_div[n], L, 2 * L);
   s2.g[3] = sg(S2G_VCOS, md->spe_vor[n], md->spe_div[n], L, 3 * L);
-  s2.g[4] = sg(S2G_PLAIN, md->spe_t[n], nullptr, L, 4 * L);
+  // FP32: T synthesised without its level means; the epilogue writes grid T (+ the means) and the
+  // anomaly itself for the next step's geopotential (the fixer's shift of T leaves it unchanged)
+  const bool anom = std::is_same<T, float>::value;
+  s2.g[4] = sg(anom ? S2G_ANOM : S2G_PLAIN, md->spe_t[n], nullptr, L, 4 * L);
   // ln ps is synthesised as ln ps - ln 1e5 (mode (0,0) shifted; P_00 = 1) and shifted back in the
   // epilogue, so its rounding scales with |ln(ps / 1e5)| ~ 0.02 instead of ln ps ~ 11.5
   s2.g[5] = sg(S2G_PLAIN, md->spe_lnps[n], nullptr, E, 5 * L);
@@ -1623,7 +1722,8 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   i2.g[1] = og(EPI_NONE, md->grid_div, L, L);
   i2.g[2] = og(EPI_DIVCOS, md->grid_u[n], L, 2 * L);
   i2.g[3] = og(EPI_DIVCOS, md->grid_v[n], L, 3 * L);
-  i2.g[4] = og(EPI_NONE, md->grid_t[n], L, 4 * L);
+  i2.g[4] = og(anom ? EPI_ANOM : EPI_NONE, md->grid_t[n], L, 4 * L, anom ? md->g_tdev : nullptr);
+  i2.g[4].ps = anom ? md->spe_t[n] : nullptr;
   i2.g[5] = og(EPI_EXP2, md->grid_lnps, E, 5 * L, md->grid_ps[n]);
   i2.g[5].shift = kLnPsRef;
   JG_TRY(launch_s2g<T>(m, s2, i2, st, md->fbuf, md->fcap));
@@ -1654,6 +1754,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ca.grav = md->P.grav;
   ca.inv_2n = 0.5 / m->nlon;
   ca.cp_t = (T)md->cp_air;
+  ca.has_dak = has_dak(md);
   // the fixers (this branch) and the next step's gradients of the new level (second branch)
   const bool serial = g_marker != nullptr;  // per-kernel timing: one stream, launches in order
   cudaStream_t br = serial ? st : md->side;
@@ -1671,7 +1772,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
                      (const T*)(md->d_scalars + 4 * E), (size_t)nd * G1, G1));
   mark(st);
   JG_CUDA(cudaGetLastError());
-  JG_TRY(issue_hs_grad<T>(md, n, br));
+  JG_TRY(issue_hs_grad<T>(md, n, br, false));
   if (md->diag_on && !serial) JG_TRY(issue_diag<T>(md, n, st));  // the new state, after the fixers
   if (!serial) {
     JG_CUDA(cudaEventRecord(md->ev_join, br));
@@ -1898,9 +1999,13 @@ extern "C" int jgcm_model_create_vert(jgcm_mesh* mesh, const jgcm_params* params
   JG_ARG((ak == nullptr) == (bk == nullptr), "ak and bk are given together");
   if (bk) {
     const int nd = mesh->nd;
-    for (int k = 0; k <= nd; k++) JG_ARG(ak[k] == 0.0, "hybrid coordinates (a_k != 0) are not supported");
-    JG_ARG(bk[0] == 0.0 && bk[nd] == 1.0, "sigma coordinates need b_0 = 0 (zero top) and b_nd = 1");
-    for (int k = 0; k < nd; k++) JG_ARG(bk[k + 1] > bk[k], "b_k must increase downwards");
+    JG_ARG(ak[0] == 0.0 && bk[0] == 0.0, "the top half level must be zero (a_0 = b_0 = 0, zero_top)");
+    JG_ARG(ak[nd] == 0.0 && bk[nd] == 1.0, "the bottom half level must be the surface (a_nd = 0, b_nd = 1)");
+    for (int k = 0; k < nd; k++)
+      for (double f : {0.9, 1.1}) {  // half-level pressures increase downwards around the reference ps
+        const double ps = f * params->ps_ref;
+        JG_ARG(ak[k + 1] + bk[k + 1] * ps > ak[k] + bk[k] * ps, "a_k + b_k ps must increase downwards (k = %d)", k);
+      }
   }
   *out = nullptr;
   JG_ARG(members >= 1 && members <= 65535, "members must be in [1, 65535]");
@@ -1920,7 +2025,10 @@ extern "C" int jgcm_model_create_vert(jgcm_mesh* mesh, const jgcm_params* params
   md->init_step = 1;
   md->sw_adv_from_n = 1;
   md->cp_air = params->rdgas / params->kappa;
-  if (bk) md->vert_bk.assign(bk, bk + mesh->nd + 1);
+  if (bk) {
+    md->vert_bk.assign(bk, bk + mesh->nd + 1);
+    md->vert_ak.assign(ak, ak + mesh->nd + 1);
+  }
   int s = model_alloc(md);
   if (s != JGCM_OK) {
     model_free(md);

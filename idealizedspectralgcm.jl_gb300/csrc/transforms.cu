@@ -151,6 +151,10 @@ __device__ __forceinline__ void ifft_store(const GridOutGroup& g, const Tables<T
     case EPI_ADJ_G2S:
       dst[idx] = x * (tb.wts[j] / (T)(2 * nlon));
       break;
+    case EPI_ANOM:
+      dst[idx] = x + ((const V2<T>*)g.ps)[k].x;
+      ((T*)g.dst2)[idx] = x;
+      break;
   }
 }
 

@@ -317,8 +317,9 @@ def Compute_Vert_Coord(nd, vert_coord_option, scale_heights=4.0, surf_res=1.0, e
     """Vert_Coordinate.jl:61-87: the half-level coefficients (ak, bk), nd+1 each, top first, zero top.
 
     Options: "even_sigma", "uneven_sigma" (built as Compute_Uneven_Sigma's docstring states; the
-    reference's own branch does not run), "mcm" (nd 14), "v197" (nd 18).  "hybrid" raises: its
-    reference branch does not run and a_k != 0 is not supported."""
+    reference's own branch does not run), "mcm" (nd 14), "v197" (nd 18), "hybrid" (pressure levels
+    above sigma 0.1, sigma levels below 0.3, Transition's sin^2 blend between; built as the reference's
+    code means it, its branch does not run).  Hybrid models step forward; their step adjoint is refused."""
     ak, bk = np.zeros(nd + 1), np.zeros(nd + 1)
     _check(lib().jgcm_vert_coord(int(nd), vert_coord_option.encode(), float(scale_heights), float(surf_res),
                                  float(exponent), _ptr(ak), _ptr(bk)))

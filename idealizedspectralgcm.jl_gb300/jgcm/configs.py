@@ -63,7 +63,8 @@ PARAMS["hs_t21l14"] = dict(PARAMS["hs_t42l20"])
 PARAMS["hs_t21l18"] = dict(PARAMS["hs_t42l20"])
 
 # Vert_Coordinate options with the grid whose level count each one needs
-VERT_COORD_CASES = [("hs_t21l14", "mcm"), ("hs_t21l18", "v197"), ("hs_t21l20", "uneven_sigma")]
+VERT_COORD_CASES = [("hs_t21l14", "mcm"), ("hs_t21l18", "v197"), ("hs_t21l20", "uneven_sigma"),
+                    ("hs_t21l20", "hybrid")]
 
 STEPS_PER_DAY = {k: DAY // v["dt"] for k, v in PARAMS.items()}
 

@@ -161,14 +161,17 @@ int jgcm_model_members(jgcm_model* model, int* members);
  * half-level coefficients ak[nd+1], bk[nd+1] (p_{k+1/2} = ak + bk ps, top first) for option
  * "even_sigma", "uneven_sigma" (scale_heights, surf_res, exponent: the reference's defaults are
  * 4, 1, 2.5; built as Compute_Uneven_Sigma's docstring states, :120-141 — the reference's code
- * for that branch does not run), "mcm" (nd 14) or "v197" (nd 18); always zero top (the
- * constructor's default, :44).  "hybrid" (a_k != 0; :71-76, which does not run in the reference)
- * returns JGCM_E_ARG. */
+ * for that branch does not run), "mcm" (nd 14), "v197" (nd 18) or "hybrid" (:71-76 as its code means
+ * it -- the reference's branch does not run: uneven sigma levels s_k serve as pressure levels
+ * 101325 s_k above s = 0.1 and as sigma levels below s = 0.3, blended by Transition's sin^2,
+ * :93-110); always zero top (the constructor's default, :44). */
 int jgcm_vert_coord(int nd, const char* option, double scale_heights, double surf_res, double exponent,
                     double* ak, double* bk);
 /* jgcm_model_create_members on the vertical coordinate ak, bk (each nd+1; NULL, NULL = even_sigma,
- * the reference drivers' choice, Spectral_Dynamics.jl:513): sigma coordinates only (ak = 0,
- * bk[0] = 0, bk[nd] = 1, increasing), else JGCM_E_ARG. */
+ * the reference drivers' choice, Spectral_Dynamics.jl:513): a zero top (ak[0] = bk[0] = 0), the
+ * surface at the bottom (ak[nd] = 0, bk[nd] = 1) and half-level pressures ak + bk ps increasing
+ * downwards for ps within 10 % of ps_ref, else JGCM_E_ARG.  Hybrid coordinates (ak != 0) run the
+ * forward model; jgcm_model_step_adjoint and jgcm_model_hs_gradient need sigma coordinates. */
 int jgcm_model_create_vert(jgcm_mesh* mesh, const jgcm_params* params, int members, const double* ak,
                            const double* bk, jgcm_model** out);
 /* Copy member src_member of src into member dst_member of dst (same mesh and model kind): every

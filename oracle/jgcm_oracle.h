@@ -61,6 +61,11 @@ void om_set_threads(int nthreads);
 /* 64: the geopotential reads the temperature synthesised without its (0,0) modes, with the level
  * constants added back exactly (the GPU's FP32 formulation), instead of grid T (stored in FP32) */
 #define OM_F32_TANOM 64
+/* 128: the fixers' column energy integrals in FP32 (summands and the sum over levels; the global
+ * fold stays FP64); 256: only the kinetic part of those energies in FP32, the c_p T part and the sums
+ * in FP64 (the GPU's FP32 path) */
+#define OM_F32_FIXER 128
+#define OM_F32_FIXER_KE 256
 void om_set_f32(int mask);
 
 /* Spectral_Spherical_Mesh.jl transforms; nlev = third dimension (nd or 1) */
@@ -106,7 +111,7 @@ typedef struct {
 } om_params;
 
 om_model* om_model_create(om_mesh* mesh, const om_params* p);
-om_model* om_model_create_vert(om_mesh* mesh, const om_params* p, const double* bk);
+om_model* om_model_create_vert(om_mesh* mesh, const om_params* p, const double* ak, const double* bk);
 int om_vert_coord(int nd, const char* option, double scale_heights, double surf_res, double exponent, double* ak,
                   double* bk);
 void om_semi_implicit_step(om_model* md, const double* const* in, double* const* out);
@@ -121,6 +126,9 @@ int om_model_update_init_step(om_model* md);
 /* one Barotropic_Dynamics! / Shallow_Water_Physics!+Shallow_Water_Dynamics! /
  * Atmosphere_Update! followed by the driver's Update_Init_Step! after the first step */
 int om_model_step(om_model* md, int nsteps);
+/* the last Held-Suarez step's fixer scalars: mean_ps_p, mean_energy_p, mean_ps_n, factor,
+ * mean_energy_n, temperature correction (out[6]) */
+void om_model_fixer_scalars(const om_model* md, double* out);
 /* Spectral_Dynamics.jl:372-449; grid_t_pert (nullable) is added to grid_t before filtering */
 int om_spectral_initialize_fields(om_model* md, const double* grid_t_pert, int vorticity_seed);
 /* Semi_Implicit.jl: copy out "div_mat" (nd*nd), "h" (nd), "wave_matrix" (nd*nd*(N+1)) */

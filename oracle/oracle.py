@@ -68,13 +68,14 @@ def lib():
             "om_apply_laplacian": (None, [P, P, I]),
             "om_area_weighted_global_mean": (D, [P, P]),
             "om_model_create": (P, [P, P]),
-            "om_model_create_vert": (P, [P, P, P]),
+            "om_model_create_vert": (P, [P, P, P, P]),
             "om_vert_coord": (I, [I, C.c_char_p, D, D, D, P, P]),
             "om_model_destroy": (None, [P]),
             "om_model_field": (L, [P, C.c_char_p, P, L, I]),
             "om_model_init_step": (I, [P]),
             "om_model_update_init_step": (I, [P]),
             "om_model_step": (I, [P, I]),
+            "om_model_fixer_scalars": (None, [P, P]),
             "om_spectral_initialize_fields": (I, [P, P, I]),
             "om_model_semi_implicit": (L, [P, C.c_char_p, P, L]),
             "om_hs_forcing": (None, [P, I, P, P, P, P, P, P, P, P, P]),
@@ -102,6 +103,8 @@ def set_threads(n: int) -> None:
 # FP32 emulation switches for error bisection (jgcm_oracle.h); 0 = the FP64 restatement
 F32_STAGES = {"fft_fwd": 1, "analysis": 2, "synthesis": 4, "fft_inv": 8, "grid": 16, "spectral": 32}
 F32_TANOM = 64  # the geopotential on T synthesised without its level means (the GPU's FP32 formulation)
+F32_FIXER = 128  # the fixers' column energy integrals in FP32, the global fold in FP64
+F32_FIXER_KE = 256  # only their kinetic part in FP32, c_p T and the sums in FP64 (the GPU's FP32 path)
 
 
 def set_f32(mask: int) -> None:
@@ -264,8 +267,6 @@ class Model:
         if isinstance(vert_coord, str):
             vert_coord = Compute_Vert_Coord(mesh.nd, vert_coord, **vert_options)
         self.ak, self.bk = (np.ascontiguousarray(x, dtype=np.float64) for x in vert_coord)
-        if np.any(self.ak != 0):
-            raise AssertionError("hybrid coordinates (a_k != 0) are not supported")
         p = _Params()
         for name, _ in _Params._fields_:
             if name == "kind":
@@ -273,7 +274,8 @@ class Model:
             elif name in params:
                 setattr(p, name, params[name])
         self._p = p
-        self._h = lib().om_model_create_vert(mesh._h, C.byref(p), self.bk.ctypes.data_as(C.c_void_p))
+        self._h = lib().om_model_create_vert(mesh._h, C.byref(p), self.ak.ctypes.data_as(C.c_void_p),
+                                             self.bk.ctypes.data_as(C.c_void_p))
         if not self._h:
             raise AssertionError("model creation failed")
 
@@ -312,6 +314,13 @@ class Model:
 
     def step(self, nsteps=1):
         lib().om_model_step(self._h, int(nsteps))
+
+    def fixer_scalars(self):
+        """The last Held-Suarez step's mean_ps_p, mean_energy_p, mean_ps_n, factor, mean_energy_n and
+        temperature correction (Compute_Corrections!)."""
+        out = np.zeros(6)
+        lib().om_model_fixer_scalars(self._h, _ptr(out))
+        return out
 
     def update_init_step(self):
         assert lib().om_model_update_init_step(self._h) == 0, "Update_Init_Step!: not in the init step"

@@ -67,10 +67,11 @@ def test_argument_errors_are_assertions(jg):
 def test_vert_coord_tables_match_the_oracle(jg, orc):
     """jgcm_vert_coord is host code: it runs without a device and equals the oracle's tables."""
     for nd, opt, kw in ((20, "even_sigma", {}), (20, "uneven_sigma", {}), (14, "mcm", {}), (18, "v197", {}),
-                        (24, "uneven_sigma", dict(scale_heights=5.0, surf_res=0.2, exponent=2.0))):
+                        (24, "uneven_sigma", dict(scale_heights=5.0, surf_res=0.2, exponent=2.0)),
+                        (20, "hybrid", {}), (30, "hybrid", dict(scale_heights=5.0, surf_res=0.5))):
         ag, bg = jg.Compute_Vert_Coord(nd, opt, **kw)
         ao, bo = orc.Compute_Vert_Coord(nd, opt, **kw)
-        assert np.array_equal(ag, ao) and np.allclose(bg, bo, rtol=2e-16, atol=0), opt
-    for nd, opt in ((20, "mcm"), (20, "hybrid"), (20, "sigma")):
+        assert np.allclose(ag, ao, rtol=1e-15, atol=0) and np.allclose(bg, bo, rtol=1e-15, atol=0), opt
+    for nd, opt in ((20, "mcm"), (20, "sigma")):
         with pytest.raises(AssertionError):
             jg.Compute_Vert_Coord(nd, opt)

@@ -155,13 +155,25 @@ def test_held_suarez_vert_coords(jg, orc, name, option, prec, tol):
         assert configs.rel_l2(gmod.get(f), omod.get(f)) < (tol if prec == "fp64" else 1e-5), f
 
 
-def test_held_suarez_refuses_hybrid_coordinates(jg):
+def test_held_suarez_vertical_coordinate_checks(jg):
+    """Model creation refuses coefficients without a zero top, without the surface at the bottom or
+    with half-level pressures that do not increase downwards; hybrid models refuse the step adjoint
+    (its reverse column kernel reads the sigma coordinates' per-level constants)."""
     gm = configs.make_mesh(jg, "hs_t21l10", precision="fp32")
+    params = configs.PARAMS["hs_t21l10"]
     ak, bk = np.linspace(0.0, 1.0e3, 11), np.linspace(0.0, 1.0, 11)
     with pytest.raises(AssertionError):
-        jg.Model(gm, configs.PARAMS["hs_t21l10"], vert_coord=(ak, bk))
+        jg.Model(gm, params, vert_coord=(ak, bk))  # a_nd != 0: the bottom is not the surface
+    ak, bk = np.zeros(11), np.linspace(0.0, 1.0, 11)
+    bk[5], bk[6] = bk[6], bk[5]
     with pytest.raises(AssertionError):
-        jg.Model(gm, configs.PARAMS["hs_t21l10"], vert_coord="hybrid")
+        jg.Model(gm, params, vert_coord=(ak, bk))  # not increasing
+    hy = jg.Model(gm, params, vert_coord="hybrid")
+    configs.init_held_suarez(jg, gm, hy)
+    hy.step(2)
+    bars = {f: np.zeros_like(hy.get(f)) for f in jg.STATE_FIELDS}
+    with pytest.raises(AssertionError):
+        jg.HS_Step_Adjoint(hy, bars)
 
 
 def test_held_suarez_restart_steady_step(jg, orc):

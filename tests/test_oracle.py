@@ -207,8 +207,9 @@ def test_vert_coord_tables(orc):
     """Compute_Vert_Coord (Vert_Coordinate.jl:61-87), zero top: even_sigma is LinRange(0, 1);
     uneven_sigma with surf_res = 1 is exp(-scale_heights (1 - k/nd)) inside, and with surf_res < 1
     stays increasing; the v197 table is symmetric about 1/2 (b_k + b_{nd-k} = 1 to its 7 printed decimals); mcm and v197 need
-    their own level counts; hybrid (a_k != 0, a branch that does not run in the reference) is
-    refused."""
+    their own level counts.  hybrid (a branch that does not run in the reference, built as its code
+    means it): a zero top, pure pressure levels (b = 0, a = 101325 s) above s = 0.1, pure sigma
+    levels (a = 0) below s = 0.3, and half-level pressures increasing for ps near 1e5 Pa."""
     ak, bk = orc.Compute_Vert_Coord(20, "even_sigma")
     assert np.all(ak == 0) and np.allclose(bk, np.linspace(0, 1, 21), rtol=0, atol=1e-15)
     ak, bk = orc.Compute_Vert_Coord(20, "uneven_sigma")
@@ -221,15 +222,23 @@ def test_vert_coord_tables(orc):
     assert np.allclose(b197 + b197[::-1], 1.0, rtol=0, atol=1.5e-7) and np.all(np.diff(b197) > 0)
     _, bmcm = orc.Compute_Vert_Coord(14, "mcm")
     assert bmcm[0] == 0 and bmcm[14] == 1 and np.all(np.diff(bmcm) > 0)
-    for nd, opt in ((20, "mcm"), (20, "v197"), (20, "hybrid"), (20, "sigma")):
+    ah, bh = orc.Compute_Vert_Coord(20, "hybrid")
+    _, s = orc.Compute_Vert_Coord(20, "uneven_sigma")
+    assert ah[0] == 0 and bh[0] == 0 and ah[20] == 0 and bh[20] == 1
+    upper, lower = (s > 0) & (s <= 0.1), s >= 0.3
+    assert np.all(bh[upper] == 0) and np.allclose(ah[upper], 101325.0 * s[upper], rtol=1e-15, atol=0)
+    assert np.all(ah[lower] == 0) and np.allclose(bh[lower], s[lower], rtol=1e-15, atol=0)
+    for ps in (0.9e5, 1.0e5, 1.1e5):
+        assert np.all(np.diff(ah + bh * ps) > 0)
+    for nd, opt in ((20, "mcm"), (20, "v197"), (20, "sigma")):
         with pytest.raises(AssertionError):
             orc.Compute_Vert_Coord(nd, opt)
 
 
 @pytest.mark.parametrize("name,option", configs.VERT_COORD_CASES)
 def test_hs_vert_coords_mass_fixer_and_step_finite(orc, name, option):
-    """Held-Suarez on the other sigma coordinates: the mass fixer holds the area-mean surface
-    pressure and the state stays finite; the half-level pressures are b_k ps."""
+    """Held-Suarez on the other vertical coordinates: the mass fixer holds the area-mean surface
+    pressure and the state stays finite; the half-level pressures are a_k + b_k ps."""
     M = configs.make_mesh(orc, name)
     md = orc.Model(M, configs.PARAMS[name], vert_coord=option)
     md.spectral_initialize_fields(configs.hs_temperature_noise(M), True)
@@ -240,7 +249,7 @@ def test_hs_vert_coords_mass_fixer_and_step_finite(orc, name, option):
     assert np.isfinite(md.get("grid_t_c")).all() and np.isfinite(md.get("spe_div_c")).all()
     ph = md.get("grid_p_half")
     ps = md.get("grid_ps_c")
-    assert np.allclose(ph, ps[:, :, :1] * md.bk[None, None, :], rtol=1e-14, atol=0)
+    assert np.allclose(ph, md.ak[None, None, :] + ps[:, :, :1] * md.bk[None, None, :], rtol=1e-14, atol=0)
 
 
 def test_barotropic_rh4_is_steady_pattern(orc):
