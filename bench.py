@@ -181,14 +181,15 @@ def algorithmic_bytes(name: str, N: int, nlat: int, nlon: int, nd: int, esize: i
     F = (N + 1) * nlat                  # Fourier coefficients per column (complex)
     c = 2 * esize                       # complex element
     table = {
-        "s2g_legendre(grad lnps,T)": (1 + nd) * S * c + (2 + 2 * nd) * F * c,
-        "ifft(grad lnps,T)": (2 + 2 * nd) * F * c + (2 + 2 * nd) * G * esize + G * esize,
         "hs_column": (10 * nd + 5) * G * esize + (5 * nd + 1) * G * esize,
         "fft(tendencies)": (4 * nd + 1) * G * esize + (4 * nd + 1) * F * c,
         "g2s_legendre(vor,div,T,lnps)": (4 * nd + 1) * F * c + (3 * nd + 1) * S * c,
         "hs_implicit": (9 * nd + 3) * S * c + (6 * nd + 2) * S * c + (N + 1) * nd * nd * 8,
-        "s2g_legendre(vor,div,u,v,T,lnps)": (3 * nd + 1) * S * c + (5 * nd + 1) * F * c,
-        "ifft(vor,div,u,v,T,lnps)": (5 * nd + 1) * F * c + (5 * nd + 2) * G * esize,
+        # the new level (vor, div, u, v, T, ln ps) and the next step's gradients of ln ps and T, from
+        # the same spectra; the FP32 path also writes T less its level means
+        "s2g_legendre(vor,div,u,v,T,lnps,grad lnps,grad T)": (3 * nd + 1) * S * c + (7 * nd + 3) * F * c,
+        "ifft(vor,div,u,v,T,lnps,grad lnps,grad T)": (7 * nd + 3) * F * c
+        + ((7 * nd + 4) + (nd if esize == 4 else 0)) * G * esize,
         "hs_corr_reduce": (3 * nd + 1) * G * esize,
         "hs_corr_apply": 2 * (nd + 1) * G * esize,
     }

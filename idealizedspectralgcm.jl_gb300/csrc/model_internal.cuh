@@ -38,10 +38,8 @@ struct jgcm_model {
   // half-level coefficients a_k, b_k given at creation (Vert_Coordinate's ak, bk); empty = even_sigma
   std::vector<double> vert_ak, vert_bk;
   // Held-Suarez: the gradients of ln ps and T of the current level are already in g_dlps ...
-  // g_dtT (computed at the end of the previous step, concurrently with the fixers)
+  // g_dtT (synthesised by the previous step together with its new level)
   int grad_ready;
-  cudaStream_t side;        // second branch of a step (the gradients next to the fixers)
-  cudaEvent_t ev_fork, ev_join;
   // on-device diagnostics (Output_Manager.jl:81-107): FP64 sums after every step of the zonal means
   // of T, T_eq, u, v ([4][ne][nd][nlat]) and of ps ([ne][nlat][nlon]), and the number of steps summed
   double* diag;

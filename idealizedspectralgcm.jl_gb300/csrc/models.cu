@@ -3,7 +3,7 @@
 //   Barotropic_Dynamics!        Barotropic_Dynamics.jl:2-46                 4 launches / step
 //   Shallow_Water_Dynamics!     Shallow_Water_Dynamics.jl:7-179             6 launches / step
 //   Atmosphere_Update! (HS)     Spectral_Dynamics.jl:206-365, 452-490,
-//                               HS_Forcing.jl:1-130, Semi_Implicit.jl       10 launches / step
+//                               HS_Forcing.jl:1-130, Semi_Implicit.jl        8 launches / step
 //
 // Dyn_Data lives on the device in the model's precision.  Time levels p/c/n rotate by
 // pointer (Time_Advance!, Dyn_Data.jl:326-364, copies instead); steady steps are captured
@@ -73,70 +73,51 @@ __device__ __forceinline__ T shfl_dn1(T x, int lane, int nd, T fill) {
   return lane + 1 >= nd ? fill : y;
 }
 
-// Block-wide deterministic fold of the FP64 partials of a (gx = column chunk, y = latitude) grid of
-// nb blocks, sum_j w_j sum_b partial[v][j][b] (v < NV): every thread of the block calls it; each
-// folds a fixed strided subset (weighted by the latitude of the block's row), then warps and lanes
-// combine in a fixed order.  The NV totals land in out[] of thread 0.  U partials per thread are
-// loaded before they are added (in their fixed order): latency hidden when a thread folds many
-// partials, at U * NV * 2 registers of the whole kernel.
-template <int NV, int U = 1>
-__device__ void fold_weighted(const double* partials, int nb, int gx, const double* wts, double* out) {
-  __shared__ double red[NV][32];
-  double s[NV];
-  for (int v = 0; v < NV; v++) s[v] = 0.0;
-  for (int b0 = threadIdx.x; b0 < nb; b0 += U * blockDim.x) {
-    double pv[U][NV], wv[U];
-#pragma unroll
-    for (int u = 0; u < U; u++) {
-      const int b = b0 + u * (int)blockDim.x;
-      wv[u] = b < nb ? wts[b / gx] : 0.0;
-#pragma unroll
-      for (int v = 0; v < NV; v++) pv[u][v] = b < nb ? __ldcg(partials + (size_t)v * nb + b) : 0.0;
-    }
-#pragma unroll
-    for (int u = 0; u < U; u++)
-      if (b0 + u * (int)blockDim.x < nb)
-#pragma unroll
-        for (int v = 0; v < NV; v++) s[v] += pv[u][v] * wv[u];
-  }
-  for (int v = 0; v < NV; v++) s[v] = warp_sum(s[v]);
-  const int nw = (blockDim.x + 31) >> 5;
-  if ((threadIdx.x & 31) == 0)
-    for (int v = 0; v < NV; v++) red[v][threadIdx.x >> 5] = s[v];
-  __syncthreads();
-  __shared__ double tot[NV];
-  if (threadIdx.x < NV) {  // one lane per total: the NV folds side by side, each in its fixed order
-    double t = 0.0;
-    for (int q = 0; q < nw; q++) t += red[threadIdx.x][q];
-    tot[threadIdx.x] = t;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0)
-    for (int v = 0; v < NV; v++) out[v] = tot[v];
+// Deterministic two-level grid reduction of FP64 block values (the fixers' global sums).  FP64
+// issues at 2 lanes per cycle per SM here (a warp instruction holds its sub-partition's FP64 pipe
+// for ~64 cycles), so the folds are laid out to keep few FP64 warp instructions on the critical
+// path and to spread them over the four sub-partitions: one warp per value, lanes over partials,
+// a fixed butterfly.  Blocks form groups of CORR_GS consecutive blocks; the last block of a group
+// (atomic ticket) folds the group's partials, and the last group's last block folds the groups'.
+constexpr int CORR_GS = 16;
+
+__host__ __device__ inline int corr_groups(int nb) { return (nb + CORR_GS - 1) / CORR_GS; }
+
+// sum of the n consecutive values at p: lane-strided in a fixed order, then the butterfly; every
+// lane of the warp returns the same total
+__device__ __forceinline__ double warp_fold(const double* p, int n, int lane) {
+  double s = 0.0;
+  for (int q = lane; q < n; q += 32) s += __ldcg(p + q);
+  return warp_sum(s);
 }
 
-// Deterministic grid-wide FP64 reduction over a (x = column chunk, y = latitude) grid.  Thread 0
-// of every block passes its NV block sums; the last block to finish (atomic ticket) folds the
-// partials (fold_weighted) and returns true with the NV totals in out[] of its thread 0.  All other
-// blocks return false.
-template <int NV, int U = 1>
-__device__ bool grid_reduce_last(const double* vals, double* partials, unsigned* counter, const double* wts,
-                                 double* out) {
-  __shared__ bool am_last;
-  const int nb = gridDim.x * gridDim.y;
-  const int bid = blockIdx.y * gridDim.x + blockIdx.x;
+// Publishes this block's arrival after its writes (made by any of its threads, each followed by
+// __threadfence) and returns, in every thread, whether it was the last of the `n` arrivals on
+// `counter`; the last one resets the counter for the next launch.
+__device__ __forceinline__ bool ticket_last(unsigned* counter, unsigned n) {
+  __shared__ bool last;
+  __syncthreads();
   if (threadIdx.x == 0) {
-    for (int v = 0; v < NV; v++) partials[(size_t)v * nb + bid] = vals[v];
-    __threadfence();
-    unsigned t = atomicAdd(counter, 1u);
-    am_last = (t == (unsigned)nb - 1);
+    const unsigned t = atomicAdd(counter, 1u);
+    last = (t == n - 1);
+    if (last) *counter = 0u;
   }
   __syncthreads();
-  if (!am_last) return false;
-  __threadfence();
-  fold_weighted<NV, U>(partials, nb, gridDim.x, wts, out);
-  if (threadIdx.x == 0) *counter = 0u;
-  return true;
+  if (last) __threadfence();  // the other blocks' partials are read after their fences
+  return last;
+}
+
+// Mercator series of log(1 + d) for |d| <= 2^-12: the remainder after the d^5 term is below
+// |d|^6 / 6 < 2^-62 |d|, under half an ulp of the sum; larger |d| take the library's log
+__device__ __forceinline__ double log_near_one(double f) {
+  const double d = f - 1.0;  // exact for f in [1/2, 2] (Sterbenz)
+  if (fabs(d) > 0x1p-12) return log(f);
+  const double c3 = 1.0 / 3.0, c5 = 1.0 / 5.0;
+  double r = fma(-d, c5, 0.25);   // 1/4 - d/5
+  r = fma(-d, r, c3);             // 1/3 - d (1/4 - d/5)
+  r = fma(-d, r, 0.5);            // 1/2 - ...
+  r = fma(-d, r, 1.0);            // 1 - d (1/2 - ...)
+  return d * r;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -757,11 +738,11 @@ struct CorrArgs {
   const double* wts;
   double *partials, *scalars;  // per member: partials + e * pstride, scalars + 4 e
   T* scal_t;                   // per member: factor and correction rounded to T (for k_hs_corr_apply)
-  unsigned* counter;
+  unsigned* counter;           // per member: corr_groups(nb) + 1 tickets
   size_t pstride;
-  // the column kernel's block partials (mean ps and column energy of the previous level) at the
-  // start of the member's region, its grid (col_gx x nlat blocks); this kernel's own partials at
-  // col_off
+  // the column kernel's block partials (ps_p and the column energy of the previous level) at the
+  // start of the member's region, its grid (col_gx x nlat blocks); this kernel's block partials at
+  // col_off (3 x nb), its group partials after them (5 x corr_groups(nb))
   int col_gx, col_nb;
   size_t col_off;
   int nd, nlat, nlon, do_mass, do_energy;
@@ -771,13 +752,18 @@ struct CorrArgs {
   T cp_t;         // cp rounded to T on the host
 };
 
+// The sums, every one weighted by the Gaussian weight of its latitude row:
+//   S0 = Σ ps_n,  S1 = Σ Σ_k E_k Δa_k,  S2 = Σ ps_n Σ_k E_k Δb_k  (E = |u|²/2 + c_p T of level n)
+//   S3 = Σ ps_p,  S4 = Σ Σ_k E_k Δp_k of level p  (the column kernel's partials)
+// mean_ps = S / (2 nlon) (Area_Weighted_Global_Mean), mean_energy = S / (2 nlon g)
+// (Mass_Weighted_Global_Integral); factor = mean_ps_p / mean_ps_n = S3 / S0, and with Δp_k =
+// Δa_k + Δb_k factor ps_n the correction grav (mean_energy_p - mean_energy_n) / (c_p mean_ps_p)
+// = (S4 - S1 - factor S2) / (c_p S3).
 template <typename T>
 __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const VertCoef* __restrict__ vcp) {
-  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   const VertCoef& vc = *vcp;
   // block = 32 consecutive columns of one latitude row x 8 level groups: warp ks reads levels
-  // ks, ks + 8, ... of the 32 columns (coalesced rows); column partial sums in the state precision,
-  // folded across level groups and columns in FP64 in a fixed order
+  // ks, ks + 8, ... of the 32 columns (coalesced rows)
   constexpr int KS = 8;
   __shared__ T s_dak[JGCM_MAX_ND], s_dbk[JGCM_MAX_ND];  // the layer coefficients in the state precision
   __shared__ double s_dak64[JGCM_MAX_ND], s_dbk64[JGCM_MAX_ND];  // and in FP64 (the c_p T sums)
@@ -788,14 +774,15 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
     s_dbk64[q] = vc.dbk[q];
   }
   __syncthreads();
-  const int i = blockIdx.x * 32 + (threadIdx.x & 31), ks = threadIdx.x >> 5, j = blockIdx.y, nd = a.nd;
-  const int e = blockIdx.z;  // member
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
+  const int lane = threadIdx.x & 31, ks = threadIdx.x >> 5, j = blockIdx.y, nd = a.nd;
+  const int i = blockIdx.x * 32 + lane, e = blockIdx.z;  // e: member
   const bool act = i < a.nlon;
   const size_t G = (size_t)a.nlat * a.nlon, col = (size_t)j * a.nlon + (act ? i : 0);
   const size_t offL = (size_t)e * nd * G, off1 = (size_t)e * G;
-  // the energy integrals sum_k E_k Δa_k, sum_k E_k Δb_k (E = |u|^2/2 + c_p T): the kinetic part in the
-  // state precision, the c_p T part (~99 %) as FP64 sums of the exact products T_k Δa_k, T_k Δb_k (the
-  // state precision's rounding of c_p T biased the energy correction by up to 1e-6 K per step)
+  // the energy integrals sum_k E_k Δa_k, sum_k E_k Δb_k: the kinetic part in the state precision,
+  // the c_p T part (~99 %) as FP64 sums of the exact products T_k Δa_k, T_k Δb_k (the state
+  // precision's rounding of c_p T biased the energy correction by up to 1e-6 K per step)
   __shared__ double part[2][KS][32];
   T ea = 0, eb = 0;
   double ta = 0, tb = 0;
@@ -812,75 +799,91 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
       tb += t * s_dbk64[k];
     }
   }
-  part[0][ks][threadIdx.x & 31] = (double)ea + a.cp * ta;
-  part[1][ks][threadIdx.x & 31] = (double)eb + a.cp * tb;
+  part[0][ks][lane] = (double)ea + a.cp * ta;
+  part[1][ks][lane] = (double)eb + a.cp * tb;
   __syncthreads();
-  // the column's level groups and the three sums over the block's columns in FP64, one warp each
-  // (FP64 runs at 1/64 of the FP32 rate: spread over three SM sub-partitions instead of one)
-  __shared__ double wsum[3];
+  // block values S0, S1, S2 (one warp each, on three sub-partitions): the level groups of each
+  // column, the butterfly over the columns, the row's weight
+  const int nb = gridDim.x * gridDim.y, bid = blockIdx.y * gridDim.x + blockIdx.x, ng = corr_groups(nb);
+  double* const pe = a.partials + e * a.pstride;
+  double* const bpart = pe + a.col_off;    // [3][nb]
+  double* const gpart = bpart + 3 * nb;    // [5][ng]
+  unsigned* const ctr = a.counter + (size_t)e * (ng + 1);
   if (ks < 3) {
-    const int c = threadIdx.x & 31;
     const T ps = act ? a.ps_n[off1 + col] : (T)0;
     double x;
     if (ks == 0) {
       x = (double)ps;
     } else {
       double sq = 0;
-      for (int q = 0; q < KS; q++) sq += part[ks - 1][q][c];
+      for (int q = 0; q < KS; q++) sq += part[ks - 1][q][lane];
       x = ks == 1 ? sq : sq * (double)ps;
     }
     x = warp_sum(x);
-    if (c == 0) wsum[ks] = x;
+    if (lane == 0) {
+      __stcg(bpart + (size_t)ks * nb + bid, x * a.wts[j]);
+      __threadfence();
+    }
+  }
+  // first level: the group's last block folds the group's block partials and its share of the
+  // column kernel's partials (S3, S4 weighted by their rows)
+  const int g = bid / CORR_GS, g0 = g * CORR_GS, gn = min(CORR_GS, nb - g0);
+  if (!ticket_last(ctr + g, (unsigned)gn)) return;
+  if (ks < 5) {
+    double x;
+    if (ks < 3) {
+      x = warp_fold(bpart + (size_t)ks * nb + g0, gn, lane);
+    } else {
+      const int per = (a.col_nb + ng - 1) / ng, q0 = g * per, q1 = min(a.col_nb, q0 + per);
+      const double* cp_ = pe + (size_t)(ks - 3) * a.col_nb;
+      double s = 0.0;
+      for (int q = q0 + lane; q < q1; q += 32) s += __ldcg(cp_ + q) * a.wts[q / a.col_gx];
+      x = warp_sum(s);
+    }
+    if (lane == 0) {
+      __stcg(gpart + (size_t)ks * ng + g, x);
+      __threadfence();
+    }
+  }
+  // second level: the last group's last block folds the group partials and applies the fixes
+  if (!ticket_last(ctr + ng, (unsigned)ng)) return;
+  __shared__ double S[5];
+  if (ks < 5) {
+    const double x = warp_fold(gpart + (size_t)ks * ng, ng, lane);
+    if (lane == 0) S[ks] = x;
   }
   __syncthreads();
-  double vals[3] = {wsum[0], wsum[1], wsum[2]};
-  double tot3[3];
-  __shared__ double fc[2];
   double* scal = a.scalars + 4 * e;
-  if (grid_reduce_last<3>(vals, a.partials + e * a.pstride + a.col_off, a.counter + e, a.wts, tot3)) {
-    // Compute_Corrections_Init: the previous level's mean ps and energy from the column kernel's
-    // partials (64-thread blocks of (nlon / (64 / S)) x nlat: 512 at T42 with S = 4)
-    double totc[2];
-    fold_weighted<2, 2>(a.partials + e * a.pstride, a.col_nb, a.col_gx, a.wts, totc);
-    // the mass factor first; then its logarithm (warp 0) and the energy correction (warp 1) side by
-    // side, each a chain of FP64 operations on its own sub-partition
-    __shared__ double s_tot[3];
-    if (threadIdx.x == 0) {
-      scal[0] = totc[0] * a.inv_2n;           // mean_ps_p   (Area_Weighted_Global_Mean)
-      scal[1] = totc[1] * a.inv_2n / a.grav;  // mean_energy_p (Mass_Weighted_Global_Integral)
-      double factor = 1.0;
-      if (a.do_mass) factor = scal[0] / (tot3[0] * a.inv_2n);  // mean_ps_p / mean_ps_n
-      fc[0] = factor;
-      s_tot[1] = tot3[1];
-      s_tot[2] = tot3[2];
-      scal[2] = factor;
-      a.scal_t[2 * e] = (T)factor;
-    }
-    __syncthreads();
-    const double factor = fc[0];
-    if (threadIdx.x == 0 && a.do_mass) {
+  __shared__ double s_corr;
+  // warp 0: the mass factor and spe_lnps_n(0,0) += log(factor); warp 1 (another sub-partition):
+  // the same factor and the energy correction; warp 2: the two means, off the critical path
+  if (ks == 0 && lane == 0) {
+    const double factor = a.do_mass ? S[3] / S[0] : 1.0;
+    scal[2] = factor;
+    a.scal_t[2 * e] = (T)factor;
+    if (a.do_mass) {
       V2<T> l = a.lnps_n[e];  // spe_lnps_n[1,1,1] += log(factor)  (P_00 = 1)
-      l.x = (T)((double)l.x + log(factor));
+      l.x = (T)((double)l.x + log_near_one(factor));
       a.lnps_n[e] = l;
     }
-    if (threadIdx.x == 32) {
-      double corr = 0.0;
-      if (a.do_energy) {
-        // Δp_k = Δa_k + Δb_k (factor ps_n): the mass correction enters linearly
-        const double mean_ps_p = scal[0], mean_energy_p = scal[1];
-        const double mean_energy_n = (s_tot[1] + factor * s_tot[2]) * a.inv_2n / a.grav;
-        corr = a.grav * (mean_energy_p - mean_energy_n) / (a.cp * mean_ps_p);
-      }
-      scal[3] = corr;
-      a.scal_t[2 * e + 1] = (T)corr;
-      fc[1] = corr;
+  } else if (ks == 1 && lane == 0) {
+    double corr = 0.0;
+    if (a.do_energy) {
+      const double factor = a.do_mass ? S[3] / S[0] : 1.0;
+      corr = fma(-factor, S[2], S[4] - S[1]) / (a.cp * S[3]);
     }
-    __syncthreads();
-    if (a.do_energy && (int)threadIdx.x < nd) {  // spe_t_n[1,1,:] .+= temperature_correction
-      V2<T> tt = a.t_spec_n[e * nd + threadIdx.x];
-      tt.x = (T)((double)tt.x + fc[1]);
-      a.t_spec_n[e * nd + threadIdx.x] = tt;
-    }
+    scal[3] = corr;
+    a.scal_t[2 * e + 1] = (T)corr;
+    s_corr = corr;
+  } else if (ks == 2 && lane == 0) {
+    scal[0] = S[3] * a.inv_2n;           // mean_ps_p   (Area_Weighted_Global_Mean)
+    scal[1] = S[4] * a.inv_2n / a.grav;  // mean_energy_p (Mass_Weighted_Global_Integral)
+  }
+  __syncthreads();
+  if (a.do_energy && (int)threadIdx.x < nd) {  // spe_t_n[1,1,:] .+= temperature_correction
+    V2<T> tt = a.t_spec_n[e * nd + threadIdx.x];
+    tt.x = (T)((double)tt.x + s_corr);
+    a.t_spec_n[e * nd + threadIdx.x] = tt;
   }
 }
 
@@ -1203,9 +1206,6 @@ void model_free(jgcm_model* md) {
   for (auto p : ps)
     if (p) cudaFree(p);
   delete[] md->div_mat;
-  if (md->ev_fork) cudaEventDestroy(md->ev_fork);
-  if (md->ev_join) cudaEventDestroy(md->ev_join);
-  if (md->side) cudaStreamDestroy(md->side);
   if (md->ev0) cudaEventDestroy(md->ev0);
   if (md->ev1) cudaEventDestroy(md->ev1);
   delete md;
@@ -1247,7 +1247,12 @@ int build_wave(jgcm_model* md) {
 // (S <= 8) first, then the fixer kernel's 3 sums over (nlon/32) x nlat blocks (both live until the
 // fixer's last block has folded them)
 size_t col_partials(const jgcm_mesh* m) { return (size_t)2 * ((m->nlon + HS_CT / 8 - 1) / (HS_CT / 8)) * m->nlat; }
-size_t partial_stride(const jgcm_mesh* m) { return col_partials(m) + (size_t)3 * ((m->nlon + 31) / 32) * m->nlat; }
+size_t partial_stride(const jgcm_mesh* m) {
+  const int nb = ((m->nlon + 31) / 32) * m->nlat;  // the fixer reduction's blocks per member
+  return col_partials(m) + (size_t)3 * nb + (size_t)5 * corr_groups(nb);
+}
+// the fixer reduction's tickets per member
+inline size_t corr_tickets(const jgcm_mesh* m) { return (size_t)corr_groups(((m->nlon + 31) / 32) * m->nlat) + 1; }
 
 int model_alloc(jgcm_model* md) {
   jgcm_mesh* m = md->mesh;
@@ -1255,7 +1260,9 @@ int model_alloc(jgcm_model* md) {
   const size_t ts = tsize(m);
   const size_t S = spec_elems(m, L) * 2 * ts, S1 = spec_elems(m, ne) * 2 * ts;
   const size_t G = grid_elems(m, L) * ts, G1 = grid_elems(m, ne) * ts;
-  md->fcap = (5 * nd + 2) * ne;
+  // the widest plan: Held-Suarez's synthesis of vor, div, u, v, T, ln ps and the next step's
+  // gradients of ln ps and T (7 nd + 3 columns per member)
+  md->fcap = (7 * nd + 3) * ne;
   JG_TRY(alloc(&md->fbuf, (size_t)(N + 1) * m->nlat * md->fcap * 2 * ts));
   for (int i = 0; i < 3; i++) {
     JG_TRY(alloc(&md->spe_vor[i], S));
@@ -1288,7 +1295,7 @@ int model_alloc(jgcm_model* md) {
   JG_TRY(alloc((void**)&md->d_partials, (size_t)ne * partial_stride(m) * 8));
   // 4 FP64 scalars per member, then each member's factor and correction in the state precision
   JG_TRY(alloc((void**)&md->d_scalars, (size_t)6 * ne * 8));
-  JG_TRY(alloc((void**)&md->d_counter, (size_t)ne * sizeof(unsigned)));
+  JG_TRY(alloc((void**)&md->d_counter, (size_t)ne * corr_tickets(m) * sizeof(unsigned)));
   int nt = (N + 1) * (ns + 1);
   JG_TRY(alloc(&md->dfac[0], (size_t)nt * ts));
   JG_TRY(alloc(&md->dfac[1], (size_t)nt * ts));
@@ -1310,9 +1317,6 @@ int model_alloc(jgcm_model* md) {
   JG_CUDA(cudaGetLastError());
   JG_CUDA(cudaEventCreate(&md->ev0));
   JG_CUDA(cudaEventCreate(&md->ev1));
-  JG_CUDA(cudaEventCreateWithFlags(&md->ev_fork, cudaEventDisableTiming));
-  JG_CUDA(cudaEventCreateWithFlags(&md->ev_join, cudaEventDisableTiming));
-  JG_CUDA(cudaStreamCreateWithFlags(&md->side, cudaStreamNonBlocking));
   md->div_mat = new double[nd * nd]();
   vertical_setup(md);
   JG_TRY(alloc((void**)&md->d_vc, sizeof(VertCoef)));
@@ -1539,16 +1543,15 @@ int issue_diag(jgcm_model* md, int lev, cudaStream_t st) {
 }
 
 // Gradients (cos θ ∇ / cos θ) of ln ps and T of time level `lev` into g_dlps, g_dtps, g_dlT, g_dtT
-// (Compute_Gradients!, Spectral_Spherical_Mesh.jl:721-741).  They read no (0,0) spectral mode (its
-// coefficients m/a and (n-1) ε_n/a vanish), so they may run while the fixers adjust those modes.
+// (Compute_Gradients!, Spectral_Spherical_Mesh.jl:721-741), and on the FP32 path T less its level
+// means (g_tdev, the column kernel's geopotential), for a state that no step synthesised (the
+// first step from a state set on the host; a step's own synthesis writes them for the next one).
 template <typename T>
-int issue_hs_grad(jgcm_model* md, int lev, cudaStream_t st, bool with_anom = true) {
+int issue_hs_grad(jgcm_model* md, int lev, cudaStream_t st) {
   const int L = md->L, E = md->ne;
   S2GPlan sp;
   memset(&sp, 0, sizeof(sp));
-  // FP32: also T less its level means for the column kernel's geopotential (S2G_ANOM), unless the
-  // step's own synthesis of the level wrote it (EPI_ANOM)
-  const bool anom = std::is_same<T, float>::value && with_anom;
+  const bool anom = std::is_same<T, float>::value;
   sp.ng = anom ? 5 : 4;
   sp.C = 2 * E + (anom ? 3 : 2) * L;
   sp.g[0] = sg(S2G_DLAM, md->spe_lnps[lev], nullptr, E, 0);
@@ -1697,11 +1700,14 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
     JG_CUDA(launch_pdl(k_hs_implicit<T, T>, dim3((md->npairs + 3) / 4, E), 128, 0, st, ia, md->d_vc));
   mark(st);
   JG_CUDA(cudaGetLastError());
-  // 5. back to the grid: vor, div, u, v, T, lnps (+ ps = exp(lnps))
+  // 5. back to the grid: vor, div, u, v, T, lnps (+ ps = exp(lnps)), and the next step's gradients
+  //    of ln ps and T (Compute_Gradients!, Spectral_Spherical_Mesh.jl:721-741): they read no (0,0)
+  //    mode (its coefficients m/a and (n-1) ε_n/a vanish), so the fixers' later shifts of those
+  //    modes leave them unchanged
   S2GPlan s2;
   memset(&s2, 0, sizeof(s2));
-  s2.ng = 6;
-  s2.C = 5 * L + E;
+  s2.ng = 10;
+  s2.C = 7 * L + 3 * E;
   s2.g[0] = sg(S2G_PLAIN, md->spe_vor[n], nullptr, L, 0);
   s2.g[1] = sg(S2G_PLAIN, md->spe_div[n], nullptr, L, L);
   s2.g[2] = sg(S2G_UCOS, md->spe_vor[n], md->spe_div[n], L, 2 * L);
@@ -1714,10 +1720,14 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   // epilogue, so its rounding scales with |ln(ps / 1e5)| ~ 0.02 instead of ln ps ~ 11.5
   s2.g[5] = sg(S2G_PLAIN, md->spe_lnps[n], nullptr, E, 5 * L);
   s2.g[5].shift = kLnPsRef;
+  s2.g[6] = sg(S2G_DLAM, md->spe_lnps[n], nullptr, E, 5 * L + E);
+  s2.g[7] = sg(S2G_DTH, md->spe_lnps[n], nullptr, E, 5 * L + 2 * E);
+  s2.g[8] = sg(S2G_DLAM, md->spe_t[n], nullptr, L, 5 * L + 3 * E);
+  s2.g[9] = sg(S2G_DTH, md->spe_t[n], nullptr, L, 6 * L + 3 * E);
   IFFTPlan i2;
   memset(&i2, 0, sizeof(i2));
-  i2.ng = 6;
-  i2.C = 5 * L + E;
+  i2.ng = s2.ng;
+  i2.C = s2.C;
   i2.g[0] = og(EPI_NONE, md->grid_vor, L, 0);
   i2.g[1] = og(EPI_NONE, md->grid_div, L, L);
   i2.g[2] = og(EPI_DIVCOS, md->grid_u[n], L, 2 * L);
@@ -1726,6 +1736,10 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   i2.g[4].ps = anom ? md->spe_t[n] : nullptr;
   i2.g[5] = og(EPI_EXP2, md->grid_lnps, E, 5 * L, md->grid_ps[n]);
   i2.g[5].shift = kLnPsRef;
+  i2.g[6] = og(EPI_DIVCOS, md->g_dlps, E, 5 * L + E);
+  i2.g[7] = og(EPI_DIVCOS, md->g_dtps, E, 5 * L + 2 * E);
+  i2.g[8] = og(EPI_DIVCOS, md->g_dlT, L, 5 * L + 3 * E);
+  i2.g[9] = og(EPI_DIVCOS, md->g_dtT, L, 6 * L + 3 * E);
   JG_TRY(launch_s2g<T>(m, s2, i2, st, md->fbuf, md->fcap));
   // 6. mass and energy fixers
   CorrArgs<T> ca;
@@ -1755,13 +1769,6 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ca.inv_2n = 0.5 / m->nlon;
   ca.cp_t = (T)md->cp_air;
   ca.has_dak = has_dak(md);
-  // the fixers (this branch) and the next step's gradients of the new level (second branch)
-  const bool serial = g_marker != nullptr;  // per-kernel timing: one stream, launches in order
-  cudaStream_t br = serial ? st : md->side;
-  if (!serial) {
-    JG_CUDA(cudaEventRecord(md->ev_fork, st));
-    JG_CUDA(cudaStreamWaitEvent(br, md->ev_fork, 0));
-  }
   JG_CUDA(launch_pdl(k_hs_corr_reduce<T>, dim3((m->nlon + 31) / 32, m->nlat, E), 256, 0, st, ca, md->d_vc));
   mark(st);
   JG_CUDA(cudaGetLastError());
@@ -1772,12 +1779,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
                      (const T*)(md->d_scalars + 4 * E), (size_t)nd * G1, G1));
   mark(st);
   JG_CUDA(cudaGetLastError());
-  JG_TRY(issue_hs_grad<T>(md, n, br, false));
-  if (md->diag_on && !serial) JG_TRY(issue_diag<T>(md, n, st));  // the new state, after the fixers
-  if (!serial) {
-    JG_CUDA(cudaEventRecord(md->ev_join, br));
-    JG_CUDA(cudaStreamWaitEvent(st, md->ev_join, 0));
-  }
+  if (md->diag_on && g_marker == nullptr) JG_TRY(issue_diag<T>(md, n, st));  // the new state, after the fixers
   return JGCM_OK;
 }
 
@@ -2091,7 +2093,7 @@ extern "C" int jgcm_model_update_init_step(jgcm_model* md) {
 }
 
 static int launches_per_step(const jgcm_model* md) {
-  return md->P.kind == JGCM_BAROTROPIC ? 4 : md->P.kind == JGCM_SHALLOW_WATER ? 6 : 10;
+  return md->P.kind == JGCM_BAROTROPIC ? 4 : md->P.kind == JGCM_SHALLOW_WATER ? 6 : 8;
 }
 
 extern "C" int jgcm_model_launches_per_step(jgcm_model* md, int* launches) {
@@ -2103,8 +2105,8 @@ extern "C" int jgcm_model_launches_per_step(jgcm_model* md, int* launches) {
 extern "C" int jgcm_model_kernel_name(jgcm_model* md, int slot, char* buf, int cap) {
   JG_ARG(md && buf && cap > 0, "bad arguments");
   static const char* hs[] = {"hs_column", "fft(tendencies)", "g2s_legendre(vor,div,T,lnps)", "hs_implicit",
-                             "s2g_legendre(vor,div,u,v,T,lnps)", "ifft(vor,div,u,v,T,lnps)", "hs_corr_reduce",
-                             "hs_corr_apply", "s2g_legendre(grad lnps,T)", "ifft(grad lnps,T)"};
+                             "s2g_legendre(vor,div,u,v,T,lnps,grad lnps,grad T)",
+                             "ifft(vor,div,u,v,T,lnps,grad lnps,grad T)", "hs_corr_reduce", "hs_corr_apply"};
   static const char* bt[] = {"fft(flux)", "g2s_legendre(vor+leapfrog)", "s2g_legendre(vor,u,v)", "ifft(vor,u,v)"};
   static const char* sw[] = {"s2g_legendre(grad h)", "ifft(grad h)", "fft(fluxes,kin,dh)",
                              "g2s_legendre(vor,div,h+implicit+leapfrog)", "s2g_legendre(vor,div,h,u,v)",
