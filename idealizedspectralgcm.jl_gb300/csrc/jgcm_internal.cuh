@@ -257,6 +257,7 @@ struct jgcm_mesh {
   int tune_gen;            // bumped when the tiles change: captured graphs of the mesh's models are stale
   int simt_legendre;       // tensor-core precision modes: 1 = run the Legendre contractions on the FP32
                            // SIMT kernels instead (chosen by the autotuner where they are faster)
+  int hs_levels;           // levels per block of the Held-Suarez analysis kernel (0 = default)
   // workspace
   int Cmax;
   void* d_fbuf;       // Fourier buffer [m][j][c] complex T, c < Cmax
@@ -350,6 +351,14 @@ int launch_g2s_legendre_tc(jgcm_mesh* m, const G2SPlan& gp, int Cin, cudaStream_
 int tc_status(jgcm_mesh* m);  // reads and clears the device error bits
 
 size_t simt_smem_need(const jgcm_mesh* m, int s2g, int g2s, int fft);
+
+// hs_transforms.cu: the Held-Suarez step's analysis as one contraction per (m pair, level group,
+// member); the forward FFT of the plan first
+bool hs_analysis_fits(const jgcm_mesh* m, int nd, int E);
+int hs_analysis_levels(const jgcm_mesh* m, int nd, int E);
+template <typename T>
+int launch_hs_analysis(jgcm_mesh* m, const FFTPlan& fp, int colU, int colV, int colE, int colT, int colP, int nd,
+                       int E, void* dvor, void* ddiv, void* dt, void* dlnps, cudaStream_t st, void* fbuf, int cap);
 
 // mesh.cu
 int mesh_build_tables(jgcm_mesh* m);

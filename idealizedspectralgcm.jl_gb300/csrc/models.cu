@@ -1658,7 +1658,11 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   gp.g[1] = og2(G2S_DIV, md->spe_ddiv, L, L, 0, L, 3 * L);
   gp.g[2] = og2(G2S_PLAIN, md->spe_dt, L, 2 * L, 2 * L, -1, -1);
   gp.g[3] = og2(G2S_PLAIN, md->spe_dlnps, E, 3 * L, 4 * L, -1, -1);
-  JG_TRY(launch_g2s<T>(m, fp, gp, st, md->fbuf, md->fcap));
+  if (hs_analysis_fits(m, nd, E))  // the same outputs, one thread per (m, n, level)
+    JG_TRY(launch_hs_analysis<T>(m, fp, 0, L, 3 * L, 2 * L, 4 * L, nd, E, md->spe_dvor, md->spe_ddiv, md->spe_dt,
+                                 md->spe_dlnps, st, md->fbuf, md->fcap));
+  else
+    JG_TRY(launch_g2s<T>(m, fp, gp, st, md->fbuf, md->fcap));
   // 4. semi-implicit correction, damping, leapfrog (FP64, warp per mode)
   ImplArgs<T> ia;
   memset(&ia, 0, sizeof(ia));
@@ -2864,12 +2868,14 @@ extern "C" int jgcm_ensemble_destroy(jgcm_ensemble* en) {
 // ------------------------------------------------------------------------------------------
 // Tiles and their autotuner.  Knobs: [0] lanes per column of the Held-Suarez column kernel
 // (model), [1] S2G columns, [2] G2S columns, [3] FFT columns per block of the SIMT transform
-// kernels (mesh: shared by the models of the mesh).  0 keeps the default.
+// kernels, [4] the Legendre engine of the tensor-core modes, [5] levels per block of the
+// Held-Suarez analysis (mesh: shared by the models of the mesh).  0 keeps the default.
 extern "C" int jgcm_model_get_tuning(jgcm_model* md, int* knobs, int n) {
   JG_ARG(md && knobs && n >= 4, "need 4 knobs");
   knobs[0] = md->hs_lanes;
   for (int i = 1; i < 4; i++) knobs[i] = md->mesh->tune[i];
   if (n >= 5) knobs[4] = md->mesh->simt_legendre;
+  if (n >= 6) knobs[5] = md->mesh->hs_levels;
   return JGCM_OK;
 }
 
@@ -2896,11 +2902,17 @@ extern "C" int jgcm_model_set_tuning(jgcm_model* md, const int* knobs, int n) {
     JG_ARG(knobs[4] == 0 || knobs[4] == 1, "Legendre engine knob must be 0 (tensor cores) or 1 (SIMT)");
     simt = m->tc.on ? knobs[4] : 0;  // meaningful for the tensor-core precision modes only
   }
-  bool changed = simt != m->simt_legendre;
+  int hsl = m->hs_levels;
+  if (n >= 6) {
+    JG_ARG(knobs[5] >= -1 && knobs[5] <= 256, "analysis levels per block out of range");
+    hsl = knobs[5];
+  }
+  bool changed = simt != m->simt_legendre || hsl != m->hs_levels;
   for (int i = 1; i < 4; i++) changed = changed || m->tune[i] != t[i];
   if (changed) {
     for (int i = 1; i < 4; i++) m->tune[i] = t[i];
     m->simt_legendre = simt;
+    m->hs_levels = hsl;
     m->tune_gen++;
   }
   return JGCM_OK;
@@ -2923,10 +2935,10 @@ extern "C" int jgcm_model_autotune(jgcm_model* md, int nsteps, int* knobs_out, i
   sc->sw_adv_from_n = md->sw_adv_from_n;
   for (int e = 0; e < md->ne; e++) JG_TRY(jgcm_model_copy_member(sc, e, md, e));
   if (sc->init_step || sc->sw_adv_from_n) JG_TRY(jgcm_model_step(sc, 1));
-  int cur[5];
-  JG_TRY(jgcm_model_get_tuning(md, cur, 5));
+  int cur[6];
+  JG_TRY(jgcm_model_get_tuning(md, cur, 6));
   auto timed = [&](const int* k, float* ms) -> int {
-    JG_TRY(jgcm_model_set_tuning(sc, k, 5));
+    JG_TRY(jgcm_model_set_tuning(sc, k, 6));
     JG_TRY(jgcm_model_step(sc, 3));  // captures the three rotation phases
     return jgcm_model_time_steps(sc, nsteps, ms);
   };
@@ -2936,13 +2948,18 @@ extern "C" int jgcm_model_autotune(jgcm_model* md, int nsteps, int* knobs_out, i
             d3 = m->nlon >= 1024 ? 1 : 1024 / m->nlon;
   std::vector<std::vector<int>> cand = {
       {1, 2, 4, 8}, {std::max(1, d1 / 2), d1, 2 * d1, 4 * d1}, {4, 8, 16, 32}, {std::max(1, d3 / 2), d3, 2 * d3},
-      {0, 1}};
+      {0, 1}, {}};
   if (md->P.kind != JGCM_HELD_SUAREZ) cand[0] = {cur[0]};
   if (!m->tc.on) cand[4] = {cur[4]};  // the Legendre engine: tensor cores or SIMT (tensor-core modes)
+  // levels per block of the Held-Suarez analysis kernel: 0 (default) and 1 .. what a block holds
+  if (md->P.kind == JGCM_HELD_SUAREZ)
+    for (int v : {0, -1, 1, 2, 3, 4, 5, 6, 8, 10})
+      if (v <= 256 / (m->N + 4)) cand[5].push_back(v);
+  if (cand[5].empty()) cand[5] = {cur[5]};
   // the Legendre engine first: the SIMT tiles searched next only matter once the engine is known
-  for (int knob : {4, 0, 1, 2, 3})
+  for (int knob : {4, 0, 1, 2, 3, 5})
     for (int v : cand[knob]) {
-      int k[5] = {cur[0], cur[1], cur[2], cur[3], cur[4]};
+      int k[6] = {cur[0], cur[1], cur[2], cur[3], cur[4], cur[5]};
       k[knob] = v;
       if (knob == 1 && v == d1) k[1] = 0;
       if (knob == 2 && v == d2) k[2] = 0;
@@ -2955,12 +2972,12 @@ extern "C" int jgcm_model_autotune(jgcm_model* md, int nsteps, int* knobs_out, i
       if (timed(k, &ms) != JGCM_OK) continue;
       if (ms < best) {
         best = ms;
-        for (int i = 0; i < 5; i++) cur[i] = k[i];
+        for (int i = 0; i < 6; i++) cur[i] = k[i];
       }
     }
-  JG_TRY(jgcm_model_set_tuning(md, cur, 5));
+  JG_TRY(jgcm_model_set_tuning(md, cur, 6));
   if (knobs_out)
-    for (int i = 0; i < std::min(n, 5); i++) knobs_out[i] = cur[i];
+    for (int i = 0; i < std::min(n, 6); i++) knobs_out[i] = cur[i];
   if (ms_out) *ms_out = best;
   return JGCM_OK;
 }

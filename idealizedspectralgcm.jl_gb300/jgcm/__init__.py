@@ -566,7 +566,7 @@ class Ensemble:
             pass
 
 
-TUNING_KNOBS = ("lanes_per_column", "s2g_columns", "g2s_columns", "fft_columns", "simt_legendre")
+TUNING_KNOBS = ("lanes_per_column", "s2g_columns", "g2s_columns", "fft_columns", "simt_legendre", "hs_analysis_levels")
 
 
 def write_arrays(path, arrays, meta=None):
@@ -604,14 +604,14 @@ def read_arrays(path):
 
 
 def get_tuning(model):
-    k = (C.c_int * 5)()
-    _check(lib().jgcm_model_get_tuning(model._h, k, 5))
+    k = (C.c_int * 6)()
+    _check(lib().jgcm_model_get_tuning(model._h, k, 6))
     return dict(zip(TUNING_KNOBS, list(k)))
 
 
 def set_tuning(model, tuning):
-    k = (C.c_int * 5)(*[int(tuning.get(n, 0)) for n in TUNING_KNOBS])
-    _check(lib().jgcm_model_set_tuning(model._h, k, 5))
+    k = (C.c_int * 6)(*[int(tuning.get(n, 0)) for n in TUNING_KNOBS])
+    _check(lib().jgcm_model_set_tuning(model._h, k, 6))
 
 
 def autotune(model, nsteps=24, cache=None):
@@ -631,9 +631,9 @@ def autotune(model, nsteps=24, cache=None):
     if key in table:
         set_tuning(model, table[key]["tuning"])
         return table[key]
-    k = (C.c_int * 5)()
+    k = (C.c_int * 6)()
     ms = C.c_float()
-    _check(lib().jgcm_model_autotune(model._h, int(nsteps), k, 5, C.byref(ms)))
+    _check(lib().jgcm_model_autotune(model._h, int(nsteps), k, 6, C.byref(ms)))
     entry = {"tuning": dict(zip(TUNING_KNOBS, list(k))), "ms_per_step": float(ms.value) / nsteps}
     if cache:
         table[key] = entry

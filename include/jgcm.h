@@ -226,9 +226,10 @@ int jgcm_model_read_diagnostics(jgcm_model* model, const char* name, double* out
  * transform kernels (the mesh: shared by its models).  0 = default; knobs[3] = -1 puts FP32 rows of
  * nlon 64 or 128 one per thread whatever their number (by default from 19456 rows on: nlon 64, and the inverse at nlon 128).  knobs[4] (read and written when
  * n >= 5): the Legendre engine of a tensor-core precision mode (0 tcgen05, 1 the FP32 SIMT
- * kernels; the mesh).  The autotuner times candidates on a scratch copy of the model (coordinate
+ * kernels; the mesh).  knobs[5] (n >= 6): levels per block of the Held-Suarez analysis kernel (the
+ * mesh; 0 = default, -1 = the general analysis kernel instead).  The autotuner times candidates on a scratch copy of the model (coordinate
  * search, nsteps captured steps each), applies the fastest, writes it to knobs (nullable; the first
- * min(n, 5) knobs, n >= 4, like jgcm_model_get_tuning) and its time per nsteps to ms (nullable). */
+ * min(n, 6) knobs, n >= 4, like jgcm_model_get_tuning) and its time per nsteps to ms (nullable). */
 int jgcm_model_get_tuning(jgcm_model* model, int* knobs, int n);
 int jgcm_model_set_tuning(jgcm_model* model, const int* knobs, int n);
 int jgcm_model_autotune(jgcm_model* model, int nsteps, int* knobs, int n, float* ms);

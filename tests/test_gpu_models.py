@@ -132,6 +132,49 @@ def test_held_suarez_steps(jg, orc, name, prec, tol):
         assert configs.rel_l2(gmod.get(f), omod.get(f)) < (tol if prec == "fp64" else 1e-5), f
 
 
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp32", 2e-5)])
+@pytest.mark.parametrize("name,members", [("hs_t42l20", 1), ("hs_t21l20", 3)])
+def test_held_suarez_analysis_kernel_matches_general(jg, orc, name, members, prec, tol):
+    """The Held-Suarez analysis kernel (one thread per (m, n, level), m pairs, tuning knob
+    hs_analysis_levels) gives the general analysis kernel's steps (knob -1) at every levels-per-block
+    setting, for one member and for a member ensemble.  The two sum the same products in a
+    different order, so they agree to rounding (FP64 1e-12, FP32 2e-5 relative L2 after 3 steps;
+    the FP32 bound is the dynamics' conditioning, as in MIXED_TOL)."""
+    params = configs.PARAMS[name]
+    om = configs.make_mesh(orc, name)
+    omod = orc.Model(om, params)
+    omod.spectral_initialize_fields(configs.hs_temperature_noise(om), True)
+    configs.add_hs_flow(orc, om, omod)
+
+    def run(levels):
+        gm = configs.make_mesh(jg, name, precision=prec)
+        one = jg.Model(gm, params)
+        configs.copy_state(omod, one, "held_suarez")
+        md = jg.Model(gm, params, members=members)
+        for e in range(members):
+            md.copy_member(e, one, 0)
+        jg.set_tuning(md, dict(jg.get_tuning(md), hs_analysis_levels=levels))
+        assert jg.get_tuning(md)["hs_analysis_levels"] == levels
+        md.step(3)
+        out = jg.Model(gm, params)
+        fields = {}
+        for e in range(members):
+            out.copy_member(0, md, e)
+            fields[e] = {f: out.get(f) for f in ("spe_vor_c", "spe_div_c", "spe_t_c", "spe_lnps_c", "grid_u_c")}
+        return fields
+
+    ref = run(-1)
+    for levels in (0, 1, 2, 5):
+        got = run(levels)
+        for e in range(members):
+            for f, a in got[e].items():
+                err = configs.rel_l2(a, ref[e][f])
+                assert err < tol, (levels, e, f, err)
+    if members > 1:  # identical members stay identical
+        for f, a in got[1].items():
+            assert np.array_equal(a, got[0][f]), f
+
+
 @pytest.mark.parametrize("name,option", configs.VERT_COORD_CASES)
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("fp32", MIXED_TOL["fp32"])])
 def test_held_suarez_vert_coords(jg, orc, name, option, prec, tol):
