@@ -238,14 +238,15 @@ PerDeviceOnce g_hs_ana_smem[2];
 }  // namespace
 
 // levels per block of the Held-Suarez analysis: the tuned value when set (clamped to what a block
-// of 256 threads holds), else enough blocks for two per SM
+// of 256 threads holds), else as many as a block holds (HS T42L20, one member: 5 levels 5.5 us,
+// 2 levels 7.1 us, 1 level 7.6 us per step in a captured graph)
 int hs_analysis_levels(const jgcm_mesh* m, int nd, int E) {
+  (void)nd;
+  (void)E;
   const int lg_max = 256 / (m->N + 4);
   if (lg_max < 1) return 0;
   if (m->hs_levels > 0) return std::min(m->hs_levels, lg_max);
-  const long pairs = m->N / 2 + 1;
-  long lg = (pairs * (nd + 1) * (long)E + 2L * m->sm_count - 1) / (2L * m->sm_count);
-  return (int)std::max(1L, std::min((long)lg_max, lg));
+  return lg_max;
 }
 
 // The Held-Suarez analysis kernel serves this mesh: not tuned away (levels per block -1), SIMT

@@ -868,10 +868,9 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
     }
   } else if (ks == 1 && lane == 0) {
     double corr = 0.0;
-    if (a.do_energy) {
-      const double factor = a.do_mass ? S[3] / S[0] : 1.0;
-      corr = fma(-factor, S[2], S[4] - S[1]) / (a.cp * S[3]);
-    }
+    if (a.do_energy)  // one division on this warp's chain: factor S2 = S3 S2 / S0
+      corr = a.do_mass ? fma(-S[3], S[2], S[0] * (S[4] - S[1])) / ((a.cp * S[3]) * S[0])
+                       : (S[4] - S[1] - S[2]) / (a.cp * S[3]);
     scal[3] = corr;
     a.scal_t[2 * e + 1] = (T)corr;
     s_corr = corr;
