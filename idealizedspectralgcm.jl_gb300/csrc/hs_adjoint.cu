@@ -1078,6 +1078,7 @@ int check_model(jgcm_model* md) {
   JG_ARG(!md->diag_on, "switch the on-device diagnostics off before differentiating");
   // the reverse column kernel reads the sigma coordinates' per-level log-pressure constants
   JG_ARG(!md->vc.hybrid, "the step adjoint is built for sigma coordinates (a_k = 0), not hybrid ones");
+  JG_ARG(md->nq == 0, "the step adjoint does not differentiate passive tracers: a model without tracers");
   return JGCM_OK;
 }
 

@@ -20,7 +20,7 @@
 
 #include "jgcm.h"
 
-#define JGCM_MAX_GROUPS 12
+#define JGCM_MAX_GROUPS 16
 #define JGCM_MAX_ND 64
 #define JGCM_MAX_DEVICES 64
 

@@ -68,6 +68,13 @@ struct jgcm_model {
   double *d_partials, *d_scalars;
   unsigned* d_counter;
   double* state_stage;  // FP64 staging of the packed host state (jgcm_model_set_state / get_state)
+  // passive tracers (jgcm_model_add_tracers; Dyn_Data.jl:36-39,63-66), advected like T: nq per
+  // member, columns member-major, then tracer, then level ((e nq + i) nd + k), LQ = ne nq nd
+  int nq, LQ;
+  void *spe_q[3], *grid_q[3];
+  void *spe_dq, *g_dq, *g_dlq, *g_dtq;  // tendency (spectral, grid), gradients of the c level (÷ cos)
+  void* g_mhalf;                        // the column kernel's mass flux M_{k+1/2} at level index k
+  double* q_stage;                      // FP64 staging of one tracer field (get / set by name)
   void* adj;            // workspace of jgcm_model_hs_gradient, kept between calls (hs_adjoint.cu)
   cudaGraphExec_t graph[3];   // one steady step, per rotation phase
   cudaGraphExec_t graph3[3];  // three steady steps (a whole rotation), per starting phase

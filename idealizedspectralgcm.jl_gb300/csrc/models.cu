@@ -138,6 +138,7 @@ struct HSColArgs {
   const T* tdev;  // T_c less its level means, synthesised as such (FP32 path); NULL: T_c - T0_k here
   int has_dak;    // some a_k differs between levels (hybrid coordinates): the energy sums need sum_k T_k Δa_k
   T *ducos, *dvcos, *dtg, *energy, *dlnps, *t_eq;
+  T* m_half;            // tracers: M_{k+1/2} at level index k (NULL: not stored)
   const V2<T>* t_spec;  // spe_t_c: its (0,0) modes are the level means of T
   const double* wts;
   double* partials;  // per member: partials + e * pstride (the block partials of mean ps_p, energy_p)
@@ -393,6 +394,7 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
       dt = dt + kap * t * x5;
       // M_{k+1/2} = -sum_{r<=k} D_r + B_{k+1/2} sum_r D_r, zero at the surface
       const T Mhi = below ? -incl + tot * s_bk[k + 1] : (T)0;
+      if (a.m_half) a.m_half[cL + x] = Mhi;
       // Vert_Advection! (second_centered_wts): flux at k+1/2 with weight dp_k / (dp_k + dp_{k+1})
       const T w1 = dp / (dp + dp1);
       const T fhu = below ? Mhi * (u + (u1 - u) * w1) : (T)0;
@@ -457,6 +459,60 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
   }
 }
 
+// Passive tracers, advected like T (the reference keeps spe_tracers / grid_tracers in Dyn_Data,
+// Dyn_Data.jl:36-39,63-66, and rotates them, but its Spectral_Dynamics! leaves "grid_q = grid_t" as
+// a todo, :235): per column and tracer, top-down, Vert_Advection! (second_centered_wts,
+// Vert_Coordinate.jl:171-210) with the column kernel's mass flux M_{k+1/2}, the flux at k+1/2
+// carried to the next level as for T, then Add_Horizontal_Advection! (Spectral_Spherical_Mesh.jl:
+// 694-718) with the synthesised gradients.  No forcing, no semi-implicit term.
+template <typename T>
+struct TracerArgs {
+  const T *u_c, *v_c, *ps_c, *q_c, *dlq, *dtq, *m_half;
+  T* dq;
+  int nd, nq, nlat, nlon;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_hs_tracers(TracerArgs<T> a, const VertCoef* __restrict__ vcp) {
+  const VertCoef& vc = *vcp;
+  __shared__ T s_dak[JGCM_MAX_ND], s_dbk[JGCM_MAX_ND];
+  const int nd = a.nd;
+  for (int q = threadIdx.x; q < nd; q += blockDim.x) {
+    s_dak[q] = (T)vc.dak[q];
+    s_dbk[q] = (T)vc.dbk[q];
+  }
+  __syncthreads();
+  pdl_wait();  // programmatic dependent launch: the column kernel's mass flux is complete
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, e = blockIdx.z;
+  if (i >= a.nlon) return;
+  const size_t G = (size_t)a.nlat * a.nlon, col = (size_t)j * a.nlon + i, cL = (size_t)e * nd * G + col;
+  const T ps = a.ps_c[(size_t)e * G + col];
+  for (int iq = 0; iq < a.nq; iq++) {
+    const size_t cQ = (size_t)(e * a.nq + iq) * nd * G + col;
+    T Mlo = 0, flq = 0, q = a.q_c[cQ], dp = s_dak[0] + s_dbk[0] * ps;
+    for (int k = 0; k < nd; k++) {
+      const size_t x = (size_t)k * G;
+      const bool below = k + 1 < nd;
+      T q1 = 0, dp1 = 1;
+      if (below) {
+        q1 = a.q_c[cQ + x + G];
+        dp1 = s_dak[k + 1] + s_dbk[k + 1] * ps;
+      }
+      const T rdp = (T)1 / dp;
+      const T Mhi = below ? a.m_half[cL + x] : (T)0;
+      const T w1 = dp / (dp + dp1);
+      const T fhq = below ? Mhi * (q + (q1 - q) * w1) : (T)0;
+      T d = (flq - fhq + q * (Mhi - Mlo)) * rdp;
+      d = d - (a.u_c[cL + x] * a.dlq[cQ + x] + a.v_c[cL + x] * a.dtq[cQ + x]);
+      a.dq[cQ + x] = d;
+      Mlo = Mhi;
+      flq = fhq;
+      q = q1;
+      dp = dp1;
+    }
+  }
+}
+
 // lanes per column for a launch: S = 4 for small grids (latency), 1 for large ensembles; the
 // autotuner may pick 8
 inline int hs_lanes(const jgcm_mesh* m, int ne, int nd) {
@@ -502,6 +558,10 @@ struct ImplArgs {
   // Laplacian eigenvalues in T
   const T* eig_t;
   T xi_t, rpsr_t, xipsr_t, kap_t, rg_t, rob_t;
+  // passive tracers: tendency, p/c/n levels (innermost index (e nq + i) nd + k of LQ = ne nq nd)
+  const V2<T>* dq;
+  V2<T> *q_p, *q_c, *q_n;
+  int nq, LQ;
 };
 
 template <typename T>
@@ -725,6 +785,18 @@ __global__ void __launch_bounds__(256) k_hs_implicit(ImplArgs<T> a, const VertCo
     o.x = (T)ln.x; o.y = (T)ln.y; a.lnps_n[s1] = o;
     o.x = (T)lc.x; o.y = (T)lc.y; a.lnps_c[s1] = o;
   }
+  // passive tracers: damping and the filtered leapfrog of T (Time_Integrator.jl:58-101)
+  if (live && act)
+    for (int iq = 0; iq < a.nq; iq++) {
+      const size_t sq = row * a.LQ + (size_t)(e * a.nq + iq) * nd + k;
+      const V2<T> g = a.dq[sq], qp0 = a.q_p[sq], qc0 = a.q_c[sq];
+      C dq = {(R)g.x, (R)g.y}, qp = {(R)qp0.x, (R)qp0.y}, qc = {(R)qc0.x, (R)qc0.y}, qn;
+      lf<R>(ini, Dt, rob, d, f, dq.x, qp.x, qc.x, qn.x);
+      lf<R>(ini, Dt, rob, d, f, dq.y, qp.y, qc.y, qn.y);
+      V2<T> o;
+      o.x = (T)qn.x; o.y = (T)qn.y; a.q_n[sq] = o;
+      o.x = (T)qc.x; o.y = (T)qc.y; a.q_c[sq] = o;
+    }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1197,6 +1269,12 @@ void model_free(jgcm_model* md) {
     if (md->graph3[i]) cudaGraphExecDestroy(md->graph3[i]);
     if (md->graph24[i]) cudaGraphExecDestroy(md->graph24[i]);
   }
+  for (int i = 0; i < 3; i++) {
+    if (md->spe_q[i]) cudaFree(md->spe_q[i]);
+    if (md->grid_q[i]) cudaFree(md->grid_q[i]);
+  }
+  for (void* p : {md->spe_dq, md->g_dq, md->g_dlq, md->g_dtq, md->g_mhalf, (void*)md->q_stage})
+    if (p) cudaFree(p);
   void* ps[] = {md->grid_vor, md->grid_div, md->grid_lnps, md->grid_t_eq, md->grid_geopots, md->grid_h_eq,
                 md->spe_zero, md->spe_dvor, md->spe_ddiv, md->spe_dlnps, md->spe_dt, md->g_dlps, md->g_dtps,
                 md->g_dlT, md->g_dtT, md->g_ducos, md->g_dvcos, md->g_dt, md->g_energy, md->g_dlnps, md->g_diag,
@@ -1567,6 +1645,16 @@ int issue_hs_grad(jgcm_model* md, int lev, cudaStream_t st) {
   ip.g[2] = og(EPI_DIVCOS, md->g_dlT, L, 2 * E);
   ip.g[3] = og(EPI_DIVCOS, md->g_dtT, L, 2 * E + L);
   if (anom) ip.g[4] = og(EPI_NONE, md->g_tdev, L, 2 * E + 2 * L);
+  if (md->nq) {  // and those of the tracers
+    const int LQ = md->LQ, c0 = sp.C;
+    sp.g[sp.ng] = sg(S2G_DLAM, md->spe_q[lev], nullptr, LQ, c0);
+    ip.g[sp.ng++] = og(EPI_DIVCOS, md->g_dlq, LQ, c0);
+    sp.g[sp.ng] = sg(S2G_DTH, md->spe_q[lev], nullptr, LQ, c0 + LQ);
+    ip.g[sp.ng++] = og(EPI_DIVCOS, md->g_dtq, LQ, c0 + LQ);
+    sp.C += 2 * LQ;
+    ip.ng = sp.ng;
+    ip.C = sp.C;
+  }
   return launch_s2g<T>(md->mesh, sp, ip, st, md->fbuf, md->fcap);
 }
 
@@ -1616,6 +1704,7 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   a.dlnps = (T*)md->g_dlnps;
   a.t_eq = (T*)md->grid_t_eq;
   a.t_spec = (const V2<T>*)md->spe_t[c];
+  a.m_half = md->nq ? (T*)md->g_mhalf : nullptr;
   a.wts = m->d_wts;
   a.partials = md->d_partials;
   a.nd = nd;
@@ -1638,6 +1727,24 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   JG_TRY(launch_hs_column<T>(a, m, E, md->hs_lanes, md->d_vc, md->vc.hybrid, st));
   mark(st);
   JG_CUDA(cudaGetLastError());
+  if (md->nq) {  // 2'. the tracers' tendencies
+    TracerArgs<T> ta;
+    ta.u_c = (const T*)md->grid_u[c];
+    ta.v_c = (const T*)md->grid_v[c];
+    ta.ps_c = (const T*)md->grid_ps[c];
+    ta.q_c = (const T*)md->grid_q[c];
+    ta.dlq = (const T*)md->g_dlq;
+    ta.dtq = (const T*)md->g_dtq;
+    ta.m_half = (const T*)md->g_mhalf;
+    ta.dq = (T*)md->g_dq;
+    ta.nd = nd;
+    ta.nq = md->nq;
+    ta.nlat = m->nlat;
+    ta.nlon = m->nlon;
+    JG_CUDA(launch_pdl(k_hs_tracers<T>, dim3((m->nlon + 127) / 128, m->nlat, E), 128, 0, st, ta, md->d_vc));
+    mark(st);
+    JG_CUDA(cudaGetLastError());
+  }
   // 3. forward transforms: δu cos, δv cos, δT, energy, δlnps -> vor/div tendencies (alpha
   //    operator, δdiv -= ∇²E), δT, δlnps
   FFTPlan fp;
@@ -1662,6 +1769,19 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
                                  md->spe_dlnps, st, md->fbuf, md->fcap));
   else
     JG_TRY(launch_g2s<T>(m, fp, gp, st, md->fbuf, md->fcap));
+  if (md->nq) {  // 3'. the tracers' tendencies to spectral space
+    FFTPlan fq;
+    memset(&fq, 0, sizeof(fq));
+    fq.ng = 1;
+    fq.C = md->LQ;
+    fq.g[0] = ig(PRO_NONE, md->g_dq, md->LQ, 0);
+    G2SPlan gq;
+    memset(&gq, 0, sizeof(gq));
+    gq.ng = 1;
+    gq.C = md->LQ;
+    gq.g[0] = og2(G2S_PLAIN, md->spe_dq, md->LQ, 0, 0, -1, -1);
+    JG_TRY(launch_g2s<T>(m, fq, gq, st, md->fbuf, md->fcap));
+  }
   // 4. semi-implicit correction, damping, leapfrog (FP64, warp per mode)
   ImplArgs<T> ia;
   memset(&ia, 0, sizeof(ia));
@@ -1693,6 +1813,14 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ia.rdgas = md->P.rdgas;
   ia.robert = md->P.robert_coef;
   impl_consts<T>(ia, tables<T>(md->mesh).eig);
+  ia.nq = md->nq;
+  ia.LQ = md->LQ;
+  if (md->nq) {
+    ia.dq = (const V*)md->spe_dq;
+    ia.q_p = (V*)md->spe_q[p];
+    ia.q_c = (V*)md->spe_q[c];
+    ia.q_n = (V*)md->spe_q[n];
+  }
   // vertical algebra in the state precision (FP64 algebra on the FP32 path measured no more
   // accurate: its error is set by FP32 storage); the wave-matrix solve is FP64 in both
   // 4 modes per block: (N+1)(N+2)/2 + N+1 modes at T42 make 248 blocks, every SM's FP64 units busy;
@@ -1743,6 +1871,17 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   i2.g[7] = og(EPI_DIVCOS, md->g_dtps, E, 5 * L + 2 * E);
   i2.g[8] = og(EPI_DIVCOS, md->g_dlT, L, 5 * L + 3 * E);
   i2.g[9] = og(EPI_DIVCOS, md->g_dtT, L, 6 * L + 3 * E);
+  if (md->nq) {  // the tracers' new level and its gradients
+    const int LQ = md->LQ, c0 = s2.C;
+    s2.g[10] = sg(S2G_PLAIN, md->spe_q[n], nullptr, LQ, c0);
+    s2.g[11] = sg(S2G_DLAM, md->spe_q[n], nullptr, LQ, c0 + LQ);
+    s2.g[12] = sg(S2G_DTH, md->spe_q[n], nullptr, LQ, c0 + 2 * LQ);
+    i2.g[10] = og(EPI_NONE, md->grid_q[n], LQ, c0);
+    i2.g[11] = og(EPI_DIVCOS, md->g_dlq, LQ, c0 + LQ);
+    i2.g[12] = og(EPI_DIVCOS, md->g_dtq, LQ, c0 + 2 * LQ);
+    s2.ng = i2.ng = 13;
+    s2.C = i2.C = c0 + 3 * LQ;
+  }
   JG_TRY(launch_s2g<T>(m, s2, i2, st, md->fbuf, md->fcap));
   // 6. mass and energy fixers
   CorrArgs<T> ca;
@@ -1943,6 +2082,8 @@ bool lookup(jgcm_model* md, const std::string& nm, FieldRef* f) {
     }
     return false;
   };
+  if (md->nq && (tl("spe_tracers", md->spe_q, nd * md->nq, true) || tl("grid_tracers", md->grid_q, nd * md->nq, false)))
+    return true;
   if (tl("spe_vor", md->spe_vor, nd, true) || tl("spe_div", md->spe_div, nd, true) ||
       tl("spe_lnps", md->spe_lnps, 1, true) || tl("spe_t", md->spe_t, nd, true) || tl("grid_u", md->grid_u, nd, false) ||
       tl("grid_v", md->grid_v, nd, false) || tl("grid_ps", md->grid_ps, 1, false) || tl("grid_t", md->grid_t, nd, false))
@@ -2044,6 +2185,55 @@ extern "C" int jgcm_model_create_vert(jgcm_mesh* mesh, const jgcm_params* params
   return JGCM_OK;
 }
 
+// Passive tracers on a Held-Suarez model: nq per member, every time level zero, advected like T
+// by every later step (k_hs_tracers, the tracers' analysis, their leapfrog in k_hs_implicit, their
+// synthesis with the new level).  Once per model; drops the captured graphs.
+extern "C" int jgcm_model_add_tracers(jgcm_model* md, int num_tracers) {
+  JG_ARG(md, "NULL model");
+  JG_ARG(md->P.kind == JGCM_HELD_SUAREZ, "tracers are advected by the Held-Suarez model only");
+  JG_ARG(md->nq == 0, "the model already has %d tracers", md->nq);
+  JG_ARG(num_tracers >= 1 && num_tracers <= 64, "num_tracers must be in [1, 64]");
+  jgcm_mesh* m = md->mesh;
+  JG_CUDA(cudaStreamSynchronize(m->stream));
+  const int nd = md->nd, ne = md->ne, LQ = num_tracers * nd * ne;
+  const size_t ts = tsize(m), S = spec_elems(m, LQ) * 2 * ts, G = grid_elems(m, LQ) * ts;
+  auto zalloc = [&](void** p, size_t bytes) -> int {
+    JG_CUDA(cudaMalloc(p, bytes));
+    JG_CUDA(cudaMemsetAsync(*p, 0, bytes, m->stream));
+    return JGCM_OK;
+  };
+  for (int i = 0; i < 3; i++) {
+    JG_TRY(zalloc(&md->spe_q[i], S));
+    JG_TRY(zalloc(&md->grid_q[i], G));
+  }
+  JG_TRY(zalloc(&md->spe_dq, S));
+  JG_TRY(zalloc(&md->g_dq, G));
+  JG_TRY(zalloc(&md->g_dlq, G));
+  JG_TRY(zalloc(&md->g_dtq, G));
+  JG_TRY(zalloc(&md->g_mhalf, grid_elems(m, md->L) * ts));
+  const size_t nstage = std::max(grid_elems(m, num_tracers * nd), 2 * spec_elems(m, num_tracers * nd));
+  JG_TRY(zalloc((void**)&md->q_stage, nstage * 8));
+  // the Fourier buffer holds the widest plan: the step's synthesis with the tracers' 3 LQ columns
+  const int fcap = (7 * nd + 3) * ne + 3 * LQ;
+  void* fbuf = nullptr;
+  JG_TRY(zalloc(&fbuf, (size_t)(m->N + 1) * m->nlat * fcap * 2 * ts));
+  JG_CUDA(cudaFree(md->fbuf));
+  md->fbuf = fbuf;
+  md->fcap = fcap;
+  md->nq = num_tracers;
+  md->LQ = LQ;
+  md->grad_ready = 0;
+  drop_graphs(md);
+  JG_CUDA(cudaStreamSynchronize(m->stream));
+  return JGCM_OK;
+}
+
+extern "C" int jgcm_model_num_tracers(jgcm_model* md, int* num_tracers) {
+  JG_ARG(md && num_tracers, "NULL argument");
+  *num_tracers = md->nq;
+  return JGCM_OK;
+}
+
 extern "C" int jgcm_model_destroy(jgcm_model* md) {
   if (!md) return JGCM_OK;
   jgcm_mesh* m = md->mesh;
@@ -2096,7 +2286,7 @@ extern "C" int jgcm_model_update_init_step(jgcm_model* md) {
 }
 
 static int launches_per_step(const jgcm_model* md) {
-  return md->P.kind == JGCM_BAROTROPIC ? 4 : md->P.kind == JGCM_SHALLOW_WATER ? 6 : 8;
+  return md->P.kind == JGCM_BAROTROPIC ? 4 : md->P.kind == JGCM_SHALLOW_WATER ? 6 : md->nq ? 11 : 8;
 }
 
 extern "C" int jgcm_model_launches_per_step(jgcm_model* md, int* launches) {
@@ -2114,7 +2304,11 @@ extern "C" int jgcm_model_kernel_name(jgcm_model* md, int slot, char* buf, int c
   static const char* sw[] = {"s2g_legendre(grad h)", "ifft(grad h)", "fft(fluxes,kin,dh)",
                              "g2s_legendre(vor,div,h+implicit+leapfrog)", "s2g_legendre(vor,div,h,u,v)",
                              "ifft(vor,div,h,u,v)"};
-  const char** names = md->P.kind == JGCM_HELD_SUAREZ ? hs : md->P.kind == JGCM_BAROTROPIC ? bt : sw;
+  static const char* hsq[] = {"hs_column", "hs_tracers", "fft(tendencies)", "g2s_legendre(vor,div,T,lnps)",
+                              "fft(tracers)", "g2s_legendre(tracers)", "hs_implicit",
+                              "s2g_legendre(vor,div,u,v,T,lnps,grad lnps,grad T,tracers)",
+                              "ifft(vor,div,u,v,T,lnps,grad lnps,grad T,tracers)", "hs_corr_reduce", "hs_corr_apply"};
+  const char** names = md->P.kind == JGCM_HELD_SUAREZ ? (md->nq ? hsq : hs) : md->P.kind == JGCM_BAROTROPIC ? bt : sw;
   JG_ARG(slot >= 0 && slot < launches_per_step(md), "slot out of range");
   snprintf(buf, cap, "%s", names[slot]);
   return JGCM_OK;
@@ -2238,7 +2432,7 @@ extern "C" int jgcm_model_get_field(jgcm_model* md, const char* name, double* ho
   if (!host) return JGCM_OK;
   JG_ARG(cap >= (long)n, "buffer too small for '%s'", name);
   cudaStream_t st = m->stream;
-  double* stage = m->d_stage;
+  double* stage = n <= 4 * m->stage_slot ? m->d_stage : md->q_stage;  // tracer fields may need their own
   if (f.derived) {
     size_t G = grid_elems(m, 1);
     int nb = (int)((G + 127) / 128);
@@ -2274,12 +2468,13 @@ extern "C" int jgcm_model_set_field(jgcm_model* md, const char* name, const doub
   size_t n = f.spec ? 2 * spec_elems(m, f.L) : grid_elems(m, f.L);
   JG_ARG(count == (long)n, "field '%s' needs %zu doubles, got %ld", name, n, count);
   cudaStream_t st = m->stream;
+  double* stage = n <= 4 * m->stage_slot ? m->d_stage : md->q_stage;  // tracer fields may need their own
   JG_CUDA(cudaStreamSynchronize(st));
-  JG_CUDA(cudaMemcpyAsync(m->d_stage, host, n * 8, cudaMemcpyHostToDevice, st));
+  JG_CUDA(cudaMemcpyAsync(stage, host, n * 8, cudaMemcpyHostToDevice, st));
   if (f.spec)
-    JG_TRY(spec_host_to_dev(m, m->d_stage, f.ptr, f.L, st));
+    JG_TRY(spec_host_to_dev(m, stage, f.ptr, f.L, st));
   else
-    JG_TRY(grid_host_to_dev(m, m->d_stage, f.ptr, n, st));
+    JG_TRY(grid_host_to_dev(m, stage, f.ptr, n, st));
   if (!strcmp(name, "spe_lnps_n")) md->sw_adv_from_n = 1;
   md->grad_ready = 0;  // the gradients of the current level are recomputed by the next step
   JG_CUDA(cudaStreamSynchronize(st));
@@ -2587,6 +2782,7 @@ extern "C" int jgcm_model_copy_member(jgcm_model* dst, int dst_member, jgcm_mode
   JG_ARG(dst->mesh == src->mesh, "members can only be copied between models of one mesh");
   JG_ARG(dst->P.kind == src->P.kind && dst->P.dt == src->P.dt, "members can only be copied between models of one kind and dt");
   JG_ARG(dst_member >= 0 && dst_member < dst->ne && src_member >= 0 && src_member < src->ne, "member out of range");
+  JG_ARG(dst->nq == src->nq, "members can only be copied between models with the same number of tracers");
   if (dst->ne > 1 && dst != src)
     JG_ARG(dst->init_step == src->init_step && dst->sw_adv_from_n == src->sw_adv_from_n,
            "ensemble members must share the time-step state (init step) of the ensemble");
@@ -2620,6 +2816,10 @@ extern "C" int jgcm_model_copy_member(jgcm_model* dst, int dst_member, jgcm_mode
     JG_TRY(grid(dst->grid_v[ld], src->grid_v[ls], nd));
     JG_TRY(grid(dst->grid_t[ld], src->grid_t[ls], nd));
     JG_TRY(grid(dst->grid_ps[ld], src->grid_ps[ls], 1));
+    if (dst->nq) {
+      JG_TRY(spec(dst->spe_q[ld], src->spe_q[ls], nd * dst->nq));
+      JG_TRY(grid(dst->grid_q[ld], src->grid_q[ls], nd * dst->nq));
+    }
   }
   JG_TRY(grid(dst->grid_vor, src->grid_vor, nd));
   JG_TRY(grid(dst->grid_div, src->grid_div, nd));

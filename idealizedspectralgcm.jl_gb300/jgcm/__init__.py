@@ -96,6 +96,8 @@ def lib():
         "jgcm_model_diagnostics": (I, [P, I]),
         "jgcm_model_read_diagnostics": (I, [P, C.c_char_p, P, Lg, C.POINTER(Lg), C.POINTER(Lg)]),
         "jgcm_model_get_tuning": (I, [P, C.POINTER(I), I]),
+        "jgcm_model_add_tracers": (I, [P, I]),
+        "jgcm_model_num_tracers": (I, [P, C.POINTER(I)]),
         "jgcm_model_set_tuning": (I, [P, C.POINTER(I), I]),
         "jgcm_model_autotune": (I, [P, I, C.POINTER(I), I, C.POINTER(C.c_float)]),
         "jgcm_ensemble_create": (I, [C.POINTER(P), I, I, PP]),
@@ -344,7 +346,7 @@ class Model:
     """
 
     def __init__(self, mesh: Spectral_Spherical_Mesh, params: dict, members: int = 1,
-                 vert_coord="even_sigma", **vert_options):
+                 vert_coord="even_sigma", num_tracers: int = 0, **vert_options):
         self.mesh = mesh
         self.params = dict(params)
         self.members = int(members)
@@ -365,6 +367,9 @@ class Model:
         h = C.c_void_p()
         _check(lib().jgcm_model_create_vert(mesh._h, C.byref(p), self.members, _ptr(ak), _ptr(bk), C.byref(h)))
         self._h = h
+        self.num_tracers = int(num_tracers)
+        if self.num_tracers:
+            _check(lib().jgcm_model_add_tracers(self._h, self.num_tracers))
 
     def diagnostics(self, on=True):
         """Start (zeroing the sums) or stop the on-device diagnostics (Held-Suarez): after every step
@@ -416,8 +421,12 @@ class Model:
         m = self.mesh
         N1, S1 = m.num_fourier + 1, m.num_spherical + 1
         if name.startswith("spe_"):
-            return (N1, S1, n // (2 * N1 * S1)), np.complex128
-        return (m.nlon, m.nlat, n // (m.nlon * m.nlat)), np.float64
+            shape, dt = (N1, S1, n // (2 * N1 * S1)), np.complex128
+        else:
+            shape, dt = (m.nlon, m.nlat, n // (m.nlon * m.nlat)), np.float64
+        if "tracers" in name:  # Dyn_Data's [.., nd, num_tracers]
+            shape = shape[:2] + (m.nd, self.num_tracers)
+        return shape, dt
 
     def get(self, name):
         n = C.c_long()

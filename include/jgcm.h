@@ -174,6 +174,16 @@ int jgcm_vert_coord(int nd, const char* option, double scale_heights, double sur
  * forward model; jgcm_model_step_adjoint and jgcm_model_hs_gradient need sigma coordinates. */
 int jgcm_model_create_vert(jgcm_mesh* mesh, const jgcm_params* params, int members, const double* ak,
                            const double* bk, jgcm_model** out);
+/* Passive tracers (Dyn_Data's spe_tracers_{n,c,p} [N+1, N+2, nd, nq] and grid_tracers_{n,c,p}
+ * [nλ, nθ, nd, nq], Dyn_Data.jl:36-39,63-66, rotated by Time_Advance! :341-342, 360-361): num_tracers
+ * per member on a Held-Suarez model, every level zero, read and written by those names.  The
+ * reference allocates them and never steps them (Spectral_Dynamics.jl:235 has "grid_q = grid_t" as
+ * a todo); here every step advects them like T: Vert_Advection! with the step's mass flux and
+ * Add_Horizontal_Advection! of spe_tracers_c, Trans_Grid_To_Spherical!, T's spectral damping and
+ * filtered leapfrog, no forcing and no semi-implicit term, then Trans_Spherical_To_Grid! of the new
+ * level.  Once per model, num_tracers in [1, 64]; the step adjoint refuses models with tracers. */
+int jgcm_model_add_tracers(jgcm_model* model, int num_tracers);
+int jgcm_model_num_tracers(jgcm_model* model, int* num_tracers);
 /* Copy member src_member of src into member dst_member of dst (same mesh and model kind): every
  * time level of the prognostic state and the grid diagnostics.  A one-member dst also takes the
  * source's time-step state (init step); an ensemble dst must already share it. */

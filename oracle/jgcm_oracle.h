@@ -118,6 +118,8 @@ void om_semi_implicit_step(om_model* md, const double* const* in, double* const*
 void om_hs_forcing(om_model* md, int Dt, const double* u, const double* v, const double* p_half,
                    const double* p_full, const double* t, double* du, double* dv, double* t_eq, double* dtt);
 void om_model_destroy(om_model* md);
+/* nq passive tracers advected like T on a Held-Suarez model (once, before the first step) */
+int om_model_add_tracers(om_model* md, int nq);
 /* named Dyn_Data fields ("spe_vor_c", "grid_u_p", ... , "grid_h_eq"); returns element count
  * (doubles) or -1 */
 long om_model_field(om_model* md, const char* name, double* host, long cap, int set);

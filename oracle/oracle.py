@@ -71,6 +71,7 @@ def lib():
             "om_model_create_vert": (P, [P, P, P, P]),
             "om_vert_coord": (I, [I, C.c_char_p, D, D, D, P, P]),
             "om_model_destroy": (None, [P]),
+            "om_model_add_tracers": (I, [P, I]),
             "om_model_field": (L, [P, C.c_char_p, P, L, I]),
             "om_model_init_step": (I, [P]),
             "om_model_update_init_step": (I, [P]),
@@ -259,9 +260,11 @@ def Compute_Vert_Coord(nd, vert_coord_option, scale_heights=4.0, surf_res=1.0, e
 class Model:
     """Dyn_Data + Filtered_Leapfrog (+ Semi_Implicit_Solver for Held-Suarez) on the oracle.
 
-    ``vert_coord``: a Vert_Coordinate option (see ``Compute_Vert_Coord``) or a pair (ak, bk)."""
+    ``vert_coord``: a Vert_Coordinate option (see ``Compute_Vert_Coord``) or a pair (ak, bk).
+    ``num_tracers``: passive tracers (Dyn_Data's spe_tracers_* / grid_tracers_*, [.., nd, nq]) advected
+    like T (Held-Suarez only)."""
 
-    def __init__(self, mesh, params: dict, vert_coord="even_sigma", **vert_options):
+    def __init__(self, mesh, params: dict, vert_coord="even_sigma", num_tracers=0, **vert_options):
         self.mesh = mesh
         self.params = dict(params)
         if isinstance(vert_coord, str):
@@ -278,6 +281,9 @@ class Model:
                                              self.bk.ctypes.data_as(C.c_void_p))
         if not self._h:
             raise AssertionError("model creation failed")
+        self.num_tracers = int(num_tracers)
+        if self.num_tracers and lib().om_model_add_tracers(self._h, self.num_tracers) != 0:
+            raise AssertionError("tracers need a Held-Suarez model and num_tracers >= 1")
 
     def __del__(self):
         if getattr(self, "_h", None):
@@ -288,8 +294,12 @@ class Model:
         m = self.mesh
         N1, S1 = m.num_fourier + 1, m.num_spherical + 1
         if name.startswith("spe_"):
-            return (N1, S1, n // (2 * N1 * S1)), np.complex128
-        return (m.nlon, m.nlat, n // (m.nlon * m.nlat)), np.float64
+            shape, dt = (N1, S1, n // (2 * N1 * S1)), np.complex128
+        else:
+            shape, dt = (m.nlon, m.nlat, n // (m.nlon * m.nlat)), np.float64
+        if "tracers" in name:  # [.., nd, nq]
+            shape = shape[:2] + (m.nd, self.num_tracers)
+        return shape, dt
 
     def get(self, name):
         n = lib().om_model_field(self._h, name.encode(), None, 0, 0)

@@ -203,6 +203,33 @@ def test_hs_mass_fixer_and_step_finite(orc):
     assert np.isfinite(md.get("grid_t_c")).all()
 
 
+def test_oracle_tracers_advect_linearly_and_keep_a_uniform_field(orc):
+    """Passive tracers (Dyn_Data's spe_tracers_*, advected like T): the step is linear in them
+    (twice the tracer gives twice the result), a uniform tracer stays uniform, and the other
+    prognostic fields do not see them."""
+    name = "hs_t21l10"
+    M = configs.make_mesh(orc, name)
+    md = orc.Model(M, configs.PARAMS[name], num_tracers=3)
+    ref = orc.Model(M, configs.PARAMS[name])
+    for m in (md, ref):
+        m.spectral_initialize_fields(configs.hs_temperature_noise(M), True)
+    t, g = md.get("spe_t_c"), md.get("grid_t_c")
+    spe = np.stack([t, 2 * t, np.zeros_like(t)], axis=3)
+    spe[0, 0, :, 2] = 1.0
+    grid = np.stack([g, 2 * g, np.ones_like(g)], axis=3)
+    for f, v in (("spe_tracers_c", spe), ("spe_tracers_p", spe), ("grid_tracers_c", grid)):
+        md.set(f, v)
+    md.step(5)
+    ref.step(5)
+    q = md.get("spe_tracers_c")
+    assert np.abs(q[..., 1] - 2 * q[..., 0]).max() <= 1e-12 * np.abs(q[..., 1]).max()
+    assert np.abs(md.get("grid_tracers_c")[..., 2] - 1.0).max() < 1e-12
+    assert configs.rel_l2(q[..., 0], md.get("spe_t_c")) > 1e-6  # stepped, not copied from T
+    assert np.array_equal(md.get("spe_vor_c"), ref.get("spe_vor_c"))
+    with pytest.raises(AssertionError):  # tracers belong to the Held-Suarez model
+        orc.Model(configs.make_mesh(orc, "barotropic_t42"), configs.PARAMS["barotropic_t42"], num_tracers=1)
+
+
 def test_vert_coord_tables(orc):
     """Compute_Vert_Coord (Vert_Coordinate.jl:61-87), zero top: even_sigma is LinRange(0, 1);
     uneven_sigma with surf_res = 1 is exp(-scale_heights (1 - k/nd)) inside, and with surf_res < 1
