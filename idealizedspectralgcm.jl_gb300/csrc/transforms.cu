@@ -456,6 +456,66 @@ __device__ __forceinline__ void warp_fft_dif(T (&re)[V], T (&im)[V], const T* tw
   }
 }
 
+// The epilogue of one warp's row (k_ifft_w): x(λ_2i) = re[r], x(λ_2i+1) = im[r] for i = lane + 32 r,
+// the group's epilogue chosen once per row and each pair of longitudes stored as one 8- or 16-byte
+// word.  ÷cos θ as a product with 1/cos θ (within an ulp of the quotient).
+template <typename T, int V>
+__device__ __forceinline__ void ifft_store_row(const GridOutGroup& g, const Tables<T>& tb, int k, int j, int nlat,
+                                               int nlon, const T (&re)[V], const T (&im)[V], int lane) {
+  using P = V2<T>;
+  const size_t row = ((size_t)k * nlat + j) * nlon;
+  P* dst = reinterpret_cast<P*>((T*)g.dst + row);
+  auto put = [](P* d, int i, T a, T b) {
+    P v;
+    v.x = a;
+    v.y = b;
+    d[i] = v;
+  };
+  switch (g.epi) {
+    case EPI_NONE:
+#pragma unroll
+      for (int r = 0; r < V; r++) put(dst, lane + 32 * r, re[r], im[r]);
+      break;
+    case EPI_DIVCOS: {
+      const T rc = (T)1 / tb.cosj[j];
+#pragma unroll
+      for (int r = 0; r < V; r++) put(dst, lane + 32 * r, re[r] * rc, im[r] * rc);
+    } break;
+    case EPI_EXP2: {
+      const T sh = pick<T>(g.shift, g.shiftf), es = pick<T>(g.eshift, g.eshiftf);
+      P* d2 = reinterpret_cast<P*>((T*)g.dst2 + row);
+#pragma unroll
+      for (int r = 0; r < V; r++) {
+        put(dst, lane + 32 * r, re[r] + sh, im[r] + sh);
+        put(d2, lane + 32 * r, exp(re[r]) * es, exp(im[r]) * es);
+      }
+    } break;
+    case EPI_DIVCOS_MULPS: {  // level k of ps
+      const T rc = (T)1 / tb.cosj[j];
+      const P* ps = reinterpret_cast<const P*>((const T*)g.ps + row);
+#pragma unroll
+      for (int r = 0; r < V; r++) {
+        const P q = ps[lane + 32 * r];
+        put(dst, lane + 32 * r, (re[r] * rc) * q.x, (im[r] * rc) * q.y);
+      }
+    } break;
+    case EPI_ADJ_G2S: {
+      const auto sc = tb.wts[j] / (T)(2 * nlon);
+#pragma unroll
+      for (int r = 0; r < V; r++) put(dst, lane + 32 * r, (T)(re[r] * sc), (T)(im[r] * sc));
+    } break;
+    case EPI_ANOM: {
+      const T mean = ((const V2<T>*)g.ps)[k].x;
+      P* d2 = reinterpret_cast<P*>((T*)g.dst2 + row);
+#pragma unroll
+      for (int r = 0; r < V; r++) {
+        put(dst, lane + 32 * r, re[r] + mean, im[r] + mean);
+        put(d2, lane + 32 * r, re[r], im[r]);
+      }
+    } break;
+  }
+}
+
 template <typename T, int V>
 __global__ void __launch_bounds__(256) k_ifft_w(IFFTPlan plan, Tables<T> tb, const V2<T>* __restrict__ F, int N,
                                                 int nlat, int nlon) {
@@ -495,12 +555,7 @@ __global__ void __launch_bounds__(256) k_ifft_w(IFFTPlan plan, Tables<T> tb, con
   warp_fft_dit<T, V>(re, im, tb.tw, lane);
   int k;
   const GridOutGroup& g = group_of(plan.g, plan.ng, c, &k);
-#pragma unroll
-  for (int r = 0; r < V; r++) {  // z[i] = x[2i] + i x[2i+1]
-    const int i = lane + 32 * r;
-    ifft_store<T>(g, tb, k, j, 2 * i, nlat, nlon, re[r]);
-    ifft_store<T>(g, tb, k, j, 2 * i + 1, nlat, nlon, im[r]);
-  }
+  ifft_store_row<T, V>(g, tb, k, j, nlat, nlon, re, im, lane);  // z[i] = x[2i] + i x[2i+1]
 }
 
 template <typename T, int V, bool PLAIN>
@@ -522,10 +577,11 @@ __global__ void __launch_bounds__(256) k_fft_w(FFTPlan plan, Tables<T> tb, V2<T>
 #pragma unroll
     for (int r = 0; r < V; r++) {  // z[i] = x[2i] + i x[2i+1], natural order
       const int i = lane + 32 * r;
-      if (PLAIN) {  // every group reads its field as it is (k_fft_rows' PLAIN)
-        const T* src = (const T*)g.src + ((size_t)k * nlat + j) * nlon;
-        re[r] = src[2 * i];
-        im[r] = src[2 * i + 1];
+      if (PLAIN) {  // every group reads its field as it is (k_fft_rows' PLAIN); a pair per load
+        const Vc* src = reinterpret_cast<const Vc*>((const T*)g.src + ((size_t)k * nlat + j) * nlon);
+        const Vc x = src[i];
+        re[r] = x.x;
+        im[r] = x.y;
       } else {
         re[r] = fft_load<T>(plan, g, k, j, 2 * i, nlat, nlon, cj);
         im[r] = fft_load<T>(plan, g, k, j, 2 * i + 1, nlat, nlon, cj);
