@@ -36,14 +36,6 @@ __device__ __forceinline__ void ld4w(const double* p, double (&w)[4]) {
   w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
 }
 
-// Ampere-style asynchronous global -> shared copy of 16 bytes (both addresses 16-byte aligned)
-__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(sdst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
 template <typename T>
 struct HSAnaArgs {
   const V2<T>* F;                       // Fourier buffer [m][j][Cin]

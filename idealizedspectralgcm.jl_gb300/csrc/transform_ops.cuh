@@ -10,6 +10,15 @@ namespace jgcm {
 template <typename T>
 using V2 = typename C2<T>::t;
 
+// Ampere-style asynchronous global -> shared copy of 16 bytes (both addresses 16-byte aligned):
+// staged tables need no registers and every copy is in flight at once
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 template <typename G>
 __device__ __forceinline__ const G& group_of(const G* g, int ng, int c, int* k) {
   int i = 0;

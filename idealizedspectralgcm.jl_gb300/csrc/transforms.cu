@@ -70,7 +70,6 @@ __device__ __forceinline__ void fft_stages(T* re, T* im, const T* tw, int nrow, 
 template <typename T>
 __global__ void __launch_bounds__(256) k_s2g_legendre(S2GPlan plan, Tables<T> tb, V2<T>* __restrict__ F, int ns,
                                                       int nlat, int CT) {
-  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
   using V = V2<T>;
   extern __shared__ __align__(16) unsigned char smem[];
   const int m = blockIdx.y;
@@ -82,22 +81,48 @@ __global__ void __launch_bounds__(256) k_s2g_legendre(S2GPlan plan, Tables<T> tb
   const int cbase = blockIdx.x * CT;
   const size_t mrow = (size_t)m * (ns + 1);
   const T* Pm = tb.P + (mrow + m) * nh;
-  for (int i = threadIdx.x; i < K * nh; i += blockDim.x) Ps[i] = Pm[i];
-  for (int i = threadIdx.x; i < K * CT; i += blockDim.x) {
-    int r = i / CT, cl = i - r * CT, n = m + r, c = cbase + cl;
-    V x;
-    x.x = 0;
-    x.y = 0;
+  // the m-block of P (constants, one contiguous run): staged before the dependency wait, by
+  // asynchronous 16-byte copies when its rows are whole chunks
+  const bool async_p = (nh * sizeof(T)) % 16 == 0;
+  if (async_p) {
+    constexpr int ce = 16 / (int)sizeof(T);
+    for (int i = threadIdx.x; i < K * nh / ce; i += blockDim.x) cp_async16(Ps + i * ce, Pm + i * ce);
+    cp_async_commit();
+  } else {
+    for (int i = threadIdx.x; i < K * nh; i += blockDim.x) Ps[i] = Pm[i];
+  }
+  pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
+  // CT divides the block (a power of two up to 256): a thread keeps one column, its group found
+  // once, and walks rows r (and below latitudes j) in steps of blockDim / CT
+  const bool fixed_col = blockDim.x % CT == 0;
+  const int cl0 = threadIdx.x % CT, rstep = blockDim.x / CT;
+  if (fixed_col) {
+    const int c = cbase + cl0;
     if (c < C) {
       int k;
       const S2GGroup& g = group_of(plan.g, plan.ng, c, &k);
-      x = s2g_input<T>(g, tb, m, n, ns, mrow, k);
+      for (int r = threadIdx.x / CT; r < K; r += rstep) X[r * CT + cl0] = s2g_input<T>(g, tb, m, m + r, ns, mrow, k);
+    } else {
+      for (int r = threadIdx.x / CT; r < K; r += rstep) X[r * CT + cl0] = V{0, 0};
     }
-    X[i] = x;
+  } else {
+    for (int i = threadIdx.x; i < K * CT; i += blockDim.x) {
+      int r = i / CT, cl = i - r * CT, n = m + r, c = cbase + cl;
+      V x;
+      x.x = 0;
+      x.y = 0;
+      if (c < C) {
+        int k;
+        const S2GGroup& g = group_of(plan.g, plan.ng, c, &k);
+        x = s2g_input<T>(g, tb, m, n, ns, mrow, k);
+      }
+      X[i] = x;
+    }
   }
+  if (async_p) cp_async_wait_all();
   __syncthreads();
-  for (int i = threadIdx.x; i < nh * CT; i += blockDim.x) {
-    int j = i / CT, cl = i - j * CT, c = cbase + cl;
+  for (int i = threadIdx.x, jf = threadIdx.x / CT; i < nh * CT; i += blockDim.x, jf += rstep) {
+    const int j = fixed_col ? jf : i / CT, cl = fixed_col ? cl0 : i - j * CT, c = cbase + cl;
     T er = 0, ei = 0, orr = 0, oi = 0;
     int r = 0;
     for (; r + 1 < K; r += 2) {
