@@ -21,6 +21,9 @@ struct VertCoef {  // Vert_Coordinate (even_sigma) and the semi-implicit referen
   double dlp_p[JGCM_MAX_ND];   // ln p_{k+1/2} - ln p_k
   double dlp_m[JGCM_MAX_ND];   // ln p_k - ln p_{k-1/2}   (k >= 1)
   double dlp[JGCM_MAX_ND];     // ln p_{k+1/2} - ln p_{k-1/2}   (k >= 1)
+  // Δa_k, Δb_k as FP32 pairs hi + lo (hi the FP32 rounding, lo that of the remainder): the FP32
+  // path forms the column sums of T_k Δa_k, T_k Δb_k to FP64 accuracy from them
+  float dak_hi[JGCM_MAX_ND], dak_lo[JGCM_MAX_ND], dbk_hi[JGCM_MAX_ND], dbk_lo[JGCM_MAX_ND];
 };
 }  // namespace jgcm
 

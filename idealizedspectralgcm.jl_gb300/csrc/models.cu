@@ -107,6 +107,23 @@ __device__ __forceinline__ bool ticket_last(unsigned* counter, unsigned n) {
   return last;
 }
 
+// Error-free transformations in FP32: the pair hi + lo carries a sum to ~2^-48 relative (FP64-class
+// accuracy from FP32 instructions: an FP64 instruction holds a sub-partition ~64 cycles on this part,
+// an FP32 one ~1).  The _rn intrinsics are never contracted into a multiply-add, which would break
+// the exactness of the two-sum.
+__device__ __forceinline__ void ds_add(float& hi, float& lo, float x) {
+  const float s = __fadd_rn(hi, x), bb = __fsub_rn(s, hi);
+  lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb)));
+  hi = s;
+}
+// hi + lo += t (ch + cl): the product t ch as its rounding plus its exact error, t cl added to lo
+__device__ __forceinline__ void ds_add_prod(float& hi, float& lo, float t, float ch, float cl) {
+  const float p = __fmul_rn(t, ch);
+  const float pe = __fmaf_rn(t, ch, -p);
+  ds_add(hi, lo, p);
+  lo = __fadd_rn(lo, __fmaf_rn(t, cl, pe));
+}
+
 // Mercator series of log(1 + d) for |d| <= 2^-12: the remainder after the d^5 term is below
 // |d|^6 / 6 < 2^-62 |d|, under half an ulp of the sum; larger |d| take the library's log
 __device__ __forceinline__ double log_near_one(double f) {
@@ -217,6 +234,7 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
   __shared__ T s_lb1;
   __shared__ T s_ak[JGCM_MAX_ND + 1];  // hybrid coordinates: a_k in the state precision
   __shared__ double s_dak64[JGCM_MAX_ND], s_dbk64[JGCM_MAX_ND];  // FP64 layer coefficients: the energy integral
+  __shared__ float s_dah[JGCM_MAX_ND], s_dal[JGCM_MAX_ND], s_dbh[JGCM_MAX_ND], s_dbl[JGCM_MAX_ND];  // as FP32 pairs
   const int nd = a.nd, nlon = a.nlon, nlat = a.nlat;
   for (int q = threadIdx.x; q <= nd; q += blockDim.x) {
     s_bk[q] = (T)vc.bk[q];
@@ -224,6 +242,10 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
     if (q < nd) {
       s_dak64[q] = vc.dak[q];
       s_dbk64[q] = vc.dbk[q];
+      s_dah[q] = vc.dak_hi[q];
+      s_dal[q] = vc.dak_lo[q];
+      s_dbh[q] = vc.dbk_hi[q];
+      s_dbl[q] = vc.dbk_lo[q];
       s_dak[q] = (T)vc.dak[q];
       s_dbk[q] = (T)vc.dbk[q];
       s_cf[q] = (T)vc.cf[q];
@@ -328,11 +350,13 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
     }
   // ---- pass 2, top-down within the segment
   // the column's energy integral (Compute_Corrections_Init): its kinetic part in the state precision,
-  // its c_p T part (~99 % of it) as FP64 sums of the exact products T_k Δa_k and T_k Δb_k (on the FP32
-  // path the state precision's rounding of c_p T, the same at nearly every point of a near-uniform
-  // temperature, biased the energy correction by up to 1e-6 K per step)
+  // its c_p T part (~99 % of it) to FP64 accuracy (on the FP32 path the state precision's rounding of
+  // c_p T, the same at nearly every point of a near-uniform temperature, biased the energy correction
+  // by up to 1e-6 K per step): FP64 sums of T_k Δa_k and T_k Δb_k on the FP64 path, the same sums as
+  // FP32 pairs (error-free products and additions, ds_add_prod) on the FP32 path
   T col_e = 0;
   double col_ta = 0, col_tb = 0;
+  float ah = 0, al = 0, bh = 0, bl = 0;
   if (act && k0 < k1) {
     T incl = incl0, Mlo = 0, flu = 0, flv = 0, flt = 0;  // M and the advective fluxes at k0-1/2
     T u = u_c[(size_t)k0 * G], v = v_c[(size_t)k0 * G], t = t_c[(size_t)k0 * G];
@@ -378,9 +402,14 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
         const T ua = up + tDt * du, va = vp + tDt * dv;
         const T te = tp + tDt * dt;
         col_e += ((T)0.5 * (ua * ua + va * va)) * (s_dak[k] + s_dbk[k] * psp);
-        const double ted = (double)te;
-        if (a.has_dak) col_ta += ted * s_dak64[k];
-        col_tb += ted * s_dbk64[k];
+        if constexpr (std::is_same<T, float>::value) {
+          if constexpr (HYB) ds_add_prod(ah, al, te, s_dah[k], s_dal[k]);  // Δa_k = 0 on sigma levels
+          ds_add_prod(bh, bl, te, s_dbh[k], s_dbl[k]);
+        } else {
+          const double ted = (double)te;
+          if (a.has_dak) col_ta += ted * s_dak64[k];
+          col_tb += ted * s_dbk64[k];
+        }
       }
       // Four_In_One! (Spectral_Dynamics.jl:88-183)
       const T x1 = (s_bk[k] * dlnp_m + s_bk[k + 1] * dlnp_p) * rdp;
@@ -421,6 +450,10 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
       t = t1;
       dp = dp1;
     }
+  }
+  if constexpr (std::is_same<T, float>::value) {
+    col_ta = (double)ah + (double)al;
+    col_tb = (double)bh + (double)bl;
   }
   double col_ed = (double)col_e + a.cp * (col_ta + col_tb * (double)psp);
   col_ed = seg_sum<S>(col_ed);
@@ -839,11 +872,16 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   constexpr int KS = 8;
   __shared__ T s_dak[JGCM_MAX_ND], s_dbk[JGCM_MAX_ND];  // the layer coefficients in the state precision
   __shared__ double s_dak64[JGCM_MAX_ND], s_dbk64[JGCM_MAX_ND];  // and in FP64 (the c_p T sums)
+  __shared__ float s_dah[JGCM_MAX_ND], s_dal[JGCM_MAX_ND], s_dbh[JGCM_MAX_ND], s_dbl[JGCM_MAX_ND];  // FP32 pairs
   for (int q = threadIdx.x; q < a.nd; q += blockDim.x) {
     s_dak[q] = (T)vc.dak[q];
     s_dbk[q] = (T)vc.dbk[q];
     s_dak64[q] = vc.dak[q];
     s_dbk64[q] = vc.dbk[q];
+    s_dah[q] = vc.dak_hi[q];
+    s_dal[q] = vc.dak_lo[q];
+    s_dbh[q] = vc.dbk_hi[q];
+    s_dbl[q] = vc.dbk_lo[q];
   }
   __syncthreads();
   pdl_wait();  // programmatic dependent launch: the predecessor's output is complete
@@ -852,28 +890,69 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   const bool act = i < a.nlon;
   const size_t G = (size_t)a.nlat * a.nlon, col = (size_t)j * a.nlon + (act ? i : 0);
   const size_t offL = (size_t)e * nd * G, off1 = (size_t)e * G;
-  // the energy integrals sum_k E_k Δa_k, sum_k E_k Δb_k: the kinetic part in the state precision,
-  // the c_p T part (~99 %) as FP64 sums of the exact products T_k Δa_k, T_k Δb_k (the state
-  // precision's rounding of c_p T biased the energy correction by up to 1e-6 K per step)
+  // the energy integrals sum_k E_k Δa_k, sum_k E_k Δb_k (E = |u|²/2 + c_p T): the kinetic part in
+  // the state precision, the c_p T part (~99 %) to FP64 accuracy (the state precision's rounding of
+  // c_p T biased the energy correction by up to 1e-6 K per step): FP64 sums of the products T_k Δa_k,
+  // T_k Δb_k on the FP64 path; on the FP32 path the same sums as FP32 pairs (error-free products
+  // against Δ_hi + Δ_lo, error-free additions), each column's pair converted to FP64 once
   __shared__ double part[2][KS][32];
-  T ea = 0, eb = 0;
-  double ta = 0, tb = 0;
-  if (act) {
+  if constexpr (std::is_same<T, float>::value) {
+    __shared__ float pk[2][KS][32], ph[2][KS][32], pl[2][KS][32];  // kinetic; c_p T part as hi + lo
+    float ea = 0, eb = 0, ah = 0, al = 0, bh = 0, bl = 0;
+    if (act) {
 #pragma unroll 4  // nd <= 32: every level's loads in flight together
-    for (int k = ks; k < nd; k += KS) {
-      size_t x = offL + (size_t)k * G + col;
-      T u = a.u_n[x], v = a.v_n[x];
-      const double t = (double)a.t_n[x];
-      T K = (T)0.5 * (u * u + v * v);
-      ea += K * s_dak[k];
-      eb += K * s_dbk[k];
-      if (a.has_dak) ta += t * s_dak64[k];
-      tb += t * s_dbk64[k];
+      for (int k = ks; k < nd; k += KS) {
+        const size_t x = offL + (size_t)k * G + col;
+        const float u = a.u_n[x], v = a.v_n[x], t = a.t_n[x];
+        const float K = 0.5f * (u * u + v * v);
+        ea += K * s_dak[k];
+        eb += K * s_dbk[k];
+        if (a.has_dak) ds_add_prod(ah, al, t, s_dah[k], s_dal[k]);
+        ds_add_prod(bh, bl, t, s_dbh[k], s_dbl[k]);
+      }
+    }
+    pk[0][ks][lane] = ea;
+    pk[1][ks][lane] = eb;
+    ph[0][ks][lane] = ah;
+    pl[0][ks][lane] = al;
+    ph[1][ks][lane] = bh;
+    pl[1][ks][lane] = bl;
+    __syncthreads();
+    if (ks == 1 || ks == 2) {  // the level groups of this lane's column, in order, then FP64 once
+      const int w = ks - 1;
+      float kh = 0, kl = 0, th = 0, tl = 0;
+      for (int q = 0; q < KS; q++) {
+        ds_add(kh, kl, pk[w][q][lane]);
+        ds_add(th, tl, ph[w][q][lane]);
+        tl = __fadd_rn(tl, pl[w][q][lane]);
+      }
+      part[w][0][lane] = ((double)kh + (double)kl) + a.cp * ((double)th + (double)tl);
+    }
+  } else {
+    T ea = 0, eb = 0;
+    double ta = 0, tb = 0;
+    if (act) {
+#pragma unroll 4
+      for (int k = ks; k < nd; k += KS) {
+        const size_t x = offL + (size_t)k * G + col;
+        const T u = a.u_n[x], v = a.v_n[x];
+        const double t = (double)a.t_n[x];
+        const T K = (T)0.5 * (u * u + v * v);
+        ea += K * s_dak[k];
+        eb += K * s_dbk[k];
+        if (a.has_dak) ta += t * s_dak64[k];
+        tb += t * s_dbk64[k];
+      }
+    }
+    part[0][ks][lane] = (double)ea + a.cp * ta;
+    part[1][ks][lane] = (double)eb + a.cp * tb;
+    __syncthreads();
+    if (ks == 1 || ks == 2) {  // the level groups of this lane's column (each lane its own column)
+      double sq = 0;
+      for (int q = 0; q < KS; q++) sq += part[ks - 1][q][lane];
+      part[ks - 1][0][lane] = sq;
     }
   }
-  part[0][ks][lane] = (double)ea + a.cp * ta;
-  part[1][ks][lane] = (double)eb + a.cp * tb;
-  __syncthreads();
   // block values S0, S1, S2 (one warp each, on three sub-partitions): the level groups of each
   // column, the butterfly over the columns, the row's weight
   const int nb = gridDim.x * gridDim.y, bid = blockIdx.y * gridDim.x + blockIdx.x, ng = corr_groups(nb);
@@ -883,14 +962,8 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   unsigned* const ctr = a.counter + (size_t)e * (ng + 1);
   if (ks < 3) {
     const T ps = act ? a.ps_n[off1 + col] : (T)0;
-    double x;
-    if (ks == 0) {
-      x = (double)ps;
-    } else {
-      double sq = 0;
-      for (int q = 0; q < KS; q++) sq += part[ks - 1][q][lane];
-      x = ks == 1 ? sq : sq * (double)ps;
-    }
+    const double colsum = ks > 0 ? part[ks - 1][0][lane] : 0.0;  // written by this warp above
+    double x = ks == 0 ? (double)ps : ks == 1 ? colsum : colsum * (double)ps;
     x = warp_sum(x);
     if (lane == 0) {
       __stcg(bpart + (size_t)ks * nb + bid, x * a.wts[j]);
@@ -1174,6 +1247,10 @@ void vertical_setup(jgcm_model* md) {
   for (int k = 0; k < nd; k++) {
     vc.dak[k] = vc.ak[k + 1] - vc.ak[k];
     vc.dbk[k] = vc.bk[k + 1] - vc.bk[k];
+    vc.dak_hi[k] = (float)vc.dak[k];
+    vc.dak_lo[k] = (float)(vc.dak[k] - (double)vc.dak_hi[k]);
+    vc.dbk_hi[k] = (float)vc.dbk[k];
+    vc.dbk_lo[k] = (float)(vc.dbk[k] - (double)vc.dbk_hi[k]);
   }
   // sigma coordinates: every log-pressure difference is a per-level constant (formed here in FP64)
   for (int k = 1; k <= nd && !vc.hybrid; k++) vc.lb[k] = std::log(vc.bk[k]);
