@@ -481,6 +481,55 @@ __device__ __forceinline__ void warp_fft_dif(T (&re)[V], T (&im)[V], const T* tw
   }
 }
 
+// The epilogue of longitudes t, t+1 (t even) of row (k, j): one 8- or 16-byte store per output,
+// ÷cos θ as a product with rc = 1/cos θ (within an ulp of the quotient)
+template <typename T>
+__device__ __forceinline__ void ifft_store_pair(const GridOutGroup& g, const Tables<T>& tb, int k, int j, int nlat,
+                                                int nlon, int t, T a, T b, T rc) {
+  using P = V2<T>;
+  const size_t idx = ((size_t)k * nlat + j) * nlon + t;
+  P v;
+  switch (g.epi) {
+    case EPI_NONE:
+      v.x = a;
+      v.y = b;
+      break;
+    case EPI_DIVCOS:
+      v.x = a * rc;
+      v.y = b * rc;
+      break;
+    case EPI_EXP2: {
+      const T sh = pick<T>(g.shift, g.shiftf), es = pick<T>(g.eshift, g.eshiftf);
+      v.x = a + sh;
+      v.y = b + sh;
+      P e;
+      e.x = exp(a) * es;
+      e.y = exp(b) * es;
+      *reinterpret_cast<P*>((T*)g.dst2 + idx) = e;
+    } break;
+    case EPI_DIVCOS_MULPS: {  // level k of ps
+      const P q = *reinterpret_cast<const P*>((const T*)g.ps + idx);
+      v.x = (a * rc) * q.x;
+      v.y = (b * rc) * q.y;
+    } break;
+    case EPI_ADJ_G2S: {
+      const auto sc = tb.wts[j] / (T)(2 * nlon);
+      v.x = (T)(a * sc);
+      v.y = (T)(b * sc);
+    } break;
+    case EPI_ANOM: {
+      const T mean = ((const V2<T>*)g.ps)[k].x;
+      v.x = a + mean;
+      v.y = b + mean;
+      P d;
+      d.x = a;
+      d.y = b;
+      *reinterpret_cast<P*>((T*)g.dst2 + idx) = d;
+    } break;
+  }
+  *reinterpret_cast<P*>((T*)g.dst + idx) = v;
+}
+
 // The epilogue of one warp's row (k_ifft_w): x(λ_2i) = re[r], x(λ_2i+1) = im[r] for i = lane + 32 r,
 // the group's epilogue chosen once per row and each pair of longitudes stored as one 8- or 16-byte
 // word.  ÷cos θ as a product with 1/cos θ (within an ulp of the quotient).
@@ -678,6 +727,12 @@ __global__ void __launch_bounds__(32 * RF_WARPS) k_fft_rows(FFTPlan plan, Tables
   float* S = rsm + (size_t)w * 32 * P;
   const int nr = min(32, C - c0);
   const float cj = tb.cosj[j];
+  // each lane finds the group of one row (its own column) once; the rows' groups are broadcast
+  int gi = 0, gk = 0;
+  if (lane < nr) {
+    while (gi < plan.ng - 1 && c0 + lane >= plan.g[gi].col0 + plan.g[gi].L) gi++;
+    gk = c0 + lane - plan.g[gi].col0;
+  }
   // row r = column c0 + r, lanes along longitude (coalesced); 16 rows' loads are issued before any
   // of them is stored, so their latencies overlap
   constexpr int RB = 16;
@@ -688,9 +743,9 @@ __global__ void __launch_bounds__(32 * RF_WARPS) k_fft_rows(FFTPlan plan, Tables
     for (int rr = 0; rr < RB; rr++) {
 #pragma unroll
       for (int q = 0; q < NLON / 32; q++) v[rr][q] = 0.f;
+      const int g_r = __shfl_sync(0xffffffffu, gi, rb + rr), k = __shfl_sync(0xffffffffu, gk, rb + rr);
       if (rb + rr < nr) {
-        int k;
-        const GridInGroup& g = group_of(plan.g, plan.ng, c0 + rb + rr, &k);
+        const GridInGroup& g = plan.g[g_r];
 #pragma unroll
         for (int q = 0; q < NLON / 32; q++)
           v[rr][q] = PLAIN ? ((const float*)g.src)[((size_t)k * nlat + j) * NLON + lane + 32 * q]
@@ -805,14 +860,21 @@ __global__ void __launch_bounds__(32 * RF_WARPS, NLON == 64 ? 6 : 1) k_ifft_rows
     }
   }
   __syncwarp();
+  // each lane finds the group of one row (its own column) once; the rows' groups are broadcast
+  int gi = 0, gk = 0;
+  if (lane < nr) {
+    while (gi < plan.ng - 1 && c0 + lane >= plan.g[gi].col0 + plan.g[gi].L) gi++;
+    gk = c0 + lane - plan.g[gi].col0;
+  }
+  const float rc = 1.f / tb.cosj[j];
 #pragma unroll 1  // stores need no unrolling to overlap; one copy of the epilogue switch in the code
-  for (int r = 0; r < 32; r++) {  // row r = column c0 + r, lanes along longitude (coalesced)
-    if (r < nr) {
-      int k;
-      const GridOutGroup& g = group_of(plan.g, plan.ng, c0 + r, &k);
+  for (int r = 0; r < nr; r++) {  // row r = column c0 + r: lane pairs along longitude (coalesced)
+    const int g_r = __shfl_sync(0xffffffffu, gi, r), k = __shfl_sync(0xffffffffu, gk, r);
+    const GridOutGroup& g = plan.g[g_r];
 #pragma unroll
-      for (int q = 0; q < NLON / 32; q++)
-        ifft_store<float>(g, tb, k, j, lane + 32 * q, nlat, NLON, S[r * P + lane + 32 * q]);
+    for (int q = 0; q < NLON / 64; q++) {
+      const int t = 2 * (lane + 32 * q);
+      ifft_store_pair<float>(g, tb, k, j, nlat, NLON, t, S[r * P + t], S[r * P + t + 1], rc);
     }
   }
 }
