@@ -370,10 +370,22 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
       flv = Mlo * (vm + (v - vm) * w);
       flt = Mlo * (tm + (t - tm) * w);
     }
+    // the column's inputs and outputs through restrict-qualified pointers: no store of a level can
+    // alias a load of the next, so the next level's loads may be issued before this level's stores
+    const T* __restrict__ upp = a.u_p + cL;
+    const T* __restrict__ vpp = a.v_p + cL;
+    const T* __restrict__ tpp = a.t_p + cL;
+    const T* __restrict__ vorp = a.vor + cL;
+    const T* __restrict__ dlTp = a.dlT + cL;
+    const T* __restrict__ dtTp = a.dtT + cL;
+    T* __restrict__ o_du = a.ducos + cL;
+    T* __restrict__ o_dv = a.dvcos + cL;
+    T* __restrict__ o_dt = a.dtg + cL;
+    T* __restrict__ o_teq = a.t_eq + cL;
+    T* __restrict__ o_mh = a.m_half ? a.m_half + cL : nullptr;
     for (int k = k0; k < k1; k++) {
       const size_t x = (size_t)k * G;
-      const T up = a.u_p[cL + x], vp = a.v_p[cL + x], tp = a.t_p[cL + x], dvg = dvgp[x], vor = a.vor[cL + x],
-              dlT = a.dlT[cL + x], dtT = a.dtT[cL + x];
+      const T up = upp[x], vp = vpp[x], tp = tpp[x], dvg = dvgp[x], vor = vorp[x], dlT = dlTp[x], dtT = dtTp[x];
       const bool below = k + 1 < nd;
       T u1 = 0, v1 = 0, t1 = 0, dp1 = 1;
       if (below) {
@@ -423,7 +435,7 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
       dt = dt + kap * t * x5;
       // M_{k+1/2} = -sum_{r<=k} D_r + B_{k+1/2} sum_r D_r, zero at the surface
       const T Mhi = below ? -incl + tot * s_bk[k + 1] : (T)0;
-      if (a.m_half) a.m_half[cL + x] = Mhi;
+      if (o_mh) o_mh[x] = Mhi;
       // Vert_Advection! (second_centered_wts): flux at k+1/2 with weight dp_k / (dp_k + dp_{k+1})
       const T w1 = dp / (dp + dp1);
       const T fhu = below ? Mhi * (u + (u1 - u) * w1) : (T)0;
@@ -437,10 +449,10 @@ __global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HS
       const T absvor = vor + fj;
       du = du + absvor * v;
       dv = dv - absvor * u;
-      a.ducos[cL + x] = du * cj;
-      a.dvcos[cL + x] = dv * cj;
-      a.dtg[cL + x] = dt;
-      a.t_eq[cL + x] = teq;
+      o_du[x] = du * cj;
+      o_dv[x] = dv * cj;
+      o_dt[x] = dt;
+      o_teq[x] = teq;
       Mlo = Mhi;
       flu = fhu;
       flv = fhv;
