@@ -53,8 +53,9 @@ __host__ __device__ constexpr int wpitch(int nh) {
   return nh + 16 / (int)sizeof(T);
 }
 
-// grid (N/2 + 1 pairs, ceil((nd + 1) / LG) level groups, members), blockDim >= (N + 4) * LG
-template <typename T>
+// grid (N/2 + 1 pairs, ceil((nd + 1) / LG) level groups, members), blockDim >= rows * LG with rows the
+// largest per-pair thread count (N + 4 for NP = 1)
+template <typename T, int NP>
 __global__ void __launch_bounds__(256) k_hs_analysis(HSAnaArgs<T> a, Tables<T> tb) {
   using V = V2<T>;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -93,9 +94,10 @@ __global__ void __launch_bounds__(256) k_hs_analysis(HSAnaArgs<T> a, Tables<T> t
   }
   pdl_wait();  // programmatic dependent launch: the forward FFT's coefficients are complete
   // 2. hemisphere folds of the block's input columns: thread (l, jh) loads its latitude pair of all
-  //    fields of both m first (up to 16 loads in flight), then folds them (LG nh <= blockDim)
-  if (threadIdx.x < LG * nh) {
-    const int l = threadIdx.x / nh, jh = threadIdx.x - l * nh, lv = g * LG + l;
+  //    fields of both m first (up to 16 loads in flight), then folds them; consecutive threads take
+  //    consecutive levels, i.e. neighbouring columns of the Fourier buffer
+  for (int item = threadIdx.x; item < LG * nh; item += blockDim.x) {
+    const int jh = item / LG, l = item - jh * LG, lv = g * LG + l;
     V x[2][4], y[2][4];
 #pragma unroll
     for (int s = 0; s < 2; s++)
@@ -130,18 +132,34 @@ __global__ void __launch_bounds__(256) k_hs_analysis(HSAnaArgs<T> a, Tables<T> t
   }
   cp_async_wait_all();
   __syncthreads();
-  // 3. one thread per (m, n, level)
-  const int q = threadIdx.x / LG, l = threadIdx.x - q * LG;
-  if (q >= K1 + K2) return;
-  const int s = q < K1 ? 0 : 1;
-  const int m = s ? m2 : m1, r = s ? q - K1 : q, n = m + r, K = s ? K2 : K1;
+  // 3. one thread per (m, level) and NP total wavenumbers of one parity, n and n + 2 (NP = 2:
+  //    each folded input loaded from shared memory serves both; rows r = 4 i + b, b < 2)
+  int q = threadIdx.x / LG;
+  const int l = threadIdx.x - q * LG;
+  const int Q1 = NP == 1 ? K1 : 2 * ((K1 + 3) / 4), Q2 = nm == 2 ? (NP == 1 ? K2 : 2 * ((K2 + 3) / 4)) : 0;
+  if (q >= Q1 + Q2) return;
+  const int s = q < Q1 ? 0 : 1;
+  if (s) q -= Q1;
+  const int m = s ? m2 : m1, K = s ? K2 : K1;
+  const int r0 = NP == 1 ? q : 4 * (q >> 1) + (q & 1);
+  if (r0 >= K) return;
   const int lv = g * LG + l;
   if (lv > nd) return;
-  const bool even = (r & 1) == 0;  // P_n^m is symmetric about the equator for n - m even
+  const bool even = (r0 & 1) == 0;  // P_n^m is symmetric about the equator for n - m even
   const T* wbase = W + (s ? (size_t)3 * K1 * wp : 0);
-  const T* pw = wbase + (size_t)r * wp;
-  const T* ca = wbase + ((size_t)K + r) * wp;
-  const T* cb = wbase + ((size_t)2 * K + r) * wp;
+  const T* pw[NP];
+  const T* ca[NP];
+  const T* cb[NP];
+  bool live[NP];
+#pragma unroll
+  for (int u = 0; u < NP; u++) {
+    const int r = r0 + 2 * u;
+    live[u] = r < K;
+    const int rr = live[u] ? r : r0;  // a row past K reads row r0's weights and is not stored
+    pw[u] = wbase + (size_t)rr * wp;
+    ca[u] = wbase + ((size_t)K + rr) * wp;
+    cb[u] = wbase + ((size_t)2 * K + rr) * wp;
+  }
   // element (f, jh, parity) of this thread's column: X[((f nh + jh) 2 + par) nm LG + s LG + l]
   const size_t pstride = (size_t)nm * LG, jstride = 2 * pstride, fstride = (size_t)nh * jstride;
   const V* xcol = X + (size_t)s * LG + l;
@@ -149,21 +167,32 @@ __global__ void __launch_bounds__(256) k_hs_analysis(HSAnaArgs<T> a, Tables<T> t
   const size_t mrow = (size_t)m * (ns + 1);
   if (lv == nd) {  // δ ln ps of member e: plain analysis
     const V* src = xcol + 3 * fstride + same;
-    T sr = 0, si = 0;
-    for (int jh = 0; jh < nh; jh += 4) {
-      T w[4];
-      ld4w(pw + jh, w);
+    T sr[NP], si[NP];
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        const V x = src[(size_t)(jh + u) * jstride];
-        sr += x.x * w[u];
-        si += x.y * w[u];
+    for (int u = 0; u < NP; u++) sr[u] = si[u] = 0;
+    for (int jh = 0; jh < nh; jh += 4) {
+      T w[NP][4];
+#pragma unroll
+      for (int u = 0; u < NP; u++) ld4w(pw[u] + jh, w[u]);
+#pragma unroll
+      for (int v = 0; v < 4; v++) {
+        const V x = src[(size_t)(jh + v) * jstride];
+#pragma unroll
+        for (int u = 0; u < NP; u++) {
+          sr[u] += x.x * w[u][v];
+          si[u] += x.y * w[u][v];
+        }
       }
     }
-    V o;
-    o.x = n == ns ? (T)0 : sr * (T)0.5;
-    o.y = n == ns ? (T)0 : si * (T)0.5;
-    a.dlnps[(mrow + n) * a.E + e] = o;
+#pragma unroll
+    for (int u = 0; u < NP; u++) {
+      const int n = m + r0 + 2 * u;
+      if (!live[u]) continue;
+      V o;
+      o.x = n == ns ? (T)0 : sr[u] * (T)0.5;
+      o.y = n == ns ? (T)0 : si[u] * (T)0.5;
+      a.dlnps[(mrow + n) * a.E + e] = o;
+    }
     return;
   }
   const V* us = xcol + same;                 // δu cos, parity of n - m
@@ -174,48 +203,62 @@ __global__ void __launch_bounds__(256) k_hs_analysis(HSAnaArgs<T> a, Tables<T> t
   const V* ts = xcol + 3 * fstride + same;   // δT
   // vorticity: alpha operator of (A = δv cos, B = δu cos), i Σ CA A - Σ CB B
   // divergence: alpha operator of (A = δu cos, B = δv cos), i Σ CA A + Σ CB B, less ∇² of the energy
-  T var = 0, vai = 0, vbr = 0, vbi = 0, dar = 0, dai = 0, dbr = 0, dbi = 0, er = 0, ei = 0, tr = 0, ti = 0;
-  for (int jh = 0; jh < nh; jh += 4) {
-    T wP[4], wA[4], wB[4];
-    ld4w(pw + jh, wP);
-    ld4w(ca + jh, wA);
-    ld4w(cb + jh, wB);
+  T var[NP], vai[NP], vbr[NP], vbi[NP], dar[NP], dai[NP], dbr[NP], dbi[NP], er[NP], ei[NP], tr[NP], ti[NP];
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const size_t o = (size_t)(jh + u) * jstride;
+  for (int u = 0; u < NP; u++)
+    var[u] = vai[u] = vbr[u] = vbi[u] = dar[u] = dai[u] = dbr[u] = dbi[u] = er[u] = ei[u] = tr[u] = ti[u] = 0;
+  for (int jh = 0; jh < nh; jh += 4) {
+    T wP[NP][4], wA[NP][4], wB[NP][4];
+#pragma unroll
+    for (int u = 0; u < NP; u++) {
+      ld4w(pw[u] + jh, wP[u]);
+      ld4w(ca[u] + jh, wA[u]);
+      ld4w(cb[u] + jh, wB[u]);
+    }
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+      const size_t o = (size_t)(jh + v) * jstride;
       const V xu = us[o], yv = vo[o], xv = vs[o], yu = uo[o], xe = es[o], xt = ts[o];
-      var += (-xv.y) * wA[u];
-      vai += xv.x * wA[u];
-      vbr += yu.x * wB[u];
-      vbi += yu.y * wB[u];
-      dar += (-xu.y) * wA[u];
-      dai += xu.x * wA[u];
-      dbr += yv.x * wB[u];
-      dbi += yv.y * wB[u];
-      er += xe.x * wP[u];
-      ei += xe.y * wP[u];
-      tr += xt.x * wP[u];
-      ti += xt.y * wP[u];
+#pragma unroll
+      for (int u = 0; u < NP; u++) {
+        var[u] += (-xv.y) * wA[u][v];
+        vai[u] += xv.x * wA[u][v];
+        vbr[u] += yu.x * wB[u][v];
+        vbi[u] += yu.y * wB[u][v];
+        dar[u] += (-xu.y) * wA[u][v];
+        dai[u] += xu.x * wA[u][v];
+        dbr[u] += yv.x * wB[u][v];
+        dbi[u] += yv.y * wB[u][v];
+        er[u] += xe.x * wP[u][v];
+        ei[u] += xe.y * wP[u][v];
+        tr[u] += xt.x * wP[u][v];
+        ti[u] += xt.y * wP[u][v];
+      }
     }
   }
-  V ov, od, ot;
-  if (n == ns) {  // row N+1 of the analysis is zero (Trans_Grid_To_Spherical!, :288-291)
-    ov.x = ov.y = od.x = od.y = ot.x = ot.y = 0;
-  } else {
-    const T eig = tb.eig[mrow + n];
-    ov.x = var + (T)-1 * vbr;
-    ov.y = vai + (T)-1 * vbi;
-    od.x = dar + dbr;
-    od.y = dai + dbi;
-    od.x = od.x - eig * (er * (T)0.5);
-    od.y = od.y - eig * (ei * (T)0.5);
-    ot.x = tr * (T)0.5;
-    ot.y = ti * (T)0.5;
+#pragma unroll
+  for (int u = 0; u < NP; u++) {
+    if (!live[u]) continue;
+    const int n = m + r0 + 2 * u;
+    V ov, od, ot;
+    if (n == ns) {  // row N+1 of the analysis is zero (Trans_Grid_To_Spherical!, :288-291)
+      ov.x = ov.y = od.x = od.y = ot.x = ot.y = 0;
+    } else {
+      const T eig = tb.eig[mrow + n];
+      ov.x = var[u] + (T)-1 * vbr[u];
+      ov.y = vai[u] + (T)-1 * vbi[u];
+      od.x = dar[u] + dbr[u];
+      od.y = dai[u] + dbi[u];
+      od.x = od.x - eig * (er[u] * (T)0.5);
+      od.y = od.y - eig * (ei[u] * (T)0.5);
+      ot.x = tr[u] * (T)0.5;
+      ot.y = ti[u] * (T)0.5;
+    }
+    const size_t sidx = (mrow + n) * a.L + (size_t)e * nd + lv;
+    a.dvor[sidx] = ov;
+    a.ddiv[sidx] = od;
+    a.dt[sidx] = ot;
   }
-  const size_t sidx = (mrow + n) * a.L + (size_t)e * nd + lv;
-  a.dvor[sidx] = ov;
-  a.ddiv[sidx] = od;
-  a.dt[sidx] = ot;
 }
 
 template <typename T>
@@ -229,13 +272,29 @@ PerDeviceOnce g_hs_ana_smem[2];
 
 }  // namespace
 
+// total wavenumbers per thread: two of one parity for member ensembles (each folded input loaded
+// from shared memory serves both: the analysis is shared-memory-bound at that scale), one otherwise
+// (shorter chains for the latency-bound single member)
+static int hs_analysis_np(int E) { return E >= 4 ? 2 : 1; }
+
+// threads per level of a block: the largest row count of an m pair (rows r = 4 i + b, b < 2, for
+// two rows per thread)
+static int hs_analysis_rows(const jgcm_mesh* m, int np) {
+  if (np == 1) return m->N + 4;
+  int q = 0;
+  for (int m1 = 0; m1 <= m->N / 2; m1++) {
+    const int m2 = m->N - m1, K1 = m->ns + 1 - m1, K2 = m2 != m1 ? m->ns + 1 - m2 : 0;
+    q = std::max(q, 2 * ((K1 + 3) / 4) + 2 * ((K2 + 3) / 4));
+  }
+  return q;
+}
+
 // levels per block of the Held-Suarez analysis: the tuned value when set (clamped to what a block
 // of 256 threads holds), else as many as a block holds (HS T42L20, one member: 5 levels 5.5 us,
 // 2 levels 7.1 us, 1 level 7.6 us per step in a captured graph)
 int hs_analysis_levels(const jgcm_mesh* m, int nd, int E) {
   (void)nd;
-  (void)E;
-  const int lg_max = 256 / (m->N + 4);
+  const int lg_max = 256 / hs_analysis_rows(m, hs_analysis_np(E));
   if (lg_max < 1) return 0;
   if (m->hs_levels > 0) return std::min(m->hs_levels, lg_max);
   return lg_max;
@@ -248,7 +307,6 @@ bool hs_analysis_fits(const jgcm_mesh* m, int nd, int E) {
   if (m->tc.on && !m->simt_legendre) return false;
   // weight rows of a power-of-two nh/4 16-byte chunks (at most 32: one warp pass per row or more)
   if (m->nh < 4 || m->nh > 128 || (m->nh & (m->nh - 1)) != 0) return false;
-  if (m->nh > m->N + 4) return false;  // a block's threads cover its (level, latitude) folds
   const int LG = hs_analysis_levels(m, nd, E);
   if (LG < 1) return false;
   const size_t sm = is_fp64(m) ? hs_analysis_smem<double>(m, LG) : hs_analysis_smem<float>(m, LG);
@@ -265,7 +323,8 @@ int launch_hs_analysis(jgcm_mesh* m, const FFTPlan& fp, int colU, int colV, int 
   const int LG = hs_analysis_levels(m, nd, E);
   const size_t sm = hs_analysis_smem<T>(m, LG);
   JG_TRY(g_hs_ana_smem[sizeof(T) == 8 ? 1 : 0].run([]() -> int {
-    JG_CUDA(cudaFuncSetAttribute(k_hs_analysis<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget));
+    JG_CUDA(cudaFuncSetAttribute(k_hs_analysis<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget));
+    JG_CUDA(cudaFuncSetAttribute(k_hs_analysis<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget));
     return JGCM_OK;
   }));
   HSAnaArgs<T> a;
@@ -288,9 +347,13 @@ int launch_hs_analysis(jgcm_mesh* m, const FFTPlan& fp, int colU, int colV, int 
   a.nlat = m->nlat;
   a.nh = m->nh;
   a.LG = LG;
-  const int threads = ((m->N + 4) * LG + 31) / 32 * 32;
+  const int np = hs_analysis_np(E);
+  const int threads = (hs_analysis_rows(m, np) * LG + 31) / 32 * 32;
   dim3 grid(m->N / 2 + 1, (nd + 1 + LG - 1) / LG, E);
-  JG_CUDA(launch_pdl(k_hs_analysis<T>, grid, threads, sm, st, a, tables<T>(m)));
+  if (np == 2)
+    JG_CUDA(launch_pdl(k_hs_analysis<T, 2>, grid, threads, sm, st, a, tables<T>(m)));
+  else
+    JG_CUDA(launch_pdl(k_hs_analysis<T, 1>, grid, threads, sm, st, a, tables<T>(m)));
   mark(st);
   JG_CUDA(cudaGetLastError());
   return JGCM_OK;

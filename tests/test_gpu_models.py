@@ -133,11 +133,11 @@ def test_held_suarez_steps(jg, orc, name, prec, tol):
 
 
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp32", 2e-5)])
-@pytest.mark.parametrize("name,members", [("hs_t42l20", 1), ("hs_t21l20", 3)])
+@pytest.mark.parametrize("name,members", [("hs_t42l20", 1), ("hs_t21l20", 3), ("hs_t21l20", 4)])
 def test_held_suarez_analysis_kernel_matches_general(jg, orc, name, members, prec, tol):
-    """The Held-Suarez analysis kernel (one thread per (m, n, level), m pairs, tuning knob
-    hs_analysis_levels) gives the general analysis kernel's steps (knob -1) at every levels-per-block
-    setting, for one member and for a member ensemble.  The two sum the same products in a
+    """The Held-Suarez analysis kernel (one thread per (m, level) and one total wavenumber, or two of
+    one parity from 4 members on; m pairs; tuning knob hs_analysis_levels) gives the general analysis
+    kernel's steps (knob -1) at every levels-per-block setting, for one member and for ensembles.  The two sum the same products in a
     different order, so they agree to rounding (FP64 1e-12, FP32 2e-5 relative L2 after 3 steps;
     the FP32 bound is the dynamics' conditioning, as in MIXED_TOL)."""
     params = configs.PARAMS[name]
