@@ -91,19 +91,21 @@ __device__ __forceinline__ double warp_fold(const double* p, int n, int lane) {
   return warp_sum(s);
 }
 
-// Publishes this block's arrival after its writes (made by any of its threads, each followed by
-// __threadfence) and returns, in every thread, whether it was the last of the `n` arrivals on
-// `counter`; the last one resets the counter for the next launch.
+// Publishes this block's arrival after its writes (made by any of its threads before the call)
+// and returns, in every thread, whether it was the last of the `n` arrivals on `counter`; the last
+// one resets the counter for the next launch.  The block barrier orders the writes before thread 0's
+// arrival, which is an acquire-release atomic at GPU scope: it releases them to the block that
+// arrives last and, in that block, acquires every earlier block's released writes (no full fences).
 __device__ __forceinline__ bool ticket_last(unsigned* counter, unsigned n) {
   __shared__ bool last;
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned t = atomicAdd(counter, 1u);
+    unsigned t;
+    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(t) : "l"(counter) : "memory");
     last = (t == n - 1);
     if (last) *counter = 0u;
   }
   __syncthreads();
-  if (last) __threadfence();  // the other blocks' partials are read after their fences
   return last;
 }
 
@@ -977,10 +979,7 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
     const double colsum = ks > 0 ? part[ks - 1][0][lane] : 0.0;  // written by this warp above
     double x = ks == 0 ? (double)ps : ks == 1 ? colsum : colsum * (double)ps;
     x = warp_sum(x);
-    if (lane == 0) {
-      __stcg(bpart + (size_t)ks * nb + bid, x * a.wts[j]);
-      __threadfence();
-    }
+    if (lane == 0) __stcg(bpart + (size_t)ks * nb + bid, x * a.wts[j]);  // released by ticket_last
   }
   // first level: the group's last block folds the group's block partials and its share of the
   // column kernel's partials (S3, S4 weighted by their rows)
@@ -997,10 +996,7 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
       for (int q = q0 + lane; q < q1; q += 32) s += __ldcg(cp_ + q) * a.wts[q / a.col_gx];
       x = warp_sum(s);
     }
-    if (lane == 0) {
-      __stcg(gpart + (size_t)ks * ng + g, x);
-      __threadfence();
-    }
+    if (lane == 0) __stcg(gpart + (size_t)ks * ng + g, x);  // released by ticket_last
   }
   // second level: the last group's last block folds the group partials and applies the fixes
   if (!ticket_last(ctr + ng, (unsigned)ng)) return;
