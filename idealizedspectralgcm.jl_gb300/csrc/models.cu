@@ -217,15 +217,18 @@ __device__ __forceinline__ R seg_excl_suffix(R x, int s) {  // sum over the lane
   return incl - x;
 }
 
-// FP32: at most 72 registers (14 blocks of 64 threads per SM): at ensemble scale the kernel streams
-// and its time follows occupancy (at 77 registers, allocated as 80, 12 blocks: 97 -> 109 us, measured)
+// FP32, one lane per column (member ensembles): at most 72 registers (14 blocks of 64 threads per SM):
+// at that scale the kernel streams and its time follows occupancy (at 77 registers, allocated as 80,
+// 12 blocks: 97 -> 109 us, measured).  Several lanes per column (small grids, a few blocks per SM):
+// registers up to 6 blocks per SM, the level loops' values held without spills
 // HYB (hybrid coordinates, a_k != 0): the log pressures of Pressure_Variables! (Press_And_Geopot.jl:
 // 36-67, Simmons-Burridge, zero top) are formed per column and level from p_{k+1/2} = a_k + b_k ps:
 // D_k = ln(p_{k+1/2} / p_{k-1/2}) = log1p(Δp_k / p_{k-1/2}) (no difference of two large logarithms),
 // ln p_{k+1/2} - ln p_k = 1 - p_{k-1/2} D_k / Δp_k, ln p_k - ln p_{k-1/2} = D_k - that; the top level
 // has ln p_1 = ln p_{3/2} - 1.  Sigma coordinates read the same quantities as per-level constants.
 template <typename T, int S, bool HYB>
-__global__ void __launch_bounds__(HS_CT, sizeof(T) == 4 ? 14 : 1) k_hs_column(HSColArgs<T> a, const VertCoef* __restrict__ vcp) {
+__global__ void __launch_bounds__(HS_CT, (sizeof(T) == 4 && S == 1) ? 14 : sizeof(T) == 4 ? 6 : 1)
+    k_hs_column(HSColArgs<T> a, const VertCoef* __restrict__ vcp) {
   const VertCoef& vc = *vcp;
   __shared__ double red[2][HS_CT / 32];
   // the vertical coefficients in the state precision, staged once per block (constants: staged
