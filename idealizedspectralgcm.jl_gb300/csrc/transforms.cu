@@ -121,6 +121,57 @@ __global__ void __launch_bounds__(256) k_s2g_legendre(S2GPlan plan, Tables<T> tb
   }
   if (async_p) cp_async_wait_all();
   __syncthreads();
+  // two or more outputs per thread (large column tiles: member ensembles): a thread takes columns cl
+  // and cl + CT/2 of one latitude, so each P weight loaded serves both (the kernel is
+  // instruction-bound there); same products in the same order per output
+  if (CT % 2 == 0 && nh * CT >= 2 * (int)blockDim.x) {
+    const int CT2 = CT / 2;
+    for (int i = threadIdx.x; i < nh * CT2; i += blockDim.x) {
+      const int j = i / CT2, cl = i - j * CT2;
+      T er0 = 0, ei0 = 0, or0 = 0, oi0 = 0, er1 = 0, ei1 = 0, or1 = 0, oi1 = 0;
+      int r = 0;
+      for (; r + 1 < K; r += 2) {
+        const T p0 = Ps[r * nh + j], p1 = Ps[(r + 1) * nh + j];
+        const V a0 = X[r * CT + cl], a1 = X[(r + 1) * CT + cl];
+        const V b0 = X[r * CT + cl + CT2], b1 = X[(r + 1) * CT + cl + CT2];
+        er0 += p0 * a0.x;
+        ei0 += p0 * a0.y;
+        or0 += p1 * a1.x;
+        oi0 += p1 * a1.y;
+        er1 += p0 * b0.x;
+        ei1 += p0 * b0.y;
+        or1 += p1 * b1.x;
+        oi1 += p1 * b1.y;
+      }
+      if (r < K) {
+        const T p0 = Ps[r * nh + j];
+        const V a0 = X[r * CT + cl], b0 = X[r * CT + cl + CT2];
+        er0 += p0 * a0.x;
+        ei0 += p0 * a0.y;
+        er1 += p0 * b0.x;
+        ei1 += p0 * b0.y;
+      }
+      const size_t rn = ((size_t)m * nlat + j) * C, rs = ((size_t)m * nlat + (nlat - 1 - j)) * C;
+      V s, nn;
+      if (cbase + cl < C) {
+        s.x = er0 + or0;
+        s.y = ei0 + oi0;
+        nn.x = er0 - or0;
+        nn.y = ei0 - oi0;
+        F[rn + cbase + cl] = s;
+        F[rs + cbase + cl] = nn;
+      }
+      if (cbase + cl + CT2 < C) {
+        s.x = er1 + or1;
+        s.y = ei1 + oi1;
+        nn.x = er1 - or1;
+        nn.y = ei1 - oi1;
+        F[rn + cbase + cl + CT2] = s;
+        F[rs + cbase + cl + CT2] = nn;
+      }
+    }
+    return;
+  }
   for (int i = threadIdx.x, jf = threadIdx.x / CT; i < nh * CT; i += blockDim.x, jf += rstep) {
     const int j = fixed_col ? jf : i / CT, cl = fixed_col ? cl0 : i - j * CT, c = cbase + cl;
     T er = 0, ei = 0, orr = 0, oi = 0;
