@@ -872,6 +872,7 @@ struct CorrArgs {
   double cp, grav;
   double inv_2n;  // 1 / (2 nlon), exact (nlon is a power of two)
   T cp_t;         // cp rounded to T on the host
+  float cp_hi, cp_lo;  // cp as an FP32 pair (hi its rounding, lo that of the remainder)
 };
 
 // The sums, every one weighted by the Gaussian weight of its latitude row:
@@ -913,8 +914,8 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   // T_k Δb_k on the FP64 path; on the FP32 path the same sums as FP32 pairs (error-free products
   // against Δ_hi + Δ_lo, error-free additions), each column's pair converted to FP64 once
   __shared__ double part[2][KS][32];
+  __shared__ float pk[2][KS][32], ph[2][KS][32], pl[2][KS][32];  // FP32 path: kinetic; c_p T part as hi + lo
   if constexpr (std::is_same<T, float>::value) {
-    __shared__ float pk[2][KS][32], ph[2][KS][32], pl[2][KS][32];  // kinetic; c_p T part as hi + lo
     float ea = 0, eb = 0, ah = 0, al = 0, bh = 0, bl = 0;
     if (act) {
 #pragma unroll 4  // nd <= 32: every level's loads in flight together
@@ -943,7 +944,14 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
         ds_add(th, tl, ph[w][q][lane]);
         tl = __fadd_rn(tl, pl[w][q][lane]);
       }
-      part[w][0][lane] = ((double)kh + (double)kl) + a.cp * ((double)th + (double)tl);
+      // E = K + c_p T as a pair: c_p (th + tl) with c_p = cp_hi + cp_lo, the product th cp_hi
+      // error-free, the small cross terms rounded
+      const float p = __fmul_rn(th, a.cp_hi), pe = __fmaf_rn(th, a.cp_hi, -p);
+      float eh = kh, el = kl;
+      ds_add(eh, el, p);
+      el = __fadd_rn(el, __fadd_rn(pe, __fmaf_rn(th, a.cp_lo, __fmul_rn(tl, a.cp_hi))));
+      ph[w][0][lane] = eh;  // this warp's own row of the staging arrays, read back below
+      pl[w][0][lane] = el;
     }
   } else {
     T ea = 0, eb = 0;
@@ -979,9 +987,32 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   unsigned* const ctr = a.counter + (size_t)e * (ng + 1);
   if (ks < 3) {
     const T ps = act ? a.ps_n[off1 + col] : (T)0;
-    const double colsum = ks > 0 ? part[ks - 1][0][lane] : 0.0;  // written by this warp above
-    double x = ks == 0 ? (double)ps : ks == 1 ? colsum : colsum * (double)ps;
-    x = warp_sum(x);
+    double x;
+    if constexpr (std::is_same<T, float>::value) {
+      // the butterfly over the block's 32 columns on FP32 pairs (error-free additions), one FP64
+      // conversion per block value
+      float h = ps, l = 0.f;
+      if (ks > 0) {
+        h = ph[ks - 1][0][lane];
+        l = pl[ks - 1][0][lane];
+        if (ks == 2) {  // (h + l) ps, the product h ps error-free
+          const float p = __fmul_rn(h, ps), pe = __fmaf_rn(h, ps, -p);
+          l = __fadd_rn(pe, __fmul_rn(l, ps));
+          h = p;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o >= 1; o >>= 1) {
+        const float h2 = __shfl_xor_sync(FULL, h, o), l2 = __shfl_xor_sync(FULL, l, o);
+        ds_add(h, l, h2);
+        l = __fadd_rn(l, l2);
+      }
+      x = (double)h + (double)l;
+    } else {
+      const double colsum = ks > 0 ? part[ks - 1][0][lane] : 0.0;  // written by this warp above
+      x = ks == 0 ? (double)ps : ks == 1 ? colsum : colsum * (double)ps;
+      x = warp_sum(x);
+    }
     if (lane == 0) __stcg(bpart + (size_t)ks * nb + bid, x * a.wts[j]);  // released by ticket_last
   }
   // first level: the group's last block folds the group's block partials and its share of the
@@ -1998,6 +2029,8 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ca.grav = md->P.grav;
   ca.inv_2n = 0.5 / m->nlon;
   ca.cp_t = (T)md->cp_air;
+  ca.cp_hi = (float)md->cp_air;
+  ca.cp_lo = (float)(md->cp_air - (double)ca.cp_hi);
   ca.has_dak = has_dak(md);
   JG_CUDA(launch_pdl(k_hs_corr_reduce<T>, dim3((m->nlon + 31) / 32, m->nlat, E), 256, 0, st, ca, md->d_vc));
   mark(st);
