@@ -18,9 +18,12 @@
 #include <string>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "jgcm_internal.cuh"
 
 using namespace jgcm;
+namespace cg = cooperative_groups;
 
 #include "model_internal.cuh"
 
@@ -77,11 +80,24 @@ __device__ __forceinline__ T shfl_dn1(T x, int lane, int nd, T fill) {
 // issues at 2 lanes per cycle per SM here (a warp instruction holds its sub-partition's FP64 pipe
 // for ~64 cycles), so the folds are laid out to keep few FP64 warp instructions on the critical
 // path and to spread them over the four sub-partitions: one warp per value, lanes over partials,
-// a fixed butterfly.  Blocks form groups of CORR_GS consecutive blocks; the last block of a group
-// (atomic ticket) folds the group's partials, and the last group's last block folds the groups'.
-constexpr int CORR_GS = 16;
+// a fixed butterfly.  The first level's units are either thread-block clusters (up to 8 blocks on
+// one GPC, folding their values through distributed shared memory at the cluster barrier) or,
+// when the grid takes more than one wave of blocks (where a cluster barrier would hold SM slots),
+// groups of CORR_GS consecutive blocks whose last block to arrive (atomic ticket) folds them.
+// Each unit publishes its values, and the last unit to arrive folds the units' values.
+constexpr int CORR_GS = 16;  // blocks per group
+constexpr int CORR_CL = 8;   // blocks per cluster at most (the portable cluster size)
 
 __host__ __device__ inline int corr_groups(int nb) { return (nb + CORR_GS - 1) / CORR_GS; }
+
+// The fixer reduction's cluster shape over its (gx = nlon/32) x nlat grid: powers of two that
+// divide the grid, x first (the blocks of one latitude row), at most CORR_CL blocks
+inline void corr_cluster(int gx, int nlat, int& cx, int& cy) {
+  cx = 1;
+  while (cx * 2 <= CORR_CL && gx % (cx * 2) == 0) cx *= 2;
+  cy = 1;
+  while (cx * cy * 2 <= CORR_CL && nlat % (cy * 2) == 0) cy *= 2;
+}
 
 // sum of the n consecutive values at p: lane-strided in a fixed order, then the butterfly; every
 // lane of the warp returns the same total
@@ -863,8 +879,8 @@ struct CorrArgs {
   unsigned* counter;           // per member: corr_groups(nb) + 1 tickets
   size_t pstride;
   // the column kernel's block partials (ps_p and the column energy of the previous level) at the
-  // start of the member's region, its grid (col_gx x nlat blocks); this kernel's block partials at
-  // col_off (3 x nb), its group partials after them (5 x corr_groups(nb))
+  // start of the member's region, its grid (col_gx x nlat blocks); this kernel's block values at
+  // col_off (3 x nb, the group form), the first level's units' values after them (5 x the units)
   int col_gx, col_nb;
   size_t col_off;
   int nd, nlat, nlon, do_mass, do_energy;
@@ -882,7 +898,21 @@ struct CorrArgs {
 // (Mass_Weighted_Global_Integral); factor = mean_ps_p / mean_ps_n = S3 / S0, and with Δp_k =
 // Δa_k + Δb_k factor ps_n the correction grav (mean_energy_p - mean_energy_n) / (c_p mean_ps_p)
 // = (S4 - S1 - factor S2) / (c_p S3).
+// Unit u's share (of nu) of the column kernel's block partials of sum v (0: ps_p, 1: the column
+// energy of level p), each weighted by its row; every lane returns the share
 template <typename T>
+__device__ __forceinline__ double corr_col_share(const CorrArgs<T>& a, const double* pe, int v, int u, int nu,
+                                                 int lane) {
+  const int per = (a.col_nb + nu - 1) / nu, q0 = u * per, q1 = min(a.col_nb, q0 + per);
+  const double* cp_ = pe + (size_t)v * a.col_nb;
+  double s = 0.0;
+  for (int q = q0 + lane; q < q1; q += 32) s += __ldcg(cp_ + q) * a.wts[q / a.col_gx];
+  return warp_sum(s);
+}
+
+// CL: the first fold level in thread-block clusters (launched with a cluster shape), else in
+// groups of CORR_GS blocks
+template <typename T, bool CL>
 __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const VertCoef* __restrict__ vcp) {
   const VertCoef& vc = *vcp;
   // block = 32 consecutive columns of one latitude row x 8 level groups: warp ks reads levels
@@ -982,12 +1012,24 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
   // column, the butterfly over the columns, the row's weight
   const int nb = gridDim.x * gridDim.y, bid = blockIdx.y * gridDim.x + blockIdx.x, ng = corr_groups(nb);
   double* const pe = a.partials + e * a.pstride;
-  double* const bpart = pe + a.col_off;    // [3][nb]
-  double* const gpart = bpart + 3 * nb;    // [5][ng]
   unsigned* const ctr = a.counter + (size_t)e * (ng + 1);
+  int rank = 0, nu, u;  // the first level's units (clusters or groups) and this block's unit
+  if constexpr (CL) {
+    const dim3 cd = cg::this_cluster().dim_blocks();
+    rank = (int)cg::this_cluster().block_rank();
+    const int gcx = gridDim.x / cd.x;
+    nu = gcx * (gridDim.y / cd.y);
+    u = (blockIdx.y / cd.y) * gcx + blockIdx.x / cd.x;
+  } else {
+    nu = ng;
+    u = bid / CORR_GS;
+  }
+  double* const bpart = pe + a.col_off;           // [3][nb] (groups)
+  double* const upart = bpart + (size_t)3 * nb;  // [5][nu]
+  __shared__ double s_bv[3];                      // this block's values (clusters)
+  double x = 0.0;
   if (ks < 3) {
     const T ps = act ? a.ps_n[off1 + col] : (T)0;
-    double x;
     if constexpr (std::is_same<T, float>::value) {
       // the butterfly over the block's 32 columns on FP32 pairs (error-free additions), one FP64
       // conversion per block value
@@ -1013,30 +1055,44 @@ __global__ void __launch_bounds__(256) k_hs_corr_reduce(CorrArgs<T> a, const Ver
       x = ks == 0 ? (double)ps : ks == 1 ? colsum : colsum * (double)ps;
       x = warp_sum(x);
     }
-    if (lane == 0) __stcg(bpart + (size_t)ks * nb + bid, x * a.wts[j]);  // released by ticket_last
-  }
-  // first level: the group's last block folds the group's block partials and its share of the
-  // column kernel's partials (S3, S4 weighted by their rows)
-  const int g = bid / CORR_GS, g0 = g * CORR_GS, gn = min(CORR_GS, nb - g0);
-  if (!ticket_last(ctr + g, (unsigned)gn)) return;
-  if (ks < 5) {
-    double x;
-    if (ks < 3) {
-      x = warp_fold(bpart + (size_t)ks * nb + g0, gn, lane);
-    } else {
-      const int per = (a.col_nb + ng - 1) / ng, q0 = g * per, q1 = min(a.col_nb, q0 + per);
-      const double* cp_ = pe + (size_t)(ks - 3) * a.col_nb;
-      double s = 0.0;
-      for (int q = q0 + lane; q < q1; q += 32) s += __ldcg(cp_ + q) * a.wts[q / a.col_gx];
-      x = warp_sum(s);
+    x *= a.wts[j];
+    if (lane == 0) {
+      if constexpr (CL)
+        s_bv[ks] = x;
+      else
+        __stcg(bpart + (size_t)ks * nb + bid, x);  // released by ticket_last
     }
-    if (lane == 0) __stcg(gpart + (size_t)ks * ng + g, x);  // released by ticket_last
+  } else if (CL && ks < 5 && rank == 0) {
+    x = corr_col_share(a, pe, ks - 3, u, nu, lane);  // the leader's share, while the others finish
   }
-  // second level: the last group's last block folds the group partials and applies the fixes
-  if (!ticket_last(ctr + ng, (unsigned)ng)) return;
+  // first level
+  if constexpr (CL) {
+    // every thread of every block of the cluster reaches both cluster barriers (no return before
+    // them): the first releases the blocks' values to the leader, the second keeps the blocks
+    // resident until the leader has read them
+    cg::cluster_group cl = cg::this_cluster();
+    cl.sync();
+    if (rank == 0 && ks < 3) {  // the cluster's blocks in rank order, the fixed butterfly
+      const double v = lane < (int)cl.num_blocks() ? *cl.map_shared_rank(&s_bv[ks], lane) : 0.0;
+      x = warp_sum(v);
+    }
+    cl.sync();
+    if (rank != 0) return;
+  } else {
+    // the group's last block folds the group's block values and its share of the column kernel's
+    const int g0 = u * CORR_GS, gn = min(CORR_GS, nb - g0);
+    if (!ticket_last(ctr + u, (unsigned)gn)) return;
+    if (ks < 3)
+      x = warp_fold(bpart + (size_t)ks * nb + g0, gn, lane);
+    else if (ks < 5)
+      x = corr_col_share(a, pe, ks - 3, u, nu, lane);
+  }
+  if (ks < 5 && lane == 0) __stcg(upart + (size_t)ks * nu + u, x);  // released by ticket_last
+  // second level: the last unit to arrive folds the units' values and applies the fixes
+  if (!ticket_last(ctr + ng, (unsigned)nu)) return;
   __shared__ double S[5];
   if (ks < 5) {
-    const double x = warp_fold(gpart + (size_t)ks * ng, ng, lane);
+    const double x = warp_fold(upart + (size_t)ks * nu, nu, lane);
     if (lane == 0) S[ks] = x;
   }
   __syncthreads();
@@ -1445,7 +1501,7 @@ int build_wave(jgcm_model* md) {
 size_t col_partials(const jgcm_mesh* m) { return (size_t)2 * ((m->nlon + HS_CT / 8 - 1) / (HS_CT / 8)) * m->nlat; }
 size_t partial_stride(const jgcm_mesh* m) {
   const int nb = ((m->nlon + 31) / 32) * m->nlat;  // the fixer reduction's blocks per member
-  return col_partials(m) + (size_t)3 * nb + (size_t)5 * corr_groups(nb);
+  return col_partials(m) + (size_t)3 * nb + (size_t)5 * nb;  // its block values, its units' (<= nb)
 }
 // the fixer reduction's tickets per member
 inline size_t corr_tickets(const jgcm_mesh* m) { return (size_t)corr_groups(((m->nlon + 31) / 32) * m->nlat) + 1; }
@@ -2032,7 +2088,18 @@ int step_held_suarez(jgcm_model* md, cudaStream_t st) {
   ca.cp_hi = (float)md->cp_air;
   ca.cp_lo = (float)(md->cp_air - (double)ca.cp_hi);
   ca.has_dak = has_dak(md);
-  JG_CUDA(launch_pdl(k_hs_corr_reduce<T>, dim3((m->nlon + 31) / 32, m->nlat, E), 256, 0, st, ca, md->d_vc));
+  {
+    // clusters when the grid is one wave of blocks (8 of these per SM), groups otherwise
+    const int gx = (m->nlon + 31) / 32;
+    if ((size_t)gx * m->nlat * E <= (size_t)8 * m->sm_count) {
+      int cx, cy;
+      corr_cluster(gx, m->nlat, cx, cy);
+      JG_CUDA(launch_pdl_cluster(k_hs_corr_reduce<T, true>, dim3(gx, m->nlat, E), 256, 0, st, dim3(cx, cy, 1), ca,
+                                 md->d_vc));
+    } else {
+      JG_CUDA(launch_pdl(k_hs_corr_reduce<T, false>, dim3(gx, m->nlat, E), 256, 0, st, ca, md->d_vc));
+    }
+  }
   mark(st);
   JG_CUDA(cudaGetLastError());
   const size_t G1 = grid_elems(m, 1);
