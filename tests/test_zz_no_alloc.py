@@ -7,7 +7,9 @@ through the C ABI twice in a row, and checks each result against the allocating 
 jgcm_trans_spherical_to_grid with the tolerances of the transform tests (FP64 1e-12, FP32 5e-6,
 TF32x3 1e-5, BF16x3 1e-4).  On the tensor-core meshes the call cannot report a Legendre kernel
 whose bounded wait gave up; jgcm_mesh_synchronize does, and the test shows that path with the
-bounded-wait self-test.  This file is named to be collected last.
+bounded-wait self-test.  A call recorded while a user stream is captured into a CUDA graph (global
+capture mode, where an allocation anywhere in the process ends the capture with an error), and the
+graph replayed, gives the same result.  This file is named to be collected last.
 """
 import ctypes as C
 
@@ -29,6 +31,16 @@ def cudart():
         _rt.cudaFree.argtypes = [C.c_void_p]
         _rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
         _rt.cudaMemset.argtypes = [C.c_void_p, C.c_int, C.c_size_t]
+        _rt.cudaStreamCreateWithFlags.argtypes = [C.POINTER(C.c_void_p), C.c_uint]
+        _rt.cudaStreamDestroy.argtypes = [C.c_void_p]
+        _rt.cudaStreamSynchronize.argtypes = [C.c_void_p]
+        _rt.cudaStreamBeginCapture.argtypes = [C.c_void_p, C.c_int]
+        _rt.cudaStreamEndCapture.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+        _rt.cudaGraphInstantiate.argtypes = [C.POINTER(C.c_void_p), C.c_void_p, C.c_ulonglong]
+        _rt.cudaGraphLaunch.argtypes = [C.c_void_p, C.c_void_p]
+        _rt.cudaGraphExecDestroy.argtypes = [C.c_void_p]
+        _rt.cudaGraphDestroy.argtypes = [C.c_void_p]
+        _rt.cudaMemGetInfo.argtypes = [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
     return _rt
 
 
@@ -103,6 +115,68 @@ def test_noalloc_matches_allocating_entry_point(jg, prec, tol):
             out = d_g.download((nd, nlat, nlon), rdt).astype(np.float64).transpose(2, 1, 0)
             assert configs.rel_l2(out, ref) < tol
     finally:
+        d_s.free()
+        d_g.free()
+
+
+def _free_bytes():
+    free, total = C.c_size_t(), C.c_size_t()
+    assert cudart().cudaMemGetInfo(C.byref(free), C.byref(total)) == 0
+    return free.value
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("fp32", 5e-6)])
+def test_noalloc_in_a_captured_graph(jg, prec, tol):
+    """The entry point called while a user stream is captured (cudaStreamCaptureModeGlobal: a
+    cudaMalloc or a synchronising call anywhere in the process during the capture fails and
+    invalidates it), the graph instantiated and replayed twice over poisoned output: each replay
+    equals the allocating entry point, and the device's free memory does not change across the
+    replays."""
+    N, nlat, nlon, nd = 42, 64, 128, 20
+    mesh = jg.Spectral_Spherical_Mesh(N, N + 1, nlat, nlon, nd, 6371.0e3, precision=prec)
+    rng = np.random.default_rng(11)
+    s = (rng.standard_normal((N + 1, N + 2, nd)) + 1j * rng.standard_normal((N + 1, N + 2, nd)))
+    s /= (1.0 + np.arange(N + 2))[None, :, None] ** 1.5
+    for m in range(N + 1):
+        s[m, :m, :] = 0
+    s = np.asfortranarray(s)
+    ref = mesh.grid(nd)
+    jg.Trans_Spherical_To_Grid(mesh, s, ref)
+    cdt, rdt = (np.complex128, np.float64) if prec == "fp64" else (np.complex64, np.float32)
+    rt = cudart()
+    d_s = DeviceBuffer(s.size * np.dtype(cdt).itemsize)
+    d_g = DeviceBuffer(nlon * nlat * nd * np.dtype(rdt).itemsize)
+    st, graph, gexec = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    assert rt.cudaStreamCreateWithFlags(C.byref(st), 1) == 0  # cudaStreamNonBlocking
+    try:
+        d_s.upload(np.ascontiguousarray(s).astype(cdt))
+        f = _entry(jg)
+        # one call outside the capture: the per-device set-up (the scratch's address, the kernels'
+        # shared-memory attributes) happens on first use
+        assert f(mesh._h, d_s.ptr, nd, d_g.ptr, st) == 0, jg.lib().jgcm_last_error()
+        assert rt.cudaStreamSynchronize(st) == 0
+        assert rt.cudaStreamBeginCapture(st, 0) == 0  # cudaStreamCaptureModeGlobal
+        rc = f(mesh._h, d_s.ptr, nd, d_g.ptr, st)
+        assert rt.cudaStreamEndCapture(st, C.byref(graph)) == 0  # an unsafe call would fail here
+        assert rc == 0, jg.lib().jgcm_last_error()
+        assert rt.cudaGraphInstantiate(C.byref(gexec), graph, 0) == 0
+        free = []
+        for _ in range(2):
+            d_g.poison()
+            assert rt.cudaDeviceSynchronize() == 0  # the memset (legacy stream) before the replay
+            assert rt.cudaGraphLaunch(gexec, st) == 0
+            assert rt.cudaStreamSynchronize(st) == 0
+            free.append(_free_bytes())
+            out = d_g.download((nd, nlat, nlon), rdt).astype(np.float64).transpose(2, 1, 0)
+            assert np.isfinite(out).all()
+            assert configs.rel_l2(out, ref) < tol
+        assert free[0] == free[1]
+    finally:
+        if gexec.value:
+            rt.cudaGraphExecDestroy(gexec)
+        if graph.value:
+            rt.cudaGraphDestroy(graph)
+        rt.cudaStreamDestroy(st)
         d_s.free()
         d_g.free()
 
