@@ -30,7 +30,7 @@ config4    The batched ensemble as stated: 128 x HS T21L20, 32 x HS T42L20, 8 x 
            tiles from the autotuner, 30 simulated days per member in one graph launch per 24 windows:
            ensemble sim-days/s, and the first and last member of each truncation against the FP64 oracle
            (and against an FP64 GPU twin) after the 30 days.
-the benchmark spec the last key: the headline figures in one short object (the driver keeps the tail of stdout).
+headline   the last key: the headline figures in one short object (a truncated log keeps the end of stdout).
 cpu_baseline  the FP64 C oracle (a restatement of the reference on the host) timed on a bounded sample.
 --impl reference  times that oracle on all host threads on the same workload (the reference itself is
            Julia and Julia is not installed on the GPU hosts).
@@ -736,12 +736,12 @@ def run_jgcm(args):
         "clocks": clk,
         **extra,
     }
-    line["north_star"] = north_star_summary(line)
+    line["headline"] = headline_summary(line)
     print(json.dumps(line), flush=True)
     return 0
 
 
-def north_star_summary(line):
+def headline_summary(line):
     """The headline figures in one short object, printed last (the end of stdout is what survives in a
     truncated log): mixed vs FP64 sim-days/s and their errors, e2e, tensor-core modes, configs 1, 2, 4."""
     r = lambda x, n=4: None if x is None else float(f"{x:.{n}g}")  # noqa: E731
