@@ -600,7 +600,7 @@ def configs_steps_per_day(params):
 
 
 def oracle_checks(jobs, log_prefix="oracle checks"):
-    """Run the FP64 oracle jobs (the checker of the error figures) in spawned worker processes after
+    """Run the FP64 oracle jobs (the reference values of the error figures) in spawned worker processes after
     the GPU work, on the host's cores; returns {job: result}."""
     import multiprocessing as mp
 
@@ -683,7 +683,7 @@ def run_jgcm(args):
     if not args.no_cpu_baseline and world == 1:
         try:
             base = cpu_baseline()
-        except Exception as e:  # the checker must not take the GPU result down
+        except Exception as e:  # an oracle failure must not take the GPU result down
             base = {"value": None, "unit": "sim-days/s", "cores": os.cpu_count(), "kind": "port",
                     "sample": f"failed: {e}"}
     launches = modmx.launches_per_step()
@@ -774,7 +774,7 @@ def headline_summary(line):
 
 
 def config_legs(jgcm, configs, args):
-    """Configs 1, 2 and 4 on the GPU, then their errors against the FP64 oracle (the checker, run in
+    """Configs 1, 2 and 4 on the GPU, then their errors against the FP64 oracle (run in
     worker processes after the GPU work)."""
     base = configs.BASE_SEED
     out = {}

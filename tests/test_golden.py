@@ -1,7 +1,7 @@
 """The committed golden fixtures (tests/golden/, written by tests/golden/make_golden.py).
 
 analytic_t21.npz pins the oracle's tables to the reference's own known answers; oracle_t21.npz pins
-the transform entry points: the oracle must reproduce it (regression of the checker itself) and the
+the transform entry points: the oracle must reproduce it (regression of the oracle itself) and the
 GPU library must match it (FP64 1e-12, FP32 5e-6 relative L2, the transform-test tolerances).
 """
 import os
